@@ -1,0 +1,394 @@
+"""Benchmark: converged singular triplets per second at residual <= 1e-8 on the dense truncated SVD
+workload (A = U diag(s) V', 8192 x 2048, Haar U and V from seeded Gaussians, s geometric 1 -> 1e-6,
+top 32 triplets), mixed-precision GB300 path vs the plain FP64 GPU path, with p50/p99 solve latency.
+
+One step = one complete solve (start block -> 32 triplets with max residual <= 1e-8 checked in FP64).
+`value` times solves whose input A is already resident in HBM; `e2e` times the same solve through the
+C ABI with A in pinned host memory (host->device copy of A and device->host copy of U, s, V inside the
+timed region).  `--impl reference` times the reference's algorithm on the host cores (the NumPy/SciPy
+restatement: the reference's own solver path exists only in MATLAB).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+M_ROWS, N_COLS, NEV, TOL = 8192, 2048, 32, 1e-8
+BLOCK, STEP, MAXITER = 64, 4, 60
+METRIC = "converged singular triplets/s at residual <= 1e-8 (dense 8192x2048 geometric-spectrum SVD, top 32)"
+UNIT = "triplets/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_problem_gpu(seed=42):
+    """A = U diag(s) V' generated on the device (FP64).  Input synthesis only."""
+    import torch
+    from mixedprecisionofrr_gb300 import api
+
+    G1 = api.randn(seed, M_ROWS, N_COLS).contiguous()
+    G2 = api.randn(seed + 1, N_COLS, N_COLS).contiguous()
+    U, R1 = torch.linalg.qr(G1)
+    U = U * torch.sign(torch.diagonal(R1))[None, :]
+    V, R2 = torch.linalg.qr(G2)
+    V = V * torch.sign(torch.diagonal(R2))[None, :]
+    s = torch.tensor(1e-6 ** (np.arange(N_COLS) / (N_COLS - 1)), dtype=torch.float64, device="cuda")
+    A = (U * s[None, :]) @ V.T
+    Acm = api.empty_cm(M_ROWS, N_COLS, api.PREC["double"])
+    Acm.copy_(A)
+    return Acm, s.cpu().numpy()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"ofrr_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flush_l2(buf):
+    buf.add_(1.0)
+
+
+def run_solver(api, A, mode, V0=None):
+    return api.subspace_iter_svd(A, M_ROWS, N_COLS, BLOCK, "single", "half", maxiter=MAXITER, step_size=STEP,
+                                 mode=mode, tol=TOL, nev=NEV, check_every=1, V0=V0, generalized_tol=0.0)
+
+
+def time_solves(api, A, mode, steps, warmup, flush_buf):
+    import torch
+
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        run_solver(api, A, mode)
+    torch.cuda.synchronize()
+    times, infos = [], []
+    ctx = api.context()
+    ctx.reset_launch_count()
+    for _ in range(steps):
+        flush_l2(flush_buf)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        U, s, V, info = run_solver(api, A, mode)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        infos.append(info)
+    launches = ctx.launch_count
+    return np.array(times), infos, launches, s
+
+
+def time_e2e(api, A_host_pinned, steps, warmup):
+    """Through the C ABI with host buffers: H2D of A, solve, D2H of U, s, V per step."""
+    import torch
+    from mixedprecisionofrr_gb300 import _lib as L
+
+    ctx = api.context()
+    stream = torch.cuda.current_stream()
+    A_dev = api.empty_cm(M_ROWS, N_COLS, L.F64)
+    U_dev = api.empty_cm(M_ROWS, BLOCK, L.F64)
+    V_dev = api.empty_cm(N_COLS, BLOCK, L.F64)
+    U_host = torch.empty((BLOCK, M_ROWS), dtype=torch.float64).pin_memory()
+    V_host = torch.empty((BLOCK, N_COLS), dtype=torch.float64).pin_memory()
+    s = np.zeros(BLOCK)
+    res = np.zeros(BLOCK)
+    inf = L.ofrr_info()
+    op = L.ofrr_operator()
+    op.kind, op.nrows, op.ncols, op.symmetric = L.OP_DENSE, M_ROWS, N_COLS, 0
+    op.dtype, op.data, op.ld = L.F64, A_dev.data_ptr(), M_ROWS
+    o = api.options(mode=L.MODE_MIXED, maxiter=MAXITER, step_size=STEP, block=BLOCK, nev=NEV, tol=TOL,
+                    use_generalized=1, generalized_tol=0.0, seed=42, check_every=1, p_compute="single",
+                    p_output="half", p_hess_compute="single", p_hess_output="half", p_rr_compute="single",
+                    p_rr_output="single")
+    lib = ctx.lib
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+
+    def one():
+        A_dev.t().copy_(A_host_pinned, non_blocking=True)
+        st = lib.ofrr_si_svd(ctx.h, C.byref(op), C.byref(o), U_dev.data_ptr(), M_ROWS, dp(s), V_dev.data_ptr(),
+                             N_COLS, dp(res), C.byref(inf))
+        U_host.copy_(U_dev.t(), non_blocking=True)
+        V_host.copy_(V_dev.t(), non_blocking=True)
+        return st
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = one()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) / 1e3)
+    h2d = M_ROWS * N_COLS * 8
+    d2h = (M_ROWS + N_COLS) * BLOCK * 8 + BLOCK * 8
+    return np.array(ts), st, h2d, d2h, float(np.max(res[:NEV]))
+
+
+def gemm_roofline(api, steps=50):
+    """Live CUDA-event timing of the dominant contraction of the low-precision phase: the 16-bit
+    A.V product (8192 x 2048 by 2048 x 64, FP32 accumulation), on the library's stream."""
+    import torch
+    from mixedprecisionofrr_gb300 import _lib as L
+
+    ctx = api.context()
+    A = api.randn(7, M_ROWS, N_COLS, "half")
+    X = api.randn(8, N_COLS, BLOCK, "half")
+    Y = api.empty_cm(M_ROWS, BLOCK, L.F16)
+    lib = ctx.lib
+
+    def call():
+        st = lib.ofrr_gemm(ctx.h, 0, 0, L.F16, L.F16, L.F32, L.F16, M_ROWS, BLOCK, N_COLS, 1.0, A.data_ptr(), M_ROWS,
+                           X.data_ptr(), N_COLS, 0.0, Y.data_ptr(), M_ROWS)
+        assert st == 0
+
+    for _ in range(5):
+        call()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dt = e0.elapsed_time(e1) / 1e3 / steps
+    algo_bytes = (M_ROWS * N_COLS + N_COLS * BLOCK + M_ROWS * BLOCK) * 2
+    flops = 2.0 * M_ROWS * N_COLS * BLOCK
+    return dt, algo_bytes, flops
+
+
+def cpu_baseline_run(A_host, max_seconds=60.0):
+    """The oracle (FP64 NumPy/SciPy restatement of the reference's MATLAB path) on this host's cores:
+    one full solve with the same block / step / tolerance, stopped at max residual <= 1e-8."""
+    from oracle import ofrr_oracle as orc
+
+    state = {"it": 0, "res": np.inf}
+    t0 = time.perf_counter()
+
+    class Stop(Exception):
+        pass
+
+    def cb(it, U, s, V):
+        r = orc.svd_residual_norms(A_host, U[:, :NEV], s[:NEV], V[:, :NEV])
+        state["it"], state["res"] = it + 1, float(np.max(r))
+        if state["res"] <= TOL or time.perf_counter() - t0 > max_seconds:
+            raise Stop()
+
+    try:
+        orc.subspace_iter_svd(A_host, M_ROWS, N_COLS, BLOCK, "double", maxiter=MAXITER, step_size=STEP,
+                              generalized_tol=0.0, callback=cb)
+    except Stop:
+        pass
+    dt = time.perf_counter() - t0
+    return dt, state
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return main_reference(args, rank, world)
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from mixedprecisionofrr_gb300 import api
+
+    A, s_true = make_problem_gpu()
+    flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    # mixed path (the product) -----------------------------------------------------------------
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        times, infos, launches, s = time_solves(api, A, "mixed", args.steps, args.warmup, flush_buf)
+    if world > 1:
+        t = torch.tensor([times.sum()], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total = float(t.item())
+        torch.distributed.barrier()
+    else:
+        total = float(times.sum())
+    value = NEV * args.steps * world / total
+    err = float(np.max(np.abs(s[:NEV] - s_true[:NEV]) / s_true[:NEV]))
+    maxres = float(max(i.max_residual for i in infos))
+    statuses = sorted({i.status for i in infos})
+    iters = float(np.mean([i.iterations for i in infos]))
+    out = None
+    if rank == 0:
+        # FP64 GPU comparison path
+        fp64 = None
+        if not args.no_fp64:
+            k64 = max(1, min(2, args.steps))
+            t64, inf64, _, s64 = time_solves(api, A, "fp64", k64, 1, flush_buf)
+            fp64 = {"value": NEV * k64 / float(t64.sum()), "unit": UNIT, "ms_per_solve": 1e3 * float(t64.mean()),
+                    "iterations": float(np.mean([i.iterations for i in inf64])),
+                    "max_residual": float(max(i.max_residual for i in inf64))}
+        # end to end through the C ABI with host buffers
+        A_host = torch.empty((N_COLS, M_ROWS), dtype=torch.float64).pin_memory()
+        A_host.copy_(A.t())
+        te, st_e, h2d, d2h, res_e = time_e2e(api, A_host, args.steps, 1)
+        e2e = {"value": NEV * args.steps / float(te.sum()), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * float(te.mean()), "status": int(st_e),
+               "max_residual": res_e}
+        # roofline of the dominant low-precision contraction (live CUDA events)
+        peaks = {}
+        pk = ROOT / "MEASURED_PEAKS.json"
+        if pk.exists():
+            peaks = json.loads(pk.read_text())
+        dt_g, bytes_g, flops_g = gemm_roofline(api)
+        hbm_peak = peaks.get("hbm_gbs", 6800.0)
+        roof = {"kernel": "A.V 16-bit GEMM 8192x2048x64 (FP32 accumulate)", "bound": "hbm",
+                "achieved": bytes_g / dt_g / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "frac": bytes_g / dt_g / 1e9 / hbm_peak, "traffic": None,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                "us_per_launch": dt_g * 1e6, "tflops": flops_g / dt_g / 1e12}
+        cpu = None
+        if not args.no_cpu_baseline:
+            A_np = A.cpu().numpy()
+            dt_c, stc = cpu_baseline_run(A_np)
+            cpu = {"value": NEV / dt_c if stc["res"] <= TOL else NEV / dt_c * 0.0, "unit": UNIT,
+                   "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"one full FP64 NumPy/SciPy solve of the same workload ({stc['it']} outer iterations, "
+                             f"max residual {stc['res']:.2e}, {dt_c:.1f} s)",
+                   "seconds": dt_c}
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f16 basis / f32 accumulate / f64 pencil",
+            "data": "synthetic (seeded Haar U, V; geometric s 1..1e-6)",
+            "config": {"workload": "dense truncated SVD 8192x2048, top 32 triplets, tol 1e-8", "block": BLOCK,
+                       "step_size": STEP, "l2_flush": "256 MB write between timed solves",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "p50_ms": 1e3 * float(np.percentile(times, 50)), "p99_ms": 1e3 * float(np.percentile(times, 99)),
+            "iterations": iters, "max_residual": maxres, "max_rel_sigma_err": err, "status": statuses,
+            "fp64_path": fp64,
+            "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
+            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def main_reference(args, rank, world):
+    """The reference's algorithm on the host cores: the NumPy/SciPy restatement (FP64), every thread."""
+    if rank != 0:
+        return
+    from oracle import ofrr_oracle as orc
+
+    A, U, s, V = orc.dense_svd_problem(M_ROWS, N_COLS, seed=42)
+    for _ in range(args.warmup):
+        cpu_baseline_run(A, max_seconds=30.0)
+    ts, its, ress = [], [], []
+    for _ in range(args.steps):
+        dt, st = cpu_baseline_run(A, max_seconds=60.0)
+        ts.append(dt)
+        its.append(st["it"])
+        ress.append(st["res"])
+    ts = np.array(ts)
+    value = NEV * len(ts) / float(ts.sum())
+    cpu = {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+           "sample": f"full FP64 NumPy/SciPy solves of the workload ({int(np.mean(its))} outer iterations each, "
+                     f"max residual {max(ress):.2e})"}
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * float(ts.mean()), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Haar U, V; geometric s 1..1e-6)",
+        "config": {"workload": "dense truncated SVD 8192x2048, top 32 triplets, tol 1e-8", "block": BLOCK,
+                   "step_size": STEP},
+        "p50_ms": 1e3 * float(np.percentile(ts, 50)), "p99_ms": 1e3 * float(np.percentile(ts, 99)),
+        "cpu_baseline": cpu,
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,266 @@
+/*
+ * ofrr.h -- C ABI of libofrr_gb300.so, the GB300 (sm_103a) implementation of the
+ * orthogonalization-free projection eigen/SVD path of MixedPrecisionOFRR.
+ *
+ * Plain pointers and sizes only.  All matrices are column-major with an explicit
+ * leading dimension.  Device pointers are marked (dev), host pointers (host).
+ * Every entry point returns an int status whose values equal msvd::MSVDStatus
+ * (reference CPP/core/utils/error_handling.hpp:24-62); no entry point throws.
+ *
+ * Each declaration names the reference interface it replaces.  The reference's
+ * C++ solver bodies are stubs; their behaviour is defined by the MATLAB code under
+ * MATLAB/+src, cited beside the solver entry points.
+ */
+#ifndef OFRR_GB300_H
+#define OFRR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes: same numeric values as msvd::MSVDStatus ------------------------- */
+enum {
+  OFRR_SUCCESS = 0,
+  OFRR_ERR_INVALID_ARGUMENT = 1000,
+  OFRR_ERR_INVALID_OPERATION = 1001,
+  OFRR_ERR_OUT_OF_MEMORY = 1002,
+  OFRR_ERR_NOT_IMPLEMENTED = 1003,
+  OFRR_ERR_INTERNAL = 1004,
+  OFRR_ERR_NAN = 1005,
+  OFRR_ERR_INF = 1006,
+  OFRR_ERR_BLAS_INVALID_LOCATION = 2000,
+  OFRR_ERR_BLAS_UNSUPPORTED_TYPE = 2003,
+  OFRR_ERR_BLAS_CUBLAS = 2004,
+  OFRR_ERR_BLAS_INVALID_SIZE = 2005,
+  OFRR_ERR_FACTORIZATION_FAILED = 3000,
+  OFRR_ERR_SINGULAR_MATRIX = 3001,
+  OFRR_ERR_SOLVER_DIVERGENCE = 4000,
+  OFRR_ERR_SOLVER_MAX_ITERATIONS = 4001,
+  OFRR_ERR_FILE_NOT_FOUND = 5000,
+  OFRR_ERR_INVALID_FORMAT = 5001,
+  OFRR_ERR_CUDA_GENERAL = 6000,
+  OFRR_ERR_CUDA_MEMORY = 6001,
+  OFRR_ERR_CUDA_LAUNCH = 6002,
+  OFRR_ERR_CUDA_SYNC = 6003,
+  /* new: a bounded device-side wait ran out; the context stays usable */
+  OFRR_ERR_DEVICE_TIMEOUT = 6004
+};
+
+/* element types (reference: T in {double, float, __half}; bf16 is new) */
+typedef enum { OFRR_F64 = 0, OFRR_F32 = 1, OFRR_F16 = 2, OFRR_BF16 = 3 } ofrr_dtype;
+
+/* ---- context ---------------------------------------------------------------------- *
+ * Replaces the process-global CUDAHandler singleton (CPP/core/utils/cuda_handler.hpp:15-81):
+ * one context per host thread, an explicit stream, a cached device workspace and the
+ * library handles.  stream == NULL means a new non-blocking stream owned by the context. */
+typedef struct ofrr_ctx ofrr_ctx;
+int ofrr_ctx_create(ofrr_ctx** ctx, int device, void* cuda_stream);
+int ofrr_ctx_destroy(ofrr_ctx* ctx);
+int ofrr_ctx_set_stream(ofrr_ctx* ctx, void* cuda_stream);
+void* ofrr_ctx_get_stream(ofrr_ctx* ctx);
+int ofrr_ctx_synchronize(ofrr_ctx* ctx);
+/* number of kernels this library has launched on ctx since creation (or the last reset) */
+uint64_t ofrr_ctx_launch_count(ofrr_ctx* ctx);
+void ofrr_ctx_reset_launch_count(ofrr_ctx* ctx);
+/* bytes of device workspace currently cached by ctx (allocated on first need) */
+size_t ofrr_ctx_workspace_bytes(ofrr_ctx* ctx);
+const char* ofrr_status_string(int status);
+const char* ofrr_version(void);
+
+/* ---- project RNG ------------------------------------------------------------------ *
+ * Counter-based N(0,1) block (splitmix64 hashes + Box-Muller, element counter i+n*j).
+ * Stands in for MATLAB rng(seed); randn(n,k) (MATLAB/+src/+subspace/subspace_iter_eig.m:53-54)
+ * and replaces Vector::fill_random (CPP/containers/vector.cu:188-225). */
+int ofrr_randn(ofrr_ctx* ctx, uint64_t seed, int64_t n, int64_t k, ofrr_dtype dt,
+               void* out /*dev*/, int64_t ld);
+void ofrr_randn_host(uint64_t seed, int64_t n, int64_t k, double* out /*host, n*k*/);
+
+/* ---- level-1/2 building blocks ---------------------------------------------------- */
+/* iamax: 1-based index of the first max |x| and the signed value there.
+ * Replaces msvd::iamax (CPP/linalg/blas/mvops.hpp:98-99, mvops.cu:799-876). */
+int ofrr_iamax(ofrr_ctx* ctx, ofrr_dtype dt, int64_t n, const void* x /*dev*/,
+               int* idx1 /*host*/, double* val /*host*/);
+/* per-column 0-based argmax |A(:,j)|, lowest row on ties.
+ * Replaces msvd::matrix_iamax (mvops.hpp:113-114, mvops.cu:955-1199). */
+int ofrr_matrix_iamax(ofrr_ctx* ctx, ofrr_dtype dt, int64_t m, int64_t n, const void* A /*dev*/,
+                      int64_t lda, int* idx /*dev, n*/);
+/* scalecols: U(:,j) = po(pc(U(:,j)) / pc(U(k_j,j))), k_j = argmax|U(:,j)|, skipped if 0.
+ * MATLAB/+src/+mvops/scalecols.m:21-34.  piv (dev, optional) receives k_j (0-based). */
+int ofrr_scalecols(ofrr_ctx* ctx, ofrr_dtype po, ofrr_dtype pc, int64_t m, int64_t n,
+                   void* U /*dev*/, int64_t ldu, int* piv /*dev or NULL*/);
+/* element cast between storage types (replaces Vector::cast, CPP/containers/vector.cu:248-290) */
+int ofrr_cast(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, int64_t m, int64_t n,
+              const void* in /*dev*/, int64_t ldin, void* out /*dev*/, int64_t ldout);
+/* NaN/Inf scan: returns OFRR_SUCCESS, OFRR_ERR_NAN or OFRR_ERR_INF.
+ * Replaces msvd::check_special_values (mvops.hpp:159-174). */
+int ofrr_check_special_values(ofrr_ctx* ctx, ofrr_dtype dt, int64_t m, int64_t n,
+                              const void* A /*dev*/, int64_t lda);
+
+/* ---- oblique basis: Hessenberg process -------------------------------------------- *
+ * Q (m x n, type tout) with |Q| <= 1 and unit entries at the pivot rows, R (n x n) with
+ * A = Q R over the selected columns, skip[j] = 1 for deselected (near-dependent) columns.
+ * Arithmetic follows MATLAB/+src/+qr/hessenberg.m:45-85 element by element (MGS order,
+ * one rounding to tout per elimination), so the result is bit-identical to the MATLAB
+ * restatement in the same precisions.  Replaces msvd::hessenberg / hessenberg_v2 /
+ * hessenberg_v3 (CPP/linalg/factorization/hessenberg.hpp:22-78, hessenberg.cu:197-748).
+ * select_tol < 0 selects the default eps(tout) (MATLAB/+src/+utils/eps.m).
+ * R_host (n*n col-major), skip_host (n) and perm_host (n, 0-based or -1) may be NULL. */
+int ofrr_hessenberg(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tcompute,
+                    int64_t m, int64_t n, const void* A /*dev*/, int64_t lda,
+                    void* Q /*dev*/, int64_t ldq, double select_tol,
+                    double* R_host, int* skip_host, int* perm_host);
+
+/* ---- dense contractions ----------------------------------------------------------- *
+ * C = alpha op(A) op(B) + beta C with MATLAB gemm.m semantics (MATLAB/+src/+mvops/gemm.m:27-59):
+ * inputs converted to tcompute, product accumulated in tcompute (FP32 accumulation for
+ * 16-bit inputs), result stored as tout.  Replaces msvd::gemm (mvops.hpp:79-90,
+ * mvops.cu:466-568).  F16/BF16 operands with F32 compute run on the tcgen05 kernel. */
+int ofrr_gemm(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype tb,
+              ofrr_dtype tcompute, ofrr_dtype tout, int64_t M, int64_t N, int64_t K,
+              double alpha, const void* A /*dev*/, int64_t lda, const void* B /*dev*/,
+              int64_t ldb, double beta, void* C /*dev*/, int64_t ldc);
+
+/* ---- sparse operator: CSR with value copies per precision ------------------------- *
+ * Mirrors MATLAB/+src/+csr/sparse2csr.m:21-50 (0-based int32 here).  Any of the value
+ * arrays may be NULL if that precision is never requested. */
+typedef struct {
+  int64_t nrows, ncols, nnz;
+  const int32_t* indptr;   /* dev, nrows+1 */
+  const int32_t* indices;  /* dev, nnz */
+  const double* a_double;  /* dev, nnz */
+  const float* a_single;   /* dev, nnz */
+  const void* a_half;      /* dev, nnz (__half) */
+} ofrr_csr;
+
+/* Y = op(A) X for nrhs columns, MATLAB/+src/+csr/csrmv.m:27-78 (compute in tcompute using
+ * the value copy of that precision, store as ty). */
+int ofrr_csrmm(ofrr_ctx* ctx, const ofrr_csr* A, int trans, ofrr_dtype tx, ofrr_dtype tcompute,
+               ofrr_dtype ty, int64_t nrhs, const void* X /*dev*/, int64_t ldx,
+               void* Y /*dev*/, int64_t ldy);
+
+/* ---- small dense FP64 eigenproblems on the device --------------------------------- *
+ * Replace the host LAPACKE wrappers msvd::syev / msvd::sygv (mvops.hpp:184-197,
+ * mvops.cu:1601-1664).  Ascending eigenvalues; A is overwritten by the eigenvectors
+ * (orthonormal for syev, B-orthonormal for sygv).  n <= 256. */
+int ofrr_syev(ofrr_ctx* ctx, int n, double* A /*dev*/, int lda, double* w /*dev*/);
+int ofrr_sygv(ofrr_ctx* ctx, int n, double* A /*dev*/, int lda, double* B /*dev*/, int ldb,
+              double* w /*dev*/);
+
+/* ---- operators and solver options ------------------------------------------------- */
+typedef enum { OFRR_OP_DENSE = 0, OFRR_OP_CSR = 1 } ofrr_op_kind;
+
+typedef struct {
+  int kind;               /* ofrr_op_kind */
+  int64_t nrows, ncols;
+  int symmetric;          /* 1: A = A' (symmetric Rayleigh-Ritz), 0: general */
+  /* dense (kind == OFRR_OP_DENSE): column-major device matrix */
+  ofrr_dtype dtype;
+  const void* data;
+  int64_t ld;
+  /* sparse (kind == OFRR_OP_CSR) */
+  ofrr_csr csr;
+} ofrr_operator;
+
+/* Solver modes.
+ * OFRR_MODE_REFERENCE: the reference's semantics -- exactly maxiter outer iterations, every
+ *   cast of the MATLAB code at the same place, precisions from the p_* fields.
+ * OFRR_MODE_MIXED: production mixed precision -- 16-bit basis storage (p_output), FP32
+ *   accumulation on tensor cores, split-precision Gram matrices, FP64 small pencil,
+ *   precision escalation and FP64 residual checks; stops when nev pairs reach tol.
+ * OFRR_MODE_FP64: the same loop with every operand in FP64 (the comparison path).
+ * In OFRR_MODE_MIXED and OFRR_MODE_FP64 the caller's basis buffers (V, U, X) hold FP64: the start
+ * block on entry and the final Ritz vectors on exit; p_output then only selects the 16-bit working
+ * precision of the mixed mode (OFRR_F16 or OFRR_BF16). */
+typedef enum { OFRR_MODE_REFERENCE = 0, OFRR_MODE_MIXED = 1, OFRR_MODE_FP64 = 2 } ofrr_mode;
+typedef enum { OFRR_ORTH_HESSENBERG = 0, OFRR_ORTH_MGS = 1 } ofrr_orth;
+
+typedef struct {
+  int mode;                /* ofrr_mode */
+  int maxiter;             /* outer iterations (subspace) or matvec budget (Krylov) */
+  int step_size;           /* power steps per outer iteration (subspace_iter_eig.m:61) */
+  int block;               /* basis width b (subspace) */
+  int nev;                 /* wanted pairs k */
+  int kdim;                /* Krylov dimension (arnoldi_hess_eig.m:24-25) */
+  double tol;              /* residual target ||Ax - lx|| / ||A||; 0 = run maxiter */
+  int use_generalized;     /* generalized Rayleigh-Ritz on the oblique basis */
+  double generalized_tol;  /* tau in eig(V'AV, V'V + tau I) (eig_rr.m:52) */
+  double select_tol;       /* Hessenberg column selection; < 0 = eps(p_hess_output) */
+  uint64_t seed;           /* start block seed when use_start_block == 0 */
+  int use_start_block;     /* 1: V (or v0) holds the start block on entry */
+  int orth;                /* ofrr_orth */
+  int reorth;              /* MGS Arnoldi re-orthogonalisation (arnoldi_mgs_eig.m:80) */
+  ofrr_dtype p_compute, p_output;            /* subspace / Krylov precisions */
+  ofrr_dtype p_hess_compute, p_hess_output;  /* basis build */
+  ofrr_dtype p_rr_compute, p_rr_output;      /* Rayleigh-Ritz Gram / update */
+  int check_every;         /* residual check period in outer iterations (>= 1) */
+} ofrr_options;
+
+typedef struct {
+  int iterations;          /* outer iterations (subspace) or restart cycles (Krylov) */
+  int matvecs;             /* operator applications (columns) */
+  int converged;           /* pairs with residual <= tol */
+  int basis_width;         /* final basis width after column selection */
+  double max_residual;     /* max over the nev returned pairs */
+  int escalations;         /* precision escalations taken (mixed mode) */
+  int status_detail;       /* first device-side error code seen, 0 if none */
+} ofrr_info;
+
+void ofrr_options_default(ofrr_options* opt);
+
+/* ---- solvers ------------------------------------------------------------------------ */
+/* Subspace iteration eigensolver.  MATLAB/+src/+subspace/subspace_iter_eig.m:50-68 with the
+ * Hessenberg orth and eig_rr wrappers of MATLAB/+tests/+test2/test.m:358-397.
+ * Replaces msvd::si_eig (CPP/linalg/solvers/eig/si_eig.hpp:24-27, si_eig.cu:10-18).
+ * V: n x block (dev, type p_output) -- start block in (if use_start_block), Ritz vectors out,
+ * sorted by descending real part of the Ritz values.  evals/resid: host, block entries. */
+int ofrr_si_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt,
+                void* V /*dev*/, int64_t ldv, double* evals /*host*/, double* resid /*host|NULL*/,
+                ofrr_info* info /*host|NULL*/);
+
+/* Rayleigh-Ritz on a given (non-orthogonal) basis.  MATLAB/+src/+rr/eig_rr.m:46-57.
+ * Replaces msvd::rr_eig (CPP/linalg/solvers/eig/rr_eig.hpp:21-22, rr_eig.cu:9-13). */
+int ofrr_rr_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, int64_t ncols,
+                void* V /*dev, n x ncols, type p_output*/, int64_t ldv, double* evals /*host*/);
+
+/* Projection with an explicit B (reference msvd::ofrr_eig, rr_eig.hpp:34-35): eigenpairs of
+ * the pencil (V'AV, V'BV + tau I) for dense symmetric A, B. */
+int ofrr_ofrr_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_operator* B,
+                  const ofrr_options* opt, int64_t ncols, void* V /*dev*/, int64_t ldv,
+                  double* evals /*host*/);
+
+/* Subspace iteration SVD.  MATLAB/+src/+subspace/subspace_iter_svd.m:53-77 + svd_rr.m:50-91.
+ * Replaces msvd::si_svd (CPP/linalg/solvers/svd/si_svd.hpp:25-28, si_svd.cu:10-18).
+ * U: m x block, V: n x block (dev, type p_output); V holds the start block if
+ * use_start_block.  s/resid: host, block entries, descending. */
+int ofrr_si_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt,
+                void* U /*dev*/, int64_t ldu, double* s /*host*/, void* V /*dev*/, int64_t ldv,
+                double* resid /*host|NULL*/, ofrr_info* info /*host|NULL*/);
+
+/* Rayleigh-Ritz SVD on given bases U (m x ncols), V (n x ncols).  MATLAB/+src/+rr/svd_rr.m.
+ * Replaces msvd::rr_svd (CPP/linalg/solvers/svd/rr_svd.hpp:22-24, rr_svd.cu:10-15). */
+int ofrr_rr_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, int64_t ncols,
+                void* U /*dev*/, int64_t ldu, double* s /*host*/, void* V /*dev*/, int64_t ldv);
+
+/* Krylov eigensolver with restarts: Hessenberg process (orth = OFRR_ORTH_HESSENBERG,
+ * MATLAB/+src/+krylov/arnoldi_hess_eig.m:51-107) or MGS Arnoldi (OFRR_ORTH_MGS,
+ * MATLAB/+src/+krylov/arnoldi_mgs_eig.m:54-113).  Replaces msvd::arnoldi_eig
+ * (CPP/linalg/solvers/eig/arnoldi_eig.hpp:25-28, arnoldi_eig.cu:10-18).
+ * v0: n (dev, type p_output) start vector when use_start_block; X: n x nev Ritz vectors out. */
+int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt,
+                     const void* v0 /*dev|NULL*/, void* X /*dev*/, int64_t ldx,
+                     double* evals /*host, nev*/, double* resid /*host|NULL*/,
+                     ofrr_info* info /*host|NULL*/);
+
+/* Residual norms ||A x_j - l_j x_j||_2 / (normA ||x_j||_2) in FP64 for ncols pairs
+ * (MATLAB/+tests/+test4/test.m:340-350 with unit-norm scaling).  normA <= 0 uses max|l|. */
+int ofrr_residual_norms(ofrr_ctx* ctx, const ofrr_operator* A, ofrr_dtype tx, int64_t ncols,
+                        const void* X /*dev*/, int64_t ldx, const double* evals /*host*/,
+                        double normA, double* resid /*host*/);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OFRR_GB300_H */

@@ -1,0 +1,140 @@
+"""ctypes binding of libofrr_gb300.so (the C ABI declared in include/ofrr.h).
+
+The library is the product; this module only declares its entry points.  Importing it on a
+machine where the library was not built raises immediately: there is no fallback path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libofrr_gb300.so"
+
+# ---- enums (include/ofrr.h) -----------------------------------------------------------------
+F64, F32, F16, BF16 = 0, 1, 2, 3
+OP_DENSE, OP_CSR = 0, 1
+MODE_REFERENCE, MODE_MIXED, MODE_FP64 = 0, 1, 2
+ORTH_HESSENBERG, ORTH_MGS = 0, 1
+
+SUCCESS = 0
+ERR_SOLVER_MAX_ITERATIONS = 4001
+
+
+class ofrr_csr(C.Structure):
+    _fields_ = [
+        ("nrows", C.c_int64), ("ncols", C.c_int64), ("nnz", C.c_int64),
+        ("indptr", C.c_void_p), ("indices", C.c_void_p),
+        ("a_double", C.c_void_p), ("a_single", C.c_void_p), ("a_half", C.c_void_p),
+    ]
+
+
+class ofrr_operator(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("nrows", C.c_int64), ("ncols", C.c_int64), ("symmetric", C.c_int),
+        ("dtype", C.c_int), ("data", C.c_void_p), ("ld", C.c_int64),
+        ("csr", ofrr_csr),
+    ]
+
+
+class ofrr_options(C.Structure):
+    _fields_ = [
+        ("mode", C.c_int), ("maxiter", C.c_int), ("step_size", C.c_int), ("block", C.c_int),
+        ("nev", C.c_int), ("kdim", C.c_int), ("tol", C.c_double), ("use_generalized", C.c_int),
+        ("generalized_tol", C.c_double), ("select_tol", C.c_double), ("seed", C.c_uint64),
+        ("use_start_block", C.c_int), ("orth", C.c_int), ("reorth", C.c_int),
+        ("p_compute", C.c_int), ("p_output", C.c_int), ("p_hess_compute", C.c_int),
+        ("p_hess_output", C.c_int), ("p_rr_compute", C.c_int), ("p_rr_output", C.c_int),
+        ("check_every", C.c_int),
+    ]
+
+
+class ofrr_info(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int), ("matvecs", C.c_int), ("converged", C.c_int), ("basis_width", C.c_int),
+        ("max_residual", C.c_double), ("escalations", C.c_int), ("status_detail", C.c_int),
+    ]
+
+
+# name -> (restype, argtypes)
+_P = C.c_void_p
+_I64 = C.c_int64
+_D = C.c_double
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int)
+SIGNATURES = {
+    "ofrr_ctx_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, _P]),
+    "ofrr_ctx_destroy": (C.c_int, [_P]),
+    "ofrr_ctx_set_stream": (C.c_int, [_P, _P]),
+    "ofrr_ctx_get_stream": (_P, [_P]),
+    "ofrr_ctx_synchronize": (C.c_int, [_P]),
+    "ofrr_ctx_launch_count": (C.c_uint64, [_P]),
+    "ofrr_ctx_reset_launch_count": (None, [_P]),
+    "ofrr_ctx_workspace_bytes": (C.c_size_t, [_P]),
+    "ofrr_status_string": (C.c_char_p, [C.c_int]),
+    "ofrr_version": (C.c_char_p, []),
+    "ofrr_randn": (C.c_int, [_P, C.c_uint64, _I64, _I64, C.c_int, _P, _I64]),
+    "ofrr_randn_host": (None, [C.c_uint64, _I64, _I64, _DP]),
+    "ofrr_iamax": (C.c_int, [_P, C.c_int, _I64, _P, _IP, _DP]),
+    "ofrr_matrix_iamax": (C.c_int, [_P, C.c_int, _I64, _I64, _P, _I64, _P]),
+    "ofrr_scalecols": (C.c_int, [_P, C.c_int, C.c_int, _I64, _I64, _P, _I64, _P]),
+    "ofrr_cast": (C.c_int, [_P, C.c_int, C.c_int, _I64, _I64, _P, _I64, _P, _I64]),
+    "ofrr_check_special_values": (C.c_int, [_P, C.c_int, _I64, _I64, _P, _I64]),
+    "ofrr_hessenberg": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _I64, _I64, _P, _I64, _P, _I64, _D,
+                                  _DP, _IP, _IP]),
+    "ofrr_gemm": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _I64, _I64, _I64, _D,
+                            _P, _I64, _P, _I64, _D, _P, _I64]),
+    "ofrr_csrmm": (C.c_int, [_P, C.POINTER(ofrr_csr), C.c_int, C.c_int, C.c_int, C.c_int, _I64, _P, _I64, _P,
+                             _I64]),
+    "ofrr_syev": (C.c_int, [_P, C.c_int, _P, C.c_int, _P]),
+    "ofrr_sygv": (C.c_int, [_P, C.c_int, _P, C.c_int, _P, C.c_int, _P]),
+    "ofrr_options_default": (None, [C.POINTER(ofrr_options)]),
+    "ofrr_si_eig": (C.c_int, [_P, C.POINTER(ofrr_operator), C.POINTER(ofrr_options), _P, _I64, _DP, _DP,
+                              C.POINTER(ofrr_info)]),
+    "ofrr_rr_eig": (C.c_int, [_P, C.POINTER(ofrr_operator), C.POINTER(ofrr_options), _I64, _P, _I64, _DP]),
+    "ofrr_ofrr_eig": (C.c_int, [_P, C.POINTER(ofrr_operator), C.POINTER(ofrr_operator),
+                                C.POINTER(ofrr_options), _I64, _P, _I64, _DP]),
+    "ofrr_si_svd": (C.c_int, [_P, C.POINTER(ofrr_operator), C.POINTER(ofrr_options), _P, _I64, _DP, _P, _I64,
+                              _DP, C.POINTER(ofrr_info)]),
+    "ofrr_rr_svd": (C.c_int, [_P, C.POINTER(ofrr_operator), C.POINTER(ofrr_options), _I64, _P, _I64, _DP, _P,
+                              _I64]),
+    "ofrr_arnoldi_eig": (C.c_int, [_P, C.POINTER(ofrr_operator), C.POINTER(ofrr_options), _P, _P, _I64, _DP,
+                                   _DP, C.POINTER(ofrr_info)]),
+    "ofrr_residual_norms": (C.c_int, [_P, C.POINTER(ofrr_operator), C.c_int, _I64, _P, _I64, _DP, _D, _DP]),
+}
+
+_lib = None
+
+
+def load(path: os.PathLike | str | None = None):
+    """Load the shared library (once) and declare every entry point of include/ofrr.h."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"{p} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(the CUDA library is required: there is no CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class OfrrError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = load().ofrr_status_string(status).decode()
+        super().__init__(f"{what}: status {status} ({msg})" if what else f"status {status} ({msg})")
+
+
+def check(status: int, what: str = "") -> int:
+    if status != SUCCESS:
+        raise OfrrError(status, what)
+    return status

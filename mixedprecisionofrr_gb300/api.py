@@ -1,0 +1,482 @@
+"""Python mirror of the reference's MATLAB interface, calling libofrr_gb300.so through its C ABI.
+
+Function names, argument meanings and defaults follow ``MATLAB/+src`` of the reference
+(``subspace_iter_eig``, ``subspace_iter_svd``, ``arnoldi_hess_eig``, ``eig_rr``, ``svd_rr``,
+``hessenberg``, ``scalecols``, ``gemm``, ``csrmv``), with precisions given by name
+('double', 'single', 'half', 'bfloat16').  Device memory comes from PyTorch (plumbing only);
+every computation is a call into the CUDA library, and a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import _lib as L
+
+try:
+    import torch
+except Exception as e:  # pragma: no cover - torch is part of the supported environment
+    raise RuntimeError("PyTorch is required for device memory management") from e
+
+PREC = {"double": L.F64, "single": L.F32, "half": L.F16, "bfloat16": L.BF16}
+TORCH_DT = {L.F64: torch.float64, L.F32: torch.float32, L.F16: torch.float16, L.BF16: torch.bfloat16}
+NP_DT = {L.F64: np.float64, L.F32: np.float32, L.F16: np.float16}
+
+
+def _p(name) -> int:
+    if isinstance(name, int):
+        return name
+    return PREC[name]
+
+
+def _eps(p: int) -> float:
+    return {L.F64: 2.0 ** -52, L.F32: 2.0 ** -23, L.F16: 2.0 ** -10, L.BF16: 2.0 ** -7}[p]
+
+
+class Context:
+    """Owns an ofrr_ctx bound to a CUDA device and stream (default: torch's current stream)."""
+
+    def __init__(self, device: int = 0, stream=None):
+        self.lib = L.load()
+        torch.cuda.init()
+        self.device = device
+        if stream is None:
+            stream = torch.cuda.current_stream(device)
+        self.stream = stream
+        h = C.c_void_p()
+        L.check(self.lib.ofrr_ctx_create(C.byref(h), device, C.c_void_p(stream.cuda_stream)), "ofrr_ctx_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ofrr_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synchronize(self):
+        L.check(self.lib.ofrr_ctx_synchronize(self.h), "synchronize")
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.ofrr_ctx_launch_count(self.h))
+
+    def reset_launch_count(self):
+        self.lib.ofrr_ctx_reset_launch_count(self.h)
+
+
+_CTX: Optional[Context] = None
+
+
+def context() -> Context:
+    global _CTX
+    if _CTX is None:
+        _CTX = Context(torch.cuda.current_device())
+    return _CTX
+
+
+# ---- column-major device buffers ----------------------------------------------------------
+def empty_cm(m: int, n: int, p: int, device="cuda") -> "torch.Tensor":
+    """m x n column-major device tensor (strides (1, m))."""
+    return torch.empty((n, m), dtype=TORCH_DT[p], device=device).t()
+
+
+def to_device_cm(x, p: int, device="cuda") -> "torch.Tensor":
+    """Copy (numpy or torch, any layout) into a fresh column-major device tensor of precision p."""
+    if isinstance(x, np.ndarray):
+        a = x if x.ndim == 2 else x.reshape(-1, 1)
+        if p in NP_DT:
+            a = a.astype(NP_DT[p], copy=False)  # numpy rounds directly (no double rounding via float)
+        t = torch.from_numpy(np.ascontiguousarray(a))
+    else:
+        t = x if x.dim() == 2 else x.reshape(-1, 1)
+    out = empty_cm(t.shape[0], t.shape[1], p, device)
+    out.copy_(t.to(device=device))
+    return out
+
+
+def is_cm(t) -> bool:
+    return isinstance(t, torch.Tensor) and t.is_cuda and t.dim() == 2 and (t.stride(0) == 1 or t.shape[1] == 1)
+
+
+def ld_of(t) -> int:
+    return max(1, t.stride(1) if t.shape[1] > 1 else t.shape[0])
+
+
+def dtype_of(t) -> int:
+    for k, v in TORCH_DT.items():
+        if t.dtype == v:
+            return k
+    raise TypeError(f"unsupported dtype {t.dtype}")
+
+
+def to_numpy(t) -> np.ndarray:
+    if t.dtype == torch.bfloat16:
+        t = t.float()
+    return t.detach().cpu().numpy()
+
+
+# ---- CSR operator -----------------------------------------------------------------------------
+class CsrMatrix:
+    """Device CSR with value copies per precision (MATLAB/+src/+csr/sparse2csr.m:21-50)."""
+
+    def __init__(self, A, symmetric: Optional[bool] = None, device="cuda"):
+        import scipy.sparse as sp
+
+        if isinstance(A, dict):
+            indptr, indices, data = A["indptr"], A["indices"], A["a_double"]
+            shape = (A["nrows"], A["ncols"])
+        else:
+            M = sp.csr_matrix(A, dtype=np.float64)
+            M.sort_indices()
+            indptr, indices, data, shape = M.indptr, M.indices, M.data, M.shape
+        self.shape = shape
+        self.nnz = int(len(data))
+        self.indptr = torch.as_tensor(np.asarray(indptr, np.int32), device=device)
+        self.indices = torch.as_tensor(np.asarray(indices, np.int32), device=device)
+        d = np.asarray(data, np.float64)
+        self.a_double = torch.as_tensor(d, device=device)
+        self.a_single = torch.as_tensor(d.astype(np.float32), device=device)
+        self.a_half = torch.as_tensor(d.astype(np.float16), device=device)
+        if symmetric is None:
+            M = sp.csr_matrix((d, np.asarray(indices), np.asarray(indptr)), shape=shape)
+            symmetric = shape[0] == shape[1] and abs(M - M.T).max() == 0
+        self.symmetric = bool(symmetric)
+
+    def struct(self) -> L.ofrr_csr:
+        s = L.ofrr_csr()
+        s.nrows, s.ncols, s.nnz = self.shape[0], self.shape[1], self.nnz
+        s.indptr = self.indptr.data_ptr()
+        s.indices = self.indices.data_ptr() if self.nnz else None
+        s.a_double = self.a_double.data_ptr() if self.nnz else None
+        s.a_single = self.a_single.data_ptr() if self.nnz else None
+        s.a_half = self.a_half.data_ptr() if self.nnz else None
+        return s
+
+
+@dataclass
+class Operator:
+    """Keeps the ofrr_operator struct and the tensors it points to alive."""
+    op: L.ofrr_operator
+    keep: tuple
+    m: int
+    n: int
+
+
+def operator(A, symmetric: Optional[bool] = None, dtype: str | int = "double") -> Operator:
+    op = L.ofrr_operator()
+    if isinstance(A, Operator):
+        return A
+    if isinstance(A, CsrMatrix):
+        op.kind = L.OP_CSR
+        op.nrows, op.ncols = A.shape
+        op.symmetric = int(A.symmetric if symmetric is None else symmetric)
+        op.dtype = L.F64
+        op.csr = A.struct()
+        return Operator(op, (A,), A.shape[0], A.shape[1])
+    t = A if is_cm(A) else to_device_cm(A if not isinstance(A, np.ndarray) else A.astype(np.float64), _p(dtype))
+    op.kind = L.OP_DENSE
+    op.nrows, op.ncols = t.shape
+    if symmetric is None:
+        symmetric = t.shape[0] == t.shape[1] and bool(torch.equal(t, t.t()))
+    op.symmetric = int(symmetric)
+    op.dtype = dtype_of(t)
+    op.data = t.data_ptr()
+    op.ld = ld_of(t)
+    return Operator(op, (t,), t.shape[0], t.shape[1])
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+# ---- building blocks --------------------------------------------------------------------------
+def randn(seed: int, n: int, k: int, precision="double"):
+    ctx = context()
+    p = _p(precision)
+    out = empty_cm(n, k, p)
+    L.check(ctx.lib.ofrr_randn(ctx.h, seed, n, k, p, out.data_ptr(), max(n, 1)), "ofrr_randn")
+    return out
+
+
+def randn_host(seed: int, n: int, k: int) -> np.ndarray:
+    out = np.zeros(n * k, np.float64)
+    L.load().ofrr_randn_host(seed, n, k, _dp(out))
+    return out.reshape(k, n).T.copy()
+
+
+def scalecols(U, precision_compute="double", precision_output=None, return_pivots=False):
+    """MATLAB/+src/+mvops/scalecols.m."""
+    ctx = context()
+    pc = _p(precision_compute)
+    po = _p(precision_output or precision_compute)
+    X = to_device_cm(U, po)
+    m, n = X.shape
+    piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    L.check(ctx.lib.ofrr_scalecols(ctx.h, po, pc, m, n, X.data_ptr(), ld_of(X), piv.data_ptr()), "scalecols")
+    return (X, piv) if return_pivots else X
+
+
+def iamax(x):
+    """1-based index of max |x| and the value there (CPP/linalg/blas/mvops.hpp:98)."""
+    ctx = context()
+    t = x if isinstance(x, torch.Tensor) and x.is_cuda else torch.as_tensor(np.asarray(x), device="cuda")
+    t = t.contiguous().reshape(-1)
+    idx = C.c_int()
+    val = C.c_double()
+    L.check(ctx.lib.ofrr_iamax(ctx.h, dtype_of(t[:, None]), t.numel(), t.data_ptr(), C.byref(idx), C.byref(val)),
+            "iamax")
+    return idx.value, val.value
+
+
+def check_special_values(X) -> int:
+    ctx = context()
+    t = X if is_cm(X) else to_device_cm(X, L.F64)
+    return ctx.lib.ofrr_check_special_values(ctx.h, dtype_of(t), t.shape[0], t.shape[1], t.data_ptr(), ld_of(t))
+
+
+def hessenberg(A, precision_compute="double", precision_output=None, select_tol=None, precision_input=None):
+    """MATLAB/+src/+qr/hessenberg.m (three-output form): returns Q (device), R, select, perm (host)."""
+    ctx = context()
+    pc = _p(precision_compute)
+    po = _p(precision_output or precision_compute)
+    pi = _p(precision_input) if precision_input else po
+    X = to_device_cm(A, pi)
+    m, n = X.shape
+    Q = empty_cm(m, n, po)
+    R = np.zeros(n * n, np.float64)
+    skip = np.zeros(n, np.int32)
+    perm = np.zeros(n, np.int32)
+    st = -1.0 if select_tol is None else float(select_tol)
+    L.check(ctx.lib.ofrr_hessenberg(ctx.h, pi, po, pc, m, n, X.data_ptr(), ld_of(X), Q.data_ptr(), ld_of(Q), st,
+                                    _dp(R), _ip(skip), _ip(perm)), "hessenberg")
+    return Q, R.reshape(n, n).T.copy(), skip == 0, perm.astype(np.int64)
+
+
+def gemm(A, trans: str, B, precision_compute="double", precision_output=None, alpha=1.0, beta=0.0, Cin=None):
+    """MATLAB/+src/+mvops/gemm.m: C = op(A) B computed in precision_compute, stored in precision_output."""
+    ctx = context()
+    pc = _p(precision_compute)
+    po = _p(precision_output or precision_compute)
+    Ad = A if is_cm(A) else to_device_cm(A, pc)
+    Bd = B if is_cm(B) else to_device_cm(B, pc)
+    tA = 1 if trans == "T" else 0
+    M = Ad.shape[1] if tA else Ad.shape[0]
+    K = Ad.shape[0] if tA else Ad.shape[1]
+    N = Bd.shape[1]
+    Cd = Cin if Cin is not None else empty_cm(M, N, po)
+    L.check(ctx.lib.ofrr_gemm(ctx.h, tA, 0, dtype_of(Ad), dtype_of(Bd), pc, po, M, N, K, alpha, Ad.data_ptr(),
+                              ld_of(Ad), Bd.data_ptr(), ld_of(Bd), beta, Cd.data_ptr(), ld_of(Cd)), "gemm")
+    return Cd
+
+
+def csrmv(Acsr: CsrMatrix, trans: str, x, precision_compute="double", precision_output=None):
+    """MATLAB/+src/+csr/csrmv.m."""
+    ctx = context()
+    pc = _p(precision_compute)
+    po = _p(precision_output or precision_compute)
+    X = x if is_cm(x) else to_device_cm(x, pc)
+    tr = 1 if trans == "T" else 0
+    nout = Acsr.shape[1] if tr else Acsr.shape[0]
+    Y = empty_cm(nout, X.shape[1], po)
+    s = Acsr.struct()
+    L.check(ctx.lib.ofrr_csrmm(ctx.h, C.byref(s), tr, dtype_of(X), pc, po, X.shape[1], X.data_ptr(), ld_of(X),
+                               Y.data_ptr(), ld_of(Y)), "csrmm")
+    return Y
+
+
+def syev(A):
+    """Ascending eigenvalues / orthonormal eigenvectors of a small symmetric matrix (FP64, device)."""
+    ctx = context()
+    X = to_device_cm(A, L.F64)
+    n = X.shape[0]
+    w = torch.zeros(n, dtype=torch.float64, device="cuda")
+    L.check(ctx.lib.ofrr_syev(ctx.h, n, X.data_ptr(), ld_of(X), w.data_ptr()), "syev")
+    return to_numpy(w), to_numpy(X)
+
+
+def sygv(A, B):
+    ctx = context()
+    X = to_device_cm(A, L.F64)
+    Bd = to_device_cm(B, L.F64)
+    n = X.shape[0]
+    w = torch.zeros(n, dtype=torch.float64, device="cuda")
+    L.check(ctx.lib.ofrr_sygv(ctx.h, n, X.data_ptr(), ld_of(X), Bd.data_ptr(), ld_of(Bd), w.data_ptr()), "sygv")
+    return to_numpy(w), to_numpy(X)
+
+
+# ---- solvers ------------------------------------------------------------------------------------
+def options(**kw) -> L.ofrr_options:
+    o = L.ofrr_options()
+    L.load().ofrr_options_default(C.byref(o))
+    for k, v in kw.items():
+        if v is None:
+            continue
+        if k.startswith("p_"):
+            v = _p(v)
+        setattr(o, k, v)
+    return o
+
+
+def _prec_opts(precision_compute, precision_output, ph_c, ph_o, prr_c, prr_o):
+    pc = precision_compute
+    po = precision_output or pc
+    return dict(p_compute=pc, p_output=po, p_hess_compute=ph_c or pc, p_hess_output=ph_o or po,
+                p_rr_compute=prr_c or pc, p_rr_output=prr_o or po)
+
+
+def eig_rr(A, V, precision_compute="double", precision_output=None, precision_rr_compute=None,
+           precision_rr_output=None, use_generalized=False, generalized_tol=None, symmetric=None):
+    """MATLAB/+src/+rr/eig_rr.m on the basis V; returns (Ritz vectors, Ritz values desc)."""
+    ctx = context()
+    op = operator(A, symmetric)
+    po = _p(precision_output or precision_compute)
+    Vd = to_device_cm(V, po)
+    b = Vd.shape[1]
+    gtol = generalized_tol
+    if gtol is None:
+        gtol = 1e-10  # eig_rr.m:105-107 (precision_eig = double)
+    o = options(use_generalized=int(use_generalized), generalized_tol=gtol,
+                **_prec_opts(precision_compute, precision_output, None, None, precision_rr_compute,
+                             precision_rr_output))
+    d = np.zeros(b)
+    L.check(ctx.lib.ofrr_rr_eig(ctx.h, C.byref(op.op), C.byref(o), b, Vd.data_ptr(), ld_of(Vd), _dp(d)), "rr_eig")
+    return Vd, d
+
+
+def svd_rr(A, U, V, precision_compute="double", precision_output=None, precision_rr_compute=None,
+           precision_rr_output=None, use_generalized=True, generalized_tol=None):
+    """MATLAB/+src/+rr/svd_rr.m (generalized form) on the bases U, V."""
+    ctx = context()
+    op = operator(A, False)
+    po = _p(precision_output or precision_compute)
+    Ud = to_device_cm(U, po)
+    Vd = to_device_cm(V, po)
+    b = Ud.shape[1]
+    o = options(use_generalized=int(use_generalized), generalized_tol=1e-10 if generalized_tol is None else float(generalized_tol),
+                **_prec_opts(precision_compute, precision_output, None, None, precision_rr_compute,
+                             precision_rr_output))
+    s = np.zeros(b)
+    L.check(ctx.lib.ofrr_rr_svd(ctx.h, C.byref(op.op), C.byref(o), b, Ud.data_ptr(), ld_of(Ud), _dp(s),
+                                Vd.data_ptr(), ld_of(Vd)), "rr_svd")
+    return Ud, s, Vd
+
+
+@dataclass
+class SolveInfo:
+    status: int
+    iterations: int
+    matvecs: int
+    converged: int
+    basis_width: int
+    max_residual: float
+    residuals: np.ndarray
+
+
+def _info(st, inf, res):
+    return SolveInfo(st, inf.iterations, inf.matvecs, inf.converged, inf.basis_width, inf.max_residual, res)
+
+
+def subspace_iter_eig(A, n: int, k: int, precision_compute="double", precision_output=None, seed: int = 42,
+                      maxiter: int = 5, step_size: int = 1, precision_hess_compute=None, precision_hess_output=None,
+                      precision_rr_compute=None, precision_rr_output=None, use_generalized=True,
+                      generalized_tol=0.0, select_tol=None, symmetric=None, V0=None, mode="reference",
+                      tol=0.0, nev=None, check_every=1):
+    """MATLAB/+src/+subspace/subspace_iter_eig.m; returns (V, d, info) with V on the device."""
+    ctx = context()
+    op = operator(A, symmetric)
+    modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
+    o = options(mode=modes[mode], maxiter=maxiter, step_size=step_size, block=min(k, n), nev=nev or min(k, n),
+                tol=tol, use_generalized=int(use_generalized), generalized_tol=generalized_tol,
+                select_tol=-1.0 if select_tol is None else select_tol, seed=seed,
+                use_start_block=int(V0 is not None), check_every=check_every,
+                **_prec_opts(precision_compute, precision_output, precision_hess_compute, precision_hess_output,
+                             precision_rr_compute, precision_rr_output))
+    po = o.p_output if mode == "reference" else L.F64
+    b = o.block
+    V = to_device_cm(V0, po) if V0 is not None else empty_cm(n, b, po)
+    d = np.zeros(b)
+    res = np.zeros(b)
+    inf = L.ofrr_info()
+    st = ctx.lib.ofrr_si_eig(ctx.h, C.byref(op.op), C.byref(o), V.data_ptr(), ld_of(V), _dp(d), _dp(res),
+                             C.byref(inf))
+    if st not in (L.SUCCESS, L.ERR_SOLVER_MAX_ITERATIONS):
+        L.check(st, "si_eig")
+    return V, d, _info(st, inf, res)
+
+
+def subspace_iter_svd(A, m: int, n: int, k: int, precision_compute="double", precision_output=None, seed: int = 42,
+                      maxiter: int = 5, step_size: int = 1, precision_hess_compute=None, precision_hess_output=None,
+                      precision_rr_compute=None, precision_rr_output=None, use_generalized=True,
+                      generalized_tol=0.0, select_tol=None, V0=None, mode="reference", tol=0.0, nev=None,
+                      check_every=1):
+    """MATLAB/+src/+subspace/subspace_iter_svd.m; returns (U, s, V, info) with U, V on the device."""
+    ctx = context()
+    op = operator(A, False)
+    modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
+    b = min(k, n)
+    o = options(mode=modes[mode], maxiter=maxiter, step_size=step_size, block=b, nev=nev or b, tol=tol,
+                use_generalized=int(use_generalized), generalized_tol=generalized_tol,
+                select_tol=-1.0 if select_tol is None else select_tol, seed=seed,
+                use_start_block=int(V0 is not None), check_every=check_every,
+                **_prec_opts(precision_compute, precision_output, precision_hess_compute, precision_hess_output,
+                             precision_rr_compute, precision_rr_output))
+    po = o.p_output if mode == "reference" else L.F64
+    V = to_device_cm(V0, po) if V0 is not None else empty_cm(n, b, po)
+    U = empty_cm(m, b, po)
+    s = np.zeros(b)
+    res = np.zeros(b)
+    inf = L.ofrr_info()
+    st = ctx.lib.ofrr_si_svd(ctx.h, C.byref(op.op), C.byref(o), U.data_ptr(), ld_of(U), _dp(s), V.data_ptr(),
+                             ld_of(V), _dp(res), C.byref(inf))
+    if st not in (L.SUCCESS, L.ERR_SOLVER_MAX_ITERATIONS):
+        L.check(st, "si_svd")
+    return U, s, V, _info(st, inf, res)
+
+
+def arnoldi_hess_eig(A, n: int, k: int, precision_compute="double", precision_output=None, seed: int = 42,
+                     maxiter: int = 5, kdim=None, select_tol=None, generalized_tol=0.0, symmetric=None, v0=None,
+                     mode="reference", tol=0.0):
+    """MATLAB/+src/+krylov/arnoldi_hess_eig.m; returns (V, d, info)."""
+    ctx = context()
+    op = operator(A, symmetric)
+    modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
+    kk = min(k, n)
+    o = options(mode=modes[mode], maxiter=maxiter, kdim=kdim or maxiter, nev=kk, tol=tol, use_generalized=1,
+                generalized_tol=generalized_tol, select_tol=-1.0 if select_tol is None else select_tol, seed=seed,
+                use_start_block=int(v0 is not None), orth=L.ORTH_HESSENBERG,
+                **_prec_opts(precision_compute, precision_output, None, None, None, None))
+    po = o.p_output if mode == "reference" else L.F64
+    v0d = to_device_cm(v0, po) if v0 is not None else None
+    X = empty_cm(n, kk, po)
+    d = np.zeros(kk)
+    res = np.zeros(kk)
+    inf = L.ofrr_info()
+    st = ctx.lib.ofrr_arnoldi_eig(ctx.h, C.byref(op.op), C.byref(o), v0d.data_ptr() if v0d is not None else None,
+                                  X.data_ptr(), ld_of(X), _dp(d), _dp(res), C.byref(inf))
+    if st not in (L.SUCCESS, L.ERR_SOLVER_MAX_ITERATIONS):
+        L.check(st, "arnoldi_eig")
+    return X, d, _info(st, inf, res)
+
+
+def residual_norms(A, X, lam, normA: float = -1.0, symmetric=None):
+    ctx = context()
+    op = operator(A, symmetric)
+    Xd = X if is_cm(X) else to_device_cm(X, L.F64)
+    k = Xd.shape[1]
+    lam = np.ascontiguousarray(lam, np.float64)
+    out = np.zeros(k)
+    L.check(ctx.lib.ofrr_residual_norms(ctx.h, C.byref(op.op), dtype_of(Xd), k, Xd.data_ptr(), ld_of(Xd), _dp(lam),
+                                        normA, _dp(out)), "residual_norms")
+    return out

@@ -1,0 +1,258 @@
+// Internal declarations shared by the translation units of libofrr_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <cublas_v2.h>
+#include <cstdint>
+#include <cstddef>
+#include <cstdio>
+#include <vector>
+
+#include "../../include/ofrr.h"
+
+// --------------------------------------------------------------------------------------
+// status helpers
+// --------------------------------------------------------------------------------------
+#define OFRR_TRY(expr)                        \
+  do {                                        \
+    int _st = (expr);                         \
+    if (_st != OFRR_SUCCESS) return _st;      \
+  } while (0)
+
+#define OFRR_CUDA(expr)                                                   \
+  do {                                                                    \
+    cudaError_t _e = (expr);                                              \
+    if (_e != cudaSuccess) {                                              \
+      ofrr::note_cuda_error(_e, #expr, __FILE__, __LINE__);               \
+      return ofrr::map_cuda_error(_e);                                    \
+    }                                                                     \
+  } while (0)
+
+#define OFRR_CUBLAS(expr)                                                 \
+  do {                                                                    \
+    cublasStatus_t _s = (expr);                                           \
+    if (_s != CUBLAS_STATUS_SUCCESS) {                                    \
+      fprintf(stderr, "[ofrr] cuBLAS error %d at %s:%d\n", (int)_s, __FILE__, __LINE__); \
+      return OFRR_ERR_BLAS_CUBLAS;                                        \
+    }                                                                     \
+  } while (0)
+
+namespace ofrr {
+
+int map_cuda_error(cudaError_t e);
+void note_cuda_error(cudaError_t e, const char* what, const char* file, int line);
+
+// --------------------------------------------------------------------------------------
+// context: stream, cuBLAS handle, chunked device workspace (never moves once handed out)
+// --------------------------------------------------------------------------------------
+struct Chunk {
+  char* ptr = nullptr;
+  size_t size = 0;
+};
+
+struct WsMark {
+  size_t chunk;
+  size_t offset;
+};
+
+}  // namespace ofrr
+
+struct ofrr_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool owns_stream = false;
+  cublasHandle_t cublas = nullptr;
+  std::vector<ofrr::Chunk> chunks;
+  size_t cur_chunk = 0;
+  size_t cur_off = 0;
+  unsigned long long launches = 0;        // kernels of this library
+  unsigned long long library_calls = 0;   // cuBLAS calls (library kernels, counted apart)
+  int* dev_flags = nullptr;        // device status words written by kernels (bounded waits etc.)
+  unsigned int* dev_counters = nullptr;  // grid "last block" counters (self-resetting)
+  void* pinned = nullptr;          // small pinned host staging buffer
+  size_t pinned_size = 0;
+};
+
+namespace ofrr {
+
+// workspace ---------------------------------------------------------------------------
+void* ws_alloc(ofrr_ctx* ctx, size_t bytes, int* status);
+inline WsMark ws_mark(ofrr_ctx* ctx) { return WsMark{ctx->cur_chunk, ctx->cur_off}; }
+inline void ws_release(ofrr_ctx* ctx, WsMark m) {
+  ctx->cur_chunk = m.chunk;
+  ctx->cur_off = m.offset;
+}
+template <class T>
+inline T* ws_get(ofrr_ctx* ctx, size_t count, int* status) {
+  return static_cast<T*>(ws_alloc(ctx, count * sizeof(T), status));
+}
+// RAII scope: everything allocated inside is released at scope exit
+struct WsScope {
+  ofrr_ctx* ctx;
+  WsMark m;
+  explicit WsScope(ofrr_ctx* c) : ctx(c), m(ws_mark(c)) {}
+  ~WsScope() { ws_release(ctx, m); }
+};
+
+// launch accounting -------------------------------------------------------------------
+int after_launch(ofrr_ctx* ctx, const char* name);
+#define OFRR_LAUNCHED(ctx, name) OFRR_TRY(ofrr::after_launch((ctx), (name)))
+
+int sync_and_check(ofrr_ctx* ctx);
+
+// element sizes -----------------------------------------------------------------------
+inline size_t dtype_size(ofrr_dtype t) {
+  switch (t) {
+    case OFRR_F64: return 8;
+    case OFRR_F32: return 4;
+    case OFRR_F16: return 2;
+    case OFRR_BF16: return 2;
+  }
+  return 0;
+}
+inline bool dtype_valid(int t) { return t >= 0 && t <= 3; }
+inline double dtype_eps(ofrr_dtype t) {
+  switch (t) {
+    case OFRR_F64: return 2.220446049250313e-16;
+    case OFRR_F32: return 1.1920928955078125e-07;
+    case OFRR_F16: return 9.765625e-04;  // 2^-10, MATLAB/+src/+utils/eps.m:24
+    case OFRR_BF16: return 7.8125e-03;   // 2^-7
+  }
+  return 0;
+}
+
+// conversions with explicit round-to-nearest-even (no contraction, no fast-math) ------
+template <class TC, class T> __device__ __forceinline__ TC to_c(T x);
+template <> __device__ __forceinline__ double to_c<double, double>(double x) { return x; }
+template <> __device__ __forceinline__ double to_c<double, float>(float x) { return (double)x; }
+template <> __device__ __forceinline__ double to_c<double, __half>(__half x) { return (double)__half2float(x); }
+template <> __device__ __forceinline__ double to_c<double, __nv_bfloat16>(__nv_bfloat16 x) { return (double)__bfloat162float(x); }
+template <> __device__ __forceinline__ float to_c<float, double>(double x) { return __double2float_rn(x); }
+template <> __device__ __forceinline__ float to_c<float, float>(float x) { return x; }
+template <> __device__ __forceinline__ float to_c<float, __half>(__half x) { return __half2float(x); }
+template <> __device__ __forceinline__ float to_c<float, __nv_bfloat16>(__nv_bfloat16 x) { return __bfloat162float(x); }
+
+template <class T, class TC> __device__ __forceinline__ T from_c(TC x);
+template <> __device__ __forceinline__ double from_c<double, double>(double x) { return x; }
+template <> __device__ __forceinline__ float from_c<float, double>(double x) { return __double2float_rn(x); }
+template <> __device__ __forceinline__ __half from_c<__half, double>(double x) { return __double2half(x); }
+template <> __device__ __forceinline__ __nv_bfloat16 from_c<__nv_bfloat16, double>(double x) { return __double2bfloat16(x); }
+template <> __device__ __forceinline__ double from_c<double, float>(float x) { return (double)x; }
+template <> __device__ __forceinline__ float from_c<float, float>(float x) { return x; }
+template <> __device__ __forceinline__ __half from_c<__half, float>(float x) { return __float2half_rn(x); }
+template <> __device__ __forceinline__ __nv_bfloat16 from_c<__nv_bfloat16, float>(float x) { return __float2bfloat16_rn(x); }
+
+// |x| as a double for comparisons (exact for every storage type)
+template <class T> __device__ __forceinline__ double absd(T x) { return fabs(to_c<double, T>(x)); }
+
+// IEEE single-rounding arithmetic helpers
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+
+// argmax reduction on (|value|, index): larger value wins, lower index on ties, NaN ignored
+struct ArgMax {
+  double v;  // -1 means "empty"
+  long long i;
+};
+__device__ __forceinline__ ArgMax argmax_pick(ArgMax a, ArgMax b) {
+  if (b.v > a.v || (b.v == a.v && b.i < a.i && b.v >= 0.0)) return b;
+  return a;
+}
+__device__ __forceinline__ ArgMax warp_argmax(ArgMax a) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    ArgMax b;
+    b.v = __shfl_down_sync(0xffffffffu, a.v, off);
+    b.i = __shfl_down_sync(0xffffffffu, a.i, off);
+    a = argmax_pick(a, b);
+  }
+  return a;
+}
+// block-wide argmax; result valid in thread 0.  smem needs blockDim/32 entries.
+__device__ __forceinline__ ArgMax block_argmax(ArgMax a, ArgMax* smem) {
+  a = warp_argmax(a);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) smem[wid] = a;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  if (wid == 0) {
+    ArgMax b = (lane < nw) ? smem[lane] : ArgMax{-1.0, 0x7fffffffffffffffLL};
+    b = warp_argmax(b);
+    if (lane == 0) smem[0] = b;
+  }
+  __syncthreads();
+  ArgMax r = smem[0];
+  __syncthreads();
+  return r;
+}
+
+// runtime dtype dispatch --------------------------------------------------------------
+#define OFRR_DISPATCH_STORAGE(dt, T, ...)                         \
+  switch (dt) {                                                   \
+    case OFRR_F64: { using T = double; __VA_ARGS__; } break;      \
+    case OFRR_F32: { using T = float; __VA_ARGS__; } break;       \
+    case OFRR_F16: { using T = __half; __VA_ARGS__; } break;      \
+    case OFRR_BF16: { using T = __nv_bfloat16; __VA_ARGS__; } break; \
+    default: return OFRR_ERR_BLAS_UNSUPPORTED_TYPE;               \
+  }
+
+#define OFRR_DISPATCH_COMPUTE(dt, TC, ...)                        \
+  switch (dt) {                                                   \
+    case OFRR_F64: { using TC = double; __VA_ARGS__; } break;     \
+    case OFRR_F32: { using TC = float; __VA_ARGS__; } break;      \
+    default: return OFRR_ERR_BLAS_UNSUPPORTED_TYPE;               \
+  }
+
+inline int grid_for(long long n, int block, int cap = 152 * 16) {
+  long long g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (int)g;
+}
+
+// ---- cross-file internal API ---------------------------------------------------------
+// dense / sparse products into caller buffers (all on ctx->stream, no host sync)
+int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype tb, ofrr_dtype tc,
+              ofrr_dtype tout, int64_t M, int64_t N, int64_t K, double alpha, const void* A,
+              int64_t lda, const void* B, int64_t ldb, double beta, void* C, int64_t ldc);
+int csrmm_impl(ofrr_ctx* ctx, const ofrr_csr* A, int trans, ofrr_dtype tx, ofrr_dtype tc, ofrr_dtype ty,
+               int64_t nrhs, const void* X, int64_t ldx, void* Y, int64_t ldy);
+int cast_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, int64_t m, int64_t n, const void* in,
+              int64_t ldin, void* out, int64_t ldout);
+int scalecols_impl(ofrr_ctx* ctx, ofrr_dtype po, ofrr_dtype pc, int64_t m, int64_t n, void* U, int64_t ldu,
+                   int* piv);
+int fill_zero(ofrr_ctx* ctx, void* p, size_t bytes);
+
+// Hessenberg basis on device: Q (m x n, tout) from A; outputs on device:
+// R (n x n FP64, col-major), select (n ints, 1 = kept), perm (n ints, -1 if dropped)
+int hessenberg_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n,
+                    const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev,
+                    int* select_dev, int* perm_dev);
+// MGS basis (orthogonal comparison path, MATLAB/+src/+qr/mgs.m)
+int mgs_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n,
+             const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev,
+             int* select_dev);
+
+// small dense FP64 solvers on device (one CTA); w ascending
+int syev_dev(ofrr_ctx* ctx, int n, double* A, int lda, double* w);
+int sygv_dev(ofrr_ctx* ctx, int n, double* A, int lda, double* B, int ldb, double* w);
+// general real pencil eig(G, M) with M SPD: eigenvalues (real parts) and real parts of the
+// eigenvectors, M-normalised; sorted descending by real part.  n <= 256.
+int geig_dev(ofrr_ctx* ctx, int n, const double* G, int ldg, const double* M, int ldm, int symmetric,
+             double* w, double* U, int ldu);
+
+// reductions
+int column_norms(ofrr_ctx* ctx, ofrr_dtype t, int64_t m, int64_t n, const void* X, int64_t ldx,
+                 double* out_dev);
+int residual_columns(ofrr_ctx* ctx, int64_t m, int64_t n, const double* AX, int64_t ldax,
+                     const double* X, int64_t ldx, const double* lam_dev, double* out_dev);
+
+}  // namespace ofrr

@@ -1,0 +1,972 @@
+// Host orchestration of the projection solvers (all device work on ctx->stream).
+//
+// Behavioural definitions (the reference's C++ solver bodies are stubs):
+//   si_eig       MATLAB/+src/+subspace/subspace_iter_eig.m:50-68 (+ test2 wrappers, +tests/+test2/test.m:358-397)
+//   rr_eig       MATLAB/+src/+rr/eig_rr.m:46-57
+//   si_svd       MATLAB/+src/+subspace/subspace_iter_svd.m:53-77
+//   rr_svd       MATLAB/+src/+rr/svd_rr.m:50-91
+//   arnoldi_eig  MATLAB/+src/+krylov/arnoldi_hess_eig.m:51-107 (Hessenberg process)
+// Convergence control (tol, nev) is new: the reference runs a fixed maxiter.
+#include "ofrr_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace ofrr {
+
+int hess_krylov_first(ofrr_ctx* ctx, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int ncolmax, void* V, int64_t ldv,
+                      double select_tol, int* select, int* perm, void* pivrows, void* pvals, double* R, int* stop);
+int hess_krylov_step(ofrr_ctx* ctx, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int ncolmax, int i, void* V,
+                     int64_t ldv, double select_tol, int* select, int* perm, void* pivrows, void* pvals, double* R,
+                     int* stop);
+int hess_scale_col(ofrr_ctx* ctx, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int i, void* V, int64_t ldv,
+                   const int* select, const void* pvals, const int* stop);
+
+namespace {
+
+// operator wrapper: dense copies per storage type are made once per solve
+struct Op {
+  const ofrr_operator* A;
+  const void* dense[4] = {nullptr, nullptr, nullptr, nullptr};
+  int64_t ld[4] = {0, 0, 0, 0};
+  int64_t m() const { return A->nrows; }
+  int64_t n() const { return A->ncols; }
+  bool is_dense() const { return A->kind == OFRR_OP_DENSE; }
+
+  int dense_as(ofrr_ctx* ctx, ofrr_dtype t, const void** p, int64_t* l) {
+    if (!dense[t]) {
+      if (A->dtype == t) {
+        dense[t] = A->data;
+        ld[t] = A->ld;
+      } else {
+        int st = OFRR_SUCCESS;
+        void* w = ws_alloc(ctx, (size_t)m() * n() * dtype_size(t), &st);
+        if (!w) return st;
+        OFRR_TRY(cast_impl(ctx, A->dtype, t, m(), n(), A->data, A->ld, w, m()));
+        dense[t] = w;
+        ld[t] = m();
+      }
+    }
+    *p = dense[t];
+    *l = ld[t];
+    return OFRR_SUCCESS;
+  }
+
+  // Y = op(A) X: dense A taken in storage type ta (the MATLAB code casts A to the output precision
+  // once, subspace_iter_eig.m:56-58), computed in tc, stored as ty.
+  int apply(ofrr_ctx* ctx, int trans, ofrr_dtype ta, ofrr_dtype tx, const void* X, int64_t ldx, int64_t nrhs,
+            ofrr_dtype tc, ofrr_dtype ty, void* Y, int64_t ldy) {
+    if (A->kind == OFRR_OP_CSR) return csrmm_impl(ctx, &A->csr, trans, tx, tc, ty, nrhs, X, ldx, Y, ldy);
+    const void* Ad;
+    int64_t lda;
+    OFRR_TRY(dense_as(ctx, ta, &Ad, &lda));
+    const int64_t M = trans ? n() : m(), K = trans ? m() : n();
+    return gemm_impl(ctx, trans, 0, ta, tx, tc, ty, M, nrhs, K, 1.0, Ad, lda, X, ldx, 0.0, Y, ldy);
+  }
+};
+
+template <class T>
+int dmalloc(ofrr_ctx* ctx, T** p, size_t count) {
+  int st = OFRR_SUCCESS;
+  *p = ws_get<T>(ctx, count, &st);
+  return *p ? OFRR_SUCCESS : st;
+}
+
+__global__ void k_add_diag(int n, double* M, int ldm, double tau) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) M[i + (int64_t)i * ldm] += tau;
+}
+
+// gather selected columns of Q (keep order) into the first w columns
+int compact_columns(ofrr_ctx* ctx, ofrr_dtype t, int64_t m, void* Q, int64_t ldq, const std::vector<int>& sel,
+                    int* width) {
+  int w = 0;
+  const size_t es = dtype_size(t);
+  for (size_t j = 0; j < sel.size(); ++j) {
+    if (!sel[j]) continue;
+    if ((int)j != w)
+      OFRR_CUDA(cudaMemcpyAsync((char*)Q + (size_t)w * ldq * es, (char*)Q + j * ldq * es, (size_t)m * es,
+                                cudaMemcpyDeviceToDevice, ctx->stream));
+    ++w;
+  }
+  *width = w;
+  return OFRR_SUCCESS;
+}
+
+struct Precisions {
+  ofrr_dtype pc, po, phc, pho, prc, pro;
+};
+
+Precisions precisions_of(const ofrr_options* o) {
+  Precisions p;
+  if (o->mode == OFRR_MODE_FP64) {
+    p.pc = p.po = p.phc = p.pho = p.prc = p.pro = OFRR_F64;
+  } else {
+    p.pc = o->p_compute;
+    p.po = o->p_output;
+    p.phc = o->p_hess_compute;
+    p.pho = o->p_hess_output;
+    p.prc = o->p_rr_compute;
+    p.pro = o->p_rr_output;
+  }
+  return p;
+}
+
+int validate_options(const ofrr_options* o) {
+  if (!o) return OFRR_ERR_INVALID_ARGUMENT;
+  if (o->mode < 0 || o->mode > 2) return OFRR_ERR_INVALID_ARGUMENT;
+  if (o->maxiter < 0 || o->step_size < 1 || o->block < 1 || o->nev < 0) return OFRR_ERR_INVALID_ARGUMENT;
+  const int ps[6] = {o->p_compute, o->p_output, o->p_hess_compute, o->p_hess_output, o->p_rr_compute,
+                     o->p_rr_output};
+  for (int p : ps)
+    if (!dtype_valid(p)) return OFRR_ERR_BLAS_UNSUPPORTED_TYPE;
+  if (o->mode != OFRR_MODE_FP64) {
+    if (o->p_compute != OFRR_F64 && o->p_compute != OFRR_F32) return OFRR_ERR_BLAS_UNSUPPORTED_TYPE;
+    if (o->p_hess_compute != OFRR_F64 && o->p_hess_compute != OFRR_F32) return OFRR_ERR_BLAS_UNSUPPORTED_TYPE;
+    if (o->p_rr_compute != OFRR_F64 && o->p_rr_compute != OFRR_F32) return OFRR_ERR_BLAS_UNSUPPORTED_TYPE;
+  }
+  return OFRR_SUCCESS;
+}
+
+int validate_op(const ofrr_operator* A) {
+  if (!A || A->nrows < 0 || A->ncols < 0) return OFRR_ERR_INVALID_ARGUMENT;
+  if (A->kind == OFRR_OP_DENSE) {
+    if (!dtype_valid(A->dtype)) return OFRR_ERR_BLAS_UNSUPPORTED_TYPE;
+    if (A->nrows > 0 && A->ncols > 0 && (!A->data || A->ld < A->nrows)) return OFRR_ERR_INVALID_ARGUMENT;
+  } else if (A->kind == OFRR_OP_CSR) {
+    if (A->csr.nrows != A->nrows || A->csr.ncols != A->ncols || !A->csr.indptr) return OFRR_ERR_INVALID_ARGUMENT;
+    if (A->csr.nnz > 0 && !A->csr.indices) return OFRR_ERR_INVALID_ARGUMENT;
+    if (!A->csr.a_double && !A->csr.a_single) return OFRR_ERR_INVALID_ARGUMENT;
+  } else {
+    return OFRR_ERR_INVALID_ARGUMENT;
+  }
+  return OFRR_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------------------
+// Rayleigh-Ritz on a basis Q (n x b, type tq): eig_rr.m:46-57.
+// Outputs: Ritz vectors into Vout (n x b, type tq), Ritz values d (device, b, descending).
+// ---------------------------------------------------------------------------------------
+int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype tq, int64_t ldq, int b,
+               ofrr_dtype pmc, ofrr_dtype pmo, ofrr_dtype pAmc, ofrr_dtype pAmo, bool use_gen, double gtol,
+               bool symmetric, void* Vout, int64_t ldvo, double* d) {
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  const int64_t n = op.m();
+  // AV = pmc(matvec(A, 'N', pAmc(Q), pAmc, pAmo)) -- kept in pAmo storage, widened by the Gram gemm
+  const void* Qa = Q;
+  int64_t ldqa = ldq;
+  if (tq != pAmc) {
+    void* w = ws_alloc(ctx, (size_t)n * b * dtype_size(pAmc), &st);
+    if (!w) return st;
+    OFRR_TRY(cast_impl(ctx, tq, pAmc, n, b, Q, ldq, w, n));
+    Qa = w;
+    ldqa = n;
+  }
+  void* AV = ws_alloc(ctx, (size_t)n * b * dtype_size(pAmo), &st);
+  if (!AV) return st;
+  OFRR_TRY(op.apply(ctx, 0, ta, pAmc, Qa, ldqa, b, pAmc, pAmo, AV, n));
+  ofrr_dtype tav = pAmo;
+  if (pAmo != pmc) {  // the MATLAB code rounds to pAmo then converts to pmc: identical values
+    // no storage change needed: gemm widens pAmo to pmc exactly
+  }
+  double *G, *M = nullptr, *U;
+  OFRR_TRY(dmalloc(ctx, &G, (size_t)b * b));
+  OFRR_TRY(dmalloc(ctx, &U, (size_t)b * b));
+  void* tmp = ws_alloc(ctx, (size_t)b * b * dtype_size(pmo), &st);
+  if (!tmp) return st;
+  // VAV = peig(gemm(V, 'T', AV, pmc, pmo))
+  OFRR_TRY(gemm_impl(ctx, 1, 0, tq, tav, pmc, pmo, b, b, n, 1.0, Q, ldq, AV, n, 0.0, tmp, b));
+  OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, G, b));
+  if (use_gen) {
+    OFRR_TRY(dmalloc(ctx, &M, (size_t)b * b));
+    OFRR_TRY(gemm_impl(ctx, 1, 0, tq, tq, pmc, pmo, b, b, n, 1.0, Q, ldq, Q, ldq, 0.0, tmp, b));
+    OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, M, b));
+    if (gtol != 0.0) {
+      k_add_diag<<<(b + 255) / 256, 256, 0, ctx->stream>>>(b, M, b, gtol);
+      OFRR_LAUNCHED(ctx, "k_add_diag");
+    }
+  }
+  OFRR_TRY(geig_dev(ctx, b, G, b, M, b, symmetric ? 1 : 0, d, U, b));
+  // V = gemm(V, 'N', U, pmc, pmo) then back to V's precision
+  void* Vn = Vout;
+  int64_t ldvn = ldvo;
+  if (pmo != tq || Vout == Q) {
+    Vn = ws_alloc(ctx, (size_t)n * b * dtype_size(pmo), &st);
+    if (!Vn) return st;
+    ldvn = n;
+  }
+  OFRR_TRY(gemm_impl(ctx, 0, 0, tq, OFRR_F64, pmc, pmo, n, b, b, 1.0, Q, ldq, U, b, 0.0, Vn, ldvn));
+  if (Vn != Vout) OFRR_TRY(cast_impl(ctx, pmo, tq, n, b, Vn, ldvn, Vout, ldvo));
+  return OFRR_SUCCESS;
+}
+
+// FP64 residuals of Ritz pairs (X in type tx), normalised by normA and ||x||
+int residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* X, int64_t ldx, int k, const double* lam_host,
+                  double normA, double* out_host) {
+  if (k <= 0) return OFRR_SUCCESS;
+  WsScope scope(ctx);
+  const int64_t n = op.m();
+  double *X64, *AX, *lam, *res, *nrm;
+  OFRR_TRY(dmalloc(ctx, &X64, (size_t)n * k));
+  OFRR_TRY(dmalloc(ctx, &AX, (size_t)n * k));
+  OFRR_TRY(dmalloc(ctx, &lam, (size_t)k));
+  OFRR_TRY(dmalloc(ctx, &res, (size_t)2 * k));
+  nrm = res + k;
+  OFRR_TRY(cast_impl(ctx, tx, OFRR_F64, n, k, X, ldx, X64, n));
+  OFRR_TRY(op.apply(ctx, 0, OFRR_F64, OFRR_F64, X64, n, k, OFRR_F64, OFRR_F64, AX, n));
+  OFRR_CUDA(cudaMemcpyAsync(lam, lam_host, sizeof(double) * k, cudaMemcpyHostToDevice, ctx->stream));
+  OFRR_TRY(residual_columns(ctx, n, k, AX, n, X64, n, lam, res));
+  OFRR_TRY(column_norms(ctx, OFRR_F64, n, k, X64, n, nrm));
+  std::vector<double> h(2 * k);
+  OFRR_CUDA(cudaMemcpyAsync(h.data(), res, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, ctx->stream));
+  OFRR_TRY(sync_and_check(ctx));
+  if (normA <= 0) {
+    normA = 0;
+    for (int j = 0; j < k; ++j) normA = std::max(normA, std::fabs(lam_host[j]));
+    if (normA == 0) normA = 1;
+  }
+  for (int j = 0; j < k; ++j) out_host[j] = (h[k + j] > 0) ? h[j] / (normA * h[k + j]) : INFINITY;
+  return OFRR_SUCCESS;
+}
+
+}  // namespace
+}  // namespace ofrr
+
+using namespace ofrr;
+
+extern "C" void ofrr_options_default(ofrr_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->mode = OFRR_MODE_REFERENCE;
+  o->maxiter = 5;  // subspace_iter_eig.m:108-110
+  o->step_size = 1;
+  o->block = 8;
+  o->nev = 8;
+  o->kdim = 0;  // 0 -> maxiter (arnoldi_hess_eig.m:165-167)
+  o->tol = 0.0;
+  o->use_generalized = 1;
+  o->generalized_tol = 0.0;
+  o->select_tol = -1.0;
+  o->seed = 42;
+  o->use_start_block = 0;
+  o->orth = OFRR_ORTH_HESSENBERG;
+  o->reorth = 1;
+  o->p_compute = o->p_output = OFRR_F64;
+  o->p_hess_compute = o->p_hess_output = OFRR_F64;
+  o->p_rr_compute = o->p_rr_output = OFRR_F64;
+  o->check_every = 1;
+}
+
+extern "C" int ofrr_rr_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, int64_t ncols, void* V,
+                           int64_t ldv, double* evals) {
+  if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
+  OFRR_TRY(validate_op(A));
+  OFRR_TRY(validate_options(opt));
+  if (A->nrows != A->ncols) return OFRR_ERR_BLAS_INVALID_SIZE;
+  const int64_t n = A->nrows;
+  if (ncols <= 0 || n == 0) return OFRR_SUCCESS;
+  if (!V || ldv < n || !evals || ncols > 1024) return OFRR_ERR_INVALID_ARGUMENT;
+  const Precisions P = precisions_of(opt);
+  WsScope scope(ctx);
+  Op op{A};
+  double* d;
+  OFRR_TRY(dmalloc(ctx, &d, (size_t)ncols));
+  // eig_rr on V (type p_output): pmc = p_rr_compute, pmo = p_rr_output, A-matvec in (p_compute, p_output)
+  OFRR_TRY(rr_eig_dev(ctx, op, P.po, V, P.po, ldv, (int)ncols, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
+                      opt->generalized_tol, A->symmetric != 0, V, ldv, d));
+  OFRR_CUDA(cudaMemcpyAsync(evals, d, sizeof(double) * ncols, cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_and_check(ctx);
+}
+
+extern "C" int ofrr_ofrr_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_operator* B, const ofrr_options* opt,
+                             int64_t ncols, void* V, int64_t ldv, double* evals) {
+  if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
+  OFRR_TRY(validate_op(A));
+  OFRR_TRY(validate_op(B));
+  OFRR_TRY(validate_options(opt));
+  const int64_t n = A->nrows;
+  if (A->ncols != n || B->nrows != n || B->ncols != n) return OFRR_ERR_BLAS_INVALID_SIZE;
+  if (ncols <= 0 || n == 0) return OFRR_SUCCESS;
+  if (!V || ldv < n || !evals || ncols > 1024) return OFRR_ERR_INVALID_ARGUMENT;
+  const Precisions P = precisions_of(opt);
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  Op opA{A}, opB{B};
+  const int b = (int)ncols;
+  void *AV, *BV, *tmp, *Vn;
+  double *G, *M, *U, *d;
+  if (!(AV = ws_alloc(ctx, (size_t)n * b * dtype_size(P.pc), &st))) return st;
+  if (!(BV = ws_alloc(ctx, (size_t)n * b * dtype_size(P.pc), &st))) return st;
+  if (!(tmp = ws_alloc(ctx, (size_t)b * b * dtype_size(P.pro), &st))) return st;
+  if (!(Vn = ws_alloc(ctx, (size_t)n * b * dtype_size(P.pro), &st))) return st;
+  OFRR_TRY(dmalloc(ctx, &G, (size_t)b * b));
+  OFRR_TRY(dmalloc(ctx, &M, (size_t)b * b));
+  OFRR_TRY(dmalloc(ctx, &U, (size_t)b * b));
+  OFRR_TRY(dmalloc(ctx, &d, (size_t)b));
+  OFRR_TRY(opA.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.pc, AV, n));
+  OFRR_TRY(opB.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.pc, BV, n));
+  OFRR_TRY(gemm_impl(ctx, 1, 0, P.po, P.pc, P.prc, P.pro, b, b, n, 1.0, V, ldv, AV, n, 0.0, tmp, b));
+  OFRR_TRY(cast_impl(ctx, P.pro, OFRR_F64, b, b, tmp, b, G, b));
+  OFRR_TRY(gemm_impl(ctx, 1, 0, P.po, P.pc, P.prc, P.pro, b, b, n, 1.0, V, ldv, BV, n, 0.0, tmp, b));
+  OFRR_TRY(cast_impl(ctx, P.pro, OFRR_F64, b, b, tmp, b, M, b));
+  if (opt->generalized_tol != 0.0) {
+    k_add_diag<<<(b + 255) / 256, 256, 0, ctx->stream>>>(b, M, b, opt->generalized_tol);
+    OFRR_LAUNCHED(ctx, "k_add_diag");
+  }
+  OFRR_TRY(geig_dev(ctx, b, G, b, M, b, 1, d, U, b));
+  OFRR_TRY(gemm_impl(ctx, 0, 0, P.po, OFRR_F64, P.prc, P.pro, n, b, b, 1.0, V, ldv, U, b, 0.0, Vn, n));
+  OFRR_TRY(cast_impl(ctx, P.pro, P.po, n, b, Vn, n, V, ldv));
+  OFRR_CUDA(cudaMemcpyAsync(evals, d, sizeof(double) * b, cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_and_check(ctx);
+}
+
+extern "C" int ofrr_residual_norms(ofrr_ctx* ctx, const ofrr_operator* A, ofrr_dtype tx, int64_t ncols, const void* X,
+                                   int64_t ldx, const double* evals, double normA, double* resid) {
+  if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
+  OFRR_TRY(validate_op(A));
+  if (!dtype_valid(tx)) return OFRR_ERR_BLAS_UNSUPPORTED_TYPE;
+  if (ncols <= 0) return OFRR_SUCCESS;
+  if (!X || !evals || !resid || ldx < A->nrows || A->nrows != A->ncols) return OFRR_ERR_INVALID_ARGUMENT;
+  WsScope scope(ctx);
+  Op op{A};
+  return residuals_dev(ctx, op, tx, X, ldx, (int)ncols, evals, normA, resid);
+}
+
+// ======================================================================================
+// subspace iteration SVD and RR-SVD
+// ======================================================================================
+namespace ofrr {
+namespace {
+
+__global__ void k_scale_f64(int64_t m, int64_t n, double* X, int64_t ldx, double s) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x)
+    X[(e % m) + (e / m) * ldx] *= s;
+}
+
+// Z = Lu^-T Y, W = Lv^-T X from the SVD of C = Lu^-1 B Lv^-T is the same pencil as
+// eig([[0,B],[B',0]], blkdiag(UU,VV)+tau I) (svd_rr.m:58-77).  We form the symmetric
+// 2b x 2b pencil explicitly and hand it to the FP64 generalized solver, which keeps the
+// reference's normalisation (M-orthonormal eigenvectors, hence the sqrt(2) of svd_rr.m:87-91).
+__global__ void k_build_aug(int b, const double* B, const double* UU, const double* VV, double* Aext, double* Mext,
+                            double tau) {
+  const int nn = 2 * b;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nn * nn; e += gridDim.x * blockDim.x) {
+    const int i = e % nn, j = e / nn;
+    double a = 0.0, m = 0.0;
+    if (i < b && j >= b) a = B[i + (j - b) * b];
+    if (i >= b && j < b) a = B[j + (i - b) * b];
+    if (i < b && j < b) m = UU[i + j * b];
+    if (i >= b && j >= b) m = VV[(i - b) + (j - b) * b];
+    if (i == j) m += tau;
+    Aext[e] = a;
+    Mext[e] = m;
+  }
+}
+
+int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* V, ofrr_dtype tq, int64_t ldu,
+               int64_t ldv, int b, ofrr_dtype pmc, ofrr_dtype pmo, ofrr_dtype pAmc, ofrr_dtype pAmo, bool use_gen,
+               double gtol, void* Uout, int64_t lduo, void* Vout, int64_t ldvo, double* s_dev) {
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  const int64_t m = op.m(), n = op.n();
+  if (!use_gen) return OFRR_ERR_NOT_IMPLEMENTED;  // svd(UAV) path: the oblique bases need the pencil
+  const void* Va = V;
+  int64_t ldva = ldv;
+  if (tq != pAmc) {
+    void* w = ws_alloc(ctx, (size_t)n * b * dtype_size(pAmc), &st);
+    if (!w) return st;
+    OFRR_TRY(cast_impl(ctx, tq, pAmc, n, b, V, ldv, w, n));
+    Va = w;
+    ldva = n;
+  }
+  void* AV = ws_alloc(ctx, (size_t)m * b * dtype_size(pAmo), &st);
+  if (!AV) return st;
+  OFRR_TRY(op.apply(ctx, 0, ta, pAmc, Va, ldva, b, pAmc, pAmo, AV, m));
+  double *B, *UU, *VV, *Aext, *Mext, *X, *d;
+  OFRR_TRY(dmalloc(ctx, &B, (size_t)b * b));
+  OFRR_TRY(dmalloc(ctx, &UU, (size_t)b * b));
+  OFRR_TRY(dmalloc(ctx, &VV, (size_t)b * b));
+  OFRR_TRY(dmalloc(ctx, &Aext, (size_t)4 * b * b));
+  OFRR_TRY(dmalloc(ctx, &Mext, (size_t)4 * b * b));
+  OFRR_TRY(dmalloc(ctx, &X, (size_t)4 * b * b));
+  OFRR_TRY(dmalloc(ctx, &d, (size_t)2 * b));
+  void* tmp = ws_alloc(ctx, (size_t)b * b * dtype_size(pmo), &st);
+  if (!tmp) return st;
+  OFRR_TRY(gemm_impl(ctx, 1, 0, tq, pAmo, pmc, pmo, b, b, m, 1.0, U, ldu, AV, m, 0.0, tmp, b));
+  OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, B, b));
+  OFRR_TRY(gemm_impl(ctx, 1, 0, tq, tq, pmc, pmo, b, b, m, 1.0, U, ldu, U, ldu, 0.0, tmp, b));
+  OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, UU, b));
+  OFRR_TRY(gemm_impl(ctx, 1, 0, tq, tq, pmc, pmo, b, b, n, 1.0, V, ldv, V, ldv, 0.0, tmp, b));
+  OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, VV, b));
+  k_build_aug<<<grid_for(4 * b * b, 256), 256, 0, ctx->stream>>>(b, B, UU, VV, Aext, Mext, gtol);
+  OFRR_LAUNCHED(ctx, "k_build_aug");
+  OFRR_TRY(geig_dev(ctx, 2 * b, Aext, 2 * b, Mext, 2 * b, 1, d, X, 2 * b));
+  OFRR_CUDA(cudaMemcpyAsync(s_dev, d, sizeof(double) * b, cudaMemcpyDeviceToDevice, ctx->stream));
+  // Z = X(1:b, 1:b), W = X(b+1:2b, 1:b), both rounded to pmo (svd_rr.m:81-82); U = sqrt2 * U Z
+  void* Zp = ws_alloc(ctx, (size_t)b * b * dtype_size(pmo), &st);
+  void* Wp = ws_alloc(ctx, (size_t)b * b * dtype_size(pmo), &st);
+  if (!Zp || !Wp) return st;
+  OFRR_TRY(cast_impl(ctx, OFRR_F64, pmo, b, b, X, 2 * b, Zp, b));
+  OFRR_TRY(cast_impl(ctx, OFRR_F64, pmo, b, b, X + b, 2 * b, Wp, b));
+  double* Un64;
+  double* Vn64;
+  OFRR_TRY(dmalloc(ctx, &Un64, (size_t)m * b));
+  OFRR_TRY(dmalloc(ctx, &Vn64, (size_t)n * b));
+  // gemm in pmc with pmo output, then scaled by pmo(sqrt 2) in pmo: emulate by rounding through pmo
+  void* Uo = ws_alloc(ctx, (size_t)m * b * dtype_size(pmo), &st);
+  void* Vo = ws_alloc(ctx, (size_t)n * b * dtype_size(pmo), &st);
+  if (!Uo || !Vo) return st;
+  OFRR_TRY(gemm_impl(ctx, 0, 0, tq, pmo, pmc, pmo, m, b, b, 1.0, U, ldu, Zp, b, 0.0, Uo, m));
+  OFRR_TRY(gemm_impl(ctx, 0, 0, tq, pmo, pmc, pmo, n, b, b, 1.0, V, ldv, Wp, b, 0.0, Vo, n));
+  OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, m, b, Uo, m, Un64, m));
+  OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, n, b, Vo, n, Vn64, n));
+  const double r2 = 1.4142135623730951;
+  k_scale_f64<<<grid_for(m * b, 256), 256, 0, ctx->stream>>>(m, b, Un64, m, r2);
+  OFRR_LAUNCHED(ctx, "k_scale_f64");
+  k_scale_f64<<<grid_for(n * b, 256), 256, 0, ctx->stream>>>(n, b, Vn64, n, r2);
+  OFRR_LAUNCHED(ctx, "k_scale_f64");
+  OFRR_TRY(cast_impl(ctx, OFRR_F64, tq, m, b, Un64, m, Uout, lduo));
+  OFRR_TRY(cast_impl(ctx, OFRR_F64, tq, n, b, Vn64, n, Vout, ldvo));
+  return OFRR_SUCCESS;
+}
+
+__global__ void k_rescol2(int64_t m, int64_t n, const double* AV, const double* U, const double* s, double* out) {
+  // ||A v_j - s_j u_j|| with unit u, v (computed after normalisation): FP64
+  __shared__ double red[32];
+  for (int64_t j = blockIdx.x; j < n; j += gridDim.x) {
+    double acc = 0.0;
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+      double r = AV[i + j * m] - s[j] * U[i + j * m];
+      acc = fma(r, r, acc);
+    }
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+      out[j] = sqrt(t);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_normalize_cols(int64_t m, int64_t n, double* X, const double* nrm) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x) {
+    const double s = nrm[e / m];
+    if (s > 0) X[e] /= s;
+  }
+}
+
+int svd_residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* U, int64_t ldu, const void* V, int64_t ldv,
+                      int k, const double* s_host, double normA, double* out_host) {
+  if (k <= 0) return OFRR_SUCCESS;
+  WsScope scope(ctx);
+  const int64_t m = op.m(), n = op.n();
+  double *U64, *V64, *AV, *ATU, *sd, *nr;
+  OFRR_TRY(dmalloc(ctx, &U64, (size_t)m * k));
+  OFRR_TRY(dmalloc(ctx, &V64, (size_t)n * k));
+  OFRR_TRY(dmalloc(ctx, &AV, (size_t)m * k));
+  OFRR_TRY(dmalloc(ctx, &ATU, (size_t)n * k));
+  OFRR_TRY(dmalloc(ctx, &sd, (size_t)k));
+  OFRR_TRY(dmalloc(ctx, &nr, (size_t)4 * k));
+  OFRR_TRY(cast_impl(ctx, tx, OFRR_F64, m, k, U, ldu, U64, m));
+  OFRR_TRY(cast_impl(ctx, tx, OFRR_F64, n, k, V, ldv, V64, n));
+  OFRR_TRY(column_norms(ctx, OFRR_F64, m, k, U64, m, nr));
+  OFRR_TRY(column_norms(ctx, OFRR_F64, n, k, V64, n, nr + k));
+  k_normalize_cols<<<grid_for(m * k, 256), 256, 0, ctx->stream>>>(m, k, U64, nr);
+  OFRR_LAUNCHED(ctx, "k_normalize_cols");
+  k_normalize_cols<<<grid_for(n * k, 256), 256, 0, ctx->stream>>>(n, k, V64, nr + k);
+  OFRR_LAUNCHED(ctx, "k_normalize_cols");
+  OFRR_TRY(op.apply(ctx, 0, OFRR_F64, OFRR_F64, V64, n, k, OFRR_F64, OFRR_F64, AV, m));
+  OFRR_TRY(op.apply(ctx, 1, OFRR_F64, OFRR_F64, U64, m, k, OFRR_F64, OFRR_F64, ATU, n));
+  OFRR_CUDA(cudaMemcpyAsync(sd, s_host, sizeof(double) * k, cudaMemcpyHostToDevice, ctx->stream));
+  k_rescol2<<<k, 256, 0, ctx->stream>>>(m, k, AV, U64, sd, nr + 2 * k);
+  OFRR_LAUNCHED(ctx, "k_rescol2");
+  k_rescol2<<<k, 256, 0, ctx->stream>>>(n, k, ATU, V64, sd, nr + 3 * k);
+  OFRR_LAUNCHED(ctx, "k_rescol2");
+  std::vector<double> h(2 * k);
+  OFRR_CUDA(cudaMemcpyAsync(h.data(), nr + 2 * k, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, ctx->stream));
+  OFRR_TRY(sync_and_check(ctx));
+  if (normA <= 0) {
+    normA = 0;
+    for (int j = 0; j < k; ++j) normA = std::max(normA, std::fabs(s_host[j]));
+    if (normA == 0) normA = 1;
+  }
+  for (int j = 0; j < k; ++j) out_host[j] = std::max(h[j], h[k + j]) / normA;
+  return OFRR_SUCCESS;
+}
+
+}  // namespace
+}  // namespace ofrr
+
+extern "C" int ofrr_rr_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, int64_t ncols, void* U,
+                           int64_t ldu, double* s, void* V, int64_t ldv) {
+  if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
+  OFRR_TRY(validate_op(A));
+  OFRR_TRY(validate_options(opt));
+  const int64_t m = A->nrows, n = A->ncols;
+  if (ncols <= 0 || m == 0 || n == 0) return OFRR_SUCCESS;
+  if (!U || !V || !s || ldu < m || ldv < n || ncols > 512) return OFRR_ERR_INVALID_ARGUMENT;
+  const Precisions P = precisions_of(opt);
+  WsScope scope(ctx);
+  Op op{A};
+  double* d;
+  OFRR_TRY(dmalloc(ctx, &d, (size_t)ncols));
+  const int b = (int)ncols;
+  int st = OFRR_SUCCESS;
+  void* Ut = ws_alloc(ctx, (size_t)m * b * dtype_size(P.po), &st);
+  void* Vt = ws_alloc(ctx, (size_t)n * b * dtype_size(P.po), &st);
+  if (!Ut || !Vt) return st;
+  OFRR_TRY(rr_svd_dev(ctx, op, P.po, U, V, P.po, ldu, ldv, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
+                      opt->generalized_tol, Ut, m, Vt, n, d));
+  OFRR_CUDA(cudaMemcpy2DAsync(U, ldu * dtype_size(P.po), Ut, m * dtype_size(P.po), m * dtype_size(P.po), b,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+  OFRR_CUDA(cudaMemcpy2DAsync(V, ldv * dtype_size(P.po), Vt, n * dtype_size(P.po), n * dtype_size(P.po), b,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+  OFRR_CUDA(cudaMemcpyAsync(s, d, sizeof(double) * b, cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_and_check(ctx);
+}
+
+// ======================================================================================
+// Krylov eigensolver: Hessenberg process with restarts (arnoldi_hess_eig.m:51-107)
+// ======================================================================================
+extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, const void* v0,
+                                void* X, int64_t ldx, double* evals, double* resid, ofrr_info* info) {
+  if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
+  OFRR_TRY(validate_op(A));
+  OFRR_TRY(validate_options(opt));
+  if (A->nrows != A->ncols) return OFRR_ERR_BLAS_INVALID_SIZE;
+  if (opt->orth != OFRR_ORTH_HESSENBERG) return OFRR_ERR_NOT_IMPLEMENTED;
+  const int64_t n = A->nrows;
+  const int kdim = opt->kdim > 0 ? opt->kdim : opt->maxiter;
+  const int nev = (int)std::min<int64_t>(opt->nev, n);
+  if (n == 0 || nev <= 0) return OFRR_SUCCESS;
+  if (!X || ldx < n || !evals || kdim < 1 || kdim + 1 > 1024 || (opt->use_start_block && !v0))
+    return OFRR_ERR_INVALID_ARGUMENT;
+  const Precisions P = precisions_of(opt);
+  const ofrr_dtype po = P.po, pc = P.pc;
+  const bool symmetric = A->symmetric != 0;
+  const int nb = kdim + 1;
+  const double stol = opt->select_tol < 0 ? dtype_eps(po) : opt->select_tol;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  Op op{A};
+  void *V, *pivrows, *pvals, *Vr;
+  double *R, *d;
+  int *sel, *perm, *stop;
+  if (!(V = ws_alloc(ctx, (size_t)n * nb * dtype_size(po), &st))) return st;
+  if (!(Vr = ws_alloc(ctx, (size_t)n * nb * dtype_size(po), &st))) return st;
+  if (!(pivrows = ws_alloc(ctx, (size_t)nb * nb * dtype_size(po), &st))) return st;
+  if (!(pvals = ws_alloc(ctx, (size_t)nb * dtype_size(po), &st))) return st;
+  OFRR_TRY(dmalloc(ctx, &R, (size_t)nb * nb));
+  OFRR_TRY(dmalloc(ctx, &d, (size_t)nb));
+  OFRR_TRY(dmalloc(ctx, &sel, (size_t)nb));
+  OFRR_TRY(dmalloc(ctx, &perm, (size_t)nb));
+  OFRR_TRY(dmalloc(ctx, &stop, (size_t)4));
+  OFRR_TRY(fill_zero(ctx, V, (size_t)n * nb * dtype_size(po)));
+  if (opt->use_start_block) {
+    OFRR_CUDA(cudaMemcpyAsync(V, v0, (size_t)n * dtype_size(po), cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
+    OFRR_TRY(ofrr_randn(ctx, opt->seed, n, 1, po, V, n));
+  }
+  int tits = 1, cycles = 0, nmv = 0;
+  std::vector<double> hd(nb), hres(nb, INFINITY);
+  int hstop[2];
+  int ncols_final = 0;
+  bool have_result = false;
+  while (tits < opt->maxiter) {
+    // column 0: pivot + scale; break if |pivot| < select_tol (arnoldi_hess_eig.m:64-71)
+    OFRR_TRY(hess_krylov_first(ctx, po, pc, n, nb, V, n, stol, sel, perm, pivrows, pvals, R, stop));
+    OFRR_CUDA(cudaMemcpyAsync(hstop, stop, sizeof(int) * 2, cudaMemcpyDeviceToHost, ctx->stream));
+    OFRR_TRY(sync_and_check(ctx));
+    if (hstop[0] >= 0) break;  // start vector below select_tol
+    int ncols = nb;
+    for (int i = 1; i <= kdim; ++i) {
+      // V(:,i) = po(matvec(A, pc(V(:,i-1)), pc, pc)); column i-1 was scaled by the previous step
+      OFRR_TRY(op.apply(ctx, 0, po, po, (char*)V + (size_t)(i - 1) * n * dtype_size(po), n, 1, pc, po,
+                        (char*)V + (size_t)i * n * dtype_size(po), n));
+      OFRR_TRY(hess_krylov_step(ctx, po, pc, n, nb, i, V, n, stol, sel, perm, pivrows, pvals, R, stop));
+      OFRR_TRY(hess_scale_col(ctx, po, pc, n, i, V, n, sel, pvals, stop));
+    }
+    OFRR_CUDA(cudaMemcpyAsync(hstop, stop, sizeof(int) * 2, cudaMemcpyDeviceToHost, ctx->stream));
+    OFRR_TRY(sync_and_check(ctx));
+    int steps = kdim;
+    if (hstop[0] >= 0) {  // breakdown at step hstop[0]: invariant subspace found
+      steps = hstop[0] - 1;
+      ncols = hstop[0];
+      tits = opt->maxiter;
+    } else {
+      tits += kdim;
+    }
+    nmv += steps;
+    cycles++;
+    // RR on the ncols columns (generalized, eig_rr.m with use_generalized = true)
+    OFRR_TRY(rr_eig_dev(ctx, op, po, V, po, n, ncols, pc, po, pc, pc, true, opt->generalized_tol, symmetric, Vr, n, d));
+    nmv += ncols;
+    ncols_final = ncols;
+    have_result = true;
+    if (tits < opt->maxiter) {
+      OFRR_CUDA(cudaMemcpyAsync(V, Vr, (size_t)n * dtype_size(po), cudaMemcpyDeviceToDevice, ctx->stream));
+      if (opt->tol > 0) {  // convergence check on the current Ritz pairs (new behaviour)
+        OFRR_CUDA(cudaMemcpyAsync(hd.data(), d, sizeof(double) * ncols, cudaMemcpyDeviceToHost, ctx->stream));
+        OFRR_TRY(sync_and_check(ctx));
+        const int k = std::min(nev, ncols);
+        OFRR_TRY(residuals_dev(ctx, op, po, Vr, n, k, hd.data(), -1.0, hres.data()));
+        bool ok = true;
+        for (int j = 0; j < k; ++j) ok = ok && (hres[j] <= opt->tol);
+        if (ok) break;
+      }
+    }
+  }
+  if (!have_result) return OFRR_ERR_SOLVER_DIVERGENCE;
+  const int k = std::min(nev, ncols_final);
+  OFRR_CUDA(cudaMemcpy2DAsync(X, ldx * dtype_size(po), Vr, n * dtype_size(po), n * dtype_size(po), k,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+  OFRR_CUDA(cudaMemcpyAsync(hd.data(), d, sizeof(double) * ncols_final, cudaMemcpyDeviceToHost, ctx->stream));
+  OFRR_TRY(sync_and_check(ctx));
+  for (int j = 0; j < nev; ++j) evals[j] = (j < k) ? hd[j] : NAN;
+  OFRR_TRY(residuals_dev(ctx, op, po, X, ldx, k, hd.data(), -1.0, hres.data()));
+  if (resid)
+    for (int j = 0; j < nev; ++j) resid[j] = (j < k) ? hres[j] : NAN;
+  int conv = 0;
+  double maxr = 0;
+  for (int j = 0; j < k; ++j) {
+    conv += (opt->tol > 0 && hres[j] <= opt->tol) ? 1 : 0;
+    maxr = std::max(maxr, hres[j]);
+  }
+  if (info) {
+    info->iterations = cycles;
+    info->matvecs = nmv;
+    info->converged = conv;
+    info->basis_width = ncols_final;
+    info->max_residual = maxr;
+    info->escalations = 0;
+    info->status_detail = 0;
+  }
+  if (opt->tol > 0 && conv < k) return OFRR_ERR_SOLVER_MAX_ITERATIONS;
+  return OFRR_SUCCESS;
+}
+
+// ======================================================================================
+// subspace iteration: one precision phase, shared by the reference, FP64 and mixed modes
+// ======================================================================================
+namespace ofrr {
+namespace {
+
+struct PhaseState {
+  int b = 0;           // current basis width
+  int it = 0;          // outer iterations done (all phases)
+  int nmv = 0;         // operator applications (columns)
+  int converged = 0;   // pairs at tol after the last check
+  bool done = false;   // all nev pairs at tol
+  std::vector<double> d, res, dprev;
+  double delta = INFINITY, delta_prev = INFINITY;
+};
+
+// Ritz-value stagnation test of the low-precision phase: relative change of the top nev values
+bool stagnated(PhaseState& S, int nev, double stag_tol, int iters_in_phase) {
+  double scale = 0;
+  for (int j = 0; j < nev; ++j) scale = std::max(scale, std::fabs(S.d[j]));
+  if (scale == 0) scale = 1;
+  double delta = 0;
+  for (int j = 0; j < nev; ++j) delta = std::max(delta, std::fabs(S.d[j] - S.dprev[j]) / scale);
+  S.delta_prev = S.delta;
+  S.delta = delta;
+  S.dprev = S.d;
+  if (iters_in_phase < 2) return false;
+  return delta <= stag_tol || (iters_in_phase >= 4 && delta > 0.7 * S.delta_prev);
+}
+
+// One phase of subspace_iter_eig.m:60-68 on the iterate V (n x b, type P.po, in the caller's buffer).
+// Exits after maxit iterations, when the nev residuals reach tol (checked every check_every) or,
+// if stag_tol > 0, when the Ritz values stop improving.
+int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* opt, void* V, int64_t ldv, int maxit,
+              double tol, int nev, double stag_tol, PhaseState& S, double* d_dev) {
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  const int64_t n = op.m();
+  const int b0 = S.b;
+  const bool symmetric = op.A->symmetric != 0;
+  void *W, *Q;
+  double* R;
+  int *sel, *perm;
+  if (!(W = ws_alloc(ctx, (size_t)n * b0 * dtype_size(P.po), &st))) return st;
+  if (!(Q = ws_alloc(ctx, (size_t)n * b0 * dtype_size(P.pho), &st))) return st;
+  OFRR_TRY(dmalloc(ctx, &R, (size_t)b0 * b0));
+  OFRR_TRY(dmalloc(ctx, &sel, (size_t)b0));
+  OFRR_TRY(dmalloc(ctx, &perm, (size_t)b0));
+  std::vector<int> hsel(b0);
+  const int check_every = std::max(1, opt->check_every);
+  void* cur = V;
+  int64_t ldcur = ldv;
+  const size_t es = dtype_size(P.po);
+  for (int k = 0; k < maxit && !S.done; ++k) {
+    int b = S.b;
+    for (int s = 0; s < opt->step_size; ++s) {
+      void* dst = (cur == V) ? W : V;
+      int64_t lddst = (cur == V) ? n : ldv;
+      OFRR_TRY(op.apply(ctx, 0, P.po, P.po, cur, ldcur, b, P.pc, P.po, dst, lddst));
+      S.nmv += b;
+      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, dst, lddst, nullptr));
+      cur = dst;
+      ldcur = lddst;
+    }
+    // [Q,~] = hessenberg(V): the economic form drops deselected columns
+    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, n, b, cur, ldcur, Q, n, opt->select_tol, R, sel, perm));
+    OFRR_CUDA(cudaMemcpyAsync(hsel.data(), sel, sizeof(int) * b, cudaMemcpyDeviceToHost, ctx->stream));
+    OFRR_TRY(sync_and_check(ctx));
+    int w = b;
+    OFRR_TRY(compact_columns(ctx, P.pho, n, Q, n, std::vector<int>(hsel.begin(), hsel.begin() + b), &w));
+    if (w == 0) return OFRR_ERR_SOLVER_DIVERGENCE;
+    S.b = b = w;
+    // [V,D] = eig_rr(A, Q), V = po(V)
+    void* dst = (cur == V) ? V : W;
+    int64_t lddst = (cur == V) ? ldv : n;
+    if (P.pho == P.po) {
+      OFRR_TRY(rr_eig_dev(ctx, op, P.po, Q, P.pho, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
+                          opt->generalized_tol, symmetric, dst, lddst, d_dev));
+    } else {
+      void* tmpv = ws_alloc(ctx, (size_t)n * b * dtype_size(P.pho), &st);
+      if (!tmpv) return st;
+      OFRR_TRY(rr_eig_dev(ctx, op, P.po, Q, P.pho, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
+                          opt->generalized_tol, symmetric, tmpv, n, d_dev));
+      OFRR_TRY(cast_impl(ctx, P.pho, P.po, n, b, tmpv, n, dst, lddst));
+    }
+    S.nmv += b;
+    S.it++;
+    cur = dst;
+    ldcur = lddst;
+    const int kk = std::min(nev, b);
+    const bool last = (k + 1 == maxit);
+    const bool check = tol > 0 && ((S.it % check_every) == 0 || last);
+    if (check || stag_tol > 0) {
+      OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d_dev, sizeof(double) * b, cudaMemcpyDeviceToHost, ctx->stream));
+      OFRR_TRY(sync_and_check(ctx));
+    }
+    if (check) {
+      OFRR_TRY(residuals_dev(ctx, op, P.po, cur, ldcur, kk, S.d.data(), -1.0, S.res.data()));
+      S.converged = 0;
+      for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= tol) ? 1 : 0;
+      if (S.converged >= kk) S.done = true;
+    }
+    if (!S.done && stag_tol > 0 && stagnated(S, kk, stag_tol, k + 1)) break;
+  }
+  if (cur != V)
+    OFRR_CUDA(cudaMemcpy2DAsync(V, ldv * es, cur, ldcur * es, n * es, S.b, cudaMemcpyDeviceToDevice, ctx->stream));
+  return OFRR_SUCCESS;
+}
+
+// One phase of subspace_iter_svd.m:60-75 on U (m x b) and V (n x b), type P.po.
+int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* opt, void* U, int64_t ldu, void* V,
+              int64_t ldv, int maxit, double tol, int nev, double stag_tol, PhaseState& S, double* d_dev) {
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  const int64_t m = op.m(), n = op.n();
+  const int b0 = S.b;
+  void *P1, *Q1, *Ut, *Vt;
+  double* R;
+  int *sel, *perm;
+  if (!(P1 = ws_alloc(ctx, (size_t)m * b0 * dtype_size(P.pho), &st))) return st;
+  if (!(Q1 = ws_alloc(ctx, (size_t)n * b0 * dtype_size(P.pho), &st))) return st;
+  if (!(Ut = ws_alloc(ctx, (size_t)m * b0 * dtype_size(P.pho), &st))) return st;
+  if (!(Vt = ws_alloc(ctx, (size_t)n * b0 * dtype_size(P.pho), &st))) return st;
+  OFRR_TRY(dmalloc(ctx, &R, (size_t)b0 * b0));
+  OFRR_TRY(dmalloc(ctx, &sel, (size_t)2 * b0));
+  OFRR_TRY(dmalloc(ctx, &perm, (size_t)b0));
+  std::vector<int> hsel(2 * b0);
+  const int check_every = std::max(1, opt->check_every);
+  for (int k = 0; k < maxit && !S.done; ++k) {
+    int b = S.b;
+    for (int j = 0; j < opt->step_size; ++j) {
+      OFRR_TRY(op.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.po, U, ldu));
+      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, m, b, U, ldu, nullptr));
+      OFRR_TRY(op.apply(ctx, 1, P.po, P.po, U, ldu, b, P.pc, P.po, V, ldv));
+      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr));
+      S.nmv += 2 * b;
+    }
+    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, m, b, U, ldu, P1, m, opt->select_tol, R, sel, perm));
+    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, n, b, V, ldv, Q1, n, opt->select_tol, R, sel + b0, perm));
+    OFRR_CUDA(cudaMemcpyAsync(hsel.data(), sel, sizeof(int) * 2 * b0, cudaMemcpyDeviceToHost, ctx->stream));
+    OFRR_TRY(sync_and_check(ctx));
+    int wu = b, wv = b;
+    OFRR_TRY(compact_columns(ctx, P.pho, m, P1, m, std::vector<int>(hsel.begin(), hsel.begin() + b), &wu));
+    OFRR_TRY(compact_columns(ctx, P.pho, n, Q1, n, std::vector<int>(hsel.begin() + b0, hsel.begin() + b0 + b), &wv));
+    const int w = std::min(wu, wv);  // svd_rr.m:61 keeps k = min(ku, kv)
+    if (w == 0) return OFRR_ERR_SOLVER_DIVERGENCE;
+    S.b = b = w;
+    OFRR_TRY(rr_svd_dev(ctx, op, P.po, P1, Q1, P.pho, m, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
+                        opt->generalized_tol, Ut, m, Vt, n, d_dev));
+    OFRR_TRY(cast_impl(ctx, P.pho, P.po, m, b, Ut, m, U, ldu));
+    OFRR_TRY(cast_impl(ctx, P.pho, P.po, n, b, Vt, n, V, ldv));
+    S.nmv += b;
+    S.it++;
+    const int kk = std::min(nev, b);
+    const bool last = (k + 1 == maxit);
+    const bool check = tol > 0 && ((S.it % check_every) == 0 || last);
+    if (check || stag_tol > 0) {
+      OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d_dev, sizeof(double) * b, cudaMemcpyDeviceToHost, ctx->stream));
+      OFRR_TRY(sync_and_check(ctx));
+    }
+    if (check) {
+      OFRR_TRY(svd_residuals_dev(ctx, op, P.po, U, ldu, V, ldv, kk, S.d.data(), -1.0, S.res.data()));
+      S.converged = 0;
+      for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= tol) ? 1 : 0;
+      if (S.converged >= kk) S.done = true;
+    }
+    if (!S.done && stag_tol > 0 && stagnated(S, kk, stag_tol, k + 1)) break;
+  }
+  return OFRR_SUCCESS;
+}
+
+// low-precision phase settings of the mixed mode
+Precisions mixed_low(const ofrr_options* o) {
+  Precisions p;
+  p.po = (o->p_output == OFRR_BF16) ? OFRR_BF16 : OFRR_F16;  // 16-bit basis storage
+  p.pho = p.po;
+  p.pc = p.phc = p.prc = OFRR_F32;  // FP32 accumulation
+  p.pro = OFRR_F32;                 // Gram matrices kept in FP32 (not rounded to 16 bits), then FP64
+  return p;
+}
+Precisions all_f64() {
+  Precisions p;
+  p.pc = p.po = p.phc = p.pho = p.prc = p.pro = OFRR_F64;
+  return p;
+}
+
+void fill_info(ofrr_info* info, const PhaseState& S, int nev, int escalations) {
+  if (!info) return;
+  double maxr = 0;
+  for (int j = 0; j < std::min(nev, S.b); ++j) maxr = std::max(maxr, S.res[j]);
+  info->iterations = S.it;
+  info->matvecs = S.nmv;
+  info->converged = S.converged;
+  info->basis_width = S.b;
+  info->max_residual = maxr;
+  info->escalations = escalations;
+  info->status_detail = 0;
+}
+
+}  // namespace
+}  // namespace ofrr
+
+// ======================================================================================
+// subspace iteration eigensolver (si_eig)
+// ======================================================================================
+extern "C" int ofrr_si_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, void* V, int64_t ldv,
+                           double* evals, double* resid, ofrr_info* info) {
+  if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
+  OFRR_TRY(validate_op(A));
+  OFRR_TRY(validate_options(opt));
+  if (A->nrows != A->ncols) return OFRR_ERR_BLAS_INVALID_SIZE;
+  const int64_t n = A->nrows;
+  const int b0 = (int)std::min<int64_t>(opt->block, n);
+  if (n == 0 || b0 == 0) return OFRR_SUCCESS;
+  if (!V || ldv < n || !evals) return OFRR_ERR_INVALID_ARGUMENT;
+  if (b0 > 1024) return OFRR_ERR_BLAS_INVALID_SIZE;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  Op op{A};
+  const int nev = std::min(opt->nev > 0 ? opt->nev : b0, b0);
+  PhaseState S;
+  S.b = b0;
+  S.d.assign(b0, 0.0);
+  S.dprev.assign(b0, 0.0);
+  S.res.assign(b0, INFINITY);
+  double* d;
+  OFRR_TRY(dmalloc(ctx, &d, (size_t)b0));
+  int escalations = 0;
+  // the caller's V holds p_output (reference mode) or FP64 (FP64 and mixed modes)
+  const ofrr_dtype tV = (opt->mode == OFRR_MODE_REFERENCE) ? opt->p_output : OFRR_F64;
+  if (opt->mode == OFRR_MODE_MIXED) {
+    const Precisions L = mixed_low(opt);
+    void* V16 = ws_alloc(ctx, (size_t)n * b0 * dtype_size(L.po), &st);
+    if (!V16) return st;
+    if (opt->use_start_block) OFRR_TRY(cast_impl(ctx, OFRR_F64, L.po, n, b0, V, ldv, V16, n));
+    else OFRR_TRY(ofrr_randn(ctx, opt->seed, n, b0, L.po, V16, n));
+    OFRR_TRY(scalecols_impl(ctx, L.po, L.pc, n, b0, V16, n, nullptr));
+    const double stag = (L.po == OFRR_BF16) ? 1e-4 : 1e-5;
+    OFRR_TRY(eig_phase(ctx, op, L, opt, V16, n, opt->maxiter, opt->tol, nev, stag, S, d));
+    OFRR_TRY(cast_impl(ctx, L.po, OFRR_F64, n, S.b, V16, n, V, ldv));
+    escalations = 1;
+    if (!S.done && S.it < opt->maxiter)
+      OFRR_TRY(eig_phase(ctx, op, all_f64(), opt, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d));
+  } else {
+    const Precisions P = precisions_of(opt);
+    if (!opt->use_start_block) OFRR_TRY(ofrr_randn(ctx, opt->seed, n, b0, P.po, V, ldv));
+    OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b0, V, ldv, nullptr));
+    OFRR_TRY(eig_phase(ctx, op, P, opt, V, ldv, opt->maxiter, opt->tol, nev, 0.0, S, d));
+  }
+  OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d, sizeof(double) * S.b, cudaMemcpyDeviceToHost, ctx->stream));
+  OFRR_TRY(sync_and_check(ctx));
+  for (int j = 0; j < b0; ++j) evals[j] = (j < S.b) ? S.d[j] : NAN;
+  if (resid) {
+    if (opt->tol <= 0) OFRR_TRY(residuals_dev(ctx, op, tV, V, ldv, S.b, S.d.data(), -1.0, S.res.data()));
+    for (int j = 0; j < b0; ++j) resid[j] = (j < S.b) ? S.res[j] : NAN;
+  }
+  fill_info(info, S, nev, escalations);
+  if (opt->tol > 0 && !S.done) return OFRR_ERR_SOLVER_MAX_ITERATIONS;
+  return OFRR_SUCCESS;
+}
+
+// ======================================================================================
+// subspace iteration SVD (si_svd)
+// ======================================================================================
+extern "C" int ofrr_si_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, void* U, int64_t ldu,
+                           double* s, void* V, int64_t ldv, double* resid, ofrr_info* info) {
+  if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
+  OFRR_TRY(validate_op(A));
+  OFRR_TRY(validate_options(opt));
+  const int64_t m = A->nrows, n = A->ncols;
+  const int b0 = (int)std::min<int64_t>(opt->block, n);
+  if (m == 0 || n == 0 || b0 == 0) return OFRR_SUCCESS;
+  if (!U || !V || ldu < m || ldv < n || !s) return OFRR_ERR_INVALID_ARGUMENT;
+  if (b0 > 512 || b0 > m) return OFRR_ERR_BLAS_INVALID_SIZE;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  Op op{A};
+  const int nev = std::min(opt->nev > 0 ? opt->nev : b0, b0);
+  PhaseState S;
+  S.b = b0;
+  S.d.assign(b0, 0.0);
+  S.dprev.assign(b0, 0.0);
+  S.res.assign(b0, INFINITY);
+  double* d;
+  OFRR_TRY(dmalloc(ctx, &d, (size_t)b0));
+  int escalations = 0;
+  const ofrr_dtype tV = (opt->mode == OFRR_MODE_REFERENCE) ? opt->p_output : OFRR_F64;
+  if (opt->mode == OFRR_MODE_MIXED) {
+    const Precisions L = mixed_low(opt);
+    void* U16 = ws_alloc(ctx, (size_t)m * b0 * dtype_size(L.po), &st);
+    void* V16 = ws_alloc(ctx, (size_t)n * b0 * dtype_size(L.po), &st);
+    if (!U16 || !V16) return st;
+    if (opt->use_start_block) OFRR_TRY(cast_impl(ctx, OFRR_F64, L.po, n, b0, V, ldv, V16, n));
+    else OFRR_TRY(ofrr_randn(ctx, opt->seed, n, b0, L.po, V16, n));
+    OFRR_TRY(scalecols_impl(ctx, L.po, L.pc, n, b0, V16, n, nullptr));
+    const double stag = (L.po == OFRR_BF16) ? 1e-4 : 1e-5;
+    OFRR_TRY(svd_phase(ctx, op, L, opt, U16, m, V16, n, opt->maxiter, opt->tol, nev, stag, S, d));
+    OFRR_TRY(cast_impl(ctx, L.po, OFRR_F64, m, S.b, U16, m, U, ldu));
+    OFRR_TRY(cast_impl(ctx, L.po, OFRR_F64, n, S.b, V16, n, V, ldv));
+    escalations = 1;
+    if (!S.done && S.it < opt->maxiter)
+      OFRR_TRY(svd_phase(ctx, op, all_f64(), opt, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d));
+  } else {
+    const Precisions P = precisions_of(opt);
+    if (!opt->use_start_block) OFRR_TRY(ofrr_randn(ctx, opt->seed, n, b0, P.po, V, ldv));
+    OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b0, V, ldv, nullptr));
+    OFRR_TRY(svd_phase(ctx, op, P, opt, U, ldu, V, ldv, opt->maxiter, opt->tol, nev, 0.0, S, d));
+  }
+  OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d, sizeof(double) * S.b, cudaMemcpyDeviceToHost, ctx->stream));
+  OFRR_TRY(sync_and_check(ctx));
+  for (int j = 0; j < b0; ++j) s[j] = (j < S.b) ? S.d[j] : NAN;
+  if (resid) {
+    if (opt->tol <= 0) OFRR_TRY(svd_residuals_dev(ctx, op, tV, U, ldu, V, ldv, S.b, S.d.data(), -1.0, S.res.data()));
+    for (int j = 0; j < b0; ++j) resid[j] = (j < S.b) ? S.res[j] : NAN;
+  }
+  fill_info(info, S, nev, escalations);
+  if (opt->tol > 0 && !S.done) return OFRR_ERR_SOLVER_MAX_ITERATIONS;
+  return OFRR_SUCCESS;
+}
