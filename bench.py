@@ -50,22 +50,27 @@ def dist_env():
     return rank, world, local
 
 
-def make_problem_gpu(seed=42):
-    """A = U diag(s) V' generated on the device (FP64).  Input synthesis only."""
-    import torch
+def make_problem_host(seed=42):
+    """A = U diag(s) V' in FP64 on the host: U, V = Q factors of seeded Gaussian blocks (the library's
+    counter-based generator), sign-fixed; s geometric from 1 to 1e-6.  Input synthesis only."""
     from mixedprecisionofrr_gb300 import api
 
-    G1 = api.randn(seed, M_ROWS, N_COLS).contiguous()
-    G2 = api.randn(seed + 1, N_COLS, N_COLS).contiguous()
-    U, R1 = torch.linalg.qr(G1)
-    U = U * torch.sign(torch.diagonal(R1))[None, :]
-    V, R2 = torch.linalg.qr(G2)
-    V = V * torch.sign(torch.diagonal(R2))[None, :]
-    s = torch.tensor(1e-6 ** (np.arange(N_COLS) / (N_COLS - 1)), dtype=torch.float64, device="cuda")
-    A = (U * s[None, :]) @ V.T
-    Acm = api.empty_cm(M_ROWS, N_COLS, api.PREC["double"])
-    Acm.copy_(A)
-    return Acm, s.cpu().numpy()
+    def haar(n, k, sd):
+        G = api.randn_host(sd, n, k)
+        Q, R = np.linalg.qr(G)
+        return Q * np.sign(np.diag(R))[None, :]
+
+    U = haar(M_ROWS, N_COLS, seed)
+    V = haar(N_COLS, N_COLS, seed + 1)
+    s = 1e-6 ** (np.arange(N_COLS) / (N_COLS - 1))
+    return (U * s[None, :]) @ V.T, s
+
+
+def make_problem_gpu(seed=42):
+    from mixedprecisionofrr_gb300 import api
+
+    A, s = make_problem_host(seed)
+    return api.to_device_cm(A, api.PREC["double"]), s
 
 
 class ClockSampler:

@@ -45,6 +45,11 @@ class Context:
         self.device = device
         if stream is None:
             stream = torch.cuda.current_stream(device)
+            if stream.cuda_stream == 0:
+                # the library never runs on the legacy default stream: give torch and the library one
+                # shared non-blocking stream so that tensor reads see the library's results in order
+                stream = torch.cuda.Stream(device)
+                torch.cuda.set_stream(stream)
         self.stream = stream
         h = C.c_void_p()
         L.check(self.lib.ofrr_ctx_create(C.byref(h), device, C.c_void_p(stream.cuda_stream)), "ofrr_ctx_create")

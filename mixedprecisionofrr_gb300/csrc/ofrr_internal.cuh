@@ -225,6 +225,8 @@ int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
               int64_t lda, const void* B, int64_t ldb, double beta, void* C, int64_t ldc);
 int csrmm_impl(ofrr_ctx* ctx, const ofrr_csr* A, int trans, ofrr_dtype tx, ofrr_dtype tc, ofrr_dtype ty,
                int64_t nrhs, const void* X, int64_t ldx, void* Y, int64_t ldy);
+int cast_transpose_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, int64_t m, int64_t n, const void* in,
+                        int64_t ldin, void* out, int64_t ldout);
 int cast_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, int64_t m, int64_t n, const void* in,
               int64_t ldin, void* out, int64_t ldout);
 int scalecols_impl(ofrr_ctx* ctx, ofrr_dtype po, ofrr_dtype pc, int64_t m, int64_t n, void* U, int64_t ldu,
@@ -248,6 +250,12 @@ int sygv_dev(ofrr_ctx* ctx, int n, double* A, int lda, double* B, int ldb, doubl
 // eigenvectors, M-normalised; sorted descending by real part.  n <= 256.
 int geig_dev(ofrr_ctx* ctx, int n, const double* G, int ldg, const double* M, int ldm, int symmetric,
              double* w, double* U, int ldu);
+
+// production small solvers (FP32 Jacobi + FP64 refinement, multi-CTA FP64 products), n <= 128:
+// eig(G, M + tau I) (M may be null) and the svd_rr pencil of B with Gram matrices UU, VV
+int geig_fast(ofrr_ctx* ctx, int n, const double* G, const double* M, double tau, double* lam, double* U);
+int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const double* VV, double tau, double* sigma,
+              double* Zf, double* Wf);
 
 // reductions
 int column_norms(ofrr_ctx* ctx, ofrr_dtype t, int64_t m, int64_t n, const void* X, int64_t ldx,

@@ -1,0 +1,407 @@
+// Fast small projected eigenproblems for the production modes (mixed and FP64).
+//
+// GB300 runs FP64 at about 2 FMA/clock per SM, 1/64 of its FP32 rate, so an FP64 Jacobi on one CTA
+// (the reference-semantics solver in smalleig.cu) costs milliseconds for n = 64..128.  This solver
+// keeps FP64 accuracy with almost no FP64 work on any single SM:
+//   1. Cholesky of the Gram matrix M + tau I (FP64, one CTA, n^3/6);
+//   2. reduction C = L^-1 G L^-T by two column-parallel triangular solves (one warp per column);
+//   3. cyclic Jacobi on C in FP32 (one CTA, shared memory) -> eigenvectors W accurate to ~1e-7;
+//   4. two steps of the Ogita-Aishima refinement for symmetric eigenproblems (Ogita & Aishima,
+//      "Iterative refinement for symmetric eigenvalue decomposition", JJIAM 2018): with
+//      P = W'W, T = W'CW (FP64), lambda_i = T_ii / P_ii (Rayleigh quotient) and, for |lambda_j - lambda_i| above a
+//      cluster threshold, E_ij = (T_ij + lambda_j (delta_ij - P_ij)) / (lambda_j - lambda_i), else
+//      E_ij = (delta_ij - P_ij) / 2; W <- W (I + E).  Each step is quadratically convergent, so two
+//      steps take FP32-accurate vectors to FP64 accuracy.  Its products are small FP64 GEMMs spread
+//      over many CTAs (one thread per output entry);
+//   5. sort by descending eigenvalue and back-transform U = L^-T W (M-orthonormal eigenvectors).
+// The SVD form (svd_rr.m's pencil [[0,B],[B',0]] vs blkdiag(U'U, V'V) + tau I) reduces with two
+// Cholesky factors to the SVD of C = Lu^-1 B Lv^-T; its right singular vectors are the eigenvectors
+// of C'C (refined as above), the left ones Y = C W diag(1/sigma).
+#include "ofrr_internal.cuh"
+
+#include <algorithm>
+
+namespace ofrr {
+
+// ---- 1. Cholesky (lower) of M + tau I; batched over blockIdx.x ------------------------------------
+__global__ void __launch_bounds__(256) k_chol_f64(int n, const double* const* Ms, int ldm, double tau,
+                                                  double* const* Ls, int* flag) {
+  extern __shared__ double S[];
+  const double* M = Ms[blockIdx.x];
+  double* L = Ls[blockIdx.x];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  __shared__ double s_maxd;
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e % n, j = e / n;
+    double v = (i >= j) ? M[i + (size_t)j * ldm] : 0.0;
+    if (i == j) v += tau;
+    S[e] = v;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double md = 0;
+    for (int k = 0; k < n; ++k) md = fmax(md, fabs(S[k + k * n]));
+    s_maxd = md;
+  }
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (tid == 0) {
+      double d = S[k + k * n];
+      const double floor_d = s_maxd * 1e-15 + 1e-300;
+      if (!(d > floor_d)) {
+        d = floor_d;
+        if (flag) *flag = 1;
+      }
+      S[k + k * n] = sqrt(d);
+    }
+    __syncthreads();
+    const double dk = S[k + k * n];
+    for (int i = k + 1 + tid; i < n; i += nt) S[i + k * n] /= dk;
+    __syncthreads();
+    const int rem = n - k - 1;
+    for (int e = tid; e < rem * rem; e += nt) {
+      const int i = k + 1 + e % rem, j = k + 1 + e / rem;
+      if (i >= j) S[i + j * n] -= S[i + k * n] * S[j + k * n];
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e % n, j = e / n;
+    L[e] = (i >= j) ? S[e] : 0.0;
+  }
+}
+
+// ---- 2. triangular solves, one warp per right-hand side ------------------------------------------
+// upper == 0: L X = B (forward); upper == 1: L' X = B (backward).  transB: right-hand side j is row j.
+__global__ void __launch_bounds__(128) k_trsm_f64(int n, int nrhs, const double* __restrict__ L, int ldl,
+                                                  const double* __restrict__ B, int ldb, int transB,
+                                                  double* __restrict__ X, int ldx, int upper) {
+  extern __shared__ double xs[];  // 4 warps x n
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int col = blockIdx.x * 4 + w;
+  if (col >= nrhs) return;
+  double* x = xs + (size_t)w * n;
+  for (int t = 0; t < n; ++t) {
+    const int i = upper ? (n - 1 - t) : t;
+    double s = 0.0;
+    if (!upper) {
+      for (int k = lane; k < i; k += 32) s += L[i + (size_t)k * ldl] * x[k];
+    } else {
+      for (int k = i + 1 + lane; k < n; k += 32) s += L[k + (size_t)i * ldl] * x[k];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      const double b = transB ? B[col + (size_t)i * ldb] : B[i + (size_t)col * ldb];
+      x[i] = (b - s) / L[i + (size_t)i * ldl];
+    }
+    __syncwarp();
+  }
+  for (int i = lane; i < n; i += 32) X[i + (size_t)col * ldx] = x[i];
+}
+
+// ---- small FP64 GEMM: C = alpha op(A) op(B) + beta C, one thread per output entry -----------------
+__global__ void __launch_bounds__(64) k_gemm_small_f64(int M, int N, int K, double alpha, const double* __restrict__ A,
+                                                       int lda, int tA, const double* __restrict__ B, int ldb, int tB,
+                                                       double beta, double* __restrict__ C, int ldc) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= M * N) return;
+  const int i = e % M, j = e / M;
+  double s = 0.0;
+  for (int k = 0; k < K; ++k) {
+    const double a = tA ? A[k + (size_t)i * lda] : A[i + (size_t)k * lda];
+    const double b = tB ? B[j + (size_t)k * ldb] : B[k + (size_t)j * ldb];
+    s = fma(a, b, s);
+  }
+  C[i + (size_t)j * ldc] = (beta == 0.0) ? alpha * s : fma(alpha, s, beta * C[i + (size_t)j * ldc]);
+}
+
+// ---- 3. FP32 cyclic Jacobi (round-robin parallel ordering), one CTA --------------------------------
+__device__ __forceinline__ int rr_idx(int i, int r, int N) { return i == 0 ? 0 : ((i - 1 + r) % (N - 1)) + 1; }
+
+__global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restrict__ Cin, int ldc,
+                                                    double* __restrict__ Wout, double* __restrict__ lam) {
+  extern __shared__ float smf[];
+  float* C = smf;
+  float* W = smf + n * n;
+  __shared__ float s_c[64], s_s[64];
+  __shared__ int s_p[64], s_q[64];
+  __shared__ float s_red[32];
+  __shared__ int s_stop;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e % n, j = e / n;
+    C[e] = (float)(0.5 * (Cin[i + (size_t)j * ldc] + Cin[j + (size_t)i * ldc]));
+    W[e] = (i == j) ? 1.f : 0.f;
+  }
+  __syncthreads();
+  const int N = n + (n & 1), npair = N / 2;
+  for (int sweep = 0; sweep < 20 && n > 1; ++sweep) {
+    float off = 0.f, tot = 0.f;
+    for (int e = tid; e < n * n; e += nt) {
+      const float v = C[e] * C[e];
+      tot += v;
+      if ((e % n) != (e / n)) off += v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_down_sync(0xffffffffu, off, o);
+      tot += __shfl_down_sync(0xffffffffu, tot, o);
+    }
+    if ((tid & 31) == 0) s_red[tid >> 5] = off;
+    __syncthreads();
+    float offs = 0.f;
+    if (tid == 0)
+      for (int w = 0; w < (nt >> 5); ++w) offs += s_red[w];
+    __syncthreads();
+    if ((tid & 31) == 0) s_red[tid >> 5] = tot;
+    __syncthreads();
+    if (tid == 0) {
+      float tots = 0.f;
+      for (int w = 0; w < (nt >> 5); ++w) tots += s_red[w];
+      s_stop = (offs <= 1e-13f * tots) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_stop) break;
+    for (int r = 0; r < N - 1; ++r) {
+      for (int k = tid; k < npair; k += nt) {
+        int p = rr_idx(k, r, N), q = rr_idx(N - 1 - k, r, N);
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        float c = 1.f, s = 0.f;
+        if (q < n) {
+          const float apq = C[p + q * n];
+          if (apq != 0.f) {
+            const float tau = (C[q + q * n] - C[p + p * n]) / (2.f * apq);
+            const float t = (tau >= 0.f) ? 1.f / (tau + sqrtf(1.f + tau * tau)) : -1.f / (-tau + sqrtf(1.f + tau * tau));
+            c = rsqrtf(1.f + t * t);
+            s = t * c;
+          }
+        }
+        s_p[k] = p;
+        s_q[k] = (q < n && s != 0.f) ? q : -1;
+        s_c[k] = c;
+        s_s[k] = s;
+      }
+      __syncthreads();
+      for (int e = tid; e < npair * n; e += nt) {
+        const int k = e / n, j = e % n, q = s_q[k];
+        if (q < 0) continue;
+        const int p = s_p[k];
+        const float c = s_c[k], s = s_s[k];
+        const float ap = C[p + j * n], aq = C[q + j * n];
+        C[p + j * n] = c * ap - s * aq;
+        C[q + j * n] = s * ap + c * aq;
+      }
+      __syncthreads();
+      for (int e = tid; e < npair * n; e += nt) {
+        const int k = e / n, i = e % n, q = s_q[k];
+        if (q < 0) continue;
+        const int p = s_p[k];
+        const float c = s_c[k], s = s_s[k];
+        float ap = C[i + p * n], aq = C[i + q * n];
+        C[i + p * n] = c * ap - s * aq;
+        C[i + q * n] = s * ap + c * aq;
+        ap = W[i + p * n];
+        aq = W[i + q * n];
+        W[i + p * n] = c * ap - s * aq;
+        W[i + q * n] = s * ap + c * aq;
+      }
+      __syncthreads();
+      for (int k = tid; k < npair; k += nt) {
+        const int q = s_q[k];
+        if (q >= 0) {
+          const int p = s_p[k];
+          C[p + q * n] = 0.f;
+          C[q + p * n] = 0.f;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int e = tid; e < n * n; e += nt) Wout[e] = (double)W[e];
+  for (int i = tid; i < n; i += nt) lam[i] = (double)C[i + i * n];
+}
+
+// ---- 4. Ogita-Aishima correction: from P = W'W and T = W'CW build lambda and F = I + E ------------
+__global__ void k_oa_correction(int n, const double* __restrict__ P, const double* __restrict__ T,
+                                double* __restrict__ lam, double* __restrict__ F, double rel_cluster) {
+  extern __shared__ double sl[];
+  __shared__ double s_scale;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sl[i] = T[i + (size_t)i * n] / P[i + (size_t)i * n];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0;
+    for (int i = 0; i < n; ++i) m = fmax(m, fabs(sl[i]));
+    s_scale = (m > 0 ? m : 1.0) * rel_cluster;
+  }
+  __syncthreads();
+  const double delta = s_scale;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e % n, j = e / n;
+    const double r = (i == j ? 1.0 : 0.0) - P[e];
+    double f;
+    if (i == j) {
+      f = 1.0 + 0.5 * r;
+    } else {
+      const double gap = sl[j] - sl[i];
+      f = (fabs(gap) > delta) ? (T[e] + sl[j] * r) / gap : 0.5 * r;
+    }
+    F[e] = f;
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) lam[i] = sl[i];
+}
+
+// ---- 5. sort descending, gather columns --------------------------------------------------------------
+__global__ void k_sort_desc(int n, const double* __restrict__ lam, const double* __restrict__ W, double* __restrict__ lam_out,
+                            double* __restrict__ Wout) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double li = lam[i];
+    int rank = 0;
+    for (int j = 0; j < n; ++j) {
+      const double lj = lam[j];
+      rank += (lj > li || (lj == li && j < i)) ? 1 : 0;
+    }
+    lam_out[rank] = li;
+    for (int r = 0; r < n; ++r) Wout[r + (size_t)rank * n] = W[r + (size_t)i * n];
+  }
+}
+
+// Y(:,j) = C W(:,j) / sigma_j (sigma_j = sqrt(max(lam_j, 0))), then the sigmas themselves
+__global__ void k_svd_left(int n, const double* __restrict__ CW, const double* __restrict__ lam, double* __restrict__ Y,
+                           double* __restrict__ sig) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n * n) {
+    const int j = e / n;
+    const double s = sqrt(fmax(lam[j], 0.0));
+    Y[e] = (s > 0.0) ? CW[e] / s : 0.0;
+    if (e % n == 0) sig[j] = s;
+  }
+}
+
+// ---- host helpers ----------------------------------------------------------------------------------
+static int gemm_small(ofrr_ctx* ctx, int M, int N, int K, double alpha, const double* A, int lda, int tA,
+                      const double* B, int ldb, int tB, double beta, double* C, int ldc) {
+  k_gemm_small_f64<<<(M * N + 63) / 64, 64, 0, ctx->stream>>>(M, N, K, alpha, A, lda, tA, B, ldb, tB, beta, C, ldc);
+  OFRR_LAUNCHED(ctx, "k_gemm_small_f64");
+  return OFRR_SUCCESS;
+}
+
+static int trsm(ofrr_ctx* ctx, int n, int nrhs, const double* L, const double* B, int ldb, int transB, double* X,
+                int upper) {
+  k_trsm_f64<<<(nrhs + 3) / 4, 128, 4 * n * sizeof(double), ctx->stream>>>(n, nrhs, L, n, B, ldb, transB, X, n, upper);
+  OFRR_LAUNCHED(ctx, "k_trsm_f64");
+  return OFRR_SUCCESS;
+}
+
+static int chol(ofrr_ctx* ctx, int n, int count, const double* const* Ms_host, int ldm, double tau,
+                double* const* Ls_host) {
+  int st = OFRR_SUCCESS;
+  const double** Md = ws_get<const double*>(ctx, 4, &st);
+  if (!Md) return st;
+  double** Ld = (double**)(Md + 2);
+  const void* hp[4] = {Ms_host[0], count > 1 ? Ms_host[1] : Ms_host[0], Ls_host[0], count > 1 ? Ls_host[1] : Ls_host[0]};
+  OFRR_CUDA(cudaMemcpyAsync(Md, hp, sizeof(hp), cudaMemcpyHostToDevice, ctx->stream));
+  const size_t smem = (size_t)n * n * sizeof(double);
+  OFRR_CUDA(cudaFuncSetAttribute(k_chol_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_chol_f64<<<count, 256, smem, ctx->stream>>>(n, Md, ldm, tau, Ld, ctx->dev_flags + 1);
+  OFRR_LAUNCHED(ctx, "k_chol_f64");
+  return OFRR_SUCCESS;
+}
+
+// eigen-decomposition of a symmetric C (n x n, FP64): W (orthonormal, columns sorted by descending
+// eigenvalue) and lam (descending)
+static int sym_eig_refined(ofrr_ctx* ctx, int n, const double* C, double* W, double* lam) {
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  double *W0 = ws_get<double>(ctx, (size_t)n * n, &st), *W1 = ws_get<double>(ctx, (size_t)n * n, &st),
+         *P = ws_get<double>(ctx, (size_t)n * n, &st), *CW = ws_get<double>(ctx, (size_t)n * n, &st),
+         *T = ws_get<double>(ctx, (size_t)n * n, &st), *F = ws_get<double>(ctx, (size_t)n * n, &st),
+         *l0 = ws_get<double>(ctx, (size_t)n, &st);
+  if (!W0 || !W1 || !P || !CW || !T || !F || !l0) return st;
+  const size_t smem = (size_t)2 * n * n * sizeof(float);
+  OFRR_CUDA(cudaFuncSetAttribute(k_jacobi_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_jacobi_f32<<<1, 512, smem, ctx->stream>>>(n, C, n, W0, l0);
+  OFRR_LAUNCHED(ctx, "k_jacobi_f32");
+  double* Wc = W0;
+  double* Wn = W1;
+  for (int it = 0; it < 2; ++it) {
+    OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, Wc, n, 0, 0.0, P, n));   // P = W'W
+    OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, C, n, 0, Wc, n, 0, 0.0, CW, n));   // CW
+    OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, CW, n, 0, 0.0, T, n));   // T = W'CW
+    k_oa_correction<<<1, 256, n * sizeof(double), ctx->stream>>>(n, P, T, l0, F, 1e-5);
+    OFRR_LAUNCHED(ctx, "k_oa_correction");
+    OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 0, F, n, 0, 0.0, Wn, n));   // W <- W (I + E)
+    std::swap(Wc, Wn);
+  }
+  // final Rayleigh quotients with the refined vectors
+  OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, Wc, n, 0, 0.0, P, n));
+  OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, C, n, 0, Wc, n, 0, 0.0, CW, n));
+  OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, CW, n, 0, 0.0, T, n));
+  k_oa_correction<<<1, 256, n * sizeof(double), ctx->stream>>>(n, P, T, l0, F, 1e-5);
+  OFRR_LAUNCHED(ctx, "k_oa_correction");
+  k_sort_desc<<<1, 256, 0, ctx->stream>>>(n, l0, Wc, lam, W);
+  OFRR_LAUNCHED(ctx, "k_sort_desc");
+  return OFRR_SUCCESS;
+}
+
+// eig(G, M + tau I) for symmetric G and SPD M: lam descending, U M-orthonormal (ldu = n)
+int geig_fast(ofrr_ctx* ctx, int n, const double* G, const double* M, double tau, double* lam, double* U) {
+  if (n <= 0) return OFRR_SUCCESS;
+  if (n > 128) return OFRR_ERR_BLAS_INVALID_SIZE;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  double *L = ws_get<double>(ctx, (size_t)n * n, &st), *Y = ws_get<double>(ctx, (size_t)n * n, &st),
+         *C = ws_get<double>(ctx, (size_t)n * n, &st), *W = ws_get<double>(ctx, (size_t)n * n, &st);
+  if (!L || !Y || !C || !W) return st;
+  if (M) {
+    const double* Ms[1] = {M};
+    double* Ls[1] = {L};
+    OFRR_TRY(chol(ctx, n, 1, Ms, n, tau, Ls));
+    OFRR_TRY(trsm(ctx, n, n, L, G, n, 0, Y, 0));  // Y = L^-1 G
+    OFRR_TRY(trsm(ctx, n, n, L, Y, n, 1, C, 0));  // C = L^-1 Y'  (= L^-1 G L^-T)
+  } else {
+    OFRR_CUDA(cudaMemcpyAsync(C, G, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  OFRR_TRY(sym_eig_refined(ctx, n, C, W, lam));
+  if (M) {
+    OFRR_TRY(trsm(ctx, n, n, L, W, n, 0, U, 1));  // U = L^-T W
+  } else {
+    OFRR_CUDA(cudaMemcpyAsync(U, W, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  return OFRR_SUCCESS;
+}
+
+// SVD pencil of svd_rr.m: returns sigma (descending) and the coefficient matrices Zf = Lu^-T Y,
+// Wf = Lv^-T X such that U Zf, V Wf are the (unit-norm in the Gram metrics) singular vectors.
+int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const double* VV, double tau, double* sigma,
+              double* Zf, double* Wf) {
+  if (b <= 0) return OFRR_SUCCESS;
+  if (b > 128) return OFRR_ERR_BLAS_INVALID_SIZE;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  double *Lu = ws_get<double>(ctx, (size_t)b * b, &st), *Lv = ws_get<double>(ctx, (size_t)b * b, &st),
+         *T1 = ws_get<double>(ctx, (size_t)b * b, &st), *C = ws_get<double>(ctx, (size_t)b * b, &st),
+         *S = ws_get<double>(ctx, (size_t)b * b, &st), *X = ws_get<double>(ctx, (size_t)b * b, &st),
+         *lam = ws_get<double>(ctx, (size_t)b, &st), *CX = ws_get<double>(ctx, (size_t)b * b, &st),
+         *Y = ws_get<double>(ctx, (size_t)b * b, &st);
+  if (!Lu || !Lv || !T1 || !C || !S || !X || !lam || !CX || !Y) return st;
+  const double* Ms[2] = {UU, VV};
+  double* Ls[2] = {Lu, Lv};
+  OFRR_TRY(chol(ctx, b, 2, Ms, b, tau, Ls));
+  OFRR_TRY(trsm(ctx, b, b, Lu, B, b, 0, T1, 0));   // T1 = Lu^-1 B
+  OFRR_TRY(trsm(ctx, b, b, Lv, T1, b, 1, C, 0));   // C' = Lv^-1 T1'  -> C holds (Lu^-1 B Lv^-T)'
+  // S = C'C with C = (stored)' : S = stored * stored'
+  OFRR_TRY(gemm_small(ctx, b, b, b, 1.0, C, b, 0, C, b, 1, 0.0, S, b));
+  OFRR_TRY(sym_eig_refined(ctx, b, S, X, lam));    // right singular vectors X, sigma^2
+  OFRR_TRY(gemm_small(ctx, b, b, b, 1.0, C, b, 1, X, b, 0, 0.0, CX, b));  // (true C) X
+  k_svd_left<<<(b * b + 255) / 256, 256, 0, ctx->stream>>>(b, CX, lam, Y, sigma);
+  OFRR_LAUNCHED(ctx, "k_svd_left");
+  OFRR_TRY(trsm(ctx, b, b, Lu, Y, b, 0, Zf, 1));  // Zf = Lu^-T Y
+  OFRR_TRY(trsm(ctx, b, b, Lv, X, b, 0, Wf, 1));  // Wf = Lv^-T X
+  return OFRR_SUCCESS;
+}
+
+}  // namespace ofrr

@@ -61,9 +61,29 @@ struct Op {
     if (A->kind == OFRR_OP_CSR) return csrmm_impl(ctx, &A->csr, trans, tx, tc, ty, nrhs, X, ldx, Y, ldy);
     const void* Ad;
     int64_t lda;
-    OFRR_TRY(dense_as(ctx, ta, &Ad, &lda));
     const int64_t M = trans ? n() : m(), K = trans ? m() : n();
+    if (!trans && tc == OFRR_F32 && ta == tx && (ta == OFRR_F16 || ta == OFRR_BF16)) {
+      // A V as (A')' V on the K-contiguous copy of A: the tensor-core TN kernel
+      OFRR_TRY(dense_t_as(ctx, ta, &Ad, &lda));
+      return gemm_impl(ctx, 1, 0, ta, tx, tc, ty, M, nrhs, K, 1.0, Ad, lda, X, ldx, 0.0, Y, ldy);
+    }
+    OFRR_TRY(dense_as(ctx, ta, &Ad, &lda));
     return gemm_impl(ctx, trans, 0, ta, tx, tc, ty, M, nrhs, K, 1.0, Ad, lda, X, ldx, 0.0, Y, ldy);
+  }
+
+  // A' stored column-major (n x m) in type t, made once per solve
+  const void* dense_t[4] = {nullptr, nullptr, nullptr, nullptr};
+  int dense_t_as(ofrr_ctx* ctx, ofrr_dtype t, const void** p, int64_t* l) {
+    if (!dense_t[t]) {
+      int st = OFRR_SUCCESS;
+      void* w = ws_alloc(ctx, (size_t)m() * n() * dtype_size(t), &st);
+      if (!w) return st;
+      OFRR_TRY(cast_transpose_impl(ctx, A->dtype, t, m(), n(), A->data, A->ld, w, n()));
+      dense_t[t] = w;
+    }
+    *p = dense_t[t];
+    *l = n();
+    return OFRR_SUCCESS;
   }
 };
 
@@ -97,12 +117,14 @@ int compact_columns(ofrr_ctx* ctx, ofrr_dtype t, int64_t m, void* Q, int64_t ldq
 
 struct Precisions {
   ofrr_dtype pc, po, phc, pho, prc, pro;
+  bool fast = false;  // production modes: refined FP32/FP64 small solver instead of the FP64 Jacobi
 };
 
 Precisions precisions_of(const ofrr_options* o) {
   Precisions p;
   if (o->mode == OFRR_MODE_FP64) {
     p.pc = p.po = p.phc = p.pho = p.prc = p.pro = OFRR_F64;
+    p.fast = true;
   } else {
     p.pc = o->p_compute;
     p.po = o->p_output;
@@ -151,7 +173,7 @@ int validate_op(const ofrr_operator* A) {
 // ---------------------------------------------------------------------------------------
 int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype tq, int64_t ldq, int b,
                ofrr_dtype pmc, ofrr_dtype pmo, ofrr_dtype pAmc, ofrr_dtype pAmo, bool use_gen, double gtol,
-               bool symmetric, void* Vout, int64_t ldvo, double* d) {
+               bool symmetric, void* Vout, int64_t ldvo, double* d, bool fast = false) {
   WsScope scope(ctx);
   int st = OFRR_SUCCESS;
   const int64_t n = op.m();
@@ -184,12 +206,16 @@ int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype t
     OFRR_TRY(dmalloc(ctx, &M, (size_t)b * b));
     OFRR_TRY(gemm_impl(ctx, 1, 0, tq, tq, pmc, pmo, b, b, n, 1.0, Q, ldq, Q, ldq, 0.0, tmp, b));
     OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, M, b));
-    if (gtol != 0.0) {
+    if (gtol != 0.0 && !(fast && symmetric && b <= 128)) {
       k_add_diag<<<(b + 255) / 256, 256, 0, ctx->stream>>>(b, M, b, gtol);
       OFRR_LAUNCHED(ctx, "k_add_diag");
     }
   }
-  OFRR_TRY(geig_dev(ctx, b, G, b, M, b, symmetric ? 1 : 0, d, U, b));
+  if (fast && symmetric && b <= 128) {
+    OFRR_TRY(geig_fast(ctx, b, G, M, use_gen ? gtol : 0.0, d, U));
+  } else {
+    OFRR_TRY(geig_dev(ctx, b, G, b, M, b, symmetric ? 1 : 0, d, U, b));
+  }
   // V = gemm(V, 'N', U, pmc, pmo) then back to V's precision
   void* Vn = Vout;
   int64_t ldvn = ldvo;
@@ -368,7 +394,7 @@ __global__ void k_build_aug(int b, const double* B, const double* UU, const doub
 
 int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* V, ofrr_dtype tq, int64_t ldu,
                int64_t ldv, int b, ofrr_dtype pmc, ofrr_dtype pmo, ofrr_dtype pAmc, ofrr_dtype pAmo, bool use_gen,
-               double gtol, void* Uout, int64_t lduo, void* Vout, int64_t ldvo, double* s_dev) {
+               double gtol, void* Uout, int64_t lduo, void* Vout, int64_t ldvo, double* s_dev, bool fast = false) {
   WsScope scope(ctx);
   int st = OFRR_SUCCESS;
   const int64_t m = op.m(), n = op.n();
@@ -401,6 +427,29 @@ int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* 
   OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, UU, b));
   OFRR_TRY(gemm_impl(ctx, 1, 0, tq, tq, pmc, pmo, b, b, n, 1.0, V, ldv, V, ldv, 0.0, tmp, b));
   OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, VV, b));
+  if (fast && b <= 128) {
+    // the same pencil through two Cholesky factors: sigma, Zf = Lu^-T Y, Wf = Lv^-T X;
+    // U Zf and V Wf are the unit singular-vector estimates (svd_rr.m's sqrt(2) U Z and sqrt(2) V W)
+    double *Zf, *Wf;
+    OFRR_TRY(dmalloc(ctx, &Zf, (size_t)b * b));
+    OFRR_TRY(dmalloc(ctx, &Wf, (size_t)b * b));
+    OFRR_TRY(gsvd_fast(ctx, b, B, UU, VV, gtol, s_dev, Zf, Wf));
+    void* Uo = Uout;
+    void* Vo = Vout;
+    int64_t lu = lduo, lv = ldvo;
+    if (pmo != tq) {
+      Uo = ws_alloc(ctx, (size_t)m * b * dtype_size(pmo), &st);
+      Vo = ws_alloc(ctx, (size_t)n * b * dtype_size(pmo), &st);
+      if (!Uo || !Vo) return st;
+      lu = m;
+      lv = n;
+    }
+    OFRR_TRY(gemm_impl(ctx, 0, 0, tq, OFRR_F64, pmc, pmo, m, b, b, 1.0, U, ldu, Zf, b, 0.0, Uo, lu));
+    OFRR_TRY(gemm_impl(ctx, 0, 0, tq, OFRR_F64, pmc, pmo, n, b, b, 1.0, V, ldv, Wf, b, 0.0, Vo, lv));
+    if (Uo != Uout) OFRR_TRY(cast_impl(ctx, pmo, tq, m, b, Uo, lu, Uout, lduo));
+    if (Vo != Vout) OFRR_TRY(cast_impl(ctx, pmo, tq, n, b, Vo, lv, Vout, ldvo));
+    return OFRR_SUCCESS;
+  }
   k_build_aug<<<grid_for(4 * b * b, 256), 256, 0, ctx->stream>>>(b, B, UU, VV, Aext, Mext, gtol);
   OFRR_LAUNCHED(ctx, "k_build_aug");
   OFRR_TRY(geig_dev(ctx, 2 * b, Aext, 2 * b, Mext, 2 * b, 1, d, X, 2 * b));
@@ -728,12 +777,12 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
     int64_t lddst = (cur == V) ? ldv : n;
     if (P.pho == P.po) {
       OFRR_TRY(rr_eig_dev(ctx, op, P.po, Q, P.pho, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
-                          opt->generalized_tol, symmetric, dst, lddst, d_dev));
+                          opt->generalized_tol, symmetric, dst, lddst, d_dev, P.fast));
     } else {
       void* tmpv = ws_alloc(ctx, (size_t)n * b * dtype_size(P.pho), &st);
       if (!tmpv) return st;
       OFRR_TRY(rr_eig_dev(ctx, op, P.po, Q, P.pho, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
-                          opt->generalized_tol, symmetric, tmpv, n, d_dev));
+                          opt->generalized_tol, symmetric, tmpv, n, d_dev, P.fast));
       OFRR_TRY(cast_impl(ctx, P.pho, P.po, n, b, tmpv, n, dst, lddst));
     }
     S.nmv += b;
@@ -799,7 +848,7 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
     if (w == 0) return OFRR_ERR_SOLVER_DIVERGENCE;
     S.b = b = w;
     OFRR_TRY(rr_svd_dev(ctx, op, P.po, P1, Q1, P.pho, m, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
-                        opt->generalized_tol, Ut, m, Vt, n, d_dev));
+                        opt->generalized_tol, Ut, m, Vt, n, d_dev, P.fast));
     OFRR_TRY(cast_impl(ctx, P.pho, P.po, m, b, Ut, m, U, ldu));
     OFRR_TRY(cast_impl(ctx, P.pho, P.po, n, b, Vt, n, V, ldv));
     S.nmv += b;
@@ -829,11 +878,13 @@ Precisions mixed_low(const ofrr_options* o) {
   p.pho = p.po;
   p.pc = p.phc = p.prc = OFRR_F32;  // FP32 accumulation
   p.pro = OFRR_F32;                 // Gram matrices kept in FP32 (not rounded to 16 bits), then FP64
+  p.fast = true;
   return p;
 }
 Precisions all_f64() {
   Precisions p;
   p.pc = p.po = p.phc = p.pho = p.prc = p.pro = OFRR_F64;
+  p.fast = true;
   return p;
 }
 

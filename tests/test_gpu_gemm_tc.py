@@ -1,0 +1,72 @@
+"""tcgen05 TN GEMM (16-bit operands, FP32 accumulation): shapes with tails in M, N and K, split-K,
+every output type, against an FP64 product of the same rounded inputs and against cuBLAS."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def api(built_lib):
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from mixedprecisionofrr_gb300 import api as a
+
+    return a
+
+
+SHAPES = [(128, 64, 64), (8192, 64, 2048), (2048, 64, 8192), (64, 64, 8192), (300, 40, 1000), (129, 33, 77),
+          (1000, 128, 256), (4096, 96, 640), (50, 16, 16)]
+
+
+@pytest.mark.parametrize("M,N,K", SHAPES)
+@pytest.mark.parametrize("pin", ["half", "bfloat16"])
+def test_tc_gemm_vs_fp64(api, M, N, K, pin):
+    from mixedprecisionofrr_gb300 import _lib as L
+
+    rng = np.random.default_rng(M * 7 + N * 3 + K)
+    A = rng.standard_normal((K, M))  # stored K x M: the TN operand layout
+    B = rng.standard_normal((K, N))
+    p = api.PREC[pin]
+    Ad = api.to_device_cm(A, p)
+    Bd = api.to_device_cm(B, p)
+    ref = Ad.double().cpu().numpy().T @ Bd.double().cpu().numpy()
+    scale = np.max(np.abs(ref))
+    for po, tol in (("single", 2e-6 * np.sqrt(K)), ("double", 2e-6 * np.sqrt(K)), ("half", 1e-3), (pin, 1e-2)):
+        Cd = api.gemm(Ad, "T", Bd, "single", po)
+        got = Cd.double().cpu().numpy()
+        assert np.max(np.abs(got - ref)) / scale < tol, (po, np.max(np.abs(got - ref)) / scale)
+    launches = api.context().launch_count
+    assert launches > 0
+
+
+def test_tc_matches_cublas(api):
+    """The same product through cuBLAS GemmEx (tensor path disabled) agrees to FP32 rounding."""
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((2048, 512))
+    B = rng.standard_normal((2048, 64))
+    Ad = api.to_device_cm(A, api.PREC["half"])
+    Bd = api.to_device_cm(B, api.PREC["half"])
+    c_tc = api.gemm(Ad, "T", Bd, "single", "single").double().cpu().numpy()
+    os.environ["OFRR_DISABLE_TC"] = "1"
+    try:
+        c_lib = api.gemm(Ad, "T", Bd, "single", "single").double().cpu().numpy()
+    finally:
+        del os.environ["OFRR_DISABLE_TC"]
+    assert np.max(np.abs(c_tc - c_lib)) / np.max(np.abs(c_lib)) < 1e-5
+
+
+def test_tc_exact_small_integers(api):
+    """Integer-valued operands with |a|,|b| <= 63 and K = 2048: every partial sum is exact in FP32,
+    so the tensor-core result must equal the exact integer product bit for bit."""
+    rng = np.random.default_rng(9)
+    A = rng.integers(-63, 64, (2048, 256)).astype(np.float64)
+    B = rng.integers(-63, 64, (2048, 64)).astype(np.float64)
+    Ad = api.to_device_cm(A, api.PREC["bfloat16"])
+    Bd = api.to_device_cm(B, api.PREC["bfloat16"])
+    got = api.gemm(Ad, "T", Bd, "single", "double").cpu().numpy()
+    assert np.array_equal(got, A.T @ B)
