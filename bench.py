@@ -217,13 +217,14 @@ def gemm_roofline(api, steps=50):
     from mixedprecisionofrr_gb300 import _lib as L
 
     ctx = api.context()
-    A = api.randn(7, M_ROWS, N_COLS, "half")
+    # the solver keeps A' (K-contiguous rows of A) and runs A V as the TN product (A')' V
+    At = api.randn(7, N_COLS, M_ROWS, "half")
     X = api.randn(8, N_COLS, BLOCK, "half")
     Y = api.empty_cm(M_ROWS, BLOCK, L.F16)
     lib = ctx.lib
 
     def call():
-        st = lib.ofrr_gemm(ctx.h, 0, 0, L.F16, L.F16, L.F32, L.F16, M_ROWS, BLOCK, N_COLS, 1.0, A.data_ptr(), M_ROWS,
+        st = lib.ofrr_gemm(ctx.h, 1, 0, L.F16, L.F16, L.F32, L.F16, M_ROWS, BLOCK, N_COLS, 1.0, At.data_ptr(), N_COLS,
                            X.data_ptr(), N_COLS, 0.0, Y.data_ptr(), M_ROWS)
         assert st == 0
 

@@ -123,6 +123,14 @@ int ofrr_gemm(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
               double alpha, const void* A /*dev*/, int64_t lda, const void* B /*dev*/,
               int64_t ldb, double beta, void* C /*dev*/, int64_t ldc);
 
+/* C (M x N) = A' B for FP64 A (K x M) and B (K x N), computed on the tcgen05 tensor cores from
+ * exact BF16 digit slices of both operands (five 7-bit digits per column after a power-of-two
+ * column scaling; digit products summed exactly in FP32, combined in FP64).  Element error is
+ * about 2^-35 |A'| |B|.  The FP64 TN case of msvd::gemm (mvops.hpp:79-90) at tensor-core speed;
+ * the mixed solver's refinement phase uses it for A V, A' U and the Gram products. */
+int ofrr_gemm_f64_emulated(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda,
+                           const double* B, int64_t ldb, double* C, int64_t ldc);
+
 /* ---- sparse operator: CSR with value copies per precision ------------------------- *
  * Mirrors MATLAB/+src/+csr/sparse2csr.m:21-50 (0-based int32 here).  Any of the value
  * arrays may be NULL if that precision is never requested. */

@@ -85,6 +85,7 @@ SIGNATURES = {
                                   _DP, _IP, _IP]),
     "ofrr_gemm": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _I64, _I64, _I64, _D,
                             _P, _I64, _P, _I64, _D, _P, _I64]),
+    "ofrr_gemm_f64_emulated": (C.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64]),
     "ofrr_csrmm": (C.c_int, [_P, C.POINTER(ofrr_csr), C.c_int, C.c_int, C.c_int, C.c_int, _I64, _P, _I64, _P,
                              _I64]),
     "ofrr_syev": (C.c_int, [_P, C.c_int, _P, C.c_int, _P]),

@@ -286,6 +286,19 @@ def gemm(A, trans: str, B, precision_compute="double", precision_output=None, al
     return Cd
 
 
+def gemm_f64_emulated(A, B):
+    """C = A' B for FP64 A (K x M), B (K x N) on the tensor cores through exact BF16 digit slices."""
+    ctx = context()
+    Ad = A if is_cm(A) else to_device_cm(A, L.F64)
+    Bd = B if is_cm(B) else to_device_cm(B, L.F64)
+    K, M = Ad.shape
+    N = Bd.shape[1]
+    Cd = empty_cm(M, N, L.F64)
+    L.check(ctx.lib.ofrr_gemm_f64_emulated(ctx.h, M, N, K, Ad.data_ptr(), ld_of(Ad), Bd.data_ptr(), ld_of(Bd),
+                                           Cd.data_ptr(), ld_of(Cd)), "gemm_f64_emulated")
+    return Cd
+
+
 def csrmv(Acsr: CsrMatrix, trans: str, x, precision_compute="double", precision_output=None):
     """MATLAB/+src/+csr/csrmv.m."""
     ctx = context()

@@ -42,12 +42,19 @@ int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
     }
     if (beta == 1.0) return OFRR_SUCCESS;
   }
+  // FP64 TN products in the refinement phase of the mixed solver: exact BF16 slices on the tensor cores
+  if (ctx->emulate_f64 && tc == OFRR_F64 && ta == OFRR_F64 && tb == OFRR_F64 && tout == OFRR_F64 && transA == 1 &&
+      transB == 0 && alpha == 1.0 && beta == 0.0 && K >= 64) {
+    SlicedOperand As;
+    OFRR_TRY(sliced_prepare(ctx, K, M, (const double*)A, lda, &As));
+    return sliced_gemm_tn(ctx, As, N, (const double*)B, ldb, (double*)C, ldc);
+  }
   // 16-bit tensor-core path
   if (tc == OFRR_F32 && ta == tb && (ta == OFRR_F16 || ta == OFRR_BF16) && alpha == 1.0 && beta == 0.0) {
     bool handled = false;
     OFRR_TRY(gemm_tc_try(ctx, transA, transB, ta, M, N, K, A, lda, B, ldb, tout, C, ldc, &handled));
     if (handled) return OFRR_SUCCESS;
-    cublasComputeType_t ct = CUBLAS_COMPUTE_32F_PEDANTIC;
+    cublasComputeType_t ct = CUBLAS_COMPUTE_32F;  // FP32 accumulation (the pedantic variant rejects bf16)
     void* Cout = C;
     int64_t ldco = ldc;
     ofrr_dtype tco = tout;

@@ -14,6 +14,7 @@
 // drains and returns, so a fault in the pipeline cannot hang the GPU.
 #include <cuda.h>
 
+#include <algorithm>
 #include <cstdlib>
 
 #include "ofrr_internal.cuh"
@@ -332,6 +333,46 @@ static int launch(ofrr_ctx* ctx, const CUtensorMap& ma, const CUtensorMap& mb, i
 }
 
 }  // namespace tc
+
+// FP32 partial products of a 16-bit TN GEMM: partial[z] (M x N, ld M) holds the sum over the z-th
+// contiguous range of kblocks_per_split * 64 entries of K.  Used by the exact-slice FP64 emulation,
+// which chooses the ranges so that every partial sum is exact.  Requires TMA-compatible layouts.
+int tc_gemm_partials(ofrr_ctx* ctx, ofrr_dtype t16, int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
+                     const void* B, int64_t ldb, int kblocks_per_split, float* partial, int* splits_out) {
+  if (K < 16 || M < 1 || N < 1) return OFRR_ERR_BLAS_INVALID_SIZE;
+  if (((uintptr_t)A & 15) || ((uintptr_t)B & 15) || ((lda * 2) & 15) || ((ldb * 2) & 15))
+    return OFRR_ERR_BLAS_INVALID_SIZE;
+  const int BN = (N <= 32) ? 32 : (N <= 64 ? 64 : 128);
+  CUtensorMap ma, mb;
+  if (!tc::make_map(&ma, t16, A, K, M, lda, tc::BM) || !tc::make_map(&mb, t16, B, K, N, ldb, BN))
+    return OFRR_ERR_INTERNAL;
+  const int kbt = (int)((K + tc::BK - 1) / tc::BK);
+  const int kbps = std::max(1, std::min(kblocks_per_split, kbt));
+  const int splits = (kbt + kbps - 1) / kbps;
+  const int gm = (int)((M + tc::BM - 1) / tc::BM), gn = (int)((N + BN - 1) / BN);
+  dim3 grid(gm, gn, splits);
+  const uint32_t idesc = tc::make_idesc(t16, BN);
+  float* none = nullptr;
+  if (BN == 32) {
+    const size_t smem = tc::Smem<32>::TOTAL;
+    OFRR_CUDA(cudaFuncSetAttribute(tc::k_gemm_tn<32, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    tc::k_gemm_tn<32, float><<<grid, tc::THREADS, smem, ctx->stream>>>(ma, mb, (int)M, (int)N, kbt, kbps, idesc, none,
+                                                                       M, partial, ctx->dev_flags + 2);
+  } else if (BN == 64) {
+    const size_t smem = tc::Smem<64>::TOTAL;
+    OFRR_CUDA(cudaFuncSetAttribute(tc::k_gemm_tn<64, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    tc::k_gemm_tn<64, float><<<grid, tc::THREADS, smem, ctx->stream>>>(ma, mb, (int)M, (int)N, kbt, kbps, idesc, none,
+                                                                       M, partial, ctx->dev_flags + 2);
+  } else {
+    const size_t smem = tc::Smem<128>::TOTAL;
+    OFRR_CUDA(cudaFuncSetAttribute(tc::k_gemm_tn<128, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    tc::k_gemm_tn<128, float><<<grid, tc::THREADS, smem, ctx->stream>>>(ma, mb, (int)M, (int)N, kbt, kbps, idesc,
+                                                                        none, M, partial, ctx->dev_flags + 2);
+  }
+  OFRR_LAUNCHED(ctx, "k_gemm_tn");
+  *splits_out = splits;
+  return OFRR_SUCCESS;
+}
 
 // Route a 16-bit TN product to the tcgen05 kernel when its layout allows TMA (16-byte aligned
 // base and leading dimensions); *handled = false leaves the call to the caller's fallback.

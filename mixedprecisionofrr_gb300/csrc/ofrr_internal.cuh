@@ -72,6 +72,7 @@ struct ofrr_ctx {
   int* dev_flags = nullptr;        // device status words written by kernels (bounded waits etc.)
   unsigned int* dev_counters = nullptr;  // grid "last block" counters (self-resetting)
   void* pinned = nullptr;          // small pinned host staging buffer
+  bool emulate_f64 = false;        // FP64 TN products through exact BF16 slices on the tensor cores
   size_t pinned_size = 0;
 };
 
@@ -260,6 +261,20 @@ int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const dou
 // reductions
 int column_norms(ofrr_ctx* ctx, ofrr_dtype t, int64_t m, int64_t n, const void* X, int64_t ldx,
                  double* out_dev);
+// exact-slice FP64 emulation (sliced.cu): digit stacks of a fixed K x M FP64 operand and the
+// product C (M x N) = X' B with X the prepared operand and B (K x N) FP64
+struct SlicedOperand {
+  int64_t K = 0, Kp = 0, M = 0;
+  __nv_bfloat16* stack = nullptr;
+  int* expo = nullptr;
+};
+constexpr int kSliceDigits = 5;
+int sliced_prepare(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, int64_t ldx, SlicedOperand* out);
+int sliced_prepare_into(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, int64_t ldx, __nv_bfloat16* stack,
+                        int* expo, SlicedOperand* out);
+int sliced_gemm_tn(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const double* B, int64_t ldb, double* C,
+                   int64_t ldc);
+
 int residual_columns(ofrr_ctx* ctx, int64_t m, int64_t n, const double* AX, int64_t ldax,
                      const double* X, int64_t ldx, const double* lam_dev, double* out_dev);
 

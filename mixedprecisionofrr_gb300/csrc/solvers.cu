@@ -62,6 +62,11 @@ struct Op {
     const void* Ad;
     int64_t lda;
     const int64_t M = trans ? n() : m(), K = trans ? m() : n();
+    if (ctx->emulate_f64 && ta == OFRR_F64 && tx == OFRR_F64 && tc == OFRR_F64 && ty == OFRR_F64 &&
+        (trans ? have_sA : have_sAt)) {
+      // FP64-accurate A V / A' U from the cached digit stacks of A (exact BF16 slices, tcgen05)
+      return sliced_gemm_tn(ctx, trans ? sA : sAt, nrhs, (const double*)X, ldx, (double*)Y, ldy);
+    }
     if (!trans && tc == OFRR_F32 && ta == tx && (ta == OFRR_F16 || ta == OFRR_BF16)) {
       // A V as (A')' V on the K-contiguous copy of A: the tensor-core TN kernel
       OFRR_TRY(dense_t_as(ctx, ta, &Ad, &lda));
@@ -69,6 +74,40 @@ struct Op {
     }
     OFRR_TRY(dense_as(ctx, ta, &Ad, &lda));
     return gemm_impl(ctx, trans, 0, ta, tx, tc, ty, M, nrhs, K, 1.0, Ad, lda, X, ldx, 0.0, Y, ldy);
+  }
+
+  // digit stacks of A for the FP64 emulation: sAt for A V (operand A', K = n), sA for A' U (K = m).
+  // Must be called in the solve's outermost workspace scope (the stacks live as long as the solve).
+  SlicedOperand sA, sAt;
+  bool have_sA = false, have_sAt = false;
+  int prepare_sliced(ofrr_ctx* ctx) {
+    if (A->kind != OFRR_OP_DENSE) return OFRR_SUCCESS;
+    const double* A64;
+    int64_t lda64;
+    {
+      const void* p;
+      OFRR_TRY(dense_as(ctx, OFRR_F64, &p, &lda64));
+      A64 = (const double*)p;
+    }
+    OFRR_TRY(sliced_prepare(ctx, m(), n(), A64, lda64, &sA));
+    have_sA = true;
+    // A' (n x m) in FP64 is only needed while slicing: allocated after the stacks, released at once
+    sAt.K = n();
+    sAt.Kp = (n() + 63) / 64 * 64;
+    sAt.M = m();
+    int st = OFRR_SUCCESS;
+    sAt.stack = ws_get<__nv_bfloat16>(ctx, (size_t)m() * kSliceDigits * sAt.Kp, &st);
+    if (!sAt.stack) return st;
+    sAt.expo = ws_get<int>(ctx, (size_t)m(), &st);
+    if (!sAt.expo) return st;
+    WsScope tmp(ctx);
+    double* At = ws_get<double>(ctx, (size_t)m() * n(), &st);
+    if (!At) return st;
+    OFRR_TRY(cast_transpose_impl(ctx, A->dtype, OFRR_F64, m(), n(), A->data, A->ld, At, n()));
+    SlicedOperand t;
+    OFRR_TRY(sliced_prepare_into(ctx, n(), m(), At, n(), sAt.stack, sAt.expo, &t));
+    have_sAt = true;
+    return OFRR_SUCCESS;
   }
 
   // A' stored column-major (n x m) in type t, made once per solve
@@ -940,11 +979,32 @@ extern "C" int ofrr_si_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
     else OFRR_TRY(ofrr_randn(ctx, opt->seed, n, b0, L.po, V16, n));
     OFRR_TRY(scalecols_impl(ctx, L.po, L.pc, n, b0, V16, n, nullptr));
     const double stag = (L.po == OFRR_BF16) ? 1e-4 : 1e-5;
+    if (op.A->kind == OFRR_OP_DENSE) {  // operator copies live for the whole solve
+      const void* p;
+      int64_t l;
+      OFRR_TRY(op.dense_as(ctx, L.po, &p, &l));
+      OFRR_TRY(op.dense_t_as(ctx, L.po, &p, &l));
+    }
     OFRR_TRY(eig_phase(ctx, op, L, opt, V16, n, opt->maxiter, opt->tol, nev, stag, S, d));
     OFRR_TRY(cast_impl(ctx, L.po, OFRR_F64, n, S.b, V16, n, V, ldv));
     escalations = 1;
-    if (!S.done && S.it < opt->maxiter)
-      OFRR_TRY(eig_phase(ctx, op, all_f64(), opt, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d));
+    if (!S.done && S.it < opt->maxiter) {
+      // refinement: FP64-accurate products from exact BF16 slices on the tensor cores
+      OFRR_TRY(op.prepare_sliced(ctx));
+      ctx->emulate_f64 = op.A->kind == OFRR_OP_DENSE;
+      st = eig_phase(ctx, op, all_f64(), opt, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d);
+      ctx->emulate_f64 = false;
+      OFRR_TRY(st);
+      if (S.done) {  // confirm with true FP64 residuals
+        OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d, sizeof(double) * S.b, cudaMemcpyDeviceToHost, ctx->stream));
+        OFRR_TRY(sync_and_check(ctx));
+        const int kk = std::min(nev, S.b);
+        OFRR_TRY(residuals_dev(ctx, op, OFRR_F64, V, ldv, kk, S.d.data(), -1.0, S.res.data()));
+        S.converged = 0;
+        for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
+        S.done = S.converged >= kk;
+      }
+    }
   } else {
     const Precisions P = precisions_of(opt);
     if (!opt->use_start_block) OFRR_TRY(ofrr_randn(ctx, opt->seed, n, b0, P.po, V, ldv));
@@ -998,12 +1058,33 @@ extern "C" int ofrr_si_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
     else OFRR_TRY(ofrr_randn(ctx, opt->seed, n, b0, L.po, V16, n));
     OFRR_TRY(scalecols_impl(ctx, L.po, L.pc, n, b0, V16, n, nullptr));
     const double stag = (L.po == OFRR_BF16) ? 1e-4 : 1e-5;
+    if (op.A->kind == OFRR_OP_DENSE) {  // operator copies live for the whole solve
+      const void* p;
+      int64_t l;
+      OFRR_TRY(op.dense_as(ctx, L.po, &p, &l));
+      OFRR_TRY(op.dense_t_as(ctx, L.po, &p, &l));
+    }
     OFRR_TRY(svd_phase(ctx, op, L, opt, U16, m, V16, n, opt->maxiter, opt->tol, nev, stag, S, d));
     OFRR_TRY(cast_impl(ctx, L.po, OFRR_F64, m, S.b, U16, m, U, ldu));
     OFRR_TRY(cast_impl(ctx, L.po, OFRR_F64, n, S.b, V16, n, V, ldv));
     escalations = 1;
-    if (!S.done && S.it < opt->maxiter)
-      OFRR_TRY(svd_phase(ctx, op, all_f64(), opt, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d));
+    if (!S.done && S.it < opt->maxiter) {
+      // refinement: FP64-accurate products from exact BF16 slices on the tensor cores
+      OFRR_TRY(op.prepare_sliced(ctx));
+      ctx->emulate_f64 = op.A->kind == OFRR_OP_DENSE;
+      st = svd_phase(ctx, op, all_f64(), opt, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d);
+      ctx->emulate_f64 = false;
+      OFRR_TRY(st);
+      if (S.done) {  // confirm with true FP64 residuals
+        OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d, sizeof(double) * S.b, cudaMemcpyDeviceToHost, ctx->stream));
+        OFRR_TRY(sync_and_check(ctx));
+        const int kk = std::min(nev, S.b);
+        OFRR_TRY(svd_residuals_dev(ctx, op, OFRR_F64, U, ldu, V, ldv, kk, S.d.data(), -1.0, S.res.data()));
+        S.converged = 0;
+        for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
+        S.done = S.converged >= kk;
+      }
+    }
   } else {
     const Precisions P = precisions_of(opt);
     if (!opt->use_start_block) OFRR_TRY(ofrr_randn(ctx, opt->seed, n, b0, P.po, V, ldv));
