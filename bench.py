@@ -40,6 +40,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="run one warm-up and one mixed solve only (for a profiler's launch list)")
     return ap.parse_args()
 
 
@@ -286,6 +288,14 @@ def main():
     from mixedprecisionofrr_gb300 import api
 
     A, s_true = make_problem_gpu()
+    if args.profile_solve:
+        run_solver(api, A, "mixed")
+        torch.cuda.synchronize()
+        U, s, V, info = run_solver(api, A, "mixed")
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_solve": True, "status": info.status, "iterations": info.iterations,
+                          "max_residual": info.max_residual}))
+        return
     flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     # mixed path (the product) -----------------------------------------------------------------
     if world > 1:

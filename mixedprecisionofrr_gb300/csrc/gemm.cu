@@ -65,12 +65,17 @@ int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
       tco = OFRR_F32;
     }
     const float fa = 1.0f, fb = 0.0f;
-    OFRR_CUBLAS(cublasGemmEx(ctx->cublas, transA ? CUBLAS_OP_T : CUBLAS_OP_N, transB ? CUBLAS_OP_T : CUBLAS_OP_N,
-                             (int)M, (int)N, (int)K, &fa, A, cuda_type(ta), (int)lda, B, cuda_type(tb), (int)ldb, &fb,
-                             Cout, cuda_type(tco), (int)ldco, ct, CUBLAS_GEMM_DEFAULT));
-    ctx->library_calls++;
-    if (Cout != C) OFRR_TRY(cast_impl(ctx, OFRR_F32, tout, M, N, Cout, ldco, C, ldc));
-    return OFRR_SUCCESS;
+    const cublasStatus_t cs =
+        cublasGemmEx(ctx->cublas, transA ? CUBLAS_OP_T : CUBLAS_OP_N, transB ? CUBLAS_OP_T : CUBLAS_OP_N, (int)M,
+                     (int)N, (int)K, &fa, A, cuda_type(ta), (int)lda, B, cuda_type(tb), (int)ldb, &fb, Cout,
+                     cuda_type(tco), (int)ldco, ct, CUBLAS_GEMM_DEFAULT);
+    if (cs == CUBLAS_STATUS_SUCCESS) {
+      ctx->library_calls++;
+      if (Cout != C) OFRR_TRY(cast_impl(ctx, OFRR_F32, tout, M, N, Cout, ldco, C, ldc));
+      return OFRR_SUCCESS;
+    }
+    if (cs != CUBLAS_STATUS_NOT_SUPPORTED) OFRR_CUBLAS(cs);
+    // unsupported layout for the 16-bit library kernels: widen to FP32 below (same values)
   }
   // widen operands to the compute type
   const void* Ac_ptr = A;
