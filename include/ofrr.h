@@ -268,6 +268,26 @@ int ofrr_residual_norms(ofrr_ctx* ctx, const ofrr_operator* A, ofrr_dtype tx, in
                         const void* X /*dev*/, int64_t ldx, const double* evals /*host*/,
                         double normA, double* resid /*host*/);
 
+/* ---- Hessenberg basis without allocation ----------------------------------------------- *
+ * No counterpart in the reference.  For callers that cannot allocate GPU memory (their pool owns
+ * all of HBM, or they must not pay cudaMalloc's implicit device synchronisation): the same
+ * arithmetic and results as ofrr_hessenberg, with no context, no workspace and no allocation.
+ * Its scratch (pivot rows and values, argmax partials, a ticket counter) is one fixed 1 MiB
+ * __device__ array that every GPU loading the library keeps until process exit, so the basis
+ * width is limited: n * n * sizeof(tout) + n * sizeof(tout) + about 5 KB must fit in 1 MiB
+ * (n <= 360 for FP64 output, <= 510 for FP32, <= 721 for 16-bit, and never above 1024); larger
+ * n returns OFRR_ERR_BLAS_INVALID_SIZE with a message on stderr.  All calls share the array:
+ * calls whose work overlaps on the GPU (different streams, or several threads) race and must be
+ * serialised by the caller.  The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) and should come before any stream capture.
+ * Outputs are device arrays: R (n x n, FP64, column-major), select (n ints, 1 = kept) and
+ * perm (n ints, pivot rows, -1 for dropped columns).  ofrr_hessenberg_noalloc_scratch_bytes()
+ * returns the scratch size. */
+int ofrr_hessenberg_noalloc(void* cuda_stream, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tcompute, int64_t m,
+                            int64_t n, const void* A /*dev*/, int64_t lda, void* Q /*dev*/, int64_t ldq,
+                            double select_tol, double* R /*dev*/, int* select /*dev*/, int* perm /*dev*/);
+size_t ofrr_hessenberg_noalloc_scratch_bytes(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -103,6 +103,9 @@ SIGNATURES = {
     "ofrr_arnoldi_eig": (C.c_int, [_P, C.POINTER(ofrr_operator), C.POINTER(ofrr_options), _P, _P, _I64, _DP,
                                    _DP, C.POINTER(ofrr_info)]),
     "ofrr_residual_norms": (C.c_int, [_P, C.POINTER(ofrr_operator), C.c_int, _I64, _P, _I64, _DP, _D, _DP]),
+    "ofrr_hessenberg_noalloc": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _I64, _I64, _P, _I64, _P, _I64, _D, _P,
+                                          _P, _P]),
+    "ofrr_hessenberg_noalloc_scratch_bytes": (C.c_size_t, []),
 }
 
 _lib = None

@@ -17,6 +17,8 @@
 // happens inside the loop, so the whole build can be captured in a CUDA graph.
 #include "ofrr_internal.cuh"
 
+#include <mutex>
+
 namespace ofrr {
 
 template <class TO, class TC>
@@ -269,5 +271,111 @@ extern "C" int ofrr_hessenberg(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, o
     if (skip_host) skip_host[j] = hsel[j] ? 0 : 1;
     if (perm_host) perm_host[j] = hperm[j];
   }
+  return OFRR_SUCCESS;
+}
+
+// ======================================================================================
+// Hessenberg basis without any allocation
+// ======================================================================================
+// Some callers of this library cannot allocate GPU memory: an application whose memory pool has
+// already reserved all of HBM (a cudaMalloc would fail), or a latency-bound request handler that
+// must not pay the implicit device-wide synchronisation of cudaMalloc/cudaFree on other streams.
+// ofrr_hessenberg needs a context (its creation allocates) and a cached workspace; this entry point
+// needs neither.  Its scratch -- the pivot rows and pivot values of the process, the per-CTA argmax
+// partials and the last-CTA ticket counter -- lives in one file-scope __device__ array of
+// kNoAllocScratchBytes (1 MiB), which every GPU that loads the library holds until the process exits.
+// The caller passes the input, the outputs and a stream.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(1) << 20;
+constexpr int kNoAllocGrid = 304;  // 2 CTAs per SM: the argmax partials need this many slots
+__device__ __align__(256) unsigned char g_hess_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[128] = {nullptr};
+
+// device address of the scratch array on the current device (set up once per device)
+int noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return map_cuda_error(e);
+  if (dev < 0 || dev >= 128) return OFRR_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_hess_noalloc_scratch);
+    if (e != cudaSuccess) {
+      note_cuda_error(e, "cudaGetSymbolAddress(g_hess_noalloc_scratch)", __FILE__, __LINE__);
+      return map_cuda_error(e);
+    }
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = (unsigned char*)g_noalloc_ptr[dev];
+  return OFRR_SUCCESS;
+}
+
+size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// bytes of scratch for an n-column basis of element size es
+size_t noalloc_bytes(int64_t n, size_t es) {
+  return align256(sizeof(unsigned int)) + align256(sizeof(ArgMax) * kNoAllocGrid) + align256((size_t)n * es) +
+         align256((size_t)n * n * es);
+}
+
+template <class TO, class TC>
+int hess_run_noalloc(ofrr_ctx* sctx, unsigned char* scratch, int64_t m, int n, TO* Q, int64_t ldq, double select_tol,
+                     double* R, int* select, int* perm) {
+  unsigned int* counter = (unsigned int*)scratch;
+  ArgMax* partial = (ArgMax*)(scratch + align256(sizeof(unsigned int)));
+  TO* pvals = (TO*)((unsigned char*)partial + align256(sizeof(ArgMax) * kNoAllocGrid));
+  TO* pivrows = (TO*)((unsigned char*)pvals + align256((size_t)n * sizeof(TO)));
+  const int block = 256;
+  const int grid = grid_for(m, block, kNoAllocGrid);
+  // everything that must start at zero: the ticket counter, R and the pivot rows
+  OFRR_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), sctx->stream));
+  OFRR_TRY(fill_zero(sctx, R, sizeof(double) * (size_t)n * n));
+  OFRR_TRY(fill_zero(sctx, pivrows, sizeof(TO) * (size_t)n * n));
+  const size_t smem = (size_t)n * (sizeof(TC) + sizeof(TO)) + 16 + (size_t)n * sizeof(int);
+  if (smem > 48 * 1024) return OFRR_ERR_BLAS_INVALID_SIZE;
+  for (int i = 0; i < n; ++i) {
+    k_hess_col<TO, TC><<<grid, block, smem, sctx->stream>>>(m, n, i, Q, ldq, select, perm, pivrows, pvals, R, partial,
+                                                             counter, select_tol, 1, nullptr);
+    OFRR_LAUNCHED(sctx, "k_hess_col");
+  }
+  k_hess_scale<TO, TC><<<grid, block, 0, sctx->stream>>>(m, n - 1, Q, ldq, select, pvals, nullptr);
+  OFRR_LAUNCHED(sctx, "k_hess_scale");
+  return OFRR_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" size_t ofrr_hessenberg_noalloc_scratch_bytes(void) { return kNoAllocScratchBytes; }
+
+extern "C" int ofrr_hessenberg_noalloc(void* stream, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tcompute, int64_t m,
+                                       int64_t n, const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol,
+                                       double* R, int* select, int* perm) {
+  if (m < 0 || n < 0 || !dtype_valid(tin) || !dtype_valid(tout)) return OFRR_ERR_INVALID_ARGUMENT;
+  if (tcompute != OFRR_F64 && tcompute != OFRR_F32) return OFRR_ERR_BLAS_UNSUPPORTED_TYPE;
+  if (m < n) return OFRR_ERR_BLAS_INVALID_SIZE;
+  if (n == 0) return OFRR_SUCCESS;
+  if (!A || !Q || !R || !select || !perm || lda < m || ldq < m) return OFRR_ERR_INVALID_ARGUMENT;
+  const size_t es = dtype_size(tout);
+  if (n > 1024 || noalloc_bytes(n, es) > kNoAllocScratchBytes) {
+    fprintf(stderr,
+            "[ofrr] ofrr_hessenberg_noalloc: %lld columns of %zu-byte elements need %zu bytes of scratch, "
+            "more than the fixed %zu-byte array\n",
+            (long long)n, es, noalloc_bytes(n, es), kNoAllocScratchBytes);
+    return OFRR_ERR_BLAS_INVALID_SIZE;
+  }
+  unsigned char* scratch = nullptr;
+  OFRR_TRY(noalloc_scratch(&scratch));
+  // a stack context that only carries the stream (no handle, no workspace, no allocation)
+  ofrr_ctx sctx;
+  sctx.stream = (cudaStream_t)stream;
+  if (select_tol < 0) select_tol = dtype_eps(tout);
+  if (A != Q || tin != tout || lda != ldq) OFRR_TRY(cast_impl(&sctx, tin, tout, m, n, A, lda, Q, ldq));
+  OFRR_DISPATCH_STORAGE(tout, TO, OFRR_DISPATCH_COMPUTE(tcompute, TC, {
+    OFRR_TRY((hess_run_noalloc<TO, TC>(&sctx, scratch, m, (int)n, (TO*)Q, ldq, select_tol, R, select, perm)));
+  }));
   return OFRR_SUCCESS;
 }
