@@ -43,10 +43,18 @@ int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
     if (beta == 1.0) return OFRR_SUCCESS;
   }
   // FP64 TN products in the refinement phase of the mixed solver: exact BF16 slices on the tensor cores
-  if (ctx->emulate_f64 && tc == OFRR_F64 && ta == OFRR_F64 && tb == OFRR_F64 && tout == OFRR_F64 && transA == 1 &&
-      transB == 0 && alpha == 1.0 && beta == 0.0 && K >= 64) {
+  if (ctx->emulate_f64 && tc == OFRR_F64 && ta == OFRR_F64 && tb == OFRR_F64 && tout == OFRR_F64 && transB == 0 &&
+      alpha == 1.0 && beta == 0.0 && K >= 16 && (transA == 1 || (M >= 1024 && K <= 1024))) {
     SlicedOperand As;
-    OFRR_TRY(sliced_prepare(ctx, K, M, (const double*)A, lda, &As));
+    if (transA == 1) {
+      OFRR_TRY(sliced_prepare(ctx, K, M, (const double*)A, lda, &As));
+    } else {
+      // tall-skinny A (M x K, e.g. the Ritz update basis x coefficients): slice the transposed copy
+      double* At = ws_get<double>(ctx, (size_t)M * K, &st);
+      if (!At) return st;
+      OFRR_TRY(cast_transpose_impl(ctx, OFRR_F64, OFRR_F64, M, K, A, lda, At, K));
+      OFRR_TRY(sliced_prepare(ctx, K, M, At, K, &As));
+    }
     return sliced_gemm_tn(ctx, As, N, (const double*)B, ldb, (double*)C, ldc);
   }
   // 16-bit tensor-core path

@@ -27,7 +27,7 @@ __global__ void __launch_bounds__(256) k_hess_col(int64_t m, int n, int i, TO* _
                                                    TO* __restrict__ pivrows, TO* __restrict__ pvals,
                                                    double* __restrict__ R, ArgMax* __restrict__ partial,
                                                    unsigned int* __restrict__ counter, double select_tol,
-                                                   int scale_prev, int* __restrict__ stop) {
+                                                   int scale_prev, int* __restrict__ stop, int stage_L) {
   extern __shared__ unsigned char smem_raw[];
   TC* s_r = reinterpret_cast<TC*>(smem_raw);                       // n entries
   TO* s_x = reinterpret_cast<TO*>(s_r + n);                        // n entries
@@ -45,6 +45,15 @@ __global__ void __launch_bounds__(256) k_hess_col(int64_t m, int n, int i, TO* _
     s_x[j] = sj ? Q[(int64_t)perm[j] + (int64_t)i * ldq] : TO(0);
   }
   if (tid == 0) s_pprev = (i > 0) ? to_c<TC, TO>(pvals[i - 1]) : TC(0);
+  // stage the strictly lower i x i block of pivot rows in shared memory when it fits, so that the
+  // sequential substitution below never waits on global memory
+  TO* s_L = stage_L ? reinterpret_cast<TO*>(((uintptr_t)(s_sel + n) + 15) & ~(uintptr_t)15) : nullptr;
+  if (stage_L) {
+    for (int e = tid; e < i * i; e += blockDim.x) {
+      const int jj = e / i, l = e % i;
+      if (l < jj) s_L[e] = pivrows[(int64_t)jj * n + l];
+    }
+  }
   __syncthreads();
 
   // forward substitution over the pivot rows (warp 0): r_j = value at perm_j after j eliminations
@@ -58,7 +67,7 @@ __global__ void __launch_bounds__(256) k_hess_col(int64_t m, int n, int i, TO* _
       const TC rc = to_c<TC, TO>(s_x[j]);
       for (int jj = j + 1 + tid; jj < i; jj += 32) {
         if (s_sel[jj]) {
-          const TC l = to_c<TC, TO>(pivrows[(int64_t)jj * n + j]);
+          const TC l = to_c<TC, TO>(stage_L ? s_L[jj * i + j] : pivrows[(int64_t)jj * n + j]);
           s_x[jj] = from_c<TO, TC>(sub_rn(to_c<TC, TO>(s_x[jj]), mul_rn(rc, l)));
         }
       }
@@ -82,11 +91,23 @@ __global__ void __launch_bounds__(256) k_hess_col(int64_t m, int n, int i, TO* _
     }
     TC v = to_c<TC, TO>(Q[row + (int64_t)i * ldq]);
     TO vo = Q[row + (int64_t)i * ldq];
-    for (int j = 0; j < i; ++j) {
-      if (!s_sel[j]) continue;
-      const TO qj = (j == i - 1) ? qprev : Q[row + (int64_t)j * ldq];
-      vo = from_c<TO, TC>(sub_rn(v, mul_rn(s_r[j], to_c<TC, TO>(qj))));
-      v = to_c<TC, TO>(vo);
+    // eliminations in MGS order; the previous columns are loaded 8 at a time ahead of the
+    // dependent chain so that the loads overlap
+    for (int j0 = 0; j0 < i; j0 += 8) {
+      TO qb[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + u;
+        qb[u] = (j < i - 1) ? Q[row + (int64_t)j * ldq] : ((j == i - 1) ? qprev : TO(0));
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + u;
+        if (j < i && s_sel[j]) {
+          vo = from_c<TO, TC>(sub_rn(v, mul_rn(s_r[j], to_c<TC, TO>(qb[u]))));
+          v = to_c<TC, TO>(vo);
+        }
+      }
     }
     Q[row + (int64_t)i * ldq] = vo;
     const double av = absd(vo);
@@ -154,19 +175,21 @@ static int hess_run(ofrr_ctx* ctx, int64_t m, int n, TO* Q, int64_t ldq, double 
   if (!pivrows) return st;
   TO* pvals = ws_get<TO>(ctx, (size_t)n, &st);
   if (!pvals) return st;
-  const int block = 256;
+  const int block = 128;  // one row per thread: 64 CTAs for 8192 rows
   int grid = grid_for(m, block, 152 * 2);
   ArgMax* partial = ws_get<ArgMax>(ctx, grid, &st);
   if (!partial) return st;
   OFRR_TRY(fill_zero(ctx, R, sizeof(double) * (size_t)n * n));
   OFRR_TRY(fill_zero(ctx, pivrows, sizeof(TO) * (size_t)n * n));
+  const int stage = ((size_t)n * n * sizeof(TO) <= 96 * 1024) ? 1 : 0;
   size_t smem = (size_t)n * (sizeof(TC) + sizeof(TO)) + 16 + (size_t)n * sizeof(int);
+  if (stage) smem += 16 + (size_t)n * n * sizeof(TO);
   if (smem > 48 * 1024) {
     OFRR_CUDA(cudaFuncSetAttribute(k_hess_col<TO, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
   for (int i = 0; i < n; ++i) {
     k_hess_col<TO, TC><<<grid, block, smem, ctx->stream>>>(m, n, i, Q, ldq, select, perm, pivrows, pvals, R, partial,
-                                                            ctx->dev_counters, select_tol, 1, nullptr);
+                                                            ctx->dev_counters, select_tol, 1, nullptr, stage);
     OFRR_LAUNCHED(ctx, "k_hess_col");
   }
   k_hess_scale<TO, TC><<<grid, block, 0, ctx->stream>>>(m, n - 1, Q, ldq, select, pvals, nullptr);
@@ -199,12 +222,14 @@ static int kry_col(ofrr_ctx* ctx, int64_t m, int nb, int i, TO* V, int64_t ldv, 
   WsScope scope(ctx);
   ArgMax* partial = ws_get<ArgMax>(ctx, grid, &st);
   if (!partial) return st;
+  const int stage = ((size_t)nb * nb * sizeof(TO) <= 96 * 1024) ? 1 : 0;
   size_t smem = (size_t)nb * (sizeof(TC) + sizeof(TO)) + 16 + (size_t)nb * sizeof(int);
+  if (stage) smem += 16 + (size_t)nb * nb * sizeof(TO);
   if (smem > 48 * 1024) {
     OFRR_CUDA(cudaFuncSetAttribute(k_hess_col<TO, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
   k_hess_col<TO, TC><<<grid, block, smem, ctx->stream>>>(m, nb, i, V, ldv, sel, perm, pivrows, pvals, R, partial,
-                                                          ctx->dev_counters, stol, 0, stop);
+                                                          ctx->dev_counters, stol, 0, stop, stage);
   OFRR_LAUNCHED(ctx, "k_hess_col");
   return OFRR_SUCCESS;
 }
@@ -339,7 +364,7 @@ int hess_run_noalloc(ofrr_ctx* sctx, unsigned char* scratch, int64_t m, int n, T
   if (smem > 48 * 1024) return OFRR_ERR_BLAS_INVALID_SIZE;
   for (int i = 0; i < n; ++i) {
     k_hess_col<TO, TC><<<grid, block, smem, sctx->stream>>>(m, n, i, Q, ldq, select, perm, pivrows, pvals, R, partial,
-                                                             counter, select_tol, 1, nullptr);
+                                                             counter, select_tol, 1, nullptr, 0);
     OFRR_LAUNCHED(sctx, "k_hess_col");
   }
   k_hess_scale<TO, TC><<<grid, block, 0, sctx->stream>>>(m, n - 1, Q, ldq, select, pvals, nullptr);

@@ -49,16 +49,18 @@ __global__ void k_slice_cols(int64_t K, int64_t Kp, int64_t N, const double* __r
     }
     __syncthreads();
     const int e = s_e;
+    // fixed point: Y = round(x 2^(BETA S - e)), |Y| <= 2^35; digits by integer arithmetic (GB300's
+    // FP64 pipe is 1/64 rate, so only one FP64 multiply and one conversion per element)
     __nv_bfloat16* col = stack + (size_t)n * S * Kp;
     for (int64_t k = threadIdx.x; k < Kp; k += blockDim.x) {
-      double y = (k < K) ? ldexp(x[k], -e) : 0.0;
+      long long r = (k < K) ? __double2ll_rn(ldexp(x[k], BETA * S - e)) : 0ll;
 #pragma unroll
-      for (int s = 0; s < S; ++s) {
-        const double t = ldexp(y, BETA);  // exact
-        const double d = rint(t);
-        y = t - d;                        // exact, |y| <= 1/2
-        col[(size_t)s * Kp + k] = __double2bfloat16(d);  // |d| <= 128: exact in bf16
+      for (int s = S - 1; s > 0; --s) {  // centred base-2^BETA digits, least significant first
+        const long long d = ((r + (1 << (BETA - 1))) & ((1 << BETA) - 1)) - (1 << (BETA - 1));
+        r = (r - d) >> BETA;  // exact: r - d is a multiple of 2^BETA
+        col[(size_t)s * Kp + k] = __float2bfloat16_rn((float)d);  // |d| <= 64
       }
+      col[k] = __float2bfloat16_rn((float)r);  // leading digit, |r| <= 128: exact in bf16
     }
     __syncthreads();
   }
@@ -94,10 +96,11 @@ __global__ void k_combine(int64_t M, int64_t N, int splits, const float* __restr
                           int64_t ldc, const int* __restrict__ ea, const int* __restrict__ eb, int shift, int first) {
   const int64_t total = M * N;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int z = 0; z < splits; ++z) s += (double)P[(size_t)z * total + e];
+    // partials are integer-valued (digit products) below 2^31 in magnitude: sum them exactly as integers
+    long long s = 0;
+    for (int z = 0; z < splits; ++z) s += (long long)__float2ll_rn(P[(size_t)z * total + e]);
     const int64_t m = e % M, n = e / M;
-    const double v = ldexp(s, ea[m] + eb[n] - shift);
+    const double v = ldexp((double)s, ea[m] + eb[n] - shift);
     double* c = C + m + n * ldc;
     *c = first ? v : (*c + v);
   }
