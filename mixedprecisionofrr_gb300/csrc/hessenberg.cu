@@ -197,6 +197,9 @@ static int hess_run(ofrr_ctx* ctx, int64_t m, int n, TO* Q, int64_t ldq, double 
   return OFRR_SUCCESS;
 }
 
+int hess_run_blocked(ofrr_ctx* ctx, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n, void* Q, int64_t ldq,
+                     double select_tol, double* R, int* select, int* perm, bool* done);
+
 int hessenberg_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n,
                     const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev,
                     int* select_dev, int* perm_dev) {
@@ -206,6 +209,10 @@ int hessenberg_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype t
   // Q <- tout(A)
   if (A != Q || tin != tout || lda != ldq) OFRR_TRY(cast_impl(ctx, tin, tout, m, n, A, lda, Q, ldq));
   WsScope scope(ctx);
+  // blocked cluster schedule (hessenberg_blocked.cu) when the block fits on chip, else per column
+  bool done = false;
+  OFRR_TRY(hess_run_blocked(ctx, tout, tc, m, n, Q, ldq, select_tol, R_dev, select_dev, perm_dev, &done));
+  if (done) return OFRR_SUCCESS;
   OFRR_DISPATCH_STORAGE(tout, TO, OFRR_DISPATCH_COMPUTE(tc, TC, {
     OFRR_TRY((hess_run<TO, TC>(ctx, m, (int)n, (TO*)Q, ldq, select_tol, R_dev, select_dev, perm_dev)));
   }));

@@ -76,10 +76,11 @@ __global__ void __launch_bounds__(256) k_chol_f64(int n, const double* const* Ms
 __global__ void __launch_bounds__(128) k_trsm_f64(int n, int nrhs, const double* __restrict__ L, int ldl,
                                                   const double* __restrict__ B, int ldb, int transB,
                                                   double* __restrict__ X, int ldx, int upper) {
-  extern __shared__ double sm_trsm[];  // L (n x n) staged, then 4 warps x n solution entries
+  extern __shared__ double sm_trsm[];  // L (n x n, padded ld n+1) staged, then 4 warps x n solution entries
+  const int ld = n + 1;
   double* Ls = sm_trsm;
-  double* xs = sm_trsm + (size_t)n * n;
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) Ls[e] = L[(e % n) + (size_t)(e / n) * ldl];
+  double* xs = sm_trsm + (size_t)n * ld;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) Ls[(e % n) + (e / n) * ld] = L[(e % n) + (size_t)(e / n) * ldl];
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int col = blockIdx.x * 4 + w;
@@ -92,13 +93,13 @@ __global__ void __launch_bounds__(128) k_trsm_f64(int n, int nrhs, const double*
     const int i = upper ? (n - 1 - t) : t;
     double s = 0.0;
     if (!upper) {
-      for (int k = lane; k < i; k += 32) s += Ls[i + k * n] * x[k];
+      for (int k = lane; k < i; k += 32) s += Ls[i + k * ld] * x[k];
     } else {
-      for (int k = i + 1 + lane; k < n; k += 32) s += Ls[k + i * n] * x[k];
+      for (int k = i + 1 + lane; k < n; k += 32) s += Ls[k + i * ld] * x[k];
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) x[i] = (x[i] - s) / Ls[i + i * n];
+    if (lane == 0) x[i] = (x[i] - s) / Ls[i + i * ld];
     __syncwarp();
   }
   for (int i = lane; i < n; i += 32) X[i + (size_t)col * ldx] = x[i];
@@ -126,8 +127,9 @@ __device__ __forceinline__ int rr_idx(int i, int r, int N) { return i == 0 ? 0 :
 __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restrict__ Cin, int ldc,
                                                     double* __restrict__ Wout, double* __restrict__ lam) {
   extern __shared__ float smf[];
+  const int ld = n + 1;  // padded: row-wise accesses at stride ld spread over the 32 banks
   float* C = smf;
-  float* W = smf + n * n;
+  float* W = smf + n * ld;
   __shared__ float s_c[64], s_s[64];
   __shared__ int s_p[64], s_q[64];
   __shared__ float s_red[32];
@@ -135,17 +137,18 @@ __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restr
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < n * n; e += nt) {
     const int i = e % n, j = e / n;
-    C[e] = (float)(0.5 * (Cin[i + (size_t)j * ldc] + Cin[j + (size_t)i * ldc]));
-    W[e] = (i == j) ? 1.f : 0.f;
+    C[i + j * ld] = (float)(0.5 * (Cin[i + (size_t)j * ldc] + Cin[j + (size_t)i * ldc]));
+    W[i + j * ld] = (i == j) ? 1.f : 0.f;
   }
   __syncthreads();
   const int N = n + (n & 1), npair = N / 2;
   for (int sweep = 0; sweep < 10 && n > 1; ++sweep) {
     float off = 0.f, tot = 0.f;
     for (int e = tid; e < n * n; e += nt) {
-      const float v = C[e] * C[e];
+      const int i = e % n, j = e / n;
+      const float v = C[i + j * ld] * C[i + j * ld];
       tot += v;
-      if ((e % n) != (e / n)) off += v;
+      if (i != j) off += v;
     }
     for (int o = 16; o > 0; o >>= 1) {
       off += __shfl_down_sync(0xffffffffu, off, o);
@@ -177,9 +180,9 @@ __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restr
         }
         float c = 1.f, s = 0.f;
         if (q < n) {
-          const float apq = C[p + q * n];
+          const float apq = C[p + q * ld];
           if (apq != 0.f) {
-            const float tau = (C[q + q * n] - C[p + p * n]) / (2.f * apq);
+            const float tau = (C[q + q * ld] - C[p + p * ld]) / (2.f * apq);
             const float t = (tau >= 0.f) ? 1.f / (tau + sqrtf(1.f + tau * tau)) : -1.f / (-tau + sqrtf(1.f + tau * tau));
             c = rsqrtf(1.f + t * t);
             s = t * c;
@@ -196,9 +199,9 @@ __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restr
         if (q < 0) continue;
         const int p = s_p[k];
         const float c = s_c[k], s = s_s[k];
-        const float ap = C[p + j * n], aq = C[q + j * n];
-        C[p + j * n] = c * ap - s * aq;
-        C[q + j * n] = s * ap + c * aq;
+        const float ap = C[p + j * ld], aq = C[q + j * ld];
+        C[p + j * ld] = c * ap - s * aq;
+        C[q + j * ld] = s * ap + c * aq;
       }
       __syncthreads();
       for (int e = tid; e < npair * n; e += nt) {
@@ -206,28 +209,28 @@ __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restr
         if (q < 0) continue;
         const int p = s_p[k];
         const float c = s_c[k], s = s_s[k];
-        float ap = C[i + p * n], aq = C[i + q * n];
-        C[i + p * n] = c * ap - s * aq;
-        C[i + q * n] = s * ap + c * aq;
-        ap = W[i + p * n];
-        aq = W[i + q * n];
-        W[i + p * n] = c * ap - s * aq;
-        W[i + q * n] = s * ap + c * aq;
+        float ap = C[i + p * ld], aq = C[i + q * ld];
+        C[i + p * ld] = c * ap - s * aq;
+        C[i + q * ld] = s * ap + c * aq;
+        ap = W[i + p * ld];
+        aq = W[i + q * ld];
+        W[i + p * ld] = c * ap - s * aq;
+        W[i + q * ld] = s * ap + c * aq;
       }
       __syncthreads();
       for (int k = tid; k < npair; k += nt) {
         const int q = s_q[k];
         if (q >= 0) {
           const int p = s_p[k];
-          C[p + q * n] = 0.f;
-          C[q + p * n] = 0.f;
+          C[p + q * ld] = 0.f;
+          C[q + p * ld] = 0.f;
         }
       }
       __syncthreads();
     }
   }
-  for (int e = tid; e < n * n; e += nt) Wout[e] = (double)W[e];
-  for (int i = tid; i < n; i += nt) lam[i] = (double)C[i + i * n];
+  for (int e = tid; e < n * n; e += nt) Wout[e] = (double)W[(e % n) + (e / n) * ld];
+  for (int i = tid; i < n; i += nt) lam[i] = (double)C[i + i * ld];
 }
 
 // ---- 4. Ogita-Aishima correction: from P = W'W and T = W'CW build lambda and F = I + E ------------
@@ -296,7 +299,7 @@ static int gemm_small(ofrr_ctx* ctx, int M, int N, int K, double alpha, const do
 
 static int trsm(ofrr_ctx* ctx, int n, int nrhs, const double* L, const double* B, int ldb, int transB, double* X,
                 int upper) {
-  const size_t smem = ((size_t)n * n + 4 * (size_t)n) * sizeof(double);
+  const size_t smem = ((size_t)n * (n + 1) + 4 * (size_t)n) * sizeof(double);
   OFRR_CUDA(cudaFuncSetAttribute(k_trsm_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_trsm_f64<<<(nrhs + 3) / 4, 128, smem, ctx->stream>>>(n, nrhs, L, n, B, ldb, transB, X, n, upper);
   OFRR_LAUNCHED(ctx, "k_trsm_f64");
@@ -328,7 +331,7 @@ static int sym_eig_refined(ofrr_ctx* ctx, int n, const double* C, double* W, dou
          *T = ws_get<double>(ctx, (size_t)n * n, &st), *F = ws_get<double>(ctx, (size_t)n * n, &st),
          *l0 = ws_get<double>(ctx, (size_t)n, &st);
   if (!W0 || !W1 || !P || !CW || !T || !F || !l0) return st;
-  const size_t smem = (size_t)2 * n * n * sizeof(float);
+  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(float);
   OFRR_CUDA(cudaFuncSetAttribute(k_jacobi_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_jacobi_f32<<<1, 512, smem, ctx->stream>>>(n, C, n, W0, l0);
   OFRR_LAUNCHED(ctx, "k_jacobi_f32");

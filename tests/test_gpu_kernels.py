@@ -192,3 +192,27 @@ def test_check_special_values(api):
     assert api.check_special_values(X) == 1005
     X[5, 1] = np.inf
     assert api.check_special_values(X) == 1006
+
+
+@pytest.mark.parametrize("pc,po,shape", [("single", "half", (3000, 64)), ("double", "double", (8192, 64)),
+                                         ("single", "single", (1500, 37)), ("single", "half", (20000, 96))])
+def test_hessenberg_blocked_equals_per_column(api, orc, pc, po, shape):
+    """The cluster-blocked schedule and the per-column schedule give bit-identical bases."""
+    import os
+
+    rng = np.random.default_rng(shape[0] + shape[1])
+    A = rng.uniform(-1, 1, shape).astype(orc._dt(po))
+    A[:, 20] = A[:, 3]  # a dependent column inside the second block
+    Qb, Rb, selb, permb = api.hessenberg(A, pc, po)
+    os.environ["OFRR_HESS_PER_COLUMN"] = "1"
+    try:
+        Qc, Rc, selc, permc = api.hessenberg(A, pc, po)
+    finally:
+        del os.environ["OFRR_HESS_PER_COLUMN"]
+    assert np.array_equal(permb, permc) and np.array_equal(selb, selc)
+    assert np.array_equal(api.to_numpy(Qb), api.to_numpy(Qc))
+    assert np.array_equal(Rb, Rc)
+    assert not selb[20]
+    if shape[0] <= 3000:
+        Qo, Ro, selo, permo = orc.hessenberg(A, pc, po)
+        assert np.array_equal(api.to_numpy(Qb), Qo) and np.array_equal(permb, permo)
