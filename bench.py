@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--profile-solve", action="store_true",
                     help="run one warm-up and one mixed solve only (for a profiler's launch list)")
+    ap.add_argument("--roofline-only", action="store_true",
+                    help="run only the live timing of the roofline kernel (for an ncu capture of it)")
     return ap.parse_args()
 
 
@@ -247,6 +249,20 @@ def gemm_roofline(api, steps=50):
     return dt, algo_bytes, flops
 
 
+def profiled_traffic():
+    """DRAM bytes per launch of the roofline kernel, from the committed ncu summary (None if absent)."""
+    p = ROOT / "profiles" / "k_gemm_tn_av_8192x64x2048.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(float(line.split(":", 1)[1].strip()))
+            except ValueError:
+                return None
+    return None
+
+
 def cpu_baseline_run(A_host, max_seconds=60.0):
     """The oracle (FP64 NumPy/SciPy restatement of the reference's MATLAB path) on this host's cores:
     one full solve with the same block / step / tolerance, stopped at max residual <= 1e-8."""
@@ -287,6 +303,10 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from mixedprecisionofrr_gb300 import api
 
+    if args.roofline_only:
+        dt_g, bytes_g, flops_g = gemm_roofline(api, steps=20)
+        print(json.dumps({"roofline_only": True, "us_per_launch": dt_g * 1e6, "GBps": bytes_g / dt_g / 1e9}))
+        return
     A, s_true = make_problem_gpu()
     if args.profile_solve:
         run_solver(api, A, "mixed")
@@ -339,9 +359,10 @@ def main():
             peaks = json.loads(pk.read_text())
         dt_g, bytes_g, flops_g = gemm_roofline(api)
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
-        roof = {"kernel": "A.V 16-bit GEMM 8192x2048x64 (FP32 accumulate)", "bound": "hbm",
+        roof = {"kernel": "k_gemm_tn: A.V 16-bit TN GEMM 8192x2048x64 (FP32 accumulate)", "bound": "hbm",
                 "achieved": bytes_g / dt_g / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                "frac": bytes_g / dt_g / 1e9 / hbm_peak, "traffic": None,
+                "frac": bytes_g / dt_g / 1e9 / hbm_peak, "traffic": profiled_traffic(),
+                "algorithmic_bytes": bytes_g,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "us_per_launch": dt_g * 1e6, "tflops": flops_g / dt_g / 1e12}
         cpu = None
