@@ -1,5 +1,7 @@
 // Context, workspace, status handling and the level-1/2 kernels of libofrr_gb300.so:
 // project RNG, casts, column argmax / scalecols, iamax, NaN/Inf scan, column norms.
+#include <type_traits>
+
 #include "ofrr_internal.cuh"
 
 #include <cmath>
@@ -116,36 +118,135 @@ __global__ void k_cast(int64_t m, int64_t n, const TI* in, int64_t ldin, TO* out
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     int64_t i = e % m, j = e / m;
-    out[i + j * ldout] = from_c<TO, double>(to_c<double, TI>(in[i + j * ldin]));
+    // through FP32 when neither side is FP64 (exact: every 16/32-bit value is a float; RN once)
+    if constexpr (std::is_same<TI, double>::value || std::is_same<TO, double>::value)
+      out[i + j * ldout] = from_c<TO, double>(to_c<double, TI>(in[i + j * ldin]));
+    else
+      out[i + j * ldout] = from_c<TO, float>(to_c<float, TI>(in[i + j * ldin]));
   }
 }
 
 // --------------------------------------------------------------------------------------
-// column argmax + scaling (scalecols.m:27-32); one CTA per column, grid-stride over rows
+// column argmax + scaling (scalecols.m:27-32)
+// Argmax on integer keys of |x| (no FP64 compares); lowest row among equal maxima.  Columns up to
+// SC_CHUNK rows: one CTA per column, values held in registers between the search and the scaling.
+// Longer columns: a grid of (chunks x columns) CTAs finds per-chunk maxima (with their values),
+// then the same grid reduces a column's chunk maxima and scales its chunk.
 // --------------------------------------------------------------------------------------
-template <class TO, class TC>
-__global__ void k_scalecols(int64_t m, int64_t n, TO* U, int64_t ldu, int* piv, int do_scale) {
-  __shared__ ArgMax red[32];
-  __shared__ TC s_t;
-  for (int64_t j = blockIdx.x; j < n; j += gridDim.x) {
-    TO* col = U + j * ldu;
-    ArgMax a{-1.0, 0x7fffffffffffffffLL};
-    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
-      double v = absd(col[i]);
-      if (v > a.v) a = ArgMax{v, i};  // per-thread rows ascend: strict > keeps the lowest
+constexpr int SC_T = 256;
+constexpr int SC_U = 8;
+constexpr int64_t SC_CHUNK = (int64_t)SC_T * SC_U;
+
+template <class TC, bool FAST>
+__device__ __forceinline__ TC scale_by(TC q, TC t, TC y, bool pf, bool is_pivot) {
+  if (FAST && pf) return is_pivot ? TC(1) : mul_rn(q, y);  // within an ulp of q / t
+  return pivot_div(q, t, y, pf);                           // correctly rounded q / t
+}
+
+template <class TO, class TC, bool FAST>
+__global__ void __launch_bounds__(SC_T) k_scalecols_small(int64_t m, TO* U, int64_t ldu, int* piv, int do_scale) {
+  __shared__ ArgMaxK red[SC_T / 32];
+  __shared__ TO s_t;
+  TO* col = U + (int64_t)blockIdx.x * ldu;
+  TO v[SC_U];
+  ArgMaxK a{-1, 0x7fffffffffffffffLL};
+#pragma unroll
+  for (int u = 0; u < SC_U; ++u) {
+    const int64_t i = threadIdx.x + (int64_t)u * SC_T;
+    v[u] = (i < m) ? col[i] : TO(0);
+  }
+#pragma unroll
+  for (int u = 0; u < SC_U; ++u) {
+    const int64_t i = threadIdx.x + (int64_t)u * SC_T;
+    if (i < m) {
+      const long long key = amax_key(v[u]);
+      if (key > a.key) a = ArgMaxK{key, i};  // per-thread rows ascend: strict > keeps the lowest
     }
-    ArgMax r = block_argmax(a, red);
-    int64_t k = (r.v < 0.0) ? 0 : r.i;
+  }
+  const ArgMaxK r = block_argmaxk(a, red);
+  const int64_t k = (r.key < 0) ? 0 : r.i;
+  if (threadIdx.x == 0) {
+    if (piv) piv[blockIdx.x] = (int)k;
+    s_t = (m > 0) ? col[k] : TO(0);
+  }
+  __syncthreads();
+  const TC t = to_c<TC, TO>(s_t);
+  if (!do_scale || t == TC(0)) return;
+  const TC y = pivot_recip(t);
+  const bool pf = pivot_fast(t);
+#pragma unroll
+  for (int u = 0; u < SC_U; ++u) {
+    const int64_t i = threadIdx.x + (int64_t)u * SC_T;
+    if (i < m) col[i] = from_c<TO, TC>(scale_by<TC, FAST>(to_c<TC, TO>(v[u]), t, y, pf, i == k));
+  }
+}
+
+template <class TO>
+__global__ void __launch_bounds__(SC_T) k_colamax(int64_t m, const TO* U, int64_t ldu, ArgMaxK* part, double* pval) {
+  __shared__ ArgMaxK red[SC_T / 32];
+  const TO* col = U + (int64_t)blockIdx.y * ldu;
+  const int64_t r0 = (int64_t)blockIdx.x * SC_CHUNK;
+  TO v[SC_U];
+  ArgMaxK a{-1, 0x7fffffffffffffffLL};
+#pragma unroll
+  for (int u = 0; u < SC_U; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * SC_T;
+    v[u] = (i < m) ? col[i] : TO(0);
+  }
+#pragma unroll
+  for (int u = 0; u < SC_U; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * SC_T;
+    if (i < m) {
+      const long long key = amax_key(v[u]);
+      if (key > a.key) a = ArgMaxK{key, i};
+    }
+  }
+  const ArgMaxK r = block_argmaxk(a, red);
+  const size_t slot = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
+  if (threadIdx.x == 0) part[slot] = r;
+  // the maximum's value, read by the thread that holds it (before any CTA scales the column)
+#pragma unroll
+  for (int u = 0; u < SC_U; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * SC_T;
+    if (r.key >= 0 && i == r.i) pval[slot] = to_c<double, TO>(v[u]);
+  }
+}
+
+template <class TO, class TC, bool FAST>
+__global__ void __launch_bounds__(SC_T) k_colscale(int64_t m, TO* U, int64_t ldu, const ArgMaxK* part,
+                                                   const double* pval, int* piv, int do_scale) {
+  __shared__ double s_t;
+  __shared__ long long s_k;
+  const int nchunks = gridDim.x;
+  TO* col = U + (int64_t)blockIdx.y * ldu;
+  if (threadIdx.x < 32) {
+    ArgMaxK b{-1, 0x7fffffffffffffffLL};
+    for (int c = threadIdx.x; c < nchunks; c += 32) b = argmaxk_pick(b, part[(size_t)blockIdx.y * nchunks + c]);
+    b = warp_argmaxk(b);
     if (threadIdx.x == 0) {
-      if (piv) piv[j] = (int)k;
-      s_t = (m > 0) ? to_c<TC, TO>(col[k]) : TC(0);
+      const int64_t k = (b.key < 0) ? 0 : b.i;
+      s_k = k;
+      s_t = (b.key < 0) ? 0.0 : pval[(size_t)blockIdx.y * nchunks + k / SC_CHUNK];
+      if (piv && blockIdx.x == 0) piv[blockIdx.y] = (int)k;
     }
-    __syncthreads();
-    const TC t = s_t;
-    if (do_scale && t != TC(0)) {
-      for (int64_t i = threadIdx.x; i < m; i += blockDim.x) col[i] = from_c<TO, TC>(div_rn(to_c<TC, TO>(col[i]), t));
-    }
-    __syncthreads();
+  }
+  __syncthreads();
+  const TC t = to_c<TC, double>(s_t);
+  if (!do_scale || t == TC(0)) return;
+  const int64_t k = s_k;
+  const TC y = pivot_recip(t);
+  const bool pf = pivot_fast(t);
+  const int64_t r0 = (int64_t)blockIdx.x * SC_CHUNK;
+  TO v[SC_U];
+#pragma unroll
+  for (int u = 0; u < SC_U; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * SC_T;
+    v[u] = (i < m) ? col[i] : TO(0);
+  }
+#pragma unroll
+  for (int u = 0; u < SC_U; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * SC_T;
+    if (i < m) col[i] = from_c<TO, TC>(scale_by<TC, FAST>(to_c<TC, TO>(v[u]), t, y, pf, i == k));
   }
 }
 
@@ -255,13 +356,39 @@ int cast_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, int64_t m, int64_t
   return OFRR_SUCCESS;
 }
 
+template <class TO, class TC, bool FAST>
+static int scalecols_t(ofrr_ctx* ctx, int64_t m, int64_t n, TO* U, int64_t ldu, int* piv, int do_scale = 1) {
+  if (m <= SC_CHUNK) {
+    k_scalecols_small<TO, TC, FAST><<<(unsigned)n, SC_T, 0, ctx->stream>>>(m, U, ldu, piv, do_scale);
+    OFRR_LAUNCHED(ctx, "k_scalecols_small");
+    return OFRR_SUCCESS;
+  }
+  int st = OFRR_SUCCESS;
+  WsScope scope(ctx);
+  const int64_t nchunks = (m + SC_CHUNK - 1) / SC_CHUNK;
+  if (nchunks > 65535) return OFRR_ERR_BLAS_INVALID_SIZE;
+  ArgMaxK* part = ws_get<ArgMaxK>(ctx, (size_t)nchunks * n, &st);
+  if (!part) return st;
+  double* pval = ws_get<double>(ctx, (size_t)nchunks * n, &st);
+  if (!pval) return st;
+  const dim3 grid((unsigned)nchunks, (unsigned)n);
+  k_colamax<TO><<<grid, SC_T, 0, ctx->stream>>>(m, U, ldu, part, pval);
+  OFRR_LAUNCHED(ctx, "k_colamax");
+  k_colscale<TO, TC, FAST><<<grid, SC_T, 0, ctx->stream>>>(m, U, ldu, part, pval, piv, do_scale);
+  OFRR_LAUNCHED(ctx, "k_colscale");
+  return OFRR_SUCCESS;
+}
+
 int scalecols_impl(ofrr_ctx* ctx, ofrr_dtype po, ofrr_dtype pc, int64_t m, int64_t n, void* U, int64_t ldu,
-                   int* piv) {
+                   int* piv, bool fast) {
   if (n <= 0) return OFRR_SUCCESS;
-  int grid = (int)(n < 65535 ? n : 65535);
+  if (n > 65535) return OFRR_ERR_BLAS_INVALID_SIZE;
+  if (fast && pc == OFRR_F64) {
+    OFRR_DISPATCH_STORAGE(po, TO, { OFRR_TRY((scalecols_t<TO, double, true>(ctx, m, n, (TO*)U, ldu, piv))); });
+    return OFRR_SUCCESS;
+  }
   OFRR_DISPATCH_STORAGE(po, TO, OFRR_DISPATCH_COMPUTE(pc, TC, {
-    k_scalecols<TO, TC><<<grid, 1024, 0, ctx->stream>>>(m, n, (TO*)U, ldu, piv, 1);
-    OFRR_LAUNCHED(ctx, "k_scalecols");
+    OFRR_TRY((scalecols_t<TO, TC, false>(ctx, m, n, (TO*)U, ldu, piv)));
   }));
   return OFRR_SUCCESS;
 }
@@ -456,11 +583,8 @@ int ofrr_matrix_iamax(ofrr_ctx* ctx, ofrr_dtype dt, int64_t m, int64_t n, const 
   if (!ctx || m < 0 || n < 0 || !dtype_valid(dt)) return OFRR_ERR_INVALID_ARGUMENT;
   if (m > 0 && n > 0 && (!A || !idx || lda < m)) return OFRR_ERR_INVALID_ARGUMENT;
   if (m == 0 || n == 0) return OFRR_SUCCESS;
-  int grid = (int)(n < 65535 ? n : 65535);
-  OFRR_DISPATCH_STORAGE(dt, T, {
-    k_scalecols<T, double><<<grid, 1024, 0, ctx->stream>>>(m, n, (T*)A, lda, idx, 0);
-    OFRR_LAUNCHED(ctx, "k_matrix_iamax");
-  });
+  if (n > 65535) return OFRR_ERR_BLAS_INVALID_SIZE;
+  OFRR_DISPATCH_STORAGE(dt, T, { OFRR_TRY((scalecols_t<T, double, false>(ctx, m, n, (T*)A, lda, idx, 0))); });
   return OFRR_SUCCESS;
 }
 

@@ -198,11 +198,11 @@ static int hess_run(ofrr_ctx* ctx, int64_t m, int n, TO* Q, int64_t ldq, double 
 }
 
 int hess_run_blocked(ofrr_ctx* ctx, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n, void* Q, int64_t ldq,
-                     double select_tol, double* R, int* select, int* perm, bool* done);
+                     double select_tol, double* R, int* select, int* perm, bool fast, bool* done);
 
 int hessenberg_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n,
                     const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev,
-                    int* select_dev, int* perm_dev) {
+                    int* select_dev, int* perm_dev, bool fast) {
   if (n <= 0 || m <= 0) return OFRR_SUCCESS;
   if (n > 4096) return OFRR_ERR_BLAS_INVALID_SIZE;
   if (select_tol < 0) select_tol = dtype_eps(tout);
@@ -211,7 +211,7 @@ int hessenberg_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype t
   WsScope scope(ctx);
   // blocked cluster schedule (hessenberg_blocked.cu) when the block fits on chip, else per column
   bool done = false;
-  OFRR_TRY(hess_run_blocked(ctx, tout, tc, m, n, Q, ldq, select_tol, R_dev, select_dev, perm_dev, &done));
+  OFRR_TRY(hess_run_blocked(ctx, tout, tc, m, n, Q, ldq, select_tol, R_dev, select_dev, perm_dev, fast, &done));
   if (done) return OFRR_SUCCESS;
   OFRR_DISPATCH_STORAGE(tout, TO, OFRR_DISPATCH_COMPUTE(tc, TC, {
     OFRR_TRY((hess_run<TO, TC>(ctx, m, (int)n, (TO*)Q, ldq, select_tol, R_dev, select_dev, perm_dev)));

@@ -2,20 +2,21 @@
 //
 // Same arithmetic as the per-column kernel in hessenberg.cu (MATLAB/+src/+qr/hessenberg.m:45-85,
 // MGS order, one rounding to the output type per elimination), so results are bit-identical; only
-// the schedule changes.  Columns are taken in blocks of HB_B = 16:
-//   1. k_hess_blockupd (one launch per block, all SMs): every column of the block is eliminated
-//      against the already final columns 0..c0-1 in order j = 0, 1, ..., c0-1.  The coefficients
-//      r_{j,i} come from a forward substitution over the c0 pivot rows (one warp per column of the
-//      block).  Each thread loads q_j(row) once per j and applies it to all block columns.
-//   2. k_hess_inblock (one launch per block, one 8-CTA cluster): the block's columns are processed
-//      one after another entirely on chip.  Each CTA keeps its slice of rows of the block in shared
-//      memory; the grid-wide argmax of a column is a cluster barrier plus reads of the other CTAs'
-//      partials through distributed shared memory; every CTA then reads the pivot row of the block
-//      from its owner (DSMEM), which holds exactly the values the later columns' substitutions need.
-// For b = 64 columns this is 7 launches instead of 65.  Used when the block's rows fit in the
-// cluster's shared memory; larger problems keep the per-column kernel.
+// the schedule changes.  Columns are taken in blocks of HB_B = 16; for a block [c0, c1):
+//   0. k_hess_blockcoef (one CTA): the coefficients r_{j,i}, j < c0, of every block column by a
+//      forward substitution over the c0 pivot rows (one warp per block column), and R(j, i).  The
+//      pivot rows are read from Q while the block columns are still untouched, before any update.
+//   1. k_hess_blockupd (all SMs): every block column is eliminated against the final columns
+//      0..c0-1 in order j = 0, 1, ..., c0-1; each thread owns one row and HB_CG block columns.
+//   2. k_hess_inblock (one cluster of 8 or 16 CTAs): the block's columns one after another entirely
+//      on chip.  Each CTA keeps its slice of rows of the block in shared memory.  Per column: local
+//      eliminations and argmax, then each CTA publishes its candidate (argmax and the block's values
+//      in that row); after ONE cluster barrier every CTA reads all candidates through distributed
+//      shared memory, picks the winner and takes the pivot row from it.
+// For b = 64 columns this is 10 launches instead of 65.
 #include <cooperative_groups.h>
 
+#include <atomic>
 #include <cstdlib>
 
 #include "ofrr_internal.cuh"
@@ -24,114 +25,163 @@ namespace cg = cooperative_groups;
 
 namespace ofrr {
 
-constexpr int HB_B = 16;        // block width (columns)
-constexpr int HB_CL = 8;        // CTAs per cluster (portable cluster size)
-constexpr int HB_T = 256;       // threads per CTA
+constexpr int HB_B = 16;     // block width (columns)
+constexpr int HB_T = 256;    // threads per CTA of the in-block kernel
+constexpr int HB_UT = 128;   // threads per CTA of the block update
+constexpr int HB_CG = 2;     // block columns per CTA of the block update
 constexpr size_t HB_SMEM_MAX = 200 * 1024;
 
-// ---- step 1: eliminate block columns [c0, c1) against final columns [0, c0) -----------------------
-template <class TO, class TC>
-__global__ void __launch_bounds__(HB_T) k_hess_blockupd(int64_t m, int n, int c0, int c1, TO* __restrict__ Q,
-                                                        int64_t ldq, const int* __restrict__ select,
-                                                        const int* __restrict__ perm, const TO* __restrict__ pivrows,
-                                                        double* __restrict__ R) {
+// One MGS elimination v - r q in the compute type.  Exact mode: the product rounded, then the
+// difference (hessenberg.m's arithmetic, bit-identical to the per-column kernel).  FAST (FP64
+// refinement phase of the mixed and FP64 solvers): one FMA, and pivot scaling by the correctly
+// rounded reciprocal; GB300's FP64 pipe is 1/64 rate, so this halves the work that bounds the build.
+template <bool FAST> __device__ __forceinline__ double elim(double v, double r, double q) {
+  return FAST ? __fma_rn(-r, q, v) : __dsub_rn(v, __dmul_rn(r, q));
+}
+template <bool FAST> __device__ __forceinline__ float elim(float v, float r, float q) {
+  return FAST ? __fmaf_rn(-r, q, v) : __fsub_rn(v, __fmul_rn(r, q));
+}
+__device__ __forceinline__ double mul_recip(double x, double y) { return __dmul_rn(x, y); }
+__device__ __forceinline__ float mul_recip(float x, float y) { return __fmul_rn(x, y); }
+
+// ---- step 0: coefficients of the block columns against the final columns [0, c0) -----------------
+template <class TO, class TC, bool FAST>
+__global__ void __launch_bounds__(HB_B * 32) k_hess_blockcoef(int n, int c0, int c1, const TO* __restrict__ Q,
+                                                              int64_t ldq, const int* __restrict__ select,
+                                                              const int* __restrict__ perm, TC* __restrict__ rcoef,
+                                                              double* __restrict__ R) {
   extern __shared__ unsigned char smem_raw[];
   const int nb = c1 - c0;
-  TC* s_r = reinterpret_cast<TC*>(smem_raw);                                // HB_B x c0
-  TO* s_x = reinterpret_cast<TO*>(s_r + HB_B * c0);                         // HB_B x c0
-  TO* s_L = reinterpret_cast<TO*>(((uintptr_t)(s_x + HB_B * c0) + 15) & ~(uintptr_t)15);  // c0 x c0
-  int* s_sel = reinterpret_cast<int*>(((uintptr_t)(s_L + c0 * c0) + 15) & ~(uintptr_t)15); // c0
+  TO* s_L = reinterpret_cast<TO*>(smem_raw);                                               // c0 x c0
+  TO* s_x = s_L + (size_t)c0 * c0;                                                          // HB_B x c0
+  int* s_sel = reinterpret_cast<int*>(((uintptr_t)(s_x + (size_t)HB_B * c0) + 15) & ~(uintptr_t)15);  // c0
+  int* s_perm = s_sel + c0;                                                                 // c0
   const int tid = threadIdx.x;
-  for (int j = tid; j < c0; j += blockDim.x) s_sel[j] = select[j];
+  for (int j = tid; j < c0; j += blockDim.x) {
+    s_sel[j] = select[j];
+    s_perm[j] = perm[j];
+  }
+  __syncthreads();
+  // pivot row jj of the final columns l < jj, and the (untouched) block columns at the pivot rows
   for (int e = tid; e < c0 * c0; e += blockDim.x) {
     const int jj = e / c0, l = e % c0;
-    if (l < jj) s_L[e] = pivrows[(int64_t)jj * n + l];
+    if (l < jj) s_L[e] = s_sel[jj] ? Q[(int64_t)s_perm[jj] + (int64_t)l * ldq] : TO(0);
   }
-  __syncthreads();
   for (int e = tid; e < nb * c0; e += blockDim.x) {
     const int t = e / c0, j = e % c0;
-    s_x[t * c0 + j] = s_sel[j] ? Q[(int64_t)perm[j] + (int64_t)(c0 + t) * ldq] : TO(0);
+    s_x[t * c0 + j] = s_sel[j] ? Q[(int64_t)s_perm[j] + (int64_t)(c0 + t) * ldq] : TO(0);
   }
   __syncthreads();
-  // forward substitution per block column (warp w handles columns w, w + 8, ...)
   const int warp = tid >> 5, lane = tid & 31;
-  for (int t = warp; t < nb; t += (blockDim.x >> 5)) {
-    TO* x = s_x + t * c0;
-    TC* r = s_r + t * c0;
+  if (warp < nb) {
+    TO* x = s_x + warp * c0;
+    TC* r = rcoef + (size_t)warp * c0;
     for (int j = 0; j < c0; ++j) {
       __syncwarp();
       if (!s_sel[j]) {
-        if (lane == 0) r[j] = TC(0);
+        if (lane == 0) {
+          r[j] = TC(0);
+          R[j + (int64_t)(c0 + warp) * n] = 0.0;
+        }
         continue;
       }
       const TC rc = to_c<TC, TO>(x[j]);
       for (int jj = j + 1 + lane; jj < c0; jj += 32) {
-        if (s_sel[jj]) x[jj] = from_c<TO, TC>(sub_rn(to_c<TC, TO>(x[jj]), mul_rn(rc, to_c<TC, TO>(s_L[jj * c0 + j]))));
+        if (s_sel[jj]) x[jj] = from_c<TO, TC>(elim<FAST>(to_c<TC, TO>(x[jj]), rc, to_c<TC, TO>(s_L[jj * c0 + j])));
       }
-      if (lane == 0) r[j] = rc;
+      if (lane == 0) {
+        r[j] = rc;
+        R[j + (int64_t)(c0 + warp) * n] = to_c<double, TC>(rc);
+      }
     }
-    __syncwarp();
   }
+}
+
+// ---- step 1: eliminate block columns against the final columns [0, c0) ----------------------------
+template <class TO, class TC, bool FAST>
+__global__ void __launch_bounds__(HB_UT) k_hess_blockupd(int64_t m, int c0, int c1, TO* __restrict__ Q, int64_t ldq,
+                                                         const int* __restrict__ select,
+                                                         const TC* __restrict__ rcoef) {
+  extern __shared__ unsigned char smem_raw[];
+  TC* s_r = reinterpret_cast<TC*>(smem_raw);                // HB_CG x c0
+  int* s_sel = reinterpret_cast<int*>(s_r + HB_CG * c0);   // c0
+  const int tid = threadIdx.x;
+  const int t0 = c0 + blockIdx.y * HB_CG;
+  const int nl = min(HB_CG, c1 - t0);
+  for (int e = tid; e < nl * c0; e += blockDim.x) s_r[e] = rcoef[(size_t)(t0 - c0) * c0 + e];
+  for (int j = tid; j < c0; j += blockDim.x) s_sel[j] = select[j];
   __syncthreads();
-  if (blockIdx.x == 0) {  // R(j, i) for j < c0
-    for (int e = tid; e < nb * c0; e += blockDim.x) {
-      const int t = e / c0, j = e % c0;
-      R[j + (int64_t)(c0 + t) * n] = s_sel[j] ? to_c<double, TC>(s_r[t * c0 + j]) : 0.0;
-    }
+  const int64_t row = blockIdx.x * (int64_t)HB_UT + tid;
+  if (row >= m) return;
+  TC v[HB_CG];
+  TO vo[HB_CG];
+#pragma unroll
+  for (int t = 0; t < HB_CG; ++t) {
+    vo[t] = (t < nl) ? Q[row + (int64_t)(t0 + t) * ldq] : TO(0);
+    v[t] = to_c<TC, TO>(vo[t]);
   }
-  // eliminations, MGS order j = 0 .. c0-1 for every block column of this thread's rows
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + tid; row < m; row += stride) {
-    TC v[HB_B];
-    TO vo[HB_B];
+  constexpr int U = 8;  // loads of Q(row, j) issued ahead of their use
+  for (int j0 = 0; j0 < c0; j0 += U) {
+    TO q[U];
 #pragma unroll
-    for (int t = 0; t < HB_B; ++t) {
-      vo[t] = (t < nb) ? Q[row + (int64_t)(c0 + t) * ldq] : TO(0);
-      v[t] = to_c<TC, TO>(vo[t]);
-    }
-    for (int j = 0; j < c0; ++j) {
-      if (!s_sel[j]) continue;
-      const TC q = to_c<TC, TO>(Q[row + (int64_t)j * ldq]);
+    for (int u = 0; u < U; ++u) q[u] = (j0 + u < c0) ? Q[row + (int64_t)(j0 + u) * ldq] : TO(0);
 #pragma unroll
-      for (int t = 0; t < HB_B; ++t) {
-        if (t < nb) {
-          vo[t] = from_c<TO, TC>(sub_rn(v[t], mul_rn(s_r[t * c0 + j], q)));
+    for (int u = 0; u < U; ++u) {
+      const int j = j0 + u;
+      if (j < c0 && s_sel[j]) {
+        const TC qc = to_c<TC, TO>(q[u]);
+#pragma unroll
+        for (int t = 0; t < HB_CG; ++t) {
+          vo[t] = from_c<TO, TC>(elim<FAST>(v[t], s_r[t * c0 + j], qc));
           v[t] = to_c<TC, TO>(vo[t]);
         }
       }
     }
-#pragma unroll
-    for (int t = 0; t < HB_B; ++t)
-      if (t < nb) Q[row + (int64_t)(c0 + t) * ldq] = vo[t];
   }
+#pragma unroll
+  for (int t = 0; t < HB_CG; ++t)
+    if (t < nl) Q[row + (int64_t)(t0 + t) * ldq] = vo[t];
 }
 
 // ---- step 2: the block's columns on one cluster ---------------------------------------------------
-template <class TO, class TC>
-__global__ void __cluster_dims__(HB_CL, 1, 1) __launch_bounds__(HB_T)
-    k_hess_inblock(int64_t m, int n, int c0, int c1, TO* __restrict__ Q, int64_t ldq, int* __restrict__ select,
-                   int* __restrict__ perm, TO* __restrict__ pivrows, TO* __restrict__ pvals, double* __restrict__ R,
-                   double select_tol, int64_t rows_per_cta) {
+template <class TO>
+struct HbCand {
+  long long key;  // argmax key of the local max |value| (-1: the CTA has no rows)
+  long long i;    // its row
+  TO vals[HB_B];  // the block's values in that row
+};
+
+template <class TO, class TC, bool FAST>
+__global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0, int c1, TO* __restrict__ Q,
+                                                       int64_t ldq, int* __restrict__ select, int* __restrict__ perm,
+                                                       double* __restrict__ R, double select_tol,
+                                                       int64_t rows_per_cta) {
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
+  const int ncl = (int)cluster.num_blocks();
   const int nb = c1 - c0;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31;
   const int64_t RR = rows_per_cta;
   const int64_t r0 = (int64_t)rank * RR;
   const int64_t r1 = (r0 + RR < m) ? r0 + RR : m;
+  const int nloc = (r1 > r0) ? (int)(r1 - r0) : 0;
   extern __shared__ unsigned char smem_raw[];
-  TO* s_blk = reinterpret_cast<TO*>(smem_raw);             // HB_B columns x RR rows (column t at t * RR)
-  TO* s_prow = s_blk + (size_t)HB_B * RR;                  // HB_B x HB_B: pivot row of block column t'
-  __shared__ ArgMax s_part;
-  __shared__ ArgMax red[32];
+  TO* s_blk = reinterpret_cast<TO*>(smem_raw);  // HB_B columns x RR rows (column t at t * RR)
+  __shared__ TO s_prow[HB_B * HB_B];            // pivot row of block column t at t * HB_B
+  __shared__ HbCand<TO> s_cand[2];              // double-buffered by column parity
+  __shared__ ArgMaxK red[HB_T / 32];
   __shared__ TC s_r[HB_B];
   __shared__ TO s_x[HB_B];
   __shared__ int s_sel[HB_B];
-  __shared__ int64_t s_k;
-  __shared__ int s_keep;
+  __shared__ long long s_k;
 
-  for (int64_t row = r0 + tid; row < r1; row += blockDim.x)
-    for (int t = 0; t < nb; ++t) s_blk[(size_t)t * RR + (row - r0)] = Q[row + (int64_t)(c0 + t) * ldq];
+  for (int lr = tid; lr < nloc; lr += HB_T) {
+    TO v[HB_B];
+#pragma unroll
+    for (int t = 0; t < HB_B; ++t) v[t] = (t < nb) ? Q[r0 + lr + (int64_t)(c0 + t) * ldq] : TO(0);
+#pragma unroll
+    for (int t = 0; t < HB_B; ++t) s_blk[(size_t)t * RR + lr] = v[t];
+  }
   __syncthreads();
   const double tol_o = to_c<double, TO>(from_c<TO, double>(select_tol));
 
@@ -149,146 +199,224 @@ __global__ void __cluster_dims__(HB_CL, 1, 1) __launch_bounds__(HB_T)
         const TC rc = to_c<TC, TO>(s_x[tp]);
         for (int tq = tp + 1 + tid; tq < t; tq += 32) {
           if (s_sel[tq])
-            s_x[tq] = from_c<TO, TC>(sub_rn(to_c<TC, TO>(s_x[tq]), mul_rn(rc, to_c<TC, TO>(s_prow[tq * HB_B + tp]))));
+            s_x[tq] = from_c<TO, TC>(elim<FAST>(to_c<TC, TO>(s_x[tq]), rc, to_c<TC, TO>(s_prow[tq * HB_B + tp])));
         }
         if (tid == 0) s_r[tp] = rc;
       }
     }
     __syncthreads();
     // (2) eliminations of this CTA's rows against the in-block columns t' < t (MGS order continues
-    //     after the j < c0 eliminations of step 1), local argmax
-    ArgMax a{-1.0, 0x7fffffffffffffffLL};
-    for (int64_t row = r0 + tid; row < r1; row += blockDim.x) {
-      const int64_t lr = row - r0;
-      TO vo = s_blk[(size_t)t * RR + lr];
-      TC v = to_c<TC, TO>(vo);
+    //     after the j < c0 eliminations of step 1), four independent rows per thread; local argmax
+    ArgMaxK a{-1, 0x7fffffffffffffffLL};
+    TO* col = s_blk + (size_t)t * RR;
+    for (int lr0 = tid; lr0 < nloc; lr0 += 4 * HB_T) {
+      TO vo[4];
+      TC v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int lr = lr0 + u * HB_T;
+        vo[u] = (lr < nloc) ? col[lr] : TO(0);
+        v[u] = to_c<TC, TO>(vo[u]);
+      }
       for (int tp = 0; tp < t; ++tp) {
         if (!s_sel[tp]) continue;
-        vo = from_c<TO, TC>(sub_rn(v, mul_rn(s_r[tp], to_c<TC, TO>(s_blk[(size_t)tp * RR + lr]))));
-        v = to_c<TC, TO>(vo);
+        const TC rc = s_r[tp];
+        const TO* ctp = s_blk + (size_t)tp * RR;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int lr = lr0 + u * HB_T;
+          const TC q = to_c<TC, TO>((lr < nloc) ? ctp[lr] : TO(0));
+          vo[u] = from_c<TO, TC>(elim<FAST>(v[u], rc, q));
+          v[u] = to_c<TC, TO>(vo[u]);
+        }
       }
-      s_blk[(size_t)t * RR + lr] = vo;
-      const double av = absd(vo);
-      if (av > a.v) a = ArgMax{av, row};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int lr = lr0 + u * HB_T;
+        if (lr < nloc) {
+          col[lr] = vo[u];
+          const long long key = amax_key(vo[u]);
+          if (key > a.key) a = ArgMaxK{key, r0 + lr};
+        }
+      }
     }
-    ArgMax r = block_argmax(a, red);
-    if (tid == 0) s_part = r;
-    // (3) cluster-wide argmax through distributed shared memory
+    const ArgMaxK loc = block_argmaxk(a, red);
+    // (3) publish this CTA's candidate, one cluster barrier, pick the winner from all candidates
+    HbCand<TO>& cand = s_cand[t & 1];
+    if (tid == 0) {
+      cand.key = loc.key;
+      cand.i = loc.i;
+    }
+    if (tid < HB_B) cand.vals[tid] = (loc.key >= 0 && tid < nb) ? s_blk[(size_t)tid * RR + (loc.i - r0)] : TO(0);
     cluster.sync();
-    if (tid == 0) {
-      ArgMax b{-1.0, 0x7fffffffffffffffLL};
-      for (int q = 0; q < HB_CL; ++q) {
-        const ArgMax* pq = cluster.map_shared_rank(&s_part, q);
-        ArgMax p;
-        p.v = pq->v;
-        p.i = pq->i;
-        b = argmax_pick(b, p);
+    if (tid < 32) {
+      ArgMaxK b{-1, 0x7fffffffffffffffLL};
+      if (lane < ncl) {
+        const HbCand<TO>* pq = cluster.map_shared_rank(&cand, lane);
+        b.key = pq->key;
+        b.i = pq->i;
       }
-      s_k = (b.v < 0.0) ? 0 : b.i;
+      b = warp_argmaxk(b);
+      const long long bk = __shfl_sync(0xffffffffu, b.key, 0);
+      const long long bi = __shfl_sync(0xffffffffu, b.i, 0);
+      const int owner = (bk < 0) ? 0 : (int)(bi / RR);
+      if (lane < HB_B) {
+        const HbCand<TO>* po = cluster.map_shared_rank(&cand, owner);
+        s_prow[t * HB_B + lane] = po->vals[lane];
+      }
+      if (lane == 0) s_k = (bk < 0) ? 0 : bi;
     }
     __syncthreads();
-    // (4) the pivot row of the block, read from the CTA that owns it
-    const int64_t k = s_k;
-    const int owner = (int)(k / RR);
-    if (tid < HB_B) {
-      const TO* ob = cluster.map_shared_rank(s_blk, owner);
-      s_prow[t * HB_B + tid] = (tid < nb) ? ob[(size_t)tid * RR + (k - (int64_t)owner * RR)] : TO(0);
-    }
-    __syncthreads();
+    const long long k = s_k;
     const TO pv = s_prow[t * HB_B + t];
-    const bool keep = absd(pv) >= tol_o && s_k >= 0;
-    if (tid == 0) {
-      s_keep = keep ? 1 : 0;
-      s_sel[t] = keep ? 1 : 0;
-    }
-    cluster.sync();  // every CTA has read the owner's row before anyone scales it
-    // (5) scale (or zero) this CTA's rows of column t
+    const bool keep = absd(pv) >= tol_o;
+    // (4) scale (or zero) this CTA's rows of column t
     const TC pc = to_c<TC, TO>(pv);
-    for (int64_t row = r0 + tid; row < r1; row += blockDim.x) {
-      const int64_t lr = row - r0;
-      const TO q = s_blk[(size_t)t * RR + lr];
-      s_blk[(size_t)t * RR + lr] = keep ? from_c<TO, TC>(div_rn(to_c<TC, TO>(q), pc)) : TO(0);
+    const TC y = pivot_recip(pc);
+    const bool pf = pivot_fast(pc);
+    for (int lr = tid; lr < nloc; lr += HB_T) {
+      const TC q = to_c<TC, TO>(col[lr]);
+      // FAST: x * RN(1/p) (within an ulp of x / p), the pivot itself exactly 1
+      const TC sq = (FAST && pf) ? ((r0 + lr == k) ? TC(1) : mul_recip(q, y)) : pivot_div(q, pc, y, pf);
+      col[lr] = keep ? from_c<TO, TC>(sq) : TO(0);
     }
-    // (6) bookkeeping (rank 0): pivot, selection, R(:, i), pivot row of Q for later blocks
+    if (tid == 0) s_sel[t] = keep ? 1 : 0;
+    // (5) bookkeeping (rank 0): pivot, selection, R(:, i)
     if (rank == 0) {
       const int i = c0 + t;
       if (tid == 0) {
         select[i] = keep ? 1 : 0;
         perm[i] = keep ? (int)k : -1;
-        pvals[i] = keep ? pv : TO(0);
         R[i + (int64_t)i * n] = to_c<double, TO>(pv);
       }
       for (int tp = tid; tp < t; tp += blockDim.x)
         R[(c0 + tp) + (int64_t)i * n] = s_sel[tp] ? to_c<double, TC>(s_r[tp]) : 0.0;
-      if (keep) {
-        for (int l = tid; l < i; l += blockDim.x)
-          pivrows[(int64_t)i * n + l] = (l < c0) ? Q[k + (int64_t)l * ldq] : s_prow[t * HB_B + (l - c0)];
-      }
     }
     __syncthreads();
   }
-  for (int64_t row = r0 + tid; row < r1; row += blockDim.x)
-    for (int t = 0; t < nb; ++t) Q[row + (int64_t)(c0 + t) * ldq] = s_blk[(size_t)t * RR + (row - r0)];
-  cluster.sync();  // no CTA leaves while another may still read its shared memory
+  for (int lr = tid; lr < nloc; lr += HB_T) {
+#pragma unroll
+    for (int t = 0; t < HB_B; ++t)
+      if (t < nb) Q[r0 + lr + (int64_t)(c0 + t) * ldq] = s_blk[(size_t)t * RR + lr];
+  }
+  cluster.sync();  // no CTA leaves while another may still read its candidates
 }
 
-// shared memory the in-block kernel needs for m rows (0 if it does not fit)
-size_t hess_blocked_smem(int64_t m, size_t es) {
-  const int64_t RR = (m + HB_CL - 1) / HB_CL;
-  const size_t bytes = (size_t)HB_B * RR * es + (size_t)HB_B * HB_B * es + 64;
+// shared memory the in-block kernel needs for m rows on ncl CTAs (0 if it does not fit)
+size_t hess_blocked_smem(int64_t m, size_t es, int ncl) {
+  const int64_t RR = (m + ncl - 1) / ncl;
+  const size_t bytes = (size_t)HB_B * RR * es;
   return bytes <= HB_SMEM_MAX ? bytes : 0;
 }
 
-template <class TO, class TC>
+// Cluster size for the in-block kernel: 16 CTAs (non-portable) when the device can co-schedule
+// them with this much shared memory and every CTA gets at least 64 rows, else the portable 8.
+template <class TO, class TC, bool FAST>
+static int inblock_cluster(int64_t m, size_t smem16) {
+  static std::atomic<long long> cache{-1};  // (smem << 8) | ncl of the last query
+  if (m < 16 * 64 || !smem16) return 8;
+  const char* env = getenv("OFRR_HESS_CLUSTER");
+  if (env && atoi(env) == 8) return 8;
+  const long long c = cache.load(std::memory_order_relaxed);
+  if (c >= 0 && (size_t)(c >> 8) == smem16) return (int)(c & 0xff);
+  int ncl = 8;
+  if (cudaFuncSetAttribute(k_hess_inblock<TO, TC, FAST>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+          cudaSuccess &&
+      cudaFuncSetAttribute(k_hess_inblock<TO, TC, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem16) ==
+          cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(HB_T);
+    cfg.dynamicSmemBytes = smem16;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_hess_inblock<TO, TC, FAST>, &cfg) == cudaSuccess && nclusters >= 1)
+      ncl = 16;
+  }
+  (void)cudaGetLastError();  // a refused query leaves the portable size
+  cache.store(((long long)smem16 << 8) | ncl, std::memory_order_relaxed);
+  return ncl;
+}
+
+template <class TO, class TC, bool FAST>
 int hess_run_blocked_t(ofrr_ctx* ctx, int64_t m, int n, TO* Q, int64_t ldq, double select_tol, double* R, int* select,
-                       int* perm) {
+                       int* perm, bool* done) {
+  const size_t smem16 = hess_blocked_smem(m, sizeof(TO), 16);
+  if (!smem16) return OFRR_SUCCESS;
+  const int ncl = inblock_cluster<TO, TC, FAST>(m, smem16);
+  const size_t smem2 = hess_blocked_smem(m, sizeof(TO), ncl);
+  if (!smem2) return OFRR_SUCCESS;  // needs 16 CTAs, and the device cannot co-schedule them
+  *done = true;
   int st = OFRR_SUCCESS;
   WsScope scope(ctx);
-  TO* pivrows = ws_get<TO>(ctx, (size_t)n * n, &st);
-  if (!pivrows) return st;
-  TO* pvals = ws_get<TO>(ctx, (size_t)n, &st);
-  if (!pvals) return st;
+  TC* rcoef = ws_get<TC>(ctx, (size_t)HB_B * n, &st);
+  if (!rcoef) return st;
   OFRR_TRY(fill_zero(ctx, R, sizeof(double) * (size_t)n * n));
-  OFRR_TRY(fill_zero(ctx, pivrows, sizeof(TO) * (size_t)n * n));
-  const int64_t RR = (m + HB_CL - 1) / HB_CL;
-  const size_t smem2 = hess_blocked_smem(m, sizeof(TO));
-  if (!smem2) return OFRR_ERR_BLAS_INVALID_SIZE;
-  OFRR_CUDA(cudaFuncSetAttribute(k_hess_inblock<TO, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
-  const int grid1 = grid_for(m, HB_T, 152 * 2);
+  const int64_t RR = (m + ncl - 1) / ncl;
+  if (ncl > 8)
+    OFRR_CUDA(cudaFuncSetAttribute(k_hess_inblock<TO, TC, FAST>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  OFRR_CUDA(cudaFuncSetAttribute(k_hess_inblock<TO, TC, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = ncl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ncl);
+  cfg.blockDim = dim3(HB_T);
+  cfg.dynamicSmemBytes = smem2;
+  cfg.stream = ctx->stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   for (int c0 = 0; c0 < n; c0 += HB_B) {
     const int c1 = (c0 + HB_B < n) ? c0 + HB_B : n;
+    const int nb = c1 - c0;
     if (c0 > 0) {
-      const size_t smem1 = (size_t)HB_B * c0 * (sizeof(TC) + sizeof(TO)) + 32 + (size_t)c0 * c0 * sizeof(TO) +
-                           (size_t)c0 * sizeof(int);
-      if (smem1 > 48 * 1024)
-        OFRR_CUDA(cudaFuncSetAttribute(k_hess_blockupd<TO, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem1));
-      k_hess_blockupd<TO, TC><<<grid1, HB_T, smem1, ctx->stream>>>(m, n, c0, c1, Q, ldq, select, perm, pivrows, R);
+      const size_t smem0 = (size_t)c0 * c0 * sizeof(TO) + (size_t)HB_B * c0 * sizeof(TO) + 16 + 2 * (size_t)c0 * 4;
+      if (smem0 > 48 * 1024)
+        OFRR_CUDA(cudaFuncSetAttribute(k_hess_blockcoef<TO, TC, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem0));
+      k_hess_blockcoef<TO, TC, FAST><<<1, HB_B * 32, smem0, ctx->stream>>>(n, c0, c1, Q, ldq, select, perm, rcoef, R);
+      OFRR_LAUNCHED(ctx, "k_hess_blockcoef");
+      const size_t smem1 = (size_t)HB_CG * c0 * sizeof(TC) + (size_t)c0 * sizeof(int);
+      const dim3 grid1((unsigned)((m + HB_UT - 1) / HB_UT), (unsigned)((nb + HB_CG - 1) / HB_CG));
+      k_hess_blockupd<TO, TC, FAST><<<grid1, HB_UT, smem1, ctx->stream>>>(m, c0, c1, Q, ldq, select, rcoef);
       OFRR_LAUNCHED(ctx, "k_hess_blockupd");
     }
-    k_hess_inblock<TO, TC><<<HB_CL, HB_T, smem2, ctx->stream>>>(m, n, c0, c1, Q, ldq, select, perm, pivrows, pvals, R,
-                                                               select_tol, RR);
+    OFRR_CUDA(cudaLaunchKernelEx(&cfg, k_hess_inblock<TO, TC, FAST>, m, n, c0, c1, Q, ldq, select, perm, R, select_tol,
+                                 RR));
     OFRR_LAUNCHED(ctx, "k_hess_inblock");
   }
   return OFRR_SUCCESS;
 }
 
 // Blocked build when it fits (m rows of the block in the cluster's shared memory, n <= 256);
-// *done = false leaves the call to the per-column path.
+// *done = false leaves the call to the per-column path.  fast selects the FMA / reciprocal arithmetic
+// for an FP64 compute type (the production refinement phases); the exact arithmetic otherwise.
 int hess_run_blocked(ofrr_ctx* ctx, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n, void* Q, int64_t ldq,
-                     double select_tol, double* R, int* select, int* perm, bool* done) {
+                     double select_tol, double* R, int* select, int* perm, bool fast, bool* done) {
   *done = false;
-  if (n > 256 || m < 2 * HB_CL || getenv("OFRR_HESS_PER_COLUMN")) return OFRR_SUCCESS;
-  if (!hess_blocked_smem(m, dtype_size(tout))) return OFRR_SUCCESS;
-  // step-1 shared memory at the last block: coefficients, working values and the c0 x c0 pivot block
+  if (n > 256 || m < 2 * 8 || getenv("OFRR_HESS_PER_COLUMN")) return OFRR_SUCCESS;
+  // step-0 shared memory at the last block: the c0 x c0 pivot block and the block's pivot-row values
   const int64_t c0max = ((n - 1) / HB_B) * HB_B;
-  const size_t es = dtype_size(tout), ec = dtype_size(tc);
-  if ((size_t)HB_B * c0max * (es + ec) + 32 + (size_t)c0max * c0max * es + (size_t)c0max * 4 > HB_SMEM_MAX)
+  const size_t es = dtype_size(tout);
+  if ((size_t)c0max * c0max * es + (size_t)HB_B * c0max * es + 16 + 2 * (size_t)c0max * 4 > HB_SMEM_MAX)
     return OFRR_SUCCESS;
+  if (fast && tc == OFRR_F64) {
+    OFRR_DISPATCH_STORAGE(tout, TO, {
+      OFRR_TRY((hess_run_blocked_t<TO, double, true>(ctx, m, (int)n, (TO*)Q, ldq, select_tol, R, select, perm, done)));
+    });
+    return OFRR_SUCCESS;
+  }
   OFRR_DISPATCH_STORAGE(tout, TO, OFRR_DISPATCH_COMPUTE(tc, TC, {
-    OFRR_TRY((hess_run_blocked_t<TO, TC>(ctx, m, (int)n, (TO*)Q, ldq, select_tol, R, select, perm)));
+    OFRR_TRY((hess_run_blocked_t<TO, TC, false>(ctx, m, (int)n, (TO*)Q, ldq, select_tol, R, select, perm, done)));
   }));
-  *done = true;
   return OFRR_SUCCESS;
 }
 

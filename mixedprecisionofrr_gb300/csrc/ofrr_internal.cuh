@@ -158,6 +158,33 @@ __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(
 __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
 
+// x / p, correctly rounded, for many x and one p (a pivot, a column maximum), given y = RN(1/p).  In FP64 (a 1/64-rate pipe on GB300) the
+// correctly rounded quotient comes from one multiply and four FMAs: q0 = RN(x y), one correction
+// q1 = RN(q0 + RN(x - p q0) y) makes q1 faithful, and by Markstein's theorem (P. Markstein, "Computation
+// of elementary functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34, 1990) the
+// second correction RN(q1 + (x - p q1) y), with x - p q1 exact, is RN(x / p).  Operands outside
+// [2^-900, 2^900] (where an intermediate could underflow or overflow) use the division itself.
+__device__ __forceinline__ double pivot_recip(double p) { return __drcp_rn(p); }
+__device__ __forceinline__ float pivot_recip(float p) { return __frcp_rn(p); }
+__device__ __forceinline__ bool pivot_fast(double p) {
+  const double a = fabs(p);
+  return a >= 0x1p-450 && a <= 0x1p+450;
+}
+__device__ __forceinline__ bool pivot_fast(float) { return false; }
+__device__ __forceinline__ double pivot_div(double x, double p, double y, bool fast) {
+  const double ax = fabs(x);
+  if (fast && ax >= 0x1p-900 && ax <= 0x1p+900) {
+    const double q0 = __dmul_rn(x, y);
+    const double r0 = __fma_rn(-p, q0, x);
+    const double q1 = __fma_rn(r0, y, q0);
+    const double r1 = __fma_rn(-p, q1, x);
+    return __fma_rn(r1, y, q1);
+  }
+  return __ddiv_rn(x, p);
+}
+__device__ __forceinline__ float pivot_div(float x, float p, float, bool) { return __fdiv_rn(x, p); }
+
+
 // argmax reduction on (|value|, index): larger value wins, lower index on ties, NaN ignored
 struct ArgMax {
   double v;  // -1 means "empty"
@@ -191,6 +218,61 @@ __device__ __forceinline__ ArgMax block_argmax(ArgMax a, ArgMax* smem) {
   }
   __syncthreads();
   ArgMax r = smem[0];
+  __syncthreads();
+  return r;
+}
+
+// Integer argmax keys.  For IEEE formats the bit pattern of |x| orders like |x|, so max-|x| searches
+// run on the integer pipes instead of FP64 compares (GB300's FP64 pipe is 1/64 rate).  key = bits + 1
+// for numbers, 0 for NaN (never preferred over a number, as with floating compares), -1 = empty.
+__device__ __forceinline__ long long amax_key(double x) {
+  const long long b = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+  return (b > 0x7ff0000000000000LL) ? 0 : b + 1;
+}
+__device__ __forceinline__ long long amax_key(float x) {
+  const int b = __float_as_int(x) & 0x7fffffff;
+  return (b > 0x7f800000) ? 0 : (long long)b + 1;
+}
+__device__ __forceinline__ long long amax_key(__half x) {
+  const int b = __half_as_ushort(x) & 0x7fff;
+  return (b > 0x7c00) ? 0 : (long long)b + 1;
+}
+__device__ __forceinline__ long long amax_key(__nv_bfloat16 x) {
+  const int b = __bfloat16_as_ushort(x) & 0x7fff;
+  return (b > 0x7f80) ? 0 : (long long)b + 1;
+}
+struct ArgMaxK {
+  long long key;  // -1 means "empty"
+  long long i;
+};
+__device__ __forceinline__ ArgMaxK argmaxk_pick(ArgMaxK a, ArgMaxK b) {
+  if (b.key > a.key || (b.key == a.key && b.i < a.i && b.key >= 0)) return b;
+  return a;
+}
+__device__ __forceinline__ ArgMaxK warp_argmaxk(ArgMaxK a) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    ArgMaxK b;
+    b.key = __shfl_down_sync(0xffffffffu, a.key, off);
+    b.i = __shfl_down_sync(0xffffffffu, a.i, off);
+    a = argmaxk_pick(a, b);
+  }
+  return a;
+}
+// block-wide argmax, result returned to every thread.  smem needs blockDim/32 entries.
+__device__ __forceinline__ ArgMaxK block_argmaxk(ArgMaxK a, ArgMaxK* smem) {
+  a = warp_argmaxk(a);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) smem[wid] = a;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  if (wid == 0) {
+    ArgMaxK b = (lane < nw) ? smem[lane] : ArgMaxK{-1, 0x7fffffffffffffffLL};
+    b = warp_argmaxk(b);
+    if (lane == 0) smem[0] = b;
+  }
+  __syncthreads();
+  ArgMaxK r = smem[0];
   __syncthreads();
   return r;
 }
@@ -230,15 +312,19 @@ int cast_transpose_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, int64_t 
                         int64_t ldin, void* out, int64_t ldout);
 int cast_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, int64_t m, int64_t n, const void* in,
               int64_t ldin, void* out, int64_t ldout);
+// fast = multiply by the reciprocal of the column's maximum (within an ulp of the quotient) for an
+// FP64 compute type; fast = false keeps scalecols.m's correctly rounded division
 int scalecols_impl(ofrr_ctx* ctx, ofrr_dtype po, ofrr_dtype pc, int64_t m, int64_t n, void* U, int64_t ldu,
-                   int* piv);
+                   int* piv, bool fast = false);
 int fill_zero(ofrr_ctx* ctx, void* p, size_t bytes);
 
 // Hessenberg basis on device: Q (m x n, tout) from A; outputs on device:
 // R (n x n FP64, col-major), select (n ints, 1 = kept), perm (n ints, -1 if dropped)
+// fast = FMA eliminations and reciprocal pivot scaling for an FP64 compute type (production
+// refinement phases; not bit-identical to hessenberg.m's arithmetic, which fast = false keeps)
 int hessenberg_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n,
                     const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev,
-                    int* select_dev, int* perm_dev);
+                    int* select_dev, int* perm_dev, bool fast = false);
 // MGS basis (orthogonal comparison path, MATLAB/+src/+qr/mgs.m)
 int mgs_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n,
              const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev,

@@ -12,14 +12,12 @@
 // would show), and the exact FP32 partials are combined and scaled in FP64.  Dropped terms
 // (s + t > LMAX) and the digit truncation are below 2^-(BETA (LMAX+1)) relative.
 #include "ofrr_internal.cuh"
+#include "tcgen05.cuh"
 
 #include <algorithm>
 #include <vector>
 
 namespace ofrr {
-
-int tc_gemm_partials(ofrr_ctx* ctx, ofrr_dtype t16, int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
-                     const void* B, int64_t ldb, int kblocks_per_split, float* partial, int* splits_out);
 
 namespace slice {
 constexpr int BETA = 7;  // digit width: |leading digit| <= 128, later digits <= 64
@@ -28,81 +26,276 @@ constexpr int LMAX = 4;  // levels kept: pairs with s + t <= 4 (15 of 25), error
 
 // Digits of every column of X (K x N, column-major).  Stacked layout: column n occupies
 // stack[(n * S + s) * Kp + k] for digit s; rows k >= K are zero.  expo[n] = exponent e_n.
-__global__ void k_slice_cols(int64_t K, int64_t Kp, int64_t N, const double* __restrict__ X, int64_t ldx,
-                             __nv_bfloat16* __restrict__ stack, int* __restrict__ expo) {
-  __shared__ double red[32];
+// Integer pipes only (GB300's FP64 pipe is 1/64 rate): the column maximum is taken on the bit
+// patterns of |x|, e_n = frexp exponent of that maximum, and round(x 2^(BETA S - e_n)) is formed from
+// the significand by a right shift with round-half-even (the same value __double2ll_rn gives).
+constexpr int SLICE_T = 512;
+__global__ void __launch_bounds__(SLICE_T) k_slice_cols(int64_t K, int64_t Kp, int64_t N, const double* __restrict__ X,
+                                                        int64_t ldx, __nv_bfloat16* __restrict__ stack,
+                                                        int* __restrict__ expo) {
+  __shared__ unsigned long long red[SLICE_T / 32];
   __shared__ int s_e;
+  constexpr int U = 8;  // loads in flight per thread
   for (int64_t n = blockIdx.x; n < N; n += gridDim.x) {
     const double* x = X + n * ldx;
-    double mx = 0.0;
-    for (int64_t k = threadIdx.x; k < K; k += blockDim.x) mx = fmax(mx, fabs(x[k]));
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    unsigned long long mx = 0;
+    for (int64_t k0 = threadIdx.x; k0 < K; k0 += (int64_t)U * SLICE_T) {
+      unsigned long long v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t k = k0 + (int64_t)u * SLICE_T;
+        v[u] = (k < K) ? (unsigned long long)__double_as_longlong(x[k]) : 0ull;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) mx = max(mx, v[u] & 0x7fffffffffffffffull);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
     __syncthreads();
     if (threadIdx.x == 0) {
-      double m = 0.0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+      unsigned long long m = 0;
+      for (int w = 0; w < SLICE_T / 32; ++w) m = max(m, red[w]);
+      // frexp exponent: m = f 2^e, f in [0.5, 1), so |x| 2^-e < 1 for the whole column
+      const int be = (int)(m >> 52);
       int e = 0;
-      if (m > 0.0) frexp(m, &e);  // m = f 2^e, f in [0.5, 1): |x| 2^-e < 1
+      if (m != 0) e = (be > 0) ? be - 1022 : (64 - __clzll((long long)m)) - 1074;
       s_e = e;
       expo[n] = e;
     }
     __syncthreads();
     const int e = s_e;
-    // fixed point: Y = round(x 2^(BETA S - e)), |Y| <= 2^35; digits by integer arithmetic (GB300's
-    // FP64 pipe is 1/64 rate, so only one FP64 multiply and one conversion per element)
     __nv_bfloat16* col = stack + (size_t)n * S * Kp;
-    for (int64_t k = threadIdx.x; k < Kp; k += blockDim.x) {
-      long long r = (k < K) ? __double2ll_rn(ldexp(x[k], BETA * S - e)) : 0ll;
+    for (int64_t k0 = threadIdx.x; k0 < Kp; k0 += (int64_t)U * SLICE_T) {
+      unsigned long long v[U];
 #pragma unroll
-      for (int s = S - 1; s > 0; --s) {  // centred base-2^BETA digits, least significant first
-        const long long d = ((r + (1 << (BETA - 1))) & ((1 << BETA) - 1)) - (1 << (BETA - 1));
-        r = (r - d) >> BETA;  // exact: r - d is a multiple of 2^BETA
-        col[(size_t)s * Kp + k] = __float2bfloat16_rn((float)d);  // |d| <= 64
+      for (int u = 0; u < U; ++u) {
+        const int64_t k = k0 + (int64_t)u * SLICE_T;
+        v[u] = (k < K) ? (unsigned long long)__double_as_longlong(x[k]) : 0ull;
       }
-      col[k] = __float2bfloat16_rn((float)r);  // leading digit, |r| <= 128: exact in bf16
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t k = k0 + (int64_t)u * SLICE_T;
+        if (k >= Kp) break;
+        // x = M 2^(be' - 1075) with M the significand (implicit bit for normal numbers, be' = max(be, 1))
+        const unsigned long long bits = v[u];
+        const int be = (int)((bits >> 52) & 0x7ff);
+        const unsigned long long M = (bits & 0x000fffffffffffffull) | (be > 0 ? (1ull << 52) : 0ull);
+        const int sh = 1075 - (BETA * S) + e - (be > 0 ? be : 1);  // 18 or more unless the maximum is subnormal
+        long long r = 0;
+        if (sh <= 53 && M != 0) {
+          unsigned long long q;
+          if (sh <= 0) {
+            q = M << (-sh);  // subnormal column maximum: exact scaling up
+          } else {
+            q = M >> sh;
+            const unsigned long long rem = M & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+            if (rem > half || (rem == half && (q & 1ull))) ++q;
+          }
+          r = (bits >> 63) ? -(long long)q : (long long)q;
+        }
+#pragma unroll
+        for (int s = S - 1; s > 0; --s) {  // centred base-2^BETA digits, least significant first
+          const long long d = ((r + (1 << (BETA - 1))) & ((1 << BETA) - 1)) - (1 << (BETA - 1));
+          r = (r - d) >> BETA;  // exact: r - d is a multiple of 2^BETA
+          col[(size_t)s * Kp + k] = __float2bfloat16_rn((float)d);  // |d| <= 64
+        }
+        col[k] = __float2bfloat16_rn((float)r);  // leading digit, |r| <= 128: exact in bf16
+      }
     }
     __syncthreads();
   }
 }
 
-// Level stacks of the second operand: for level L, column n holds [d_L; d_{L-1}; ...; d_0]
-// (length (L+1) Kp), built from the digit stack of k_slice_cols.  Level L starts at offset
-// off(L) = N Kp L (L+1) / 2.
-__global__ void k_level_stacks(int64_t Kp, int64_t N, const __nv_bfloat16* __restrict__ digits,
-                               __nv_bfloat16* __restrict__ levels) {
-  const int64_t per = (int64_t)N * Kp;
-  const int64_t total = per * (LMAX + 1) * (LMAX + 2) / 2;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    // locate level L and the position p inside column n
-    int L = 0;
-    int64_t base = 0;
-    while (L < LMAX && e >= base + per * (L + 1)) {
-      base += per * (L + 1);
-      ++L;
+// Fused exact-slice product.  One CTA owns a 128 x SBN tile of C and a range of at most 16 k-blocks
+// (1024 entries of K, so that the level-0 and level-1 FP32 sums are exact).  Per k-block the B digits
+// d'_0..d'_4 (5 tiles) are loaded once into a B slot, and the A digits d_0..d_4 stream through an
+// A ring one tile at a time; for A digit s the MMA warp issues the pairs (s, t), t <= LMAX - s,
+// into the TMEM accumulator of level L = s + t (5 accumulators of SBN columns).  A is therefore read
+// once per product (not once per level).  The epilogue converts each level to an integer, combines
+// acc = sum_L S_L 2^(BETA (LMAX - L)) exactly in 64 bits and writes it (one split) as
+// C = 2^(ea + eb - BETA (LMAX + 2)) acc, or as an int64 partial for k_sliced_finish.
+constexpr int SBN = 64;
+constexpr int SL_ATILE = tc::BM * tc::BK * 2;  // 16 KB: one digit of a 128-row k-block
+constexpr int SL_BTILE = SBN * tc::BK * 2;     // 8 KB
+constexpr int SL_ASLOTS = 6;
+constexpr int SL_BSLOTS = 2;
+constexpr int SL_THREADS = 192;
+constexpr int SL_KB_MAX = 16;
+constexpr int SL_SHIFT = BETA * (LMAX + 2);
+constexpr size_t SL_SMEM = (size_t)SL_ASLOTS * SL_ATILE + (size_t)SL_BSLOTS * S * SL_BTILE + 1024 + 256;
+constexpr uint32_t SL_TMEM_COLS = 512;  // LMAX + 1 accumulators of SBN columns, rounded to a power of two
+static_assert((LMAX + 1) * SBN <= (int)SL_TMEM_COLS, "TMEM columns");
+
+__global__ void __launch_bounds__(SL_THREADS, 1)
+    k_sliced_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N,
+                int64_t Kp, int kb_total, int kb_per_split, uint32_t idesc, long long* __restrict__ partial,
+                double* __restrict__ C, int64_t ldc, const int* __restrict__ ea, const int* __restrict__ eb,
+                int* __restrict__ err) {
+  using namespace tc;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* sA = base;
+  uint8_t* sB = base + SL_ASLOTS * SL_ATILE;
+  uint64_t* bars = (uint64_t*)(sB + SL_BSLOTS * S * SL_BTILE);
+  uint64_t* a_full = bars;
+  uint64_t* a_empty = bars + SL_ASLOTS;
+  uint64_t* b_full = bars + 2 * SL_ASLOTS;
+  uint64_t* b_empty = b_full + SL_BSLOTS;
+  uint64_t* accum = b_empty + SL_BSLOTS;
+  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * SBN;
+  const int kb0 = blockIdx.z * kb_per_split;
+  const int kb1 = min(kb0 + kb_per_split, kb_total);
+  const int nkb = max(kb1 - kb0, 0);
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < SL_ASLOTS; ++i) {
+      mbar_init(&a_full[i], 1);
+      mbar_init(&a_empty[i], 1);
     }
-    const int64_t r = e - base;
-    const int64_t len = (int64_t)(L + 1) * Kp;
-    const int64_t n = r / len, q = r % len;
-    const int p = (int)(q / Kp);
-    const int64_t k = q % Kp;
-    const int s = L - p;
-    levels[e] = digits[((size_t)n * S + s) * Kp + k];
+    for (int i = 0; i < SL_BSLOTS; ++i) {
+      mbar_init(&b_full[i], 1);
+      mbar_init(&b_empty[i], 1);
+    }
+    mbar_init(accum, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(SL_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+      int a_issued = 0, b_issued = 0;
+      bool ok = true;
+      for (int i = 0; i < nkb && ok; ++i) {
+        const int bs = i % SL_BSLOTS;
+        if (i >= SL_BSLOTS && !mbar_wait(&b_empty[bs], ((i / SL_BSLOTS) + 1) & 1, err, 21)) break;
+        const int kx = (kb0 + i) * BK;
+        mbar_expect_tx(&b_full[bs], S * SL_BTILE);
+        for (int t = 0; t < S; ++t)
+          tma_load_2d(&tmB, &b_full[bs], sB + (bs * S + t) * SL_BTILE, (int)(t * Kp) + kx, n0);
+        b_issued = i + 1;
+        for (int s = 0; s < S; ++s) {
+          const int as = a_issued % SL_ASLOTS;
+          if (a_issued >= SL_ASLOTS && !mbar_wait(&a_empty[as], ((a_issued / SL_ASLOTS) + 1) & 1, err, 22)) {
+            ok = false;
+            break;
+          }
+          mbar_expect_tx(&a_full[as], SL_ATILE);
+          tma_load_2d(&tmA, &a_full[as], sA + as * SL_ATILE, (int)(s * Kp) + kx, m0);
+          ++a_issued;
+        }
+      }
+      // drain: every issued copy must have landed before the CTA may exit
+      for (int j = max(0, a_issued - SL_ASLOTS); j < a_issued; ++j)
+        mbar_wait(&a_full[j % SL_ASLOTS], (j / SL_ASLOTS) & 1, err, 23);
+      for (int j = max(0, b_issued - SL_BSLOTS); j < b_issued; ++j)
+        mbar_wait(&b_full[j % SL_BSLOTS], (j / SL_BSLOTS) & 1, err, 24);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int a_used = 0;
+      bool ok = true;
+      for (int i = 0; i < nkb && ok; ++i) {
+        const int bs = i % SL_BSLOTS;
+        if (!mbar_wait(&b_full[bs], (i / SL_BSLOTS) & 1, err, 25)) break;
+        fence_after();
+        for (int s = 0; s < S; ++s) {
+          const int as = a_used % SL_ASLOTS;
+          if (!mbar_wait(&a_full[as], (a_used / SL_ASLOTS) & 1, err, 26)) {
+            ok = false;
+            break;
+          }
+          fence_after();
+          const uint32_t a0 = smem_u32(sA + as * SL_ATILE);
+          for (int t = 0; t + s <= LMAX; ++t) {
+            const uint32_t b0 = smem_u32(sB + (bs * S + t) * SL_BTILE);
+            const uint32_t d = tmem + (uint32_t)((s + t) * SBN);
+#pragma unroll
+            for (int k = 0; k < BK / 16; ++k)
+              umma_f16(d, desc_sw128(a0 + 32 * k), desc_sw128(b0 + 32 * k), idesc,
+                       (i > 0 || s > 0 || k > 0) ? 1u : 0u);
+          }
+          umma_commit(&a_empty[as]);
+          ++a_used;
+        }
+        umma_commit(&b_empty[bs]);
+      }
+      umma_commit(accum);
+    }
+    __syncwarp();
+  } else {
+    // epilogue warps 2..5 -> TMEM lane quarter (warp % 4)
+    const int q = warp & 3;
+    const bool ok = mbar_wait(accum, 0, err, 27);
+    fence_after();
+    const int row = m0 + 32 * q + lane;
+    const int erow = (row < M) ? ea[row] : 0;
+#pragma unroll 1
+    for (int c = 0; c < SBN; c += 16) {
+      long long acc[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) acc[j] = 0;
+#pragma unroll 1
+      for (int L = 0; L <= LMAX; ++L) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(L * SBN + c), v);
+        const long long w = 1ll << (BETA * (LMAX - L));
+#pragma unroll
+        for (int j = 0; j < 16; ++j) acc[j] += (long long)__float2ll_rn(v[j]) * w;
+      }
+      if (!ok || nkb == 0) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) acc[j] = 0;
+      }
+      if (row < M) {
+        if (partial != nullptr) {
+          long long* P = partial + (size_t)blockIdx.z * (size_t)M * N;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = n0 + c + j;
+            if (n < N) P[row + (size_t)n * M] = acc[j];
+          }
+        } else {
+#pragma unroll 4
+          for (int j = 0; j < 16; ++j) {
+            const int n = n0 + c + j;
+            if (n < N) C[row + (size_t)n * ldc] = ldexp((double)acc[j], erow + eb[n] - SL_SHIFT);
+          }
+        }
+      }
+    }
+    fence_before();
+  }
+  __syncthreads();
+  if (warp == 1) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(SL_TMEM_COLS) : "memory");
   }
 }
 
-// C (+)= 2^{ea_m + eb_n - shift} * sum_z P_z   (FP64)
-__global__ void k_combine(int64_t M, int64_t N, int splits, const float* __restrict__ P, double* __restrict__ C,
-                          int64_t ldc, const int* __restrict__ ea, const int* __restrict__ eb, int shift, int first) {
+// C = 2^(ea + eb - BETA (LMAX + 2)) * sum_z P_z  (64-bit integer partials, exact in any order)
+__global__ void k_sliced_finish(int64_t M, int64_t N, int splits, const long long* __restrict__ P,
+                                double* __restrict__ C, int64_t ldc, const int* __restrict__ ea,
+                                const int* __restrict__ eb) {
   const int64_t total = M * N;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    // partials are integer-valued (digit products) below 2^31 in magnitude: sum them exactly as integers
     long long s = 0;
-    for (int z = 0; z < splits; ++z) s += (long long)__float2ll_rn(P[(size_t)z * total + e]);
+    for (int z = 0; z < splits; ++z) s += P[(size_t)z * total + e];
     const int64_t m = e % M, n = e / M;
-    const double v = ldexp((double)s, ea[m] + eb[n] - shift);
-    double* c = C + m + n * ldc;
-    *c = first ? v : (*c + v);
+    C[m + n * ldc] = ldexp((double)s, ea[m] + eb[n] - SL_SHIFT);
   }
 }
 
@@ -119,7 +312,7 @@ int sliced_prepare_into(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, in
   out->stack = stack;
   out->expo = expo;
   const int grid = (int)std::min<int64_t>(M, 65535);
-  slice::k_slice_cols<<<grid, 256, 0, ctx->stream>>>(K, out->Kp, M, X, ldx, out->stack, out->expo);
+  slice::k_slice_cols<<<grid, slice::SLICE_T, 0, ctx->stream>>>(K, out->Kp, M, X, ldx, out->stack, out->expo);
   OFRR_LAUNCHED(ctx, "k_slice_cols");
   return OFRR_SUCCESS;
 }
@@ -140,39 +333,40 @@ int sliced_gemm_tn(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const doubl
                    int64_t ldc) {
   using namespace slice;
   const int64_t K = A.K, Kp = A.Kp, M = A.M;
+  // the combined 64-bit integer is bounded by K 2^(2 BETA + BETA LMAX) (1 + 2^-6): K <= 2^20 keeps it below 2^63
+  if (K > (1ll << 20) || M > (1ll << 30) || N > (1ll << 30)) return OFRR_ERR_BLAS_INVALID_SIZE;
   WsScope scope(ctx);
   int st = OFRR_SUCCESS;
   SlicedOperand Bs;
   OFRR_TRY(sliced_prepare(ctx, K, N, B, ldb, &Bs));
-  __nv_bfloat16* levels = ws_get<__nv_bfloat16>(ctx, (size_t)N * Kp * (LMAX + 1) * (LMAX + 2) / 2, &st);
-  if (!levels) return st;
-  slice::k_level_stacks<<<grid_for(N * Kp * 15, 256, 4096), 256, 0, ctx->stream>>>(Kp, N, Bs.stack, levels);
-  OFRR_LAUNCHED(ctx, "k_level_stacks");
-  // partial buffer: largest split count over the levels
-  const int64_t kb = Kp / 64;
-  const int tiles = (int)(((M + 127) / 128) * ((N + 63) / 64));
-  std::vector<int> kbps(LMAX + 1);
-  int max_splits = 1;
-  for (int L = 0; L <= LMAX; ++L) {
-    const int64_t kbl = kb * (L + 1);
-    // exact ranges on the two leading levels: |d_s d_t| <= 2^14 (L = 0), 2^13 (L = 1); 2^24 bound
-    int64_t lim = (L == 0) ? (1 << 10) / 64 : (L == 1 ? (1 << 11) / 64 : kbl);
-    int64_t per = std::min<int64_t>(lim, kbl);
-    // at least ~one wave of CTAs
-    while (tiles * ((kbl + per - 1) / per) < 148 && per > 2) per = (per + 1) / 2;
-    kbps[L] = (int)per;
-    max_splits = std::max<int>(max_splits, (int)((kbl + per - 1) / per));
+  CUtensorMap ma, mb;
+  if (!tc::make_map(&ma, OFRR_BF16, A.stack, S * Kp, M, S * Kp, tc::BM) ||
+      !tc::make_map(&mb, OFRR_BF16, Bs.stack, S * Kp, N, S * Kp, SBN))
+    return OFRR_ERR_INTERNAL;
+  const int kbt = (int)(Kp / tc::BK);
+  const int tiles = (int)(((M + tc::BM - 1) / tc::BM) * ((N + SBN - 1) / SBN));
+  // K ranges of at most 16 k-blocks (exactness), and about one wave of CTAs
+  int splits = std::max((kbt + SL_KB_MAX - 1) / SL_KB_MAX, std::min(kbt, std::max(1, 148 / tiles)));
+  const int kbps = (kbt + splits - 1) / splits;
+  splits = (kbt + kbps - 1) / kbps;
+  long long* P = nullptr;
+  if (splits > 1) {
+    P = ws_get<long long>(ctx, (size_t)splits * M * N, &st);
+    if (!P) return st;
   }
-  float* P = ws_get<float>(ctx, (size_t)max_splits * M * N, &st);
-  if (!P) return st;
-  for (int L = 0; L <= LMAX; ++L) {
-    const __nv_bfloat16* Bl = levels + (size_t)N * Kp * L * (L + 1) / 2;
-    int splits = 0;
-    OFRR_TRY(tc_gemm_partials(ctx, OFRR_BF16, M, N, (L + 1) * Kp, A.stack, S * Kp, Bl, (L + 1) * Kp, kbps[L], P,
-                              &splits));
-    slice::k_combine<<<grid_for(M * N, 256, 2048), 256, 0, ctx->stream>>>(M, N, splits, P, C, ldc, A.expo, Bs.expo,
-                                                                         BETA * (L + 2), L == 0 ? 1 : 0);
-    OFRR_LAUNCHED(ctx, "k_combine");
+  static bool attr_set = false;
+  if (!attr_set) {
+    OFRR_CUDA(cudaFuncSetAttribute(k_sliced_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL_SMEM));
+    attr_set = true;
+  }
+  dim3 grid((unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)((N + SBN - 1) / SBN), (unsigned)splits);
+  k_sliced_tn<<<grid, SL_THREADS, SL_SMEM, ctx->stream>>>(ma, mb, (int)M, (int)N, Kp, kbt, kbps,
+                                                        tc::make_idesc(OFRR_BF16, SBN), P, C, ldc, A.expo, Bs.expo,
+                                                        ctx->dev_flags + 2);
+  OFRR_LAUNCHED(ctx, "k_sliced_tn");
+  if (splits > 1) {
+    k_sliced_finish<<<grid_for(M * N, 256, 2048), 256, 0, ctx->stream>>>(M, N, splits, P, C, ldc, A.expo, Bs.expo);
+    OFRR_LAUNCHED(ctx, "k_sliced_finish");
   }
   return OFRR_SUCCESS;
 }

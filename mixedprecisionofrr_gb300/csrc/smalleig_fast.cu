@@ -24,24 +24,27 @@
 namespace ofrr {
 
 // ---- 1. Cholesky (lower) of M + tau I; batched over blockIdx.x ------------------------------------
+// Right-looking; per column one reciprocal square root (thread 0), the column scaled by it, and the
+// lower triangle of the trailing block updated with one warp per column (no index division).
 __global__ void __launch_bounds__(256) k_chol_f64(int n, const double* const* Ms, int ldm, double tau,
                                                   double* const* Ls, int* flag) {
   extern __shared__ double S[];
   const double* M = Ms[blockIdx.x];
   double* L = Ls[blockIdx.x];
-  const int tid = threadIdx.x, nt = blockDim.x;
-  __shared__ double s_maxd;
-  for (int e = tid; e < n * n; e += nt) {
-    const int i = e % n, j = e / n;
-    double v = (i >= j) ? M[i + (size_t)j * ldm] : 0.0;
-    if (i == j) v += tau;
-    S[e] = v;
-  }
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  __shared__ double s_maxd, s_rinv;
+  for (int j = warp; j < n; j += nw)
+    for (int i = lane; i < n; i += 32) {
+      double v = (i >= j) ? M[i + (size_t)j * ldm] : 0.0;
+      if (i == j) v += tau;
+      S[i + j * n] = v;
+    }
   __syncthreads();
-  if (tid == 0) {
-    double md = 0;
-    for (int k = 0; k < n; ++k) md = fmax(md, fabs(S[k + k * n]));
-    s_maxd = md;
+  if (tid < 32) {
+    long long kmax = -1;
+    for (int k = lane; k < n; k += 32) kmax = max(kmax, amax_key(S[k + k * n]));
+    for (int o = 16; o > 0; o >>= 1) kmax = max(kmax, (long long)__shfl_xor_sync(0xffffffffu, kmax, o));
+    if (lane == 0) s_maxd = (kmax > 0) ? __longlong_as_double(kmax - 1) : 0.0;
   }
   __syncthreads();
   for (int k = 0; k < n; ++k) {
@@ -52,78 +55,135 @@ __global__ void __launch_bounds__(256) k_chol_f64(int n, const double* const* Ms
         d = floor_d;
         if (flag) *flag = 1;
       }
-      S[k + k * n] = sqrt(d);
+      const double r = rsqrt(d);
+      S[k + k * n] = d * r;  // sqrt(d)
+      s_rinv = r;
     }
     __syncthreads();
-    const double dk = S[k + k * n];
-    for (int i = k + 1 + tid; i < n; i += nt) S[i + k * n] /= dk;
+    const double rinv = s_rinv;
+    for (int i = k + 1 + tid; i < n; i += nt) S[i + k * n] *= rinv;
     __syncthreads();
-    const int rem = n - k - 1;
-    for (int e = tid; e < rem * rem; e += nt) {
-      const int i = k + 1 + e % rem, j = k + 1 + e / rem;
-      if (i >= j) S[i + j * n] -= S[i + k * n] * S[j + k * n];
+    for (int j = k + 1 + warp; j < n; j += nw) {
+      const double ljk = S[j + k * n];
+      for (int i = j + lane; i < n; i += 32) S[i + j * n] = fma(-S[i + k * n], ljk, S[i + j * n]);
     }
     __syncthreads();
   }
-  for (int e = tid; e < n * n; e += nt) {
-    const int i = e % n, j = e / n;
-    L[e] = (i >= j) ? S[e] : 0.0;
-  }
+  for (int j = warp; j < n; j += nw)
+    for (int i = lane; i < n; i += 32) L[i + j * n] = (i >= j) ? S[i + j * n] : 0.0;
 }
 
 // ---- 2. triangular solves, one warp per right-hand side ------------------------------------------
 // upper == 0: L X = B (forward); upper == 1: L' X = B (backward).  transB: right-hand side j is row j.
+// Column-oriented: lane l holds rows l, l+32, l+64, l+96 of its right-hand side in registers; for each
+// i the owner broadcasts x_i = x_i / L_ii (multiplied by the staged reciprocal) and every lane
+// updates its rows with one FMA each -- about three FP64 warp instructions per row (GB300's FP64 pipe
+// is 1/64 rate, so a shuffle-reduced dot product per row would cost several times more).
+constexpr int TRSM_R = 4;  // rows per lane: n <= 128
 __global__ void __launch_bounds__(128) k_trsm_f64(int n, int nrhs, const double* __restrict__ L, int ldl,
                                                   const double* __restrict__ B, int ldb, int transB,
                                                   double* __restrict__ X, int ldx, int upper) {
-  extern __shared__ double sm_trsm[];  // L (n x n, padded ld n+1) staged, then 4 warps x n solution entries
+  extern __shared__ double sm_trsm[];  // L (n x n, padded ld n+1), then the n diagonal reciprocals
   const int ld = n + 1;
   double* Ls = sm_trsm;
-  double* xs = sm_trsm + (size_t)n * ld;
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) Ls[(e % n) + (e / n) * ld] = L[(e % n) + (size_t)(e / n) * ldl];
+  double* rd = sm_trsm + (size_t)n * ld;
+  const int nn = n * n;
+  for (int e0 = threadIdx.x; e0 < nn; e0 += 4 * blockDim.x) {
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = e0 + u * blockDim.x;
+      v[u] = (e < nn) ? L[(e % n) + (size_t)(e / n) * ldl] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = e0 + u * blockDim.x;
+      if (e < nn) Ls[(e % n) + (e / n) * ld] = v[u];
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) rd[i] = 1.0 / Ls[i + i * ld];
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int col = blockIdx.x * 4 + w;
   if (col >= nrhs) return;
-  double* x = xs + (size_t)w * n;
-  // right-hand side into shared memory first (coalesced when not transposed)
-  for (int i = lane; i < n; i += 32) x[i] = transB ? B[col + (size_t)i * ldb] : B[i + (size_t)col * ldb];
-  __syncwarp();
-  for (int t = 0; t < n; ++t) {
-    const int i = upper ? (n - 1 - t) : t;
-    double s = 0.0;
-    if (!upper) {
-      for (int k = lane; k < i; k += 32) s += Ls[i + k * ld] * x[k];
-    } else {
-      for (int k = i + 1 + lane; k < n; k += 32) s += Ls[k + i * ld] * x[k];
-    }
+  double x[TRSM_R];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) x[i] = (x[i] - s) / Ls[i + i * ld];
-    __syncwarp();
+  for (int u = 0; u < TRSM_R; ++u) {
+    const int i = lane + 32 * u;
+    x[u] = (i < n) ? (transB ? B[col + (size_t)i * ldb] : B[i + (size_t)col * ldb]) : 0.0;
   }
-  for (int i = lane; i < n; i += 32) X[i + (size_t)col * ldx] = x[i];
+  if (!upper) {
+#pragma unroll
+    for (int u = 0; u < TRSM_R; ++u) {
+      for (int il = 0; il < 32; ++il) {
+        const int i = 32 * u + il;
+        if (i >= n) break;
+        const double xi = __shfl_sync(0xffffffffu, x[u], il) * rd[i];
+        if (lane == il) x[u] = xi;
+#pragma unroll
+        for (int v = u; v < TRSM_R; ++v) {
+          const int k = lane + 32 * v;
+          if (k > i && k < n) x[v] = fma(-Ls[k + i * ld], xi, x[v]);
+        }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int u = TRSM_R - 1; u >= 0; --u) {
+      for (int il = 31; il >= 0; --il) {
+        const int i = 32 * u + il;
+        if (i >= n) continue;
+        const double xi = __shfl_sync(0xffffffffu, x[u], il) * rd[i];
+        if (lane == il) x[u] = xi;
+#pragma unroll
+        for (int v = 0; v <= u; ++v) {
+          const int k = lane + 32 * v;
+          if (k < i) x[v] = fma(-Ls[i + k * ld], xi, x[v]);  // (L')(k, i) = L(i, k)
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < TRSM_R; ++u) {
+    const int i = lane + 32 * u;
+    if (i < n) X[i + (size_t)col * ldx] = x[u];
+  }
 }
 
 // ---- small FP64 GEMM: C = alpha op(A) op(B) + beta C, one thread per output entry -----------------
+// Loads are issued eight k-steps ahead of their FMAs and two accumulators halve the dependent chain.
 __global__ void __launch_bounds__(64) k_gemm_small_f64(int M, int N, int K, double alpha, const double* __restrict__ A,
                                                        int lda, int tA, const double* __restrict__ B, int ldb, int tB,
                                                        double beta, double* __restrict__ C, int ldc) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= M * N) return;
   const int i = e % M, j = e / M;
-  double s = 0.0;
-  for (int k = 0; k < K; ++k) {
-    const double a = tA ? A[k + (size_t)i * lda] : A[i + (size_t)k * lda];
-    const double b = tB ? B[j + (size_t)k * ldb] : B[k + (size_t)j * ldb];
-    s = fma(a, b, s);
+  double s0 = 0.0, s1 = 0.0;
+  for (int k0 = 0; k0 < K; k0 += 8) {
+    double a[8], b[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int k = k0 + u;
+      a[u] = (k < K) ? (tA ? A[k + (size_t)i * lda] : A[i + (size_t)k * lda]) : 0.0;
+      b[u] = (k < K) ? (tB ? B[j + (size_t)k * ldb] : B[k + (size_t)j * ldb]) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u += 2) {
+      s0 = fma(a[u], b[u], s0);
+      s1 = fma(a[u + 1], b[u + 1], s1);
+    }
   }
+  const double s = s0 + s1;
   C[i + (size_t)j * ldc] = (beta == 0.0) ? alpha * s : fma(alpha, s, beta * C[i + (size_t)j * ldc]);
 }
 
 // ---- 3. FP32 cyclic Jacobi (round-robin parallel ordering), one CTA --------------------------------
 __device__ __forceinline__ int rr_idx(int i, int r, int N) { return i == 0 ? 0 : ((i - 1 + r) % (N - 1)) + 1; }
 
+// Each round applies n/2 disjoint rotations J.  C <- J' C J is done block-wise: the 2 x 2 block of C
+// on the rows of pair a and the columns of pair b depends only on that block, so one pass updates all
+// blocks (and W <- W J) between two barriers.
 __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restrict__ Cin, int ldc,
                                                     double* __restrict__ Wout, double* __restrict__ lam) {
   extern __shared__ float smf[];
@@ -131,7 +191,7 @@ __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restr
   float* C = smf;
   float* W = smf + n * ld;
   __shared__ float s_c[64], s_s[64];
-  __shared__ int s_p[64], s_q[64];
+  __shared__ int s_p[64], s_q[64];  // the pair's indices (q may be n: the padding index for odd n)
   __shared__ float s_red[32];
   __shared__ int s_stop;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -189,42 +249,45 @@ __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restr
           }
         }
         s_p[k] = p;
-        s_q[k] = (q < n && s != 0.f) ? q : -1;
+        s_q[k] = q;
         s_c[k] = c;
         s_s[k] = s;
       }
       __syncthreads();
-      for (int e = tid; e < npair * n; e += nt) {
-        const int k = e / n, j = e % n, q = s_q[k];
-        if (q < 0) continue;
-        const int p = s_p[k];
-        const float c = s_c[k], s = s_s[k];
-        const float ap = C[p + j * ld], aq = C[q + j * ld];
-        C[p + j * ld] = c * ap - s * aq;
-        C[q + j * ld] = s * ap + c * aq;
+      // rows of pair a rotated by J_a', then columns of pair b by J_b; diagonal blocks lose their
+      // off-diagonal pair entries exactly
+      for (int e = tid; e < npair * npair; e += nt) {
+        const int ka = e % npair, kb = e / npair;
+        const int pa = s_p[ka], qa = s_q[ka], pb = s_p[kb], qb = s_q[kb];
+        const float ca = s_c[ka], sa = s_s[ka], cb = s_c[kb], sb = s_s[kb];
+        if (sa == 0.f && sb == 0.f) continue;
+        const bool qav = qa < n, qbv = qb < n;
+        const float x11 = C[pa + pb * ld];
+        const float x12 = qbv ? C[pa + qb * ld] : 0.f;
+        const float x21 = qav ? C[qa + pb * ld] : 0.f;
+        const float x22 = (qav && qbv) ? C[qa + qb * ld] : 0.f;
+        const float y11 = ca * x11 - sa * x21, y12 = ca * x12 - sa * x22;
+        const float y21 = sa * x11 + ca * x21, y22 = sa * x12 + ca * x22;
+        float z11 = cb * y11 - sb * y12, z12 = sb * y11 + cb * y12;
+        float z21 = cb * y21 - sb * y22, z22 = sb * y21 + cb * y22;
+        if (ka == kb) {
+          z12 = 0.f;
+          z21 = 0.f;
+        }
+        C[pa + pb * ld] = z11;
+        if (qbv) C[pa + qb * ld] = z12;
+        if (qav) C[qa + pb * ld] = z21;
+        if (qav && qbv) C[qa + qb * ld] = z22;
       }
-      __syncthreads();
       for (int e = tid; e < npair * n; e += nt) {
-        const int k = e / n, i = e % n, q = s_q[k];
-        if (q < 0) continue;
-        const int p = s_p[k];
-        const float c = s_c[k], s = s_s[k];
-        float ap = C[i + p * ld], aq = C[i + q * ld];
-        C[i + p * ld] = c * ap - s * aq;
-        C[i + q * ld] = s * ap + c * aq;
-        ap = W[i + p * ld];
-        aq = W[i + q * ld];
+        const int k = e / n, i = e % n;
+        const float s = s_s[k];
+        if (s == 0.f) continue;
+        const int p = s_p[k], q = s_q[k];
+        const float c = s_c[k];
+        const float ap = W[i + p * ld], aq = W[i + q * ld];
         W[i + p * ld] = c * ap - s * aq;
         W[i + q * ld] = s * ap + c * aq;
-      }
-      __syncthreads();
-      for (int k = tid; k < npair; k += nt) {
-        const int q = s_q[k];
-        if (q >= 0) {
-          const int p = s_p[k];
-          C[p + q * ld] = 0.f;
-          C[q + p * ld] = 0.f;
-        }
       }
       __syncthreads();
     }
@@ -234,20 +297,27 @@ __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restr
 }
 
 // ---- 4. Ogita-Aishima correction: from P = W'W and T = W'CW build lambda and F = I + E ------------
-__global__ void k_oa_correction(int n, const double* __restrict__ P, const double* __restrict__ T,
-                                double* __restrict__ lam, double* __restrict__ F, double rel_cluster) {
+// One thread per entry of F over a grid of CTAs; every CTA forms the n Rayleigh quotients itself.
+__global__ void __launch_bounds__(256) k_oa_correction(int n, const double* __restrict__ P, const double* __restrict__ T,
+                                                       double* __restrict__ lam, double* __restrict__ F,
+                                                       double rel_cluster) {
   extern __shared__ double sl[];
   __shared__ double s_scale;
   for (int i = threadIdx.x; i < n; i += blockDim.x) sl[i] = T[i + (size_t)i * n] / P[i + (size_t)i * n];
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double m = 0;
-    for (int i = 0; i < n; ++i) m = fmax(m, fabs(sl[i]));
-    s_scale = (m > 0 ? m : 1.0) * rel_cluster;
+  if (threadIdx.x < 32) {
+    long long kmax = -1;
+    for (int i = threadIdx.x; i < n; i += 32) kmax = max(kmax, amax_key(sl[i]));
+    for (int o = 16; o > 0; o >>= 1) kmax = max(kmax, (long long)__shfl_xor_sync(0xffffffffu, kmax, o));
+    if (threadIdx.x == 0) {
+      const double m = (kmax > 1) ? __longlong_as_double(kmax - 1) : 0.0;
+      s_scale = (m > 0 ? m : 1.0) * rel_cluster;
+    }
   }
   __syncthreads();
   const double delta = s_scale;
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n * n) {
     const int i = e % n, j = e / n;
     const double r = (i == j ? 1.0 : 0.0) - P[e];
     double f;
@@ -259,21 +329,36 @@ __global__ void k_oa_correction(int n, const double* __restrict__ P, const doubl
     }
     F[e] = f;
   }
-  for (int i = threadIdx.x; i < n; i += blockDim.x) lam[i] = sl[i];
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) lam[i] = sl[i];
 }
 
 // ---- 5. sort descending, gather columns --------------------------------------------------------------
-__global__ void k_sort_desc(int n, const double* __restrict__ lam, const double* __restrict__ W, double* __restrict__ lam_out,
-                            double* __restrict__ Wout) {
+// Ranks from order-preserving integer keys of the doubles (no FP64 compares); then a parallel gather.
+__device__ __forceinline__ long long order_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return (b < 0) ? (b ^ 0x7fffffffffffffffLL) : b;
+}
+__global__ void __launch_bounds__(256) k_sort_desc(int n, const double* __restrict__ lam, const double* __restrict__ W,
+                                                   double* __restrict__ lam_out, double* __restrict__ Wout) {
+  __shared__ long long s_key[256];
+  __shared__ int s_rank[256];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s_key[i] = order_key(lam[i]);
+  __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double li = lam[i];
+    const long long ki = s_key[i];
     int rank = 0;
     for (int j = 0; j < n; ++j) {
-      const double lj = lam[j];
-      rank += (lj > li || (lj == li && j < i)) ? 1 : 0;
+      const long long kj = s_key[j];
+      rank += (kj > ki || (kj == ki && j < i)) ? 1 : 0;
     }
-    lam_out[rank] = li;
-    for (int r = 0; r < n; ++r) Wout[r + (size_t)rank * n] = W[r + (size_t)i * n];
+    s_rank[i] = rank;
+    lam_out[rank] = lam[i];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, r = e % n;
+    Wout[r + (size_t)s_rank[i] * n] = W[r + (size_t)i * n];
   }
 }
 
@@ -299,7 +384,7 @@ static int gemm_small(ofrr_ctx* ctx, int M, int N, int K, double alpha, const do
 
 static int trsm(ofrr_ctx* ctx, int n, int nrhs, const double* L, const double* B, int ldb, int transB, double* X,
                 int upper) {
-  const size_t smem = ((size_t)n * (n + 1) + 4 * (size_t)n) * sizeof(double);
+  const size_t smem = ((size_t)n * (n + 1) + (size_t)n) * sizeof(double);
   OFRR_CUDA(cudaFuncSetAttribute(k_trsm_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_trsm_f64<<<(nrhs + 3) / 4, 128, smem, ctx->stream>>>(n, nrhs, L, n, B, ldb, transB, X, n, upper);
   OFRR_LAUNCHED(ctx, "k_trsm_f64");
@@ -341,7 +426,7 @@ static int sym_eig_refined(ofrr_ctx* ctx, int n, const double* C, double* W, dou
     OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, Wc, n, 0, 0.0, P, n));   // P = W'W
     OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, C, n, 0, Wc, n, 0, 0.0, CW, n));   // CW
     OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, CW, n, 0, 0.0, T, n));   // T = W'CW
-    k_oa_correction<<<1, 256, n * sizeof(double), ctx->stream>>>(n, P, T, l0, F, 1e-5);
+    k_oa_correction<<<(n * n + 255) / 256, 256, n * sizeof(double), ctx->stream>>>(n, P, T, l0, F, 1e-5);
     OFRR_LAUNCHED(ctx, "k_oa_correction");
     OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 0, F, n, 0, 0.0, Wn, n));   // W <- W (I + E)
     std::swap(Wc, Wn);
@@ -350,7 +435,7 @@ static int sym_eig_refined(ofrr_ctx* ctx, int n, const double* C, double* W, dou
   OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, Wc, n, 0, 0.0, P, n));
   OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, C, n, 0, Wc, n, 0, 0.0, CW, n));
   OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, CW, n, 0, 0.0, T, n));
-  k_oa_correction<<<1, 256, n * sizeof(double), ctx->stream>>>(n, P, T, l0, F, 1e-5);
+  k_oa_correction<<<(n * n + 255) / 256, 256, n * sizeof(double), ctx->stream>>>(n, P, T, l0, F, 1e-5);
   OFRR_LAUNCHED(ctx, "k_oa_correction");
   k_sort_desc<<<1, 256, 0, ctx->stream>>>(n, l0, Wc, lam, W);
   OFRR_LAUNCHED(ctx, "k_sort_desc");

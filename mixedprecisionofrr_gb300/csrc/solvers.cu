@@ -799,12 +799,12 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
       int64_t lddst = (cur == V) ? n : ldv;
       OFRR_TRY(op.apply(ctx, 0, P.po, P.po, cur, ldcur, b, P.pc, P.po, dst, lddst));
       S.nmv += b;
-      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, dst, lddst, nullptr));
+      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, dst, lddst, nullptr, P.fast));
       cur = dst;
       ldcur = lddst;
     }
     // [Q,~] = hessenberg(V): the economic form drops deselected columns
-    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, n, b, cur, ldcur, Q, n, opt->select_tol, R, sel, perm));
+    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, n, b, cur, ldcur, Q, n, opt->select_tol, R, sel, perm, P.fast));
     OFRR_CUDA(cudaMemcpyAsync(hsel.data(), sel, sizeof(int) * b, cudaMemcpyDeviceToHost, ctx->stream));
     OFRR_TRY(sync_and_check(ctx));
     int w = b;
@@ -871,13 +871,13 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
     int b = S.b;
     for (int j = 0; j < opt->step_size; ++j) {
       OFRR_TRY(op.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.po, U, ldu));
-      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, m, b, U, ldu, nullptr));
+      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, m, b, U, ldu, nullptr, P.fast));
       OFRR_TRY(op.apply(ctx, 1, P.po, P.po, U, ldu, b, P.pc, P.po, V, ldv));
-      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr));
+      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr, P.fast));
       S.nmv += 2 * b;
     }
-    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, m, b, U, ldu, P1, m, opt->select_tol, R, sel, perm));
-    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, n, b, V, ldv, Q1, n, opt->select_tol, R, sel + b0, perm));
+    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, m, b, U, ldu, P1, m, opt->select_tol, R, sel, perm, P.fast));
+    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, n, b, V, ldv, Q1, n, opt->select_tol, R, sel + b0, perm, P.fast));
     OFRR_CUDA(cudaMemcpyAsync(hsel.data(), sel, sizeof(int) * 2 * b0, cudaMemcpyDeviceToHost, ctx->stream));
     OFRR_TRY(sync_and_check(ctx));
     int wu = b, wv = b;

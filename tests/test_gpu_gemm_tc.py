@@ -72,7 +72,8 @@ def test_tc_exact_small_integers(api):
     assert np.array_equal(got, A.T @ B)
 
 
-@pytest.mark.parametrize("M,N,K", [(2048, 64, 8192), (8192, 64, 2048), (64, 64, 8192), (300, 17, 1000), (77, 5, 64)])
+@pytest.mark.parametrize("M,N,K", [(2048, 64, 8192), (8192, 64, 2048), (64, 64, 8192), (300, 17, 1000), (77, 5, 64),
+                                   (20000, 64, 512), (1000, 130, 3000), (128, 64, 1)])
 def test_f64_emulated_gemm(api, M, N, K):
     """Exact-slice FP64 emulation: element error within 2^-33 |A'| |B| (two bits of margin over the
     2^-35 design bound), on operands with widely varying column scales."""
@@ -83,6 +84,25 @@ def test_f64_emulated_gemm(api, M, N, K):
     ref = A.T @ B
     bound = np.abs(A).T @ np.abs(B)
     assert np.all(np.abs(C - ref) <= 2.0 ** -33 * bound + 1e-300)
+    # integer accumulation: the result does not depend on the schedule (bit-identical on repeat)
+    assert np.array_equal(api.gemm_f64_emulated(A, B).cpu().numpy(), C)
+
+
+def test_f64_emulated_gemm_extreme_scales(api):
+    """Columns with subnormal, huge, unit and zero scales (the digit split works on the bit patterns)."""
+    rng = np.random.default_rng(7)
+    K = 700
+    A = rng.standard_normal((K, 6))
+    A[:, 0] *= 1e-310
+    A[:, 1] *= 1e300
+    A[:, 3] = 0.0
+    A[5, 4] = 5e-324  # one denormal entry in an otherwise normal column
+    B = rng.standard_normal((K, 3))
+    C = api.gemm_f64_emulated(A, B).cpu().numpy()
+    ref = A.T @ B
+    bound = np.abs(A).T @ np.abs(B)
+    assert np.all(np.abs(C - ref) <= 2.0 ** -33 * bound + 1e-320)
+    assert np.array_equal(C[3], np.zeros(3))
 
 
 def test_f64_emulated_gemm_zero_columns(api):

@@ -72,6 +72,26 @@ def test_scalecols_bit_exact(api, orc, pc, po):
     assert np.array_equal(api.to_numpy(out), ref)
 
 
+@pytest.mark.parametrize("m", [2048, 2049, 6000])
+def test_scalecols_chunked_ties(api, orc, m):
+    """Columns longer than one CTA's chunk: equal maxima in different chunks pick the lowest row."""
+    rng = np.random.default_rng(m)
+    U = rng.uniform(-1, 1, (m, 5))
+    U[[2047, m - 1], 0] = [-3.0, 3.0]   # tie across the chunk boundary: row 2047 wins
+    U[[m - 1, 5], 1] = [4.0, -4.0]      # tie, lower row first in the column
+    U[:, 2] = 0.0
+    U[m // 2, 3] = np.nan               # NaN is never the pivot
+    for pc, po in (("double", "double"), ("single", "half")):
+        Ui = U.astype(orc._dt(po))
+        out, piv = api.scalecols(Ui, pc, po, return_pivots=True)
+        ref, rpiv = orc.scalecols(Ui, pc, po, return_pivots=True)
+        piv = api.to_numpy(piv)
+        assert piv[0] == 2047 and piv[1] == 5 and piv[2] == 0
+        assert np.array_equal(piv[[0, 1, 2, 4]], rpiv[[0, 1, 2, 4]])
+        got = api.to_numpy(out)
+        assert np.array_equal(got[:, [0, 1, 2, 4]], ref[:, [0, 1, 2, 4]])
+
+
 def test_scalecols_golden(api, gold):
     out = api.scalecols(gold["scal_U"], "single", "half")
     assert np.array_equal(api.to_numpy(out), gold["scal_out"])
@@ -195,7 +215,8 @@ def test_check_special_values(api):
 
 
 @pytest.mark.parametrize("pc,po,shape", [("single", "half", (3000, 64)), ("double", "double", (8192, 64)),
-                                         ("single", "single", (1500, 37)), ("single", "half", (20000, 96))])
+                                         ("single", "single", (1500, 37)), ("single", "half", (20000, 96)),
+                                         ("double", "double", (2047, 80)), ("single", "half", (8192, 64))])
 def test_hessenberg_blocked_equals_per_column(api, orc, pc, po, shape):
     """The cluster-blocked schedule and the per-column schedule give bit-identical bases."""
     import os
@@ -209,10 +230,18 @@ def test_hessenberg_blocked_equals_per_column(api, orc, pc, po, shape):
         Qc, Rc, selc, permc = api.hessenberg(A, pc, po)
     finally:
         del os.environ["OFRR_HESS_PER_COLUMN"]
+    os.environ["OFRR_HESS_CLUSTER"] = "8"  # portable cluster size (the default may be 16 CTAs)
+    try:
+        Q8, R8, sel8, perm8 = api.hessenberg(A, pc, po)
+    finally:
+        del os.environ["OFRR_HESS_CLUSTER"]
     assert np.array_equal(permb, permc) and np.array_equal(selb, selc)
     assert np.array_equal(api.to_numpy(Qb), api.to_numpy(Qc))
     assert np.array_equal(Rb, Rc)
-    assert not selb[20]
+    assert np.array_equal(perm8, permc) and np.array_equal(api.to_numpy(Q8), api.to_numpy(Qc))
+    assert np.array_equal(R8, Rc)
+    if po != "double":  # in FP64 the duplicate's rounding residual can exceed the default eps threshold
+        assert not selb[20]
     if shape[0] <= 3000:
         Qo, Ro, selo, permo = orc.hessenberg(A, pc, po)
         assert np.array_equal(api.to_numpy(Qb), Qo) and np.array_equal(permb, permo)
