@@ -215,6 +215,7 @@ int gemm_tc_try(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype t16, int64_t M
   const int kbt = (int)((K + tc::BK - 1) / tc::BK);
   int splits = 1;
   while (tiles * splits < 148 && splits * 2 <= kbt && splits < 64) splits *= 2;
+  if (const char* e = getenv("OFRR_TC_SPLITS")) splits = std::max(1, std::min(atoi(e), kbt));  // tuning override
   int st = OFRR_SUCCESS;
   OFRR_DISPATCH_STORAGE(tout, TO, {
     if (BN == 32) st = tc::launch<32, TO>(ctx, ma, mb, (int)M, (int)N, (int)K, t16, (TO*)C, ldc, splits);

@@ -9,10 +9,11 @@
 //   1. k_hess_blockupd (all SMs): every block column is eliminated against the final columns
 //      0..c0-1 in order j = 0, 1, ..., c0-1; each thread owns one row and HB_CG block columns.
 //   2. k_hess_inblock (one cluster of 8 or 16 CTAs): the block's columns one after another entirely
-//      on chip.  Each CTA keeps its slice of rows of the block in shared memory.  Per column: local
-//      eliminations and argmax, then each CTA publishes its candidate (argmax and the block's values
-//      in that row); after ONE cluster barrier every CTA reads all candidates through distributed
-//      shared memory, picks the winner and takes the pivot row from it.
+//      on chip, right-looking.  Each CTA keeps its slice of rows of the block in shared memory.  Per
+//      column: each CTA publishes its candidate (local argmax and the block's values in that row);
+//      after ONE cluster barrier every CTA reads all candidates through distributed shared memory,
+//      takes the winner's row as the pivot row, scales the column and eliminates the later block
+//      columns against it (their coefficients are the pivot row's values).
 // For b = 64 columns this is 10 launches instead of 65.
 #include <cooperative_groups.h>
 
@@ -144,11 +145,16 @@ __global__ void __launch_bounds__(HB_UT) k_hess_blockupd(int64_t m, int c0, int 
 }
 
 // ---- step 2: the block's columns on one cluster ---------------------------------------------------
+// Right-looking within the block: when column t's pivot row k is known, the coefficients r_{t,u} of
+// the later block columns are simply their current values in row k (they have been eliminated against
+// the columns before t), so no substitution is needed.  Every element still sees its eliminations in
+// the order j = 0, 1, ..., u-1 with the same operands, so the result is bit-identical to the
+// left-looking per-column kernel.
 template <class TO>
 struct HbCand {
   long long key;  // argmax key of the local max |value| (-1: the CTA has no rows)
   long long i;    // its row
-  TO vals[HB_B];  // the block's values in that row
+  TO vals[HB_B];  // the block's current values in that row
 };
 
 template <class TO, class TC, bool FAST>
@@ -167,12 +173,9 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
   const int nloc = (r1 > r0) ? (int)(r1 - r0) : 0;
   extern __shared__ unsigned char smem_raw[];
   TO* s_blk = reinterpret_cast<TO*>(smem_raw);  // HB_B columns x RR rows (column t at t * RR)
-  __shared__ TO s_prow[HB_B * HB_B];            // pivot row of block column t at t * HB_B
   __shared__ HbCand<TO> s_cand[2];              // double-buffered by column parity
   __shared__ ArgMaxK red[HB_T / 32];
-  __shared__ TC s_r[HB_B];
-  __shared__ TO s_x[HB_B];
-  __shared__ int s_sel[HB_B];
+  __shared__ TO s_pr[HB_B];                     // pivot row of the current column (current values)
   __shared__ long long s_k;
 
   for (int lr = tid; lr < nloc; lr += HB_T) {
@@ -182,73 +185,25 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
 #pragma unroll
     for (int t = 0; t < HB_B; ++t) s_blk[(size_t)t * RR + lr] = v[t];
   }
-  __syncthreads();
   const double tol_o = to_c<double, TO>(from_c<TO, double>(select_tol));
-
-  for (int t = 0; t < nb; ++t) {
-    // (1) forward substitution over the in-block pivot rows t' < t (warp 0; every CTA alike)
-    if (tid < 32) {
-      for (int tp = tid; tp < t; tp += 32) s_x[tp] = s_prow[tp * HB_B + t];
-      __syncwarp();
-      for (int tp = 0; tp < t; ++tp) {
-        __syncwarp();
-        if (!s_sel[tp]) {
-          if (tid == 0) s_r[tp] = TC(0);
-          continue;
-        }
-        const TC rc = to_c<TC, TO>(s_x[tp]);
-        for (int tq = tp + 1 + tid; tq < t; tq += 32) {
-          if (s_sel[tq])
-            s_x[tq] = from_c<TO, TC>(elim<FAST>(to_c<TC, TO>(s_x[tq]), rc, to_c<TC, TO>(s_prow[tq * HB_B + tp])));
-        }
-        if (tid == 0) s_r[tp] = rc;
-      }
-    }
-    __syncthreads();
-    // (2) eliminations of this CTA's rows against the in-block columns t' < t (MGS order continues
-    //     after the j < c0 eliminations of step 1), four independent rows per thread; local argmax
+  {  // candidate for column 0 (already eliminated against the columns before the block)
     ArgMaxK a{-1, 0x7fffffffffffffffLL};
-    TO* col = s_blk + (size_t)t * RR;
-    for (int lr0 = tid; lr0 < nloc; lr0 += 4 * HB_T) {
-      TO vo[4];
-      TC v[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int lr = lr0 + u * HB_T;
-        vo[u] = (lr < nloc) ? col[lr] : TO(0);
-        v[u] = to_c<TC, TO>(vo[u]);
-      }
-      for (int tp = 0; tp < t; ++tp) {
-        if (!s_sel[tp]) continue;
-        const TC rc = s_r[tp];
-        const TO* ctp = s_blk + (size_t)tp * RR;
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int lr = lr0 + u * HB_T;
-          const TC q = to_c<TC, TO>((lr < nloc) ? ctp[lr] : TO(0));
-          vo[u] = from_c<TO, TC>(elim<FAST>(v[u], rc, q));
-          v[u] = to_c<TC, TO>(vo[u]);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int lr = lr0 + u * HB_T;
-        if (lr < nloc) {
-          col[lr] = vo[u];
-          const long long key = amax_key(vo[u]);
-          if (key > a.key) a = ArgMaxK{key, r0 + lr};
-        }
-      }
+    for (int lr = tid; lr < nloc; lr += HB_T) {
+      const long long key = amax_key(s_blk[lr]);
+      if (key > a.key) a = ArgMaxK{key, r0 + lr};
     }
     const ArgMaxK loc = block_argmaxk(a, red);
-    // (3) publish this CTA's candidate, one cluster barrier, pick the winner from all candidates
-    HbCand<TO>& cand = s_cand[t & 1];
     if (tid == 0) {
-      cand.key = loc.key;
-      cand.i = loc.i;
+      s_cand[0].key = loc.key;
+      s_cand[0].i = loc.i;
     }
-    if (tid < HB_B) cand.vals[tid] = (loc.key >= 0 && tid < nb) ? s_blk[(size_t)tid * RR + (loc.i - r0)] : TO(0);
+    if (tid < HB_B) s_cand[0].vals[tid] = (loc.key >= 0 && tid < nb) ? s_blk[(size_t)tid * RR + (loc.i - r0)] : TO(0);
+  }
+
+  for (int t = 0; t < nb; ++t) {
+    // (1) one cluster barrier; the winner among all CTAs' candidates (lowest row among equal maxima)
     cluster.sync();
+    HbCand<TO>& cand = s_cand[t & 1];
     if (tid < 32) {
       ArgMaxK b{-1, 0x7fffffffffffffffLL};
       if (lane < ncl) {
@@ -262,26 +217,15 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
       const int owner = (bk < 0) ? 0 : (int)(bi / RR);
       if (lane < HB_B) {
         const HbCand<TO>* po = cluster.map_shared_rank(&cand, owner);
-        s_prow[t * HB_B + lane] = po->vals[lane];
+        s_pr[lane] = po->vals[lane];
       }
       if (lane == 0) s_k = (bk < 0) ? 0 : bi;
     }
     __syncthreads();
     const long long k = s_k;
-    const TO pv = s_prow[t * HB_B + t];
+    const TO pv = s_pr[t];
     const bool keep = absd(pv) >= tol_o;
-    // (4) scale (or zero) this CTA's rows of column t
-    const TC pc = to_c<TC, TO>(pv);
-    const TC y = pivot_recip(pc);
-    const bool pf = pivot_fast(pc);
-    for (int lr = tid; lr < nloc; lr += HB_T) {
-      const TC q = to_c<TC, TO>(col[lr]);
-      // FAST: x * RN(1/p) (within an ulp of x / p), the pivot itself exactly 1
-      const TC sq = (FAST && pf) ? ((r0 + lr == k) ? TC(1) : mul_recip(q, y)) : pivot_div(q, pc, y, pf);
-      col[lr] = keep ? from_c<TO, TC>(sq) : TO(0);
-    }
-    if (tid == 0) s_sel[t] = keep ? 1 : 0;
-    // (5) bookkeeping (rank 0): pivot, selection, R(:, i)
+    // (2) bookkeeping (rank 0): pivot, selection, row i of R (R(i, c0+u) = r_{t,u} for u > t)
     if (rank == 0) {
       const int i = c0 + t;
       if (tid == 0) {
@@ -289,11 +233,47 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
         perm[i] = keep ? (int)k : -1;
         R[i + (int64_t)i * n] = to_c<double, TO>(pv);
       }
-      for (int tp = tid; tp < t; tp += blockDim.x)
-        R[(c0 + tp) + (int64_t)i * n] = s_sel[tp] ? to_c<double, TC>(s_r[tp]) : 0.0;
+      for (int u = t + 1 + tid; u < nb; u += blockDim.x)
+        R[i + (int64_t)(c0 + u) * n] = keep ? to_c<double, TC>(to_c<TC, TO>(s_pr[u])) : 0.0;
     }
-    __syncthreads();
+    // (3) scale (or zero) column t, eliminate the later block columns against it, argmax of column t+1
+    const TC pc = to_c<TC, TO>(pv);
+    const TC y = pivot_recip(pc);
+    const bool pf = pivot_fast(pc);
+    const bool has_next = t + 1 < nb;
+    ArgMaxK a{-1, 0x7fffffffffffffffLL};
+    for (int lr = tid; lr < nloc; lr += HB_T) {
+      TO* row = s_blk + lr;
+      if (keep) {
+        const TC q = to_c<TC, TO>(row[(size_t)t * RR]);
+        // FAST: x * RN(1/p) (within an ulp of x / p), the pivot itself exactly 1
+        const TC sq = (FAST && pf) ? ((r0 + lr == k) ? TC(1) : mul_recip(q, y)) : pivot_div(q, pc, y, pf);
+        const TO so = from_c<TO, TC>(sq);
+        row[(size_t)t * RR] = so;
+        const TC qs = to_c<TC, TO>(so);
+        for (int u = t + 1; u < nb; ++u) {
+          TO* e = row + (size_t)u * RR;
+          *e = from_c<TO, TC>(elim<FAST>(to_c<TC, TO>(*e), to_c<TC, TO>(s_pr[u]), qs));
+        }
+      } else {
+        row[(size_t)t * RR] = TO(0);
+      }
+      if (has_next) {
+        const long long key = amax_key(row[(size_t)(t + 1) * RR]);
+        if (key > a.key) a = ArgMaxK{key, r0 + lr};
+      }
+    }
+    if (has_next) {  // publish the candidate for column t+1 (its buffer was last read before this barrier)
+      const ArgMaxK loc = block_argmaxk(a, red);
+      HbCand<TO>& nc = s_cand[(t + 1) & 1];
+      if (tid == 0) {
+        nc.key = loc.key;
+        nc.i = loc.i;
+      }
+      if (tid < HB_B) nc.vals[tid] = (loc.key >= 0 && tid < nb) ? s_blk[(size_t)tid * RR + (loc.i - r0)] : TO(0);
+    }
   }
+  __syncthreads();
   for (int lr = tid; lr < nloc; lr += HB_T) {
 #pragma unroll
     for (int t = 0; t < HB_B; ++t)
