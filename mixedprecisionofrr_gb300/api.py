@@ -488,6 +488,31 @@ def arnoldi_hess_eig(A, n: int, k: int, precision_compute="double", precision_ou
     return X, d, _info(st, inf, res)
 
 
+def arnoldi_mgs_eig(A, n: int, k: int, precision_compute="double", precision_output=None, seed: int = 42,
+                    maxiter: int = 5, kdim=None, reorth: bool = True, use_generalized: bool = False,
+                    generalized_tol=0.0, select_tol=None, symmetric=None, v0=None, tol=0.0):
+    """MATLAB/+src/+krylov/arnoldi_mgs_eig.m (orthogonal comparison path); returns (V, d, info)."""
+    ctx = context()
+    op = operator(A, symmetric)
+    kk = min(k, n)
+    o = options(mode=L.MODE_REFERENCE, maxiter=maxiter, kdim=kdim or maxiter, nev=kk, tol=tol,
+                use_generalized=int(use_generalized), generalized_tol=generalized_tol,
+                select_tol=-1.0 if select_tol is None else select_tol, seed=seed, use_start_block=int(v0 is not None),
+                orth=L.ORTH_MGS, reorth=int(reorth), **_prec_opts(precision_compute, precision_output, None, None, None,
+                                                                  None))
+    po = o.p_output
+    v0d = to_device_cm(v0, po) if v0 is not None else None
+    X = empty_cm(n, kk, po)
+    d = np.zeros(kk)
+    res = np.zeros(kk)
+    inf = L.ofrr_info()
+    st = ctx.lib.ofrr_arnoldi_eig(ctx.h, C.byref(op.op), C.byref(o), v0d.data_ptr() if v0d is not None else None,
+                                  X.data_ptr(), ld_of(X), _dp(d), _dp(res), C.byref(inf))
+    if st not in (L.SUCCESS, L.ERR_SOLVER_MAX_ITERATIONS):
+        L.check(st, "arnoldi_eig")
+    return X, d, _info(st, inf, res)
+
+
 def residual_norms(A, X, lam, normA: float = -1.0, symmetric=None):
     ctx = context()
     op = operator(A, symmetric)

@@ -340,9 +340,18 @@ int geig_dev(ofrr_ctx* ctx, int n, const double* G, int ldg, const double* M, in
 
 // production small solvers (FP32 Jacobi + FP64 refinement, multi-CTA FP64 products), n <= 128:
 // eig(G, M + tau I) (M may be null) and the svd_rr pencil of B with Gram matrices UU, VV
-int geig_fast(ofrr_ctx* ctx, int n, const double* G, const double* M, double tau, double* lam, double* U);
+// refine = number of Ogita-Aishima FP64 refinement steps after the FP32 Jacobi (each squares the
+// vectors' error: 2 give FP64-accurate vectors; 16-bit bases use 1); the values are always FP64
+// Rayleigh quotients of the final vectors
+// eig(C) for a nonsymmetric n x n C (n <= 128), FP32 Hessenberg-QR: real/imaginary parts, eigenvectors
+// (real parts, unit norm), unsorted
+int nonsym_eig_dev(ofrr_ctx* ctx, int n, const double* C, double* wr, double* wi, double* X);
+// eig(G, M) for nonsymmetric G, SPD M (or M null): real parts descending, unit real-part eigenvectors
+int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U);
+int geig_fast(ofrr_ctx* ctx, int n, const double* G, const double* M, double tau, double* lam, double* U,
+              int refine = 2);
 int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const double* VV, double tau, double* sigma,
-              double* Zf, double* Wf);
+              double* Zf, double* Wf, int refine = 2);
 
 // reductions
 int column_norms(ofrr_ctx* ctx, ofrr_dtype t, int64_t m, int64_t n, const void* X, int64_t ldx,

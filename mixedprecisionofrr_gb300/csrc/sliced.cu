@@ -29,80 +29,86 @@ constexpr int LMAX = 4;  // levels kept: pairs with s + t <= 4 (15 of 25), error
 // Integer pipes only (GB300's FP64 pipe is 1/64 rate): the column maximum is taken on the bit
 // patterns of |x|, e_n = frexp exponent of that maximum, and round(x 2^(BETA S - e_n)) is formed from
 // the significand by a right shift with round-half-even (the same value __double2ll_rn gives).
-constexpr int SLICE_T = 512;
-__global__ void __launch_bounds__(SLICE_T) k_slice_cols(int64_t K, int64_t Kp, int64_t N, const double* __restrict__ X,
-                                                        int64_t ldx, __nv_bfloat16* __restrict__ stack,
-                                                        int* __restrict__ expo) {
+// Two passes over a (row chunk x column) grid: maxima by atomicMax on the bit patterns, then digits.
+constexpr int SLICE_T = 256;
+constexpr int SLICE_U = 4;
+constexpr int64_t SLICE_CHUNK = (int64_t)SLICE_T * SLICE_U;  // rows per CTA
+
+__global__ void __launch_bounds__(SLICE_T) k_slice_max(int64_t K, int64_t N, const double* __restrict__ X, int64_t ldx,
+                                                       unsigned long long* __restrict__ colmax) {
   __shared__ unsigned long long red[SLICE_T / 32];
-  __shared__ int s_e;
-  constexpr int U = 8;  // loads in flight per thread
-  for (int64_t n = blockIdx.x; n < N; n += gridDim.x) {
+  const int64_t k0 = (int64_t)blockIdx.x * SLICE_CHUNK + threadIdx.x;
+  for (int64_t n = blockIdx.y; n < N; n += gridDim.y) {
     const double* x = X + n * ldx;
-    unsigned long long mx = 0;
-    for (int64_t k0 = threadIdx.x; k0 < K; k0 += (int64_t)U * SLICE_T) {
-      unsigned long long v[U];
+    unsigned long long v[SLICE_U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int64_t k = k0 + (int64_t)u * SLICE_T;
-        v[u] = (k < K) ? (unsigned long long)__double_as_longlong(x[k]) : 0ull;
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) mx = max(mx, v[u] & 0x7fffffffffffffffull);
+    for (int u = 0; u < SLICE_U; ++u) {
+      const int64_t k = k0 + (int64_t)u * SLICE_T;
+      v[u] = (k < K) ? ((unsigned long long)__double_as_longlong(x[k]) & 0x7fffffffffffffffull) : 0ull;
     }
+    unsigned long long mx = 0;
+#pragma unroll
+    for (int u = 0; u < SLICE_U; ++u) mx = max(mx, v[u]);
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
     __syncthreads();
     if (threadIdx.x == 0) {
       unsigned long long m = 0;
       for (int w = 0; w < SLICE_T / 32; ++w) m = max(m, red[w]);
-      // frexp exponent: m = f 2^e, f in [0.5, 1), so |x| 2^-e < 1 for the whole column
-      const int be = (int)(m >> 52);
-      int e = 0;
-      if (m != 0) e = (be > 0) ? be - 1022 : (64 - __clzll((long long)m)) - 1074;
-      s_e = e;
-      expo[n] = e;
+      if (m != 0) atomicMax(colmax + n, m);
     }
     __syncthreads();
-    const int e = s_e;
+  }
+}
+
+__global__ void __launch_bounds__(SLICE_T) k_slice_digits(int64_t K, int64_t Kp, int64_t N, const double* __restrict__ X,
+                                                          int64_t ldx, const unsigned long long* __restrict__ colmax,
+                                                          __nv_bfloat16* __restrict__ stack, int* __restrict__ expo) {
+  const int64_t k0 = (int64_t)blockIdx.x * SLICE_CHUNK + threadIdx.x;
+  for (int64_t n = blockIdx.y; n < N; n += gridDim.y) {
+    // frexp exponent of the column maximum: m = f 2^e, f in [0.5, 1), so |x| 2^-e < 1 for the column
+    const unsigned long long m = colmax[n];
+    const int bm = (int)(m >> 52);
+    int e = 0;
+    if (m != 0) e = (bm > 0) ? bm - 1022 : (64 - __clzll((long long)m)) - 1074;
+    if (blockIdx.x == 0 && threadIdx.x == 0) expo[n] = e;
+    const double* x = X + n * ldx;
     __nv_bfloat16* col = stack + (size_t)n * S * Kp;
-    for (int64_t k0 = threadIdx.x; k0 < Kp; k0 += (int64_t)U * SLICE_T) {
-      unsigned long long v[U];
+    unsigned long long v[SLICE_U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int64_t k = k0 + (int64_t)u * SLICE_T;
-        v[u] = (k < K) ? (unsigned long long)__double_as_longlong(x[k]) : 0ull;
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int64_t k = k0 + (int64_t)u * SLICE_T;
-        if (k >= Kp) break;
-        // x = M 2^(be' - 1075) with M the significand (implicit bit for normal numbers, be' = max(be, 1))
-        const unsigned long long bits = v[u];
-        const int be = (int)((bits >> 52) & 0x7ff);
-        const unsigned long long M = (bits & 0x000fffffffffffffull) | (be > 0 ? (1ull << 52) : 0ull);
-        const int sh = 1075 - (BETA * S) + e - (be > 0 ? be : 1);  // 18 or more unless the maximum is subnormal
-        long long r = 0;
-        if (sh <= 53 && M != 0) {
-          unsigned long long q;
-          if (sh <= 0) {
-            q = M << (-sh);  // subnormal column maximum: exact scaling up
-          } else {
-            q = M >> sh;
-            const unsigned long long rem = M & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
-            if (rem > half || (rem == half && (q & 1ull))) ++q;
-          }
-          r = (bits >> 63) ? -(long long)q : (long long)q;
-        }
-#pragma unroll
-        for (int s = S - 1; s > 0; --s) {  // centred base-2^BETA digits, least significant first
-          const long long d = ((r + (1 << (BETA - 1))) & ((1 << BETA) - 1)) - (1 << (BETA - 1));
-          r = (r - d) >> BETA;  // exact: r - d is a multiple of 2^BETA
-          col[(size_t)s * Kp + k] = __float2bfloat16_rn((float)d);  // |d| <= 64
-        }
-        col[k] = __float2bfloat16_rn((float)r);  // leading digit, |r| <= 128: exact in bf16
-      }
+    for (int u = 0; u < SLICE_U; ++u) {
+      const int64_t k = k0 + (int64_t)u * SLICE_T;
+      v[u] = (k < K) ? (unsigned long long)__double_as_longlong(x[k]) : 0ull;
     }
-    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < SLICE_U; ++u) {
+      const int64_t k = k0 + (int64_t)u * SLICE_T;
+      if (k >= Kp) break;
+      // x = M 2^(be' - 1075) with M the significand (implicit bit for normal numbers, be' = max(be, 1))
+      const unsigned long long bits = v[u];
+      const int be = (int)((bits >> 52) & 0x7ff);
+      const unsigned long long M = (bits & 0x000fffffffffffffull) | (be > 0 ? (1ull << 52) : 0ull);
+      const int sh = 1075 - (BETA * S) + e - (be > 0 ? be : 1);  // 18 or more unless the maximum is subnormal
+      long long r = 0;
+      if (sh <= 53 && M != 0) {
+        unsigned long long q;
+        if (sh <= 0) {
+          q = M << (-sh);  // subnormal column maximum: exact scaling up
+        } else {
+          q = M >> sh;
+          const unsigned long long rem = M & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+          if (rem > half || (rem == half && (q & 1ull))) ++q;
+        }
+        r = (bits >> 63) ? -(long long)q : (long long)q;
+      }
+#pragma unroll
+      for (int s = S - 1; s > 0; --s) {  // centred base-2^BETA digits, least significant first
+        const long long d = ((r + (1 << (BETA - 1))) & ((1 << BETA) - 1)) - (1 << (BETA - 1));
+        r = (r - d) >> BETA;  // exact: r - d is a multiple of 2^BETA
+        col[(size_t)s * Kp + k] = __float2bfloat16_rn((float)d);  // |d| <= 64
+      }
+      col[k] = __float2bfloat16_rn((float)r);  // leading digit, |r| <= 128: exact in bf16
+    }
   }
 }
 
@@ -311,9 +317,17 @@ int sliced_prepare_into(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, in
   out->M = M;
   out->stack = stack;
   out->expo = expo;
-  const int grid = (int)std::min<int64_t>(M, 65535);
-  slice::k_slice_cols<<<grid, slice::SLICE_T, 0, ctx->stream>>>(K, out->Kp, M, X, ldx, out->stack, out->expo);
-  OFRR_LAUNCHED(ctx, "k_slice_cols");
+  int st = OFRR_SUCCESS;
+  WsScope scope(ctx);
+  unsigned long long* colmax = ws_get<unsigned long long>(ctx, (size_t)M, &st);
+  if (!colmax) return st;
+  OFRR_CUDA(cudaMemsetAsync(colmax, 0, sizeof(unsigned long long) * (size_t)M, ctx->stream));
+  const dim3 g1((unsigned)((K + slice::SLICE_CHUNK - 1) / slice::SLICE_CHUNK), (unsigned)std::min<int64_t>(M, 65535));
+  slice::k_slice_max<<<g1, slice::SLICE_T, 0, ctx->stream>>>(K, M, X, ldx, colmax);
+  OFRR_LAUNCHED(ctx, "k_slice_max");
+  const dim3 g2((unsigned)((out->Kp + slice::SLICE_CHUNK - 1) / slice::SLICE_CHUNK), g1.y);
+  slice::k_slice_digits<<<g2, slice::SLICE_T, 0, ctx->stream>>>(K, out->Kp, M, X, ldx, colmax, out->stack, out->expo);
+  OFRR_LAUNCHED(ctx, "k_slice_digits");
   return OFRR_SUCCESS;
 }
 

@@ -296,6 +296,78 @@ __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restr
   for (int i = tid; i < n; i += nt) lam[i] = (double)C[i + i * ld];
 }
 
+// ---- 3b. FP32 one-sided (Hestenes) Jacobi on the columns of G: G V = U Sigma ------------------------
+// The SVD form's starting vectors: the right singular vectors of C directly (better conditioned than
+// an eigen-solve of C'C).  Round-robin pairs, one warp per pair: three dot products reduced with warp
+// shuffles, then the two columns of G and of V rotated; one barrier per round.  A pair rotates when
+// |g_p . g_q| > 3e-5 ||g_p|| ||g_q|| (above FP32 rounding noise); sweeps stop when no pair rotates
+// (at most 12).
+__global__ void __launch_bounds__(1024) k_jacobi1_f32(int n, const double* __restrict__ Gin, int ldg, int trans,
+                                                      double* __restrict__ Vout) {
+  extern __shared__ float sm1[];
+  const int ld = n + 1;
+  float* G = sm1;
+  float* V = sm1 + n * ld;
+  __shared__ int s_any;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e % n, j = e / n;
+    G[i + j * ld] = (float)(trans ? Gin[j + (size_t)i * ldg] : Gin[i + (size_t)j * ldg]);
+    V[i + j * ld] = (i == j) ? 1.f : 0.f;
+  }
+  const int N = n + (n & 1), npair = N / 2;
+  const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  for (int sweep = 0; sweep < 12 && n > 1; ++sweep) {
+    if (tid == 0) s_any = 0;
+    __syncthreads();
+    int any = 0;
+    for (int r = 0; r < N - 1; ++r) {
+      for (int k = warp; k < npair; k += nw) {
+        int p = rr_idx(k, r, N), q = rr_idx(N - 1 - k, r, N);
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        if (q >= n) continue;
+        float a = 0.f, b = 0.f, g = 0.f;
+        for (int i = lane; i < n; i += 32) {
+          const float gp = G[i + p * ld], gq = G[i + q * ld];
+          a = fmaf(gp, gp, a);
+          b = fmaf(gq, gq, b);
+          g = fmaf(gp, gq, g);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          a += __shfl_xor_sync(0xffffffffu, a, o);
+          b += __shfl_xor_sync(0xffffffffu, b, o);
+          g += __shfl_xor_sync(0xffffffffu, g, o);
+        }
+        if (g != 0.f && fabsf(g) > 3e-5f * sqrtf(a * b)) {
+          any = 1;
+          const float zeta = (b - a) / (2.f * g);
+          const float t = (zeta >= 0.f) ? 1.f / (zeta + sqrtf(1.f + zeta * zeta)) : -1.f / (-zeta + sqrtf(1.f + zeta * zeta));
+          const float c = rsqrtf(1.f + t * t), sn = t * c;
+          for (int i = lane; i < n; i += 32) {
+            const float gp = G[i + p * ld], gq = G[i + q * ld];
+            G[i + p * ld] = c * gp - sn * gq;
+            G[i + q * ld] = sn * gp + c * gq;
+            const float vp = V[i + p * ld], vq = V[i + q * ld];
+            V[i + p * ld] = c * vp - sn * vq;
+            V[i + q * ld] = sn * vp + c * vq;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (any) s_any = 1;
+    __syncthreads();
+    if (!s_any) break;
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += nt) Vout[e] = (double)V[(e % n) + (e / n) * ld];
+}
+
 // ---- 4. Ogita-Aishima correction: from P = W'W and T = W'CW build lambda and F = I + E ------------
 // One thread per entry of F over a grid of CTAs; every CTA forms the n Rayleigh quotients itself.
 __global__ void __launch_bounds__(256) k_oa_correction(int n, const double* __restrict__ P, const double* __restrict__ T,
@@ -406,23 +478,18 @@ static int chol(ofrr_ctx* ctx, int n, int count, const double* const* Ms_host, i
   return OFRR_SUCCESS;
 }
 
-// eigen-decomposition of a symmetric C (n x n, FP64): W (orthonormal, columns sorted by descending
-// eigenvalue) and lam (descending)
-static int sym_eig_refined(ofrr_ctx* ctx, int n, const double* C, double* W, double* lam) {
+// Ogita-Aishima refinement of approximate eigenvectors W0 (n x n, overwritten) of a symmetric C
+// (FP64): W (orthonormal, columns sorted by descending eigenvalue) and lam (descending)
+static int eig_refine(ofrr_ctx* ctx, int n, const double* C, double* W0, double* W, double* lam, int steps) {
   WsScope scope(ctx);
   int st = OFRR_SUCCESS;
-  double *W0 = ws_get<double>(ctx, (size_t)n * n, &st), *W1 = ws_get<double>(ctx, (size_t)n * n, &st),
-         *P = ws_get<double>(ctx, (size_t)n * n, &st), *CW = ws_get<double>(ctx, (size_t)n * n, &st),
-         *T = ws_get<double>(ctx, (size_t)n * n, &st), *F = ws_get<double>(ctx, (size_t)n * n, &st),
-         *l0 = ws_get<double>(ctx, (size_t)n, &st);
-  if (!W0 || !W1 || !P || !CW || !T || !F || !l0) return st;
-  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(float);
-  OFRR_CUDA(cudaFuncSetAttribute(k_jacobi_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_jacobi_f32<<<1, 512, smem, ctx->stream>>>(n, C, n, W0, l0);
-  OFRR_LAUNCHED(ctx, "k_jacobi_f32");
+  double *W1 = ws_get<double>(ctx, (size_t)n * n, &st), *P = ws_get<double>(ctx, (size_t)n * n, &st),
+         *CW = ws_get<double>(ctx, (size_t)n * n, &st), *T = ws_get<double>(ctx, (size_t)n * n, &st),
+         *F = ws_get<double>(ctx, (size_t)n * n, &st), *l0 = ws_get<double>(ctx, (size_t)n, &st);
+  if (!W1 || !P || !CW || !T || !F || !l0) return st;
   double* Wc = W0;
   double* Wn = W1;
-  for (int it = 0; it < 2; ++it) {
+  for (int it = 0; it < steps; ++it) {
     OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, Wc, n, 0, 0.0, P, n));   // P = W'W
     OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, C, n, 0, Wc, n, 0, 0.0, CW, n));   // CW
     OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, CW, n, 0, 0.0, T, n));   // T = W'CW
@@ -442,8 +509,70 @@ static int sym_eig_refined(ofrr_ctx* ctx, int n, const double* C, double* W, dou
   return OFRR_SUCCESS;
 }
 
+// eigen-decomposition of a symmetric C (n x n, FP64): W (orthonormal, columns sorted by descending
+// eigenvalue) and lam (descending); FP32 two-sided Jacobi, then the FP64 refinement
+static int sym_eig_refined(ofrr_ctx* ctx, int n, const double* C, double* W, double* lam, int steps) {
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  double *W0 = ws_get<double>(ctx, (size_t)n * n, &st), *l0 = ws_get<double>(ctx, (size_t)n, &st);
+  if (!W0 || !l0) return st;
+  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(float);
+  OFRR_CUDA(cudaFuncSetAttribute(k_jacobi_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_jacobi_f32<<<1, 512, smem, ctx->stream>>>(n, C, n, W0, l0);
+  OFRR_LAUNCHED(ctx, "k_jacobi_f32");
+  return eig_refine(ctx, n, C, W0, W, lam, steps);
+}
+
+// unit 2-norm columns (n x n, ld n), one warp per column
+__global__ void k_unit_cols(int n, double* __restrict__ U) {
+  const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (w >= n) return;
+  double* u = U + (size_t)w * n;
+  double s = 0.0;
+  for (int i = lane; i < n; i += 32) s = fma(u[i], u[i], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  const double inv = (s > 0.0) ? 1.0 / sqrt(s) : 0.0;
+  for (int i = lane; i < n; i += 32) u[i] *= inv;
+}
+
+// eig(G, M) for a nonsymmetric G and SPD M (M null: eig(G)): lam = real parts, descending (stable);
+// U (ld n) the real parts of the eigenvectors, unit 2-norm.  M is reduced away with its FP64
+// Cholesky factor (C = L^-1 G L^-T, U = L^-T X); C is solved in FP32 (smalleig_nonsym.cu).
+int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U) {
+  if (n <= 0) return OFRR_SUCCESS;
+  if (n > 128) return OFRR_ERR_BLAS_INVALID_SIZE;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  double *L = ws_get<double>(ctx, (size_t)n * n, &st), *Z = ws_get<double>(ctx, (size_t)n * n, &st),
+         *C = ws_get<double>(ctx, (size_t)n * n, &st), *X = ws_get<double>(ctx, (size_t)n * n, &st),
+         *W = ws_get<double>(ctx, (size_t)n * n, &st), *wr = ws_get<double>(ctx, (size_t)n, &st),
+         *wi = ws_get<double>(ctx, (size_t)n, &st);
+  if (!L || !Z || !C || !X || !W || !wr || !wi) return st;
+  const double* Cs = G;
+  if (M) {
+    const double* Ms[1] = {M};
+    double* Ls[1] = {L};
+    OFRR_TRY(chol(ctx, n, 1, Ms, n, 0.0, Ls));
+    OFRR_TRY(trsm(ctx, n, n, L, G, n, 1, Z, 0));  // Z = L^-1 G'
+    OFRR_TRY(trsm(ctx, n, n, L, Z, n, 1, C, 0));  // C = L^-1 Z' = L^-1 G L^-T
+    Cs = C;
+  }
+  OFRR_TRY(nonsym_eig_dev(ctx, n, Cs, wr, wi, X));
+  if (M) {
+    OFRR_TRY(trsm(ctx, n, n, L, X, n, 0, W, 1));  // W = L^-T X
+    k_unit_cols<<<(n + 3) / 4, 128, 0, ctx->stream>>>(n, W);
+    OFRR_LAUNCHED(ctx, "k_unit_cols");
+  } else {
+    OFRR_CUDA(cudaMemcpyAsync(W, X, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  k_sort_desc<<<1, 256, 0, ctx->stream>>>(n, wr, W, lam, U);
+  OFRR_LAUNCHED(ctx, "k_sort_desc");
+  return OFRR_SUCCESS;
+}
+
 // eig(G, M + tau I) for symmetric G and SPD M: lam descending, U M-orthonormal (ldu = n)
-int geig_fast(ofrr_ctx* ctx, int n, const double* G, const double* M, double tau, double* lam, double* U) {
+int geig_fast(ofrr_ctx* ctx, int n, const double* G, const double* M, double tau, double* lam, double* U,
+              int refine) {
   if (n <= 0) return OFRR_SUCCESS;
   if (n > 128) return OFRR_ERR_BLAS_INVALID_SIZE;
   WsScope scope(ctx);
@@ -460,7 +589,7 @@ int geig_fast(ofrr_ctx* ctx, int n, const double* G, const double* M, double tau
   } else {
     OFRR_CUDA(cudaMemcpyAsync(C, G, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, ctx->stream));
   }
-  OFRR_TRY(sym_eig_refined(ctx, n, C, W, lam));
+  OFRR_TRY(sym_eig_refined(ctx, n, C, W, lam, refine));
   if (M) {
     OFRR_TRY(trsm(ctx, n, n, L, W, n, 0, U, 1));  // U = L^-T W
   } else {
@@ -472,7 +601,7 @@ int geig_fast(ofrr_ctx* ctx, int n, const double* G, const double* M, double tau
 // SVD pencil of svd_rr.m: returns sigma (descending) and the coefficient matrices Zf = Lu^-T Y,
 // Wf = Lv^-T X such that U Zf, V Wf are the (unit-norm in the Gram metrics) singular vectors.
 int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const double* VV, double tau, double* sigma,
-              double* Zf, double* Wf) {
+              double* Zf, double* Wf, int refine) {
   if (b <= 0) return OFRR_SUCCESS;
   if (b > 128) return OFRR_ERR_BLAS_INVALID_SIZE;
   WsScope scope(ctx);
@@ -490,7 +619,15 @@ int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const dou
   OFRR_TRY(trsm(ctx, b, b, Lv, T1, b, 1, C, 0));   // C' = Lv^-1 T1'  -> C holds (Lu^-1 B Lv^-T)'
   // S = C'C with C = (stored)' : S = stored * stored'
   OFRR_TRY(gemm_small(ctx, b, b, b, 1.0, C, b, 0, C, b, 1, 0.0, S, b));
-  OFRR_TRY(sym_eig_refined(ctx, b, S, X, lam));    // right singular vectors X, sigma^2
+  {  // starting vectors: FP32 one-sided Jacobi on the columns of C (= rows of the stored matrix)
+    double* X0 = ws_get<double>(ctx, (size_t)b * b, &st);
+    if (!X0) return st;
+    const size_t smem = (size_t)2 * b * (b + 1) * sizeof(float);
+    OFRR_CUDA(cudaFuncSetAttribute(k_jacobi1_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_jacobi1_f32<<<1, 1024, smem, ctx->stream>>>(b, C, b, 1, X0);
+    OFRR_LAUNCHED(ctx, "k_jacobi1_f32");
+    OFRR_TRY(eig_refine(ctx, b, S, X0, X, lam, refine));  // right singular vectors X, sigma^2 (FP64)
+  }
   OFRR_TRY(gemm_small(ctx, b, b, b, 1.0, C, b, 1, X, b, 0, 0.0, CX, b));  // (true C) X
   k_svd_left<<<(b * b + 255) / 256, 256, 0, ctx->stream>>>(b, CX, lam, Y, sigma);
   OFRR_LAUNCHED(ctx, "k_svd_left");

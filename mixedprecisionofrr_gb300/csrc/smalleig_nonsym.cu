@@ -1,0 +1,470 @@
+// Small nonsymmetric projected eigenproblems: eig(G, M + tau I) for the Krylov Rayleigh-Ritz step of
+// arnoldi_hess_eig.m:93-95 (eig_rr.m:52-55 with a nonsymmetric operator) and for the upper
+// Hessenberg matrix of the orthogonal Arnoldi comparison path (arnoldi_mgs_eig.m:95-100).
+//
+// The pencil is reduced to a standard problem with the FP64 Cholesky factor of M + tau I
+// (C = L^-1 G L^-T, smalleig_fast.cu's kernels); C is then solved in FP32 on one warp by the
+// classical dense algorithm: Householder reduction to upper Hessenberg form with the
+// transformations accumulated, Francis double-shift QR iteration to real Schur form (with the
+// EISPACK/JAMA exceptional shifts at 10 and 30 iterations), and back substitution on the
+// quasi-triangular factor for the eigenvectors (complex pairs in real arithmetic).  Scalar
+// decisions are computed redundantly by every lane from shared memory, so the whole warp follows
+// one control flow; the O(n) row and column updates are spread over the lanes.  The eigenvectors
+// of the quasi-triangular factor are found one per lane (each lane owns one eigenvalue).
+//
+// Outputs follow the oracle's convention for real arithmetic: eigenvalues are the real parts, an
+// eigenvector of a complex pair is the real part of the complex eigenvector, every vector has unit
+// 2-norm, and pairs are sorted by descending real part (stable).  Accuracy is FP32 relative to
+// ||C||; the callers are the 16-bit/32-bit Krylov bases of the mixed schedule.
+#include "ofrr_internal.cuh"
+
+namespace ofrr {
+
+constexpr int NS_MAX = 128;
+
+__device__ __forceinline__ void cdivf(float xr, float xi, float yr, float yi, float& cr, float& ci) {
+  float r, d;
+  if (fabsf(yr) > fabsf(yi)) {
+    r = yi / yr;
+    d = yr + r * yi;
+    cr = (xr + r * xi) / d;
+    ci = (xi - r * xr) / d;
+  } else {
+    r = yr / yi;
+    d = yi + r * yr;
+    cr = (r * xr + xi) / d;
+    ci = (r * xi - xr) / d;
+  }
+}
+
+// One warp.  C: n x n (FP64, ld ldc).  Outputs: wr, wi (n), X (n x n, FP64, ld n): eigenvectors of C
+// (real parts, unit norm), unsorted; *flag = 1 when the QR iteration did not converge.
+__global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __restrict__ C, int ldc,
+                                                       double* __restrict__ wr, double* __restrict__ wi,
+                                                       double* __restrict__ X, int* __restrict__ flag) {
+  extern __shared__ float sm[];
+  const int ld = nn + 1;
+  float* H = sm;             // n x n (row i, column j at i + j * ld)
+  float* V = H + nn * ld;    // Schur vectors
+  float* Y = V + nn * ld;    // eigenvectors of the quasi-triangular factor
+  float* ort = Y + nn * ld;  // n
+  float* d = ort + nn;       // n
+  float* e = d + nn;         // n
+  const int lane = threadIdx.x;
+#define HH(i, j) H[(i) + (j) * ld]
+#define VV(i, j) V[(i) + (j) * ld]
+#define YY(i, j) Y[(i) + (j) * ld]
+  for (int idx = lane; idx < nn * nn; idx += 32) {
+    const int i = idx % nn, j = idx / nn;
+    HH(i, j) = (float)C[i + (size_t)j * ldc];
+    VV(i, j) = (i == j) ? 1.f : 0.f;
+    YY(i, j) = 0.f;
+  }
+  __syncwarp();
+  const int low = 0, high = nn - 1;
+  // ---- Householder reduction to upper Hessenberg form ----
+  for (int m = low + 1; m <= high - 1; ++m) {
+    float scale = 0.f;
+    for (int i = m + lane; i <= high; i += 32) scale += fabsf(HH(i, m - 1));
+    for (int o = 16; o > 0; o >>= 1) scale += __shfl_xor_sync(0xffffffffu, scale, o);
+    if (scale == 0.f) continue;
+    float h = 0.f;
+    for (int i = m + lane; i <= high; i += 32) {
+      ort[i] = HH(i, m - 1) / scale;
+      h += ort[i] * ort[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    __syncwarp();
+    float g = sqrtf(h);
+    if (ort[m] > 0.f) g = -g;
+    h = h - ort[m] * g;
+    __syncwarp();
+    if (lane == 0) ort[m] = ort[m] - g;
+    __syncwarp();
+    // H = (I - u u'/h) H (I - u u'/h)
+    for (int j = m + lane; j < nn; j += 32) {
+      float f = 0.f;
+      for (int i = high; i >= m; --i) f += ort[i] * HH(i, j);
+      f /= h;
+      for (int i = m; i <= high; ++i) HH(i, j) -= f * ort[i];
+    }
+    __syncwarp();
+    for (int i = lane; i <= high; i += 32) {
+      float f = 0.f;
+      for (int j = high; j >= m; --j) f += ort[j] * HH(i, j);
+      f /= h;
+      for (int j = m; j <= high; ++j) HH(i, j) -= f * ort[j];
+    }
+    __syncwarp();
+    if (lane == 0) {
+      ort[m] = scale * ort[m];
+      HH(m, m - 1) = scale * g;
+    }
+    __syncwarp();
+  }
+  // accumulate the transformations (the reflectors below the subdiagonal and in ort)
+  for (int m = high - 1; m >= low + 1; --m) {
+    if (HH(m, m - 1) == 0.f) continue;
+    for (int i = m + 1 + lane; i <= high; i += 32) ort[i] = HH(i, m - 1);
+    __syncwarp();
+    for (int j = m + lane; j <= high; j += 32) {
+      float g = 0.f;
+      for (int i = m; i <= high; ++i) g += ort[i] * VV(i, j);
+      g = (g / ort[m]) / HH(m, m - 1);  // double division avoids underflow
+      for (int i = m; i <= high; ++i) VV(i, j) += g * ort[i];
+    }
+    __syncwarp();
+  }
+  for (int idx = lane; idx < nn * nn; idx += 32) {  // clear the reflector storage below the subdiagonal
+    const int i = idx % nn, j = idx / nn;
+    if (i > j + 1) HH(i, j) = 0.f;
+  }
+  __syncwarp();
+
+  // ---- Francis double-shift QR to real Schur form (EISPACK hqr2) ----
+  const float eps = 1.1920929e-07f;
+  int n = nn - 1;
+  float exshift = 0.f, p = 0.f, q = 0.f, r = 0.f, s = 0.f, z = 0.f, t, w, x, y;
+  float norm = 0.f;
+  for (int i = 0; i < nn; ++i)
+    for (int j = (i > 0 ? i - 1 : 0); j < nn; ++j) norm += fabsf(HH(i, j));
+  int iter = 0, total_iter = 0;
+  const int max_total = 40 * nn;
+  bool failed = false;
+  while (n >= low) {
+    int l = n;
+    while (l > low) {
+      s = fabsf(HH(l - 1, l - 1)) + fabsf(HH(l, l));
+      if (s == 0.f) s = norm;
+      if (fabsf(HH(l, l - 1)) < eps * s) break;
+      --l;
+    }
+    if (l == n) {  // one root
+      const float hn = HH(n, n) + exshift;
+      __syncwarp();
+      if (lane == 0) {
+        HH(n, n) = hn;
+        d[n] = hn;
+        e[n] = 0.f;
+      }
+      __syncwarp();
+      --n;
+      iter = 0;
+    } else if (l == n - 1) {  // two roots
+      w = HH(n, n - 1) * HH(n - 1, n);
+      p = (HH(n - 1, n - 1) - HH(n, n)) / 2.f;
+      q = p * p + w;
+      z = sqrtf(fabsf(q));
+      const float hnn = HH(n, n) + exshift, hmm = HH(n - 1, n - 1) + exshift;
+      __syncwarp();
+      if (lane == 0) {
+        HH(n, n) = hnn;
+        HH(n - 1, n - 1) = hmm;
+      }
+      __syncwarp();
+      x = hnn;
+      if (q >= 0.f) {  // real pair
+        z = (p >= 0.f) ? p + z : p - z;
+        const float dn1 = x + z;
+        const float dn = (z != 0.f) ? x - w / z : dn1;
+        x = HH(n, n - 1);
+        s = fabsf(x) + fabsf(z);
+        p = x / s;
+        q = z / s;
+        r = sqrtf(p * p + q * q);
+        p /= r;
+        q /= r;
+        __syncwarp();
+        if (lane == 0) {
+          d[n - 1] = dn1;
+          d[n] = dn;
+          e[n - 1] = 0.f;
+          e[n] = 0.f;
+        }
+        for (int j = n - 1 + lane; j < nn; j += 32) {  // row modification
+          const float zz = HH(n - 1, j);
+          HH(n - 1, j) = q * zz + p * HH(n, j);
+          HH(n, j) = q * HH(n, j) - p * zz;
+        }
+        __syncwarp();
+        for (int i = lane; i <= n; i += 32) {  // column modification
+          const float zz = HH(i, n - 1);
+          HH(i, n - 1) = q * zz + p * HH(i, n);
+          HH(i, n) = q * HH(i, n) - p * zz;
+        }
+        for (int i = low + lane; i <= high; i += 32) {  // accumulate
+          const float zz = VV(i, n - 1);
+          VV(i, n - 1) = q * zz + p * VV(i, n);
+          VV(i, n) = q * VV(i, n) - p * zz;
+        }
+        __syncwarp();
+      } else {  // complex pair
+        __syncwarp();
+        if (lane == 0) {
+          d[n - 1] = x + p;
+          d[n] = x + p;
+          e[n - 1] = z;
+          e[n] = -z;
+        }
+        __syncwarp();
+      }
+      n -= 2;
+      iter = 0;
+    } else {  // no convergence yet: one double-shift step
+      if (++total_iter > max_total) {
+        failed = true;
+        break;
+      }
+      x = HH(n, n);
+      y = 0.f;
+      w = 0.f;
+      if (l < n) {
+        y = HH(n - 1, n - 1);
+        w = HH(n, n - 1) * HH(n - 1, n);
+      }
+      if (iter == 10) {  // Wilkinson's ad hoc shift
+        exshift += x;
+        __syncwarp();
+        for (int i = low + lane; i <= n; i += 32) HH(i, i) -= x;
+        __syncwarp();
+        s = fabsf(HH(n, n - 1)) + fabsf(HH(n - 1, n - 2));
+        x = y = 0.75f * s;
+        w = -0.4375f * s * s;
+      }
+      if (iter == 30) {  // the second ad hoc shift
+        s = (y - x) / 2.f;
+        s = s * s + w;
+        if (s > 0.f) {
+          s = sqrtf(s);
+          if (y < x) s = -s;
+          s = x - w / ((y - x) / 2.f + s);
+          __syncwarp();
+          for (int i = low + lane; i <= n; i += 32) HH(i, i) -= s;
+          __syncwarp();
+          exshift += s;
+          x = y = w = 0.964f;
+        }
+      }
+      ++iter;
+      // two consecutive small subdiagonal elements
+      int m = n - 2;
+      while (m >= l) {
+        z = HH(m, m);
+        r = x - z;
+        s = y - z;
+        p = (r * s - w) / HH(m + 1, m) + HH(m, m + 1);
+        q = HH(m + 1, m + 1) - z - r - s;
+        r = HH(m + 2, m + 1);
+        s = fabsf(p) + fabsf(q) + fabsf(r);
+        p /= s;
+        q /= s;
+        r /= s;
+        if (m == l) break;
+        if (fabsf(HH(m, m - 1)) * (fabsf(q) + fabsf(r)) <
+            eps * (fabsf(p) * (fabsf(HH(m - 1, m - 1)) + fabsf(z) + fabsf(HH(m + 1, m + 1)))))
+          break;
+        --m;
+      }
+      __syncwarp();
+      for (int i = m + 2 + lane; i <= n; i += 32) {
+        HH(i, i - 2) = 0.f;
+        if (i > m + 2) HH(i, i - 3) = 0.f;
+      }
+      __syncwarp();
+      // double QR step on rows l..n and columns m..n
+      for (int k = m; k <= n - 1; ++k) {
+        const bool notlast = (k != n - 1);
+        if (k != m) {
+          p = HH(k, k - 1);
+          q = HH(k + 1, k - 1);
+          r = notlast ? HH(k + 2, k - 1) : 0.f;
+          x = fabsf(p) + fabsf(q) + fabsf(r);
+          if (x == 0.f) continue;
+          p /= x;
+          q /= x;
+          r /= x;
+        }
+        s = sqrtf(p * p + q * q + r * r);
+        if (p < 0.f) s = -s;
+        if (s == 0.f) continue;
+        const float hk = (k != m) ? -s * x : ((l != m) ? -HH(k, k - 1) : 0.f);
+        const bool set_hk = (k != m) || (l != m);
+        p = p + s;
+        x = p / s;
+        y = q / s;
+        z = r / s;
+        q = q / p;
+        r = r / p;
+        __syncwarp();
+        if (lane == 0 && set_hk) HH(k, k - 1) = hk;
+        for (int j = k + lane; j < nn; j += 32) {  // row modification
+          float pp = HH(k, j) + q * HH(k + 1, j);
+          if (notlast) {
+            pp += r * HH(k + 2, j);
+            HH(k + 2, j) -= pp * z;
+          }
+          HH(k, j) -= pp * x;
+          HH(k + 1, j) -= pp * y;
+        }
+        __syncwarp();
+        const int imax = (n < k + 3) ? n : k + 3;
+        for (int i = lane; i <= imax; i += 32) {  // column modification
+          float pp = x * HH(i, k) + y * HH(i, k + 1);
+          if (notlast) {
+            pp += z * HH(i, k + 2);
+            HH(i, k + 2) -= pp * r;
+          }
+          HH(i, k) -= pp;
+          HH(i, k + 1) -= pp * q;
+        }
+        for (int i = low + lane; i <= high; i += 32) {  // accumulate
+          float pp = x * VV(i, k) + y * VV(i, k + 1);
+          if (notlast) {
+            pp += z * VV(i, k + 2);
+            VV(i, k + 2) -= pp * r;
+          }
+          VV(i, k) -= pp;
+          VV(i, k + 1) -= pp * q;
+        }
+        __syncwarp();
+      }
+    }
+  }
+  if (failed) {
+    if (lane == 0 && flag) *flag = 1;
+    for (int i = lane; i < nn; i += 32) {
+      wr[i] = 0.0;
+      wi[i] = 0.0;
+    }
+    for (int idx = lane; idx < nn * nn; idx += 32) X[idx] = 0.0;
+    return;
+  }
+  __syncwarp();
+  // ---- eigenvectors of the quasi-triangular factor: one lane per eigenvalue ----
+  if (norm != 0.f) {
+    for (int nv = nn - 1 - lane; nv >= 0; nv -= 32) {
+      const float pr = d[nv], qi = e[nv];
+      if (qi == 0.f) {  // real vector
+        int l = nv;
+        YY(nv, nv) = 1.f;
+        float zs = 0.f, ss = 0.f;
+        for (int i = nv - 1; i >= 0; --i) {
+          const float ww = HH(i, i) - pr;
+          float rr = 0.f;
+          for (int j = l; j <= nv; ++j) rr += HH(i, j) * YY(j, nv);
+          if (e[i] < 0.f) {
+            zs = ww;
+            ss = rr;
+          } else {
+            l = i;
+            if (e[i] == 0.f) {
+              YY(i, nv) = (ww != 0.f) ? -rr / ww : -rr / (eps * norm);
+            } else {  // real 2x2 block
+              const float xx = HH(i, i + 1), yy = HH(i + 1, i);
+              const float qq = (d[i] - pr) * (d[i] - pr) + e[i] * e[i];
+              const float tt = (xx * ss - zs * rr) / qq;
+              YY(i, nv) = tt;
+              YY(i + 1, nv) = (fabsf(xx) > fabsf(zs)) ? (-rr - ww * tt) / xx : (-ss - yy * tt) / zs;
+            }
+            const float tt = fabsf(YY(i, nv));
+            if ((eps * tt) * tt > 1.f)
+              for (int j = i; j <= nv; ++j) YY(j, nv) /= tt;
+          }
+        }
+      } else if (qi < 0.f) {  // complex vector: columns nv-1 (real part) and nv (imaginary part)
+        int l = nv - 1;
+        if (fabsf(HH(nv, nv - 1)) > fabsf(HH(nv - 1, nv))) {
+          YY(nv - 1, nv - 1) = qi / HH(nv, nv - 1);
+          YY(nv - 1, nv) = -(HH(nv, nv) - pr) / HH(nv, nv - 1);
+        } else {
+          float cr, ci;
+          cdivf(0.f, -HH(nv - 1, nv), HH(nv - 1, nv - 1) - pr, qi, cr, ci);
+          YY(nv - 1, nv - 1) = cr;
+          YY(nv - 1, nv) = ci;
+        }
+        YY(nv, nv - 1) = 0.f;
+        YY(nv, nv) = 1.f;
+        float zs = 0.f, rs = 0.f, ss = 0.f;
+        for (int i = nv - 2; i >= 0; --i) {
+          float ra = 0.f, sa = 0.f;
+          for (int j = l; j <= nv; ++j) {
+            ra += HH(i, j) * YY(j, nv - 1);
+            sa += HH(i, j) * YY(j, nv);
+          }
+          const float ww = HH(i, i) - pr;
+          if (e[i] < 0.f) {
+            zs = ww;
+            rs = ra;
+            ss = sa;
+          } else {
+            l = i;
+            float cr, ci;
+            if (e[i] == 0.f) {
+              cdivf(-ra, -sa, ww, qi, cr, ci);
+              YY(i, nv - 1) = cr;
+              YY(i, nv) = ci;
+            } else {
+              const float xx = HH(i, i + 1), yy = HH(i + 1, i);
+              float vr = (d[i] - pr) * (d[i] - pr) + e[i] * e[i] - qi * qi;
+              const float vi = (d[i] - pr) * 2.f * qi;
+              if (vr == 0.f && vi == 0.f)
+                vr = eps * norm * (fabsf(ww) + fabsf(qi) + fabsf(xx) + fabsf(yy) + fabsf(zs));
+              cdivf(xx * rs - zs * ra + qi * sa, xx * ss - zs * sa - qi * ra, vr, vi, cr, ci);
+              YY(i, nv - 1) = cr;
+              YY(i, nv) = ci;
+              if (fabsf(xx) > fabsf(zs) + fabsf(qi)) {
+                YY(i + 1, nv - 1) = (-ra - ww * YY(i, nv - 1) + qi * YY(i, nv)) / xx;
+                YY(i + 1, nv) = (-sa - ww * YY(i, nv) - qi * YY(i, nv - 1)) / xx;
+              } else {
+                cdivf(-rs - yy * YY(i, nv - 1), -ss - yy * YY(i, nv), zs, qi, cr, ci);
+                YY(i + 1, nv - 1) = cr;
+                YY(i + 1, nv) = ci;
+              }
+            }
+            const float tt = fmaxf(fabsf(YY(i, nv - 1)), fabsf(YY(i, nv)));
+            if ((eps * tt) * tt > 1.f)
+              for (int j = i; j <= nv; ++j) {
+                YY(j, nv - 1) /= tt;
+                YY(j, nv) /= tt;
+              }
+          }
+        }
+      }
+    }
+  }
+  __syncwarp();
+  // ---- back transformation X = V Y (upper part of Y), real parts, unit norm ----
+  for (int j = lane; j < nn; j += 32) {
+    // the vector for eigenvalue j: column j, or for the second member of a complex pair the real part
+    // (column j - 1) of the pair's vector
+    const int src = (e[j] < 0.f) ? j - 1 : j;
+    const int top = (e[j] != 0.f) ? ((e[j] > 0.f) ? j + 1 : j) : j;  // last nonzero row of column src
+    float nrm = 0.f;
+    for (int i = 0; i < nn; ++i) {
+      float zz = 0.f;
+      for (int k = 0; k <= top; ++k) zz += VV(i, k) * YY(k, src);
+      nrm += zz * zz;
+      X[i + (size_t)j * nn] = (double)zz;
+    }
+    const double inv = (nrm > 0.f) ? 1.0 / sqrt((double)nrm) : 0.0;
+    for (int i = 0; i < nn; ++i) X[i + (size_t)j * nn] *= inv;
+    wr[j] = (double)d[j];
+    wi[j] = (double)e[j];
+  }
+#undef HH
+#undef VV
+#undef YY
+}
+
+// eig(C) for a nonsymmetric n x n C (FP64, ld n): wr/wi (n), X (n x n, ld n), unsorted
+int nonsym_eig_dev(ofrr_ctx* ctx, int n, const double* C, double* wr, double* wi, double* X) {
+  if (n <= 0) return OFRR_SUCCESS;
+  if (n > NS_MAX) return OFRR_ERR_BLAS_INVALID_SIZE;
+  const size_t smem = ((size_t)3 * n * (n + 1) + 3 * (size_t)n) * sizeof(float);
+  OFRR_CUDA(cudaFuncSetAttribute(k_nonsym_eig_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_nonsym_eig_f32<<<1, 32, smem, ctx->stream>>>(n, C, n, wr, wi, X, ctx->dev_flags + 3);
+  OFRR_LAUNCHED(ctx, "k_nonsym_eig_f32");
+  return OFRR_SUCCESS;
+}
+
+}  // namespace ofrr

@@ -18,6 +18,9 @@ namespace ofrr {
 
 int hess_krylov_first(ofrr_ctx* ctx, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int ncolmax, void* V, int64_t ldv,
                       double select_tol, int* select, int* perm, void* pivrows, void* pvals, double* R, int* stop);
+size_t mgs_scratch_bytes();
+int mgs_step(ofrr_ctx* ctx, ofrr_dtype po, ofrr_dtype pc, int64_t n, int i, void* V, int64_t ldv, bool reorth,
+             double stol, int* stop, void* scratch);
 int hess_krylov_step(ofrr_ctx* ctx, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int ncolmax, int i, void* V,
                      int64_t ldv, double select_tol, int* select, int* perm, void* pivrows, void* pvals, double* R,
                      int* stop);
@@ -156,7 +159,9 @@ int compact_columns(ofrr_ctx* ctx, ofrr_dtype t, int64_t m, void* Q, int64_t ldq
 
 struct Precisions {
   ofrr_dtype pc, po, phc, pho, prc, pro;
-  bool fast = false;  // production modes: refined FP32/FP64 small solver instead of the FP64 Jacobi
+  bool fast = false;  // production modes: FP32 Jacobi + FP64 refinement small solver, FMA/reciprocal FP64
+                      // Hessenberg and column scaling
+  int refine = 2;     // FP64 refinement steps of the small solver (0 for 16-bit bases)
 };
 
 Precisions precisions_of(const ofrr_options* o) {
@@ -212,7 +217,7 @@ int validate_op(const ofrr_operator* A) {
 // ---------------------------------------------------------------------------------------
 int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype tq, int64_t ldq, int b,
                ofrr_dtype pmc, ofrr_dtype pmo, ofrr_dtype pAmc, ofrr_dtype pAmo, bool use_gen, double gtol,
-               bool symmetric, void* Vout, int64_t ldvo, double* d, bool fast = false) {
+               bool symmetric, void* Vout, int64_t ldvo, double* d, bool fast = false, int refine = 2) {
   WsScope scope(ctx);
   int st = OFRR_SUCCESS;
   const int64_t n = op.m();
@@ -251,7 +256,9 @@ int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype t
     }
   }
   if (fast && symmetric && b <= 128) {
-    OFRR_TRY(geig_fast(ctx, b, G, M, use_gen ? gtol : 0.0, d, U));
+    OFRR_TRY(geig_fast(ctx, b, G, M, use_gen ? gtol : 0.0, d, U, refine));
+  } else if (!symmetric && b <= 128) {
+    OFRR_TRY(geig_nonsym(ctx, b, G, M, d, U));  // M already holds VV + gtol I
   } else {
     OFRR_TRY(geig_dev(ctx, b, G, b, M, b, symmetric ? 1 : 0, d, U, b));
   }
@@ -433,7 +440,8 @@ __global__ void k_build_aug(int b, const double* B, const double* UU, const doub
 
 int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* V, ofrr_dtype tq, int64_t ldu,
                int64_t ldv, int b, ofrr_dtype pmc, ofrr_dtype pmo, ofrr_dtype pAmc, ofrr_dtype pAmo, bool use_gen,
-               double gtol, void* Uout, int64_t lduo, void* Vout, int64_t ldvo, double* s_dev, bool fast = false) {
+               double gtol, void* Uout, int64_t lduo, void* Vout, int64_t ldvo, double* s_dev, bool fast = false,
+               int refine = 2) {
   WsScope scope(ctx);
   int st = OFRR_SUCCESS;
   const int64_t m = op.m(), n = op.n();
@@ -472,7 +480,7 @@ int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* 
     double *Zf, *Wf;
     OFRR_TRY(dmalloc(ctx, &Zf, (size_t)b * b));
     OFRR_TRY(dmalloc(ctx, &Wf, (size_t)b * b));
-    OFRR_TRY(gsvd_fast(ctx, b, B, UU, VV, gtol, s_dev, Zf, Wf));
+    OFRR_TRY(gsvd_fast(ctx, b, B, UU, VV, gtol, s_dev, Zf, Wf, refine));
     void* Uo = Uout;
     void* Vo = Vout;
     int64_t lu = lduo, lv = ldvo;
@@ -628,7 +636,8 @@ extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofr
   OFRR_TRY(validate_op(A));
   OFRR_TRY(validate_options(opt));
   if (A->nrows != A->ncols) return OFRR_ERR_BLAS_INVALID_SIZE;
-  if (opt->orth != OFRR_ORTH_HESSENBERG) return OFRR_ERR_NOT_IMPLEMENTED;
+  if (opt->orth != OFRR_ORTH_HESSENBERG && opt->orth != OFRR_ORTH_MGS) return OFRR_ERR_INVALID_ARGUMENT;
+  const bool mgs = opt->orth == OFRR_ORTH_MGS;
   const int64_t n = A->nrows;
   const int kdim = opt->kdim > 0 ? opt->kdim : opt->maxiter;
   const int nev = (int)std::min<int64_t>(opt->nev, n);
@@ -655,6 +664,11 @@ extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofr
   OFRR_TRY(dmalloc(ctx, &sel, (size_t)nb));
   OFRR_TRY(dmalloc(ctx, &perm, (size_t)nb));
   OFRR_TRY(dmalloc(ctx, &stop, (size_t)4));
+  void* mscratch = nullptr;
+  if (mgs) {
+    if (!(mscratch = ws_alloc(ctx, mgs_scratch_bytes(), &st))) return st;
+    OFRR_TRY(fill_zero(ctx, mscratch, mgs_scratch_bytes()));
+  }
   OFRR_TRY(fill_zero(ctx, V, (size_t)n * nb * dtype_size(po)));
   if (opt->use_start_block) {
     OFRR_CUDA(cudaMemcpyAsync(V, v0, (size_t)n * dtype_size(po), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -667,8 +681,14 @@ extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofr
   int ncols_final = 0;
   bool have_result = false;
   while (tits < opt->maxiter) {
-    // column 0: pivot + scale; break if |pivot| < select_tol (arnoldi_hess_eig.m:64-71)
-    OFRR_TRY(hess_krylov_first(ctx, po, pc, n, nb, V, n, stol, sel, perm, pivrows, pvals, R, stop));
+    // column 0: pivot + scale (Hessenberg, arnoldi_hess_eig.m:64-71) or normalise (MGS,
+    // arnoldi_mgs_eig.m:60-65); break if the pivot / norm is below select_tol
+    if (mgs) {
+      OFRR_CUDA(cudaMemsetAsync(stop, 0xFF, 2 * sizeof(int), ctx->stream));
+      OFRR_TRY(mgs_step(ctx, po, pc, n, 0, V, n, opt->reorth != 0, stol, stop, mscratch));
+    } else {
+      OFRR_TRY(hess_krylov_first(ctx, po, pc, n, nb, V, n, stol, sel, perm, pivrows, pvals, R, stop));
+    }
     OFRR_CUDA(cudaMemcpyAsync(hstop, stop, sizeof(int) * 2, cudaMemcpyDeviceToHost, ctx->stream));
     OFRR_TRY(sync_and_check(ctx));
     if (hstop[0] >= 0) break;  // start vector below select_tol
@@ -677,8 +697,12 @@ extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofr
       // V(:,i) = po(matvec(A, pc(V(:,i-1)), pc, pc)); column i-1 was scaled by the previous step
       OFRR_TRY(op.apply(ctx, 0, po, po, (char*)V + (size_t)(i - 1) * n * dtype_size(po), n, 1, pc, po,
                         (char*)V + (size_t)i * n * dtype_size(po), n));
-      OFRR_TRY(hess_krylov_step(ctx, po, pc, n, nb, i, V, n, stol, sel, perm, pivrows, pvals, R, stop));
-      OFRR_TRY(hess_scale_col(ctx, po, pc, n, i, V, n, sel, pvals, stop));
+      if (mgs) {
+        OFRR_TRY(mgs_step(ctx, po, pc, n, i, V, n, opt->reorth != 0, stol, stop, mscratch));
+      } else {
+        OFRR_TRY(hess_krylov_step(ctx, po, pc, n, nb, i, V, n, stol, sel, perm, pivrows, pvals, R, stop));
+        OFRR_TRY(hess_scale_col(ctx, po, pc, n, i, V, n, sel, pvals, stop));
+      }
     }
     OFRR_CUDA(cudaMemcpyAsync(hstop, stop, sizeof(int) * 2, cudaMemcpyDeviceToHost, ctx->stream));
     OFRR_TRY(sync_and_check(ctx));
@@ -692,8 +716,10 @@ extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofr
     }
     nmv += steps;
     cycles++;
-    // RR on the ncols columns (generalized, eig_rr.m with use_generalized = true)
-    OFRR_TRY(rr_eig_dev(ctx, op, po, V, po, n, ncols, pc, po, pc, pc, true, opt->generalized_tol, symmetric, Vr, n, d));
+    // RR on the ncols columns: generalized for the oblique Hessenberg basis (arnoldi_hess_eig.m:93),
+    // as the options say for the orthonormal MGS basis (arnoldi_mgs_eig.m:95-100)
+    OFRR_TRY(rr_eig_dev(ctx, op, po, V, po, n, ncols, pc, po, pc, pc, mgs ? opt->use_generalized != 0 : true,
+                        opt->generalized_tol, symmetric, Vr, n, d));
     nmv += ncols;
     ncols_final = ncols;
     have_result = true;
@@ -816,12 +842,12 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
     int64_t lddst = (cur == V) ? ldv : n;
     if (P.pho == P.po) {
       OFRR_TRY(rr_eig_dev(ctx, op, P.po, Q, P.pho, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
-                          opt->generalized_tol, symmetric, dst, lddst, d_dev, P.fast));
+                          opt->generalized_tol, symmetric, dst, lddst, d_dev, P.fast, P.refine));
     } else {
       void* tmpv = ws_alloc(ctx, (size_t)n * b * dtype_size(P.pho), &st);
       if (!tmpv) return st;
       OFRR_TRY(rr_eig_dev(ctx, op, P.po, Q, P.pho, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
-                          opt->generalized_tol, symmetric, tmpv, n, d_dev, P.fast));
+                          opt->generalized_tol, symmetric, tmpv, n, d_dev, P.fast, P.refine));
       OFRR_TRY(cast_impl(ctx, P.pho, P.po, n, b, tmpv, n, dst, lddst));
     }
     S.nmv += b;
@@ -887,7 +913,7 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
     if (w == 0) return OFRR_ERR_SOLVER_DIVERGENCE;
     S.b = b = w;
     OFRR_TRY(rr_svd_dev(ctx, op, P.po, P1, Q1, P.pho, m, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
-                        opt->generalized_tol, Ut, m, Vt, n, d_dev, P.fast));
+                        opt->generalized_tol, Ut, m, Vt, n, d_dev, P.fast, P.refine));
     OFRR_TRY(cast_impl(ctx, P.pho, P.po, m, b, Ut, m, U, ldu));
     OFRR_TRY(cast_impl(ctx, P.pho, P.po, n, b, Vt, n, V, ldv));
     S.nmv += b;
@@ -918,6 +944,9 @@ Precisions mixed_low(const ofrr_options* o) {
   p.pc = p.phc = p.prc = OFRR_F32;  // FP32 accumulation
   p.pro = OFRR_F32;                 // Gram matrices kept in FP32 (not rounded to 16 bits), then FP64
   p.fast = true;
+  // one FP64 refinement step: the FP32 Jacobi vectors' errors (~3e-5 / relative gap) would otherwise
+  // leave ~1e-5 noise in the Ritz values that drive the stagnation test
+  p.refine = 1;
   return p;
 }
 Precisions all_f64() {

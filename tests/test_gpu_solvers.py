@@ -71,6 +71,58 @@ def test_rr_eig_vs_oracle(api, orc):
         assert np.min(cos) > 1 - 1e-9
 
 
+@pytest.mark.parametrize("gen", [False, True])
+def test_rr_eig_nonsymmetric_vs_oracle(api, orc, gen):
+    """Nonsymmetric projected pencils (convection-diffusion operator): FP32 Hessenberg-QR eigensolver
+    after the FP64 Cholesky reduction; Ritz values (real parts) within 1e-5 of ||C||."""
+    A = orc.convdiff_3d(6).toarray()  # n = 216, real spectrum
+    V = orc.randn_block(5, 216, 24)
+    Vg, d = api.eig_rr(A, V, "double", use_generalized=gen, generalized_tol=1e-10, symmetric=False)
+    Vo, do = orc.eig_rr(A, V, "double", use_generalized=gen, generalized_tol=1e-10, symmetric=False)
+    scale = np.max(np.abs(do))
+    assert np.max(np.abs(d - do)) <= 1e-5 * scale
+    # every Ritz pair satisfies the projected equation to FP32 accuracy: V'(A x - d x) ~ 0
+    X = api.to_numpy(Vg)
+    R = V.T @ (A @ X - X * d[None, :])
+    assert np.max(np.abs(R)) <= 1e-4 * scale * np.max(np.abs(V.T @ X))
+
+
+def test_rr_eig_nonsymmetric_complex_pairs(api, orc):
+    """A rotation-dominated operator with complex Ritz values: real parts match the oracle."""
+    rng = np.random.default_rng(11)
+    n = 120
+    B = rng.standard_normal((n, n))
+    A = B - B.T + np.diag(np.linspace(0.0, 1.0, n))  # skew part gives complex pairs
+    V = orc.randn_block(8, n, 40)
+    Vg, d = api.eig_rr(A, V, "double", use_generalized=False, symmetric=False)
+    Vo, do = orc.eig_rr(A, V, "double", use_generalized=False, symmetric=False)
+    assert np.max(np.abs(np.sort(d) - np.sort(do))) <= 1e-4 * np.max(np.abs(np.linalg.eigvals(V.T @ A @ V)))
+
+
+def test_arnoldi_hess_nonsymmetric_vs_oracle(api, orc):
+    """Hessenberg-process Krylov with restarts on the (nonsymmetric) convection-diffusion operator."""
+    A = orc.convdiff_3d(8)
+    Ac = orc.sparse2csr(A)
+    v0 = orc.randn_block(13, A.shape[0], 1)[:, 0]
+    X, d, info = api.arnoldi_hess_eig(api.CsrMatrix(A), A.shape[0], 4, "double", maxiter=61, kdim=30, v0=v0,
+                                      symmetric=False)
+    Xo, do, inf = orc.arnoldi_hess_eig(Ac, A.shape[0], 4, "double", maxiter=61, kdim=30, v0=v0, symmetric=False)
+    assert np.max(np.abs(d - do)) <= 1e-5 * np.max(np.abs(do))
+
+
+@pytest.mark.parametrize("symmetric", [True, False])
+def test_arnoldi_mgs_vs_oracle(api, orc, symmetric):
+    """Orthogonal MGS Arnoldi with re-orthogonalisation (the FP64 comparison path) on the GPU."""
+    A = orc.laplacian_2d(14) if symmetric else orc.convdiff_3d(7)
+    Ac = orc.sparse2csr(A)
+    v0 = orc.randn_block(17, A.shape[0], 1)[:, 0]
+    X, d, info = api.arnoldi_mgs_eig(api.CsrMatrix(A), A.shape[0], 4, "double", maxiter=41, kdim=20, v0=v0,
+                                     symmetric=symmetric)
+    Xo, do = orc.arnoldi_mgs_eig(Ac, A.shape[0], 4, "double", maxiter=41, kdim=20, v0=v0, symmetric=symmetric)
+    tol = 1e-10 if symmetric else 1e-5
+    assert np.max(np.abs(d - do)) <= tol * np.max(np.abs(do))
+
+
 def test_rr_svd_vs_oracle(api, orc):
     A, U, s, V = orc.dense_svd_problem(400, 80, seed=6, smin=1e-3)
     P = orc.randn_block(1, 400, 12)
@@ -111,6 +163,21 @@ def test_si_eig_laplacian_converges_fp64(api, orc):
     assert info.status == 0, info
     assert np.allclose(d[:8], orc.laplacian_2d_eigs(32)[:8], rtol=1e-9)
     assert np.max(info.residuals[:8]) <= 1e-10
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_si_eig_laplacian_c1_full(api, orc, mode):
+    """The C1 workload at full size: 64x64 Dirichlet Laplacian (n = 4096, CSR FP64), block 16, top 8,
+    tol 1e-10, against the analytic spectrum (the top 8 close a multiplet)."""
+    L = orc.laplacian_2d(64)
+    V, d, info = api.subspace_iter_eig(api.CsrMatrix(L), L.shape[0], 16, "double", maxiter=2000, step_size=8,
+                                      mode=mode, tol=1e-10, nev=8, check_every=10)
+    assert info.status == 0, info
+    assert np.allclose(d[:8], orc.laplacian_2d_eigs(64)[:8], rtol=1e-10)
+    assert np.max(info.residuals[:8]) <= 1e-10
+    X = api.to_numpy(V)[:, :8]
+    r = np.linalg.norm(L @ X - X * d[:8], axis=0) / np.linalg.norm(X, axis=0) / 8.0  # ||L|| < 8
+    assert np.max(r) <= 1e-10
 
 
 def test_si_svd_geometric_converges_fp64(api, orc):
