@@ -131,6 +131,14 @@ int ofrr_gemm(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
 int ofrr_gemm_f64_emulated(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda,
                            const double* B, int64_t ldb, double* C, int64_t ldc);
 
+/* Profiling form of ofrr_gemm_f64_emulated (no reference counterpart): slices A and B once, then
+ * runs the fused product kernel reps (>= 2) times and returns its mean time per launch (CUDA events
+ * on the context's stream, synchronous) and the kernel's algorithmic bytes per launch (digit stacks
+ * read once, partial results written once).  C holds A' B afterwards. */
+int ofrr_profile_gemm_f64_emulated(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda,
+                                   const double* B, int64_t ldb, double* C, int64_t ldc, int reps,
+                                   double* us_per_launch, double* bytes_per_launch);
+
 /* ---- sparse operator: CSR with value copies per precision ------------------------- *
  * Mirrors MATLAB/+src/+csr/sparse2csr.m:21-50 (0-based int32 here).  Any of the value
  * arrays may be NULL if that precision is never requested. */
@@ -287,6 +295,51 @@ int ofrr_hessenberg_noalloc(void* cuda_stream, ofrr_dtype tin, ofrr_dtype tout, 
                             int64_t n, const void* A /*dev*/, int64_t lda, void* Q /*dev*/, int64_t ldq,
                             double select_tol, double* R /*dev*/, int* select /*dev*/, int* perm /*dev*/);
 size_t ofrr_hessenberg_noalloc_scratch_bytes(void);
+
+/* ---- solve engine: batched solves and a serving queue ------------------------------- *
+ * No counterpart in the reference (its C++ solvers are stubs and it has no batch or serving
+ * layer).  An engine owns `workers` host threads, each with its own ofrr_ctx (stream, cuBLAS
+ * handle, cached workspace), so independent solves overlap on one GPU.  Requests run in FIFO
+ * order; each is charged an estimate of its device workspace against hbm_budget_bytes (0 = half
+ * of the free memory) and starts when the charge fits (a request larger than the budget runs
+ * alone).  The caller owns every buffer a request points to (operator data, outputs; host arrays
+ * for values/resid/info) and keeps them valid until the request has completed.  A ticket is
+ * released by ofrr_serve_wait.  Results do not depend on the other requests in flight. */
+typedef struct ofrr_serve ofrr_serve;
+typedef enum { OFRR_REQ_SI_EIG = 0, OFRR_REQ_SI_SVD = 1, OFRR_REQ_ARNOLDI_EIG = 2 } ofrr_request_kind;
+typedef struct {
+  int kind;               /* ofrr_request_kind */
+  ofrr_operator A;
+  ofrr_options opt;
+  void* V;                /* dev: si_eig V (in/out), si_svd V (out), arnoldi X (out) */
+  int64_t ldv;
+  void* U;                /* dev: si_svd U (out) */
+  int64_t ldu;
+  const void* v0;         /* dev: arnoldi start vector (opt.use_start_block) */
+  double* values;         /* host: eigen/singular values (block, or nev for arnoldi) */
+  double* resid;          /* host|NULL */
+  ofrr_info* info;        /* host|NULL */
+} ofrr_request;
+typedef struct {
+  uint64_t completed, failed, queued;
+  size_t charged_bytes, budget_bytes;
+  double wall_ms;         /* first submit to last completion */
+  double busy_ms;         /* summed solve time over workers */
+  double p50_ms, p99_ms;  /* submit-to-completion latency */
+} ofrr_serve_report;
+int ofrr_serve_create(ofrr_serve** engine, int device, int workers, size_t hbm_budget_bytes);
+int ofrr_serve_destroy(ofrr_serve* engine); /* finishes queued requests first */
+int ofrr_serve_submit(ofrr_serve* engine, const ofrr_request* request, uint64_t* ticket);
+int ofrr_serve_poll(ofrr_serve* engine, uint64_t ticket, int* done, int* status);
+int ofrr_serve_wait(ofrr_serve* engine, uint64_t ticket, int* status, double* latency_ms);
+int ofrr_serve_stats(ofrr_serve* engine, ofrr_serve_report* stats);
+/* count independent si_eig solves with shared options through the engine (submit all, wait all);
+ * per-problem status in statuses[i]; returns the first submission error, if any. */
+int ofrr_batch_si_eig(ofrr_serve* engine, int count, const ofrr_operator* ops, const ofrr_options* opt,
+                      void* const* V /*dev*/, const int64_t* ldv, double* const* evals /*host*/,
+                      double* const* resid /*host|NULL*/, ofrr_info* infos /*host|NULL*/, int* statuses);
+/* releases a context's cached workspace (no allocation of it may be live: call between solves) */
+int ofrr_ctx_trim(ofrr_ctx* ctx);
 
 #ifdef __cplusplus
 }

@@ -58,6 +58,20 @@ class ofrr_info(C.Structure):
 
 
 # name -> (restype, argtypes)
+class ofrr_request(C.Structure):
+    _fields_ = [("kind", C.c_int), ("A", ofrr_operator), ("opt", ofrr_options), ("V", C.c_void_p), ("ldv", C.c_int64),
+                ("U", C.c_void_p), ("ldu", C.c_int64), ("v0", C.c_void_p), ("values", C.POINTER(C.c_double)),
+                ("resid", C.POINTER(C.c_double)), ("info", C.POINTER(ofrr_info))]
+
+
+class ofrr_serve_report(C.Structure):
+    _fields_ = [("completed", C.c_uint64), ("failed", C.c_uint64), ("queued", C.c_uint64),
+                ("charged_bytes", C.c_size_t), ("budget_bytes", C.c_size_t), ("wall_ms", C.c_double),
+                ("busy_ms", C.c_double), ("p50_ms", C.c_double), ("p99_ms", C.c_double)]
+
+
+REQ_SI_EIG, REQ_SI_SVD, REQ_ARNOLDI_EIG = 0, 1, 2
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _D = C.c_double
@@ -86,6 +100,8 @@ SIGNATURES = {
     "ofrr_gemm": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _I64, _I64, _I64, _D,
                             _P, _I64, _P, _I64, _D, _P, _I64]),
     "ofrr_gemm_f64_emulated": (C.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64]),
+    "ofrr_profile_gemm_f64_emulated": (C.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, C.c_int,
+                                                  _DP, _DP]),
     "ofrr_csrmm": (C.c_int, [_P, C.POINTER(ofrr_csr), C.c_int, C.c_int, C.c_int, C.c_int, _I64, _P, _I64, _P,
                              _I64]),
     "ofrr_syev": (C.c_int, [_P, C.c_int, _P, C.c_int, _P]),
@@ -106,6 +122,15 @@ SIGNATURES = {
     "ofrr_hessenberg_noalloc": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _I64, _I64, _P, _I64, _P, _I64, _D, _P,
                                           _P, _P]),
     "ofrr_hessenberg_noalloc_scratch_bytes": (C.c_size_t, []),
+    "ofrr_serve_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_size_t]),
+    "ofrr_serve_destroy": (C.c_int, [_P]),
+    "ofrr_serve_submit": (C.c_int, [_P, C.POINTER(ofrr_request), C.POINTER(C.c_uint64)]),
+    "ofrr_serve_poll": (C.c_int, [_P, C.c_uint64, _IP, _IP]),
+    "ofrr_serve_wait": (C.c_int, [_P, C.c_uint64, _IP, _DP]),
+    "ofrr_serve_stats": (C.c_int, [_P, C.POINTER(ofrr_serve_report)]),
+    "ofrr_batch_si_eig": (C.c_int, [_P, C.c_int, C.POINTER(ofrr_operator), C.POINTER(ofrr_options), C.POINTER(_P),
+                                    C.POINTER(_I64), C.POINTER(_DP), C.POINTER(_DP), C.POINTER(ofrr_info), _IP]),
+    "ofrr_ctx_trim": (C.c_int, [_P]),
 }
 
 _lib = None

@@ -523,3 +523,114 @@ def residual_norms(A, X, lam, normA: float = -1.0, symmetric=None):
     L.check(ctx.lib.ofrr_residual_norms(ctx.h, C.byref(op.op), dtype_of(Xd), k, Xd.data_ptr(), ld_of(Xd), _dp(lam),
                                         normA, _dp(out)), "residual_norms")
     return out
+
+
+# ---- solve engine: batched solves and a serving queue -----------------------------------------
+class Server:
+    """Worker threads with one library context each; requests run concurrently on the GPU.
+
+    ``submit_si_eig`` / ``submit_si_svd`` return a ticket; ``wait(ticket)`` returns
+    (status, latency_ms) and the request's outputs (device tensors, host arrays).  The request's
+    operator and outputs are kept alive by the server until the ticket is collected."""
+
+    def __init__(self, workers: int = 4, hbm_budget_bytes: int = 0, device: Optional[int] = None):
+        self.lib = L.load()
+        torch.cuda.init()
+        h = C.c_void_p()
+        dev = torch.cuda.current_device() if device is None else device
+        L.check(self.lib.ofrr_serve_create(C.byref(h), dev, workers, hbm_budget_bytes), "ofrr_serve_create")
+        self.h = h
+        self._live = {}
+
+    def _submit(self, req, keep):
+        t = C.c_uint64()
+        L.check(self.lib.ofrr_serve_submit(self.h, C.byref(req), C.byref(t)), "ofrr_serve_submit")
+        self._live[t.value] = (req, keep)
+        return t.value
+
+    def submit_si_eig(self, A, k: int, mode: str = "mixed", tol: float = 1e-8, nev: Optional[int] = None,
+                      maxiter: int = 200, step_size: int = 4, p_output: str = "half", symmetric=None, seed: int = 42,
+                      check_every: int = 1):
+        op = operator(A, symmetric)
+        modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
+        o = options(mode=modes[mode], maxiter=maxiter, step_size=step_size, block=min(k, op.n), nev=nev or min(k, op.n),
+                    tol=tol, seed=seed, check_every=check_every, p_output=p_output if mode == "mixed" else None)
+        po = o.p_output if mode == "reference" else L.F64
+        V = empty_cm(op.m, o.block, po)
+        d = np.zeros(o.block)
+        res = np.zeros(o.block)
+        inf = L.ofrr_info()
+        req = L.ofrr_request(kind=L.REQ_SI_EIG, A=op.op, opt=o, V=V.data_ptr(), ldv=ld_of(V), values=_dp(d),
+                             resid=_dp(res), info=C.pointer(inf))
+        return self._submit(req, (op, V, d, res, inf))
+
+    def submit_si_svd(self, A, k: int, mode: str = "mixed", tol: float = 1e-8, nev: Optional[int] = None,
+                      maxiter: int = 200, step_size: int = 4, p_output: str = "half", seed: int = 42,
+                      check_every: int = 1):
+        op = operator(A, False)
+        modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
+        b = min(k, op.m, op.n)
+        o = options(mode=modes[mode], maxiter=maxiter, step_size=step_size, block=b, nev=nev or b, tol=tol, seed=seed,
+                    check_every=check_every, p_output=p_output if mode == "mixed" else None)
+        po = o.p_output if mode == "reference" else L.F64
+        U = empty_cm(op.m, b, po)
+        V = empty_cm(op.n, b, po)
+        sv = np.zeros(b)
+        res = np.zeros(b)
+        inf = L.ofrr_info()
+        req = L.ofrr_request(kind=L.REQ_SI_SVD, A=op.op, opt=o, V=V.data_ptr(), ldv=ld_of(V), U=U.data_ptr(),
+                             ldu=ld_of(U), values=_dp(sv), resid=_dp(res), info=C.pointer(inf))
+        return self._submit(req, (op, U, V, sv, res, inf))
+
+    def poll(self, ticket: int):
+        done, st = C.c_int(), C.c_int()
+        L.check(self.lib.ofrr_serve_poll(self.h, ticket, C.byref(done), C.byref(st)), "ofrr_serve_poll")
+        return bool(done.value), st.value
+
+    def wait(self, ticket: int):
+        """(status, latency_ms, outputs) with outputs the request's (operator, tensors..., values, resid, info)."""
+        st, lat = C.c_int(), C.c_double()
+        L.check(self.lib.ofrr_serve_wait(self.h, ticket, C.byref(st), C.byref(lat)), "ofrr_serve_wait")
+        req, keep = self._live.pop(ticket)
+        return st.value, lat.value, keep
+
+    def stats(self) -> dict:
+        r = L.ofrr_serve_report()
+        L.check(self.lib.ofrr_serve_stats(self.h, C.byref(r)), "ofrr_serve_stats")
+        return {k: getattr(r, k) for k, _ in r._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ofrr_serve_destroy(self.h)
+            self.h = None
+            self._live.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_si_eig(server: Server, As, k: int, mode: str = "mixed", tol: float = 1e-7, nev: Optional[int] = None,
+                 maxiter: int = 200, step_size: int = 4, p_output: str = "bfloat16", symmetric=True):
+    """Independent si_eig solves of every matrix in As with shared options (ofrr_batch_si_eig).
+    Returns (list of V, list of values, statuses)."""
+    ops = [operator(A, symmetric) for A in As]
+    cnt = len(ops)
+    modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
+    b = min([k] + [o.n for o in ops])
+    o = options(mode=modes[mode], maxiter=maxiter, step_size=step_size, block=b, nev=nev or b, tol=tol,
+                p_output=p_output if mode == "mixed" else None)
+    po = o.p_output if mode == "reference" else L.F64
+    Vs = [empty_cm(op.m, b, po) for op in ops]
+    vals = [np.zeros(b) for _ in ops]
+    opsarr = (L.ofrr_operator * cnt)(*[op.op for op in ops])
+    Vp = (C.c_void_p * cnt)(*[V.data_ptr() for V in Vs])
+    ldv = (C.c_int64 * cnt)(*[ld_of(V) for V in Vs])
+    evp = (L._DP * cnt)(*[_dp(v) for v in vals])
+    infos = (L.ofrr_info * cnt)()
+    sts = np.zeros(cnt, dtype=np.int32)
+    st = server.lib.ofrr_batch_si_eig(server.h, cnt, opsarr, C.byref(o), Vp, ldv, evp, None, infos, _ip(sts))
+    L.check(st, "ofrr_batch_si_eig")
+    return Vs, vals, sts

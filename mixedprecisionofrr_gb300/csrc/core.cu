@@ -1,5 +1,7 @@
 // Context, workspace, status handling and the level-1/2 kernels of libofrr_gb300.so:
 // project RNG, casts, column argmax / scalecols, iamax, NaN/Inf scan, column norms.
+#include <mutex>
+#include <set>
 #include <type_traits>
 
 #include "ofrr_internal.cuh"
@@ -9,6 +11,23 @@
 #include <new>
 
 namespace ofrr {
+
+int allow_dynamic_smem(const void* func) {
+  static std::mutex mu;
+  static std::set<std::pair<int, const void*>> done;
+  int dev = 0;
+  OFRR_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if (done.count({dev, func})) return OFRR_SUCCESS;
+  int optin = 0;
+  OFRR_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  OFRR_CUDA(cudaFuncGetAttributes(&fa, func));
+  const int cap = optin - (int)fa.sharedSizeBytes;
+  OFRR_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+  done.insert({dev, func});
+  return OFRR_SUCCESS;
+}
 
 int map_cuda_error(cudaError_t e) {
   switch (e) {
@@ -24,6 +43,7 @@ int map_cuda_error(cudaError_t e) {
 void note_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
   fprintf(stderr, "[ofrr] CUDA error %s (%d) in %s at %s:%d\n", cudaGetErrorString(e), (int)e, what, file,
           line);
+  (void)cudaGetLastError();  // reported here: do not charge it to this thread's next launch
 }
 
 void* ws_alloc(ofrr_ctx* ctx, size_t bytes, int* status) {
@@ -533,6 +553,15 @@ uint64_t ofrr_ctx_launch_count(ofrr_ctx* ctx) { return ctx ? ctx->launches : 0; 
 void ofrr_ctx_reset_launch_count(ofrr_ctx* ctx) {
   if (ctx) ctx->launches = 0;
 }
+int ofrr_ctx_trim(ofrr_ctx* ctx) {
+  if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
+  if (ctx->cur_chunk != 0 || ctx->cur_off != 0) return OFRR_ERR_INVALID_ARGUMENT;  // allocations live
+  OFRR_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (Chunk& c : ctx->chunks) cudaFree(c.ptr);
+  ctx->chunks.clear();
+  return OFRR_SUCCESS;
+}
+
 size_t ofrr_ctx_workspace_bytes(ofrr_ctx* ctx) {
   size_t s = 0;
   if (ctx)

@@ -15,6 +15,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 
 #include "ofrr_internal.cuh"
@@ -178,9 +179,9 @@ static int launch(ofrr_ctx* ctx, const CUtensorMap& ma, const CUtensorMap& mb, i
     if (!partial) return st;
   }
   const size_t smem = Smem<BN>::TOTAL;
-  static bool attr_set = false;
+  static std::atomic<bool> attr_set{false};
   if (!attr_set) {
-    OFRR_CUDA(cudaFuncSetAttribute(k_gemm_tn<BN, TOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OFRR_TRY(allow_smem(k_gemm_tn<BN, TOUT>));
     attr_set = true;
   }
   dim3 grid(gm, gn, splits);

@@ -185,7 +185,7 @@ static int hess_run(ofrr_ctx* ctx, int64_t m, int n, TO* Q, int64_t ldq, double 
   size_t smem = (size_t)n * (sizeof(TC) + sizeof(TO)) + 16 + (size_t)n * sizeof(int);
   if (stage) smem += 16 + (size_t)n * n * sizeof(TO);
   if (smem > 48 * 1024) {
-    OFRR_CUDA(cudaFuncSetAttribute(k_hess_col<TO, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OFRR_TRY(allow_smem(k_hess_col<TO, TC>));
   }
   for (int i = 0; i < n; ++i) {
     k_hess_col<TO, TC><<<grid, block, smem, ctx->stream>>>(m, n, i, Q, ldq, select, perm, pivrows, pvals, R, partial,
@@ -233,7 +233,7 @@ static int kry_col(ofrr_ctx* ctx, int64_t m, int nb, int i, TO* V, int64_t ldv, 
   size_t smem = (size_t)nb * (sizeof(TC) + sizeof(TO)) + 16 + (size_t)nb * sizeof(int);
   if (stage) smem += 16 + (size_t)nb * nb * sizeof(TO);
   if (smem > 48 * 1024) {
-    OFRR_CUDA(cudaFuncSetAttribute(k_hess_col<TO, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OFRR_TRY(allow_smem(k_hess_col<TO, TC>));
   }
   k_hess_col<TO, TC><<<grid, block, smem, ctx->stream>>>(m, nb, i, V, ldv, sel, perm, pivrows, pvals, R, partial,
                                                           ctx->dev_counters, stol, 0, stop, stage);

@@ -302,8 +302,7 @@ static int inblock_cluster(int64_t m, size_t smem16) {
   int ncl = 8;
   if (cudaFuncSetAttribute(k_hess_inblock<TO, TC, FAST>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
           cudaSuccess &&
-      cudaFuncSetAttribute(k_hess_inblock<TO, TC, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem16) ==
-          cudaSuccess) {
+      allow_smem(k_hess_inblock<TO, TC, FAST>) == OFRR_SUCCESS) {
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -341,7 +340,7 @@ int hess_run_blocked_t(ofrr_ctx* ctx, int64_t m, int n, TO* Q, int64_t ldq, doub
   const int64_t RR = (m + ncl - 1) / ncl;
   if (ncl > 8)
     OFRR_CUDA(cudaFuncSetAttribute(k_hess_inblock<TO, TC, FAST>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-  OFRR_CUDA(cudaFuncSetAttribute(k_hess_inblock<TO, TC, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+  OFRR_TRY(allow_smem(k_hess_inblock<TO, TC, FAST>));
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = ncl;
@@ -360,8 +359,7 @@ int hess_run_blocked_t(ofrr_ctx* ctx, int64_t m, int n, TO* Q, int64_t ldq, doub
     if (c0 > 0) {
       const size_t smem0 = (size_t)c0 * c0 * sizeof(TO) + (size_t)HB_B * c0 * sizeof(TO) + 16 + 2 * (size_t)c0 * 4;
       if (smem0 > 48 * 1024)
-        OFRR_CUDA(cudaFuncSetAttribute(k_hess_blockcoef<TO, TC, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem0));
+        OFRR_TRY(allow_smem(k_hess_blockcoef<TO, TC, FAST>));
       k_hess_blockcoef<TO, TC, FAST><<<1, HB_B * 32, smem0, ctx->stream>>>(n, c0, c1, Q, ldq, select, perm, rcoef, R);
       OFRR_LAUNCHED(ctx, "k_hess_blockcoef");
       const size_t smem1 = (size_t)HB_CG * c0 * sizeof(TC) + (size_t)c0 * sizeof(int);

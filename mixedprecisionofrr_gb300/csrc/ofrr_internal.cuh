@@ -103,6 +103,16 @@ int after_launch(ofrr_ctx* ctx, const char* name);
 
 int sync_and_check(ofrr_ctx* ctx);
 
+// kernel attributes ---------------------------------------------------------------------
+// Raises a kernel's dynamic shared memory cap to the device's opt-in maximum, once per (device,
+// kernel).  Kernels size their shared memory per launch; a fixed cap keeps concurrent host threads
+// (the solve engine) from lowering each other's limit between an attribute call and a launch.
+int allow_dynamic_smem(const void* func);
+template <class F>
+inline int allow_smem(F* f) {
+  return allow_dynamic_smem(reinterpret_cast<const void*>(f));
+}
+
 // element sizes -----------------------------------------------------------------------
 inline size_t dtype_size(ofrr_dtype t) {
   switch (t) {
@@ -345,9 +355,10 @@ int geig_dev(ofrr_ctx* ctx, int n, const double* G, int ldg, const double* M, in
 // Rayleigh quotients of the final vectors
 // eig(C) for a nonsymmetric n x n C (n <= 128), FP32 Hessenberg-QR: real/imaginary parts, eigenvectors
 // (real parts, unit norm), unsorted
-int nonsym_eig_dev(ofrr_ctx* ctx, int n, const double* C, double* wr, double* wi, double* X);
-// eig(G, M) for nonsymmetric G, SPD M (or M null): real parts descending, unit real-part eigenvectors
-int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U);
+int nonsym_eig_dev(ofrr_ctx* ctx, int n, const double* C, double* wr, double* wi, double* X, bool refine);
+// eig(G, M) for nonsymmetric G, SPD M (or M null): real parts descending, unit real-part eigenvectors;
+// refine = FP64 Newton steps on the real pairs (for FP32/FP64 bases)
+int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U, bool refine);
 int geig_fast(ofrr_ctx* ctx, int n, const double* G, const double* M, double tau, double* lam, double* U,
               int refine = 2);
 int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const double* VV, double tau, double* sigma,

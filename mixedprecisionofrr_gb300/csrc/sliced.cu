@@ -15,6 +15,7 @@
 #include "tcgen05.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 namespace ofrr {
@@ -343,8 +344,10 @@ int sliced_prepare(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, int64_t
 }
 
 // C (M x N, FP64) = A_op' B with A_op the prepared stack (K x M) and B (K x N, FP64, column-major)
-int sliced_gemm_tn(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const double* B, int64_t ldb, double* C,
-                   int64_t ldc) {
+// C (M x N, FP64) = A_op' B with A_op the prepared stack (K x M) and B (K x N, FP64, column-major).
+// reps > 1 (profiling) repeats the product kernel and reports its mean time per launch in *us.
+static int sliced_gemm_run(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const double* B, int64_t ldb, double* C,
+                           int64_t ldc, int reps, double* us, double* bytes) {
   using namespace slice;
   const int64_t K = A.K, Kp = A.Kp, M = A.M;
   // the combined 64-bit integer is bounded by K 2^(2 BETA + BETA LMAX) (1 + 2^-6): K <= 2^20 keeps it below 2^63
@@ -368,21 +371,45 @@ int sliced_gemm_tn(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const doubl
     P = ws_get<long long>(ctx, (size_t)splits * M * N, &st);
     if (!P) return st;
   }
-  static bool attr_set = false;
+  static std::atomic<bool> attr_set{false};
   if (!attr_set) {
-    OFRR_CUDA(cudaFuncSetAttribute(k_sliced_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL_SMEM));
+    OFRR_TRY(allow_smem(k_sliced_tn));
     attr_set = true;
   }
   dim3 grid((unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)((N + SBN - 1) / SBN), (unsigned)splits);
-  k_sliced_tn<<<grid, SL_THREADS, SL_SMEM, ctx->stream>>>(ma, mb, (int)M, (int)N, Kp, kbt, kbps,
-                                                        tc::make_idesc(OFRR_BF16, SBN), P, C, ldc, A.expo, Bs.expo,
-                                                        ctx->dev_flags + 2);
-  OFRR_LAUNCHED(ctx, "k_sliced_tn");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (reps > 1) {
+    OFRR_CUDA(cudaEventCreate(&e0));
+    OFRR_CUDA(cudaEventCreate(&e1));
+    OFRR_CUDA(cudaEventRecord(e0, ctx->stream));
+  }
+  for (int r = 0; r < (reps > 1 ? reps : 1); ++r) {
+    k_sliced_tn<<<grid, SL_THREADS, SL_SMEM, ctx->stream>>>(ma, mb, (int)M, (int)N, Kp, kbt, kbps,
+                                                          tc::make_idesc(OFRR_BF16, SBN), P, C, ldc, A.expo, Bs.expo,
+                                                          ctx->dev_flags + 2);
+    OFRR_LAUNCHED(ctx, "k_sliced_tn");
+  }
+  if (reps > 1) {
+    OFRR_CUDA(cudaEventRecord(e1, ctx->stream));
+    OFRR_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    OFRR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (us) *us = 1e3 * (double)ms / reps;
+    if (bytes)  // digit stacks read once, int64 partials (or FP64 C) written once
+      *bytes = (double)S * Kp * 2 * (double)(M + N) + (double)M * N * 8 * (splits > 1 ? splits : 1);
+  }
   if (splits > 1) {
     k_sliced_finish<<<grid_for(M * N, 256, 2048), 256, 0, ctx->stream>>>(M, N, splits, P, C, ldc, A.expo, Bs.expo);
     OFRR_LAUNCHED(ctx, "k_sliced_finish");
   }
   return OFRR_SUCCESS;
+}
+
+int sliced_gemm_tn(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const double* B, int64_t ldb, double* C,
+                   int64_t ldc) {
+  return sliced_gemm_run(ctx, A, N, B, ldb, C, ldc, 1, nullptr, nullptr);
 }
 
 }  // namespace ofrr
@@ -399,4 +426,18 @@ extern "C" int ofrr_gemm_f64_emulated(ofrr_ctx* ctx, int64_t M, int64_t N, int64
   SlicedOperand As;
   OFRR_TRY(sliced_prepare(ctx, K, M, A, lda, &As));
   return sliced_gemm_tn(ctx, As, N, B, ldb, C, ldc);
+}
+
+// Profiling entry point: prepares the digit stacks of A and B once, then times `reps` launches of the
+// fused exact-slice product kernel alone (CUDA events on the context's stream); C = A' B as above.
+extern "C" int ofrr_profile_gemm_f64_emulated(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const double* A,
+                                              int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc,
+                                              int reps, double* us_per_launch, double* bytes_per_launch) {
+  if (!ctx || M < 1 || N < 1 || K < 1 || reps < 2 || !us_per_launch || !bytes_per_launch)
+    return OFRR_ERR_INVALID_ARGUMENT;
+  if (!A || !B || !C || lda < K || ldb < K || ldc < M) return OFRR_ERR_INVALID_ARGUMENT;
+  WsScope scope(ctx);
+  SlicedOperand As;
+  OFRR_TRY(sliced_prepare(ctx, K, M, A, lda, &As));
+  return sliced_gemm_run(ctx, As, N, B, ldb, C, ldc, reps, us_per_launch, bytes_per_launch);
 }

@@ -249,7 +249,7 @@ static int geig_launch(ofrr_ctx* ctx, GeigParams P) {
   if (need <= 200 * 1024) {
     smem = need;
     P.gws = nullptr;
-    OFRR_CUDA(cudaFuncSetAttribute(k_geig_sym, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem > 0 ? smem : 1)));
+    OFRR_TRY(allow_smem(k_geig_sym));
   } else {
     P.gws = ws_get<double>(ctx, (size_t)3 * P.n * P.n, &st);
     if (!P.gws) return st;

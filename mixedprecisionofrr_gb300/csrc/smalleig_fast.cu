@@ -457,7 +457,7 @@ static int gemm_small(ofrr_ctx* ctx, int M, int N, int K, double alpha, const do
 static int trsm(ofrr_ctx* ctx, int n, int nrhs, const double* L, const double* B, int ldb, int transB, double* X,
                 int upper) {
   const size_t smem = ((size_t)n * (n + 1) + (size_t)n) * sizeof(double);
-  OFRR_CUDA(cudaFuncSetAttribute(k_trsm_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  OFRR_TRY(allow_smem(k_trsm_f64));
   k_trsm_f64<<<(nrhs + 3) / 4, 128, smem, ctx->stream>>>(n, nrhs, L, n, B, ldb, transB, X, n, upper);
   OFRR_LAUNCHED(ctx, "k_trsm_f64");
   return OFRR_SUCCESS;
@@ -472,7 +472,7 @@ static int chol(ofrr_ctx* ctx, int n, int count, const double* const* Ms_host, i
   const void* hp[4] = {Ms_host[0], count > 1 ? Ms_host[1] : Ms_host[0], Ls_host[0], count > 1 ? Ls_host[1] : Ls_host[0]};
   OFRR_CUDA(cudaMemcpyAsync(Md, hp, sizeof(hp), cudaMemcpyHostToDevice, ctx->stream));
   const size_t smem = (size_t)n * n * sizeof(double);
-  OFRR_CUDA(cudaFuncSetAttribute(k_chol_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  OFRR_TRY(allow_smem(k_chol_f64));
   k_chol_f64<<<count, 256, smem, ctx->stream>>>(n, Md, ldm, tau, Ld, ctx->dev_flags + 1);
   OFRR_LAUNCHED(ctx, "k_chol_f64");
   return OFRR_SUCCESS;
@@ -517,7 +517,7 @@ static int sym_eig_refined(ofrr_ctx* ctx, int n, const double* C, double* W, dou
   double *W0 = ws_get<double>(ctx, (size_t)n * n, &st), *l0 = ws_get<double>(ctx, (size_t)n, &st);
   if (!W0 || !l0) return st;
   const size_t smem = (size_t)2 * n * (n + 1) * sizeof(float);
-  OFRR_CUDA(cudaFuncSetAttribute(k_jacobi_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  OFRR_TRY(allow_smem(k_jacobi_f32));
   k_jacobi_f32<<<1, 512, smem, ctx->stream>>>(n, C, n, W0, l0);
   OFRR_LAUNCHED(ctx, "k_jacobi_f32");
   return eig_refine(ctx, n, C, W0, W, lam, steps);
@@ -538,7 +538,7 @@ __global__ void k_unit_cols(int n, double* __restrict__ U) {
 // eig(G, M) for a nonsymmetric G and SPD M (M null: eig(G)): lam = real parts, descending (stable);
 // U (ld n) the real parts of the eigenvectors, unit 2-norm.  M is reduced away with its FP64
 // Cholesky factor (C = L^-1 G L^-T, U = L^-T X); C is solved in FP32 (smalleig_nonsym.cu).
-int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U) {
+int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U, bool refine) {
   if (n <= 0) return OFRR_SUCCESS;
   if (n > 128) return OFRR_ERR_BLAS_INVALID_SIZE;
   WsScope scope(ctx);
@@ -557,7 +557,7 @@ int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* 
     OFRR_TRY(trsm(ctx, n, n, L, Z, n, 1, C, 0));  // C = L^-1 Z' = L^-1 G L^-T
     Cs = C;
   }
-  OFRR_TRY(nonsym_eig_dev(ctx, n, Cs, wr, wi, X));
+  OFRR_TRY(nonsym_eig_dev(ctx, n, Cs, wr, wi, X, refine));
   if (M) {
     OFRR_TRY(trsm(ctx, n, n, L, X, n, 0, W, 1));  // W = L^-T X
     k_unit_cols<<<(n + 3) / 4, 128, 0, ctx->stream>>>(n, W);
@@ -623,7 +623,7 @@ int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const dou
     double* X0 = ws_get<double>(ctx, (size_t)b * b, &st);
     if (!X0) return st;
     const size_t smem = (size_t)2 * b * (b + 1) * sizeof(float);
-    OFRR_CUDA(cudaFuncSetAttribute(k_jacobi1_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OFRR_TRY(allow_smem(k_jacobi1_f32));
     k_jacobi1_f32<<<1, 1024, smem, ctx->stream>>>(b, C, b, 1, X0);
     OFRR_LAUNCHED(ctx, "k_jacobi1_f32");
     OFRR_TRY(eig_refine(ctx, b, S, X0, X, lam, refine));  // right singular vectors X, sigma^2 (FP64)

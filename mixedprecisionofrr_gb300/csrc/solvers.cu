@@ -258,7 +258,8 @@ int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype t
   if (fast && symmetric && b <= 128) {
     OFRR_TRY(geig_fast(ctx, b, G, M, use_gen ? gtol : 0.0, d, U, refine));
   } else if (!symmetric && b <= 128) {
-    OFRR_TRY(geig_nonsym(ctx, b, G, M, d, U));  // M already holds VV + gtol I
+    // M already holds VV + gtol I; FP64 refinement unless the basis is 16-bit
+    OFRR_TRY(geig_nonsym(ctx, b, G, M, d, U, tq == OFRR_F64 || tq == OFRR_F32));
   } else {
     OFRR_TRY(geig_dev(ctx, b, G, b, M, b, symmetric ? 1 : 0, d, U, b));
   }
@@ -275,9 +276,68 @@ int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype t
   return OFRR_SUCCESS;
 }
 
+__global__ void k_normalize_cols(int64_t m, int64_t n, double* X, const double* nrm);
+
+// |X| rounded to T (16-bit), column-major
+template <class TI, class T>
+__global__ void k_abs_cast(int64_t m, int64_t n, const TI* __restrict__ X, int64_t ldx, T* __restrict__ Y,
+                           int64_t ldy) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % m, j = e / m;
+    Y[i + j * ldy] = from_c<T, float>(fabsf(to_c<float, TI>(X[i + j * ldx])));
+  }
+}
+__global__ void k_abs_cast_f64(int64_t m, int64_t n, const double* __restrict__ X, int64_t ldx, __half* Yh,
+                               __nv_bfloat16* Yb, int64_t ldy) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % m, j = e / m;
+    const double a = fabs(X[i + j * ldx]);
+    if (Yh) Yh[i + j * ldy] = __double2half(a);
+    else Yb[i + j * ldy] = __double2bfloat16(a);
+  }
+}
+
+// Bound on the exact-slice emulation error of Y = op(A) X for unit columns X (FP64, ld ldx):
+// |Y_emul - Y| <= 2^-33 |op(A)| |X| element-wise (the tested bound of the emulated product), and
+// ||(|op(A)| |x_j|)||_2 is computed from the 16-bit copies of A (abs, exact) and |x_j| rounded to
+// 16 bits with FP32 accumulation of non-negative terms; the factor 1.01 covers those roundings
+// (2^-8 relative for the 16-bit values, K 2^-24 for the sums).  out[j] = the bound for column j.
+int emulation_bounds(ofrr_ctx* ctx, Op& op, int trans, ofrr_dtype t16, const double* X, int64_t ldx, int k,
+                     double* out_dev) {
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  const int64_t m = op.m(), n = op.n();
+  const int64_t M = trans ? n : m, K = trans ? m : n;
+  // |op(A)| as the K-contiguous operand of the TN kernel: A' (K = n) for A X, A itself (K = m) for A' X
+  const void* Ap;
+  int64_t lda;
+  if (trans) OFRR_TRY(op.dense_as(ctx, t16, &Ap, &lda));
+  else OFRR_TRY(op.dense_t_as(ctx, t16, &Ap, &lda));
+  void* absA = ws_alloc(ctx, (size_t)K * M * 2, &st);
+  void* absX = ws_alloc(ctx, (size_t)K * k * 2, &st);
+  float* Bnd = ws_get<float>(ctx, (size_t)M * k, &st);
+  if (!absA || !absX || !Bnd) return st;
+  if (t16 == OFRR_F16) {
+    k_abs_cast<__half, __half><<<grid_for(K * M, 256), 256, 0, ctx->stream>>>(K, M, (const __half*)Ap, lda,
+                                                                             (__half*)absA, K);
+    OFRR_LAUNCHED(ctx, "k_abs_cast");
+    k_abs_cast_f64<<<grid_for(K * k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, (__half*)absX, nullptr, K);
+  } else {
+    k_abs_cast<__nv_bfloat16, __nv_bfloat16><<<grid_for(K * M, 256), 256, 0, ctx->stream>>>(
+        K, M, (const __nv_bfloat16*)Ap, lda, (__nv_bfloat16*)absA, K);
+    OFRR_LAUNCHED(ctx, "k_abs_cast");
+    k_abs_cast_f64<<<grid_for(K * k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, nullptr, (__nv_bfloat16*)absX, K);
+  }
+  OFRR_LAUNCHED(ctx, "k_abs_cast_f64");
+  OFRR_TRY(gemm_impl(ctx, 1, 0, t16, t16, OFRR_F32, OFRR_F32, M, k, K, 1.0, absA, K, absX, K, 0.0, Bnd, M));
+  OFRR_TRY(column_norms(ctx, OFRR_F32, M, k, Bnd, M, out_dev));
+  return OFRR_SUCCESS;
+}
+constexpr double kEmulBound = 1.01 * 1.16415321826934814453125e-10;  // 1.01 * 2^-33
+
 // FP64 residuals of Ritz pairs (X in type tx), normalised by normA and ||x||
 int residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* X, int64_t ldx, int k, const double* lam_host,
-                  double normA, double* out_host) {
+                  double normA, double* out_host, int certify16 = -1) {
   if (k <= 0) return OFRR_SUCCESS;
   WsScope scope(ctx);
   const int64_t n = op.m();
@@ -292,7 +352,15 @@ int residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* X, int64_t l
   OFRR_CUDA(cudaMemcpyAsync(lam, lam_host, sizeof(double) * k, cudaMemcpyHostToDevice, ctx->stream));
   OFRR_TRY(residual_columns(ctx, n, k, AX, n, X64, n, lam, res));
   OFRR_TRY(column_norms(ctx, OFRR_F64, n, k, X64, n, nrm));
-  std::vector<double> h(2 * k);
+  std::vector<double> h(3 * k, 0.0);
+  double* bnd = nullptr;
+  if (certify16 >= 0) {  // emulated A X: add the bound on its error (unit columns)
+    OFRR_TRY(dmalloc(ctx, &bnd, (size_t)k));
+    k_normalize_cols<<<grid_for(n * k, 256), 256, 0, ctx->stream>>>(n, k, X64, nrm);
+    OFRR_LAUNCHED(ctx, "k_normalize_cols");
+    OFRR_TRY(emulation_bounds(ctx, op, 0, (ofrr_dtype)certify16, X64, n, k, bnd));
+    OFRR_CUDA(cudaMemcpyAsync(h.data() + 2 * k, bnd, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+  }
   OFRR_CUDA(cudaMemcpyAsync(h.data(), res, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, ctx->stream));
   OFRR_TRY(sync_and_check(ctx));
   if (normA <= 0) {
@@ -300,7 +368,8 @@ int residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* X, int64_t l
     for (int j = 0; j < k; ++j) normA = std::max(normA, std::fabs(lam_host[j]));
     if (normA == 0) normA = 1;
   }
-  for (int j = 0; j < k; ++j) out_host[j] = (h[k + j] > 0) ? h[j] / (normA * h[k + j]) : INFINITY;
+  for (int j = 0; j < k; ++j)
+    out_host[j] = (h[k + j] > 0) ? h[j] / (normA * h[k + j]) + kEmulBound * h[2 * k + j] / normA : INFINITY;
   return OFRR_SUCCESS;
 }
 
@@ -558,7 +627,7 @@ __global__ void k_normalize_cols(int64_t m, int64_t n, double* X, const double* 
 }
 
 int svd_residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* U, int64_t ldu, const void* V, int64_t ldv,
-                      int k, const double* s_host, double normA, double* out_host) {
+                      int k, const double* s_host, double normA, double* out_host, int certify16 = -1) {
   if (k <= 0) return OFRR_SUCCESS;
   WsScope scope(ctx);
   const int64_t m = op.m(), n = op.n();
@@ -584,7 +653,14 @@ int svd_residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* U, int64
   OFRR_LAUNCHED(ctx, "k_rescol2");
   k_rescol2<<<k, 256, 0, ctx->stream>>>(n, k, ATU, V64, sd, nr + 3 * k);
   OFRR_LAUNCHED(ctx, "k_rescol2");
-  std::vector<double> h(2 * k);
+  std::vector<double> h(4 * k, 0.0);
+  if (certify16 >= 0) {  // emulated A v and A' u: add the bounds on their errors (unit columns)
+    double* bnd;
+    OFRR_TRY(dmalloc(ctx, &bnd, (size_t)2 * k));
+    OFRR_TRY(emulation_bounds(ctx, op, 0, (ofrr_dtype)certify16, V64, n, k, bnd));
+    OFRR_TRY(emulation_bounds(ctx, op, 1, (ofrr_dtype)certify16, U64, m, k, bnd + k));
+    OFRR_CUDA(cudaMemcpyAsync(h.data() + 2 * k, bnd, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, ctx->stream));
+  }
   OFRR_CUDA(cudaMemcpyAsync(h.data(), nr + 2 * k, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, ctx->stream));
   OFRR_TRY(sync_and_check(ctx));
   if (normA <= 0) {
@@ -592,7 +668,8 @@ int svd_residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* U, int64
     for (int j = 0; j < k; ++j) normA = std::max(normA, std::fabs(s_host[j]));
     if (normA == 0) normA = 1;
   }
-  for (int j = 0; j < k; ++j) out_host[j] = std::max(h[j], h[k + j]) / normA;
+  for (int j = 0; j < k; ++j)
+    out_host[j] = std::max(h[j] + kEmulBound * h[2 * k + j], h[k + j] + kEmulBound * h[3 * k + j]) / normA;
   return OFRR_SUCCESS;
 }
 
@@ -1026,13 +1103,23 @@ extern "C" int ofrr_si_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
       st = eig_phase(ctx, op, all_f64(), opt, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d);
       ctx->emulate_f64 = false;
       OFRR_TRY(st);
-      if (S.done) {  // confirm with true FP64 residuals
+      if (S.done && op.A->kind == OFRR_OP_DENSE) {
+        // certify: the emulated residuals plus the bound on the emulation error must meet tol;
+        // otherwise the residuals are recomputed with true FP64 products
         OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d, sizeof(double) * S.b, cudaMemcpyDeviceToHost, ctx->stream));
         OFRR_TRY(sync_and_check(ctx));
         const int kk = std::min(nev, S.b);
-        OFRR_TRY(residuals_dev(ctx, op, OFRR_F64, V, ldv, kk, S.d.data(), -1.0, S.res.data()));
+        ctx->emulate_f64 = true;
+        st = residuals_dev(ctx, op, OFRR_F64, V, ldv, kk, S.d.data(), -1.0, S.res.data(), (int)L.po);
+        ctx->emulate_f64 = false;
+        OFRR_TRY(st);
         S.converged = 0;
         for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
+        if (S.converged < kk) {
+          OFRR_TRY(residuals_dev(ctx, op, OFRR_F64, V, ldv, kk, S.d.data(), -1.0, S.res.data()));
+          S.converged = 0;
+          for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
+        }
         S.done = S.converged >= kk;
       }
     }
@@ -1108,13 +1195,23 @@ extern "C" int ofrr_si_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
       st = svd_phase(ctx, op, all_f64(), opt, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d);
       ctx->emulate_f64 = false;
       OFRR_TRY(st);
-      if (S.done) {  // confirm with true FP64 residuals
+      if (S.done && op.A->kind == OFRR_OP_DENSE) {
+        // certify: the emulated residuals plus the bounds on the emulation errors must meet tol;
+        // otherwise the residuals are recomputed with true FP64 products
         OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d, sizeof(double) * S.b, cudaMemcpyDeviceToHost, ctx->stream));
         OFRR_TRY(sync_and_check(ctx));
         const int kk = std::min(nev, S.b);
-        OFRR_TRY(svd_residuals_dev(ctx, op, OFRR_F64, U, ldu, V, ldv, kk, S.d.data(), -1.0, S.res.data()));
+        ctx->emulate_f64 = true;
+        st = svd_residuals_dev(ctx, op, OFRR_F64, U, ldu, V, ldv, kk, S.d.data(), -1.0, S.res.data(), (int)L.po);
+        ctx->emulate_f64 = false;
+        OFRR_TRY(st);
         S.converged = 0;
         for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
+        if (S.converged < kk) {
+          OFRR_TRY(svd_residuals_dev(ctx, op, OFRR_F64, U, ldu, V, ldv, kk, S.d.data(), -1.0, S.res.data()));
+          S.converged = 0;
+          for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
+        }
         S.done = S.converged >= kk;
       }
     }
