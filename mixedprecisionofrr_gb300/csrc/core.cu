@@ -12,6 +12,26 @@
 
 namespace ofrr {
 
+int aux_begin(ofrr_ctx* ctx, ofrr_ctx** aux) {
+  if (!ctx->aux) {
+    OFRR_TRY(ofrr_ctx_create(&ctx->aux, ctx->device, nullptr));
+    OFRR_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+    OFRR_CUDA(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+  }
+  ctx->aux->emulate_f64 = ctx->emulate_f64;
+  OFRR_CUDA(cudaEventRecord(ctx->ev_fork, ctx->stream));
+  OFRR_CUDA(cudaStreamWaitEvent(ctx->aux->stream, ctx->ev_fork, 0));
+  *aux = ctx->aux;
+  return OFRR_SUCCESS;
+}
+
+int aux_end(ofrr_ctx* ctx) {
+  if (!ctx->aux) return OFRR_SUCCESS;
+  OFRR_CUDA(cudaEventRecord(ctx->ev_join, ctx->aux->stream));
+  OFRR_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+  return OFRR_SUCCESS;
+}
+
 int allow_dynamic_smem(const void* func) {
   static std::mutex mu;
   static std::set<std::pair<int, const void*>> done;
@@ -519,6 +539,9 @@ int ofrr_ctx_create(ofrr_ctx** out, int device, void* stream) {
 int ofrr_ctx_destroy(ofrr_ctx* ctx) {
   if (!ctx) return OFRR_SUCCESS;
   cudaSetDevice(ctx->device);
+  if (ctx->aux) ofrr_ctx_destroy(ctx->aux);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto& c : ctx->chunks) cudaFree(c.ptr);
   if (ctx->dev_flags) cudaFree(ctx->dev_flags);
@@ -549,9 +572,12 @@ int ofrr_ctx_synchronize(ofrr_ctx* ctx) {
   return sync_and_check(ctx);
 }
 
-uint64_t ofrr_ctx_launch_count(ofrr_ctx* ctx) { return ctx ? ctx->launches : 0; }
+uint64_t ofrr_ctx_launch_count(ofrr_ctx* ctx) {
+  return ctx ? ctx->launches + (ctx->aux ? ctx->aux->launches : 0) : 0;
+}
 void ofrr_ctx_reset_launch_count(ofrr_ctx* ctx) {
   if (ctx) ctx->launches = 0;
+  if (ctx && ctx->aux) ctx->aux->launches = 0;
 }
 int ofrr_ctx_trim(ofrr_ctx* ctx) {
   if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;

@@ -74,6 +74,8 @@ struct ofrr_ctx {
   void* pinned = nullptr;          // small pinned host staging buffer
   bool emulate_f64 = false;        // FP64 TN products through exact BF16 slices on the tensor cores
   size_t pinned_size = 0;
+  ofrr_ctx* aux = nullptr;         // second stream + workspace for independent work run beside this one
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace ofrr {
@@ -102,6 +104,13 @@ int after_launch(ofrr_ctx* ctx, const char* name);
 #define OFRR_LAUNCHED(ctx, name) OFRR_TRY(ofrr::after_launch((ctx), (name)))
 
 int sync_and_check(ofrr_ctx* ctx);
+
+// Concurrency inside one solve: aux_begin() returns the context's auxiliary context (created on
+// first use: same device, its own stream, cuBLAS handle and workspace) after ordering its stream
+// behind everything queued on ctx's stream; work queued on it runs beside ctx's own; aux_end()
+// orders ctx's stream behind it again.
+int aux_begin(ofrr_ctx* ctx, ofrr_ctx** aux);
+int aux_end(ofrr_ctx* ctx);
 
 // kernel attributes ---------------------------------------------------------------------
 // Raises a kernel's dynamic shared memory cap to the device's opt-in maximum, once per (device,

@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(SLICE_T) k_slice_digits(int64_t K, int64_t Kp,
 // (1024 entries of K, so that the level-0 and level-1 FP32 sums are exact).  Per k-block the B digits
 // d'_0..d'_4 (5 tiles) are loaded once into a B slot, and the A digits d_0..d_4 stream through an
 // A ring one tile at a time; for A digit s the MMA warp issues the pairs (s, t), t <= LMAX - s,
-// into the TMEM accumulator of level L = s + t (5 accumulators of SBN columns).  A is therefore read
+// into the TMEM accumulator of level L = s + t (5 accumulators of SBN columns), as one wide MMA.  A is therefore read
 // once per product (not once per level).  The epilogue converts each level to an integer, combines
 // acc = sum_L S_L 2^(BETA (LMAX - L)) exactly in 64 bits and writes it (one split) as
 // C = 2^(ea + eb - BETA (LMAX + 2)) acc, or as an int64 partial for k_sliced_finish.
@@ -132,6 +132,11 @@ constexpr int SL_SHIFT = BETA * (LMAX + 2);
 constexpr size_t SL_SMEM = (size_t)SL_ASLOTS * SL_ATILE + (size_t)SL_BSLOTS * S * SL_BTILE + 1024 + 256;
 constexpr uint32_t SL_TMEM_COLS = 512;  // LMAX + 1 accumulators of SBN columns, rounded to a power of two
 static_assert((LMAX + 1) * SBN <= (int)SL_TMEM_COLS, "TMEM columns");
+
+// instruction descriptor with its N field (bits 17-22, N >> 3) replaced
+__device__ __forceinline__ uint32_t idesc_with_n(uint32_t idesc, int n) {
+  return (idesc & ~(0x3Fu << 17)) | ((uint32_t)(n >> 3) << 17);
+}
 
 __global__ void __launch_bounds__(SL_THREADS, 1)
     k_sliced_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N,
@@ -226,14 +231,22 @@ __global__ void __launch_bounds__(SL_THREADS, 1)
             break;
           }
           fence_after();
+          // A digit s against the B digits 0..LMAX-s at once: the slot's B tiles are adjacent rows of
+          // one K-major operand and the level accumulators s..LMAX adjacent TMEM columns, so one MMA
+          // of N = (LMAX-s+1) SBN (at most 256; the rest in a second MMA) replaces LMAX-s+1 MMAs
           const uint32_t a0 = smem_u32(sA + as * SL_ATILE);
-          for (int t = 0; t + s <= LMAX; ++t) {
-            const uint32_t b0 = smem_u32(sB + (bs * S + t) * SL_BTILE);
-            const uint32_t d = tmem + (uint32_t)((s + t) * SBN);
+          const uint32_t b0 = smem_u32(sB + (bs * S) * SL_BTILE);
+          const int nt = LMAX - s + 1;
+          const int n1 = nt < 4 ? nt : 4;
+          const uint32_t id1 = idesc_with_n(idesc, n1 * SBN), id2 = idesc_with_n(idesc, (nt - n1) * SBN);
+          const uint32_t d = tmem + (uint32_t)(s * SBN);
 #pragma unroll
-            for (int k = 0; k < BK / 16; ++k)
-              umma_f16(d, desc_sw128(a0 + 32 * k), desc_sw128(b0 + 32 * k), idesc,
-                       (i > 0 || s > 0 || k > 0) ? 1u : 0u);
+          for (int k = 0; k < BK / 16; ++k) {
+            const uint32_t acc = (i > 0 || s > 0 || k > 0) ? 1u : 0u;
+            umma_f16(d, desc_sw128(a0 + 32 * k), desc_sw128(b0 + 32 * k), id1, acc);
+            if (nt > n1)
+              umma_f16(d + (uint32_t)(n1 * SBN), desc_sw128(a0 + 32 * k), desc_sw128(b0 + n1 * SL_BTILE + 32 * k),
+                       id2, acc);
           }
           umma_commit(&a_empty[as]);
           ++a_used;

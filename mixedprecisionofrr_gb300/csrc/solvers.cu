@@ -959,15 +959,17 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
   const int64_t m = op.m(), n = op.n();
   const int b0 = S.b;
   void *P1, *Q1, *Ut, *Vt;
-  double* R;
-  int *sel, *perm;
+  double *R, *R2;
+  int *sel, *perm, *perm2;
   if (!(P1 = ws_alloc(ctx, (size_t)m * b0 * dtype_size(P.pho), &st))) return st;
   if (!(Q1 = ws_alloc(ctx, (size_t)n * b0 * dtype_size(P.pho), &st))) return st;
   if (!(Ut = ws_alloc(ctx, (size_t)m * b0 * dtype_size(P.pho), &st))) return st;
   if (!(Vt = ws_alloc(ctx, (size_t)n * b0 * dtype_size(P.pho), &st))) return st;
   OFRR_TRY(dmalloc(ctx, &R, (size_t)b0 * b0));
+  OFRR_TRY(dmalloc(ctx, &R2, (size_t)b0 * b0));
   OFRR_TRY(dmalloc(ctx, &sel, (size_t)2 * b0));
   OFRR_TRY(dmalloc(ctx, &perm, (size_t)b0));
+  OFRR_TRY(dmalloc(ctx, &perm2, (size_t)b0));
   std::vector<int> hsel(2 * b0);
   const int check_every = std::max(1, opt->check_every);
   for (int k = 0; k < maxit && !S.done; ++k) {
@@ -979,8 +981,13 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
       OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr, P.fast));
       S.nmv += 2 * b;
     }
+    // the two bases are independent: V's is built on the auxiliary stream beside U's
+    ofrr_ctx* aux = nullptr;
+    OFRR_TRY(aux_begin(ctx, &aux));
+    OFRR_TRY(hessenberg_impl(aux, P.po, P.pho, P.phc, n, b, V, ldv, Q1, n, opt->select_tol, R2, sel + b0, perm2,
+                             P.fast));
     OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, m, b, U, ldu, P1, m, opt->select_tol, R, sel, perm, P.fast));
-    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, n, b, V, ldv, Q1, n, opt->select_tol, R, sel + b0, perm, P.fast));
+    OFRR_TRY(aux_end(ctx));
     OFRR_CUDA(cudaMemcpyAsync(hsel.data(), sel, sizeof(int) * 2 * b0, cudaMemcpyDeviceToHost, ctx->stream));
     OFRR_TRY(sync_and_check(ctx));
     int wu = b, wv = b;
