@@ -27,7 +27,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 M_ROWS, N_COLS, NEV, TOL = 8192, 2048, 32, 1e-8
-BLOCK, STEP, MAXITER = 64, 4, 60
+BLOCK, STEP, MAXITER = 64, 8, 80  # defaults (the reference arm's); main() autotunes each GPU path
+CFG = {"mixed": (BLOCK, STEP), "fp64": (BLOCK, STEP)}
 METRIC = "converged singular triplets/s at residual <= 1e-8 (dense 8192x2048 geometric-spectrum SVD, top 32)"
 UNIT = "triplets/s"
 
@@ -135,7 +136,8 @@ def flush_l2(buf):
 
 
 def run_solver(api, A, mode, V0=None):
-    return api.subspace_iter_svd(A, M_ROWS, N_COLS, BLOCK, "single", "half", maxiter=MAXITER, step_size=STEP,
+    b, st = CFG.get(mode, (BLOCK, STEP))
+    return api.subspace_iter_svd(A, M_ROWS, N_COLS, b, "single", "half", maxiter=MAXITER, step_size=st,
                                  mode=mode, tol=TOL, nev=NEV, check_every=1, V0=V0, generalized_tol=0.0)
 
 
@@ -171,6 +173,7 @@ def time_e2e(api, A_host_pinned, steps, warmup):
 
     ctx = api.context()
     stream = torch.cuda.current_stream()
+    BLOCK, STEP = CFG["mixed"]
     A_dev = api.empty_cm(M_ROWS, N_COLS, L.F64)
     U_dev = api.empty_cm(M_ROWS, BLOCK, L.F64)
     V_dev = api.empty_cm(N_COLS, BLOCK, L.F64)
@@ -223,6 +226,7 @@ def gemm_roofline(api, steps=20):
 
     ctx = api.context()
     # the solver keeps A' (K-contiguous rows of A) and runs A V as the TN product (A')' V
+    BLOCK = CFG["mixed"][0]
     At = api.randn(7, N_COLS, M_ROWS, "half")
     X = api.randn(8, N_COLS, BLOCK, "half")
     Y = api.empty_cm(M_ROWS, BLOCK, L.F16)
@@ -265,6 +269,7 @@ def sliced_roofline(api, reps=20):
     from mixedprecisionofrr_gb300 import _lib as L
 
     ctx = api.context()
+    BLOCK = CFG["mixed"][0]
     At = api.randn(11, N_COLS, M_ROWS, "double")  # A' (K x M, FP64)
     X = api.randn(12, N_COLS, BLOCK, "double")
     Y = api.empty_cm(M_ROWS, BLOCK, L.F64)
@@ -310,7 +315,8 @@ def cpu_baseline_run(A_host, max_seconds=60.0):
             raise Stop()
 
     try:
-        orc.subspace_iter_svd(A_host, M_ROWS, N_COLS, BLOCK, "double", maxiter=MAXITER, step_size=STEP,
+        b, st = CFG["fp64"]
+        orc.subspace_iter_svd(A_host, M_ROWS, N_COLS, b, "double", maxiter=MAXITER, step_size=st,
                               generalized_tol=0.0, callback=cb)
     except Stop:
         pass
@@ -348,6 +354,13 @@ def main():
                           "max_residual": info.max_residual}))
         return
     flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    # block width and power steps per path from the solver autotuner (untimed; b >= 40)
+    tune = {}
+    for mode in ("mixed",) + (() if args.no_fp64 else ("fp64",)):
+        t = api.autotune_svd(A, M_ROWS, N_COLS, NEV, TOL, mode=mode, blocks=(64, 96, 128), steps=(4, 6, 8),
+                             reps=1 if mode == "fp64" else 2, maxiter=MAXITER)
+        CFG[mode] = (t["block"], t["step_size"])
+        tune[mode] = {"block": t["block"], "step_size": t["step_size"], "candidates": len(t["table"])}
     # mixed path (the product) -----------------------------------------------------------------
     if world > 1:
         torch.distributed.barrier()
@@ -392,15 +405,17 @@ def main():
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
         src = "measured" if "hbm_gbs" in peaks else "fallback"
         dt_s, bytes_s = sliced_roofline(api)
-        roof = {"kernel": "k_sliced_tn: exact-slice FP64 A.V, 8192x64 = (5-digit A' 2048x8192)' V", "bound": "hbm",
+        bb = CFG["mixed"][0]
+        roof = {"kernel": f"k_sliced_tn: exact-slice FP64 A.V, 8192x{bb} = (5-digit A' 2048x8192)' V", "bound": "hbm",
                 "achieved": bytes_s / dt_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                "frac": bytes_s / dt_s / 1e9 / hbm_peak, "traffic": profiled_traffic(),
+                "frac": bytes_s / dt_s / 1e9 / hbm_peak, "traffic": profiled_traffic() if bb == 64 else None,
                 "algorithmic_bytes": bytes_s, "peak_source": src, "us_per_launch": dt_s * 1e6}
         dt_g, bytes_g, flops_g = gemm_roofline(api)
-        roof16 = {"kernel": "k_gemm_tn: A.V 16-bit TN GEMM 8192x2048x64 (FP32 accumulate, incl. split-K reduce)",
+        roof16 = {"kernel": f"k_gemm_tn: A.V 16-bit TN GEMM 8192x2048x{bb} (FP32 accumulate, incl. split-K reduce)",
                   "bound": "hbm", "achieved": bytes_g / dt_g / 1e9, "peak": hbm_peak, "unit": "GB/s",
                   "frac": bytes_g / dt_g / 1e9 / hbm_peak,
-                  "traffic": profiled_traffic("k_gemm_tn_av_8192x64x2048.md"), "algorithmic_bytes": bytes_g,
+                  "traffic": profiled_traffic("k_gemm_tn_av_8192x64x2048.md") if bb == 64 else None,
+                  "algorithmic_bytes": bytes_g,
                   "peak_source": src, "us_per_launch": dt_g * 1e6, "tflops": flops_g / dt_g / 1e12}
         cpu = None
         if not args.no_cpu_baseline:
@@ -416,8 +431,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f16 basis / f32 accumulate / f64 pencil",
             "data": "synthetic (seeded Haar U, V; geometric s 1..1e-6)",
-            "config": {"workload": "dense truncated SVD 8192x2048, top 32 triplets, tol 1e-8", "block": BLOCK,
-                       "step_size": STEP, "l2_flush": "256 MB write between timed solves",
+            "config": {"workload": "dense truncated SVD 8192x2048, top 32 triplets, tol 1e-8",
+                       "block": CFG["mixed"][0], "step_size": CFG["mixed"][1], "autotuned": tune,
+                       "l2_flush": "256 MB write between timed solves",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "p50_ms": 1e3 * float(np.percentile(times, 50)), "p99_ms": 1e3 * float(np.percentile(times, 99)),
             "iterations": iters, "max_residual": maxres, "max_rel_sigma_err": err, "status": statuses,

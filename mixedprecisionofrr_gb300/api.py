@@ -634,3 +634,42 @@ def batch_si_eig(server: Server, As, k: int, mode: str = "mixed", tol: float = 1
     st = server.lib.ofrr_batch_si_eig(server.h, cnt, opsarr, C.byref(o), Vp, ldv, evp, None, infos, _ip(sts))
     L.check(st, "ofrr_batch_si_eig")
     return Vs, vals, sts
+
+
+# ---- autotuner -------------------------------------------------------------------------------
+def autotune_svd(A, m: int, n: int, nev: int, tol: float, mode: str = "mixed", blocks=(64, 96, 128),
+                 steps=(4, 6, 8), reps: int = 2, min_block: int = 40, **kw):
+    """Pick the block width and power-step count of subspace_iter_svd for this problem by timing
+    each candidate solve (CUDA events on the library's stream, median of reps after one warm-up)
+    and keeping the fastest one that converges.  Returns {"block", "step_size", "ms", "iterations",
+    "table"}; the table lists every candidate."""
+    stream = torch.cuda.current_stream()
+    table = []
+    best = None
+    for b in blocks:
+        if b < max(min_block, nev) or b > min(m, n):
+            continue
+        for st in steps:
+            args = dict(maxiter=kw.get("maxiter", 80), step_size=st, mode=mode, tol=tol, nev=nev,
+                        check_every=kw.get("check_every", 1), generalized_tol=kw.get("generalized_tol", 0.0))
+            U, s, V, info = subspace_iter_svd(A, m, n, b, kw.get("precision_compute", "single"),
+                                              kw.get("precision_output", "half"), **args)
+            ts = []
+            for _ in range(reps):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                U, s, V, info = subspace_iter_svd(A, m, n, b, kw.get("precision_compute", "single"),
+                                                  kw.get("precision_output", "half"), **args)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ms = float(np.median(ts))
+            ok = info.status == 0 and info.max_residual <= tol
+            table.append({"block": b, "step_size": st, "ms": ms, "iterations": info.iterations, "converged": ok})
+            if ok and (best is None or ms < best["ms"]):
+                best = {"block": b, "step_size": st, "ms": ms, "iterations": info.iterations}
+    if best is None:
+        raise RuntimeError("autotune_svd: no candidate converged")
+    best["table"] = table
+    return best

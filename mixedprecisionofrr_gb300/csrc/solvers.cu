@@ -526,7 +526,6 @@ int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* 
   }
   void* AV = ws_alloc(ctx, (size_t)m * b * dtype_size(pAmo), &st);
   if (!AV) return st;
-  OFRR_TRY(op.apply(ctx, 0, ta, pAmc, Va, ldva, b, pAmc, pAmo, AV, m));
   double *B, *UU, *VV, *Aext, *Mext, *X, *d;
   OFRR_TRY(dmalloc(ctx, &B, (size_t)b * b));
   OFRR_TRY(dmalloc(ctx, &UU, (size_t)b * b));
@@ -536,13 +535,20 @@ int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* 
   OFRR_TRY(dmalloc(ctx, &X, (size_t)4 * b * b));
   OFRR_TRY(dmalloc(ctx, &d, (size_t)2 * b));
   void* tmp = ws_alloc(ctx, (size_t)b * b * dtype_size(pmo), &st);
-  if (!tmp) return st;
+  void* tmpu = ws_alloc(ctx, (size_t)b * b * dtype_size(pmo), &st);
+  void* tmpv = ws_alloc(ctx, (size_t)b * b * dtype_size(pmo), &st);
+  if (!tmp || !tmpu || !tmpv) return st;
+  // the Gram matrices U'U and V'V do not depend on A V: auxiliary stream
+  ofrr_ctx* aux = nullptr;
+  OFRR_TRY(aux_begin(ctx, &aux));
+  OFRR_TRY(gemm_impl(aux, 1, 0, tq, tq, pmc, pmo, b, b, m, 1.0, U, ldu, U, ldu, 0.0, tmpu, b));
+  OFRR_TRY(cast_impl(aux, pmo, OFRR_F64, b, b, tmpu, b, UU, b));
+  OFRR_TRY(gemm_impl(aux, 1, 0, tq, tq, pmc, pmo, b, b, n, 1.0, V, ldv, V, ldv, 0.0, tmpv, b));
+  OFRR_TRY(cast_impl(aux, pmo, OFRR_F64, b, b, tmpv, b, VV, b));
+  OFRR_TRY(op.apply(ctx, 0, ta, pAmc, Va, ldva, b, pAmc, pAmo, AV, m));
   OFRR_TRY(gemm_impl(ctx, 1, 0, tq, pAmo, pmc, pmo, b, b, m, 1.0, U, ldu, AV, m, 0.0, tmp, b));
   OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, B, b));
-  OFRR_TRY(gemm_impl(ctx, 1, 0, tq, tq, pmc, pmo, b, b, m, 1.0, U, ldu, U, ldu, 0.0, tmp, b));
-  OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, UU, b));
-  OFRR_TRY(gemm_impl(ctx, 1, 0, tq, tq, pmc, pmo, b, b, n, 1.0, V, ldv, V, ldv, 0.0, tmp, b));
-  OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, VV, b));
+  OFRR_TRY(aux_end(ctx));
   if (fast && b <= 128) {
     // the same pencil through two Cholesky factors: sigma, Zf = Lu^-T Y, Wf = Lv^-T X;
     // U Zf and V Wf are the unit singular-vector estimates (svd_rr.m's sqrt(2) U Z and sqrt(2) V W)
@@ -560,10 +566,13 @@ int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* 
       lu = m;
       lv = n;
     }
+    // the two back-transforms are independent: V's on the auxiliary stream
+    OFRR_TRY(aux_begin(ctx, &aux));
+    OFRR_TRY(gemm_impl(aux, 0, 0, tq, OFRR_F64, pmc, pmo, n, b, b, 1.0, V, ldv, Wf, b, 0.0, Vo, lv));
+    if (Vo != Vout) OFRR_TRY(cast_impl(aux, pmo, tq, n, b, Vo, lv, Vout, ldvo));
     OFRR_TRY(gemm_impl(ctx, 0, 0, tq, OFRR_F64, pmc, pmo, m, b, b, 1.0, U, ldu, Zf, b, 0.0, Uo, lu));
-    OFRR_TRY(gemm_impl(ctx, 0, 0, tq, OFRR_F64, pmc, pmo, n, b, b, 1.0, V, ldv, Wf, b, 0.0, Vo, lv));
     if (Uo != Uout) OFRR_TRY(cast_impl(ctx, pmo, tq, m, b, Uo, lu, Uout, lduo));
-    if (Vo != Vout) OFRR_TRY(cast_impl(ctx, pmo, tq, n, b, Vo, lv, Vout, ldvo));
+    OFRR_TRY(aux_end(ctx));
     return OFRR_SUCCESS;
   }
   k_build_aug<<<grid_for(4 * b * b, 256), 256, 0, ctx->stream>>>(b, B, UU, VV, Aext, Mext, gtol);
