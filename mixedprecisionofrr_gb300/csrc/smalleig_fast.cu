@@ -298,10 +298,11 @@ __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restr
 
 // ---- 3b. FP32 one-sided (Hestenes) Jacobi on the columns of G: G V = U Sigma ------------------------
 // The SVD form's starting vectors: the right singular vectors of C directly (better conditioned than
-// an eigen-solve of C'C).  Round-robin pairs, one warp per pair: three dot products reduced with warp
-// shuffles, then the two columns of G and of V rotated; one barrier per round.  A pair rotates when
-// |g_p . g_q| > 3e-5 ||g_p|| ||g_q|| (above FP32 rounding noise); sweeps stop when no pair rotates
-// (at most 12).
+// an eigen-solve of C'C).  Round-robin pairs, one warp per pair: the pair's dot product reduced with
+// warp shuffles (the squared column norms are kept in shared memory, updated with each rotation and
+// recomputed every sweep), then the two columns of G and of V rotated; one barrier per round.  A pair
+// rotates when |g_p . g_q| > 3e-5 ||g_p|| ||g_q|| (above FP32 rounding noise); sweeps stop when no
+// pair rotates (at most 12).
 __global__ void __launch_bounds__(1024) k_jacobi1_f32(int n, const double* __restrict__ Gin, int ldg, int trans,
                                                       double* __restrict__ Vout) {
   extern __shared__ float sm1[];
@@ -309,6 +310,7 @@ __global__ void __launch_bounds__(1024) k_jacobi1_f32(int n, const double* __res
   float* G = sm1;
   float* V = sm1 + n * ld;
   __shared__ int s_any;
+  __shared__ float nrm[128];  // squared column norms, updated with each rotation, recomputed per sweep
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < n * n; e += nt) {
     const int i = e % n, j = e / n;
@@ -320,6 +322,13 @@ __global__ void __launch_bounds__(1024) k_jacobi1_f32(int n, const double* __res
   for (int sweep = 0; sweep < 12 && n > 1; ++sweep) {
     if (tid == 0) s_any = 0;
     __syncthreads();
+    for (int j = warp; j < n; j += nw) {
+      float s2 = 0.f;
+      for (int i = lane; i < n; i += 32) s2 = fmaf(G[i + j * ld], G[i + j * ld], s2);
+      for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      if (lane == 0) nrm[j] = s2;
+    }
+    __syncthreads();
     int any = 0;
     for (int r = 0; r < N - 1; ++r) {
       for (int k = warp; k < npair; k += nw) {
@@ -330,19 +339,11 @@ __global__ void __launch_bounds__(1024) k_jacobi1_f32(int n, const double* __res
           q = t;
         }
         if (q >= n) continue;
-        float a = 0.f, b = 0.f, g = 0.f;
-        for (int i = lane; i < n; i += 32) {
-          const float gp = G[i + p * ld], gq = G[i + q * ld];
-          a = fmaf(gp, gp, a);
-          b = fmaf(gq, gq, b);
-          g = fmaf(gp, gq, g);
-        }
+        float g = 0.f;
+        for (int i = lane; i < n; i += 32) g = fmaf(G[i + p * ld], G[i + q * ld], g);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          a += __shfl_xor_sync(0xffffffffu, a, o);
-          b += __shfl_xor_sync(0xffffffffu, b, o);
-          g += __shfl_xor_sync(0xffffffffu, g, o);
-        }
+        for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
+        const float a = nrm[p], b = nrm[q];
         if (g != 0.f && fabsf(g) > 3e-5f * sqrtf(a * b)) {
           any = 1;
           const float zeta = (b - a) / (2.f * g);
@@ -355,6 +356,11 @@ __global__ void __launch_bounds__(1024) k_jacobi1_f32(int n, const double* __res
             const float vp = V[i + p * ld], vq = V[i + q * ld];
             V[i + p * ld] = c * vp - sn * vq;
             V[i + q * ld] = sn * vp + c * vq;
+          }
+          if (lane == 0) {  // norms after the rotation (exact arithmetic; drift is reset each sweep)
+            const float cc = c * c, ss = sn * sn, cs2 = 2.f * c * sn * g;
+            nrm[p] = cc * a + ss * b - cs2;
+            nrm[q] = ss * a + cc * b + cs2;
           }
         }
       }
