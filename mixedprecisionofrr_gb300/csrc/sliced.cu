@@ -30,7 +30,8 @@ constexpr int LMAX = 4;  // levels kept: pairs with s + t <= 4 (15 of 25), error
 // Integer pipes only (GB300's FP64 pipe is 1/64 rate): the column maximum is taken on the bit
 // patterns of |x|, e_n = frexp exponent of that maximum, and round(x 2^(BETA S - e_n)) is formed from
 // the significand by a right shift with round-half-even (the same value __double2ll_rn gives).
-// Two passes over a (row chunk x column) grid: maxima by atomicMax on the bit patterns, then digits.
+// Columns of up to 8192 entries take one pass (k_slice_cols below); longer ones two passes over a
+// (row chunk x column) grid: maxima by atomicMax on the bit patterns, then digits.
 constexpr int SLICE_T = 256;
 constexpr int SLICE_U = 4;
 constexpr int64_t SLICE_CHUNK = (int64_t)SLICE_T * SLICE_U;  // rows per CTA
@@ -62,16 +63,47 @@ __global__ void __launch_bounds__(SLICE_T) k_slice_max(int64_t K, int64_t N, con
   }
 }
 
+// frexp exponent of a column maximum given as the bit pattern of |x|: m = f 2^e with f in [0.5, 1),
+// so |x| 2^-e < 1 for every entry of the column (0 for an all-zero column)
+__device__ __forceinline__ int colmax_expo(unsigned long long m) {
+  const int bm = (int)(m >> 52);
+  return (m == 0) ? 0 : (bm > 0) ? bm - 1022 : (64 - __clzll((long long)m)) - 1074;
+}
+
+// The S digits of one entry (bit pattern `bits`) of a column with exponent e, stored at col[s * Kp + k]
+__device__ __forceinline__ void slice_store(unsigned long long bits, int e, __nv_bfloat16* __restrict__ col, int64_t Kp,
+                                            int64_t k) {
+  // x = M 2^(be' - 1075) with M the significand (implicit bit for normal numbers, be' = max(be, 1))
+  const int be = (int)((bits >> 52) & 0x7ff);
+  const unsigned long long M = (bits & 0x000fffffffffffffull) | (be > 0 ? (1ull << 52) : 0ull);
+  const int sh = 1075 - (BETA * S) + e - (be > 0 ? be : 1);  // 18 or more unless the maximum is subnormal
+  long long r = 0;
+  if (sh <= 53 && M != 0) {
+    unsigned long long q;
+    if (sh <= 0) {
+      q = M << (-sh);  // subnormal column maximum: exact scaling up
+    } else {
+      q = M >> sh;
+      const unsigned long long rem = M & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+      if (rem > half || (rem == half && (q & 1ull))) ++q;
+    }
+    r = (bits >> 63) ? -(long long)q : (long long)q;
+  }
+#pragma unroll
+  for (int s = S - 1; s > 0; --s) {  // centred base-2^BETA digits, least significant first
+    const long long d = ((r + (1 << (BETA - 1))) & ((1 << BETA) - 1)) - (1 << (BETA - 1));
+    r = (r - d) >> BETA;  // exact: r - d is a multiple of 2^BETA
+    col[(size_t)s * Kp + k] = __float2bfloat16_rn((float)d);  // |d| <= 64
+  }
+  col[k] = __float2bfloat16_rn((float)r);  // leading digit, |r| <= 128: exact in bf16
+}
+
 __global__ void __launch_bounds__(SLICE_T) k_slice_digits(int64_t K, int64_t Kp, int64_t N, const double* __restrict__ X,
                                                           int64_t ldx, const unsigned long long* __restrict__ colmax,
                                                           __nv_bfloat16* __restrict__ stack, int* __restrict__ expo) {
   const int64_t k0 = (int64_t)blockIdx.x * SLICE_CHUNK + threadIdx.x;
   for (int64_t n = blockIdx.y; n < N; n += gridDim.y) {
-    // frexp exponent of the column maximum: m = f 2^e, f in [0.5, 1), so |x| 2^-e < 1 for the column
-    const unsigned long long m = colmax[n];
-    const int bm = (int)(m >> 52);
-    int e = 0;
-    if (m != 0) e = (bm > 0) ? bm - 1022 : (64 - __clzll((long long)m)) - 1074;
+    const int e = colmax_expo(colmax[n]);
     if (blockIdx.x == 0 && threadIdx.x == 0) expo[n] = e;
     const double* x = X + n * ldx;
     __nv_bfloat16* col = stack + (size_t)n * S * Kp;
@@ -85,31 +117,44 @@ __global__ void __launch_bounds__(SLICE_T) k_slice_digits(int64_t K, int64_t Kp,
     for (int u = 0; u < SLICE_U; ++u) {
       const int64_t k = k0 + (int64_t)u * SLICE_T;
       if (k >= Kp) break;
-      // x = M 2^(be' - 1075) with M the significand (implicit bit for normal numbers, be' = max(be, 1))
-      const unsigned long long bits = v[u];
-      const int be = (int)((bits >> 52) & 0x7ff);
-      const unsigned long long M = (bits & 0x000fffffffffffffull) | (be > 0 ? (1ull << 52) : 0ull);
-      const int sh = 1075 - (BETA * S) + e - (be > 0 ? be : 1);  // 18 or more unless the maximum is subnormal
-      long long r = 0;
-      if (sh <= 53 && M != 0) {
-        unsigned long long q;
-        if (sh <= 0) {
-          q = M << (-sh);  // subnormal column maximum: exact scaling up
-        } else {
-          q = M >> sh;
-          const unsigned long long rem = M & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
-          if (rem > half || (rem == half && (q & 1ull))) ++q;
-        }
-        r = (bits >> 63) ? -(long long)q : (long long)q;
-      }
-#pragma unroll
-      for (int s = S - 1; s > 0; --s) {  // centred base-2^BETA digits, least significant first
-        const long long d = ((r + (1 << (BETA - 1))) & ((1 << BETA) - 1)) - (1 << (BETA - 1));
-        r = (r - d) >> BETA;  // exact: r - d is a multiple of 2^BETA
-        col[(size_t)s * Kp + k] = __float2bfloat16_rn((float)d);  // |d| <= 64
-      }
-      col[k] = __float2bfloat16_rn((float)r);  // leading digit, |r| <= 128: exact in bf16
+      slice_store(v[u], e, col, Kp, k);
     }
+  }
+}
+
+// Single-pass form for columns of at most SC_T * U entries: one CTA per column keeps the column in
+// registers, takes its maximum with a block reduction and writes the digits (no second read, no
+// atomics, no zeroed scratch).
+constexpr int SC_T = 512;
+template <int U>
+__global__ void __launch_bounds__(SC_T) k_slice_cols(int64_t K, int64_t Kp, int64_t N, const double* __restrict__ X,
+                                                     int64_t ldx, __nv_bfloat16* __restrict__ stack,
+                                                     int* __restrict__ expo) {
+  __shared__ unsigned long long red[SC_T / 32];
+  for (int64_t n = blockIdx.x; n < N; n += gridDim.x) {
+    const double* x = X + n * ldx;
+    unsigned long long v[U];
+    unsigned long long mx = 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t k = threadIdx.x + (int64_t)u * SC_T;
+      v[u] = (k < K) ? (unsigned long long)__double_as_longlong(x[k]) : 0ull;
+      mx = max(mx, v[u] & 0x7fffffffffffffffull);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+#pragma unroll
+    for (int w = 0; w < SC_T / 32; ++w) mx = max(mx, red[w]);
+    const int e = colmax_expo(mx);
+    if (threadIdx.x == 0) expo[n] = e;
+    __nv_bfloat16* col = stack + (size_t)n * S * Kp;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t k = threadIdx.x + (int64_t)u * SC_T;
+      if (k < Kp) slice_store(v[u], e, col, Kp, k);
+    }
+    __syncthreads();  // red is reused by the next column
   }
 }
 
@@ -331,6 +376,20 @@ int sliced_prepare_into(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, in
   out->M = M;
   out->stack = stack;
   out->expo = expo;
+  if (out->Kp <= slice::SC_T * 16) {
+    const unsigned grid = (unsigned)std::min<int64_t>(M, 65535);
+    const int64_t u = (out->Kp + slice::SC_T - 1) / slice::SC_T;
+    if (u <= 2)
+      slice::k_slice_cols<2><<<grid, slice::SC_T, 0, ctx->stream>>>(K, out->Kp, M, X, ldx, stack, expo);
+    else if (u <= 4)
+      slice::k_slice_cols<4><<<grid, slice::SC_T, 0, ctx->stream>>>(K, out->Kp, M, X, ldx, stack, expo);
+    else if (u <= 8)
+      slice::k_slice_cols<8><<<grid, slice::SC_T, 0, ctx->stream>>>(K, out->Kp, M, X, ldx, stack, expo);
+    else
+      slice::k_slice_cols<16><<<grid, slice::SC_T, 0, ctx->stream>>>(K, out->Kp, M, X, ldx, stack, expo);
+    OFRR_LAUNCHED(ctx, "k_slice_cols");
+    return OFRR_SUCCESS;
+  }
   int st = OFRR_SUCCESS;
   WsScope scope(ctx);
   unsigned long long* colmax = ws_get<unsigned long long>(ctx, (size_t)M, &st);

@@ -73,7 +73,7 @@ def test_tc_exact_small_integers(api):
 
 
 @pytest.mark.parametrize("M,N,K", [(2048, 64, 8192), (8192, 64, 2048), (64, 64, 8192), (300, 17, 1000), (77, 5, 64),
-                                   (20000, 64, 512), (1000, 130, 3000), (128, 64, 1)])
+                                   (20000, 64, 512), (1000, 130, 3000), (128, 64, 1), (96, 16, 9000)])
 def test_f64_emulated_gemm(api, M, N, K):
     """Exact-slice FP64 emulation: element error within 2^-33 |A'| |B| (two bits of margin over the
     2^-35 design bound), on operands with widely varying column scales."""
