@@ -114,7 +114,21 @@ int after_launch(ofrr_ctx* ctx, const char* name) {
 }
 
 int sync_and_check(ofrr_ctx* ctx) {
+  // words 2..4 of this context and of its auxiliary context (ordered behind ctx's stream by aux_end)
+  OFRR_CUDA(cudaMemcpyAsync(ctx->host_flags, ctx->dev_flags + kFlagTcWait, 3 * sizeof(int), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+  if (ctx->aux)
+    OFRR_CUDA(cudaMemcpyAsync(ctx->host_flags + 3, ctx->aux->dev_flags + kFlagTcWait, 3 * sizeof(int),
+                              cudaMemcpyDeviceToHost, ctx->stream));
   OFRR_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int* h = ctx->host_flags;
+  const bool timed_out = h[0] || h[2] || (ctx->aux && (h[3] || h[5]));
+  if (timed_out) {
+    OFRR_CUDA(cudaMemsetAsync(ctx->dev_flags + kFlagTcWait, 0, 3 * sizeof(int), ctx->stream));
+    if (ctx->aux) OFRR_CUDA(cudaMemsetAsync(ctx->aux->dev_flags + kFlagTcWait, 0, 3 * sizeof(int), ctx->stream));
+    OFRR_CUDA(cudaStreamSynchronize(ctx->stream));
+    return OFRR_ERR_DEVICE_TIMEOUT;
+  }
   return OFRR_SUCCESS;
 }
 
@@ -154,10 +168,7 @@ __global__ void k_randn(uint64_t key, int64_t n, int64_t k, T* out, int64_t ld) 
 // --------------------------------------------------------------------------------------
 template <class TI, class TO>
 __global__ void k_cast(int64_t m, int64_t n, const TI* in, int64_t ldin, TO* out, int64_t ldout) {
-  const int64_t total = m * n;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    int64_t i = e % m, j = e / m;
+  OFRR_FOR_2D(i, j, m, n) {
     // through FP32 when neither side is FP64 (exact: every 16/32-bit value is a float; RN once)
     if constexpr (std::is_same<TI, double>::value || std::is_same<TO, double>::value)
       out[i + j * ldout] = from_c<TO, double>(to_c<double, TI>(in[i + j * ldin]));
@@ -330,10 +341,9 @@ __global__ void k_iamax(int64_t n, const T* x, ArgMax* partial, unsigned int* co
 
 template <class T>
 __global__ void k_special(int64_t m, int64_t n, const T* A, int64_t lda, int* flags) {
-  const int64_t total = m * n;
   int nan = 0, inf = 0;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    double v = to_c<double, T>(A[(e % m) + (e / m) * lda]);
+  OFRR_FOR_2D(i, j, m, n) {
+    double v = to_c<double, T>(A[i + j * lda]);
     if (isnan(v)) nan = 1;
     else if (isinf(v)) inf = 1;
   }
@@ -390,7 +400,7 @@ int cast_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, int64_t m, int64_t
               void* out, int64_t ldout) {
   if (m <= 0 || n <= 0) return OFRR_SUCCESS;
   OFRR_DISPATCH_STORAGE(tin, TI, OFRR_DISPATCH_STORAGE(tout, TO, {
-    k_cast<TI, TO><<<grid_for(m * n, 256), 256, 0, ctx->stream>>>(m, n, (const TI*)in, ldin, (TO*)out, ldout);
+    k_cast<TI, TO><<<grid_2d(m, n, 256), 256, 0, ctx->stream>>>(m, n, (const TI*)in, ldin, (TO*)out, ldout);
     OFRR_LAUNCHED(ctx, "k_cast");
   }));
   return OFRR_SUCCESS;
@@ -528,6 +538,8 @@ int ofrr_ctx_create(ofrr_ctx** out, int device, void* stream) {
     ctx->pinned_size = 1 << 20;
     e = cudaMallocHost(&ctx->pinned, ctx->pinned_size);
   }
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->host_flags, 8 * sizeof(int));
+  if (e == cudaSuccess) memset(ctx->host_flags, 0, 8 * sizeof(int));
   if (e != cudaSuccess) {
     ofrr_ctx_destroy(ctx);
     return map_cuda_error(e);
@@ -547,6 +559,7 @@ int ofrr_ctx_destroy(ofrr_ctx* ctx) {
   if (ctx->dev_flags) cudaFree(ctx->dev_flags);
   if (ctx->dev_counters) cudaFree(ctx->dev_counters);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  if (ctx->host_flags) cudaFreeHost(ctx->host_flags);
   if (ctx->cublas) cublasDestroy(ctx->cublas);
   if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -677,7 +690,7 @@ int ofrr_check_special_values(ofrr_ctx* ctx, ofrr_dtype dt, int64_t m, int64_t n
   if (!A || lda < m) return OFRR_ERR_INVALID_ARGUMENT;
   OFRR_CUDA(cudaMemsetAsync(ctx->dev_flags, 0, sizeof(int), ctx->stream));
   OFRR_DISPATCH_STORAGE(dt, T, {
-    k_special<T><<<grid_for(m * n, 256, 1024), 256, 0, ctx->stream>>>(m, n, (const T*)A, lda, ctx->dev_flags);
+    k_special<T><<<grid_2d(m, n, 256), 256, 0, ctx->stream>>>(m, n, (const T*)A, lda, ctx->dev_flags);
     OFRR_LAUNCHED(ctx, "k_special");
   });
   int* hp = (int*)ctx->pinned;

@@ -155,10 +155,10 @@ template <class TOUT>
 __global__ void k_splitk_reduce(int M, int N, int splits, const float* __restrict__ partial, TOUT* __restrict__ D,
                                 int64_t ldd) {
   const int64_t total = (int64_t)M * N;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+  OFRR_FOR_2D(m, n, M, N) {
+    const int64_t e = m + n * (int64_t)M;
     float s = 0.f;
     for (int z = 0; z < splits; ++z) s += partial[(size_t)z * total + e];  // fixed order: deterministic
-    const int64_t m = e % M, n = e / M;
     D[m + n * ldd] = cvt_out<TOUT>(s);
   }
 }
@@ -186,10 +186,10 @@ static int launch(ofrr_ctx* ctx, const CUtensorMap& ma, const CUtensorMap& mb, i
   }
   dim3 grid(gm, gn, splits);
   k_gemm_tn<BN, TOUT><<<grid, THREADS, smem, ctx->stream>>>(ma, mb, M, N, kbt, kbps, make_idesc(t16, BN), D, ldd,
-                                                            partial, ctx->dev_flags + 2);
+                                                            partial, ctx->dev_flags + kFlagTcWait);
   OFRR_LAUNCHED(ctx, "k_gemm_tn");
   if (splits > 1) {
-    k_splitk_reduce<TOUT><<<grid_for((int64_t)M * N, 256, 1024), 256, 0, ctx->stream>>>(M, N, splits, partial, D, ldd);
+    k_splitk_reduce<TOUT><<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, splits, partial, D, ldd);
     OFRR_LAUNCHED(ctx, "k_splitk_reduce");
   }
   return OFRR_SUCCESS;

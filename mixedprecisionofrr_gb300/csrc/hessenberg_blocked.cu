@@ -21,6 +21,7 @@
 #include <cstdlib>
 
 #include "ofrr_internal.cuh"
+#include "tcgen05.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -151,33 +152,59 @@ __global__ void __launch_bounds__(HB_UT) k_hess_blockupd(int64_t m, int c0, int 
 // the order j = 0, 1, ..., u-1 with the same operands, so the result is bit-identical to the
 // left-looking per-column kernel.
 template <class TO>
-struct HbCand {
+struct __align__(16) HbCand {
   long long key;  // argmax key of the local max |value| (-1: the CTA has no rows)
   long long i;    // its row
   TO vals[HB_B];  // the block's current values in that row
 };
+constexpr int HB_CL_MAX = 16;
 
+__device__ __forceinline__ uint32_t cluster_addr(const void* p, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(tc::smem_u32(p)), "r"(rank));
+  return r;
+}
+
+// Candidates travel by push: each CTA stores its candidate for column t into slot [rank] of every
+// CTA's receive buffer t & 1 with st.async (16-byte remote stores completing on the receiver's
+// mbarrier), so a column costs one one-way DSMEM transfer instead of a cluster barrier plus remote
+// reads.  Buffer / barrier t & 1 is reused for column t + 2 only after every CTA has received all
+// candidates of column t + 1, which each CTA sends after it finished reading column t's buffer.
+// Within a CTA the argmax of column t + 1 takes one barrier: every warp leaves its (key, row) in
+// shared memory and warp 0 alone combines them and sends.
 template <class TO, class TC, bool FAST>
 __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0, int c1, TO* __restrict__ Q,
                                                        int64_t ldq, int* __restrict__ select, int* __restrict__ perm,
                                                        double* __restrict__ R, double select_tol,
-                                                       int64_t rows_per_cta) {
+                                                       int64_t rows_per_cta, int* __restrict__ err) {
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const int ncl = (int)cluster.num_blocks();
   const int nb = c1 - c0;
-  const int tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int64_t RR = rows_per_cta;
   const int64_t r0 = (int64_t)rank * RR;
   const int64_t r1 = (r0 + RR < m) ? r0 + RR : m;
   const int nloc = (r1 > r0) ? (int)(r1 - r0) : 0;
+  constexpr uint32_t CB = sizeof(HbCand<TO>);
+  constexpr int NCH = (int)(CB / 16);  // 16-byte chunks per candidate
+  static_assert(CB % 16 == 0, "candidates move in 16-byte stores");
   extern __shared__ unsigned char smem_raw[];
   TO* s_blk = reinterpret_cast<TO*>(smem_raw);  // HB_B columns x RR rows (column t at t * RR)
-  __shared__ HbCand<TO> s_cand[2];              // double-buffered by column parity
+  __shared__ HbCand<TO> s_recv[2][HB_CL_MAX];   // candidates of column t in [t & 1][source rank]
+  __shared__ HbCand<TO> s_send;                 // this CTA's candidate, staged for the stores
+  __shared__ __align__(8) uint64_t s_bar[2];
   __shared__ ArgMaxK red[HB_T / 32];
-  __shared__ TO s_pr[HB_B];                     // pivot row of the current column (current values)
-  __shared__ long long s_k;
+  __shared__ int s_abort;
 
+  if (tid == 0) {
+    tc::mbar_init(&s_bar[0], 1);
+    tc::mbar_init(&s_bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    tc::mbar_expect_tx(&s_bar[0], ncl * CB);
+    if (nb > 1) tc::mbar_expect_tx(&s_bar[1], ncl * CB);
+    s_abort = 0;
+  }
   for (int lr = tid; lr < nloc; lr += HB_T) {
     TO v[HB_B];
 #pragma unroll
@@ -185,6 +212,36 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
 #pragma unroll
     for (int t = 0; t < HB_B; ++t) s_blk[(size_t)t * RR + lr] = v[t];
   }
+  cluster.sync();  // every CTA's barriers are armed before the first push
+
+  // Warp argmax `a` of every warp -> this CTA's candidate for column t, sent to all CTAs.  Called by
+  // all threads; the caller's writes to s_blk precede the barrier here.
+  auto publish = [&](int t, ArgMaxK a) {
+    a = warp_argmaxk_all(a);
+    if (lane == 0) red[wid] = a;
+    __syncthreads();
+    if (wid == 0) {
+      ArgMaxK loc = (lane < HB_T / 32) ? red[lane] : ArgMaxK{-1, 0x7fffffffffffffffLL};
+      loc = warp_argmaxk_all(loc);
+      if (lane < HB_B) {
+        s_send.vals[lane] = (loc.key >= 0 && lane < nb) ? s_blk[(size_t)lane * RR + (loc.i - r0)] : TO(0);
+        if (lane == 0) {
+          s_send.key = loc.key;
+          s_send.i = loc.i;
+        }
+      }
+      __syncwarp();
+      const uint64_t* src = reinterpret_cast<const uint64_t*>(&s_send);
+      for (int x = lane; x < ncl * NCH; x += 32) {
+        const int d = x / NCH, c = x - d * NCH;
+        asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.b64 [%0], {%1, %2}, [%3];" ::"r"(
+                         cluster_addr(reinterpret_cast<const char*>(&s_recv[t & 1][rank]) + 16 * c, d)),
+                     "l"(src[2 * c]), "l"(src[2 * c + 1]), "r"(cluster_addr(&s_bar[t & 1], d))
+                     : "memory");
+      }
+    }
+  };
+
   const double tol_o = to_c<double, TO>(from_c<TO, double>(select_tol));
   {  // candidate for column 0 (already eliminated against the columns before the block)
     ArgMaxK a{-1, 0x7fffffffffffffffLL};
@@ -192,38 +249,24 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
       const long long key = amax_key(s_blk[lr]);
       if (key > a.key) a = ArgMaxK{key, r0 + lr};
     }
-    const ArgMaxK loc = block_argmaxk(a, red);
-    if (tid == 0) {
-      s_cand[0].key = loc.key;
-      s_cand[0].i = loc.i;
-    }
-    if (tid < HB_B) s_cand[0].vals[tid] = (loc.key >= 0 && tid < nb) ? s_blk[(size_t)tid * RR + (loc.i - r0)] : TO(0);
+    publish(0, a);
   }
 
   for (int t = 0; t < nb; ++t) {
-    // (1) one cluster barrier; the winner among all CTAs' candidates (lowest row among equal maxima)
-    cluster.sync();
-    HbCand<TO>& cand = s_cand[t & 1];
-    if (tid < 32) {
-      ArgMaxK b{-1, 0x7fffffffffffffffLL};
-      if (lane < ncl) {
-        const HbCand<TO>* pq = cluster.map_shared_rank(&cand, lane);
-        b.key = pq->key;
-        b.i = pq->i;
-      }
-      b = warp_argmaxk(b);
-      const long long bk = __shfl_sync(0xffffffffu, b.key, 0);
-      const long long bi = __shfl_sync(0xffffffffu, b.i, 0);
-      const int owner = (bk < 0) ? 0 : (int)(bi / RR);
-      if (lane < HB_B) {
-        const HbCand<TO>* po = cluster.map_shared_rank(&cand, owner);
-        s_pr[lane] = po->vals[lane];
-      }
-      if (lane == 0) s_k = (bk < 0) ? 0 : bi;
-    }
-    __syncthreads();
-    const long long k = s_k;
-    const TO pv = s_pr[t];
+    // (1) all candidates of column t; the winner (lowest row among equal maxima), in every warp
+    const int b = t & 1;
+    if (!tc::mbar_wait(&s_bar[b], (uint32_t)((t >> 1) & 1), err, 41)) s_abort = 1;
+    if (tid == 0 && t + 2 < nb) tc::mbar_expect_tx(&s_bar[b], ncl * CB);  // re-arm for column t + 2
+    const HbCand<TO>* rc = s_recv[b];
+    ArgMaxK w{-1, 0x7fffffffffffffffLL};
+    if (lane < ncl) w = ArgMaxK{rc[lane].key, rc[lane].i};
+    const ArgMaxK mine = w;
+    w = warp_argmaxk_all(w);
+    const long long bk = w.key, bi = w.i;
+    const unsigned hit = __ballot_sync(0xffffffffu, lane < ncl && mine.key == bk && mine.i == bi);
+    const TO* pr = rc[hit ? __ffs(hit) - 1 : 0].vals;  // the pivot row's current values
+    const long long k = (bk < 0) ? 0 : bi;
+    const TO pv = pr[t];
     const bool keep = absd(pv) >= tol_o;
     // (2) bookkeeping (rank 0): pivot, selection, row i of R (R(i, c0+u) = r_{t,u} for u > t)
     if (rank == 0) {
@@ -234,7 +277,7 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
         R[i + (int64_t)i * n] = to_c<double, TO>(pv);
       }
       for (int u = t + 1 + tid; u < nb; u += blockDim.x)
-        R[i + (int64_t)(c0 + u) * n] = keep ? to_c<double, TC>(to_c<TC, TO>(s_pr[u])) : 0.0;
+        R[i + (int64_t)(c0 + u) * n] = keep ? to_c<double, TC>(to_c<TC, TO>(pr[u])) : 0.0;
     }
     // (3) scale (or zero) column t, eliminate the later block columns against it, argmax of column t+1
     const TC pc = to_c<TC, TO>(pv);
@@ -253,7 +296,7 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
         const TC qs = to_c<TC, TO>(so);
         for (int u = t + 1; u < nb; ++u) {
           TO* e = row + (size_t)u * RR;
-          *e = from_c<TO, TC>(elim<FAST>(to_c<TC, TO>(*e), to_c<TC, TO>(s_pr[u]), qs));
+          *e = from_c<TO, TC>(elim<FAST>(to_c<TC, TO>(*e), to_c<TC, TO>(pr[u]), qs));
         }
       } else {
         row[(size_t)t * RR] = TO(0);
@@ -263,15 +306,9 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
         if (key > a.key) a = ArgMaxK{key, r0 + lr};
       }
     }
-    if (has_next) {  // publish the candidate for column t+1 (its buffer was last read before this barrier)
-      const ArgMaxK loc = block_argmaxk(a, red);
-      HbCand<TO>& nc = s_cand[(t + 1) & 1];
-      if (tid == 0) {
-        nc.key = loc.key;
-        nc.i = loc.i;
-      }
-      if (tid < HB_B) nc.vals[tid] = (loc.key >= 0 && tid < nb) ? s_blk[(size_t)tid * RR + (loc.i - r0)] : TO(0);
-    }
+    if (!has_next) break;
+    publish(t + 1, a);  // its barrier also makes s_abort visible to every thread
+    if (s_abort) break;  // a peer stopped answering: leave (the status word is set)
   }
   __syncthreads();
   for (int lr = tid; lr < nloc; lr += HB_T) {
@@ -279,7 +316,7 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
     for (int t = 0; t < HB_B; ++t)
       if (t < nb) Q[r0 + lr + (int64_t)(c0 + t) * ldq] = s_blk[(size_t)t * RR + lr];
   }
-  cluster.sync();  // no CTA leaves while another may still read its candidates
+  cluster.sync();  // every push into this CTA has landed before any CTA leaves
 }
 
 // shared memory the in-block kernel needs for m rows on ncl CTAs (0 if it does not fit)
@@ -368,7 +405,7 @@ int hess_run_blocked_t(ofrr_ctx* ctx, int64_t m, int n, TO* Q, int64_t ldq, doub
       OFRR_LAUNCHED(ctx, "k_hess_blockupd");
     }
     OFRR_CUDA(cudaLaunchKernelEx(&cfg, k_hess_inblock<TO, TC, FAST>, m, n, c0, c1, Q, ldq, select, perm, R, select_tol,
-                                 RR));
+                                 RR, ctx->dev_flags + kFlagHessWait));
     OFRR_LAUNCHED(ctx, "k_hess_inblock");
   }
   return OFRR_SUCCESS;

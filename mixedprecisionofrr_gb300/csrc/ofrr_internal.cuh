@@ -70,6 +70,7 @@ struct ofrr_ctx {
   unsigned long long launches = 0;        // kernels of this library
   unsigned long long library_calls = 0;   // cuBLAS calls (library kernels, counted apart)
   int* dev_flags = nullptr;        // device status words written by kernels (bounded waits etc.)
+  int* host_flags = nullptr;       // pinned copy of the wait-timeout words, read after each stream sync
   unsigned int* dev_counters = nullptr;  // grid "last block" counters (self-resetting)
   void* pinned = nullptr;          // small pinned host staging buffer
   bool emulate_f64 = false;        // FP64 TN products through exact BF16 slices on the tensor cores
@@ -103,6 +104,14 @@ struct WsScope {
 int after_launch(ofrr_ctx* ctx, const char* name);
 #define OFRR_LAUNCHED(ctx, name) OFRR_TRY(ofrr::after_launch((ctx), (name)))
 
+// Device status words (ctx->dev_flags): 0 special values found by the input check, 1 small-solver
+// breakdown, 2 a tcgen05 pipeline wait that ran out (TMA / MMA / epilogue barriers), 3 non-convergence
+// of the nonsymmetric small solver, 4 a cluster wait of the blocked Hessenberg build that ran out.
+constexpr int kFlagTcWait = 2;
+constexpr int kFlagHessWait = 4;
+
+// Synchronise ctx's stream; OFRR_ERR_DEVICE_TIMEOUT when a bounded device wait gave up since the
+// last check (the words are cleared again).
 int sync_and_check(ofrr_ctx* ctx);
 
 // Concurrency inside one solve: aux_begin() returns the context's auxiliary context (created on
@@ -278,6 +287,22 @@ __device__ __forceinline__ ArgMaxK warp_argmaxk(ArgMaxK a) {
   }
   return a;
 }
+// Same result as warp_argmaxk, in every lane, from three warp-wide integer reductions (redux.sync):
+// the larger key (as two 32-bit halves), then the lowest row among lanes holding it.  Rows must lie
+// in [0, 2^32 - 2] for non-empty entries.
+__device__ __forceinline__ ArgMaxK warp_argmaxk_all(ArgMaxK a) {
+  const unsigned long long k1 = (unsigned long long)(a.key + 1);  // 0: empty
+  const unsigned hi = (unsigned)(k1 >> 32), lo = (unsigned)k1;
+  const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+  const bool win = (hi == mhi && lo == mlo);
+  const unsigned mi = __reduce_min_sync(0xffffffffu, win ? (unsigned)a.i : 0xffffffffu);
+  ArgMaxK r;
+  r.key = (long long)(((unsigned long long)mhi << 32) | mlo) - 1;
+  r.i = (r.key >= 0) ? (long long)mi : 0x7fffffffffffffffLL;
+  return r;
+}
+
 // block-wide argmax, result returned to every thread.  smem needs blockDim/32 entries.
 __device__ __forceinline__ ArgMaxK block_argmaxk(ArgMaxK a, ArgMaxK* smem) {
   a = warp_argmaxk(a);
@@ -319,6 +344,23 @@ inline int grid_for(long long n, int block, int cap = 152 * 16) {
   if (g > cap) g = cap;
   return (int)g;
 }
+
+// Element-wise kernels over an m x n column-major matrix run on a 2-D grid (rows along x, columns
+// along y) instead of dividing a flat 64-bit index (a 64-bit division is a long software sequence);
+// about 4096 CTAs at most, each thread striding over rows.
+inline dim3 grid_2d(long long m, long long n, int block) {
+  long long gy = n < 1 ? 1 : (n > 65535 ? 65535 : n);
+  long long gx = (m + block - 1) / block;
+  long long cap = 4096 / gy;
+  if (cap < 1) cap = 1;
+  if (gx > cap) gx = cap;
+  if (gx < 1) gx = 1;
+  return dim3((unsigned)gx, (unsigned)gy);
+}
+#define OFRR_FOR_2D(i, j, m, n)                                                   \
+  for (int64_t j = blockIdx.y; j < (int64_t)(n); j += gridDim.y)                  \
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)(m); \
+         i += (int64_t)gridDim.x * blockDim.x)
 
 // ---- cross-file internal API ---------------------------------------------------------
 // dense / sparse products into caller buffers (all on ctx->stream, no host sync)

@@ -63,6 +63,27 @@ __global__ void __launch_bounds__(SLICE_T) k_slice_max(int64_t K, int64_t N, con
   }
 }
 
+// s 2^e as a double, rounded once to nearest-even (the value (double)s then an exact power-of-two
+// scaling gives), built on the integer pipes: GB300's FP64 pipe runs at 1/64 of the FP32 rate and a
+// 64-bit integer conversion plus ldexp per element would bound the product's epilogue.  Results
+// outside the normal range (never met by scaled operands of moderate range) take the FP64 path.
+// |s| < 2^63 (the combined sums are bounded well below that).
+__device__ __forceinline__ double i64_ldexp(long long s, int e) {
+  if (s == 0) return 0.0;
+  const unsigned long long sign = (s < 0) ? (1ull << 63) : 0ull;
+  const unsigned long long u = (s < 0) ? (unsigned long long)(-s) : (unsigned long long)s;
+  const int lz = __clzll((long long)u);
+  const int be = (63 - lz) + e + 1023;  // biased exponent of the result (u in [2^(63-lz), 2^(64-lz)))
+  if (be <= 0 || be >= 2047) return ldexp((double)s, e);
+  const unsigned long long v = u << lz;  // leading one at bit 63
+  unsigned long long mant = v >> 11;     // 53 significant bits
+  const unsigned long long rem = v & 0x7ffull;
+  if (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ++mant;
+  // the leading one (bit 52) lifts the exponent field from be - 1 to be; a rounding carry to 2^53
+  // lifts it once more, and an exponent of 2047 with a zero fraction is the infinity RN gives
+  return __longlong_as_double((long long)(sign | (((unsigned long long)(be - 1) << 52) + mant)));
+}
+
 // frexp exponent of a column maximum given as the bit pattern of |x|: m = f 2^e with f in [0.5, 1),
 // so |x| 2^-e < 1 for every entry of the column (0 for an all-zero column)
 __device__ __forceinline__ int colmax_expo(unsigned long long m) {
@@ -93,9 +114,9 @@ __device__ __forceinline__ void slice_store(unsigned long long bits, int e, __nv
   for (int s = S - 1; s > 0; --s) {  // centred base-2^BETA digits, least significant first
     const long long d = ((r + (1 << (BETA - 1))) & ((1 << BETA) - 1)) - (1 << (BETA - 1));
     r = (r - d) >> BETA;  // exact: r - d is a multiple of 2^BETA
-    col[(size_t)s * Kp + k] = __float2bfloat16_rn((float)d);  // |d| <= 64
+    col[(size_t)s * Kp + k] = __float2bfloat16_rn((float)(int)d);  // |d| <= 64
   }
-  col[k] = __float2bfloat16_rn((float)r);  // leading digit, |r| <= 128: exact in bf16
+  col[k] = __float2bfloat16_rn((float)(int)r);  // leading digit, |r| <= 128: exact in bf16
 }
 
 __global__ void __launch_bounds__(SLICE_T) k_slice_digits(int64_t K, int64_t Kp, int64_t N, const double* __restrict__ X,
@@ -317,9 +338,9 @@ __global__ void __launch_bounds__(SL_THREADS, 1)
       for (int L = 0; L <= LMAX; ++L) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(L * SBN + c), v);
-        const long long w = 1ll << (BETA * (LMAX - L));
+        // every level sum is an integer below 2^25 in magnitude (at most 1024 terms of at most 2^14.3)
 #pragma unroll
-        for (int j = 0; j < 16; ++j) acc[j] += (long long)__float2ll_rn(v[j]) * w;
+        for (int j = 0; j < 16; ++j) acc[j] += (long long)__float2int_rn(v[j]) * (1ll << (BETA * (LMAX - L)));
       }
       if (!ok || nkb == 0) {
 #pragma unroll
@@ -337,7 +358,7 @@ __global__ void __launch_bounds__(SL_THREADS, 1)
 #pragma unroll 4
           for (int j = 0; j < 16; ++j) {
             const int n = n0 + c + j;
-            if (n < N) C[row + (size_t)n * ldc] = ldexp((double)acc[j], erow + eb[n] - SL_SHIFT);
+            if (n < N) C[row + (size_t)n * ldc] = i64_ldexp(acc[j], erow + eb[n] - SL_SHIFT);
           }
         }
       }
@@ -356,11 +377,11 @@ __global__ void k_sliced_finish(int64_t M, int64_t N, int splits, const long lon
                                 double* __restrict__ C, int64_t ldc, const int* __restrict__ ea,
                                 const int* __restrict__ eb) {
   const int64_t total = M * N;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+  OFRR_FOR_2D(m, n, M, N) {
+    const int64_t e = m + n * M;
     long long s = 0;
     for (int z = 0; z < splits; ++z) s += P[(size_t)z * total + e];
-    const int64_t m = e % M, n = e / M;
-    C[m + n * ldc] = ldexp((double)s, ea[m] + eb[n] - SL_SHIFT);
+    C[m + n * ldc] = i64_ldexp(s, ea[m] + eb[n] - SL_SHIFT);
   }
 }
 
@@ -458,7 +479,7 @@ static int sliced_gemm_run(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, con
   for (int r = 0; r < (reps > 1 ? reps : 1); ++r) {
     k_sliced_tn<<<grid, SL_THREADS, SL_SMEM, ctx->stream>>>(ma, mb, (int)M, (int)N, Kp, kbt, kbps,
                                                           tc::make_idesc(OFRR_BF16, SBN), P, C, ldc, A.expo, Bs.expo,
-                                                          ctx->dev_flags + 2);
+                                                          ctx->dev_flags + kFlagTcWait);
     OFRR_LAUNCHED(ctx, "k_sliced_tn");
   }
   if (reps > 1) {
@@ -473,7 +494,7 @@ static int sliced_gemm_run(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, con
       *bytes = (double)S * Kp * 2 * (double)(M + N) + (double)M * N * 8 * (splits > 1 ? splits : 1);
   }
   if (splits > 1) {
-    k_sliced_finish<<<grid_for(M * N, 256, 2048), 256, 0, ctx->stream>>>(M, N, splits, P, C, ldc, A.expo, Bs.expo);
+    k_sliced_finish<<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, splits, P, C, ldc, A.expo, Bs.expo);
     OFRR_LAUNCHED(ctx, "k_sliced_finish");
   }
   return OFRR_SUCCESS;

@@ -276,21 +276,22 @@ int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype t
   return OFRR_SUCCESS;
 }
 
+// at most 4 CTAs per column: each thread handles several rows of one column
+inline dim3 grid_cols(int64_t m, int64_t n) {
+  return dim3(std::min(grid_2d(m, n, 256).x, 4u), (unsigned)std::min<int64_t>(n, 65535));
+}
+
 __global__ void k_normalize_cols(int64_t m, int64_t n, double* X, const double* nrm);
 
 // |X| rounded to T (16-bit), column-major
 template <class TI, class T>
 __global__ void k_abs_cast(int64_t m, int64_t n, const TI* __restrict__ X, int64_t ldx, T* __restrict__ Y,
                            int64_t ldy) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e % m, j = e / m;
-    Y[i + j * ldy] = from_c<T, float>(fabsf(to_c<float, TI>(X[i + j * ldx])));
-  }
+  OFRR_FOR_2D(i, j, m, n) Y[i + j * ldy] = from_c<T, float>(fabsf(to_c<float, TI>(X[i + j * ldx])));
 }
 __global__ void k_abs_cast_f64(int64_t m, int64_t n, const double* __restrict__ X, int64_t ldx, __half* Yh,
                                __nv_bfloat16* Yb, int64_t ldy) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e % m, j = e / m;
+  OFRR_FOR_2D(i, j, m, n) {
     const double a = fabs(X[i + j * ldx]);
     if (Yh) Yh[i + j * ldy] = __double2half(a);
     else Yb[i + j * ldy] = __double2bfloat16(a);
@@ -318,15 +319,15 @@ int emulation_bounds(ofrr_ctx* ctx, Op& op, int trans, ofrr_dtype t16, const dou
   float* Bnd = ws_get<float>(ctx, (size_t)M * k, &st);
   if (!absA || !absX || !Bnd) return st;
   if (t16 == OFRR_F16) {
-    k_abs_cast<__half, __half><<<grid_for(K * M, 256), 256, 0, ctx->stream>>>(K, M, (const __half*)Ap, lda,
+    k_abs_cast<__half, __half><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(K, M, (const __half*)Ap, lda,
                                                                              (__half*)absA, K);
     OFRR_LAUNCHED(ctx, "k_abs_cast");
-    k_abs_cast_f64<<<grid_for(K * k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, (__half*)absX, nullptr, K);
+    k_abs_cast_f64<<<grid_2d(K, k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, (__half*)absX, nullptr, K);
   } else {
-    k_abs_cast<__nv_bfloat16, __nv_bfloat16><<<grid_for(K * M, 256), 256, 0, ctx->stream>>>(
+    k_abs_cast<__nv_bfloat16, __nv_bfloat16><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(
         K, M, (const __nv_bfloat16*)Ap, lda, (__nv_bfloat16*)absA, K);
     OFRR_LAUNCHED(ctx, "k_abs_cast");
-    k_abs_cast_f64<<<grid_for(K * k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, nullptr, (__nv_bfloat16*)absX, K);
+    k_abs_cast_f64<<<grid_2d(K, k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, nullptr, (__nv_bfloat16*)absX, K);
   }
   OFRR_LAUNCHED(ctx, "k_abs_cast_f64");
   OFRR_TRY(gemm_impl(ctx, 1, 0, t16, t16, OFRR_F32, OFRR_F32, M, k, K, 1.0, absA, K, absX, K, 0.0, Bnd, M));
@@ -356,7 +357,7 @@ int residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* X, int64_t l
   double* bnd = nullptr;
   if (certify16 >= 0) {  // emulated A X: add the bound on its error (unit columns)
     OFRR_TRY(dmalloc(ctx, &bnd, (size_t)k));
-    k_normalize_cols<<<grid_for(n * k, 256), 256, 0, ctx->stream>>>(n, k, X64, nrm);
+    k_normalize_cols<<<grid_cols(n, k), 256, 0, ctx->stream>>>(n, k, X64, nrm);
     OFRR_LAUNCHED(ctx, "k_normalize_cols");
     OFRR_TRY(emulation_bounds(ctx, op, 0, (ofrr_dtype)certify16, X64, n, k, bnd));
     OFRR_CUDA(cudaMemcpyAsync(h.data() + 2 * k, bnd, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
@@ -483,8 +484,7 @@ namespace ofrr {
 namespace {
 
 __global__ void k_scale_f64(int64_t m, int64_t n, double* X, int64_t ldx, double s) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x)
-    X[(e % m) + (e / m) * ldx] *= s;
+  OFRR_FOR_2D(i, j, m, n) X[i + j * ldx] *= s;
 }
 
 // Z = Lu^-T Y, W = Lv^-T X from the SVD of C = Lu^-1 B Lv^-T is the same pencil as
@@ -598,9 +598,9 @@ int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* 
   OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, m, b, Uo, m, Un64, m));
   OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, n, b, Vo, n, Vn64, n));
   const double r2 = 1.4142135623730951;
-  k_scale_f64<<<grid_for(m * b, 256), 256, 0, ctx->stream>>>(m, b, Un64, m, r2);
+  k_scale_f64<<<grid_2d(m, b, 256), 256, 0, ctx->stream>>>(m, b, Un64, m, r2);
   OFRR_LAUNCHED(ctx, "k_scale_f64");
-  k_scale_f64<<<grid_for(n * b, 256), 256, 0, ctx->stream>>>(n, b, Vn64, n, r2);
+  k_scale_f64<<<grid_2d(n, b, 256), 256, 0, ctx->stream>>>(n, b, Vn64, n, r2);
   OFRR_LAUNCHED(ctx, "k_scale_f64");
   OFRR_TRY(cast_impl(ctx, OFRR_F64, tq, m, b, Un64, m, Uout, lduo));
   OFRR_TRY(cast_impl(ctx, OFRR_F64, tq, n, b, Vn64, n, Vout, ldvo));
@@ -628,10 +628,15 @@ __global__ void k_rescol2(int64_t m, int64_t n, const double* AV, const double* 
   }
 }
 
+// X(:, j) *= 1 / nrm[j] (columns of zero norm untouched); one reciprocal per thread and column, the
+// FP64 pipe being 1/64 rate.  The unit columns feed residual estimates only.
 __global__ void k_normalize_cols(int64_t m, int64_t n, double* X, const double* nrm) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x) {
-    const double s = nrm[e / m];
-    if (s > 0) X[e] /= s;
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+    const double s = nrm[j];
+    if (!(s > 0)) continue;
+    const double r = 1.0 / s;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+      X[i + j * m] *= r;
   }
 }
 
@@ -651,9 +656,9 @@ int svd_residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* U, int64
   OFRR_TRY(cast_impl(ctx, tx, OFRR_F64, n, k, V, ldv, V64, n));
   OFRR_TRY(column_norms(ctx, OFRR_F64, m, k, U64, m, nr));
   OFRR_TRY(column_norms(ctx, OFRR_F64, n, k, V64, n, nr + k));
-  k_normalize_cols<<<grid_for(m * k, 256), 256, 0, ctx->stream>>>(m, k, U64, nr);
+  k_normalize_cols<<<grid_cols(m, k), 256, 0, ctx->stream>>>(m, k, U64, nr);
   OFRR_LAUNCHED(ctx, "k_normalize_cols");
-  k_normalize_cols<<<grid_for(n * k, 256), 256, 0, ctx->stream>>>(n, k, V64, nr + k);
+  k_normalize_cols<<<grid_cols(n, k), 256, 0, ctx->stream>>>(n, k, V64, nr + k);
   OFRR_LAUNCHED(ctx, "k_normalize_cols");
   OFRR_TRY(op.apply(ctx, 0, OFRR_F64, OFRR_F64, V64, n, k, OFRR_F64, OFRR_F64, AV, m));
   OFRR_TRY(op.apply(ctx, 1, OFRR_F64, OFRR_F64, U64, m, k, OFRR_F64, OFRR_F64, ATU, n));

@@ -4,24 +4,28 @@
 #include "ofrr_internal.cuh"
 
 #include <algorithm>
+#include <type_traits>
 
 namespace ofrr {
 
 template <class TI, class TO>
 __global__ void k_cast_transpose(int64_t m, int64_t n, const TI* __restrict__ in, int64_t ldin, TO* __restrict__ out,
                                  int64_t ldout) {
-  __shared__ double tile[32][33];
+  // staged in FP32 unless a side is FP64 (every 16/32-bit value is a float; one rounding either way)
+  using TT = typename std::conditional<std::is_same<TI, double>::value || std::is_same<TO, double>::value, double,
+                                       float>::type;
+  __shared__ TT tile[32][33];
   for (int64_t bj = blockIdx.y; bj * 32 < n; bj += gridDim.y) {
     for (int64_t bi = blockIdx.x; bi * 32 < m; bi += gridDim.x) {
       const int64_t i0 = bi * 32, j0 = bj * 32;
       for (int r = threadIdx.y; r < 32; r += blockDim.y) {
         const int64_t i = i0 + threadIdx.x, j = j0 + r;
-        tile[r][threadIdx.x] = (i < m && j < n) ? to_c<double, TI>(in[i + j * ldin]) : 0.0;
+        tile[r][threadIdx.x] = (i < m && j < n) ? to_c<TT, TI>(in[i + j * ldin]) : TT(0);
       }
       __syncthreads();
       for (int r = threadIdx.y; r < 32; r += blockDim.y) {
         const int64_t j = j0 + threadIdx.x, i = i0 + r;  // out(j, i) = in(i, j)
-        if (i < m && j < n) out[j + i * ldout] = from_c<TO, double>(tile[threadIdx.x][r]);
+        if (i < m && j < n) out[j + i * ldout] = from_c<TO, TT>(tile[threadIdx.x][r]);
       }
       __syncthreads();
     }
