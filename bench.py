@@ -45,6 +45,8 @@ def parse():
                     help="run one warm-up and one mixed solve only (for a profiler's launch list)")
     ap.add_argument("--roofline-only", action="store_true",
                     help="run only the live timing of the roofline kernel (for an ncu capture of it)")
+    ap.add_argument("--mixed-config", default=None, metavar="B,S",
+                    help="block width and power steps of the mixed path instead of the autotuner's choice")
     return ap.parse_args()
 
 
@@ -357,10 +359,17 @@ def main():
     # block width and power steps per path from the solver autotuner (untimed; b >= 40)
     tune = {}
     for mode in ("mixed",) + (() if args.no_fp64 else ("fp64",)):
+        if mode == "mixed" and args.mixed_config:
+            b, st = (int(x) for x in args.mixed_config.split(","))
+            CFG[mode] = (b, st)
+            tune[mode] = {"block": b, "step_size": st, "fixed": True}
+            continue
         t = api.autotune_svd(A, M_ROWS, N_COLS, NEV, TOL, mode=mode, blocks=(64, 96, 128), steps=(4, 6, 8),
-                             reps=1 if mode == "fp64" else 2, maxiter=MAXITER)
+                             reps=1 if mode == "fp64" else 3, maxiter=MAXITER)
         CFG[mode] = (t["block"], t["step_size"])
         tune[mode] = {"block": t["block"], "step_size": t["step_size"], "candidates": len(t["table"])}
+        for row in t["table"]:
+            print(f"autotune {mode}: {row}", file=sys.stderr)
     # mixed path (the product) -----------------------------------------------------------------
     if world > 1:
         torch.distributed.barrier()

@@ -341,6 +341,13 @@ int ofrr_batch_si_eig(ofrr_serve* engine, int count, const ofrr_operator* ops, c
 /* releases a context's cached workspace (no allocation of it may be live: call between solves) */
 int ofrr_ctx_trim(ofrr_ctx* ctx);
 
+/* Failure-detection self-test: queues one kernel that waits on an mbarrier nothing arrives on, with the
+ * same bounded wait the library's pipelines use (timeout_ns, clamped to [1 us, 1 s]); when the wait gives
+ * up the kernel records a timeout in the context's status words and returns.  The next
+ * ofrr_ctx_synchronize then returns OFRR_ERR_DEVICE_TIMEOUT and clears the words; the context stays
+ * usable.  No fault, trap or unbounded wait is involved. */
+int ofrr_debug_bounded_wait(ofrr_ctx* ctx, int64_t timeout_ns);
+
 #ifdef __cplusplus
 }
 #endif

@@ -131,6 +131,7 @@ SIGNATURES = {
     "ofrr_batch_si_eig": (C.c_int, [_P, C.c_int, C.POINTER(ofrr_operator), C.POINTER(ofrr_options), C.POINTER(_P),
                                     C.POINTER(_I64), C.POINTER(_DP), C.POINTER(_DP), C.POINTER(ofrr_info), _IP]),
     "ofrr_ctx_trim": (C.c_int, [_P]),
+    "ofrr_debug_bounded_wait": (C.c_int, [_P, _I64]),
 }
 
 _lib = None

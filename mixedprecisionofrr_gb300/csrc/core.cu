@@ -462,6 +462,31 @@ int residual_columns(ofrr_ctx* ctx, int64_t m, int64_t n, const double* AX, int6
   return OFRR_SUCCESS;
 }
 
+// One CTA waits on an mbarrier that nothing arrives on; the bounded wait gives up after timeout_ns,
+// records the timeout in the status word of the tcgen05 pipelines and returns.
+__global__ void k_bounded_wait_probe(unsigned long long timeout_ns, int* err) {
+  __shared__ __align__(8) unsigned long long bar;
+  const unsigned baddr = (unsigned)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(baddr) : "memory");
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  unsigned long long t0, t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  while (true) {
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok)
+                 : "r"(baddr)
+                 : "memory");
+    if (ok) return;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 > timeout_ns) {
+      atomicCAS(err, 0, 99);
+      return;
+    }
+  }
+}
+
 }  // namespace ofrr
 
 using namespace ofrr;
@@ -579,6 +604,14 @@ int ofrr_ctx_set_stream(ofrr_ctx* ctx, void* stream) {
 }
 
 void* ofrr_ctx_get_stream(ofrr_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int ofrr_debug_bounded_wait(ofrr_ctx* ctx, int64_t timeout_ns) {
+  if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
+  const long long t = timeout_ns < 1000 ? 1000 : (timeout_ns > 1000000000LL ? 1000000000LL : timeout_ns);
+  ofrr::k_bounded_wait_probe<<<1, 32, 0, ctx->stream>>>((unsigned long long)t, ctx->dev_flags + kFlagTcWait);
+  OFRR_LAUNCHED(ctx, "k_bounded_wait_probe");
+  return OFRR_SUCCESS;
+}
 
 int ofrr_ctx_synchronize(ofrr_ctx* ctx) {
   if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;

@@ -298,66 +298,106 @@ __global__ void __launch_bounds__(512) k_jacobi_f32(int n, const double* __restr
 
 // ---- 3b. FP32 one-sided (Hestenes) Jacobi on the columns of G: G V = U Sigma ------------------------
 // The SVD form's starting vectors: the right singular vectors of C directly (better conditioned than
-// an eigen-solve of C'C).  Round-robin pairs, one warp per pair: the pair's dot product reduced with
-// warp shuffles (the squared column norms are kept in shared memory, updated with each rotation and
-// recomputed every sweep), then the two columns of G and of V rotated; one barrier per round.  A pair
-// rotates when |g_p . g_q| > 3e-5 ||g_p|| ||g_q|| (above FP32 rounding noise); sweeps stop when no
-// pair rotates (at most 12).
-__global__ void __launch_bounds__(1024) k_jacobi1_f32(int n, const double* __restrict__ Gin, int ldg, int trans,
-                                                      double* __restrict__ Vout) {
+// an eigen-solve of C'C).  Round-robin pairs: the pair's dot product reduced with shuffles (the squared
+// column norms are kept in shared memory, updated with each rotation and recomputed every sweep), then
+// the two columns of G and of V rotated; one barrier per round.  A pair rotates when
+// |g_p . g_q| > 3e-5 ||g_p|| ||g_q|| (above FP32 rounding noise); sweeps stop when no pair rotates (at
+// most 12).
+// Round-robin partner of position i in round r for N positions (position 0 fixed), without a division.
+__device__ __forceinline__ int rr_pos(int i, int r, int N) {
+  if (i == 0) return 0;
+  int x = i - 1 + r;
+  if (x >= N - 1) x -= N - 1;
+  return x + 1;
+}
+
+// Eight lanes per column pair (each lane holds rows sl, sl + 8, ... of both columns in registers), four
+// pairs per warp: the kernel is bound by instruction issue, and the per-pair scalar work (the angle, the
+// threshold test, the norm update) is then shared by four pairs in one warp instruction stream.  The
+// angle need not be exact, only the rotation orthogonal: c = 1/sqrt(1 + t^2) is refined by one Newton
+// step so that c^2 + s^2 = 1 to rounding (the accumulated V stays orthogonal to FP32 accuracy).
+template <int R>  // rows per lane: n <= 8 R
+__global__ void __launch_bounds__(256, 1) k_jacobi1_f32(int n, const double* __restrict__ Gin, int ldg, int trans,
+                                                     double* __restrict__ Vout) {
   extern __shared__ float sm1[];
   const int ld = n + 1;
   float* G = sm1;
   float* V = sm1 + n * ld;
   __shared__ int s_any;
-  __shared__ float nrm[128];  // squared column norms, updated with each rotation, recomputed per sweep
+  __shared__ float nrm[8 * R];  // squared column norms, updated with each rotation, recomputed per sweep
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int e = tid; e < n * n; e += nt) {
-    const int i = e % n, j = e / n;
-    G[i + j * ld] = (float)(trans ? Gin[j + (size_t)i * ldg] : Gin[i + (size_t)j * ldg]);
-    V[i + j * ld] = (i == j) ? 1.f : 0.f;
-  }
+  for (int j = tid >> 5; j < n; j += nt >> 5)
+    for (int i = tid & 31; i < n; i += 32) {
+      G[i + j * ld] = (float)(trans ? Gin[j + (size_t)i * ldg] : Gin[i + (size_t)j * ldg]);
+      V[i + j * ld] = (i == j) ? 1.f : 0.f;
+    }
   const int N = n + (n & 1), npair = N / 2;
-  const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  const int grp = tid >> 3, sl = tid & 7, ngrp = nt >> 3;
   for (int sweep = 0; sweep < 12 && n > 1; ++sweep) {
     if (tid == 0) s_any = 0;
     __syncthreads();
-    for (int j = warp; j < n; j += nw) {
+    for (int jb = 0; jb < n; jb += ngrp) {  // uniform trip count: the shuffles need whole warps
+      const int j = jb + grp;
       float s2 = 0.f;
-      for (int i = lane; i < n; i += 32) s2 = fmaf(G[i + j * ld], G[i + j * ld], s2);
-      for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-      if (lane == 0) nrm[j] = s2;
+#pragma unroll
+      for (int u = 0; u < R; ++u) {
+        const int i = sl + 8 * u;
+        const float x = (j < n && i < n) ? G[i + j * ld] : 0.f;
+        s2 = fmaf(x, x, s2);
+      }
+      s2 += __shfl_xor_sync(0xffffffffu, s2, 4);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, 2);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, 1);
+      if (sl == 0 && j < n) nrm[j] = s2;
     }
     __syncthreads();
     int any = 0;
     for (int r = 0; r < N - 1; ++r) {
-      for (int k = warp; k < npair; k += nw) {
-        int p = rr_idx(k, r, N), q = rr_idx(N - 1 - k, r, N);
+      for (int kb = 0; kb < npair; kb += ngrp) {
+        const int k = kb + grp;
+        int p = rr_pos(k, r, N), q = rr_pos(N - 1 - k, r, N);
         if (p > q) {
           const int t = p;
           p = q;
           q = t;
         }
-        if (q >= n) continue;
+        const bool live = k < npair && q < n;
+        float gp[R], gq[R];
         float g = 0.f;
-        for (int i = lane; i < n; i += 32) g = fmaf(G[i + p * ld], G[i + q * ld], g);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
+        for (int u = 0; u < R; ++u) {
+          const int i = sl + 8 * u;
+          const bool in = live && i < n;
+          gp[u] = in ? G[i + p * ld] : 0.f;
+          gq[u] = in ? G[i + q * ld] : 0.f;
+          g = fmaf(gp[u], gq[u], g);
+        }
+        g += __shfl_xor_sync(0xffffffffu, g, 4);
+        g += __shfl_xor_sync(0xffffffffu, g, 2);
+        g += __shfl_xor_sync(0xffffffffu, g, 1);
+        if (!live || g == 0.f) continue;
         const float a = nrm[p], b = nrm[q];
-        if (g != 0.f && fabsf(g) > 3e-5f * sqrtf(a * b)) {
+        if (fabsf(g) * rsqrtf(a) * rsqrtf(b) > 3e-5f) {
           any = 1;
-          const float zeta = (b - a) / (2.f * g);
-          const float t = (zeta >= 0.f) ? 1.f / (zeta + sqrtf(1.f + zeta * zeta)) : -1.f / (-zeta + sqrtf(1.f + zeta * zeta));
-          const float c = rsqrtf(1.f + t * t), sn = t * c;
-          for (int i = lane; i < n; i += 32) {
-            const float gp = G[i + p * ld], gq = G[i + q * ld];
-            G[i + p * ld] = c * gp - sn * gq;
-            G[i + q * ld] = sn * gp + c * gq;
-            const float vp = V[i + p * ld], vq = V[i + q * ld];
-            V[i + p * ld] = c * vp - sn * vq;
-            V[i + q * ld] = sn * vp + c * vq;
+          const float zeta = __fdividef(b - a, 2.f * g);
+          const float z1 = fmaf(zeta, zeta, 1.f);
+          const float t = __fdividef(copysignf(1.f, zeta), fabsf(zeta) + z1 * rsqrtf(z1));
+          const float x = fmaf(t, t, 1.f);
+          float c = rsqrtf(x);
+          c = c * fmaf(-0.5f * x * c, c, 1.5f);  // Newton step for 1/sqrt(x)
+          const float sn = t * c;
+#pragma unroll
+          for (int u = 0; u < R; ++u) {
+            const int i = sl + 8 * u;
+            if (i < n) {
+              G[i + p * ld] = c * gp[u] - sn * gq[u];
+              G[i + q * ld] = sn * gp[u] + c * gq[u];
+              const float vp = V[i + p * ld], vq = V[i + q * ld];
+              V[i + p * ld] = c * vp - sn * vq;
+              V[i + q * ld] = sn * vp + c * vq;
+            }
           }
-          if (lane == 0) {  // norms after the rotation (exact arithmetic; drift is reset each sweep)
+          if (sl == 0) {  // norms after the rotation (exact arithmetic; drift is reset each sweep)
             const float cc = c * c, ss = sn * sn, cs2 = 2.f * c * sn * g;
             nrm[p] = cc * a + ss * b - cs2;
             nrm[q] = ss * a + cc * b + cs2;
@@ -371,7 +411,8 @@ __global__ void __launch_bounds__(1024) k_jacobi1_f32(int n, const double* __res
     if (!s_any) break;
   }
   __syncthreads();
-  for (int e = tid; e < n * n; e += nt) Vout[e] = (double)V[(e % n) + (e / n) * ld];
+  for (int j = tid >> 5; j < n; j += nt >> 5)
+    for (int i = tid & 31; i < n; i += 32) Vout[i + (size_t)j * n] = (double)V[i + j * ld];
 }
 
 // ---- 4. Ogita-Aishima correction: from P = W'W and T = W'CW build lambda and F = I + E ------------
@@ -629,8 +670,13 @@ int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const dou
     double* X0 = ws_get<double>(ctx, (size_t)b * b, &st);
     if (!X0) return st;
     const size_t smem = (size_t)2 * b * (b + 1) * sizeof(float);
-    OFRR_TRY(allow_smem(k_jacobi1_f32));
-    k_jacobi1_f32<<<1, 1024, smem, ctx->stream>>>(b, C, b, 1, X0);
+    if (b <= 64) {
+      OFRR_TRY(allow_smem(k_jacobi1_f32<8>));
+      k_jacobi1_f32<8><<<1, 256, smem, ctx->stream>>>(b, C, b, 1, X0);
+    } else {
+      OFRR_TRY(allow_smem(k_jacobi1_f32<16>));
+      k_jacobi1_f32<16><<<1, 256, smem, ctx->stream>>>(b, C, b, 1, X0);
+    }
     OFRR_LAUNCHED(ctx, "k_jacobi1_f32");
     OFRR_TRY(eig_refine(ctx, b, S, X0, X, lam, refine));  // right singular vectors X, sigma^2 (FP64)
   }
