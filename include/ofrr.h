@@ -348,6 +348,13 @@ int ofrr_ctx_trim(ofrr_ctx* ctx);
  * usable.  No fault, trap or unbounded wait is involved. */
 int ofrr_debug_bounded_wait(ofrr_ctx* ctx, int64_t timeout_ns);
 
+/* Per-solve tracing: with a path set, every si_eig / si_svd / arnoldi_eig solve on this context appends
+ * one JSON line to that file (solver, sizes, status, iterations, residual, kernel launches, total and
+ * per-phase device time from CUDA events on the context's stream).  NULL or "" turns it off.  A context
+ * created while the environment variable OFRR_TRACE_FILE is set starts with that path.  NVTX ranges
+ * name the same phases for external profilers whether or not a path is set. */
+int ofrr_ctx_set_trace(ofrr_ctx* ctx, const char* path);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,6 +69,10 @@ class Context:
     def synchronize(self):
         L.check(self.lib.ofrr_ctx_synchronize(self.h), "synchronize")
 
+    def set_trace(self, path=None):
+        """Append one JSON line per solve on this context to `path` (None: tracing off)."""
+        L.check(self.lib.ofrr_ctx_set_trace(self.h, str(path).encode() if path else None), "ofrr_ctx_set_trace")
+
     @property
     def launch_count(self) -> int:
         return int(self.lib.ofrr_ctx_launch_count(self.h))

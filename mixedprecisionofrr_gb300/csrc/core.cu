@@ -7,6 +7,7 @@
 #include "ofrr_internal.cuh"
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -15,6 +16,7 @@ namespace ofrr {
 int aux_begin(ofrr_ctx* ctx, ofrr_ctx** aux) {
   if (!ctx->aux) {
     OFRR_TRY(ofrr_ctx_create(&ctx->aux, ctx->device, nullptr));
+    trace_destroy(ctx->aux);  // phases are traced on the main context only
     OFRR_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
     OFRR_CUDA(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
   }
@@ -565,6 +567,10 @@ int ofrr_ctx_create(ofrr_ctx** out, int device, void* stream) {
   }
   if (e == cudaSuccess) e = cudaMallocHost(&ctx->host_flags, 8 * sizeof(int));
   if (e == cudaSuccess) memset(ctx->host_flags, 0, 8 * sizeof(int));
+  if (e == cudaSuccess) {
+    const char* tp = getenv("OFRR_TRACE_FILE");
+    if (tp && *tp) ofrr_ctx_set_trace(ctx, tp);
+  }
   if (e != cudaSuccess) {
     ofrr_ctx_destroy(ctx);
     return map_cuda_error(e);
@@ -577,6 +583,7 @@ int ofrr_ctx_destroy(ofrr_ctx* ctx) {
   if (!ctx) return OFRR_SUCCESS;
   cudaSetDevice(ctx->device);
   if (ctx->aux) ofrr_ctx_destroy(ctx->aux);
+  trace_destroy(ctx);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);

@@ -57,6 +57,8 @@ struct WsMark {
   size_t offset;
 };
 
+struct Tracer;
+
 }  // namespace ofrr
 
 struct ofrr_ctx {
@@ -76,6 +78,7 @@ struct ofrr_ctx {
   bool emulate_f64 = false;        // FP64 TN products through exact BF16 slices on the tensor cores
   size_t pinned_size = 0;
   ofrr_ctx* aux = nullptr;         // second stream + workspace for independent work run beside this one
+  ofrr::Tracer* tracer = nullptr;  // per-solve phase events and the JSON-lines sink (trace.cu), or null
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
@@ -119,6 +122,22 @@ int sync_and_check(ofrr_ctx* ctx);
 // behind everything queued on ctx's stream; work queued on it runs beside ctx's own; aux_end()
 // orders ctx's stream behind it again.
 int aux_begin(ofrr_ctx* ctx, ofrr_ctx** aux);
+
+// Phase tracing (trace.cu): a TraceScope opens an NVTX range and, with a sink set on the context,
+// brackets the phase with CUDA events on ctx's stream; trace_end_solve appends the solve's record.
+struct TraceScope {
+  ofrr_ctx* ctx;
+  int idx = -1;
+  TraceScope(ofrr_ctx* c, const char* name);
+  ~TraceScope();
+  void next(const char* name);  // ends this phase and opens the next one
+  TraceScope(const TraceScope&) = delete;
+  TraceScope& operator=(const TraceScope&) = delete;
+};
+void trace_begin_solve(ofrr_ctx* ctx);
+void trace_end_solve(ofrr_ctx* ctx, const char* solver, int64_t m, int64_t n, const ofrr_options* opt, int status,
+                     const ofrr_info* info, unsigned long long launches);
+void trace_destroy(ofrr_ctx* ctx);
 int aux_end(ofrr_ctx* ctx);
 
 // kernel attributes ---------------------------------------------------------------------

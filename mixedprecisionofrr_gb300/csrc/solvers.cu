@@ -687,6 +687,64 @@ int svd_residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* U, int64
   return OFRR_SUCCESS;
 }
 
+// The certification's fallback for the columns J only: those columns are gathered into contiguous
+// buffers and their residuals recomputed with true FP64 products (normA is the full set's, so the
+// values are the ones the full recomputation gives).  Usually one or two columns miss the
+// certified bound by a hair; the others keep their certified values.
+double norm_of_values(const double* v, int k) {
+  double a = 0;
+  for (int j = 0; j < k; ++j) a = std::max(a, std::fabs(v[j]));
+  return a > 0 ? a : 1.0;
+}
+
+int svd_residuals_subset(ofrr_ctx* ctx, Op& op, const double* U, int64_t ldu, const double* V, int64_t ldv,
+                         const std::vector<int>& J, const double* s_host, double normA, double* out_host) {
+  if (J.empty()) return OFRR_SUCCESS;
+  WsScope scope(ctx);
+  const int64_t m = op.m(), n = op.n();
+  const int q = (int)J.size();
+  double *Ug, *Vg;
+  OFRR_TRY(dmalloc(ctx, &Ug, (size_t)m * q));
+  OFRR_TRY(dmalloc(ctx, &Vg, (size_t)n * q));
+  std::vector<double> sq(q), rq(q);
+  for (int t = 0; t < q; ++t) {
+    OFRR_CUDA(cudaMemcpyAsync(Ug + (size_t)t * m, U + (size_t)J[t] * ldu, sizeof(double) * m,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+    OFRR_CUDA(cudaMemcpyAsync(Vg + (size_t)t * n, V + (size_t)J[t] * ldv, sizeof(double) * n,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+    sq[t] = s_host[J[t]];
+  }
+  OFRR_TRY(svd_residuals_dev(ctx, op, OFRR_F64, Ug, m, Vg, n, q, sq.data(), normA, rq.data()));
+  for (int t = 0; t < q; ++t) out_host[J[t]] = rq[t];
+  return OFRR_SUCCESS;
+}
+
+int residuals_subset(ofrr_ctx* ctx, Op& op, const double* X, int64_t ldx, const std::vector<int>& J,
+                     const double* lam_host, double normA, double* out_host) {
+  if (J.empty()) return OFRR_SUCCESS;
+  WsScope scope(ctx);
+  const int64_t n = op.m();
+  const int q = (int)J.size();
+  double* Xg;
+  OFRR_TRY(dmalloc(ctx, &Xg, (size_t)n * q));
+  std::vector<double> lq(q), rq(q);
+  for (int t = 0; t < q; ++t) {
+    OFRR_CUDA(cudaMemcpyAsync(Xg + (size_t)t * n, X + (size_t)J[t] * ldx, sizeof(double) * n,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+    lq[t] = lam_host[J[t]];
+  }
+  OFRR_TRY(residuals_dev(ctx, op, OFRR_F64, Xg, n, q, lq.data(), normA, rq.data()));
+  for (int t = 0; t < q; ++t) out_host[J[t]] = rq[t];
+  return OFRR_SUCCESS;
+}
+
+std::vector<int> failing(const std::vector<double>& res, int k, double tol) {
+  std::vector<int> J;
+  for (int j = 0; j < k; ++j)
+    if (!(res[j] <= tol)) J.push_back(j);
+  return J;
+}
+
 }  // namespace
 }  // namespace ofrr
 
@@ -721,8 +779,8 @@ extern "C" int ofrr_rr_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
 // ======================================================================================
 // Krylov eigensolver: Hessenberg process with restarts (arnoldi_hess_eig.m:51-107)
 // ======================================================================================
-extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, const void* v0,
-                                void* X, int64_t ldx, double* evals, double* resid, ofrr_info* info) {
+static int arnoldi_eig_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, const void* v0,
+                            void* X, int64_t ldx, double* evals, double* resid, ofrr_info* info) {
   if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
   OFRR_TRY(validate_op(A));
   OFRR_TRY(validate_options(opt));
@@ -772,6 +830,7 @@ extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofr
   int ncols_final = 0;
   bool have_result = false;
   while (tits < opt->maxiter) {
+    TraceScope ts(ctx, "krylov");
     // column 0: pivot + scale (Hessenberg, arnoldi_hess_eig.m:64-71) or normalise (MGS,
     // arnoldi_mgs_eig.m:60-65); break if the pivot / norm is below select_tol
     if (mgs) {
@@ -807,6 +866,7 @@ extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofr
     }
     nmv += steps;
     cycles++;
+    ts.next("rr");
     // RR on the ncols columns: generalized for the oblique Hessenberg basis (arnoldi_hess_eig.m:93),
     // as the options say for the orthonormal MGS basis (arnoldi_mgs_eig.m:95-100)
     OFRR_TRY(rr_eig_dev(ctx, op, po, V, po, n, ncols, pc, po, pc, pc, mgs ? opt->use_generalized != 0 : true,
@@ -814,6 +874,7 @@ extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofr
     nmv += ncols;
     ncols_final = ncols;
     have_result = true;
+    ts.next("check");
     if (tits < opt->maxiter) {
       OFRR_CUDA(cudaMemcpyAsync(V, Vr, (size_t)n * dtype_size(po), cudaMemcpyDeviceToDevice, ctx->stream));
       if (opt->tol > 0) {  // convergence check on the current Ritz pairs (new behaviour)
@@ -854,6 +915,19 @@ extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofr
   }
   if (opt->tol > 0 && conv < k) return OFRR_ERR_SOLVER_MAX_ITERATIONS;
   return OFRR_SUCCESS;
+}
+
+extern "C" int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, const void* v0,
+                                void* X, int64_t ldx, double* evals, double* resid, ofrr_info* info) {
+  if (!ctx || !ctx->tracer) return arnoldi_eig_body(ctx, A, opt, v0, X, ldx, evals, resid, info);
+  ofrr_info local{};
+  ofrr_info* inf = info ? info : &local;
+  const unsigned long long l0 = ofrr_ctx_launch_count(ctx);
+  trace_begin_solve(ctx);
+  const int st = arnoldi_eig_body(ctx, A, opt, v0, X, ldx, evals, resid, inf);
+  trace_end_solve(ctx, "arnoldi_eig", A ? A->nrows : 0, A ? A->ncols : 0, opt, st, inf,
+                  ofrr_ctx_launch_count(ctx) - l0);
+  return st;
 }
 
 // ======================================================================================
@@ -909,8 +983,10 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
   void* cur = V;
   int64_t ldcur = ldv;
   const size_t es = dtype_size(P.po);
+  const bool f64 = P.po == OFRR_F64;
   for (int k = 0; k < maxit && !S.done; ++k) {
     int b = S.b;
+    TraceScope ts(ctx, f64 ? "power.f64" : "power.16bit");
     for (int s = 0; s < opt->step_size; ++s) {
       void* dst = (cur == V) ? W : V;
       int64_t lddst = (cur == V) ? n : ldv;
@@ -920,6 +996,7 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
       cur = dst;
       ldcur = lddst;
     }
+    ts.next(f64 ? "basis.f64" : "basis.16bit");
     // [Q,~] = hessenberg(V): the economic form drops deselected columns
     OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, n, b, cur, ldcur, Q, n, opt->select_tol, R, sel, perm, P.fast));
     OFRR_CUDA(cudaMemcpyAsync(hsel.data(), sel, sizeof(int) * b, cudaMemcpyDeviceToHost, ctx->stream));
@@ -928,6 +1005,7 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
     OFRR_TRY(compact_columns(ctx, P.pho, n, Q, n, std::vector<int>(hsel.begin(), hsel.begin() + b), &w));
     if (w == 0) return OFRR_ERR_SOLVER_DIVERGENCE;
     S.b = b = w;
+    ts.next(f64 ? "rr.f64" : "rr.16bit");
     // [V,D] = eig_rr(A, Q), V = po(V)
     void* dst = (cur == V) ? V : W;
     int64_t lddst = (cur == V) ? ldv : n;
@@ -945,6 +1023,7 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
     S.it++;
     cur = dst;
     ldcur = lddst;
+    ts.next(f64 ? "check.f64" : "check.16bit");
     const int kk = std::min(nev, b);
     const bool last = (k + 1 == maxit);
     const bool check = tol > 0 && ((S.it % check_every) == 0 || last);
@@ -986,39 +1065,51 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
   OFRR_TRY(dmalloc(ctx, &perm2, (size_t)b0));
   std::vector<int> hsel(2 * b0);
   const int check_every = std::max(1, opt->check_every);
+  const bool f64 = P.po == OFRR_F64;
   for (int k = 0; k < maxit && !S.done; ++k) {
     int b = S.b;
-    for (int j = 0; j < opt->step_size; ++j) {
-      OFRR_TRY(op.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.po, U, ldu));
-      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, m, b, U, ldu, nullptr, P.fast));
-      OFRR_TRY(op.apply(ctx, 1, P.po, P.po, U, ldu, b, P.pc, P.po, V, ldv));
-      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr, P.fast));
-      S.nmv += 2 * b;
+    {
+      TraceScope ts(ctx, f64 ? "power.f64" : "power.16bit");
+      for (int j = 0; j < opt->step_size; ++j) {
+        OFRR_TRY(op.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.po, U, ldu));
+        OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, m, b, U, ldu, nullptr, P.fast));
+        OFRR_TRY(op.apply(ctx, 1, P.po, P.po, U, ldu, b, P.pc, P.po, V, ldv));
+        OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr, P.fast));
+        S.nmv += 2 * b;
+      }
     }
-    // the two bases are independent: V's is built on the auxiliary stream beside U's
-    ofrr_ctx* aux = nullptr;
-    OFRR_TRY(aux_begin(ctx, &aux));
-    OFRR_TRY(hessenberg_impl(aux, P.po, P.pho, P.phc, n, b, V, ldv, Q1, n, opt->select_tol, R2, sel + b0, perm2,
-                             P.fast));
-    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, m, b, U, ldu, P1, m, opt->select_tol, R, sel, perm, P.fast));
-    OFRR_TRY(aux_end(ctx));
-    OFRR_CUDA(cudaMemcpyAsync(hsel.data(), sel, sizeof(int) * 2 * b0, cudaMemcpyDeviceToHost, ctx->stream));
-    OFRR_TRY(sync_and_check(ctx));
-    int wu = b, wv = b;
-    OFRR_TRY(compact_columns(ctx, P.pho, m, P1, m, std::vector<int>(hsel.begin(), hsel.begin() + b), &wu));
-    OFRR_TRY(compact_columns(ctx, P.pho, n, Q1, n, std::vector<int>(hsel.begin() + b0, hsel.begin() + b0 + b), &wv));
-    const int w = std::min(wu, wv);  // svd_rr.m:61 keeps k = min(ku, kv)
-    if (w == 0) return OFRR_ERR_SOLVER_DIVERGENCE;
-    S.b = b = w;
-    OFRR_TRY(rr_svd_dev(ctx, op, P.po, P1, Q1, P.pho, m, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
-                        opt->generalized_tol, Ut, m, Vt, n, d_dev, P.fast, P.refine));
-    OFRR_TRY(cast_impl(ctx, P.pho, P.po, m, b, Ut, m, U, ldu));
-    OFRR_TRY(cast_impl(ctx, P.pho, P.po, n, b, Vt, n, V, ldv));
+    {
+      // the two bases are independent: V's is built on the auxiliary stream beside U's
+      TraceScope ts(ctx, f64 ? "basis.f64" : "basis.16bit");
+      ofrr_ctx* aux = nullptr;
+      OFRR_TRY(aux_begin(ctx, &aux));
+      OFRR_TRY(hessenberg_impl(aux, P.po, P.pho, P.phc, n, b, V, ldv, Q1, n, opt->select_tol, R2, sel + b0, perm2,
+                               P.fast));
+      OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, m, b, U, ldu, P1, m, opt->select_tol, R, sel, perm, P.fast));
+      OFRR_TRY(aux_end(ctx));
+      OFRR_CUDA(cudaMemcpyAsync(hsel.data(), sel, sizeof(int) * 2 * b0, cudaMemcpyDeviceToHost, ctx->stream));
+      OFRR_TRY(sync_and_check(ctx));
+    }
+    {
+      TraceScope ts(ctx, f64 ? "rr.f64" : "rr.16bit");
+      int wu = b, wv = b;
+      OFRR_TRY(compact_columns(ctx, P.pho, m, P1, m, std::vector<int>(hsel.begin(), hsel.begin() + b), &wu));
+      OFRR_TRY(
+          compact_columns(ctx, P.pho, n, Q1, n, std::vector<int>(hsel.begin() + b0, hsel.begin() + b0 + b), &wv));
+      const int w = std::min(wu, wv);  // svd_rr.m:61 keeps k = min(ku, kv)
+      if (w == 0) return OFRR_ERR_SOLVER_DIVERGENCE;
+      S.b = b = w;
+      OFRR_TRY(rr_svd_dev(ctx, op, P.po, P1, Q1, P.pho, m, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
+                          opt->generalized_tol, Ut, m, Vt, n, d_dev, P.fast, P.refine));
+      OFRR_TRY(cast_impl(ctx, P.pho, P.po, m, b, Ut, m, U, ldu));
+      OFRR_TRY(cast_impl(ctx, P.pho, P.po, n, b, Vt, n, V, ldv));
+    }
     S.nmv += b;
     S.it++;
     const int kk = std::min(nev, b);
     const bool last = (k + 1 == maxit);
     const bool check = tol > 0 && ((S.it % check_every) == 0 || last);
+    TraceScope ts(ctx, f64 ? "check.f64" : "check.16bit");
     if (check || stag_tol > 0) {
       OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d_dev, sizeof(double) * b, cudaMemcpyDeviceToHost, ctx->stream));
       OFRR_TRY(sync_and_check(ctx));
@@ -1073,8 +1164,8 @@ void fill_info(ofrr_info* info, const PhaseState& S, int nev, int escalations) {
 // ======================================================================================
 // subspace iteration eigensolver (si_eig)
 // ======================================================================================
-extern "C" int ofrr_si_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, void* V, int64_t ldv,
-                           double* evals, double* resid, ofrr_info* info) {
+static int si_eig_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, void* V, int64_t ldv,
+                       double* evals, double* resid, ofrr_info* info) {
   if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
   OFRR_TRY(validate_op(A));
   OFRR_TRY(validate_options(opt));
@@ -1126,7 +1217,8 @@ extern "C" int ofrr_si_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
       OFRR_TRY(st);
       if (S.done && op.A->kind == OFRR_OP_DENSE) {
         // certify: the emulated residuals plus the bound on the emulation error must meet tol;
-        // otherwise the residuals are recomputed with true FP64 products
+        // otherwise the residuals of the columns that miss it are recomputed with true FP64 products
+        TraceScope ts(ctx, "certify");
         OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d, sizeof(double) * S.b, cudaMemcpyDeviceToHost, ctx->stream));
         OFRR_TRY(sync_and_check(ctx));
         const int kk = std::min(nev, S.b);
@@ -1137,7 +1229,8 @@ extern "C" int ofrr_si_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
         S.converged = 0;
         for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
         if (S.converged < kk) {
-          OFRR_TRY(residuals_dev(ctx, op, OFRR_F64, V, ldv, kk, S.d.data(), -1.0, S.res.data()));
+          OFRR_TRY(residuals_subset(ctx, op, (const double*)V, ldv, failing(S.res, kk, opt->tol), S.d.data(),
+                                    norm_of_values(S.d.data(), kk), S.res.data()));
           S.converged = 0;
           for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
         }
@@ -1162,11 +1255,23 @@ extern "C" int ofrr_si_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
   return OFRR_SUCCESS;
 }
 
+extern "C" int ofrr_si_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, void* V, int64_t ldv,
+                           double* evals, double* resid, ofrr_info* info) {
+  if (!ctx || !ctx->tracer) return si_eig_body(ctx, A, opt, V, ldv, evals, resid, info);
+  ofrr_info local{};
+  ofrr_info* inf = info ? info : &local;
+  const unsigned long long l0 = ofrr_ctx_launch_count(ctx);
+  trace_begin_solve(ctx);
+  const int st = si_eig_body(ctx, A, opt, V, ldv, evals, resid, inf);
+  trace_end_solve(ctx, "si_eig", A ? A->nrows : 0, A ? A->ncols : 0, opt, st, inf, ofrr_ctx_launch_count(ctx) - l0);
+  return st;
+}
+
 // ======================================================================================
 // subspace iteration SVD (si_svd)
 // ======================================================================================
-extern "C" int ofrr_si_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, void* U, int64_t ldu,
-                           double* s, void* V, int64_t ldv, double* resid, ofrr_info* info) {
+static int si_svd_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, void* U, int64_t ldu, double* s,
+                       void* V, int64_t ldv, double* resid, ofrr_info* info) {
   if (!ctx) return OFRR_ERR_INVALID_ARGUMENT;
   OFRR_TRY(validate_op(A));
   OFRR_TRY(validate_options(opt));
@@ -1211,14 +1316,18 @@ extern "C" int ofrr_si_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
     escalations = 1;
     if (!S.done && S.it < opt->maxiter) {
       // refinement: FP64-accurate products from exact BF16 slices on the tensor cores
-      OFRR_TRY(op.prepare_sliced(ctx));
+      {
+        TraceScope ts(ctx, "prepare.f64");
+        OFRR_TRY(op.prepare_sliced(ctx));
+      }
       ctx->emulate_f64 = op.A->kind == OFRR_OP_DENSE;
       st = svd_phase(ctx, op, all_f64(), opt, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d);
       ctx->emulate_f64 = false;
       OFRR_TRY(st);
       if (S.done && op.A->kind == OFRR_OP_DENSE) {
         // certify: the emulated residuals plus the bounds on the emulation errors must meet tol;
-        // otherwise the residuals are recomputed with true FP64 products
+        // otherwise the residuals of the columns that miss it are recomputed with true FP64 products
+        TraceScope ts(ctx, "certify");
         OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d, sizeof(double) * S.b, cudaMemcpyDeviceToHost, ctx->stream));
         OFRR_TRY(sync_and_check(ctx));
         const int kk = std::min(nev, S.b);
@@ -1229,7 +1338,9 @@ extern "C" int ofrr_si_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
         S.converged = 0;
         for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
         if (S.converged < kk) {
-          OFRR_TRY(svd_residuals_dev(ctx, op, OFRR_F64, U, ldu, V, ldv, kk, S.d.data(), -1.0, S.res.data()));
+          OFRR_TRY(svd_residuals_subset(ctx, op, (const double*)U, ldu, (const double*)V, ldv,
+                                        failing(S.res, kk, opt->tol), S.d.data(), norm_of_values(S.d.data(), kk),
+                                        S.res.data()));
           S.converged = 0;
           for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
         }
@@ -1252,4 +1363,16 @@ extern "C" int ofrr_si_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
   fill_info(info, S, nev, escalations);
   if (opt->tol > 0 && !S.done) return OFRR_ERR_SOLVER_MAX_ITERATIONS;
   return OFRR_SUCCESS;
+}
+
+extern "C" int ofrr_si_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, void* U, int64_t ldu,
+                           double* s, void* V, int64_t ldv, double* resid, ofrr_info* info) {
+  if (!ctx || !ctx->tracer) return si_svd_body(ctx, A, opt, U, ldu, s, V, ldv, resid, info);
+  ofrr_info local{};
+  ofrr_info* inf = info ? info : &local;
+  const unsigned long long l0 = ofrr_ctx_launch_count(ctx);
+  trace_begin_solve(ctx);
+  const int st = si_svd_body(ctx, A, opt, U, ldu, s, V, ldv, resid, inf);
+  trace_end_solve(ctx, "si_svd", A ? A->nrows : 0, A ? A->ncols : 0, opt, st, inf, ofrr_ctx_launch_count(ctx) - l0);
+  return st;
 }
