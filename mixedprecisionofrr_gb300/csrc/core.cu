@@ -182,7 +182,8 @@ __global__ void k_cast(int64_t m, int64_t n, const TI* in, int64_t ldin, TO* out
 // --------------------------------------------------------------------------------------
 // column argmax + scaling (scalecols.m:27-32)
 // Argmax on integer keys of |x| (no FP64 compares); lowest row among equal maxima.  Columns up to
-// SC_CHUNK rows: one CTA per column, values held in registers between the search and the scaling.
+// 4 SC_CHUNK rows: one CTA (256 or 1024 threads) per column, values held in registers between the
+// search and the scaling.
 // Longer columns: a grid of (chunks x columns) CTAs finds per-chunk maxima (with their values),
 // then the same grid reduces a column's chunk maxima and scales its chunk.
 // --------------------------------------------------------------------------------------
@@ -196,21 +197,21 @@ __device__ __forceinline__ TC scale_by(TC q, TC t, TC y, bool pf, bool is_pivot)
   return pivot_div(q, t, y, pf);                           // correctly rounded q / t
 }
 
-template <class TO, class TC, bool FAST>
-__global__ void __launch_bounds__(SC_T) k_scalecols_small(int64_t m, TO* U, int64_t ldu, int* piv, int do_scale) {
-  __shared__ ArgMaxK red[SC_T / 32];
+template <class TO, class TC, bool FAST, int T>
+__global__ void __launch_bounds__(T) k_scalecols_small(int64_t m, TO* U, int64_t ldu, int* piv, int do_scale) {
+  __shared__ ArgMaxK red[T / 32];
   __shared__ TO s_t;
   TO* col = U + (int64_t)blockIdx.x * ldu;
   TO v[SC_U];
   ArgMaxK a{-1, 0x7fffffffffffffffLL};
 #pragma unroll
   for (int u = 0; u < SC_U; ++u) {
-    const int64_t i = threadIdx.x + (int64_t)u * SC_T;
+    const int64_t i = threadIdx.x + (int64_t)u * T;
     v[u] = (i < m) ? col[i] : TO(0);
   }
 #pragma unroll
   for (int u = 0; u < SC_U; ++u) {
-    const int64_t i = threadIdx.x + (int64_t)u * SC_T;
+    const int64_t i = threadIdx.x + (int64_t)u * T;
     if (i < m) {
       const long long key = amax_key(v[u]);
       if (key > a.key) a = ArgMaxK{key, i};  // per-thread rows ascend: strict > keeps the lowest
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(SC_T) k_scalecols_small(int64_t m, TO* U, int6
   const bool pf = pivot_fast(t);
 #pragma unroll
   for (int u = 0; u < SC_U; ++u) {
-    const int64_t i = threadIdx.x + (int64_t)u * SC_T;
+    const int64_t i = threadIdx.x + (int64_t)u * T;
     if (i < m) col[i] = from_c<TO, TC>(scale_by<TC, FAST>(to_c<TC, TO>(v[u]), t, y, pf, i == k));
   }
 }
@@ -411,7 +412,12 @@ int cast_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, int64_t m, int64_t
 template <class TO, class TC, bool FAST>
 static int scalecols_t(ofrr_ctx* ctx, int64_t m, int64_t n, TO* U, int64_t ldu, int* piv, int do_scale = 1) {
   if (m <= SC_CHUNK) {
-    k_scalecols_small<TO, TC, FAST><<<(unsigned)n, SC_T, 0, ctx->stream>>>(m, U, ldu, piv, do_scale);
+    k_scalecols_small<TO, TC, FAST, SC_T><<<(unsigned)n, SC_T, 0, ctx->stream>>>(m, U, ldu, piv, do_scale);
+    OFRR_LAUNCHED(ctx, "k_scalecols_small");
+    return OFRR_SUCCESS;
+  }
+  if (m <= 4 * SC_CHUNK) {  // up to 8192 rows: still one CTA per column, 1024 threads
+    k_scalecols_small<TO, TC, FAST, 4 * SC_T><<<(unsigned)n, 4 * SC_T, 0, ctx->stream>>>(m, U, ldu, piv, do_scale);
     OFRR_LAUNCHED(ctx, "k_scalecols_small");
     return OFRR_SUCCESS;
   }

@@ -33,12 +33,23 @@ __global__ void __launch_bounds__(256) k_chol_f64(int n, const double* const* Ms
   double* L = Ls[blockIdx.x];
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   __shared__ double s_maxd, s_rinv;
-  for (int j = warp; j < n; j += nw)
-    for (int i = lane; i < n; i += 32) {
-      double v = (i >= j) ? M[i + (size_t)j * ldm] : 0.0;
-      if (i == j) v += tau;
-      S[i + j * n] = v;
+  // stage M + tau I (lower triangle) with 16 loads per thread in flight (the kernel is latency-bound)
+  const int nn = n * n;
+  for (int e0 = tid; e0 < nn; e0 += 16 * nt) {
+    double v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int e = e0 + u * nt;
+      const int j = e / n, i = e - j * n;
+      v[u] = (e < nn && i >= j) ? M[i + (size_t)j * ldm] : 0.0;
     }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int e = e0 + u * nt;
+      const int j = e / n, i = e - j * n;
+      if (e < nn) S[e] = v[u] + ((i == j) ? tau : 0.0);
+    }
+  }
   __syncthreads();
   if (tid < 32) {
     long long kmax = -1;
@@ -88,17 +99,19 @@ __global__ void __launch_bounds__(128) k_trsm_f64(int n, int nrhs, const double*
   double* Ls = sm_trsm;
   double* rd = sm_trsm + (size_t)n * ld;
   const int nn = n * n;
-  for (int e0 = threadIdx.x; e0 < nn; e0 += 4 * blockDim.x) {
-    double v[4];
+  for (int e0 = threadIdx.x; e0 < nn; e0 += 16 * blockDim.x) {  // 16 loads per thread in flight
+    double v[16];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 16; ++u) {
       const int e = e0 + u * blockDim.x;
-      v[u] = (e < nn) ? L[(e % n) + (size_t)(e / n) * ldl] : 0.0;
+      const int j = e / n, i = e - j * n;
+      v[u] = (e < nn) ? L[i + (size_t)j * ldl] : 0.0;
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 16; ++u) {
       const int e = e0 + u * blockDim.x;
-      if (e < nn) Ls[(e % n) + (e / n) * ld] = v[u];
+      const int j = e / n, i = e - j * n;
+      if (e < nn) Ls[i + j * ld] = v[u];
     }
   }
   __syncthreads();
@@ -152,24 +165,26 @@ __global__ void __launch_bounds__(128) k_trsm_f64(int n, int nrhs, const double*
 }
 
 // ---- small FP64 GEMM: C = alpha op(A) op(B) + beta C, one thread per output entry -----------------
-// Loads are issued eight k-steps ahead of their FMAs and two accumulators halve the dependent chain.
-__global__ void __launch_bounds__(64) k_gemm_small_f64(int M, int N, int K, double alpha, const double* __restrict__ A,
+// 32-thread CTAs (one output column segment each, so the B loads are broadcasts and the A loads
+// coalesced for op(A) = A) spread the FP64 work over many SMs; K is consumed in chunks of GS_K with all
+// of a chunk's loads issued before its FMAs, so a 64-deep product waits for two rounds of L2 latency.
+constexpr int GS_K = 32;
+__global__ void __launch_bounds__(32) k_gemm_small_f64(int M, int N, int K, double alpha, const double* __restrict__ A,
                                                        int lda, int tA, const double* __restrict__ B, int ldb, int tB,
                                                        double beta, double* __restrict__ C, int ldc) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= M * N) return;
-  const int i = e % M, j = e / M;
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y;
+  if (i >= M || j >= N) return;
   double s0 = 0.0, s1 = 0.0;
-  for (int k0 = 0; k0 < K; k0 += 8) {
-    double a[8], b[8];
+  for (int k0 = 0; k0 < K; k0 += GS_K) {
+    double a[GS_K], b[GS_K];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < GS_K; ++u) {
       const int k = k0 + u;
       a[u] = (k < K) ? (tA ? A[k + (size_t)i * lda] : A[i + (size_t)k * lda]) : 0.0;
       b[u] = (k < K) ? (tB ? B[j + (size_t)k * ldb] : B[k + (size_t)j * ldb]) : 0.0;
     }
 #pragma unroll
-    for (int u = 0; u < 8; u += 2) {
+    for (int u = 0; u < GS_K; u += 2) {
       s0 = fma(a[u], b[u], s0);
       s1 = fma(a[u + 1], b[u + 1], s1);
     }
@@ -326,11 +341,24 @@ __global__ void __launch_bounds__(256, 1) k_jacobi1_f32(int n, const double* __r
   __shared__ int s_any;
   __shared__ float nrm[8 * R];  // squared column norms, updated with each rotation, recomputed per sweep
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int j = tid >> 5; j < n; j += nt >> 5)
-    for (int i = tid & 31; i < n; i += 32) {
-      G[i + j * ld] = (float)(trans ? Gin[j + (size_t)i * ldg] : Gin[i + (size_t)j * ldg]);
-      V[i + j * ld] = (i == j) ? 1.f : 0.f;
+  for (int e0 = tid; e0 < n * n; e0 += 16 * nt) {  // 16 loads per thread in flight
+    double v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int e = e0 + u * nt;
+      const int j = e / n, i = e - j * n;
+      v[u] = (e < n * n) ? (trans ? Gin[j + (size_t)i * ldg] : Gin[i + (size_t)j * ldg]) : 0.0;
     }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int e = e0 + u * nt;
+      const int j = e / n, i = e - j * n;
+      if (e < n * n) {
+        G[i + j * ld] = (float)v[u];
+        V[i + j * ld] = (i == j) ? 1.f : 0.f;
+      }
+    }
+  }
   const int N = n + (n & 1), npair = N / 2;
   const int grp = tid >> 3, sl = tid & 7, ngrp = nt >> 3;
   for (int sweep = 0; sweep < 12 && n > 1; ++sweep) {
@@ -475,9 +503,19 @@ __global__ void __launch_bounds__(256) k_sort_desc(int n, const double* __restri
     lam_out[rank] = lam[i];
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-    const int i = e / n, r = e % n;
-    Wout[r + (size_t)s_rank[i] * n] = W[r + (size_t)i * n];
+  for (int e0 = threadIdx.x; e0 < n * n; e0 += 16 * blockDim.x) {  // 16 loads per thread in flight
+    double v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int e = e0 + u * blockDim.x;
+      v[u] = (e < n * n) ? W[e] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int e = e0 + u * blockDim.x;
+      const int i = e / n, r = e - i * n;
+      if (e < n * n) Wout[r + (size_t)s_rank[i] * n] = v[u];
+    }
   }
 }
 
@@ -496,7 +534,9 @@ __global__ void k_svd_left(int n, const double* __restrict__ CW, const double* _
 // ---- host helpers ----------------------------------------------------------------------------------
 static int gemm_small(ofrr_ctx* ctx, int M, int N, int K, double alpha, const double* A, int lda, int tA,
                       const double* B, int ldb, int tB, double beta, double* C, int ldc) {
-  k_gemm_small_f64<<<(M * N + 63) / 64, 64, 0, ctx->stream>>>(M, N, K, alpha, A, lda, tA, B, ldb, tB, beta, C, ldc);
+  if (M <= 0 || N <= 0) return OFRR_SUCCESS;
+  k_gemm_small_f64<<<dim3((unsigned)((M + 31) / 32), (unsigned)N), 32, 0, ctx->stream>>>(M, N, K, alpha, A, lda, tA, B,
+                                                                                       ldb, tB, beta, C, ldc);
   OFRR_LAUNCHED(ctx, "k_gemm_small_f64");
   return OFRR_SUCCESS;
 }

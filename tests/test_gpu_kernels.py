@@ -72,9 +72,10 @@ def test_scalecols_bit_exact(api, orc, pc, po):
     assert np.array_equal(api.to_numpy(out), ref)
 
 
-@pytest.mark.parametrize("m", [2048, 2049, 6000])
+@pytest.mark.parametrize("m", [2048, 2049, 6000, 8192, 9000])
 def test_scalecols_chunked_ties(api, orc, m):
-    """Columns longer than one CTA's chunk: equal maxima in different chunks pick the lowest row."""
+    """Columns over 2048 rows (one 1024-thread CTA up to 8192 rows, chunked beyond): equal maxima in
+    different chunks pick the lowest row."""
     rng = np.random.default_rng(m)
     U = rng.uniform(-1, 1, (m, 5))
     U[[2047, m - 1], 0] = [-3.0, 3.0]   # tie across the chunk boundary: row 2047 wins
