@@ -191,11 +191,6 @@ constexpr int SC_T = 256;
 constexpr int SC_U = 8;
 constexpr int64_t SC_CHUNK = (int64_t)SC_T * SC_U;
 
-template <class TC, bool FAST>
-__device__ __forceinline__ TC scale_by(TC q, TC t, TC y, bool pf, bool is_pivot) {
-  if (FAST && pf) return is_pivot ? TC(1) : mul_rn(q, y);  // within an ulp of q / t
-  return pivot_div(q, t, y, pf);                           // correctly rounded q / t
-}
 
 template <class TO, class TC, bool FAST, int T>
 __global__ void __launch_bounds__(T) k_scalecols_small(int64_t m, TO* U, int64_t ldu, int* piv, int do_scale) {

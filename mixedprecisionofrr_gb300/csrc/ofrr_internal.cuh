@@ -231,6 +231,14 @@ __device__ __forceinline__ double pivot_div(double x, double p, double y, bool f
 }
 __device__ __forceinline__ float pivot_div(float x, float p, float, bool) { return __fdiv_rn(x, p); }
 
+// q / t for scalecols: FAST (FP64 production phase) multiplies by the reciprocal (within an ulp of
+// q / t, the pivot itself exactly 1), otherwise the correctly rounded quotient
+template <class TC, bool FAST>
+__device__ __forceinline__ TC scale_by(TC q, TC t, TC y, bool pf, bool is_pivot) {
+  if (FAST && pf) return is_pivot ? TC(1) : mul_rn(q, y);
+  return pivot_div(q, t, y, pf);
+}
+
 
 // argmax reduction on (|value|, index): larger value wins, lower index on ties, NaN ignored
 struct ArgMax {
@@ -448,6 +456,12 @@ constexpr int kSliceDigits = 5;
 int sliced_prepare(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, int64_t ldx, SlicedOperand* out);
 int sliced_prepare_into(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, int64_t ldx, __nv_bfloat16* stack,
                         int* expo, SlicedOperand* out);
+// scalecols (FAST, FP64) fused with the digit split of the scaled columns: U (m x n) is scaled in place
+// and *out describes its digit stack in caller buffers (n * 5 * roundup(m, 64) bf16, n ints); m <= 8192
+int scalecols_sliced(ofrr_ctx* ctx, int64_t m, int64_t n, double* U, int64_t ldu, __nv_bfloat16* stack, int* expo,
+                     SlicedOperand* out);
+// C (M x N) = A_op' B with both operands already split (B.K == A.K, N = B.M)
+int sliced_gemm_tn_pre(ofrr_ctx* ctx, const SlicedOperand& A, const SlicedOperand& B, double* C, int64_t ldc);
 int sliced_gemm_tn(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const double* B, int64_t ldb, double* C,
                    int64_t ldc);
 

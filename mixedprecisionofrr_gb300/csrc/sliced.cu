@@ -179,6 +179,70 @@ __global__ void __launch_bounds__(SC_T) k_slice_cols(int64_t K, int64_t Kp, int6
   }
 }
 
+// scalecols (FP64, FAST: reciprocal multiply, pivot exactly 1) fused with the digit split of the
+// scaled column, for columns of at most 8 T rows: one CTA per column keeps the column in registers,
+// finds the pivot (integer argmax keys, lowest row on ties), scales, writes the FP64 column, takes
+// the scaled column's maximum on the bit patterns and writes its digits -- the operand of the next
+// exact-slice product, without reading the column again.
+constexpr int SCS_U = 8;
+template <int T>
+__global__ void __launch_bounds__(T) k_scalecols_slice(int64_t m, int64_t Kp, double* __restrict__ U, int64_t ldu,
+                                                       __nv_bfloat16* __restrict__ stack, int* __restrict__ expo) {
+  __shared__ ArgMaxK red[T / 32];
+  __shared__ unsigned long long redm[T / 32];
+  __shared__ double s_t;
+  const int n = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double* col = U + (int64_t)n * ldu;
+  double v[SCS_U];
+  ArgMaxK a{-1, 0x7fffffffffffffffLL};
+#pragma unroll
+  for (int u = 0; u < SCS_U; ++u) {
+    const int64_t i = threadIdx.x + (int64_t)u * T;
+    v[u] = (i < m) ? col[i] : 0.0;
+  }
+#pragma unroll
+  for (int u = 0; u < SCS_U; ++u) {
+    const int64_t i = threadIdx.x + (int64_t)u * T;
+    if (i < m) {
+      const long long key = amax_key(v[u]);
+      if (key > a.key) a = ArgMaxK{key, i};  // per-thread rows ascend: strict > keeps the lowest
+    }
+  }
+  const ArgMaxK r = block_argmaxk(a, red);
+  const int64_t k = (r.key < 0) ? 0 : r.i;
+  if (threadIdx.x == 0) s_t = (m > 0) ? col[k] : 0.0;
+  __syncthreads();
+  const double t = s_t;
+  if (t != 0.0) {
+    const double y = pivot_recip(t);
+    const bool pf = pivot_fast(t);
+#pragma unroll
+    for (int u = 0; u < SCS_U; ++u) {
+      const int64_t i = threadIdx.x + (int64_t)u * T;
+      if (i < m) {
+        v[u] = scale_by<double, true>(v[u], t, y, pf, i == k);
+        col[i] = v[u];
+      }
+    }
+  }
+  unsigned long long mx = 0;
+#pragma unroll
+  for (int u = 0; u < SCS_U; ++u) mx = max(mx, (unsigned long long)__double_as_longlong(v[u]) & 0x7fffffffffffffffull);
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) redm[wid] = mx;
+  __syncthreads();
+#pragma unroll
+  for (int w = 0; w < T / 32; ++w) mx = max(mx, redm[w]);
+  const int e = colmax_expo(mx);
+  if (threadIdx.x == 0) expo[n] = e;
+  __nv_bfloat16* dst = stack + (size_t)n * S * Kp;
+#pragma unroll
+  for (int u = 0; u < SCS_U; ++u) {
+    const int64_t i = threadIdx.x + (int64_t)u * T;
+    if (i < Kp) slice_store((unsigned long long)__double_as_longlong(v[u]), e, dst, Kp, i);
+  }
+}
+
 // Fused exact-slice product.  One CTA owns a 128 x SBN tile of C and a range of at most 16 k-blocks
 // (1024 entries of K, so that the level-0 and level-1 FP32 sums are exact).  Per k-block the B digits
 // d'_0..d'_4 (5 tiles) are loaded once into a B slot, and the A digits d_0..d_4 stream through an
@@ -440,7 +504,7 @@ int sliced_prepare(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, int64_t
 // C (M x N, FP64) = A_op' B with A_op the prepared stack (K x M) and B (K x N, FP64, column-major).
 // reps > 1 (profiling) repeats the product kernel and reports its mean time per launch in *us.
 static int sliced_gemm_run(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const double* B, int64_t ldb, double* C,
-                           int64_t ldc, int reps, double* us, double* bytes) {
+                           int64_t ldc, int reps, double* us, double* bytes, const SlicedOperand* Bpre = nullptr) {
   using namespace slice;
   const int64_t K = A.K, Kp = A.Kp, M = A.M;
   // the combined 64-bit integer is bounded by K 2^(2 BETA + BETA LMAX) (1 + 2^-6): K <= 2^20 keeps it below 2^63
@@ -448,7 +512,12 @@ static int sliced_gemm_run(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, con
   WsScope scope(ctx);
   int st = OFRR_SUCCESS;
   SlicedOperand Bs;
-  OFRR_TRY(sliced_prepare(ctx, K, N, B, ldb, &Bs));
+  if (Bpre) {
+    if (Bpre->K != K || Bpre->Kp != Kp || Bpre->M != N) return OFRR_ERR_INVALID_ARGUMENT;
+    Bs = *Bpre;
+  } else {
+    OFRR_TRY(sliced_prepare(ctx, K, N, B, ldb, &Bs));
+  }
   CUtensorMap ma, mb;
   if (!tc::make_map(&ma, OFRR_BF16, A.stack, S * Kp, M, S * Kp, tc::BM) ||
       !tc::make_map(&mb, OFRR_BF16, Bs.stack, S * Kp, N, S * Kp, SBN))
@@ -503,6 +572,27 @@ static int sliced_gemm_run(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, con
 int sliced_gemm_tn(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const double* B, int64_t ldb, double* C,
                    int64_t ldc) {
   return sliced_gemm_run(ctx, A, N, B, ldb, C, ldc, 1, nullptr, nullptr);
+}
+
+int sliced_gemm_tn_pre(ofrr_ctx* ctx, const SlicedOperand& A, const SlicedOperand& B, double* C, int64_t ldc) {
+  return sliced_gemm_run(ctx, A, B.M, nullptr, 0, C, ldc, 1, nullptr, nullptr, &B);
+}
+
+int scalecols_sliced(ofrr_ctx* ctx, int64_t m, int64_t n, double* U, int64_t ldu, __nv_bfloat16* stack, int* expo,
+                     SlicedOperand* out) {
+  if (m < 1 || m > 8192 || n < 1 || n > 65535) return OFRR_ERR_BLAS_INVALID_SIZE;
+  out->K = m;
+  out->Kp = (m + 63) / 64 * 64;
+  out->M = n;
+  out->stack = stack;
+  out->expo = expo;
+  if (m <= 2048) {
+    slice::k_scalecols_slice<256><<<(unsigned)n, 256, 0, ctx->stream>>>(m, out->Kp, U, ldu, stack, expo);
+  } else {
+    slice::k_scalecols_slice<1024><<<(unsigned)n, 1024, 0, ctx->stream>>>(m, out->Kp, U, ldu, stack, expo);
+  }
+  OFRR_LAUNCHED(ctx, "k_scalecols_slice");
+  return OFRR_SUCCESS;
 }
 
 }  // namespace ofrr

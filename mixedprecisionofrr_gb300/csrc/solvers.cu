@@ -79,6 +79,14 @@ struct Op {
     return gemm_impl(ctx, trans, 0, ta, tx, tc, ty, M, nrhs, K, 1.0, Ad, lda, X, ldx, 0.0, Y, ldy);
   }
 
+  // Y = op(A) X for X already split into digits (scalecols_sliced); dense operators in the emulated mode
+  bool can_apply_pre(const ofrr_ctx* ctx) const {
+    return ctx->emulate_f64 && A->kind == OFRR_OP_DENSE && have_sA && have_sAt;
+  }
+  int apply_pre(ofrr_ctx* ctx, int trans, const SlicedOperand& Xs, double* Y, int64_t ldy) {
+    return sliced_gemm_tn_pre(ctx, trans ? sA : sAt, Xs, Y, ldy);
+  }
+
   // digit stacks of A for the FP64 emulation: sAt for A V (operand A', K = n), sA for A' U (K = m).
   // Must be called in the solve's outermost workspace scope (the stacks live as long as the solve).
   SlicedOperand sA, sAt;
@@ -1066,16 +1074,42 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
   std::vector<int> hsel(2 * b0);
   const int check_every = std::max(1, opt->check_every);
   const bool f64 = P.po == OFRR_F64;
+  // fused scaling + digit split for the emulated FP64 products (columns of at most 8192 rows)
+  const bool fused = f64 && P.fast && op.can_apply_pre(ctx) && m <= 8192 && n <= 8192;
+  __nv_bfloat16 *dig_u = nullptr, *dig_v = nullptr;
+  int *exp_u = nullptr, *exp_v = nullptr;
+  if (fused) {
+    dig_u = ws_get<__nv_bfloat16>(ctx, (size_t)b0 * kSliceDigits * ((m + 63) / 64 * 64), &st);
+    dig_v = ws_get<__nv_bfloat16>(ctx, (size_t)b0 * kSliceDigits * ((n + 63) / 64 * 64), &st);
+    exp_u = ws_get<int>(ctx, (size_t)b0, &st);
+    exp_v = ws_get<int>(ctx, (size_t)b0, &st);
+    if (!dig_u || !dig_v || !exp_u || !exp_v) return st;
+  }
   for (int k = 0; k < maxit && !S.done; ++k) {
     int b = S.b;
     {
       TraceScope ts(ctx, f64 ? "power.f64" : "power.16bit");
-      for (int j = 0; j < opt->step_size; ++j) {
-        OFRR_TRY(op.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.po, U, ldu));
-        OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, m, b, U, ldu, nullptr, P.fast));
-        OFRR_TRY(op.apply(ctx, 1, P.po, P.po, U, ldu, b, P.pc, P.po, V, ldv));
-        OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr, P.fast));
-        S.nmv += 2 * b;
+      if (fused) {
+        // emulated FP64 products: each scalecols also writes the digits of the scaled block, the
+        // operand of the next product (bit-identical to scaling, then splitting)
+        SlicedOperand Us, Vs;
+        for (int j = 0; j < opt->step_size; ++j) {
+          if (j == 0) OFRR_TRY(op.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.po, U, ldu));
+          else OFRR_TRY(op.apply_pre(ctx, 0, Vs, (double*)U, ldu));
+          OFRR_TRY(scalecols_sliced(ctx, m, b, (double*)U, ldu, dig_u, exp_u, &Us));
+          OFRR_TRY(op.apply_pre(ctx, 1, Us, (double*)V, ldv));
+          if (j + 1 < opt->step_size) OFRR_TRY(scalecols_sliced(ctx, n, b, (double*)V, ldv, dig_v, exp_v, &Vs));
+          else OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr, P.fast));
+          S.nmv += 2 * b;
+        }
+      } else {
+        for (int j = 0; j < opt->step_size; ++j) {
+          OFRR_TRY(op.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.po, U, ldu));
+          OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, m, b, U, ldu, nullptr, P.fast));
+          OFRR_TRY(op.apply(ctx, 1, P.po, P.po, U, ldu, b, P.pc, P.po, V, ldv));
+          OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr, P.fast));
+          S.nmv += 2 * b;
+        }
       }
     }
     {
