@@ -196,6 +196,8 @@ template <class TO, class TC, bool FAST, int T>
 __global__ void __launch_bounds__(T) k_scalecols_small(int64_t m, TO* U, int64_t ldu, int* piv, int do_scale) {
   __shared__ ArgMaxK red[T / 32];
   __shared__ TO s_t;
+  __shared__ TC s_y;
+  __shared__ bool s_pf;
   TO* col = U + (int64_t)blockIdx.x * ldu;
   TO v[SC_U];
   ArgMaxK a{-1, 0x7fffffffffffffffLL};
@@ -217,12 +219,16 @@ __global__ void __launch_bounds__(T) k_scalecols_small(int64_t m, TO* U, int64_t
   if (threadIdx.x == 0) {
     if (piv) piv[blockIdx.x] = (int)k;
     s_t = (m > 0) ? col[k] : TO(0);
+    const TC t0 = to_c<TC, TO>(s_t);
+    // the reciprocal once per column: an FP64 reciprocal is a sequence of 1/64-rate instructions
+    s_y = (t0 != TC(0)) ? pivot_recip(t0) : TC(0);
+    s_pf = pivot_fast(t0);
   }
   __syncthreads();
   const TC t = to_c<TC, TO>(s_t);
   if (!do_scale || t == TC(0)) return;
-  const TC y = pivot_recip(t);
-  const bool pf = pivot_fast(t);
+  const TC y = s_y;
+  const bool pf = s_pf;
 #pragma unroll
   for (int u = 0; u < SC_U; ++u) {
     const int64_t i = threadIdx.x + (int64_t)u * T;
@@ -266,6 +272,8 @@ __global__ void __launch_bounds__(SC_T) k_colscale(int64_t m, TO* U, int64_t ldu
                                                    const double* pval, int* piv, int do_scale) {
   __shared__ double s_t;
   __shared__ long long s_k;
+  __shared__ TC s_y;
+  __shared__ bool s_pf;
   const int nchunks = gridDim.x;
   TO* col = U + (int64_t)blockIdx.y * ldu;
   if (threadIdx.x < 32) {
@@ -277,14 +285,17 @@ __global__ void __launch_bounds__(SC_T) k_colscale(int64_t m, TO* U, int64_t ldu
       s_k = k;
       s_t = (b.key < 0) ? 0.0 : pval[(size_t)blockIdx.y * nchunks + k / SC_CHUNK];
       if (piv && blockIdx.x == 0) piv[blockIdx.y] = (int)k;
+      const TC t0 = to_c<TC, double>(s_t);
+      s_y = (t0 != TC(0)) ? pivot_recip(t0) : TC(0);
+      s_pf = pivot_fast(t0);
     }
   }
   __syncthreads();
   const TC t = to_c<TC, double>(s_t);
   if (!do_scale || t == TC(0)) return;
   const int64_t k = s_k;
-  const TC y = pivot_recip(t);
-  const bool pf = pivot_fast(t);
+  const TC y = s_y;
+  const bool pf = s_pf;
   const int64_t r0 = (int64_t)blockIdx.x * SC_CHUNK;
   TO v[SC_U];
 #pragma unroll

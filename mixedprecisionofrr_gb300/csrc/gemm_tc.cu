@@ -151,14 +151,26 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
-template <class TOUT>
+// Fixed-order sum of the K-split partials (deterministic).  WIDE (many splits): loads issued eight at
+// a time; otherwise the plain loop, whose low register count keeps more loads resident.
+template <class TOUT, bool WIDE>
 __global__ void k_splitk_reduce(int M, int N, int splits, const float* __restrict__ partial, TOUT* __restrict__ D,
                                 int64_t ldd) {
   const int64_t total = (int64_t)M * N;
   OFRR_FOR_2D(m, n, M, N) {
     const int64_t e = m + n * (int64_t)M;
     float s = 0.f;
-    for (int z = 0; z < splits; ++z) s += partial[(size_t)z * total + e];  // fixed order: deterministic
+    int z = 0;
+    if (WIDE) {
+      for (; z + 8 <= splits; z += 8) {
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = partial[(size_t)(z + u) * total + e];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += v[u];
+      }
+    }
+    for (; z < splits; ++z) s += partial[(size_t)z * total + e];
     D[m + n * ldd] = cvt_out<TOUT>(s);
   }
 }
@@ -189,7 +201,10 @@ static int launch(ofrr_ctx* ctx, const CUtensorMap& ma, const CUtensorMap& mb, i
                                                             partial, ctx->dev_flags + kFlagTcWait);
   OFRR_LAUNCHED(ctx, "k_gemm_tn");
   if (splits > 1) {
-    k_splitk_reduce<TOUT><<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, splits, partial, D, ldd);
+    if (splits >= 12)
+      k_splitk_reduce<TOUT, true><<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, splits, partial, D, ldd);
+    else
+      k_splitk_reduce<TOUT, false><<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, splits, partial, D, ldd);
     OFRR_LAUNCHED(ctx, "k_splitk_reduce");
   }
   return OFRR_SUCCESS;

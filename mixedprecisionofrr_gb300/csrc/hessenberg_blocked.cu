@@ -19,6 +19,7 @@
 
 #include <atomic>
 #include <cstdlib>
+#include <type_traits>
 
 #include "ofrr_internal.cuh"
 #include "tcgen05.cuh"
@@ -196,6 +197,8 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
   __shared__ __align__(8) uint64_t s_bar[2];
   __shared__ ArgMaxK red[HB_T / 32];
   __shared__ int s_abort;
+  __shared__ TC s_y;
+  __shared__ bool s_pf;
 
   if (tid == 0) {
     tc::mbar_init(&s_bar[0], 1);
@@ -281,8 +284,22 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
     }
     // (3) scale (or zero) column t, eliminate the later block columns against it, argmax of column t+1
     const TC pc = to_c<TC, TO>(pv);
-    const TC y = pivot_recip(pc);
-    const bool pf = pivot_fast(pc);
+    TC y;
+    bool pf;
+    if constexpr (std::is_same<TC, double>::value) {
+      // one FP64 reciprocal per column (a sequence of 1/64-rate instructions), shared through
+      // shared memory: s_y is rewritten only after the next column's exchange, past every read
+      if (tid == 0) {
+        s_y = pivot_recip(pc);
+        s_pf = pivot_fast(pc);
+      }
+      __syncthreads();
+      y = s_y;
+      pf = s_pf;
+    } else {
+      y = pivot_recip(pc);
+      pf = pivot_fast(pc);
+    }
     const bool has_next = t + 1 < nb;
     ArgMaxK a{-1, 0x7fffffffffffffffLL};
     for (int lr = tid; lr < nloc; lr += HB_T) {

@@ -147,18 +147,18 @@ __global__ void __launch_bounds__(SLICE_T) k_slice_digits(int64_t K, int64_t Kp,
 // registers, takes its maximum with a block reduction and writes the digits (no second read, no
 // atomics, no zeroed scratch).
 constexpr int SC_T = 512;
-template <int U>
-__global__ void __launch_bounds__(SC_T) k_slice_cols(int64_t K, int64_t Kp, int64_t N, const double* __restrict__ X,
-                                                     int64_t ldx, __nv_bfloat16* __restrict__ stack,
-                                                     int* __restrict__ expo) {
-  __shared__ unsigned long long red[SC_T / 32];
+template <int U, int T = SC_T>
+__global__ void __launch_bounds__(T) k_slice_cols(int64_t K, int64_t Kp, int64_t N, const double* __restrict__ X,
+                                                  int64_t ldx, __nv_bfloat16* __restrict__ stack,
+                                                  int* __restrict__ expo) {
+  __shared__ unsigned long long red[T / 32];
   for (int64_t n = blockIdx.x; n < N; n += gridDim.x) {
     const double* x = X + n * ldx;
     unsigned long long v[U];
     unsigned long long mx = 0;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const int64_t k = threadIdx.x + (int64_t)u * SC_T;
+      const int64_t k = threadIdx.x + (int64_t)u * T;
       v[u] = (k < K) ? (unsigned long long)__double_as_longlong(x[k]) : 0ull;
       mx = max(mx, v[u] & 0x7fffffffffffffffull);
     }
@@ -166,13 +166,13 @@ __global__ void __launch_bounds__(SC_T) k_slice_cols(int64_t K, int64_t Kp, int6
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
     __syncthreads();
 #pragma unroll
-    for (int w = 0; w < SC_T / 32; ++w) mx = max(mx, red[w]);
+    for (int w = 0; w < T / 32; ++w) mx = max(mx, red[w]);
     const int e = colmax_expo(mx);
     if (threadIdx.x == 0) expo[n] = e;
     __nv_bfloat16* col = stack + (size_t)n * S * Kp;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const int64_t k = threadIdx.x + (int64_t)u * SC_T;
+      const int64_t k = threadIdx.x + (int64_t)u * T;
       if (k < Kp) slice_store(v[u], e, col, Kp, k);
     }
     __syncthreads();  // red is reused by the next column
@@ -190,7 +190,8 @@ __global__ void __launch_bounds__(T) k_scalecols_slice(int64_t m, int64_t Kp, do
                                                        __nv_bfloat16* __restrict__ stack, int* __restrict__ expo) {
   __shared__ ArgMaxK red[T / 32];
   __shared__ unsigned long long redm[T / 32];
-  __shared__ double s_t;
+  __shared__ double s_t, s_y;
+  __shared__ bool s_pf;
   const int n = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   double* col = U + (int64_t)n * ldu;
   double v[SCS_U];
@@ -210,12 +211,16 @@ __global__ void __launch_bounds__(T) k_scalecols_slice(int64_t m, int64_t Kp, do
   }
   const ArgMaxK r = block_argmaxk(a, red);
   const int64_t k = (r.key < 0) ? 0 : r.i;
-  if (threadIdx.x == 0) s_t = (m > 0) ? col[k] : 0.0;
+  if (threadIdx.x == 0) {
+    s_t = (m > 0) ? col[k] : 0.0;
+    s_y = (s_t != 0.0) ? pivot_recip(s_t) : 0.0;  // once per column (1/64-rate FP64 pipe)
+    s_pf = pivot_fast(s_t);
+  }
   __syncthreads();
   const double t = s_t;
   if (t != 0.0) {
-    const double y = pivot_recip(t);
-    const bool pf = pivot_fast(t);
+    const double y = s_y;
+    const bool pf = s_pf;
 #pragma unroll
     for (int u = 0; u < SCS_U; ++u) {
       const int64_t i = threadIdx.x + (int64_t)u * T;
@@ -436,7 +441,10 @@ __global__ void __launch_bounds__(SL_THREADS, 1)
   }
 }
 
-// C = 2^(ea + eb - BETA (LMAX + 2)) * sum_z P_z  (64-bit integer partials, exact in any order)
+// C = 2^(ea + eb - BETA (LMAX + 2)) * sum_z P_z  (64-bit integer partials, exact in any order).
+// WIDE (many K ranges): eight independent accumulators keep eight loads in flight; otherwise the
+// plain loop, whose low register count keeps more threads (and loads) resident.
+template <bool WIDE>
 __global__ void k_sliced_finish(int64_t M, int64_t N, int splits, const long long* __restrict__ P,
                                 double* __restrict__ C, int64_t ldc, const int* __restrict__ ea,
                                 const int* __restrict__ eb) {
@@ -444,7 +452,19 @@ __global__ void k_sliced_finish(int64_t M, int64_t N, int splits, const long lon
   OFRR_FOR_2D(m, n, M, N) {
     const int64_t e = m + n * M;
     long long s = 0;
-    for (int z = 0; z < splits; ++z) s += P[(size_t)z * total + e];
+    if (WIDE) {
+      long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      int z = 0;
+      for (; z + 8 <= splits; z += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc[u] += P[(size_t)(z + u) * total + e];
+      }
+      for (; z < splits; ++z) acc[0] += P[(size_t)z * total + e];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) s += acc[u];
+    } else {
+      for (int z = 0; z < splits; ++z) s += P[(size_t)z * total + e];
+    }
     C[m + n * ldc] = i64_ldexp(s, ea[m] + eb[n] - SL_SHIFT);
   }
 }
@@ -461,6 +481,12 @@ int sliced_prepare_into(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, in
   out->M = M;
   out->stack = stack;
   out->expo = expo;
+  if (out->Kp <= 128) {  // short columns (back-transform coefficients): 64 threads per column
+    slice::k_slice_cols<2, 64><<<(unsigned)std::min<int64_t>(M, 65535), 64, 0, ctx->stream>>>(K, out->Kp, M, X, ldx,
+                                                                                            stack, expo);
+    OFRR_LAUNCHED(ctx, "k_slice_cols");
+    return OFRR_SUCCESS;
+  }
   if (out->Kp <= slice::SC_T * 16) {
     const unsigned grid = (unsigned)std::min<int64_t>(M, 65535);
     const int64_t u = (out->Kp + slice::SC_T - 1) / slice::SC_T;
@@ -526,6 +552,8 @@ static int sliced_gemm_run(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, con
   const int tiles = (int)(((M + tc::BM - 1) / tc::BM) * ((N + SBN - 1) / SBN));
   // K ranges of at most 16 k-blocks (exactness), and about one wave of CTAs
   int splits = std::max((kbt + SL_KB_MAX - 1) / SL_KB_MAX, std::min(kbt, std::max(1, 148 / tiles)));
+  // few output tiles (Gram products): at most 32 K ranges, so the partial sums stay cheap to combine
+  if (tiles <= 4) splits = std::min(splits, std::max((kbt + SL_KB_MAX - 1) / SL_KB_MAX, 32));
   const int kbps = (kbt + splits - 1) / splits;
   splits = (kbt + kbps - 1) / kbps;
   long long* P = nullptr;
@@ -563,7 +591,10 @@ static int sliced_gemm_run(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, con
       *bytes = (double)S * Kp * 2 * (double)(M + N) + (double)M * N * 8 * (splits > 1 ? splits : 1);
   }
   if (splits > 1) {
-    k_sliced_finish<<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, splits, P, C, ldc, A.expo, Bs.expo);
+    if (splits >= 12)
+      k_sliced_finish<true><<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, splits, P, C, ldc, A.expo, Bs.expo);
+    else
+      k_sliced_finish<false><<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, splits, P, C, ldc, A.expo, Bs.expo);
     OFRR_LAUNCHED(ctx, "k_sliced_finish");
   }
   return OFRR_SUCCESS;

@@ -331,11 +331,16 @@ __device__ __forceinline__ int rr_pos(int i, int r, int N) {
 // threshold test, the norm update) is then shared by four pairs in one warp instruction stream.  The
 // angle need not be exact, only the rotation orthogonal: c = 1/sqrt(1 + t^2) is refined by one Newton
 // step so that c^2 + s^2 = 1 to rounding (the accumulated V stays orthogonal to FP32 accuracy).
+// Column stride of G and V in shared memory: ld = 8 (mod 32), so that the columns of the four pairs a
+// warp handles (adjacent positions of the round-robin order, mostly adjacent column indices) fall in
+// disjoint groups of eight banks.
+__host__ __device__ __forceinline__ int j1_ld(int n) { return n + (40 - n % 32) % 32; }
+
 template <int R>  // rows per lane: n <= 8 R
 __global__ void __launch_bounds__(256, 1) k_jacobi1_f32(int n, const double* __restrict__ Gin, int ldg, int trans,
                                                      double* __restrict__ Vout) {
   extern __shared__ float sm1[];
-  const int ld = n + 1;
+  const int ld = j1_ld(n);
   float* G = sm1;
   float* V = sm1 + n * ld;
   __shared__ int s_any;
@@ -709,7 +714,7 @@ int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const dou
   {  // starting vectors: FP32 one-sided Jacobi on the columns of C (= rows of the stored matrix)
     double* X0 = ws_get<double>(ctx, (size_t)b * b, &st);
     if (!X0) return st;
-    const size_t smem = (size_t)2 * b * (b + 1) * sizeof(float);
+    const size_t smem = (size_t)2 * b * j1_ld(b) * sizeof(float);
     if (b <= 64) {
       OFRR_TRY(allow_smem(k_jacobi1_f32<8>));
       k_jacobi1_f32<8><<<1, 256, smem, ctx->stream>>>(b, C, b, 1, X0);

@@ -223,6 +223,78 @@ int validate_op(const ofrr_operator* A) {
 // Rayleigh-Ritz on a basis Q (n x b, type tq): eig_rr.m:46-57.
 // Outputs: Ritz vectors into Vout (n x b, type tq), Ritz values d (device, b, descending).
 // ---------------------------------------------------------------------------------------
+// Ritz back-transform of a 16-bit basis with FP32 arithmetic: Out = tq(Q (m x b) * f32(Cf) (b x b)),
+// one thread per row and 32 output columns, the coefficient block in shared memory (FP32), the FP32
+// result rounded once to the basis type.  Replaces widening Q to FP32, a library SGEMM and a cast.
+template <class TQ>
+__global__ void __launch_bounds__(128) k_backtransform16(int64_t m, int b, const TQ* __restrict__ Q, int64_t ldq,
+                                                         const double* __restrict__ Cf, int ldc, TQ* __restrict__ Out,
+                                                         int64_t ldo) {
+  __shared__ float Zs[128][33];
+  const int j0 = blockIdx.y * 32;
+  const int nj = min(32, b - j0);
+  for (int e = threadIdx.x; e < b * 32; e += blockDim.x) {
+    const int k = e >> 5, jj = e & 31;
+    Zs[k][jj] = (jj < nj) ? __double2float_rn(Cf[k + (size_t)(j0 + jj) * ldc]) : 0.f;
+  }
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  float acc[32];
+#pragma unroll
+  for (int jj = 0; jj < 32; ++jj) acc[jj] = 0.f;
+  for (int k0 = 0; k0 < b; k0 += 64) {  // the row's basis entries loaded 64 at a time (one latency)
+    float u[64];
+#pragma unroll
+    for (int t = 0; t < 64; ++t) u[t] = (k0 + t < b) ? to_c<float, TQ>(Q[i + (int64_t)(k0 + t) * ldq]) : 0.f;
+#pragma unroll
+    for (int t = 0; t < 64; ++t) {
+      if (k0 + t < b) {
+#pragma unroll
+        for (int jj = 0; jj < 32; ++jj) acc[jj] = fmaf(u[t], Zs[k0 + t][jj], acc[jj]);
+      }
+    }
+  }
+#pragma unroll
+  for (int jj = 0; jj < 32; ++jj)
+    if (jj < nj) Out[i + (int64_t)(j0 + jj) * ldo] = from_c<TQ, float>(acc[jj]);
+}
+
+// Out (type tq) = tq(gemm(Q, Cf, pmc) rounded to pmo): the fused kernel for 16-bit bases with FP32
+// compute and output, the general product and cast otherwise
+int back_transform(ofrr_ctx* ctx, ofrr_dtype tq, ofrr_dtype pmc, ofrr_dtype pmo, int64_t m, int b, const void* Q,
+                   int64_t ldq, const double* Cf, void* Out, int64_t ldo) {
+  if ((tq == OFRR_F16 || tq == OFRR_BF16) && pmc == OFRR_F32 && pmo == OFRR_F32 && b <= 128 && Out != Q) {
+    const dim3 grid((unsigned)((m + 127) / 128), (unsigned)((b + 31) / 32));
+    if (tq == OFRR_F16)
+      k_backtransform16<__half><<<grid, 128, 0, ctx->stream>>>(m, b, (const __half*)Q, ldq, Cf, b, (__half*)Out, ldo);
+    else
+      k_backtransform16<__nv_bfloat16><<<grid, 128, 0, ctx->stream>>>(m, b, (const __nv_bfloat16*)Q, ldq, Cf, b,
+                                                                     (__nv_bfloat16*)Out, ldo);
+    OFRR_LAUNCHED(ctx, "k_backtransform16");
+    return OFRR_SUCCESS;
+  }
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  void* Vn = Out;
+  int64_t ldvn = ldo;
+  if (pmo != tq || Out == Q) {
+    Vn = ws_alloc(ctx, (size_t)m * b * dtype_size(pmo), &st);
+    if (!Vn) return st;
+    ldvn = m;
+  }
+  OFRR_TRY(gemm_impl(ctx, 0, 0, tq, OFRR_F64, pmc, pmo, m, b, b, 1.0, Q, ldq, Cf, b, 0.0, Vn, ldvn));
+  if (Vn != Out) OFRR_TRY(cast_impl(ctx, pmo, tq, m, b, Vn, ldvn, Out, ldo));
+  return OFRR_SUCCESS;
+}
+
+// A V with a dense 16-bit A and a basis of the same 16-bit type, accumulated in FP32: the basis
+// values are exact in FP32, so widening it first changes nothing but the route (a library SGEMM on a
+// widened A instead of the tensor cores)
+bool tc16_direct(const Op& op, ofrr_dtype ta, ofrr_dtype tq, ofrr_dtype pAmc) {
+  return op.A->kind == OFRR_OP_DENSE && (ta == OFRR_F16 || ta == OFRR_BF16) && tq == ta && pAmc == OFRR_F32;
+}
+
 int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype tq, int64_t ldq, int b,
                ofrr_dtype pmc, ofrr_dtype pmo, ofrr_dtype pAmc, ofrr_dtype pAmo, bool use_gen, double gtol,
                bool symmetric, void* Vout, int64_t ldvo, double* d, bool fast = false, int refine = 2) {
@@ -232,7 +304,10 @@ int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype t
   // AV = pmc(matvec(A, 'N', pAmc(Q), pAmc, pAmo)) -- kept in pAmo storage, widened by the Gram gemm
   const void* Qa = Q;
   int64_t ldqa = ldq;
-  if (tq != pAmc) {
+  ofrr_dtype tqa = pAmc;
+  if (tc16_direct(op, ta, tq, pAmc)) {
+    tqa = tq;  // 16-bit A and basis, FP32 accumulation: the tensor-core product reads the basis as is
+  } else if (tq != pAmc) {
     void* w = ws_alloc(ctx, (size_t)n * b * dtype_size(pAmc), &st);
     if (!w) return st;
     OFRR_TRY(cast_impl(ctx, tq, pAmc, n, b, Q, ldq, w, n));
@@ -241,7 +316,7 @@ int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype t
   }
   void* AV = ws_alloc(ctx, (size_t)n * b * dtype_size(pAmo), &st);
   if (!AV) return st;
-  OFRR_TRY(op.apply(ctx, 0, ta, pAmc, Qa, ldqa, b, pAmc, pAmo, AV, n));
+  OFRR_TRY(op.apply(ctx, 0, ta, tqa, Qa, ldqa, b, pAmc, pAmo, AV, n));
   ofrr_dtype tav = pAmo;
   if (pAmo != pmc) {  // the MATLAB code rounds to pAmo then converts to pmc: identical values
     // no storage change needed: gemm widens pAmo to pmc exactly
@@ -272,16 +347,7 @@ int rr_eig_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* Q, ofrr_dtype t
     OFRR_TRY(geig_dev(ctx, b, G, b, M, b, symmetric ? 1 : 0, d, U, b));
   }
   // V = gemm(V, 'N', U, pmc, pmo) then back to V's precision
-  void* Vn = Vout;
-  int64_t ldvn = ldvo;
-  if (pmo != tq || Vout == Q) {
-    Vn = ws_alloc(ctx, (size_t)n * b * dtype_size(pmo), &st);
-    if (!Vn) return st;
-    ldvn = n;
-  }
-  OFRR_TRY(gemm_impl(ctx, 0, 0, tq, OFRR_F64, pmc, pmo, n, b, b, 1.0, Q, ldq, U, b, 0.0, Vn, ldvn));
-  if (Vn != Vout) OFRR_TRY(cast_impl(ctx, pmo, tq, n, b, Vn, ldvn, Vout, ldvo));
-  return OFRR_SUCCESS;
+  return back_transform(ctx, tq, pmc, pmo, n, b, Q, ldq, U, Vout, ldvo);
 }
 
 // at most 4 CTAs per column: each thread handles several rows of one column
@@ -525,7 +591,10 @@ int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* 
   if (!use_gen) return OFRR_ERR_NOT_IMPLEMENTED;  // svd(UAV) path: the oblique bases need the pencil
   const void* Va = V;
   int64_t ldva = ldv;
-  if (tq != pAmc) {
+  ofrr_dtype tva = pAmc;
+  if (tc16_direct(op, ta, tq, pAmc)) {
+    tva = tq;  // 16-bit A and basis, FP32 accumulation: the tensor-core product reads the basis as is
+  } else if (tq != pAmc) {
     void* w = ws_alloc(ctx, (size_t)n * b * dtype_size(pAmc), &st);
     if (!w) return st;
     OFRR_TRY(cast_impl(ctx, tq, pAmc, n, b, V, ldv, w, n));
@@ -553,7 +622,7 @@ int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* 
   OFRR_TRY(cast_impl(aux, pmo, OFRR_F64, b, b, tmpu, b, UU, b));
   OFRR_TRY(gemm_impl(aux, 1, 0, tq, tq, pmc, pmo, b, b, n, 1.0, V, ldv, V, ldv, 0.0, tmpv, b));
   OFRR_TRY(cast_impl(aux, pmo, OFRR_F64, b, b, tmpv, b, VV, b));
-  OFRR_TRY(op.apply(ctx, 0, ta, pAmc, Va, ldva, b, pAmc, pAmo, AV, m));
+  OFRR_TRY(op.apply(ctx, 0, ta, tva, Va, ldva, b, pAmc, pAmo, AV, m));
   OFRR_TRY(gemm_impl(ctx, 1, 0, tq, pAmo, pmc, pmo, b, b, m, 1.0, U, ldu, AV, m, 0.0, tmp, b));
   OFRR_TRY(cast_impl(ctx, pmo, OFRR_F64, b, b, tmp, b, B, b));
   OFRR_TRY(aux_end(ctx));
@@ -564,22 +633,10 @@ int rr_svd_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype ta, const void* U, const void* 
     OFRR_TRY(dmalloc(ctx, &Zf, (size_t)b * b));
     OFRR_TRY(dmalloc(ctx, &Wf, (size_t)b * b));
     OFRR_TRY(gsvd_fast(ctx, b, B, UU, VV, gtol, s_dev, Zf, Wf, refine));
-    void* Uo = Uout;
-    void* Vo = Vout;
-    int64_t lu = lduo, lv = ldvo;
-    if (pmo != tq) {
-      Uo = ws_alloc(ctx, (size_t)m * b * dtype_size(pmo), &st);
-      Vo = ws_alloc(ctx, (size_t)n * b * dtype_size(pmo), &st);
-      if (!Uo || !Vo) return st;
-      lu = m;
-      lv = n;
-    }
     // the two back-transforms are independent: V's on the auxiliary stream
     OFRR_TRY(aux_begin(ctx, &aux));
-    OFRR_TRY(gemm_impl(aux, 0, 0, tq, OFRR_F64, pmc, pmo, n, b, b, 1.0, V, ldv, Wf, b, 0.0, Vo, lv));
-    if (Vo != Vout) OFRR_TRY(cast_impl(aux, pmo, tq, n, b, Vo, lv, Vout, ldvo));
-    OFRR_TRY(gemm_impl(ctx, 0, 0, tq, OFRR_F64, pmc, pmo, m, b, b, 1.0, U, ldu, Zf, b, 0.0, Uo, lu));
-    if (Uo != Uout) OFRR_TRY(cast_impl(ctx, pmo, tq, m, b, Uo, lu, Uout, lduo));
+    OFRR_TRY(back_transform(aux, tq, pmc, pmo, n, b, V, ldv, Wf, Vout, ldvo));
+    OFRR_TRY(back_transform(ctx, tq, pmc, pmo, m, b, U, ldu, Zf, Uout, lduo));
     OFRR_TRY(aux_end(ctx));
     return OFRR_SUCCESS;
   }
@@ -1133,10 +1190,15 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
       const int w = std::min(wu, wv);  // svd_rr.m:61 keeps k = min(ku, kv)
       if (w == 0) return OFRR_ERR_SOLVER_DIVERGENCE;
       S.b = b = w;
-      OFRR_TRY(rr_svd_dev(ctx, op, P.po, P1, Q1, P.pho, m, n, b, P.prc, P.pro, P.pc, P.po, opt->use_generalized != 0,
-                          opt->generalized_tol, Ut, m, Vt, n, d_dev, P.fast, P.refine));
-      OFRR_TRY(cast_impl(ctx, P.pho, P.po, m, b, Ut, m, U, ldu));
-      OFRR_TRY(cast_impl(ctx, P.pho, P.po, n, b, Vt, n, V, ldv));
+      if (P.pho == P.po) {  // the Ritz vectors go straight into U and V (the bases live in P1, Q1)
+        OFRR_TRY(rr_svd_dev(ctx, op, P.po, P1, Q1, P.pho, m, n, b, P.prc, P.pro, P.pc, P.po,
+                            opt->use_generalized != 0, opt->generalized_tol, U, ldu, V, ldv, d_dev, P.fast, P.refine));
+      } else {
+        OFRR_TRY(rr_svd_dev(ctx, op, P.po, P1, Q1, P.pho, m, n, b, P.prc, P.pro, P.pc, P.po,
+                            opt->use_generalized != 0, opt->generalized_tol, Ut, m, Vt, n, d_dev, P.fast, P.refine));
+        OFRR_TRY(cast_impl(ctx, P.pho, P.po, m, b, Ut, m, U, ldu));
+        OFRR_TRY(cast_impl(ctx, P.pho, P.po, n, b, Vt, n, V, ldv));
+      }
     }
     S.nmv += b;
     S.it++;
