@@ -382,6 +382,89 @@ __global__ void k_colnorm(int64_t m, int64_t n, const T* X, int64_t ldx, double*
   }
 }
 
+// sqrt(sum_i f(i, j)^2) per column j over a grid of (row chunks x columns) CTAs: each CTA reduces its
+// chunk in a fixed order (rows loaded CS_R at a time), the last CTA of a column (a self-resetting
+// counter) adds the chunk sums in chunk order -- deterministic, and the FP64 work of a column spread
+// over many SMs (one CTA per column was bound by one SM's 1/64-rate FP64 pipe).
+constexpr int CS_T = 256, CS_R = 4;
+template <class F>
+__global__ void __launch_bounds__(CS_T) k_colsumsq(int64_t m, F f, double* __restrict__ part,
+                                                  unsigned int* __restrict__ counters, double* __restrict__ out) {
+  __shared__ double red[CS_T / 32];
+  __shared__ bool last;
+  const int64_t j = blockIdx.y;
+  const int64_t r0 = (int64_t)blockIdx.x * CS_T * CS_R;
+  double v[CS_R];
+#pragma unroll
+  for (int u = 0; u < CS_R; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * CS_T;
+    v[u] = (i < m) ? f(i, j) : 0.0;
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int u = 0; u < CS_R; ++u) s = fma(v[u], v[u], s);
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < CS_T / 32; ++w) t += red[w];
+    part[j * gridDim.x + blockIdx.x] = t;
+    __threadfence();
+    last = (atomicAdd(&counters[j], 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  const volatile double* pp = part + j * gridDim.x;
+  double t = 0.0;
+  for (unsigned c = 0; c < gridDim.x; ++c) t += pp[c];
+  counters[j] = 0u;
+  out[j] = sqrt(t);
+}
+
+template <class T>
+struct ColValue {
+  const T* X;
+  int64_t ldx;
+  __device__ double operator()(int64_t i, int64_t j) const { return to_c<double, T>(X[i + j * ldx]); }
+};
+struct ColResidualX {  // A x_j - lam_j x_j (separate leading dimensions)
+  const double* AX;
+  int64_t ldax;
+  const double* X;
+  int64_t ldx;
+  const double* lam;
+  __device__ double operator()(int64_t i, int64_t j) const { return AX[i + j * ldax] - lam[j] * X[i + j * ldx]; }
+};
+struct ColResidual {  // A v_j - s_j u_j
+  const double* AV;
+  const double* U;
+  const double* s;
+  int64_t ld;
+  __device__ double operator()(int64_t i, int64_t j) const { return AV[i + j * ld] - s[j] * U[i + j * ld]; }
+};
+
+template <class F>
+static int colsumsq_launch(ofrr_ctx* ctx, int64_t m, int64_t n, F f, double* out) {
+  int st = OFRR_SUCCESS;
+  WsScope scope(ctx);
+  const int64_t chunks = (m + CS_T * CS_R - 1) / (CS_T * CS_R);
+  double* part = ws_get<double>(ctx, (size_t)chunks * n, &st);
+  if (!part) return st;
+  k_colsumsq<F><<<dim3((unsigned)chunks, (unsigned)n), CS_T, 0, ctx->stream>>>(m, f, part, ctx->dev_counters, out);
+  OFRR_LAUNCHED(ctx, "k_colsumsq");
+  return OFRR_SUCCESS;
+}
+
+// ||A v_j - s_j u_j||_2 per column (FP64; AV and U m x n with leading dimension m)
+int residual_columns2(ofrr_ctx* ctx, int64_t m, int64_t n, const double* AV, const double* U, const double* s,
+                      double* out) {
+  if (n <= 0) return OFRR_SUCCESS;
+  if (n > 1024 || m <= 0 || (m + CS_T * CS_R - 1) / (CS_T * CS_R) > 65535) return OFRR_ERR_BLAS_INVALID_SIZE;
+  return colsumsq_launch(ctx, m, n, ColResidual{AV, U, s, m}, out);
+}
+
 // ||AX(:,j) - lam_j X(:,j)||_2 per column, FP64
 __global__ void k_rescol(int64_t m, int64_t n, const double* AX, int64_t ldax, const double* X, int64_t ldx,
                          const double* lam, double* out) {
@@ -459,6 +542,10 @@ int scalecols_impl(ofrr_ctx* ctx, ofrr_dtype po, ofrr_dtype pc, int64_t m, int64
 
 int column_norms(ofrr_ctx* ctx, ofrr_dtype t, int64_t m, int64_t n, const void* X, int64_t ldx, double* out) {
   if (n <= 0) return OFRR_SUCCESS;
+  if (n <= 1024 && m >= 2048 && (m + CS_T * CS_R - 1) / (CS_T * CS_R) <= 65535) {  // tall columns: many CTAs each
+    OFRR_DISPATCH_STORAGE(t, T, { OFRR_TRY(colsumsq_launch(ctx, m, n, ColValue<T>{(const T*)X, ldx}, out)); });
+    return OFRR_SUCCESS;
+  }
   int grid = (int)(n < 65535 ? n : 65535);
   OFRR_DISPATCH_STORAGE(t, T, {
     k_colnorm<T><<<grid, 256, 0, ctx->stream>>>(m, n, (const T*)X, ldx, out);
@@ -470,6 +557,8 @@ int column_norms(ofrr_ctx* ctx, ofrr_dtype t, int64_t m, int64_t n, const void* 
 int residual_columns(ofrr_ctx* ctx, int64_t m, int64_t n, const double* AX, int64_t ldax, const double* X,
                      int64_t ldx, const double* lam, double* out) {
   if (n <= 0) return OFRR_SUCCESS;
+  if (n <= 1024 && m >= 2048 && (m + CS_T * CS_R - 1) / (CS_T * CS_R) <= 65535)
+    return colsumsq_launch(ctx, m, n, ColResidualX{AX, ldax, X, ldx, lam}, out);
   int grid = (int)(n < 65535 ? n : 65535);
   k_rescol<<<grid, 256, 0, ctx->stream>>>(m, n, AX, ldax, X, ldx, lam, out);
   OFRR_LAUNCHED(ctx, "k_rescol");

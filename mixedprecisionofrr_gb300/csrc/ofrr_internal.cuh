@@ -443,6 +443,9 @@ int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const dou
               double* Zf, double* Wf, int refine = 2);
 
 // reductions
+// ||AV(:,j) - s_j U(:,j)||_2 per column, FP64 (ld m; n <= 1024), over many CTAs per column
+int residual_columns2(ofrr_ctx* ctx, int64_t m, int64_t n, const double* AV, const double* U, const double* s,
+                      double* out);
 int column_norms(ofrr_ctx* ctx, ofrr_dtype t, int64_t m, int64_t n, const void* X, int64_t ldx,
                  double* out_dev);
 // exact-slice FP64 emulation (sliced.cu): digit stacks of a fixed K x M FP64 operand and the

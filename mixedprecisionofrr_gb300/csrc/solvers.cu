@@ -728,10 +728,15 @@ int svd_residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* U, int64
   OFRR_TRY(op.apply(ctx, 0, OFRR_F64, OFRR_F64, V64, n, k, OFRR_F64, OFRR_F64, AV, m));
   OFRR_TRY(op.apply(ctx, 1, OFRR_F64, OFRR_F64, U64, m, k, OFRR_F64, OFRR_F64, ATU, n));
   OFRR_CUDA(cudaMemcpyAsync(sd, s_host, sizeof(double) * k, cudaMemcpyHostToDevice, ctx->stream));
-  k_rescol2<<<k, 256, 0, ctx->stream>>>(m, k, AV, U64, sd, nr + 2 * k);
-  OFRR_LAUNCHED(ctx, "k_rescol2");
-  k_rescol2<<<k, 256, 0, ctx->stream>>>(n, k, ATU, V64, sd, nr + 3 * k);
-  OFRR_LAUNCHED(ctx, "k_rescol2");
+  if (k <= 1024) {
+    OFRR_TRY(residual_columns2(ctx, m, k, AV, U64, sd, nr + 2 * k));
+    OFRR_TRY(residual_columns2(ctx, n, k, ATU, V64, sd, nr + 3 * k));
+  } else {
+    k_rescol2<<<k, 256, 0, ctx->stream>>>(m, k, AV, U64, sd, nr + 2 * k);
+    OFRR_LAUNCHED(ctx, "k_rescol2");
+    k_rescol2<<<k, 256, 0, ctx->stream>>>(n, k, ATU, V64, sd, nr + 3 * k);
+    OFRR_LAUNCHED(ctx, "k_rescol2");
+  }
   std::vector<double> h(4 * k, 0.0);
   if (certify16 >= 0) {  // emulated A v and A' u: add the bounds on their errors (unit columns)
     double* bnd;
