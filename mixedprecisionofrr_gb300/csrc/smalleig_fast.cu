@@ -24,15 +24,15 @@
 namespace ofrr {
 
 // ---- 1. Cholesky (lower) of M + tau I; batched over blockIdx.x ------------------------------------
-// Right-looking; per column one reciprocal square root (thread 0), the column scaled by it, and the
-// lower triangle of the trailing block updated with one warp per column (no index division).
+// Right-looking; per column one reciprocal square root, the column scaled by it, and the lower
+// triangle of the trailing block updated with one warp per column (no index division).
 __global__ void __launch_bounds__(256) k_chol_f64(int n, const double* const* Ms, int ldm, double tau,
                                                   double* const* Ls, int* flag) {
   extern __shared__ double S[];
   const double* M = Ms[blockIdx.x];
   double* L = Ls[blockIdx.x];
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-  __shared__ double s_maxd, s_rinv;
+  __shared__ double s_maxd, s_rinv2[2];
   // stage M + tau I (lower triangle) with 16 loads per thread in flight (the kernel is latency-bound)
   const int nn = n * n;
   for (int e0 = tid; e0 < nn; e0 += 16 * nt) {
@@ -58,25 +58,39 @@ __global__ void __launch_bounds__(256) k_chol_f64(int n, const double* const* Ms
     if (lane == 0) s_maxd = (kmax > 0) ? __longlong_as_double(kmax - 1) : 0.0;
   }
   __syncthreads();
-  for (int k = 0; k < n; ++k) {
-    if (tid == 0) {
-      double d = S[k + k * n];
-      const double floor_d = s_maxd * 1e-15 + 1e-300;
-      if (!(d > floor_d)) {
-        d = floor_d;
-        if (flag) *flag = 1;
-      }
-      const double r = rsqrt(d);
-      S[k + k * n] = d * r;  // sqrt(d)
-      s_rinv = r;
+  // The pivot's reciprocal square root (~430 cycles of dependent 1/64-rate FP64 instructions) is the
+  // serial part of each column.  It is pipelined: while warps 0..nw-2 apply column k to the trailing
+  // block, the last warp updates the next diagonal entry S(k+1, k+1) itself and computes its
+  // reciprocal square root, so the two overlap.  The arithmetic and its order are unchanged.
+  const double floor_d = s_maxd * 1e-15 + 1e-300;
+  auto pivot = [&](int k) {  // one thread: floor, reciprocal square root, L_kk = sqrt(d)
+    double d = S[k + k * n];
+    if (!(d > floor_d)) {
+      d = floor_d;
+      if (flag) *flag = 1;
     }
-    __syncthreads();
-    const double rinv = s_rinv;
+    const double r = rsqrt(d);
+    S[k + k * n] = d * r;
+    s_rinv2[k & 1] = r;
+  };
+  if (tid == 0 && n > 0) pivot(0);
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    const double rinv = s_rinv2[k & 1];
     for (int i = k + 1 + tid; i < n; i += nt) S[i + k * n] *= rinv;
     __syncthreads();
-    for (int j = k + 1 + warp; j < n; j += nw) {
-      const double ljk = S[j + k * n];
-      for (int i = j + lane; i < n; i += 32) S[i + j * n] = fma(-S[i + k * n], ljk, S[i + j * n]);
+    if (warp == nw - 1) {
+      if (lane == 0 && k + 1 < n) {
+        const double l = S[k + 1 + k * n];
+        S[k + 1 + (k + 1) * n] = fma(-l, l, S[k + 1 + (k + 1) * n]);
+        pivot(k + 1);
+      }
+    } else {
+      for (int j = k + 1 + warp; j < n; j += nw - 1) {
+        const double ljk = S[j + k * n];
+        for (int i = (j == k + 1 ? j + 1 : j) + lane; i < n; i += 32)
+          S[i + j * n] = fma(-S[i + k * n], ljk, S[i + j * n]);
+      }
     }
     __syncthreads();
   }
