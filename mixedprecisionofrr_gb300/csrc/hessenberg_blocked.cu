@@ -33,6 +33,7 @@ constexpr int HB_T = 256;    // threads per CTA of the in-block kernel
 constexpr int HB_UT = 128;   // threads per CTA of the block update
 constexpr int HB_CG = 2;     // block columns per CTA of the block update
 constexpr size_t HB_SMEM_MAX = 200 * 1024;
+constexpr int HBC_R = 8;  // block coefficients: entries per lane (c0 <= 256)
 
 // One MGS elimination v - r q in the compute type.  Exact mode: the product rounded, then the
 // difference (hessenberg.m's arithmetic, bit-identical to the per-column kernel).  FAST (FP64
@@ -46,6 +47,43 @@ template <bool FAST> __device__ __forceinline__ float elim(float v, float r, flo
 }
 __device__ __forceinline__ double mul_recip(double x, double y) { return __dmul_rn(x, y); }
 __device__ __forceinline__ float mul_recip(float x, float y) { return __fmul_rn(x, y); }
+
+// Forward substitution of one block column over the c0 pivot rows, by one warp with the column's
+// entries in registers (lane l holds entries l, l+32, .., NR of them): the coefficient of step j is a
+// shuffle from its owner, then every later entry is updated; the same roundings as the shared-memory
+// form (each update rounded to the storage type).
+template <int NR, class TO, class TC, bool FAST>
+__device__ __forceinline__ void blockcoef_subst(int c0, int n, int warp, int lane, const TO* x, const TO* s_L,
+                                                const int* s_sel, TC* r, double* R) {
+  TC xv[NR];
+  bool sv[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    const int jj = lane + 32 * q;
+    xv[q] = (jj < c0) ? to_c<TC, TO>(x[jj]) : TC(0);
+    sv[q] = (jj < c0) ? (s_sel[jj] != 0) : false;
+  }
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    for (int jl = 0; jl < 32; ++jl) {
+      const int j = 32 * q + jl;
+      if (j >= c0) break;
+      const bool selj = s_sel[j] != 0;
+      const TC rc = __shfl_sync(0xffffffffu, xv[q], jl);
+      if (lane == 0) {
+        r[j] = selj ? rc : TC(0);
+        R[j + (int64_t)(c0 + warp) * n] = selj ? to_c<double, TC>(rc) : 0.0;
+      }
+      if (!selj) continue;
+#pragma unroll
+      for (int w = q; w < NR; ++w) {
+        const int jj = lane + 32 * w;
+        if (jj > j && jj < c0 && sv[w])
+          xv[w] = to_c<TC, TO>(from_c<TO, TC>(elim<FAST>(xv[w], rc, to_c<TC, TO>(s_L[jj * c0 + j]))));
+      }
+    }
+  }
+}
 
 // ---- step 0: coefficients of the block columns against the final columns [0, c0) -----------------
 template <class TO, class TC, bool FAST>
@@ -65,18 +103,54 @@ __global__ void __launch_bounds__(HB_B * 32) k_hess_blockcoef(int n, int c0, int
     s_perm[j] = perm[j];
   }
   __syncthreads();
-  // pivot row jj of the final columns l < jj, and the (untouched) block columns at the pivot rows
-  for (int e = tid; e < c0 * c0; e += blockDim.x) {
-    const int jj = e / c0, l = e % c0;
-    if (l < jj) s_L[e] = s_sel[jj] ? Q[(int64_t)s_perm[jj] + (int64_t)l * ldq] : TO(0);
+  // pivot row jj of the final columns l < jj, and the (untouched) block columns at the pivot rows;
+  // the gathers issued eight per thread at a time
+  for (int e0 = tid; e0 < c0 * c0; e0 += 8 * blockDim.x) {
+    TO v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = e0 + u * blockDim.x;
+      const int jj = e / c0, l = e - jj * c0;
+      v[u] = (e < c0 * c0 && l < jj && s_sel[jj]) ? Q[(int64_t)s_perm[jj] + (int64_t)l * ldq] : TO(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = e0 + u * blockDim.x;
+      if (e < c0 * c0) s_L[e] = v[u];
+    }
   }
-  for (int e = tid; e < nb * c0; e += blockDim.x) {
-    const int t = e / c0, j = e % c0;
-    s_x[t * c0 + j] = s_sel[j] ? Q[(int64_t)s_perm[j] + (int64_t)(c0 + t) * ldq] : TO(0);
+  for (int e0 = tid; e0 < nb * c0; e0 += 8 * blockDim.x) {
+    TO v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = e0 + u * blockDim.x;
+      const int t = e / c0, j = e - t * c0;
+      v[u] = (e < nb * c0 && s_sel[j]) ? Q[(int64_t)s_perm[j] + (int64_t)(c0 + t) * ldq] : TO(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = e0 + u * blockDim.x;
+      if (e < nb * c0) s_x[e] = v[u];
+    }
   }
   __syncthreads();
   const int warp = tid >> 5, lane = tid & 31;
-  if (warp < nb) {
+  if (warp < nb && c0 <= 32 * HBC_R) {
+    const int nr = (c0 + 31) / 32;  // registers per lane actually used: predicated-off FP64 slots would
+                                    // still occupy the 1/64-rate pipe, so the width is a template
+    TO* x = s_x + warp * c0;
+    TC* r = rcoef + (size_t)warp * c0;
+    switch (nr) {
+      case 1: blockcoef_subst<1, TO, TC, FAST>(c0, n, warp, lane, x, s_L, s_sel, r, R); break;
+      case 2: blockcoef_subst<2, TO, TC, FAST>(c0, n, warp, lane, x, s_L, s_sel, r, R); break;
+      case 3: blockcoef_subst<3, TO, TC, FAST>(c0, n, warp, lane, x, s_L, s_sel, r, R); break;
+      case 4: blockcoef_subst<4, TO, TC, FAST>(c0, n, warp, lane, x, s_L, s_sel, r, R); break;
+      case 5: blockcoef_subst<5, TO, TC, FAST>(c0, n, warp, lane, x, s_L, s_sel, r, R); break;
+      case 6: blockcoef_subst<6, TO, TC, FAST>(c0, n, warp, lane, x, s_L, s_sel, r, R); break;
+      case 7: blockcoef_subst<7, TO, TC, FAST>(c0, n, warp, lane, x, s_L, s_sel, r, R); break;
+      default: blockcoef_subst<8, TO, TC, FAST>(c0, n, warp, lane, x, s_L, s_sel, r, R); break;
+    }
+  } else if (warp < nb) {
     TO* x = s_x + warp * c0;
     TC* r = rcoef + (size_t)warp * c0;
     for (int j = 0; j < c0; ++j) {

@@ -104,7 +104,9 @@ __global__ void __launch_bounds__(256) k_chol_f64(int n, const double* const* Ms
 // i the owner broadcasts x_i = x_i / L_ii (multiplied by the staged reciprocal) and every lane
 // updates its rows with one FMA each -- about three FP64 warp instructions per row (GB300's FP64 pipe
 // is 1/64 rate, so a shuffle-reduced dot product per row would cost several times more).
-constexpr int TRSM_R = 4;  // rows per lane: n <= 128
+// TRSM_R: rows per lane (n <= 32 TRSM_R), a template so that no predicated-off FP64 instruction
+// occupies the 1/64-rate pipe.
+template <int TRSM_R>
 __global__ void __launch_bounds__(128) k_trsm_f64(int n, int nrhs, const double* __restrict__ L, int ldl,
                                                   const double* __restrict__ B, int ldb, int transB,
                                                   double* __restrict__ X, int ldx, int upper) {
@@ -183,6 +185,51 @@ __global__ void __launch_bounds__(128) k_trsm_f64(int n, int nrhs, const double*
 // coalesced for op(A) = A) spread the FP64 work over many SMs; K is consumed in chunks of GS_K with all
 // of a chunk's loads issued before its FMAs, so a 64-deep product waits for two rounds of L2 latency.
 constexpr int GS_K = 32;
+struct GemmSmall {
+  int M, N, K;
+  double alpha;
+  const double* A;
+  int lda, tA;
+  const double* B;
+  int ldb, tB;
+  double beta;
+  double* C;
+  int ldc;
+};
+__device__ __forceinline__ void gemm_small_entry(const GemmSmall& g, int i, int j);
+
+// up to two independent products in one launch (blockIdx.z selects), so that the ones that do not
+// depend on each other share a launch
+__global__ void __launch_bounds__(32) k_gemm_small2_f64(GemmSmall g0, GemmSmall g1) {
+  const GemmSmall& g = blockIdx.z ? g1 : g0;
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y;
+  if (i >= g.M || j >= g.N) return;
+  gemm_small_entry(g, i, j);
+}
+
+__device__ __forceinline__ void gemm_small_entry(const GemmSmall& g, int i, int j) {
+  const int K = g.K, lda = g.lda, ldb = g.ldb, tA = g.tA, tB = g.tB;
+  const double* __restrict__ A = g.A;
+  const double* __restrict__ B = g.B;
+  double s0 = 0.0, s1 = 0.0;
+  for (int k0 = 0; k0 < K; k0 += GS_K) {
+    double a[GS_K], b[GS_K];
+#pragma unroll
+    for (int u = 0; u < GS_K; ++u) {
+      const int k = k0 + u;
+      a[u] = (k < K) ? (tA ? A[k + (size_t)i * lda] : A[i + (size_t)k * lda]) : 0.0;
+      b[u] = (k < K) ? (tB ? B[j + (size_t)k * ldb] : B[k + (size_t)j * ldb]) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < GS_K; u += 2) {
+      s0 = fma(a[u], b[u], s0);
+      s1 = fma(a[u + 1], b[u + 1], s1);
+    }
+  }
+  const double s = s0 + s1;
+  g.C[i + (size_t)j * g.ldc] = (g.beta == 0.0) ? g.alpha * s : fma(g.alpha, s, g.beta * g.C[i + (size_t)j * g.ldc]);
+}
+
 __global__ void __launch_bounds__(32) k_gemm_small_f64(int M, int N, int K, double alpha, const double* __restrict__ A,
                                                        int lda, int tA, const double* __restrict__ B, int ldb, int tB,
                                                        double beta, double* __restrict__ C, int ldc) {
@@ -560,13 +607,30 @@ static int gemm_small(ofrr_ctx* ctx, int M, int N, int K, double alpha, const do
   return OFRR_SUCCESS;
 }
 
-static int trsm(ofrr_ctx* ctx, int n, int nrhs, const double* L, const double* B, int ldb, int transB, double* X,
-                int upper) {
+static int gemm_small2(ofrr_ctx* ctx, const GemmSmall& g0, const GemmSmall& g1) {
+  const int M = std::max(g0.M, g1.M), N = std::max(g0.N, g1.N);
+  if (M <= 0 || N <= 0) return OFRR_SUCCESS;
+  k_gemm_small2_f64<<<dim3((unsigned)((M + 31) / 32), (unsigned)N, 2), 32, 0, ctx->stream>>>(g0, g1);
+  OFRR_LAUNCHED(ctx, "k_gemm_small2_f64");
+  return OFRR_SUCCESS;
+}
+
+template <int R>
+static int trsm_r(ofrr_ctx* ctx, int n, int nrhs, const double* L, const double* B, int ldb, int transB, double* X,
+                  int upper) {
   const size_t smem = ((size_t)n * (n + 1) + (size_t)n) * sizeof(double);
-  OFRR_TRY(allow_smem(k_trsm_f64));
-  k_trsm_f64<<<(nrhs + 3) / 4, 128, smem, ctx->stream>>>(n, nrhs, L, n, B, ldb, transB, X, n, upper);
+  OFRR_TRY(allow_smem(k_trsm_f64<R>));
+  k_trsm_f64<R><<<(nrhs + 3) / 4, 128, smem, ctx->stream>>>(n, nrhs, L, n, B, ldb, transB, X, n, upper);
   OFRR_LAUNCHED(ctx, "k_trsm_f64");
   return OFRR_SUCCESS;
+}
+
+static int trsm(ofrr_ctx* ctx, int n, int nrhs, const double* L, const double* B, int ldb, int transB, double* X,
+                int upper) {
+  if (n <= 32) return trsm_r<1>(ctx, n, nrhs, L, B, ldb, transB, X, upper);
+  if (n <= 64) return trsm_r<2>(ctx, n, nrhs, L, B, ldb, transB, X, upper);
+  if (n <= 96) return trsm_r<3>(ctx, n, nrhs, L, B, ldb, transB, X, upper);
+  return trsm_r<4>(ctx, n, nrhs, L, B, ldb, transB, X, upper);
 }
 
 static int chol(ofrr_ctx* ctx, int n, int count, const double* const* Ms_host, int ldm, double tau,
@@ -596,8 +660,8 @@ static int eig_refine(ofrr_ctx* ctx, int n, const double* C, double* W0, double*
   double* Wc = W0;
   double* Wn = W1;
   for (int it = 0; it < steps; ++it) {
-    OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, Wc, n, 0, 0.0, P, n));   // P = W'W
-    OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, C, n, 0, Wc, n, 0, 0.0, CW, n));   // CW
+    OFRR_TRY(gemm_small2(ctx, GemmSmall{n, n, n, 1.0, Wc, n, 1, Wc, n, 0, 0.0, P, n},     // P = W'W
+                         GemmSmall{n, n, n, 1.0, C, n, 0, Wc, n, 0, 0.0, CW, n}));     // CW
     OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, CW, n, 0, 0.0, T, n));   // T = W'CW
     k_oa_correction<<<(n * n + 255) / 256, 256, n * sizeof(double), ctx->stream>>>(n, P, T, l0, F, 1e-5);
     OFRR_LAUNCHED(ctx, "k_oa_correction");
@@ -605,8 +669,8 @@ static int eig_refine(ofrr_ctx* ctx, int n, const double* C, double* W0, double*
     std::swap(Wc, Wn);
   }
   // final Rayleigh quotients with the refined vectors
-  OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, Wc, n, 0, 0.0, P, n));
-  OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, C, n, 0, Wc, n, 0, 0.0, CW, n));
+  OFRR_TRY(gemm_small2(ctx, GemmSmall{n, n, n, 1.0, Wc, n, 1, Wc, n, 0, 0.0, P, n},
+                       GemmSmall{n, n, n, 1.0, C, n, 0, Wc, n, 0, 0.0, CW, n}));
   OFRR_TRY(gemm_small(ctx, n, n, n, 1.0, Wc, n, 1, CW, n, 0, 0.0, T, n));
   k_oa_correction<<<(n * n + 255) / 256, 256, n * sizeof(double), ctx->stream>>>(n, P, T, l0, F, 1e-5);
   OFRR_LAUNCHED(ctx, "k_oa_correction");
