@@ -91,6 +91,11 @@ struct Op {
   // Must be called in the solve's outermost workspace scope (the stacks live as long as the solve).
   SlicedOperand sA, sAt;
   bool have_sA = false, have_sAt = false;
+  // |A| in a 16-bit type in both K-contiguous orientations (absA[0] = |A'| for A X, absA[1] = |A| for
+  // A' X), for the bounds on the emulation error; made once per solve by prepare_abs
+  void* absA[2] = {nullptr, nullptr};
+  ofrr_dtype abs_t = OFRR_F16;
+  int prepare_abs(ofrr_ctx* ctx, ofrr_dtype t16);
   int prepare_sliced(ofrr_ctx* ctx) {
     if (A->kind != OFRR_OP_DENSE) return OFRR_SUCCESS;
     const double* A64;
@@ -388,19 +393,24 @@ int emulation_bounds(ofrr_ctx* ctx, Op& op, int trans, ofrr_dtype t16, const dou
   int64_t lda;
   if (trans) OFRR_TRY(op.dense_as(ctx, t16, &Ap, &lda));
   else OFRR_TRY(op.dense_t_as(ctx, t16, &Ap, &lda));
-  void* absA = ws_alloc(ctx, (size_t)K * M * 2, &st);
+  const bool cached = op.absA[trans] != nullptr && op.abs_t == t16;
+  void* absA = cached ? op.absA[trans] : ws_alloc(ctx, (size_t)K * M * 2, &st);
   void* absX = ws_alloc(ctx, (size_t)K * k * 2, &st);
   float* Bnd = ws_get<float>(ctx, (size_t)M * k, &st);
   if (!absA || !absX || !Bnd) return st;
   if (t16 == OFRR_F16) {
-    k_abs_cast<__half, __half><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(K, M, (const __half*)Ap, lda,
-                                                                             (__half*)absA, K);
-    OFRR_LAUNCHED(ctx, "k_abs_cast");
+    if (!cached) {
+      k_abs_cast<__half, __half><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(K, M, (const __half*)Ap, lda,
+                                                                               (__half*)absA, K);
+      OFRR_LAUNCHED(ctx, "k_abs_cast");
+    }
     k_abs_cast_f64<<<grid_2d(K, k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, (__half*)absX, nullptr, K);
   } else {
-    k_abs_cast<__nv_bfloat16, __nv_bfloat16><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(
-        K, M, (const __nv_bfloat16*)Ap, lda, (__nv_bfloat16*)absA, K);
-    OFRR_LAUNCHED(ctx, "k_abs_cast");
+    if (!cached) {
+      k_abs_cast<__nv_bfloat16, __nv_bfloat16><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(
+          K, M, (const __nv_bfloat16*)Ap, lda, (__nv_bfloat16*)absA, K);
+      OFRR_LAUNCHED(ctx, "k_abs_cast");
+    }
     k_abs_cast_f64<<<grid_2d(K, k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, nullptr, (__nv_bfloat16*)absX, K);
   }
   OFRR_LAUNCHED(ctx, "k_abs_cast_f64");
@@ -410,9 +420,37 @@ int emulation_bounds(ofrr_ctx* ctx, Op& op, int trans, ofrr_dtype t16, const dou
 }
 constexpr double kEmulBound = 1.01 * 1.16415321826934814453125e-10;  // 1.01 * 2^-33
 
+// |A| in t16 in both orientations, in the caller's (solve-lifetime) workspace scope
+int Op::prepare_abs(ofrr_ctx* ctx, ofrr_dtype t16) {
+  if (A->kind != OFRR_OP_DENSE || (t16 != OFRR_F16 && t16 != OFRR_BF16)) return OFRR_SUCCESS;
+  int st = OFRR_SUCCESS;
+  for (int trans = 0; trans < 2; ++trans) {
+    const int64_t M = trans ? n() : m(), K = trans ? m() : n();
+    const void* Ap;
+    int64_t lda;
+    if (trans) OFRR_TRY(dense_as(ctx, t16, &Ap, &lda));
+    else OFRR_TRY(dense_t_as(ctx, t16, &Ap, &lda));
+    void* w = ws_alloc(ctx, (size_t)K * M * 2, &st);
+    if (!w) return st;
+    if (t16 == OFRR_F16)
+      k_abs_cast<__half, __half><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(K, M, (const __half*)Ap, lda,
+                                                                               (__half*)w, K);
+    else
+      k_abs_cast<__nv_bfloat16, __nv_bfloat16><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(
+          K, M, (const __nv_bfloat16*)Ap, lda, (__nv_bfloat16*)w, K);
+    OFRR_LAUNCHED(ctx, "k_abs_cast");
+    absA[trans] = w;
+  }
+  abs_t = t16;
+  return OFRR_SUCCESS;
+}
+
 // FP64 residuals of Ritz pairs (X in type tx), normalised by normA and ||x||
+// certify16 >= 0: emulated products; the bound on their error is added, computed only when every
+// emulated residual is at most bounds_below
 int residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* X, int64_t ldx, int k, const double* lam_host,
-                  double normA, double* out_host, int certify16 = -1) {
+                  double normA, double* out_host, int certify16 = -1, double* emul_host = nullptr,
+                  double bounds_below = INFINITY) {
   if (k <= 0) return OFRR_SUCCESS;
   WsScope scope(ctx);
   const int64_t n = op.m();
@@ -428,14 +466,6 @@ int residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* X, int64_t l
   OFRR_TRY(residual_columns(ctx, n, k, AX, n, X64, n, lam, res));
   OFRR_TRY(column_norms(ctx, OFRR_F64, n, k, X64, n, nrm));
   std::vector<double> h(3 * k, 0.0);
-  double* bnd = nullptr;
-  if (certify16 >= 0) {  // emulated A X: add the bound on its error (unit columns)
-    OFRR_TRY(dmalloc(ctx, &bnd, (size_t)k));
-    k_normalize_cols<<<grid_cols(n, k), 256, 0, ctx->stream>>>(n, k, X64, nrm);
-    OFRR_LAUNCHED(ctx, "k_normalize_cols");
-    OFRR_TRY(emulation_bounds(ctx, op, 0, (ofrr_dtype)certify16, X64, n, k, bnd));
-    OFRR_CUDA(cudaMemcpyAsync(h.data() + 2 * k, bnd, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
-  }
   OFRR_CUDA(cudaMemcpyAsync(h.data(), res, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, ctx->stream));
   OFRR_TRY(sync_and_check(ctx));
   if (normA <= 0) {
@@ -443,8 +473,21 @@ int residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* X, int64_t l
     for (int j = 0; j < k; ++j) normA = std::max(normA, std::fabs(lam_host[j]));
     if (normA == 0) normA = 1;
   }
-  for (int j = 0; j < k; ++j)
+  double emax = 0;
+  for (int j = 0; j < k; ++j) emax = std::max(emax, (h[k + j] > 0) ? h[j] / (normA * h[k + j]) : INFINITY);
+  if (certify16 >= 0 && emax <= bounds_below) {  // emulated A X: the bound on its error (unit columns)
+    double* bnd = nullptr;
+    OFRR_TRY(dmalloc(ctx, &bnd, (size_t)k));
+    k_normalize_cols<<<grid_cols(n, k), 256, 0, ctx->stream>>>(n, k, X64, nrm);
+    OFRR_LAUNCHED(ctx, "k_normalize_cols");
+    OFRR_TRY(emulation_bounds(ctx, op, 0, (ofrr_dtype)certify16, X64, n, k, bnd));
+    OFRR_CUDA(cudaMemcpyAsync(h.data() + 2 * k, bnd, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+    OFRR_TRY(sync_and_check(ctx));
+  }
+  for (int j = 0; j < k; ++j) {
     out_host[j] = (h[k + j] > 0) ? h[j] / (normA * h[k + j]) + kEmulBound * h[2 * k + j] / normA : INFINITY;
+    if (emul_host) emul_host[j] = (h[k + j] > 0) ? h[j] / (normA * h[k + j]) : INFINITY;
+  }
   return OFRR_SUCCESS;
 }
 
@@ -705,8 +748,11 @@ __global__ void k_normalize_cols(int64_t m, int64_t n, double* X, const double* 
   }
 }
 
+// certify16 >= 0: emulated products; the bounds on their errors are added to the residuals, computed
+// only when every emulated residual is at most bounds_below (they decide nothing otherwise)
 int svd_residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* U, int64_t ldu, const void* V, int64_t ldv,
-                      int k, const double* s_host, double normA, double* out_host, int certify16 = -1) {
+                      int k, const double* s_host, double normA, double* out_host, int certify16 = -1,
+                      double* emul_host = nullptr, double bounds_below = INFINITY) {
   if (k <= 0) return OFRR_SUCCESS;
   WsScope scope(ctx);
   const int64_t m = op.m(), n = op.n();
@@ -738,13 +784,6 @@ int svd_residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* U, int64
     OFRR_LAUNCHED(ctx, "k_rescol2");
   }
   std::vector<double> h(4 * k, 0.0);
-  if (certify16 >= 0) {  // emulated A v and A' u: add the bounds on their errors (unit columns)
-    double* bnd;
-    OFRR_TRY(dmalloc(ctx, &bnd, (size_t)2 * k));
-    OFRR_TRY(emulation_bounds(ctx, op, 0, (ofrr_dtype)certify16, V64, n, k, bnd));
-    OFRR_TRY(emulation_bounds(ctx, op, 1, (ofrr_dtype)certify16, U64, m, k, bnd + k));
-    OFRR_CUDA(cudaMemcpyAsync(h.data() + 2 * k, bnd, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, ctx->stream));
-  }
   OFRR_CUDA(cudaMemcpyAsync(h.data(), nr + 2 * k, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, ctx->stream));
   OFRR_TRY(sync_and_check(ctx));
   if (normA <= 0) {
@@ -752,8 +791,20 @@ int svd_residuals_dev(ofrr_ctx* ctx, Op& op, ofrr_dtype tx, const void* U, int64
     for (int j = 0; j < k; ++j) normA = std::max(normA, std::fabs(s_host[j]));
     if (normA == 0) normA = 1;
   }
-  for (int j = 0; j < k; ++j)
+  double emax = 0;
+  for (int j = 0; j < k; ++j) emax = std::max(emax, std::max(h[j], h[k + j]) / normA);
+  if (certify16 >= 0 && emax <= bounds_below) {  // emulated A v and A' u: the bounds on their errors
+    double* bnd;
+    OFRR_TRY(dmalloc(ctx, &bnd, (size_t)2 * k));
+    OFRR_TRY(emulation_bounds(ctx, op, 0, (ofrr_dtype)certify16, V64, n, k, bnd));
+    OFRR_TRY(emulation_bounds(ctx, op, 1, (ofrr_dtype)certify16, U64, m, k, bnd + k));
+    OFRR_CUDA(cudaMemcpyAsync(h.data() + 2 * k, bnd, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, ctx->stream));
+    OFRR_TRY(sync_and_check(ctx));
+  }
+  for (int j = 0; j < k; ++j) {
     out_host[j] = std::max(h[j] + kEmulBound * h[2 * k + j], h[k + j] + kEmulBound * h[3 * k + j]) / normA;
+    if (emul_host) emul_host[j] = std::max(h[j], h[k + j]) / normA;
+  }
   return OFRR_SUCCESS;
 }
 
@@ -808,12 +859,6 @@ int residuals_subset(ofrr_ctx* ctx, Op& op, const double* X, int64_t ldx, const 
   return OFRR_SUCCESS;
 }
 
-std::vector<int> failing(const std::vector<double>& res, int k, double tol) {
-  std::vector<int> J;
-  for (int j = 0; j < k; ++j)
-    if (!(res[j] <= tol)) J.push_back(j);
-  return J;
-}
 
 }  // namespace
 }  // namespace ofrr
@@ -1034,7 +1079,7 @@ bool stagnated(PhaseState& S, int nev, double stag_tol, int iters_in_phase) {
 // Exits after maxit iterations, when the nev residuals reach tol (checked every check_every) or,
 // if stag_tol > 0, when the Ritz values stop improving.
 int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* opt, void* V, int64_t ldv, int maxit,
-              double tol, int nev, double stag_tol, PhaseState& S, double* d_dev) {
+              double tol, int nev, double stag_tol, PhaseState& S, double* d_dev, int certify16 = -1) {
   WsScope scope(ctx);
   int st = OFRR_SUCCESS;
   const int64_t n = op.m();
@@ -1101,7 +1146,31 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
       OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d_dev, sizeof(double) * b, cudaMemcpyDeviceToHost, ctx->stream));
       OFRR_TRY(sync_and_check(ctx));
     }
-    if (check) {
+    if (check && certify16 >= 0) {
+      // certified check (emulated products), as in svd_phase
+      std::vector<double> emul(kk);
+      OFRR_TRY(residuals_dev(ctx, op, P.po, cur, ldcur, kk, S.d.data(), -1.0, S.res.data(), certify16, emul.data(),
+                             tol));
+      std::vector<int> J;
+      bool hopeless = false;
+      for (int j = 0; j < kk; ++j)
+        if (!(S.res[j] <= tol)) {
+          if (emul[j] <= tol) J.push_back(j);
+          else hopeless = true;
+        }
+      if (!hopeless && !J.empty()) {
+        TraceScope tsc(ctx, "certify.fp64");
+        const bool em = ctx->emulate_f64;
+        ctx->emulate_f64 = false;
+        const int st2 = residuals_subset(ctx, op, (const double*)cur, ldcur, J, S.d.data(),
+                                         norm_of_values(S.d.data(), kk), S.res.data());
+        ctx->emulate_f64 = em;
+        OFRR_TRY(st2);
+      }
+      S.converged = 0;
+      for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= tol) ? 1 : 0;
+      if (S.converged >= kk) S.done = true;
+    } else if (check) {
       OFRR_TRY(residuals_dev(ctx, op, P.po, cur, ldcur, kk, S.d.data(), -1.0, S.res.data()));
       S.converged = 0;
       for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= tol) ? 1 : 0;
@@ -1116,7 +1185,8 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
 
 // One phase of subspace_iter_svd.m:60-75 on U (m x b) and V (n x b), type P.po.
 int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* opt, void* U, int64_t ldu, void* V,
-              int64_t ldv, int maxit, double tol, int nev, double stag_tol, PhaseState& S, double* d_dev) {
+              int64_t ldv, int maxit, double tol, int nev, double stag_tol, PhaseState& S, double* d_dev,
+              int certify16 = -1) {
   WsScope scope(ctx);
   int st = OFRR_SUCCESS;
   const int64_t m = op.m(), n = op.n();
@@ -1215,7 +1285,32 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
       OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d_dev, sizeof(double) * b, cudaMemcpyDeviceToHost, ctx->stream));
       OFRR_TRY(sync_and_check(ctx));
     }
-    if (check) {
+    if (check && certify16 >= 0) {
+      // certified check (emulated products): the emulated residuals plus the bounds on the emulation
+      // errors must meet tol; columns that miss only by the bound get a true FP64 residual instead
+      std::vector<double> emul(kk);
+      OFRR_TRY(svd_residuals_dev(ctx, op, P.po, U, ldu, V, ldv, kk, S.d.data(), -1.0, S.res.data(), certify16,
+                                 emul.data(), tol));
+      std::vector<int> J;
+      bool hopeless = false;
+      for (int j = 0; j < kk; ++j)
+        if (!(S.res[j] <= tol)) {
+          if (emul[j] <= tol) J.push_back(j);
+          else hopeless = true;
+        }
+      if (!hopeless && !J.empty()) {
+        TraceScope tsc(ctx, "certify.fp64");
+        const bool em = ctx->emulate_f64;
+        ctx->emulate_f64 = false;
+        const int st2 = svd_residuals_subset(ctx, op, (const double*)U, ldu, (const double*)V, ldv, J, S.d.data(),
+                                             norm_of_values(S.d.data(), kk), S.res.data());
+        ctx->emulate_f64 = em;
+        OFRR_TRY(st2);
+      }
+      S.converged = 0;
+      for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= tol) ? 1 : 0;
+      if (S.converged >= kk) S.done = true;
+    } else if (check) {
       OFRR_TRY(svd_residuals_dev(ctx, op, P.po, U, ldu, V, ldv, kk, S.d.data(), -1.0, S.res.data()));
       S.converged = 0;
       for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= tol) ? 1 : 0;
@@ -1311,32 +1406,18 @@ static int si_eig_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
     escalations = 1;
     if (!S.done && S.it < opt->maxiter) {
       // refinement: FP64-accurate products from exact BF16 slices on the tensor cores
-      OFRR_TRY(op.prepare_sliced(ctx));
-      ctx->emulate_f64 = op.A->kind == OFRR_OP_DENSE;
-      st = eig_phase(ctx, op, all_f64(), opt, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d);
+      const bool dense = op.A->kind == OFRR_OP_DENSE;
+      {
+        TraceScope ts(ctx, "prepare.f64");
+        OFRR_TRY(op.prepare_sliced(ctx));
+        if (dense) OFRR_TRY(op.prepare_abs(ctx, L.po));
+      }
+      // certified checks in the FP64 phase (see si_svd)
+      ctx->emulate_f64 = dense;
+      st = eig_phase(ctx, op, all_f64(), opt, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d,
+                     dense ? (int)L.po : -1);
       ctx->emulate_f64 = false;
       OFRR_TRY(st);
-      if (S.done && op.A->kind == OFRR_OP_DENSE) {
-        // certify: the emulated residuals plus the bound on the emulation error must meet tol;
-        // otherwise the residuals of the columns that miss it are recomputed with true FP64 products
-        TraceScope ts(ctx, "certify");
-        OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d, sizeof(double) * S.b, cudaMemcpyDeviceToHost, ctx->stream));
-        OFRR_TRY(sync_and_check(ctx));
-        const int kk = std::min(nev, S.b);
-        ctx->emulate_f64 = true;
-        st = residuals_dev(ctx, op, OFRR_F64, V, ldv, kk, S.d.data(), -1.0, S.res.data(), (int)L.po);
-        ctx->emulate_f64 = false;
-        OFRR_TRY(st);
-        S.converged = 0;
-        for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
-        if (S.converged < kk) {
-          OFRR_TRY(residuals_subset(ctx, op, (const double*)V, ldv, failing(S.res, kk, opt->tol), S.d.data(),
-                                    norm_of_values(S.d.data(), kk), S.res.data()));
-          S.converged = 0;
-          for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
-        }
-        S.done = S.converged >= kk;
-      }
     }
   } else {
     const Precisions P = precisions_of(opt);
@@ -1417,36 +1498,19 @@ static int si_svd_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
     escalations = 1;
     if (!S.done && S.it < opt->maxiter) {
       // refinement: FP64-accurate products from exact BF16 slices on the tensor cores
+      const bool dense = op.A->kind == OFRR_OP_DENSE;
       {
         TraceScope ts(ctx, "prepare.f64");
         OFRR_TRY(op.prepare_sliced(ctx));
+        if (dense) OFRR_TRY(op.prepare_abs(ctx, L.po));
       }
-      ctx->emulate_f64 = op.A->kind == OFRR_OP_DENSE;
-      st = svd_phase(ctx, op, all_f64(), opt, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d);
+      // the FP64 phase's checks are certified (emulated residuals plus the bounds on the emulation
+      // errors, true FP64 residuals for the columns that miss only by the bound)
+      ctx->emulate_f64 = dense;
+      st = svd_phase(ctx, op, all_f64(), opt, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d,
+                     dense ? (int)L.po : -1);
       ctx->emulate_f64 = false;
       OFRR_TRY(st);
-      if (S.done && op.A->kind == OFRR_OP_DENSE) {
-        // certify: the emulated residuals plus the bounds on the emulation errors must meet tol;
-        // otherwise the residuals of the columns that miss it are recomputed with true FP64 products
-        TraceScope ts(ctx, "certify");
-        OFRR_CUDA(cudaMemcpyAsync(S.d.data(), d, sizeof(double) * S.b, cudaMemcpyDeviceToHost, ctx->stream));
-        OFRR_TRY(sync_and_check(ctx));
-        const int kk = std::min(nev, S.b);
-        ctx->emulate_f64 = true;
-        st = svd_residuals_dev(ctx, op, OFRR_F64, U, ldu, V, ldv, kk, S.d.data(), -1.0, S.res.data(), (int)L.po);
-        ctx->emulate_f64 = false;
-        OFRR_TRY(st);
-        S.converged = 0;
-        for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
-        if (S.converged < kk) {
-          OFRR_TRY(svd_residuals_subset(ctx, op, (const double*)U, ldu, (const double*)V, ldv,
-                                        failing(S.res, kk, opt->tol), S.d.data(), norm_of_values(S.d.data(), kk),
-                                        S.res.data()));
-          S.converged = 0;
-          for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= opt->tol) ? 1 : 0;
-        }
-        S.done = S.converged >= kk;
-      }
     }
   } else {
     const Precisions P = precisions_of(opt);
