@@ -29,7 +29,7 @@ namespace cg = cooperative_groups;
 namespace ofrr {
 
 constexpr int HB_B = 16;     // block width (columns)
-constexpr int HB_T = 256;    // threads per CTA of the in-block kernel
+constexpr int HB_T = 512;    // threads per CTA of the in-block kernel (one row per thread at 8192 rows)
 constexpr int HB_UT = 128;   // threads per CTA of the block update
 constexpr int HB_CG = 2;     // block columns per CTA of the block update
 constexpr size_t HB_SMEM_MAX = 200 * 1024;
