@@ -107,9 +107,15 @@ __global__ void __launch_bounds__(256) k_chol_f64(int n, const double* const* Ms
 // TRSM_R: rows per lane (n <= 32 TRSM_R), a template so that no predicated-off FP64 instruction
 // occupies the 1/64-rate pipe.
 template <int TRSM_R>
-__global__ void __launch_bounds__(128) k_trsm_f64(int n, int nrhs, const double* __restrict__ L, int ldl,
-                                                  const double* __restrict__ B, int ldb, int transB,
-                                                  double* __restrict__ X, int ldx, int upper) {
+// blockIdx.y selects one of up to two independent systems (L, B, X), (L2, B2, X2) of the same shape
+__global__ void __launch_bounds__(128) k_trsm_f64(int n, int nrhs, const double* __restrict__ L1, int ldl,
+                                                  const double* __restrict__ B1, int ldb, int transB,
+                                                  double* __restrict__ X1, int ldx, int upper,
+                                                  const double* __restrict__ L2, const double* __restrict__ B2,
+                                                  double* __restrict__ X2) {
+  const double* __restrict__ L = blockIdx.y ? L2 : L1;
+  const double* __restrict__ B = blockIdx.y ? B2 : B1;
+  double* __restrict__ X = blockIdx.y ? X2 : X1;
   extern __shared__ double sm_trsm[];  // L (n x n, padded ld n+1), then the n diagonal reciprocals
   const int ld = n + 1;
   double* Ls = sm_trsm;
@@ -617,20 +623,22 @@ static int gemm_small2(ofrr_ctx* ctx, const GemmSmall& g0, const GemmSmall& g1) 
 
 template <int R>
 static int trsm_r(ofrr_ctx* ctx, int n, int nrhs, const double* L, const double* B, int ldb, int transB, double* X,
-                  int upper) {
+                  int upper, const double* L2, const double* B2, double* X2) {
   const size_t smem = ((size_t)n * (n + 1) + (size_t)n) * sizeof(double);
   OFRR_TRY(allow_smem(k_trsm_f64<R>));
-  k_trsm_f64<R><<<(nrhs + 3) / 4, 128, smem, ctx->stream>>>(n, nrhs, L, n, B, ldb, transB, X, n, upper);
+  const dim3 grid((unsigned)((nrhs + 3) / 4), L2 ? 2u : 1u);
+  k_trsm_f64<R><<<grid, 128, smem, ctx->stream>>>(n, nrhs, L, n, B, ldb, transB, X, n, upper, L2, B2, X2);
   OFRR_LAUNCHED(ctx, "k_trsm_f64");
   return OFRR_SUCCESS;
 }
 
+// X = L^-1 B (upper == 0) or L^-T B (upper == 1); with L2 set, X2 = (same op of L2) B2 in the same launch
 static int trsm(ofrr_ctx* ctx, int n, int nrhs, const double* L, const double* B, int ldb, int transB, double* X,
-                int upper) {
-  if (n <= 32) return trsm_r<1>(ctx, n, nrhs, L, B, ldb, transB, X, upper);
-  if (n <= 64) return trsm_r<2>(ctx, n, nrhs, L, B, ldb, transB, X, upper);
-  if (n <= 96) return trsm_r<3>(ctx, n, nrhs, L, B, ldb, transB, X, upper);
-  return trsm_r<4>(ctx, n, nrhs, L, B, ldb, transB, X, upper);
+                int upper, const double* L2 = nullptr, const double* B2 = nullptr, double* X2 = nullptr) {
+  if (n <= 32) return trsm_r<1>(ctx, n, nrhs, L, B, ldb, transB, X, upper, L2, B2, X2);
+  if (n <= 64) return trsm_r<2>(ctx, n, nrhs, L, B, ldb, transB, X, upper, L2, B2, X2);
+  if (n <= 96) return trsm_r<3>(ctx, n, nrhs, L, B, ldb, transB, X, upper, L2, B2, X2);
+  return trsm_r<4>(ctx, n, nrhs, L, B, ldb, transB, X, upper, L2, B2, X2);
 }
 
 static int chol(ofrr_ctx* ctx, int n, int count, const double* const* Ms_host, int ldm, double tau,
@@ -806,8 +814,7 @@ int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const dou
   OFRR_TRY(gemm_small(ctx, b, b, b, 1.0, C, b, 1, X, b, 0, 0.0, CX, b));  // (true C) X
   k_svd_left<<<(b * b + 255) / 256, 256, 0, ctx->stream>>>(b, CX, lam, Y, sigma);
   OFRR_LAUNCHED(ctx, "k_svd_left");
-  OFRR_TRY(trsm(ctx, b, b, Lu, Y, b, 0, Zf, 1));  // Zf = Lu^-T Y
-  OFRR_TRY(trsm(ctx, b, b, Lv, X, b, 0, Wf, 1));  // Wf = Lv^-T X
+  OFRR_TRY(trsm(ctx, b, b, Lu, Y, b, 0, Zf, 1, Lv, X, Wf));  // Zf = Lu^-T Y, Wf = Lv^-T X (one launch)
   return OFRR_SUCCESS;
 }
 
