@@ -197,3 +197,32 @@ def test_si_svd_geometric_converges_fp64(api, orc):
     assert np.allclose(sg[:16], s[:16], rtol=1e-9)
     r = orc.svd_residual_norms(A, api.to_numpy(Ug)[:, :16], sg[:16], api.to_numpy(Vg)[:, :16])
     assert np.max(r) < 1e-8
+
+
+def test_si_svd_mixed_dense_certified(api, orc):
+    """The benchmark path at a quarter of its size: dense 4096 x 1024 geometric-spectrum SVD, mixed
+    mode (16-bit bases, then FP64 emulated on the tensor cores with certified checks), tol 1e-8.
+    The singular values match the truth, the true FP64 residuals (NumPy) meet tol, and every reported
+    residual bounds the true one (the certification is an upper bound, never an estimate below)."""
+    A, U, s, V = orc.dense_svd_problem(4096, 1024, seed=7, smin=1e-6)
+    Ug, sg, Vg, info = api.subspace_iter_svd(A, 4096, 1024, 64, "single", "half", maxiter=80, step_size=6,
+                                             mode="mixed", tol=1e-8, nev=16, check_every=1, generalized_tol=0.0)
+    assert info.status == 0, info
+    assert np.allclose(sg[:16], s[:16], rtol=1e-9)
+    r = orc.svd_residual_norms(A, api.to_numpy(Ug)[:, :16], sg[:16], api.to_numpy(Vg)[:, :16])
+    assert np.max(r) <= 1e-8
+    assert np.all(r <= info.residuals[:16] * (1 + 1e-6) + 1e-15)
+
+
+def test_si_eig_mixed_dense_certified(api, orc):
+    """Dense symmetric 2048 x 2048 (Haar Q, log-uniform spectrum), mixed mode, tol 1e-8: eigenvalues,
+    true FP64 residuals and the certified residuals as an upper bound."""
+    A, lam = orc.dense_sym_problem(2048, seed=11)
+    Vg, d, info = api.subspace_iter_eig(A, 2048, 48, "single", "half", maxiter=200, step_size=6, mode="mixed",
+                                       tol=1e-8, nev=8, check_every=1, symmetric=True)
+    assert info.status == 0, info
+    assert np.allclose(d[:8], lam[:8], rtol=1e-9)
+    X = api.to_numpy(Vg)[:, :8]
+    r = orc.residual_norms(A, X, d[:8], normA=float(np.max(np.abs(d[:8]))))
+    assert np.max(r) <= 1e-8
+    assert np.all(r <= info.residuals[:8] * (1 + 1e-6) + 1e-15)
