@@ -348,6 +348,16 @@ int ofrr_ctx_trim(ofrr_ctx* ctx);
  * usable.  No fault, trap or unbounded wait is involved. */
 int ofrr_debug_bounded_wait(ofrr_ctx* ctx, int64_t timeout_ns);
 
+/* Self-test of the fused scale-and-split kernels of the emulated FP64 power iteration (no reference
+ * counterpart; the power loop of subspace_iter_svd.m:63-69, scalecols.m after each product).
+ * mode 0: X (M x N, M <= 8192) is scaled in place as ofrr_scalecols does (FP64, reciprocal multiply);
+ * mode 1: X = A' B (A: K x M, B: K x N, FP64) by the exact-slice product, its partial sums combined
+ * inside the scaling kernel, then scaled likewise; mode 2: X is left as it is.  Every mode writes the
+ * digit stack of the resulting X (N columns of 5 x roundup(M, 64) BF16 digits, device) and the N
+ * column exponents (device ints). */
+int ofrr_debug_scale_slice(ofrr_ctx* ctx, int mode, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda,
+                           const double* B, int64_t ldb, double* X, int64_t ldx, void* digits, int* expo);
+
 /* Per-solve tracing: with a path set, every si_eig / si_svd / arnoldi_eig solve on this context appends
  * one JSON line to that file (solver, sizes, status, iterations, residual, kernel launches, total and
  * per-phase device time from CUDA events on the context's stream).  NULL or "" turns it off.  A context

@@ -465,6 +465,8 @@ int scalecols_sliced(ofrr_ctx* ctx, int64_t m, int64_t n, double* U, int64_t ldu
                      SlicedOperand* out);
 // C (M x N) = A_op' B with both operands already split (B.K == A.K, N = B.M)
 int sliced_gemm_tn_pre(ofrr_ctx* ctx, const SlicedOperand& A, const SlicedOperand& B, double* C, int64_t ldc);
+int sliced_gemm_scalecols_pre(ofrr_ctx* ctx, const SlicedOperand& A, const SlicedOperand& B, double* U, int64_t ldu,
+                              bool write_u, __nv_bfloat16* stack, int* expo, SlicedOperand* out);
 int sliced_gemm_tn(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const double* B, int64_t ldb, double* C,
                    int64_t ldc);
 

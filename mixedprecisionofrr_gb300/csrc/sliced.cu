@@ -16,6 +16,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 namespace ofrr {
@@ -180,72 +182,163 @@ __global__ void __launch_bounds__(T) k_slice_cols(int64_t K, int64_t Kp, int64_t
 }
 
 // scalecols (FP64, FAST: reciprocal multiply, pivot exactly 1) fused with the digit split of the
-// scaled column, for columns of at most 8 T rows: one CTA per column keeps the column in registers,
-// finds the pivot (integer argmax keys, lowest row on ties), scales, writes the FP64 column, takes
-// the scaled column's maximum on the bit patterns and writes its digits -- the operand of the next
-// exact-slice product, without reading the column again.
-constexpr int SCS_U = 8;
-template <int T>
-__global__ void __launch_bounds__(T) k_scalecols_slice(int64_t m, int64_t Kp, double* __restrict__ U, int64_t ldu,
-                                                       __nv_bfloat16* __restrict__ stack, int* __restrict__ expo) {
-  __shared__ ArgMaxK red[T / 32];
-  __shared__ unsigned long long redm[T / 32];
+// scaled column, for columns of at most SCS_T U CL rows: a cluster of CL CTAs per column keeps the
+// column in registers (CTA r holds rows [r SCS_T U, (r + 1) SCS_T U)), finds the pivot (integer
+// argmax keys, lowest row on ties), scales, writes the FP64 column, takes the scaled column's maximum
+// on the bit patterns and writes its digits -- the operand of the next exact-slice product, without
+// reading the column again.  With CL = 2 the CTAs exchange their pivot candidates and maxima through
+// distributed shared memory; the result is the same as one CTA over the whole column.
+constexpr int SCS_T = 1024;
+
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// shared-memory address of this CTA's variable p in CTA `rank` of the cluster
+__device__ __forceinline__ unsigned cluster_map(const void* p, unsigned rank) {
+  unsigned a = (unsigned)__cvta_generic_to_shared(p), r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_cluster_u64(unsigned addr, unsigned long long v) {
+  asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+
+// Body shared by k_scalecols_slice and k_finish_scalecols_slice: v[u] holds row r0 + threadIdx.x +
+// u SCS_T of column n (0 beyond m), r0 = this CTA's first row.  col != nullptr also stores the scaled
+// column there.  For CL > 1 the caller has done cluster_arrive_relaxed() once on entry.
+template <int U, int CL>
+__device__ __forceinline__ void scalecols_slice_body(int64_t m, int64_t Kp, int n, int64_t r0, double (&v)[U],
+                                                     double* __restrict__ col, __nv_bfloat16* __restrict__ stack,
+                                                     int* __restrict__ expo) {
+  __shared__ ArgMaxK red[SCS_T / 32];
+  __shared__ unsigned long long redm[SCS_T / 32];
   __shared__ double s_t, s_y;
+  __shared__ long long s_k;
   __shared__ bool s_pf;
-  const int n = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double* col = U + (int64_t)n * ldu;
-  double v[SCS_U];
+  __shared__ unsigned long long s_ckey[CL], s_crow[CL], s_cval[CL], s_cmax[CL];  // filled by the cluster
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   ArgMaxK a{-1, 0x7fffffffffffffffLL};
 #pragma unroll
-  for (int u = 0; u < SCS_U; ++u) {
-    const int64_t i = threadIdx.x + (int64_t)u * T;
-    v[u] = (i < m) ? col[i] : 0.0;
-  }
-#pragma unroll
-  for (int u = 0; u < SCS_U; ++u) {
-    const int64_t i = threadIdx.x + (int64_t)u * T;
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * SCS_T;
     if (i < m) {
       const long long key = amax_key(v[u]);
       if (key > a.key) a = ArgMaxK{key, i};  // per-thread rows ascend: strict > keeps the lowest
     }
   }
   const ArgMaxK r = block_argmaxk(a, red);
-  const int64_t k = (r.key < 0) ? 0 : r.i;
-  if (threadIdx.x == 0) {
-    s_t = (m > 0) ? col[k] : 0.0;
-    s_y = (s_t != 0.0) ? pivot_recip(s_t) : 0.0;  // once per column (1/64-rate FP64 pipe)
-    s_pf = pivot_fast(s_t);
+  // the owner of this CTA's candidate row publishes its value (every column has a row 0, so the
+  // first CTA always has a candidate)
+  if (r.key >= 0 && threadIdx.x == (int)((r.i - r0) % SCS_T)) {
+    const int ku = (int)((r.i - r0) / SCS_T);
+    double pv = 0.0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) pv = (u == ku) ? v[u] : pv;
+    if (CL == 1) {
+      s_t = pv;
+      s_k = r.i;
+      s_y = (pv != 0.0) ? pivot_recip(pv) : 0.0;  // once per column (1/64-rate FP64 pipe)
+      s_pf = pivot_fast(pv);
+    } else {
+      s_t = pv;
+    }
+  }
+  if (CL > 1) {
+    __syncthreads();
+    cluster_wait();  // every CTA of the cluster has started: its shared memory may be written
+    const unsigned me = cluster_rank();
+    if (threadIdx.x < CL) {
+      st_cluster_u64(cluster_map(&s_ckey[me], threadIdx.x), (unsigned long long)r.key);
+      st_cluster_u64(cluster_map(&s_crow[me], threadIdx.x), (unsigned long long)r.i);
+      st_cluster_u64(cluster_map(&s_cval[me], threadIdx.x),
+                     (unsigned long long)__double_as_longlong(r.key >= 0 ? s_t : 0.0));
+    }
+    cluster_arrive();
+    cluster_wait();
+    if (threadIdx.x == 0) {
+      ArgMaxK g{-1, 0x7fffffffffffffffLL};
+      double gv = 0.0;
+#pragma unroll
+      for (int q = 0; q < CL; ++q) {  // in row order: max key, lowest row on ties
+        const ArgMaxK c{(long long)s_ckey[q], (long long)s_crow[q]};
+        const ArgMaxK p = argmaxk_pick(g, c);
+        if (p.key != g.key || p.i != g.i) gv = __longlong_as_double((long long)s_cval[q]);
+        g = p;
+      }
+      s_t = gv;
+      s_k = g.i;
+      s_y = (gv != 0.0) ? pivot_recip(gv) : 0.0;
+      s_pf = pivot_fast(gv);
+    }
   }
   __syncthreads();
   const double t = s_t;
+  const int64_t k = s_k;
   if (t != 0.0) {
     const double y = s_y;
     const bool pf = s_pf;
 #pragma unroll
-    for (int u = 0; u < SCS_U; ++u) {
-      const int64_t i = threadIdx.x + (int64_t)u * T;
-      if (i < m) {
-        v[u] = scale_by<double, true>(v[u], t, y, pf, i == k);
-        col[i] = v[u];
-      }
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = r0 + threadIdx.x + (int64_t)u * SCS_T;
+      if (i < m) v[u] = scale_by<double, true>(v[u], t, y, pf, i == k);
+    }
+  }
+  if (col) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = r0 + threadIdx.x + (int64_t)u * SCS_T;
+      if (i < m) col[i] = v[u];
     }
   }
   unsigned long long mx = 0;
 #pragma unroll
-  for (int u = 0; u < SCS_U; ++u) mx = max(mx, (unsigned long long)__double_as_longlong(v[u]) & 0x7fffffffffffffffull);
+  for (int u = 0; u < U; ++u) mx = max(mx, (unsigned long long)__double_as_longlong(v[u]) & 0x7fffffffffffffffull);
   for (int o = 16; o > 0; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, mx, o));
   if (lane == 0) redm[wid] = mx;
   __syncthreads();
 #pragma unroll
-  for (int w = 0; w < T / 32; ++w) mx = max(mx, redm[w]);
+  for (int w = 0; w < SCS_T / 32; ++w) mx = max(mx, redm[w]);
+  if (CL > 1) {
+    const unsigned me = cluster_rank();
+    if (threadIdx.x < CL) st_cluster_u64(cluster_map(&s_cmax[me], threadIdx.x), mx);
+    cluster_arrive();
+    cluster_wait();  // the last access to another CTA's shared memory is before this barrier
+#pragma unroll
+    for (int q = 0; q < CL; ++q) mx = max(mx, s_cmax[q]);
+  }
   const int e = colmax_expo(mx);
-  if (threadIdx.x == 0) expo[n] = e;
+  if (threadIdx.x == 0 && r0 == 0) expo[n] = e;
   __nv_bfloat16* dst = stack + (size_t)n * S * Kp;
 #pragma unroll
-  for (int u = 0; u < SCS_U; ++u) {
-    const int64_t i = threadIdx.x + (int64_t)u * T;
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * SCS_T;
     if (i < Kp) slice_store((unsigned long long)__double_as_longlong(v[u]), e, dst, Kp, i);
   }
+}
+
+// CL CTAs per column (a cluster of CL along x): column blockIdx.x / CL, rows from (blockIdx.x % CL) SCS_T U
+template <int U, int CL>
+__global__ void __launch_bounds__(SCS_T) k_scalecols_slice(int64_t m, int64_t Kp, double* __restrict__ X,
+                                                           int64_t ldx, __nv_bfloat16* __restrict__ stack,
+                                                           int* __restrict__ expo) {
+  if (CL > 1) cluster_arrive_relaxed();
+  const int n = blockIdx.x / CL;
+  const int64_t r0 = (int64_t)(blockIdx.x % CL) * SCS_T * U;
+  double* col = X + (int64_t)n * ldx;
+  double v[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * SCS_T;
+    v[u] = (i < m) ? col[i] : 0.0;
+  }
+  scalecols_slice_body<U, CL>(m, Kp, n, r0, v, col, stack, expo);
 }
 
 // Fused exact-slice product.  One CTA owns a 128 x SBN tile of C and a range of at most 16 k-blocks
@@ -469,6 +562,42 @@ __global__ void k_sliced_finish(int64_t M, int64_t N, int splits, const long lon
   }
 }
 
+// k_sliced_finish fused with k_scalecols_slice for a product C (m x N) that is only needed scaled and
+// split: each CTA sums the int64 partials of its rows (same values as k_sliced_finish), then scales
+// and splits them.  WRITE_U also stores the scaled FP64 column.
+template <int U, int CL, bool WRITE_U>
+__global__ void __launch_bounds__(SCS_T) k_finish_scalecols_slice(int64_t m, int64_t N, int64_t Kp, int splits,
+                                                                  const long long* __restrict__ P,
+                                                                  const int* __restrict__ ea,
+                                                                  const int* __restrict__ eb, double* __restrict__ C,
+                                                                  int64_t ldc, __nv_bfloat16* __restrict__ stack,
+                                                                  int* __restrict__ expo) {
+  if (CL > 1) cluster_arrive_relaxed();
+  const int n = blockIdx.x / CL;
+  const int64_t r0 = (int64_t)(blockIdx.x % CL) * SCS_T * U;
+  const int64_t total = m * N;
+  const long long* pc = P + (int64_t)n * m;
+  long long s[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) s[u] = 0;
+#pragma unroll 4
+  for (int z = 0; z < splits; ++z) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = r0 + threadIdx.x + (int64_t)u * SCS_T;
+      if (i < m) s[u] += pc[(size_t)z * total + i];
+    }
+  }
+  const int ebn = eb[n];
+  double v[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * SCS_T;
+    v[u] = (i < m) ? i64_ldexp(s[u], ea[i] + ebn - SL_SHIFT) : 0.0;
+  }
+  scalecols_slice_body<U, CL>(m, Kp, n, r0, v, WRITE_U ? C + (int64_t)n * ldc : nullptr, stack, expo);
+}
+
 }  // namespace slice
 
 static_assert(slice::S == kSliceDigits, "digit count");
@@ -529,8 +658,46 @@ int sliced_prepare(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, int64_t
 // C (M x N, FP64) = A_op' B with A_op the prepared stack (K x M) and B (K x N, FP64, column-major)
 // C (M x N, FP64) = A_op' B with A_op the prepared stack (K x M) and B (K x N, FP64, column-major).
 // reps > 1 (profiling) repeats the product kernel and reports its mean time per launch in *us.
+// Launch of a per-column scaling kernel: ncols clusters of cl CTAs of SCS_T threads
+template <typename... Exp, typename... Act>
+static int launch_cols(ofrr_ctx* ctx, int cl, int64_t ncols, void (*k)(Exp...), Act&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)(ncols * cl));
+  cfg.blockDim = dim3(slice::SCS_T);
+  cfg.stream = ctx->stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = cl > 1 ? 1 : 0;
+  OFRR_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<Act>(args)...));
+  return OFRR_SUCCESS;
+}
+// rows per thread U and CTAs per column CL for columns of m <= 8192 rows (every row of the padded
+// column below CL SCS_T U)
+template <class F>
+static int scs_dispatch(int64_t m, F&& f) {
+  using I1 = std::integral_constant<int, 1>;
+  using I2 = std::integral_constant<int, 2>;
+  using I4 = std::integral_constant<int, 4>;
+  if (m <= 1024) return f(I1(), I1());
+  if (m <= 2048) return f(I2(), I1());
+  if (m <= 4096) return f(I2(), I2());
+  return f(I4(), I2());
+}
+
+// fs != nullptr (with several K ranges): the partial sums go straight to k_finish_scalecols_slice.
+struct FusedScale {
+  bool write_u;
+  __nv_bfloat16* stack;
+  int* expo;
+  bool done = false;
+};
 static int sliced_gemm_run(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const double* B, int64_t ldb, double* C,
-                           int64_t ldc, int reps, double* us, double* bytes, const SlicedOperand* Bpre = nullptr) {
+                           int64_t ldc, int reps, double* us, double* bytes, const SlicedOperand* Bpre = nullptr,
+                           FusedScale* fs = nullptr) {
   using namespace slice;
   const int64_t K = A.K, Kp = A.Kp, M = A.M;
   // the combined 64-bit integer is bounded by K 2^(2 BETA + BETA LMAX) (1 + 2^-6): K <= 2^20 keeps it below 2^63
@@ -590,7 +757,19 @@ static int sliced_gemm_run(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, con
     if (bytes)  // digit stacks read once, int64 partials (or FP64 C) written once
       *bytes = (double)S * Kp * 2 * (double)(M + N) + (double)M * N * 8 * (splits > 1 ? splits : 1);
   }
-  if (splits > 1) {
+  if (splits > 1 && fs) {
+    const int64_t Kpc = (M + 63) / 64 * 64;
+    OFRR_TRY(scs_dispatch(M, [&](auto u, auto cl) {
+      constexpr int RU = decltype(u)::value, CL = decltype(cl)::value;
+      if (fs->write_u)
+        return launch_cols(ctx, CL, N, k_finish_scalecols_slice<RU, CL, true>, M, N, Kpc, splits, (const long long*)P,
+                           (const int*)A.expo, (const int*)Bs.expo, C, ldc, fs->stack, fs->expo);
+      return launch_cols(ctx, CL, N, k_finish_scalecols_slice<RU, CL, false>, M, N, Kpc, splits, (const long long*)P,
+                         (const int*)A.expo, (const int*)Bs.expo, C, ldc, fs->stack, fs->expo);
+    }));
+    OFRR_LAUNCHED(ctx, "k_finish_scalecols_slice");
+    fs->done = true;
+  } else if (splits > 1) {
     if (splits >= 12)
       k_sliced_finish<true><<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, splits, P, C, ldc, A.expo, Bs.expo);
     else
@@ -609,6 +788,25 @@ int sliced_gemm_tn_pre(ofrr_ctx* ctx, const SlicedOperand& A, const SlicedOperan
   return sliced_gemm_run(ctx, A, B.M, nullptr, 0, C, ldc, 1, nullptr, nullptr, &B);
 }
 
+// U (m x N) = A_op' B, then scalecols and the digit split of the scaled block into stack / expo (out
+// describes them), as sliced_gemm_tn_pre followed by scalecols_sliced and with the same results.  With
+// several K ranges the partial sums are combined inside the scaling kernel, and write_u = false
+// leaves U unwritten (a block that only feeds the next product through its digits).
+int sliced_gemm_scalecols_pre(ofrr_ctx* ctx, const SlicedOperand& A, const SlicedOperand& B, double* U, int64_t ldu,
+                              bool write_u, __nv_bfloat16* stack, int* expo, SlicedOperand* out) {
+  const int64_t m = A.M, n = B.M;
+  if (m < 1 || m > 8192 || n < 1 || n > 65535) return OFRR_ERR_BLAS_INVALID_SIZE;
+  FusedScale fs{write_u, stack, expo};
+  OFRR_TRY(sliced_gemm_run(ctx, A, n, nullptr, 0, U, ldu, 1, nullptr, nullptr, &B, &fs));
+  if (!fs.done) return scalecols_sliced(ctx, m, n, U, ldu, stack, expo, out);
+  out->K = m;
+  out->Kp = (m + 63) / 64 * 64;
+  out->M = n;
+  out->stack = stack;
+  out->expo = expo;
+  return OFRR_SUCCESS;
+}
+
 int scalecols_sliced(ofrr_ctx* ctx, int64_t m, int64_t n, double* U, int64_t ldu, __nv_bfloat16* stack, int* expo,
                      SlicedOperand* out) {
   if (m < 1 || m > 8192 || n < 1 || n > 65535) return OFRR_ERR_BLAS_INVALID_SIZE;
@@ -617,11 +815,10 @@ int scalecols_sliced(ofrr_ctx* ctx, int64_t m, int64_t n, double* U, int64_t ldu
   out->M = n;
   out->stack = stack;
   out->expo = expo;
-  if (m <= 2048) {
-    slice::k_scalecols_slice<256><<<(unsigned)n, 256, 0, ctx->stream>>>(m, out->Kp, U, ldu, stack, expo);
-  } else {
-    slice::k_scalecols_slice<1024><<<(unsigned)n, 1024, 0, ctx->stream>>>(m, out->Kp, U, ldu, stack, expo);
-  }
+  OFRR_TRY(scs_dispatch(m, [&](auto u, auto cl) {
+    constexpr int RU = decltype(u)::value, CL = decltype(cl)::value;
+    return launch_cols(ctx, CL, n, slice::k_scalecols_slice<RU, CL>, m, out->Kp, U, ldu, stack, expo);
+  }));
   OFRR_LAUNCHED(ctx, "k_scalecols_slice");
   return OFRR_SUCCESS;
 }
@@ -654,4 +851,26 @@ extern "C" int ofrr_profile_gemm_f64_emulated(ofrr_ctx* ctx, int64_t M, int64_t 
   SlicedOperand As;
   OFRR_TRY(sliced_prepare(ctx, K, M, A, lda, &As));
   return sliced_gemm_run(ctx, As, N, B, ldb, C, ldc, reps, us_per_launch, bytes_per_launch);
+}
+
+// Self-test of the fused scale-and-split steps of the emulated FP64 power iteration.  mode 0: X (M x N)
+// scaled in place (scalecols_sliced); mode 1: X = A' B (A: K x M, B: K x N) by the exact-slice product
+// whose partial sums are combined inside the scaling kernel (sliced_gemm_scalecols_pre, X written);
+// mode 2: the stand-alone slicer on X as it is.  All modes write the digit stack (N columns of
+// 5 roundup(M, 64) BF16 values) and the column exponents.
+extern "C" int ofrr_debug_scale_slice(ofrr_ctx* ctx, int mode, int64_t M, int64_t N, int64_t K, const double* A,
+                                      int64_t lda, const double* B, int64_t ldb, double* X, int64_t ldx,
+                                      void* digits, int* expo) {
+  if (!ctx || mode < 0 || mode > 2 || M < 1 || M > 8192 || N < 1 || N > 65535 || !X || ldx < M || !digits || !expo)
+    return OFRR_ERR_INVALID_ARGUMENT;
+  __nv_bfloat16* stack = (__nv_bfloat16*)digits;
+  SlicedOperand out;
+  if (mode == 0) return scalecols_sliced(ctx, M, N, X, ldx, stack, expo, &out);
+  if (mode == 2) return sliced_prepare_into(ctx, M, N, X, ldx, stack, expo, &out);
+  if (K < 1 || !A || !B || lda < K || ldb < K) return OFRR_ERR_INVALID_ARGUMENT;
+  WsScope scope(ctx);
+  SlicedOperand As, Bs;
+  OFRR_TRY(sliced_prepare(ctx, K, M, A, lda, &As));
+  OFRR_TRY(sliced_prepare(ctx, K, N, B, ldb, &Bs));
+  return sliced_gemm_scalecols_pre(ctx, As, Bs, X, ldx, true, stack, expo, &out);
 }

@@ -86,6 +86,11 @@ struct Op {
   int apply_pre(ofrr_ctx* ctx, int trans, const SlicedOperand& Xs, double* Y, int64_t ldy) {
     return sliced_gemm_tn_pre(ctx, trans ? sA : sAt, Xs, Y, ldy);
   }
+  // apply_pre, then scalecols and the digit split of Y (into Ys); write_y = false may leave Y unwritten
+  int apply_pre_scale(ofrr_ctx* ctx, int trans, const SlicedOperand& Xs, double* Y, int64_t ldy, bool write_y,
+                      __nv_bfloat16* stack, int* expo, SlicedOperand* Ys) {
+    return sliced_gemm_scalecols_pre(ctx, trans ? sA : sAt, Xs, Y, ldy, write_y, stack, expo, Ys);
+  }
 
   // digit stacks of A for the FP64 emulation: sAt for A V (operand A', K = n), sA for A' U (K = m).
   // Must be called in the solve's outermost workspace scope (the stacks live as long as the solve).
@@ -1223,15 +1228,24 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
       TraceScope ts(ctx, f64 ? "power.f64" : "power.16bit");
       if (fused) {
         // emulated FP64 products: each scalecols also writes the digits of the scaled block, the
-        // operand of the next product (bit-identical to scaling, then splitting)
+        // operand of the next product (bit-identical to scaling, then splitting); inside the loop
+        // the scaling kernel also combines the product's partial sums, and the FP64 blocks are
+        // stored only where the steps after the loop read them
         SlicedOperand Us, Vs;
         for (int j = 0; j < opt->step_size; ++j) {
-          if (j == 0) OFRR_TRY(op.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.po, U, ldu));
-          else OFRR_TRY(op.apply_pre(ctx, 0, Vs, (double*)U, ldu));
-          OFRR_TRY(scalecols_sliced(ctx, m, b, (double*)U, ldu, dig_u, exp_u, &Us));
-          OFRR_TRY(op.apply_pre(ctx, 1, Us, (double*)V, ldv));
-          if (j + 1 < opt->step_size) OFRR_TRY(scalecols_sliced(ctx, n, b, (double*)V, ldv, dig_v, exp_v, &Vs));
-          else OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr, P.fast));
+          const bool last = j + 1 == opt->step_size;
+          if (j == 0) {
+            OFRR_TRY(op.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.po, U, ldu));
+            OFRR_TRY(scalecols_sliced(ctx, m, b, (double*)U, ldu, dig_u, exp_u, &Us));
+          } else {
+            OFRR_TRY(op.apply_pre_scale(ctx, 0, Vs, (double*)U, ldu, last, dig_u, exp_u, &Us));
+          }
+          if (!last) {
+            OFRR_TRY(op.apply_pre_scale(ctx, 1, Us, (double*)V, ldv, false, dig_v, exp_v, &Vs));
+          } else {
+            OFRR_TRY(op.apply_pre(ctx, 1, Us, (double*)V, ldv));
+            OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr, P.fast));
+          }
           S.nmv += 2 * b;
         }
       } else {
