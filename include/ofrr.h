@@ -358,6 +358,14 @@ int ofrr_debug_bounded_wait(ofrr_ctx* ctx, int64_t timeout_ns);
 int ofrr_debug_scale_slice(ofrr_ctx* ctx, int mode, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda,
                            const double* B, int64_t ldb, double* X, int64_t ldx, void* digits, int* expo);
 
+/* Self-test of the 16-bit power step (no reference counterpart; subspace_iter_svd.m:63-69 in the
+ * low-precision phase): C = A' B for 16-bit A (K x M, M <= 8192) and B (K x N) of type t16 (OFRR_F16 or
+ * OFRR_BF16), FP32 accumulation, C stored as t16, then scalecols of C computed in FP32 (fast != 0: the
+ * production form).  The split-K partial sums are combined inside the scaling kernel.  Returns
+ * OFRR_ERR_INVALID_ARGUMENT when the shape or layout (16-byte aligned operands) does not take that path. */
+int ofrr_debug_gemm16_scalecols(ofrr_ctx* ctx, int t16, int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
+                                const void* B, int64_t ldb, void* C, int64_t ldc, int fast);
+
 /* Per-solve tracing: with a path set, every si_eig / si_svd / arnoldi_eig solve on this context appends
  * one JSON line to that file (solver, sizes, status, iterations, residual, kernel launches, total and
  * per-phase device time from CUDA events on the context's stream).  NULL or "" turns it off.  A context

@@ -133,6 +133,7 @@ SIGNATURES = {
     "ofrr_ctx_trim": (C.c_int, [_P]),
     "ofrr_debug_bounded_wait": (C.c_int, [_P, _I64]),
     "ofrr_debug_scale_slice": (C.c_int, [_P, C.c_int, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _P]),
+    "ofrr_debug_gemm16_scalecols": (C.c_int, [_P, C.c_int, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, C.c_int]),
     "ofrr_ctx_set_trace": (C.c_int, [_P, C.c_char_p]),
 }
 

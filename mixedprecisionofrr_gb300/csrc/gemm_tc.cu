@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdlib>
+#include <type_traits>
 
 #include "ofrr_internal.cuh"
 #include "tcgen05.cuh"
@@ -175,10 +176,106 @@ __global__ void k_splitk_reduce(int M, int N, int splits, const float* __restric
   }
 }
 
+// The split-K reduction fused with scalecols (16-bit storage TO, FP32 compute) for a product the power
+// iteration scales at once (subspace_iter_svd.m:63-69): each CTA sums the FP32 partials of its rows in
+// the order k_splitk_reduce uses and rounds them to TO (the values that kernel would store), then
+// scales them as k_scalecols_small does (pivot: lowest row of maximum modulus, across the cluster of
+// CL CTAs that shares a column).  The result is the reduction followed by scalecols, bit for bit.
+template <class TO, bool FAST, int U, int CL>
+__global__ void __launch_bounds__(SCS_T) k_splitk_scalecols(int M, int N, int splits, const float* __restrict__ partial,
+                                                            TO* __restrict__ D, int64_t ldd) {
+  using TC = float;
+  if (CL > 1) cluster_arrive_relaxed();
+  __shared__ ArgMaxK red[SCS_T / 32];
+  __shared__ TC s_t, s_y;
+  __shared__ long long s_k;
+  __shared__ bool s_pf;
+  __shared__ unsigned long long s_ckey[CL], s_crow[CL], s_cval[CL];  // filled by the cluster
+  const int n = blockIdx.x / CL;
+  const int64_t r0 = (int64_t)(blockIdx.x % CL) * SCS_T * U;
+  const int64_t total = (int64_t)M * N;
+  const float* pc = partial + (int64_t)n * M;
+  float acc[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) acc[u] = 0.f;
+#pragma unroll 4
+  for (int z = 0; z < splits; ++z) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = r0 + threadIdx.x + (int64_t)u * SCS_T;
+      if (i < M) acc[u] += pc[(size_t)z * total + i];
+    }
+  }
+  TO v[U];
+  ArgMaxK a{-1, 0x7fffffffffffffffLL};
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * SCS_T;
+    v[u] = (i < M) ? cvt_out<TO>(acc[u]) : TO(0);
+    if (i < M) {
+      const long long key = amax_key(v[u]);
+      if (key > a.key) a = ArgMaxK{key, i};  // per-thread rows ascend: strict > keeps the lowest
+    }
+  }
+  const ArgMaxK r = block_argmaxk(a, red);
+  if (r.key >= 0 && threadIdx.x == (int)((r.i - r0) % SCS_T)) {  // the owner of this CTA's candidate
+    const int ku = (int)((r.i - r0) / SCS_T);
+    TO pv = TO(0);
+#pragma unroll
+    for (int u = 0; u < U; ++u) pv = (u == ku) ? v[u] : pv;
+    const TC t0 = to_c<TC, TO>(pv);
+    s_t = t0;
+    if (CL == 1) {
+      s_k = r.i;
+      s_y = (t0 != TC(0)) ? pivot_recip(t0) : TC(0);  // once per column
+      s_pf = pivot_fast(t0);
+    }
+  }
+  if (CL > 1) {
+    __syncthreads();
+    cluster_wait();  // every CTA of the cluster has started: its shared memory may be written
+    const unsigned me = cluster_rank();
+    if (threadIdx.x < CL) {
+      st_cluster_u64(cluster_map(&s_ckey[me], threadIdx.x), (unsigned long long)r.key);
+      st_cluster_u64(cluster_map(&s_crow[me], threadIdx.x), (unsigned long long)r.i);
+      st_cluster_u64(cluster_map(&s_cval[me], threadIdx.x), (unsigned long long)__float_as_uint(r.key >= 0 ? s_t : 0.f));
+    }
+    cluster_arrive();
+    cluster_wait();  // the last access to another CTA's shared memory is before this barrier
+    if (threadIdx.x == 0) {
+      ArgMaxK g{-1, 0x7fffffffffffffffLL};
+      TC gv = TC(0);
+#pragma unroll
+      for (int q = 0; q < CL; ++q) {  // in row order: max key, lowest row on ties
+        const ArgMaxK c{(long long)s_ckey[q], (long long)s_crow[q]};
+        const ArgMaxK pk = argmaxk_pick(g, c);
+        if (pk.key != g.key || pk.i != g.i) gv = __uint_as_float((unsigned)s_cval[q]);
+        g = pk;
+      }
+      s_t = gv;
+      s_k = g.i;
+      s_y = (gv != TC(0)) ? pivot_recip(gv) : TC(0);
+      s_pf = pivot_fast(gv);
+    }
+  }
+  __syncthreads();
+  const TC t = s_t, y = s_y;
+  const int64_t k = s_k;
+  const bool pf = s_pf;
+  TO* col = D + (int64_t)n * ldd;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = r0 + threadIdx.x + (int64_t)u * SCS_T;
+    if (i < M) col[i] = (t != TC(0)) ? from_c<TO, TC>(scale_by<TC, FAST>(to_c<TC, TO>(v[u]), t, y, pf, i == k)) : v[u];
+  }
+}
+
 // ---- host side ------------------------------------------------------------------------
+// scale >= 0: the product is followed by scalecols (FAST when scale == 1) of the 16-bit result, fused
+// with the split-K reduction when K is split
 template <int BN, class TOUT>
 static int launch(ofrr_ctx* ctx, const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int K, ofrr_dtype t16,
-                  TOUT* D, int64_t ldd, int splits) {
+                  TOUT* D, int64_t ldd, int splits, int scale = -1) {
   const int kbt = (K + BK - 1) / BK;
   const int kbps = (kbt + splits - 1) / splits;
   splits = (kbt + kbps - 1) / kbps;
@@ -200,6 +297,23 @@ static int launch(ofrr_ctx* ctx, const CUtensorMap& ma, const CUtensorMap& mb, i
   k_gemm_tn<BN, TOUT><<<grid, THREADS, smem, ctx->stream>>>(ma, mb, M, N, kbt, kbps, make_idesc(t16, BN), D, ldd,
                                                             partial, ctx->dev_flags + kFlagTcWait);
   OFRR_LAUNCHED(ctx, "k_gemm_tn");
+  constexpr bool k16 = std::is_same<TOUT, __half>::value || std::is_same<TOUT, __nv_bfloat16>::value;
+  if (scale >= 0 && !k16) return OFRR_ERR_INTERNAL;
+  if constexpr (k16) {
+    if (scale >= 0 && splits > 1) {
+      OFRR_TRY(scs_dispatch(M, [&](auto u, auto cl) {
+        constexpr int RU = decltype(u)::value, CL = decltype(cl)::value;
+        if (scale == 1)
+          return launch_cols(ctx, CL, N, k_splitk_scalecols<TOUT, true, RU, CL>, M, N, splits, (const float*)partial,
+                             D, ldd);
+        return launch_cols(ctx, CL, N, k_splitk_scalecols<TOUT, false, RU, CL>, M, N, splits, (const float*)partial,
+                           D, ldd);
+      }));
+      OFRR_LAUNCHED(ctx, "k_splitk_scalecols");
+      return OFRR_SUCCESS;
+    }
+    if (scale >= 0) return scalecols_impl(ctx, t16, OFRR_F32, M, N, D, ldd, nullptr, scale == 1);
+  }
   if (splits > 1) {
     if (splits >= 12)
       k_splitk_reduce<TOUT, true><<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, splits, partial, D, ldd);
@@ -210,6 +324,18 @@ static int launch(ofrr_ctx* ctx, const CUtensorMap& ma, const CUtensorMap& mb, i
   return OFRR_SUCCESS;
 }
 
+}  // namespace tc
+
+namespace tc {
+// enough CTAs to cover the SMs: split K when the output grid is small
+static int plan_splits(int64_t M, int64_t N, int64_t K, int BN) {
+  const int tiles = (int)(((M + BM - 1) / BM) * ((N + BN - 1) / BN));
+  const int kbt = (int)((K + BK - 1) / BK);
+  int splits = 1;
+  while (tiles * splits < 148 && splits * 2 <= kbt && splits < 64) splits *= 2;
+  if (const char* e = getenv("OFRR_TC_SPLITS")) splits = std::max(1, std::min(atoi(e), kbt));  // tuning override
+  return splits;
+}
 }  // namespace tc
 
 // Route a 16-bit TN product to the tcgen05 kernel when its layout allows TMA (16-byte aligned
@@ -226,12 +352,7 @@ int gemm_tc_try(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype t16, int64_t M
   CUtensorMap ma, mb;
   if (!tc::make_map(&ma, t16, A, K, M, lda, tc::BM)) return OFRR_SUCCESS;
   if (!tc::make_map(&mb, t16, B, K, N, ldb, BN)) return OFRR_SUCCESS;
-  // enough CTAs to cover the SMs: split K when the output grid is small
-  const int tiles = (int)(((M + tc::BM - 1) / tc::BM) * ((N + BN - 1) / BN));
-  const int kbt = (int)((K + tc::BK - 1) / tc::BK);
-  int splits = 1;
-  while (tiles * splits < 148 && splits * 2 <= kbt && splits < 64) splits *= 2;
-  if (const char* e = getenv("OFRR_TC_SPLITS")) splits = std::max(1, std::min(atoi(e), kbt));  // tuning override
+  const int splits = tc::plan_splits(M, N, K, BN);
   int st = OFRR_SUCCESS;
   OFRR_DISPATCH_STORAGE(tout, TO, {
     if (BN == 32) st = tc::launch<32, TO>(ctx, ma, mb, (int)M, (int)N, (int)K, t16, (TO*)C, ldc, splits);
@@ -243,4 +364,50 @@ int gemm_tc_try(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype t16, int64_t M
   return OFRR_SUCCESS;
 }
 
+// C (t16, M x N) = A' B (16-bit TN product, FP32 accumulation), then scalecols of C in FP32 (fast: the
+// reciprocal-multiply form): the power step of the 16-bit phase.  With K split, the partial sums are
+// combined inside the scaling kernel; the result equals gemm_tc_try followed by scalecols_impl bit for
+// bit.  *handled = false (nothing launched) leaves both steps to the caller.
+int gemm_tc_scalecols(ofrr_ctx* ctx, ofrr_dtype t16, int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
+                      const void* B, int64_t ldb, void* C, int64_t ldc, bool fast, bool* handled) {
+  *handled = false;
+  if (t16 != OFRR_F16 && t16 != OFRR_BF16) return OFRR_SUCCESS;
+  if (K < 16 || M < 1 || N < 1 || M > 8192 || N > 65535 || K > (1 << 30)) return OFRR_SUCCESS;
+  if (((uintptr_t)A & 15) || ((uintptr_t)B & 15) || ((lda * 2) & 15) || ((ldb * 2) & 15)) return OFRR_SUCCESS;
+  if (getenv("OFRR_DISABLE_TC")) return OFRR_SUCCESS;
+  const int BN = (N <= 32) ? 32 : (N <= 64 ? 64 : 128);
+  CUtensorMap ma, mb;
+  if (!tc::make_map(&ma, t16, A, K, M, lda, tc::BM)) return OFRR_SUCCESS;
+  if (!tc::make_map(&mb, t16, B, K, N, ldb, BN)) return OFRR_SUCCESS;
+  const int splits = tc::plan_splits(M, N, K, BN);
+  const int sc = fast ? 1 : 0;
+  int st;
+  if (t16 == OFRR_F16) {
+    if (BN == 32) st = tc::launch<32, __half>(ctx, ma, mb, (int)M, (int)N, (int)K, t16, (__half*)C, ldc, splits, sc);
+    else if (BN == 64) st = tc::launch<64, __half>(ctx, ma, mb, (int)M, (int)N, (int)K, t16, (__half*)C, ldc, splits, sc);
+    else st = tc::launch<128, __half>(ctx, ma, mb, (int)M, (int)N, (int)K, t16, (__half*)C, ldc, splits, sc);
+  } else {
+    using B16 = __nv_bfloat16;
+    if (BN == 32) st = tc::launch<32, B16>(ctx, ma, mb, (int)M, (int)N, (int)K, t16, (B16*)C, ldc, splits, sc);
+    else if (BN == 64) st = tc::launch<64, B16>(ctx, ma, mb, (int)M, (int)N, (int)K, t16, (B16*)C, ldc, splits, sc);
+    else st = tc::launch<128, B16>(ctx, ma, mb, (int)M, (int)N, (int)K, t16, (B16*)C, ldc, splits, sc);
+  }
+  if (st != OFRR_SUCCESS) return st;
+  *handled = true;
+  return OFRR_SUCCESS;
+}
+
 }  // namespace ofrr
+
+using namespace ofrr;
+
+// Self-test of the 16-bit power step: C = A' B (A: K x M, B: K x N, both t16; C t16), then scalecols of C
+// in FP32, with the split-K reduction fused into the scaling kernel.  Returns OFRR_ERR_INVALID_ARGUMENT
+// for a shape or layout the fused path does not take.
+extern "C" int ofrr_debug_gemm16_scalecols(ofrr_ctx* ctx, int t16, int64_t M, int64_t N, int64_t K, const void* A,
+                                           int64_t lda, const void* B, int64_t ldb, void* C, int64_t ldc, int fast) {
+  if (!ctx || !A || !B || !C || ldc < M) return OFRR_ERR_INVALID_ARGUMENT;
+  bool handled = false;
+  OFRR_TRY(gemm_tc_scalecols(ctx, (ofrr_dtype)t16, M, N, K, A, lda, B, ldb, C, ldc, fast != 0, &handled));
+  return handled ? OFRR_SUCCESS : OFRR_ERR_INVALID_ARGUMENT;
+}

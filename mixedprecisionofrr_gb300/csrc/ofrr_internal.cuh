@@ -2,6 +2,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <type_traits>
+#include <utility>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 #include <cublas_v2.h>
@@ -348,6 +350,59 @@ __device__ __forceinline__ ArgMaxK block_argmaxk(ArgMaxK a, ArgMaxK* smem) {
   return r;
 }
 
+// Per-column kernels over a cluster of CL CTAs of SCS_T threads (scale and split, split-K combine and
+// scale): CTA r of a column's cluster holds rows [r SCS_T U, (r + 1) SCS_T U), U per thread.
+constexpr int SCS_T = 1024;
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// shared-memory address of this CTA's variable p in CTA `rank` of the cluster
+__device__ __forceinline__ unsigned cluster_map(const void* p, unsigned rank) {
+  unsigned a = (unsigned)__cvta_generic_to_shared(p), r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_cluster_u64(unsigned addr, unsigned long long v) {
+  asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+
+// Launch of a per-column scaling kernel: ncols clusters of cl CTAs of SCS_T threads
+template <typename... Exp, typename... Act>
+static int launch_cols(ofrr_ctx* ctx, int cl, int64_t ncols, void (*k)(Exp...), Act&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)(ncols * cl));
+  cfg.blockDim = dim3(SCS_T);
+  cfg.stream = ctx->stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = cl > 1 ? 1 : 0;
+  OFRR_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<Act>(args)...));
+  return OFRR_SUCCESS;
+}
+// rows per thread U and CTAs per column CL for columns of m <= 8192 rows (every row of the padded
+// column below CL SCS_T U)
+template <class F>
+static int scs_dispatch(int64_t m, F&& f) {
+  using I1 = std::integral_constant<int, 1>;
+  using I2 = std::integral_constant<int, 2>;
+  using I4 = std::integral_constant<int, 4>;
+  if (m <= 1024) return f(I1(), I1());
+  if (m <= 2048) return f(I2(), I1());
+  if (m <= 4096) return f(I2(), I2());
+  return f(I4(), I2());
+}
+
 // runtime dtype dispatch --------------------------------------------------------------
 #define OFRR_DISPATCH_STORAGE(dt, T, ...)                         \
   switch (dt) {                                                   \
@@ -391,6 +446,8 @@ inline dim3 grid_2d(long long m, long long n, int block) {
 
 // ---- cross-file internal API ---------------------------------------------------------
 // dense / sparse products into caller buffers (all on ctx->stream, no host sync)
+int gemm_tc_scalecols(ofrr_ctx* ctx, ofrr_dtype t16, int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
+                      const void* B, int64_t ldb, void* C, int64_t ldc, bool fast, bool* handled);
 int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype tb, ofrr_dtype tc,
               ofrr_dtype tout, int64_t M, int64_t N, int64_t K, double alpha, const void* A,
               int64_t lda, const void* B, int64_t ldb, double beta, void* C, int64_t ldc);

@@ -16,8 +16,6 @@
 
 #include <algorithm>
 #include <atomic>
-#include <type_traits>
-#include <utility>
 #include <vector>
 
 namespace ofrr {
@@ -188,28 +186,6 @@ __global__ void __launch_bounds__(T) k_slice_cols(int64_t K, int64_t Kp, int64_t
 // on the bit patterns and writes its digits -- the operand of the next exact-slice product, without
 // reading the column again.  With CL = 2 the CTAs exchange their pivot candidates and maxima through
 // distributed shared memory; the result is the same as one CTA over the whole column.
-constexpr int SCS_T = 1024;
-
-__device__ __forceinline__ void cluster_arrive_relaxed() {
-  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
-__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
-__device__ __forceinline__ unsigned cluster_rank() {
-  unsigned r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-// shared-memory address of this CTA's variable p in CTA `rank` of the cluster
-__device__ __forceinline__ unsigned cluster_map(const void* p, unsigned rank) {
-  unsigned a = (unsigned)__cvta_generic_to_shared(p), r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
-  return r;
-}
-__device__ __forceinline__ void st_cluster_u64(unsigned addr, unsigned long long v) {
-  asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
-}
-
 // Body shared by k_scalecols_slice and k_finish_scalecols_slice: v[u] holds row r0 + threadIdx.x +
 // u SCS_T of column n (0 beyond m), r0 = this CTA's first row.  col != nullptr also stores the scaled
 // column there.  For CL > 1 the caller has done cluster_arrive_relaxed() once on entry.
@@ -658,36 +634,6 @@ int sliced_prepare(ofrr_ctx* ctx, int64_t K, int64_t M, const double* X, int64_t
 // C (M x N, FP64) = A_op' B with A_op the prepared stack (K x M) and B (K x N, FP64, column-major)
 // C (M x N, FP64) = A_op' B with A_op the prepared stack (K x M) and B (K x N, FP64, column-major).
 // reps > 1 (profiling) repeats the product kernel and reports its mean time per launch in *us.
-// Launch of a per-column scaling kernel: ncols clusters of cl CTAs of SCS_T threads
-template <typename... Exp, typename... Act>
-static int launch_cols(ofrr_ctx* ctx, int cl, int64_t ncols, void (*k)(Exp...), Act&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = (unsigned)cl;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.gridDim = dim3((unsigned)(ncols * cl));
-  cfg.blockDim = dim3(slice::SCS_T);
-  cfg.stream = ctx->stream;
-  cfg.attrs = attr;
-  cfg.numAttrs = cl > 1 ? 1 : 0;
-  OFRR_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<Act>(args)...));
-  return OFRR_SUCCESS;
-}
-// rows per thread U and CTAs per column CL for columns of m <= 8192 rows (every row of the padded
-// column below CL SCS_T U)
-template <class F>
-static int scs_dispatch(int64_t m, F&& f) {
-  using I1 = std::integral_constant<int, 1>;
-  using I2 = std::integral_constant<int, 2>;
-  using I4 = std::integral_constant<int, 4>;
-  if (m <= 1024) return f(I1(), I1());
-  if (m <= 2048) return f(I2(), I1());
-  if (m <= 4096) return f(I2(), I2());
-  return f(I4(), I2());
-}
-
 // fs != nullptr (with several K ranges): the partial sums go straight to k_finish_scalecols_slice.
 struct FusedScale {
   bool write_u;

@@ -79,6 +79,24 @@ struct Op {
     return gemm_impl(ctx, trans, 0, ta, tx, tc, ty, M, nrhs, K, 1.0, Ad, lda, X, ldx, 0.0, Y, ldy);
   }
 
+  // Y = op(A) X, then scalecols(Y) (storage t, compute tc): one power step.  16-bit dense products with
+  // FP32 accumulation combine their split-K partial sums inside the scaling kernel (same results).
+  int apply_scale(ofrr_ctx* ctx, int trans, ofrr_dtype t, ofrr_dtype tc, const void* X, int64_t ldx, int64_t nrhs,
+                  void* Y, int64_t ldy, bool fast) {
+    const int64_t M = trans ? n() : m(), K = trans ? m() : n();
+    if (A->kind == OFRR_OP_DENSE && tc == OFRR_F32 && (t == OFRR_F16 || t == OFRR_BF16)) {
+      const void* Ad;
+      int64_t lda;
+      if (trans) OFRR_TRY(dense_as(ctx, t, &Ad, &lda));
+      else OFRR_TRY(dense_t_as(ctx, t, &Ad, &lda));
+      bool handled = false;
+      OFRR_TRY(gemm_tc_scalecols(ctx, t, M, nrhs, K, Ad, lda, X, ldx, Y, ldy, fast, &handled));
+      if (handled) return OFRR_SUCCESS;
+    }
+    OFRR_TRY(apply(ctx, trans, t, t, X, ldx, nrhs, tc, t, Y, ldy));
+    return scalecols_impl(ctx, t, tc, M, nrhs, Y, ldy, nullptr, fast);
+  }
+
   // Y = op(A) X for X already split into digits (scalecols_sliced); dense operators in the emulated mode
   bool can_apply_pre(const ofrr_ctx* ctx) const {
     return ctx->emulate_f64 && A->kind == OFRR_OP_DENSE && have_sA && have_sAt;
@@ -1110,9 +1128,8 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
     for (int s = 0; s < opt->step_size; ++s) {
       void* dst = (cur == V) ? W : V;
       int64_t lddst = (cur == V) ? n : ldv;
-      OFRR_TRY(op.apply(ctx, 0, P.po, P.po, cur, ldcur, b, P.pc, P.po, dst, lddst));
+      OFRR_TRY(op.apply_scale(ctx, 0, P.po, P.pc, cur, ldcur, b, dst, lddst, P.fast));
       S.nmv += b;
-      OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, dst, lddst, nullptr, P.fast));
       cur = dst;
       ldcur = lddst;
     }
@@ -1250,10 +1267,8 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
         }
       } else {
         for (int j = 0; j < opt->step_size; ++j) {
-          OFRR_TRY(op.apply(ctx, 0, P.po, P.po, V, ldv, b, P.pc, P.po, U, ldu));
-          OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, m, b, U, ldu, nullptr, P.fast));
-          OFRR_TRY(op.apply(ctx, 1, P.po, P.po, U, ldu, b, P.pc, P.po, V, ldv));
-          OFRR_TRY(scalecols_impl(ctx, P.po, P.pc, n, b, V, ldv, nullptr, P.fast));
+          OFRR_TRY(op.apply_scale(ctx, 0, P.po, P.pc, V, ldv, b, U, ldu, P.fast));
+          OFRR_TRY(op.apply_scale(ctx, 1, P.po, P.pc, U, ldu, b, V, ldv, P.fast));
           S.nmv += 2 * b;
         }
       }

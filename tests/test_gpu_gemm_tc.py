@@ -112,3 +112,29 @@ def test_f64_emulated_gemm_zero_columns(api):
     C = api.gemm_f64_emulated(A, B).cpu().numpy()
     assert np.array_equal(C[[0, 1, 2, 4]], np.zeros((4, 8)))
     assert np.allclose(C[3], B.sum(0), rtol=1e-12)
+
+
+@pytest.mark.parametrize("M,N,K", [(8192, 64, 2048), (2048, 64, 8192), (3000, 7, 5000), (700, 33, 4096),
+                                   (4096, 64, 64), (6000, 5, 1000)])
+@pytest.mark.parametrize("pin", ["half", "bfloat16"])
+def test_tc_gemm_scalecols_fused(api, M, N, K, pin):
+    """The 16-bit power step: product with the split-K reduction fused into scalecols equals the
+    product (ofrr_gemm) followed by ofrr_scalecols, bit for bit (both FP32 scaling forms)."""
+    import torch
+    from mixedprecisionofrr_gb300 import _lib as L
+
+    rng = np.random.default_rng(M + N + K)
+    A = rng.standard_normal((K, M))
+    B = rng.standard_normal((K, N))
+    B[:, 0] = 0.0  # zero column of C: left unscaled
+    p = api.PREC[pin]
+    Ad = api.to_device_cm(A, p)
+    Bd = api.to_device_cm(B, p)
+    ref = api.scalecols(api.gemm(Ad, "T", Bd, "single", pin), "single", pin)
+    ctx = api.context()
+    for fast in (1, 0):
+        Cd = api.empty_cm(M, N, p)
+        assert ctx.lib.ofrr_debug_gemm16_scalecols(ctx.h, p, M, N, K, Ad.data_ptr(), api.ld_of(Ad), Bd.data_ptr(),
+                                                   api.ld_of(Bd), Cd.data_ptr(), api.ld_of(Cd), fast) == L.SUCCESS
+        assert ctx.lib.ofrr_ctx_synchronize(ctx.h) == L.SUCCESS
+        assert torch.equal(Cd.view(torch.int16), ref.view(torch.int16))
