@@ -629,4 +629,50 @@ MSVDStatus arnoldi_svd(const Matrix<T_I>& A, Matrix<T_O>& U, Matrix<T_O>& S, Mat
   return MSVDStatus::kErrorNotImplemented;
 }
 
+// ---- on-disk CSR (CPP/io/matrix_reader.hpp:7-44): host arrays, as the reference returns them ---------
+class CSRMatrix {
+ public:
+  std::vector<int> row_ptr;
+  std::vector<int> col_ind;
+  std::vector<double> values;
+  int rows;
+  int cols;
+  CSRMatrix() : rows(0), cols(0) {}
+};
+
+class MatrixReader {
+ public:
+  // <prefix>_row_ptr.bin, _col_ind.bin, _values.bin; throws std::runtime_error when a file is missing,
+  // empty or malformed (matrix_reader.cpp:8-45)
+  static CSRMatrix read_csr_matrix(const std::string& prefix) {
+    int64_t nrows = 0, nnz = 0, ncols = 0;
+    int st = ofrr_csr_file_sizes(prefix.c_str(), &nrows, &nnz);
+    if (st != OFRR_SUCCESS) throw std::runtime_error("read_csr_matrix(" + prefix + "): " + ofrr_status_string(st));
+    CSRMatrix m;
+    m.row_ptr.resize((size_t)nrows + 1);
+    m.col_ind.resize((size_t)nnz);
+    m.values.resize((size_t)nnz);
+    st = ofrr_csr_file_read(nullptr, prefix.c_str(), nrows, nnz, m.row_ptr.data(), m.col_ind.data(), m.values.data(),
+                            &ncols, 0);
+    if (st != OFRR_SUCCESS) throw std::runtime_error("read_csr_matrix(" + prefix + "): " + ofrr_status_string(st));
+    m.rows = (int)nrows;
+    m.cols = (int)ncols;
+    return m;
+  }
+  // <prefix>_singular_values.bin; empty when the file cannot be read (matrix_reader.cpp:47-50)
+  static std::vector<double> read_singular_values(const std::string& prefix) {
+    int64_t n = 0;
+    if (ofrr_read_singular_values(prefix.c_str(), &n, nullptr) != OFRR_SUCCESS) return {};
+    std::vector<double> v((size_t)n);
+    if (ofrr_read_singular_values(prefix.c_str(), &n, v.data()) != OFRR_SUCCESS) return {};
+    return v;
+  }
+};
+
+// device operator from a file-read CSRMatrix
+template <typename T>
+CsrMatrix<T> to_device(const CSRMatrix& m, bool symmetric) {
+  return CsrMatrix<T>((size_t)m.rows, (size_t)m.cols, m.row_ptr, m.col_ind, m.values, symmetric);
+}
+
 }  // namespace msvd

@@ -157,6 +157,23 @@ int ofrr_csrmm(ofrr_ctx* ctx, const ofrr_csr* A, int trans, ofrr_dtype tx, ofrr_
                ofrr_dtype ty, int64_t nrhs, const void* X /*dev*/, int64_t ldx,
                void* Y /*dev*/, int64_t ldy);
 
+/* ---- on-disk CSR matrices (CPP/io/matrix_reader.cpp:8-50) -------------------------- *
+ * <prefix>_row_ptr.bin (int32, nrows+1), <prefix>_col_ind.bin (int32, 0-based, nnz) and
+ * <prefix>_values.bin (float64, nnz); element counts from the file sizes, ncols = largest column
+ * index + 1.  Missing file: OFRR_ERR_FILE_NOT_FOUND; empty file, partial element, col_ind/values
+ * length mismatch or a malformed structure (row_ptr[0] != 0, decreasing row_ptr,
+ * row_ptr[nrows] != nnz, negative column index): OFRR_ERR_INVALID_FORMAT.
+ * ofrr_csr_file_read fills caller buffers of the sizes ofrr_csr_file_sizes reported: host buffers
+ * (on_device = 0, ctx may be NULL) or device buffers (on_device = 1: streamed through pinned staging
+ * buffers on the context's stream and validated on the GPU; synchronous). */
+int ofrr_csr_file_sizes(const char* prefix, int64_t* nrows, int64_t* nnz);
+int ofrr_csr_file_read(ofrr_ctx* ctx, const char* prefix, int64_t nrows, int64_t nnz, int32_t* indptr,
+                       int32_t* indices, double* values, int64_t* ncols, int on_device);
+/* <prefix>_singular_values.bin (float64, matrix_reader.cpp:47-50).  values == NULL: *count = the
+ * number of values; otherwise *count is the capacity of values (host) on entry and the number read
+ * on return. */
+int ofrr_read_singular_values(const char* prefix, int64_t* count, double* values);
+
 /* ---- small dense FP64 eigenproblems on the device --------------------------------- *
  * Replace the host LAPACKE wrappers msvd::syev / msvd::sygv (mvops.hpp:184-197,
  * mvops.cu:1601-1664).  Ascending eigenvalues; A is overwritten by the eigenvectors

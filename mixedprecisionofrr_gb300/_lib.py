@@ -133,6 +133,9 @@ SIGNATURES = {
     "ofrr_ctx_trim": (C.c_int, [_P]),
     "ofrr_debug_bounded_wait": (C.c_int, [_P, _I64]),
     "ofrr_debug_scale_slice": (C.c_int, [_P, C.c_int, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _P]),
+    "ofrr_csr_file_sizes": (C.c_int, [C.c_char_p, C.POINTER(_I64), C.POINTER(_I64)]),
+    "ofrr_csr_file_read": (C.c_int, [_P, C.c_char_p, _I64, _I64, _P, _P, _P, C.POINTER(_I64), C.c_int]),
+    "ofrr_read_singular_values": (C.c_int, [C.c_char_p, C.POINTER(_I64), _P]),
     "ofrr_debug_gemm16_scalecols": (C.c_int, [_P, C.c_int, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, C.c_int]),
     "ofrr_ctx_set_trace": (C.c_int, [_P, C.c_char_p]),
 }

@@ -9,6 +9,7 @@ every computation is a call into the CUDA library, and a missing library raises.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 from typing import Optional
 
@@ -159,6 +160,30 @@ class CsrMatrix:
             symmetric = shape[0] == shape[1] and abs(M - M.T).max() == 0
         self.symmetric = bool(symmetric)
 
+    @classmethod
+    def from_device(cls, indptr, indices, a_double, shape, symmetric: Optional[bool] = None):
+        """Wrap device arrays (int32 indptr / indices, FP64 values) without a host round trip; the FP32
+        and FP16 value copies are rounded once from the FP64 values on the device (ofrr_cast), as
+        sparse2csr.m:48-49 rounds them."""
+        self = cls.__new__(cls)
+        self.shape = (int(shape[0]), int(shape[1]))
+        self.nnz = nnz = int(a_double.numel())
+        self.indptr, self.indices, self.a_double = indptr, indices, a_double
+        self.a_single = torch.empty(nnz, dtype=torch.float32, device=a_double.device)
+        self.a_half = torch.empty(nnz, dtype=torch.float16, device=a_double.device)
+        if nnz:
+            ctx = context()
+            for t, code in ((self.a_single, L.F32), (self.a_half, L.F16)):
+                L.check(ctx.lib.ofrr_cast(ctx.h, L.F64, code, nnz, 1, a_double.data_ptr(), nnz, t.data_ptr(), nnz),
+                        "cast")
+        if symmetric is None:
+            import scipy.sparse as sp
+
+            M = sp.csr_matrix((a_double.cpu().numpy(), indices.cpu().numpy(), indptr.cpu().numpy()), shape=self.shape)
+            symmetric = self.shape[0] == self.shape[1] and abs(M - M.T).max() == 0
+        self.symmetric = bool(symmetric)
+        return self
+
     def struct(self) -> L.ofrr_csr:
         s = L.ofrr_csr()
         s.nrows, s.ncols, s.nnz = self.shape[0], self.shape[1], self.nnz
@@ -168,6 +193,48 @@ class CsrMatrix:
         s.a_single = self.a_single.data_ptr() if self.nnz else None
         s.a_half = self.a_half.data_ptr() if self.nnz else None
         return s
+
+
+def read_csr(prefix: str, symmetric: Optional[bool] = None, on_device: bool = True) -> CsrMatrix:
+    """CPP/io/matrix_reader.cpp:8-45 (MatrixReader::read_csr_matrix): <prefix>_row_ptr.bin,
+    _col_ind.bin (int32, 0-based) and _values.bin (float64) into a device CsrMatrix; columns = largest
+    column index + 1.  on_device streams the files into HBM through pinned staging buffers and
+    validates the structure on the GPU; otherwise they are read and checked on the host, then copied.
+    Raises OfrrError (FILE_NOT_FOUND / INVALID_FORMAT) where the reference throws."""
+    nrows, nnz = C.c_int64(), C.c_int64()
+    pfx = os.fsencode(prefix)
+    lib = L.load()
+    L.check(lib.ofrr_csr_file_sizes(pfx, C.byref(nrows), C.byref(nnz)), "read_csr")
+    ncols = C.c_int64()
+    if on_device:
+        ctx = context()
+        ip = torch.empty(nrows.value + 1, dtype=torch.int32, device="cuda")
+        ix = torch.empty(nnz.value, dtype=torch.int32, device="cuda")
+        va = torch.empty(nnz.value, dtype=torch.float64, device="cuda")
+        L.check(lib.ofrr_csr_file_read(ctx.h, pfx, nrows.value, nnz.value, ip.data_ptr(), ix.data_ptr(), va.data_ptr(),
+                                       C.byref(ncols), 1), "read_csr")
+        return CsrMatrix.from_device(ip, ix, va, (nrows.value, ncols.value), symmetric)
+    ip = np.empty(nrows.value + 1, np.int32)
+    ix = np.empty(nnz.value, np.int32)
+    va = np.empty(nnz.value, np.float64)
+    L.check(lib.ofrr_csr_file_read(None, pfx, nrows.value, nnz.value, ip.ctypes.data, ix.ctypes.data, va.ctypes.data,
+                                   C.byref(ncols), 0), "read_csr")
+    return CsrMatrix({"indptr": ip, "indices": ix, "a_double": va, "nrows": nrows.value, "ncols": ncols.value},
+                     symmetric)
+
+
+def read_singular_values(prefix: str) -> np.ndarray:
+    """CPP/io/matrix_reader.cpp:47-50: <prefix>_singular_values.bin (float64); empty when the file is
+    missing or unreadable, as in the reference."""
+    lib = L.load()
+    pfx = os.fsencode(prefix)
+    n = C.c_int64(0)
+    if lib.ofrr_read_singular_values(pfx, C.byref(n), None) != L.SUCCESS:
+        return np.empty(0)
+    out = np.empty(n.value, np.float64)
+    if lib.ofrr_read_singular_values(pfx, C.byref(n), out.ctypes.data) != L.SUCCESS:
+        return np.empty(0)
+    return out
 
 
 @dataclass

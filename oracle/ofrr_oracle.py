@@ -199,6 +199,35 @@ def sparse2csr(A) -> dict:
     }
 
 
+def read_csr_matrix(prefix: str) -> dict:
+    """``CPP/io/matrix_reader.cpp:8-45`` (MatrixReader::read_csr_matrix): ``<prefix>_row_ptr.bin``
+    (int32), ``_col_ind.bin`` (int32, 0-based), ``_values.bin`` (float64), counts from the file sizes,
+    ``cols`` = largest column index + 1 (``:40-43``).  Raises ``RuntimeError`` where the reference
+    throws (a missing or empty file, ``:15-17``, ``:27-29``, ``:34-36``)."""
+    out = {}
+    for key, suffix, dt in (("indptr", "_row_ptr.bin", np.int32), ("indices", "_col_ind.bin", np.int32),
+                            ("a_double", "_values.bin", np.float64)):
+        try:
+            a = np.fromfile(prefix + suffix, dtype=dt)  # whole elements only (matrix_reader.cpp:63-66)
+        except OSError as e:
+            raise RuntimeError(f"Failed to read {prefix + suffix}") from e
+        if a.size == 0:
+            raise RuntimeError(f"Failed to read {prefix + suffix}")
+        out[key] = a
+    out["nrows"] = out["indptr"].size - 1
+    out["ncols"] = int(out["indices"].max()) + 1
+    return out
+
+
+def read_singular_values(prefix: str) -> np.ndarray:
+    """``CPP/io/matrix_reader.cpp:47-50``: ``<prefix>_singular_values.bin`` (float64), empty when the
+    file cannot be opened (``:55-59``)."""
+    try:
+        return np.fromfile(prefix + "_singular_values.bin", dtype=np.float64)
+    except OSError:
+        return np.empty(0)
+
+
 def _csr_values(Acsr: dict, pc: str):
     return {"double": Acsr["a_double"], "single": Acsr["a_single"], "half": Acsr["a_half"]}[pc]
 

@@ -1,8 +1,9 @@
 // Drop-in check: code written against the reference's C++ API (msvd::Matrix, hessenberg, syev,
-// sygv, si_eig, si_svd) compiles against include/msvd.hpp and runs on libofrr_gb300.so.
+// sygv, si_eig, si_svd, MatrixReader) compiles against include/msvd.hpp and runs on libofrr_gb300.so.
 // Prints one line per check; exits non-zero on the first failure.
 #include <cmath>
 #include <cstdio>
+#include <string>
 #include <vector>
 
 #include "msvd.hpp"
@@ -14,7 +15,7 @@ static int fail(const char* what) {
   return 1;
 }
 
-int main() {
+int main(int argc, char** argv) {
   CUDAHandler::init();
   // hessenberg_test.cpp:30-92 shape: A = QR and the duplicated-column skip pattern
   {
@@ -98,6 +99,50 @@ int main() {
     for (size_t i = 0; i < 4; ++i)
       if (std::fabs(S(i, i) - std::pow(0.8, (double)i)) > 1e-9) return fail("si_svd values");
     std::printf("si_svd ok S(1,1)=%.12f\n", S(1, 1));
+  }
+  // MatrixReader (matrix_reader.hpp:21-44): a diagonal CSR written to <argv[1]>_*.bin, read back,
+  // solved through the CSR overload of si_eig; the _singular_values file holds the spectrum
+  if (argc > 1) {
+    const std::string prefix = argv[1];
+    const int n = 120;
+    std::vector<int> ip(n + 1), ix(n);
+    std::vector<double> va(n), sv(n);
+    for (int i = 0; i < n; ++i) {
+      ip[i] = i;
+      ix[i] = i;
+      va[i] = sv[i] = std::pow(0.7, (double)i);
+    }
+    ip[n] = n;
+    auto put = [&](const char* suffix, const void* p, size_t bytes) {
+      FILE* f = std::fopen((prefix + suffix).c_str(), "wb");
+      if (!f) return false;
+      const bool ok = std::fwrite(p, 1, bytes, f) == bytes;
+      std::fclose(f);
+      return ok;
+    };
+    if (!put("_row_ptr.bin", ip.data(), ip.size() * 4) || !put("_col_ind.bin", ix.data(), ix.size() * 4) ||
+        !put("_values.bin", va.data(), va.size() * 8) || !put("_singular_values.bin", sv.data(), sv.size() * 8))
+      return fail("write csr files");
+    CSRMatrix m = MatrixReader::read_csr_matrix(prefix);
+    if (m.rows != n || m.cols != n || m.values != va || m.row_ptr != ip) return fail("read_csr_matrix");
+    std::vector<double> s = MatrixReader::read_singular_values(prefix);
+    if (s != sv) return fail("read_singular_values");
+    if (!MatrixReader::read_singular_values(prefix + "_missing").empty()) return fail("missing singular values");
+    bool threw = false;
+    try {
+      MatrixReader::read_csr_matrix(prefix + "_missing");
+    } catch (const std::runtime_error&) {
+      threw = true;
+    }
+    if (!threw) return fail("read_csr_matrix on a missing file");
+    CsrMatrix<double> A = to_device<double>(m, true);
+    Matrix<double> V(n, 12, Location::kDEVICE), D(12, 12, Location::kHOST);
+    V.fill_random(42);
+    MSVDStatus st = si_eig<double, double, double>(A, V, D, 200, 1e-10, true, 1e-10);
+    if (st != MSVDStatus::kSuccess) return fail("si_eig on the file operator");
+    for (int i = 0; i < 4; ++i)
+      if (std::fabs(D(i, i) - s[i]) > 1e-9) return fail("si_eig values on the file operator");
+    std::printf("MatrixReader ok rows=%d nnz=%zu D(0,0)=%.12f\n", m.rows, m.values.size(), D(0, 0));
   }
   CUDAHandler::finalize();
   std::printf("ALL OK\n");

@@ -22,6 +22,6 @@ def test_cpp_drop_in(built_lib, tmp_path):
            f"-Xlinker=-rpath,{built_lib.parent}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([str(exe), str(tmp_path / "diag")], capture_output=True, text=True, timeout=300)
     print(r.stdout)
-    assert r.returncode == 0 and "ALL OK" in r.stdout, r.stdout + r.stderr
+    assert r.returncode == 0 and "ALL OK" in r.stdout and "MatrixReader ok" in r.stdout, r.stdout + r.stderr
