@@ -45,6 +45,8 @@ def parse():
                     help="run one warm-up and one mixed solve only (for a profiler's launch list)")
     ap.add_argument("--roofline-only", action="store_true",
                     help="run only the live timing of the roofline kernel (for an ncu capture of it)")
+    ap.add_argument("--orth-compare", action="store_true",
+                    help="basis build and FP64 solve of the dense SVD with the Hessenberg, MGS and CGS bases")
     ap.add_argument("--csr-load", action="store_true",
                     help="time reading the 128^3 7-point CSR operator (on-disk format) into HBM")
     ap.add_argument("--mixed-config", default=None, metavar="B,S",
@@ -301,6 +303,42 @@ def profiled_traffic(name="k_sliced_tn_av_8192x64x2048.md"):
     return None
 
 
+def orth_compare_run(api, A, reps=3):
+    """The paper's comparison on the dense 8192 x 2048 problem: one basis build of an 8192 x 64 FP64 block
+    (scaled power iterate) with each basis, and the FP64-mode solve (top 32, residual <= 1e-8) with the
+    same basis for both blocks; CUDA events around each, median of reps."""
+    import torch
+
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        ts, out = [], None
+        for r in range(reps + 1):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts[1:])), out
+
+    X = api.scalecols(api.gemm(A, "N", api.randn(42, N_COLS, 64), "double", "double"), "double", "double")
+    res = {"orth_compare": True, "block": [M_ROWS, 64]}
+    for orth in ("hessenberg", "mgs", "cgs"):
+        if orth == "hessenberg":
+            ms_b, _ = timed(lambda: api.hessenberg(X, "double", "double"))
+        else:
+            ms_b, _ = timed(lambda: api.gs_basis(X, orth == "cgs", "double", "double"))
+        b, st = CFG.get("fp64", (BLOCK, STEP))
+        ms_s, out = timed(lambda: api.subspace_iter_svd(A, M_ROWS, N_COLS, b, "double", "double", maxiter=MAXITER,
+                                                        step_size=st, mode="fp64", tol=TOL, nev=NEV, orth=orth))
+        info = out[3]
+        res[orth] = {"basis_ms": ms_b, "fp64_solve_ms": ms_s, "iterations": info.iterations,
+                     "max_residual": info.max_residual, "status": info.status}
+    return res
+
+
 def csr_load_run(api, N=128, reps=3):
     """The on-disk CSR format (<prefix>_row_ptr.bin / _col_ind.bin / _values.bin) of a 7-point
     operator on an N^3 grid (n = 2,097,152 and nnz = 14,581,760 at N = 128, seeded values), written to
@@ -392,6 +430,9 @@ def main():
         print(json.dumps(csr_load_run(api)))
         return
     A, s_true = make_problem_gpu()
+    if args.orth_compare:
+        print(json.dumps(orth_compare_run(api, A)))
+        return
     if args.profile_solve:
         run_solver(api, A, "mixed")
         torch.cuda.synchronize()

@@ -18,6 +18,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -415,6 +416,53 @@ template <typename T_I, typename T_O, typename T_COMPUTE>
 std::vector<int> hessenberg_v3(const Matrix<T_I>& A, Matrix<T_O>& Q, Matrix<T_O>& R, T_O select_tol = T_O(-1.0),
                                T_O orth_tol = T_O(0.0), T_O reorth_tol = T_O(0.0)) {
   return hessenberg<T_I, T_O, T_COMPUTE>(A, Q, R, select_tol, orth_tol, reorth_tol);
+}
+
+// ---- orthogonal comparison bases (CPP/linalg/factorization/qr.hpp:21-132) -------------------------
+// mgs: MATLAB/+src/+qr/mgs.m with adaptive re-orthogonalisation; mgs_v2: one MGS pass (its
+// orth_tol / reorth_tol are placeholders in the reference, qr.hpp:33-41); cgs2: classical
+// Gram-Schmidt with the same re-orthogonalisation (cgs.m).  Defaults eps(T_O), eps(T_O), 1/sqrt(2);
+// a negative select_tol also selects eps(T_O).  Q on the device, R on the host, skip flags returned.
+namespace detail {
+template <typename T_I, typename T_O, typename T_COMPUTE>
+std::vector<int> gs(const Matrix<T_I>& A, Matrix<T_O>& Q, Matrix<T_O>& R, int classical, double select_tol,
+                    double orth_tol, double reorth_tol, const char* what) {
+  need(A, Location::kDEVICE, "Input matrix A");
+  need(Q, Location::kDEVICE, "Output matrix Q");
+  need(R, Location::kHOST, "Output matrix R");
+  const size_t m = A.rows(), n = A.cols();
+  if (Q.rows() != m || Q.cols() != n) throw std::runtime_error("Output matrix Q has incorrect dimensions");
+  if (R.rows() != n || R.cols() != n) throw std::runtime_error("Output matrix R has incorrect dimensions");
+  std::vector<double> Rh(n * n);
+  std::vector<int> skip(n);
+  const ofrr_dtype tc = std::is_same<T_COMPUTE, double>::value ? OFRR_F64 : OFRR_F32;
+  int s = ofrr_gs_basis(CUDAHandler::ctx(), classical, dt<T_I>(), dt<T_O>(), tc, (int64_t)m, (int64_t)n, A.data(),
+                        (int64_t)A.ld(), Q.data(), (int64_t)Q.ld(), select_tol, orth_tol, reorth_tol, Rh.data(),
+                        skip.data());
+  if (s != OFRR_SUCCESS) throw std::runtime_error(std::string(what) + ": " + ofrr_status_string(s));
+  for (size_t j = 0; j < n; ++j)
+    for (size_t i = 0; i < n; ++i) R(i, j) = (T_O)Rh[i + j * n];
+  return skip;
+}
+}  // namespace detail
+
+template <typename T_I, typename T_O, typename T_COMPUTE>
+std::vector<int> mgs(const Matrix<T_I>& A, Matrix<T_O>& Q, Matrix<T_O>& R, T_O select_tol = T_O(-1.0),
+                     T_O orth_tol = T_O(-1.0), T_O reorth_tol = T_O(0.70710678118654752)) {
+  const double ot = (double)orth_tol < 0 ? NAN : (double)orth_tol;
+  return detail::gs<T_I, T_O, T_COMPUTE>(A, Q, R, 0, (double)select_tol, ot, (double)reorth_tol, "mgs");
+}
+template <typename T_I, typename T_O, typename T_COMPUTE>
+std::vector<int> mgs_v2(const Matrix<T_I>& A, Matrix<T_O>& Q, Matrix<T_O>& R, T_O select_tol = T_O(-1.0),
+                        T_O orth_tol = T_O(-1.0), T_O reorth_tol = T_O(-1.0)) {
+  (void)orth_tol, (void)reorth_tol;
+  return detail::gs<T_I, T_O, T_COMPUTE>(A, Q, R, 0, (double)select_tol, NAN, -1.0, "mgs_v2");
+}
+template <typename T_I, typename T_O, typename T_COMPUTE>
+std::vector<int> cgs2(const Matrix<T_I>& A, Matrix<T_O>& Q, Matrix<T_O>& R, T_O select_tol = T_O(-1.0),
+                      T_O orth_tol = T_O(-1.0), T_O reorth_tol = T_O(0.70710678118654752)) {
+  const double ot = (double)orth_tol < 0 ? NAN : (double)orth_tol;
+  return detail::gs<T_I, T_O, T_COMPUTE>(A, Q, R, 1, (double)select_tol, ot, (double)reorth_tol, "cgs2");
 }
 
 template <typename T, typename T_O = T>

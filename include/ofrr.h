@@ -157,6 +157,19 @@ int ofrr_csrmm(ofrr_ctx* ctx, const ofrr_csr* A, int trans, ofrr_dtype tx, ofrr_
                ofrr_dtype ty, int64_t nrhs, const void* X /*dev*/, int64_t ldx,
                void* Y /*dev*/, int64_t ldy);
 
+/* Gram-Schmidt basis of A (m x n, m >= n): MATLAB/+src/+qr/mgs.m (classical = 0) or cgs.m
+ * (classical = 1), element arithmetic as those files (one rounding to tout per projection term, dots
+ * and norms in tcompute then rounded to tout; summation order of the dots is the GPU's), adaptive
+ * re-orthogonalisation while the norm stays at least orth_tol and drops below reorth_tol times the
+ * previous one (reorth_tol < 0: none), columns with a norm below select_tol dropped.  Defaults of the
+ * reference (qr.hpp:21-29): select_tol < 0 -> eps(tout); orth_tol NaN -> eps(tout); reorth_tol NaN
+ * -> 1/sqrt(2); all are rounded to tout.  Q (m x n) keeps the column positions, dropped columns zero;
+ * R_host (n*n, col-major) and skip_host (n) may be NULL.  Replaces msvd::mgs / mgs_v2 / cgs2
+ * (CPP/linalg/factorization/qr.hpp:21-132) for the comparison runs. */
+int ofrr_gs_basis(ofrr_ctx* ctx, int classical, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tcompute, int64_t m,
+                  int64_t n, const void* A /*dev*/, int64_t lda, void* Q /*dev*/, int64_t ldq, double select_tol,
+                  double orth_tol, double reorth_tol, double* R_host, int* skip_host);
+
 /* ---- on-disk CSR matrices (CPP/io/matrix_reader.cpp:8-50) -------------------------- *
  * <prefix>_row_ptr.bin (int32, nrows+1), <prefix>_col_ind.bin (int32, 0-based, nnz) and
  * <prefix>_values.bin (float64, nnz); element counts from the file sizes, ncols = largest column
@@ -208,7 +221,12 @@ typedef struct {
  * block on entry and the final Ritz vectors on exit; p_output then only selects the 16-bit working
  * precision of the mixed mode (OFRR_F16 or OFRR_BF16). */
 typedef enum { OFRR_MODE_REFERENCE = 0, OFRR_MODE_MIXED = 1, OFRR_MODE_FP64 = 2 } ofrr_mode;
-typedef enum { OFRR_ORTH_HESSENBERG = 0, OFRR_ORTH_MGS = 1 } ofrr_orth;
+/* Basis of a block: the Hessenberg process (orthogonalization-free, the default here); Gram-Schmidt
+ * QR as the orthogonal comparison -- modified (MATLAB/+src/+qr/mgs.m, the reference's default
+ * function_orth of subspace_iter_eig.m:114-115) or classical (cgs.m), both with the adaptive
+ * re-orthogonalisation of those files.  si_eig / si_svd accept all three; arnoldi_eig the first two
+ * (OFRR_ORTH_MGS there is the MGS Arnoldi of arnoldi_mgs_eig.m). */
+typedef enum { OFRR_ORTH_HESSENBERG = 0, OFRR_ORTH_MGS = 1, OFRR_ORTH_CGS = 2 } ofrr_orth;
 
 typedef struct {
   int mode;                /* ofrr_mode */

@@ -16,7 +16,7 @@ LIB_PATH = _PKG / "libofrr_gb300.so"
 F64, F32, F16, BF16 = 0, 1, 2, 3
 OP_DENSE, OP_CSR = 0, 1
 MODE_REFERENCE, MODE_MIXED, MODE_FP64 = 0, 1, 2
-ORTH_HESSENBERG, ORTH_MGS = 0, 1
+ORTH_HESSENBERG, ORTH_MGS, ORTH_CGS = 0, 1, 2
 
 SUCCESS = 0
 ERR_SOLVER_MAX_ITERATIONS = 4001
@@ -133,6 +133,8 @@ SIGNATURES = {
     "ofrr_ctx_trim": (C.c_int, [_P]),
     "ofrr_debug_bounded_wait": (C.c_int, [_P, _I64]),
     "ofrr_debug_scale_slice": (C.c_int, [_P, C.c_int, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _P]),
+    "ofrr_gs_basis": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _I64, _I64, _P, _I64, _P, _I64, _D, _D, _D,
+                                _DP, _IP]),
     "ofrr_csr_file_sizes": (C.c_int, [C.c_char_p, C.POINTER(_I64), C.POINTER(_I64)]),
     "ofrr_csr_file_read": (C.c_int, [_P, C.c_char_p, _I64, _I64, _P, _P, _P, C.POINTER(_I64), C.c_int]),
     "ofrr_read_singular_values": (C.c_int, [C.c_char_p, C.POINTER(_I64), _P]),

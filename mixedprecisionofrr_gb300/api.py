@@ -405,6 +405,31 @@ def sygv(A, B):
     return to_numpy(w), to_numpy(X)
 
 
+def gs_basis(A, classical: bool = False, precision_compute="double", precision_output=None, select_tol=None,
+             orth_tol=None, reorth_tol=None, precision_input=None):
+    """MATLAB/+src/+qr/mgs.m (classical=False) or cgs.m: returns (Q, R, skip) with Q on the device at
+    the input's column positions (dropped columns zero), R (n x n) and skip flags on the host."""
+    ctx = context()
+    pc = _p(precision_compute)
+    po = _p(precision_output or precision_compute)
+    pin = _p(precision_input) if precision_input else po
+    Ad = A if (is_cm(A) and dtype_of(A) == pin) else to_device_cm(A, pin)
+    m, n = Ad.shape
+    Q = empty_cm(m, n, po)
+    R = np.zeros(n * n)  # column-major from the library
+    skip = np.zeros(n, np.int32)
+    nan = float("nan")
+    L.check(ctx.lib.ofrr_gs_basis(ctx.h, int(classical), dtype_of(Ad), po, pc, m, n, Ad.data_ptr(), ld_of(Ad),
+                                  Q.data_ptr(), ld_of(Q), -1.0 if select_tol is None else select_tol,
+                                  nan if orth_tol is None else orth_tol, nan if reorth_tol is None else reorth_tol,
+                                  R.ctypes.data_as(C.POINTER(C.c_double)), skip.ctypes.data_as(C.POINTER(C.c_int))),
+            "gs_basis")
+    return Q, R.reshape((n, n), order="F"), skip
+
+
+ORTH = {"hessenberg": L.ORTH_HESSENBERG, "mgs": L.ORTH_MGS, "cgs": L.ORTH_CGS}
+
+
 # ---- solvers ------------------------------------------------------------------------------------
 def options(**kw) -> L.ofrr_options:
     o = L.ofrr_options()
@@ -481,15 +506,16 @@ def subspace_iter_eig(A, n: int, k: int, precision_compute="double", precision_o
                       maxiter: int = 5, step_size: int = 1, precision_hess_compute=None, precision_hess_output=None,
                       precision_rr_compute=None, precision_rr_output=None, use_generalized=True,
                       generalized_tol=0.0, select_tol=None, symmetric=None, V0=None, mode="reference",
-                      tol=0.0, nev=None, check_every=1):
-    """MATLAB/+src/+subspace/subspace_iter_eig.m; returns (V, d, info) with V on the device."""
+                      tol=0.0, nev=None, check_every=1, orth="hessenberg"):
+    """MATLAB/+src/+subspace/subspace_iter_eig.m; returns (V, d, info) with V on the device.  orth: the
+    basis ("hessenberg"; "mgs" = the MATLAB file's default function_orth; "cgs")."""
     ctx = context()
     op = operator(A, symmetric)
     modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
     o = options(mode=modes[mode], maxiter=maxiter, step_size=step_size, block=min(k, n), nev=nev or min(k, n),
                 tol=tol, use_generalized=int(use_generalized), generalized_tol=generalized_tol,
                 select_tol=-1.0 if select_tol is None else select_tol, seed=seed,
-                use_start_block=int(V0 is not None), check_every=check_every,
+                use_start_block=int(V0 is not None), check_every=check_every, orth=ORTH[orth],
                 **_prec_opts(precision_compute, precision_output, precision_hess_compute, precision_hess_output,
                              precision_rr_compute, precision_rr_output))
     po = o.p_output if mode == "reference" else L.F64
@@ -509,8 +535,9 @@ def subspace_iter_svd(A, m: int, n: int, k: int, precision_compute="double", pre
                       maxiter: int = 5, step_size: int = 1, precision_hess_compute=None, precision_hess_output=None,
                       precision_rr_compute=None, precision_rr_output=None, use_generalized=True,
                       generalized_tol=0.0, select_tol=None, V0=None, mode="reference", tol=0.0, nev=None,
-                      check_every=1):
-    """MATLAB/+src/+subspace/subspace_iter_svd.m; returns (U, s, V, info) with U, V on the device."""
+                      check_every=1, orth="hessenberg"):
+    """MATLAB/+src/+subspace/subspace_iter_svd.m; returns (U, s, V, info) with U, V on the device.  orth:
+    the basis of both blocks ("hessenberg", "mgs" or "cgs")."""
     ctx = context()
     op = operator(A, False)
     modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
@@ -518,7 +545,7 @@ def subspace_iter_svd(A, m: int, n: int, k: int, precision_compute="double", pre
     o = options(mode=modes[mode], maxiter=maxiter, step_size=step_size, block=b, nev=nev or b, tol=tol,
                 use_generalized=int(use_generalized), generalized_tol=generalized_tol,
                 select_tol=-1.0 if select_tol is None else select_tol, seed=seed,
-                use_start_block=int(V0 is not None), check_every=check_every,
+                use_start_block=int(V0 is not None), check_every=check_every, orth=ORTH[orth],
                 **_prec_opts(precision_compute, precision_output, precision_hess_compute, precision_hess_output,
                              precision_rr_compute, precision_rr_output))
     po = o.p_output if mode == "reference" else L.F64

@@ -7,6 +7,7 @@
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 #include <cublas_v2.h>
+#include <cmath>
 #include <cstdint>
 #include <cstddef>
 #include <cstdio>
@@ -470,10 +471,10 @@ int fill_zero(ofrr_ctx* ctx, void* p, size_t bytes);
 int hessenberg_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n,
                     const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev,
                     int* select_dev, int* perm_dev, bool fast = false);
-// MGS basis (orthogonal comparison path, MATLAB/+src/+qr/mgs.m)
-int mgs_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n,
-             const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev,
-             int* select_dev);
+// Gram-Schmidt bases (orthogonal comparison path): MATLAB/+src/+qr/mgs.m, or cgs.m when classical
+int gs_basis_impl(ofrr_ctx* ctx, bool classical, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m,
+                  int64_t n, const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev,
+                  int* select_dev, double orth_tol = NAN, double reorth_tol = NAN);
 
 // small dense FP64 solvers on device (one CTA); w ascending
 int syev_dev(ofrr_ctx* ctx, int n, double* A, int lda, double* w);

@@ -216,10 +216,24 @@ Precisions precisions_of(const ofrr_options* o) {
   return p;
 }
 
+// The basis of a block (the `function_orth` of subspace_iter_eig.m:65 / subspace_iter_svd.m): the
+// Hessenberg process (the orthogonalization-free default of this library), or a Gram-Schmidt QR --
+// mgs.m, the reference's own default (subspace_iter_eig.m:114-115), or cgs.m -- as the orthogonal
+// comparison.  Both leave Q at the input's column positions with select flags.
+int basis_impl(ofrr_ctx* ctx, int orth, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n,
+               const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R, int* sel, int* perm,
+               bool fast) {
+  if (orth == OFRR_ORTH_MGS || orth == OFRR_ORTH_CGS)
+    return gs_basis_impl(ctx, orth == OFRR_ORTH_CGS, tin, tout, tc, m, n, A, lda, Q, ldq, select_tol, R, sel);
+  return hessenberg_impl(ctx, tin, tout, tc, m, n, A, lda, Q, ldq, select_tol, R, sel, perm, fast);
+}
+
 int validate_options(const ofrr_options* o) {
   if (!o) return OFRR_ERR_INVALID_ARGUMENT;
   if (o->mode < 0 || o->mode > 2) return OFRR_ERR_INVALID_ARGUMENT;
   if (o->maxiter < 0 || o->step_size < 1 || o->block < 1 || o->nev < 0) return OFRR_ERR_INVALID_ARGUMENT;
+  if (o->orth != OFRR_ORTH_HESSENBERG && o->orth != OFRR_ORTH_MGS && o->orth != OFRR_ORTH_CGS)
+    return OFRR_ERR_INVALID_ARGUMENT;
   const int ps[6] = {o->p_compute, o->p_output, o->p_hess_compute, o->p_hess_output, o->p_rr_compute,
                      o->p_rr_output};
   for (int p : ps)
@@ -1135,7 +1149,8 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
     }
     ts.next(f64 ? "basis.f64" : "basis.16bit");
     // [Q,~] = hessenberg(V): the economic form drops deselected columns
-    OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, n, b, cur, ldcur, Q, n, opt->select_tol, R, sel, perm, P.fast));
+    OFRR_TRY(basis_impl(ctx, opt->orth, P.po, P.pho, P.phc, n, b, cur, ldcur, Q, n, opt->select_tol, R, sel, perm,
+                        P.fast));
     OFRR_CUDA(cudaMemcpyAsync(hsel.data(), sel, sizeof(int) * b, cudaMemcpyDeviceToHost, ctx->stream));
     OFRR_TRY(sync_and_check(ctx));
     int w = b;
@@ -1278,9 +1293,10 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
       TraceScope ts(ctx, f64 ? "basis.f64" : "basis.16bit");
       ofrr_ctx* aux = nullptr;
       OFRR_TRY(aux_begin(ctx, &aux));
-      OFRR_TRY(hessenberg_impl(aux, P.po, P.pho, P.phc, n, b, V, ldv, Q1, n, opt->select_tol, R2, sel + b0, perm2,
-                               P.fast));
-      OFRR_TRY(hessenberg_impl(ctx, P.po, P.pho, P.phc, m, b, U, ldu, P1, m, opt->select_tol, R, sel, perm, P.fast));
+      OFRR_TRY(basis_impl(aux, opt->orth, P.po, P.pho, P.phc, n, b, V, ldv, Q1, n, opt->select_tol, R2, sel + b0,
+                          perm2, P.fast));
+      OFRR_TRY(basis_impl(ctx, opt->orth, P.po, P.pho, P.phc, m, b, U, ldu, P1, m, opt->select_tol, R, sel, perm,
+                          P.fast));
       OFRR_TRY(aux_end(ctx));
       OFRR_CUDA(cudaMemcpyAsync(hsel.data(), sel, sizeof(int) * 2 * b0, cudaMemcpyDeviceToHost, ctx->stream));
       OFRR_TRY(sync_and_check(ctx));

@@ -319,27 +319,70 @@ def hessenberg_economic(A, pc="double", po=None, select_tol=None):
     return Q[:, select], R[select, :]
 
 
-def mgs(A, pc: str = "double", po: Optional[str] = None, select_tol: Optional[float] = None):
-    """Orthogonal comparison basis, following ``+src/+qr/mgs.m`` (2-norm scaling)."""
+def _orth_gs(A, classical: bool, pc: str, po: Optional[str], select_tol, orth_tol, reorth_tol):
+    """Shared body of ``+src/+qr/mgs.m:49-101`` (classical=False) and ``+src/+qr/cgs.m:49-110``
+    (classical=True).  Column i: ``normv = norm2(v)``; below select_tol the column is dropped;
+    projections against the selected earlier columns (MGS: dot then update per j; CGS: all dots,
+    then the updates in j order); then, while ``t = norm2(v)`` is at least orth_tol and below
+    reorth_tol * normv, one more projection pass accumulated into R; finally v / t, R(i,i) = t, or
+    the column is dropped when t < select_tol."""
     po = po or pc
     A = _cast(A, po)
     m, n = A.shape
-    st = eps(po) if select_tol is None else select_tol
+    assert m >= n, "A must be a tall-thin matrix"
+    e = eps(po)
+    stol = e if select_tol is None else float(_cast(select_tol, po))
+    otol = e if orth_tol is None else float(_cast(orth_tol, po))
+    rtol = float(1.0 / np.sqrt(2.0)) if reorth_tol is None else float(_cast(reorth_tol, po))
     Q = np.zeros((m, n), dtype=_dt(po))
     R = np.zeros((n, n), dtype=_dt(po))
     select = np.ones(n, dtype=bool)
+
+    def project(v, rcol, accumulate):
+        js = [j for j in range(i) if select[j]]
+        if classical:
+            r = {j: dot(v, Q[:, j], pc, po) for j in js}
+        for j in js:
+            rj = r[j] if classical else dot(v, Q[:, j], pc, po)
+            v = _cast(_cast(v, pc) - _cast(rj, pc) * _cast(Q[:, j], pc), po)
+            rcol[j] = _cast(_cast(rcol[j], pc) + _cast(rj, pc), po) if accumulate else rj
+        return v
+
     for i in range(n):
         v = A[:, i].copy()
-        for j in range(i):
-            if select[j]:
-                R[j, i] = dot(Q[:, j], v, pc, po)
-                v = _cast(_cast(v, pc) - _cast(R[j, i], pc) * _cast(Q[:, j], pc), po)
-        R[i, i] = norm2(v, pc, po)
-        if float(R[i, i]) < st:
+        normv = float(norm2(v, pc, po))
+        if normv < stol:
+            select[i] = False
+            continue
+        rcol = R[:, i]
+        v = project(v, rcol, False)
+        t = float(norm2(v, pc, po))
+        while rtol >= 0 and (t >= otol and t < rtol * normv):
+            normv = t
+            v = project(v, rcol, True)
+            t = float(norm2(v, pc, po))
+        if t < stol:
             select[i] = False
         else:
-            Q[:, i] = _cast(_cast(v, pc) / _cast(R[i, i], pc), po)
-    return Q[:, select], R[select, :]
+            Q[:, i] = _cast(_cast(v, pc) / _cast(t, pc), po)
+            R[i, i] = t
+    return Q, R, select
+
+
+def mgs(A, pc: str = "double", po: Optional[str] = None, select_tol: Optional[float] = None,
+        orth_tol: Optional[float] = None, reorth_tol: Optional[float] = None, full: bool = False):
+    """Orthogonal comparison basis, ``+src/+qr/mgs.m`` (the default ``function_orth`` of
+    ``subspace_iter_eig.m:114-115``).  Returns ``(Q(:,select), R(select,:))`` as the two-output form
+    (``mgs.m:103-105``), or ``(Q, R, select)`` with ``full``."""
+    Q, R, select = _orth_gs(A, False, pc, po, select_tol, orth_tol, reorth_tol)
+    return (Q, R, select) if full else (Q[:, select], R[select, :])
+
+
+def cgs(A, pc: str = "double", po: Optional[str] = None, select_tol: Optional[float] = None,
+        orth_tol: Optional[float] = None, reorth_tol: Optional[float] = None, full: bool = False):
+    """Classical Gram-Schmidt with the same adaptive re-orthogonalisation, ``+src/+qr/cgs.m``."""
+    Q, R, select = _orth_gs(A, True, pc, po, select_tol, orth_tol, reorth_tol)
+    return (Q, R, select) if full else (Q[:, select], R[select, :])
 
 
 # --------------------------------------------------------------------------------------
@@ -477,10 +520,7 @@ def subspace_iter_eig(A, n: int, k: int, pc: str = "double", po: Optional[str] =
         for _ in range(step_size):
             V = matvec_auto(A, "N", V, pc, po)
             V = scalecols(V, pc, po)
-        if orth == "hessenberg":
-            Q, _ = hessenberg_economic(V, ph_c, ph_o, select_tol)
-        else:
-            Q, _ = mgs(V, ph_c, ph_o, select_tol)
+        Q = _basis(V, orth, ph_c, ph_o, select_tol)
         V, d = eig_rr(A, Q, prr_c, prr_o, pc, po, peig, use_generalized, generalized_tol, symmetric)
         V = _cast(V, po)
         if callback is not None:
@@ -488,8 +528,18 @@ def subspace_iter_eig(A, n: int, k: int, pc: str = "double", po: Optional[str] =
     return V, d
 
 
+def _basis(V, orth: str, ph_c: str, ph_o: str, select_tol):
+    """``function_orth`` of ``subspace_iter_eig.m:65``: hessenberg (the orthogonalization-free runs),
+    mgs (the file's default, ``:114-115``) or cgs; the two-output (economic) form."""
+    if orth == "hessenberg":
+        return hessenberg_economic(V, ph_c, ph_o, select_tol)[0]
+    if orth == "cgs":
+        return cgs(V, ph_c, ph_o, select_tol)[0]
+    return mgs(V, ph_c, ph_o, select_tol)[0]
+
+
 def subspace_iter_svd(A, m: int, n: int, k: int, pc: str = "double", po: Optional[str] = None,
-                      seed: int = 42, maxiter: int = 5, step_size: int = 1,
+                      seed: int = 42, maxiter: int = 5, step_size: int = 1, orth: str = "hessenberg",
                       ph_c: Optional[str] = None, ph_o: Optional[str] = None,
                       prr_c: Optional[str] = None, prr_o: Optional[str] = None, peig: str = "double",
                       use_generalized: bool = True, generalized_tol: float = 0.0,
@@ -515,8 +565,8 @@ def subspace_iter_svd(A, m: int, n: int, k: int, pc: str = "double", po: Optiona
             U = scalecols(U, pc, po)
             V = matvec_auto(A, "T", U, pc, po)
             V = scalecols(V, pc, po)
-        P, _ = hessenberg_economic(U, ph_c, ph_o, select_tol)
-        Q, _ = hessenberg_economic(V, ph_c, ph_o, select_tol)
+        P = _basis(U, orth, ph_c, ph_o, select_tol)
+        Q = _basis(V, orth, ph_c, ph_o, select_tol)
         U, s, V = svd_rr(A, P, Q, prr_c, prr_o, pc, po, peig, use_generalized, generalized_tol)
         U = _cast(U, po)
         V = _cast(V, po)

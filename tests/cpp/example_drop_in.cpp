@@ -100,6 +100,24 @@ int main(int argc, char** argv) {
       if (std::fabs(S(i, i) - std::pow(0.8, (double)i)) > 1e-9) return fail("si_svd values");
     std::printf("si_svd ok S(1,1)=%.12f\n", S(1, 1));
   }
+  // mgs / cgs2 (qr.hpp:21-132): columns 3..5 duplicate 0..2 and are skipped; A = QR
+  {
+    const size_t m = 300, n = 20;
+    Matrix<double> A(m, n, Location::kHOST);
+    for (size_t j = 0; j < n; ++j)
+      for (size_t i = 0; i < m; ++i) A(i, j) = std::sin(0.37 * (double)(i + 1) * (double)(j % 17 + 1) + 0.1 * j);
+    for (size_t j = 3; j < 6; ++j)
+      for (size_t i = 0; i < m; ++i) A(i, j) = A(i, j - 3);
+    A.to_device();
+    for (int variant = 0; variant < 2; ++variant) {
+      Matrix<double> Q(m, n, Location::kDEVICE), R(n, n, Location::kHOST);
+      std::vector<int> skip = variant == 0 ? mgs<double, double, double>(A, Q, R, 1e-12)
+                                           : cgs2<double, double, double>(A, Q, R, 1e-12);
+      for (size_t j = 0; j < n; ++j)
+        if (skip[j] != (j >= 3 && j <= 5 ? 1 : 0)) return fail("gram-schmidt skip pattern");
+    }
+    std::printf("mgs/cgs2 ok\n");
+  }
   // MatrixReader (matrix_reader.hpp:21-44): a diagonal CSR written to <argv[1]>_*.bin, read back,
   // solved through the CSR overload of si_eig; the _singular_values file holds the spectrum
   if (argc > 1) {

@@ -150,3 +150,25 @@ def test_golden_regression():
     _, _, sel, _ = orc.hessenberg(g["hess_dup_A"], "single", "half", select_tol=1e-2)
     assert np.array_equal(sel, g["hess_dup_sel"])
     assert np.array_equal(orc.scalecols(g["scal_U"], "single", "half"), g["scal_out"])
+
+
+@pytest.mark.parametrize("classical", [False, True])
+@pytest.mark.parametrize("p,tol,stol", [("double", 1e-10, 1e-12), ("single", 2e-6, 1e-6)])
+def test_oracle_gram_schmidt_reference_contract(classical, p, tol, stol):
+    """mgs.m / cgs.m restated: the checks of CPP/tests/qr_test.cpp:30-118 (uniform random 2000 x 200:
+    Q'Q = I and A = QR within tol; columns 3..5 duplicating 0..2 are skipped, and the skipped
+    columns' projections kept in R still give A = QR)."""
+    from oracle import ofrr_oracle as o
+
+    rng = np.random.default_rng(7)
+    A = rng.uniform(0, 1, (2000, 200)).astype(o._dt(p))
+    f = o.cgs if classical else o.mgs
+    Q, R, sel = f(A, p, p, full=True)
+    Qd, Rd = Q.astype(np.float64), R.astype(np.float64)
+    assert sel.all()
+    assert np.max(np.abs(Qd.T @ Qd - np.eye(200))) < tol
+    assert np.max(np.abs(A - Qd @ Rd)) < tol
+    A[:, 3:6] = A[:, 0:3]
+    Q, R, sel = f(A, p, p, select_tol=stol, full=True)
+    assert [i for i in range(200) if not sel[i]] == [3, 4, 5]
+    assert np.max(np.abs(A - Q.astype(np.float64) @ R.astype(np.float64))) < tol
