@@ -47,6 +47,8 @@ def parse():
                     help="run only the live timing of the roofline kernel (for an ncu capture of it)")
     ap.add_argument("--orth-compare", action="store_true",
                     help="basis build and FP64 solve of the dense SVD with the Hessenberg, MGS and CGS bases")
+    ap.add_argument("--kernel-gen", action="store_true",
+                    help="time the Gaussian kernel generator (16384 points in 3D) against the HBM peak")
     ap.add_argument("--csr-load", action="store_true",
                     help="time reading the 128^3 7-point CSR operator (on-disk format) into HBM")
     ap.add_argument("--mixed-config", default=None, metavar="B,S",
@@ -339,6 +341,41 @@ def orth_compare_run(api, A, reps=3):
     return res
 
 
+def measured_hbm_peak():
+    pk = ROOT / "MEASURED_PEAKS.json"
+    return json.loads(pk.read_text()).get("hbm_gbs") if pk.exists() else None
+
+
+def kernel_gen_run(api, n=16384, d=3, reps=5):
+    """generate_gaussian_kernel's matrix for n points in [0, n^(1/3))^3 (the largest dense size of the
+    serving mix), one launch writing n^2 entries: CUDA events, median of reps, HBM-write rate against
+    the measured copy peak."""
+    import torch
+    from mixedprecisionofrr_gb300 import _lib as L
+
+    ctx = api.context()
+    X = api.rand_points(1, n, d, 0)
+    out = {"kernel_gen": True, "n": n, "d": d}
+    peak = measured_hbm_peak()
+    for prec, code, es in (("double", L.F64, 8), ("single", L.F32, 4), ("half", L.F16, 2)):
+        K = api.empty_cm(n, n, code)
+        ts = []
+        for r in range(reps + 1):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            L.check(ctx.lib.ofrr_gaussian_kernel(ctx.h, 0, n, n, d, X.data_ptr(), n, X.data_ptr(), n, 1.0, 1.0, 0.1,
+                                                 code, K.data_ptr(), n), "gaussian_kernel")
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ms = float(np.median(ts[1:]))
+        gbs = n * n * es / ms / 1e6
+        out[prec] = {"ms": ms, "write_GBps": gbs, "frac_of_hbm_peak": gbs / peak if peak else None}
+        del K
+    return out
+
+
 def csr_load_run(api, N=128, reps=3):
     """The on-disk CSR format (<prefix>_row_ptr.bin / _col_ind.bin / _values.bin) of a 7-point
     operator on an N^3 grid (n = 2,097,152 and nnz = 14,581,760 at N = 128, seeded values), written to
@@ -425,6 +462,9 @@ def main():
         dt_g, bytes_g, flops_g = gemm_roofline(api)
         print(json.dumps({"roofline_only": True, "k_sliced_tn_us": dt_s * 1e6, "k_sliced_tn_GBps": bytes_s / dt_s / 1e9,
                           "k_gemm_tn_us": dt_g * 1e6, "k_gemm_tn_GBps": bytes_g / dt_g / 1e9}))
+        return
+    if args.kernel_gen:
+        print(json.dumps(kernel_gen_run(api)))
         return
     if args.csr_load:
         print(json.dumps(csr_load_run(api)))

@@ -723,4 +723,27 @@ CsrMatrix<T> to_device(const CSRMatrix& m, bool symmetric) {
   return CsrMatrix<T>((size_t)m.rows, (size_t)m.cols, m.row_ptr, m.col_ind, m.values, symmetric);
 }
 
+// ---- test problems (CPP/testproblems/gaussian_kernel.hpp:14-77) -------------------------------------
+// Gaussian kernel of n points uniform in [0, n^(1/d))^d, computed on the GPU in FP64 and rounded to T;
+// returned on the host as the reference does.  The points come from the library's seeded counter-based
+// generator (the reference's host generator cannot be reproduced), so the same seed gives the same
+// matrix as api.generate_gaussian_kernel, not as the reference.
+template <typename T>
+Matrix<T> generate_gaussian_kernel(double f, double l, double s, unsigned long long seed, int n, int d) {
+  if (l <= 0.0) throw std::invalid_argument("Length scale l must be positive");
+  if (s < 0.0) throw std::invalid_argument("Noise scale s must be non-negative");
+  if (n <= 0 || d <= 0) throw std::invalid_argument("Data dimensions must be positive");
+  Matrix<double> X((size_t)n, (size_t)d, Location::kDEVICE);
+  Matrix<T> K((size_t)n, (size_t)n, Location::kDEVICE);
+  ofrr_ctx* ctx = CUDAHandler::ctx();
+  int st = ofrr_rand_points(ctx, (uint64_t)seed, n, d, 0, X.data(), (int64_t)X.ld());
+  if (st == OFRR_SUCCESS)
+    st = ofrr_gaussian_kernel(ctx, 0, n, n, d, X.data(), (int64_t)X.ld(), X.data(), (int64_t)X.ld(), l, f, s,
+                              detail::dt<T>(), K.data(), (int64_t)K.ld());
+  if (st == OFRR_SUCCESS) st = ofrr_ctx_synchronize(ctx);
+  if (st != OFRR_SUCCESS) throw std::runtime_error(std::string("generate_gaussian_kernel: ") + ofrr_status_string(st));
+  K.to_host();
+  return K;
+}
+
 }  // namespace msvd

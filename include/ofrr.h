@@ -170,6 +170,21 @@ int ofrr_gs_basis(ofrr_ctx* ctx, int classical, ofrr_dtype tin, ofrr_dtype tout,
                   int64_t n, const void* A /*dev*/, int64_t lda, void* Q /*dev*/, int64_t ldq, double select_tol,
                   double orth_tol, double reorth_tol, double* R_host, int* skip_host);
 
+/* ---- test-problem generators (CPP/testproblems/gaussian_kernel.hpp, MATLAB/+src/+kernel) ---- *
+ * ofrr_rand_points: n points (X: n x d, FP64, device) of generate_pts.m's types 20 (square), 30 (cube),
+ * 21 (disk), 22 (circle), 23 (grid, n a square), 31 (ball), 32 (sphere), or type 0: the uniform box
+ * [0, n^(1/d))^d of generate_gaussian_kernel for any d.  Uniform draws from the library's counter-based
+ * generator (splitmix64 of the seed-keyed element counter; the reference's std / MATLAB generators
+ * cannot be reproduced).  ofrr_gaussian_kernel: K (m x n, tout, device) in FP64 then rounded once;
+ * form 0 = generate_gaussian_kernel (gaussian_kernel.hpp:14-77; X == Y, m == n; diagonal
+ * f^2 (1 + s^2), off-diagonal f^2 exp(-|x_i - x_j|^2 / (2 l^2)), 0 below exp(-700)); form 1 =
+ * gaussian.m:21-27 (K(X, Y) = f^2 exp(-D2 / (2 l^2)) + s^2 eye, D2 = -2 X Y' + |x|^2 + |y|^2).
+ * l <= 0, s < 0, non-positive sizes: OFRR_ERR_INVALID_ARGUMENT (the reference throws). */
+int ofrr_rand_points(ofrr_ctx* ctx, uint64_t seed, int64_t n, int d, int type, double* X /*dev*/, int64_t ldx);
+int ofrr_gaussian_kernel(ofrr_ctx* ctx, int form, int64_t m, int64_t n, int d, const double* X /*dev*/, int64_t ldx,
+                         const double* Y /*dev*/, int64_t ldy, double l, double f, double s, ofrr_dtype tout,
+                         void* K /*dev*/, int64_t ldk);
+
 /* ---- on-disk CSR matrices (CPP/io/matrix_reader.cpp:8-50) -------------------------- *
  * <prefix>_row_ptr.bin (int32, nrows+1), <prefix>_col_ind.bin (int32, 0-based, nnz) and
  * <prefix>_values.bin (float64, nnz); element counts from the file sizes, ncols = largest column

@@ -135,6 +135,9 @@ SIGNATURES = {
     "ofrr_debug_scale_slice": (C.c_int, [_P, C.c_int, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _P]),
     "ofrr_gs_basis": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _I64, _I64, _P, _I64, _P, _I64, _D, _D, _D,
                                 _DP, _IP]),
+    "ofrr_rand_points": (C.c_int, [_P, C.c_uint64, _I64, C.c_int, C.c_int, _P, _I64]),
+    "ofrr_gaussian_kernel": (C.c_int, [_P, C.c_int, _I64, _I64, C.c_int, _P, _I64, _P, _I64, _D, _D, _D, C.c_int, _P,
+                                       _I64]),
     "ofrr_csr_file_sizes": (C.c_int, [C.c_char_p, C.POINTER(_I64), C.POINTER(_I64)]),
     "ofrr_csr_file_read": (C.c_int, [_P, C.c_char_p, _I64, _I64, _P, _P, _P, C.POINTER(_I64), C.c_int]),
     "ofrr_read_singular_values": (C.c_int, [C.c_char_p, C.POINTER(_I64), _P]),

@@ -223,6 +223,42 @@ def read_csr(prefix: str, symmetric: Optional[bool] = None, on_device: bool = Tr
                      symmetric)
 
 
+def rand_points(seed: int, n: int, d: int, type: int = 0):
+    """n x d point set on the device (MATLAB/+src/+kernel/generate_pts.m types 20/21/22/23/30/31/32, or
+    type 0: the uniform box of CPP/testproblems/gaussian_kernel.hpp:36-40), FP64, column-major."""
+    ctx = context()
+    X = empty_cm(n, d, L.F64)
+    L.check(ctx.lib.ofrr_rand_points(ctx.h, seed, n, d, type, X.data_ptr(), ld_of(X)), "rand_points")
+    return X
+
+
+def gaussian(X, Y, l: float, f: float, s: float, precision_output="double"):
+    """MATLAB/+src/+kernel/gaussian.m: K(X, Y) = f^2 exp(-D2 / (2 l^2)) + s^2 eye on the device."""
+    ctx = context()
+    Xd = X if (is_cm(X) and dtype_of(X) == L.F64) else to_device_cm(X, L.F64)
+    Yd = Y if (is_cm(Y) and dtype_of(Y) == L.F64) else to_device_cm(Y, L.F64)
+    po = _p(precision_output)
+    K = empty_cm(Xd.shape[0], Yd.shape[0], po)
+    L.check(ctx.lib.ofrr_gaussian_kernel(ctx.h, 1, Xd.shape[0], Yd.shape[0], Xd.shape[1], Xd.data_ptr(), ld_of(Xd),
+                                         Yd.data_ptr(), ld_of(Yd), l, f, s, po, K.data_ptr(), ld_of(K)), "gaussian")
+    return K
+
+
+def generate_gaussian_kernel(f: float, l: float, s: float, seed: int, n: int, d: int, precision="double"):
+    """CPP/testproblems/gaussian_kernel.hpp:14-77 on the device: points uniform in [0, n^(1/d))^d (seeded
+    counter-based draws), K = f^2 (1 + s^2) on the diagonal, f^2 exp(-|x_i - x_j|^2 / (2 l^2)) off it;
+    returns (K, X) on the device.  Raises OfrrError (INVALID_ARGUMENT) where the reference throws."""
+    ctx = context()
+    if not (l > 0 and s >= 0 and n > 0 and d > 0):
+        L.check(1000, "generate_gaussian_kernel")  # OFRR_ERR_INVALID_ARGUMENT
+    X = rand_points(seed, n, d, 0)
+    po = _p(precision)
+    K = empty_cm(n, n, po)
+    L.check(ctx.lib.ofrr_gaussian_kernel(ctx.h, 0, n, n, d, X.data_ptr(), ld_of(X), X.data_ptr(), ld_of(X), l, f, s,
+                                         po, K.data_ptr(), ld_of(K)), "generate_gaussian_kernel")
+    return K, X
+
+
 def read_singular_values(prefix: str) -> np.ndarray:
     """CPP/io/matrix_reader.cpp:47-50: <prefix>_singular_values.bin (float64); empty when the file is
     missing or unreadable, as in the reference."""

@@ -199,6 +199,60 @@ def sparse2csr(A) -> dict:
     }
 
 
+def rand_uniform(seed: int, count: int) -> np.ndarray:
+    """The library's uniform draws u(e) = (splitmix64(splitmix64(seed) + e) >> 11) 2^-53, e = 0..count-1
+    (stands in for the reference's std / MATLAB ``rand``, which cannot be reproduced)."""
+    key = _splitmix64(np.array([seed], dtype=np.uint64))[0]
+    with np.errstate(over="ignore"):
+        h = _splitmix64(key + np.arange(count, dtype=np.uint64))
+    return (h >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+
+
+def rand_points(seed: int, n: int, d: int, type: int = 0) -> np.ndarray:
+    """``+src/+kernel/generate_pts.m`` (types 20, 21, 22, 23, 30, 31, 32) and the uniform box of
+    ``CPP/testproblems/gaussian_kernel.hpp:36-40`` (type 0); draw j of a point i is u(i + n j)."""
+    u = rand_uniform(seed, max(d, 3) * n).reshape(max(d, 3), n)
+    if type in (0, 20, 30):
+        return (n ** (1.0 / d)) * u[:d].T
+    if type in (21, 22):
+        theta = 2 * math.pi * u[0]
+        r = (n / math.pi) ** 0.5 * np.sqrt(u[1]) if type == 21 else n / 2 / math.pi
+        return np.stack([r * np.sin(theta), r * np.cos(theta)], axis=1)
+    if type == 23:
+        nx = int(round(math.sqrt(n)))
+        i = np.arange(n)
+        return np.stack([i % nx + 1, i // nx + 1], axis=1).astype(np.float64)
+    el = np.arcsin(2.0 * u[0] - 1.0)
+    az = 2 * math.pi * u[1]
+    r = (3 * n / 4 / math.pi) ** (1.0 / 3) * np.cbrt(u[2]) if type == 31 else (n / 4 / math.pi) ** 0.5
+    rc = r * np.cos(el)
+    return np.stack([rc * np.cos(az), rc * np.sin(az), r * np.sin(el)], axis=1)
+
+
+def generate_gaussian_kernel(f: float, l: float, s: float, X: np.ndarray) -> np.ndarray:
+    """``CPP/testproblems/gaussian_kernel.hpp:14-77`` on given points: diagonal f^2 (1 + s^2), off the
+    diagonal f^2 exp(-|x_i - x_j|^2 / (2 l^2)) with the squared distance summed in coordinate order,
+    0 where the exponent is below -700."""
+    if l <= 0 or s < 0:
+        raise ValueError("invalid parameters (gaussian_kernel.hpp:18-29)")
+    n, d = X.shape
+    dist = np.zeros((n, n))
+    for k in range(d):
+        diff = X[:, k][:, None] - X[:, k][None, :]
+        dist = dist + diff * diff
+    arg = -dist / (2.0 * l * l)
+    K = np.where(arg < -700.0, 0.0, np.exp(arg)) * (f * f)
+    np.fill_diagonal(K, (1.0 + s * s) * (f * f))
+    return K
+
+
+def gaussian(X, Y, l: float, f: float, s: float) -> np.ndarray:
+    """``+src/+kernel/gaussian.m:21-27``."""
+    XY = X @ Y.T
+    D2 = (-2 * XY + np.sum(X ** 2, 1)[:, None]) + np.sum(Y ** 2, 1)[None, :]
+    return f ** 2 * np.exp(-D2 / (2 * l ** 2)) + s ** 2 * np.eye(X.shape[0], Y.shape[0])
+
+
 def read_csr_matrix(prefix: str) -> dict:
     """``CPP/io/matrix_reader.cpp:8-45`` (MatrixReader::read_csr_matrix): ``<prefix>_row_ptr.bin``
     (int32), ``_col_ind.bin`` (int32, 0-based), ``_values.bin`` (float64), counts from the file sizes,

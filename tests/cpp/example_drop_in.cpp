@@ -118,6 +118,29 @@ int main(int argc, char** argv) {
     }
     std::printf("mgs/cgs2 ok\n");
   }
+  // generate_gaussian_kernel (gaussian_kernel.hpp:14-77): symmetric, diagonal f^2 (1 + s^2), entries in
+  // [0, f^2]; invalid parameters throw std::invalid_argument
+  {
+    const double f = 1.5, l = 2.0, s = 0.1;
+    Matrix<double> K = generate_gaussian_kernel<double>(f, l, s, 42, 10, 3);
+    if (K.rows() != 10 || K.cols() != 10 || K.location() != Location::kHOST) return fail("kernel shape");
+    for (int i = 0; i < 10; ++i)
+      for (int j = 0; j < 10; ++j) {
+        if (K(i, j) != K(j, i)) return fail("kernel symmetry");
+        if (i == j && K(i, i) != f * f * (1.0 + s * s)) return fail("kernel diagonal");
+        if (i != j && !(K(i, j) >= 0.0 && K(i, j) <= f * f)) return fail("kernel range");
+      }
+    bool threw = false;
+    try {
+      generate_gaussian_kernel<double>(1.0, 0.0, 0.1, 42, 10, 3);
+    } catch (const std::invalid_argument&) {
+      threw = true;
+    }
+    if (!threw) return fail("kernel invalid length scale");
+    Matrix<float> Kf = generate_gaussian_kernel<float>(1.0, 1.0, 0.05, 123, 5, 2);
+    if (Kf(0, 0) != (float)(1.0 * 1.0 * (1.0 + 0.05 * 0.05))) return fail("float kernel diagonal");
+    std::printf("generate_gaussian_kernel ok K(0,1)=%.12f\n", K(0, 1));
+  }
   // MatrixReader (matrix_reader.hpp:21-44): a diagonal CSR written to <argv[1]>_*.bin, read back,
   // solved through the CSR overload of si_eig; the _singular_values file holds the spectrum
   if (argc > 1) {
