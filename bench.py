@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--roofline-only", action="store_true",
                     help="run only the live timing of the roofline kernel (for an ncu capture of it)")
     ap.add_argument("--orth-compare", action="store_true",
-                    help="basis build and FP64 solve of the dense SVD with the Hessenberg, MGS and CGS bases")
+                    help="basis build and FP64 solve of the dense SVD with the Hessenberg, LU, MGS and CGS bases")
     ap.add_argument("--kernel-gen", action="store_true",
                     help="time the Gaussian kernel generator (16384 points in 3D) against the HBM peak")
     ap.add_argument("--csr-load", action="store_true",
@@ -327,9 +327,11 @@ def orth_compare_run(api, A, reps=3):
 
     X = api.scalecols(api.gemm(A, "N", api.randn(42, N_COLS, 64), "double", "double"), "double", "double")
     res = {"orth_compare": True, "block": [M_ROWS, 64]}
-    for orth in ("hessenberg", "mgs", "cgs"):
+    for orth in ("hessenberg", "lu", "mgs", "cgs"):
         if orth == "hessenberg":
             ms_b, _ = timed(lambda: api.hessenberg(X, "double", "double"))
+        elif orth == "lu":
+            ms_b, _ = timed(lambda: api.lu_basis(X, "double", "double"))
         else:
             ms_b, _ = timed(lambda: api.gs_basis(X, orth == "cgs", "double", "double"))
         b, st = CFG.get("fp64", (BLOCK, STEP))

@@ -185,6 +185,16 @@ int ofrr_gaussian_kernel(ofrr_ctx* ctx, int form, int64_t m, int64_t n, int d, c
                          const double* Y /*dev*/, int64_t ldy, double l, double f, double s, ofrr_dtype tout,
                          void* K /*dev*/, int64_t ldk);
 
+/* Column-pivoted LU basis of A (m x n, m >= n), MATLAB/+src/+qr/lu.m:47-94: right-looking with the
+ * rows swapped in place (pivot = first maximum of |A_work(j:m, j)| in the current row order), a
+ * column whose maximum is below select_tol dropped (its row consumed; select_tol < 0: eps(tout)),
+ * arithmetic in tcompute rounded to tout per operation as lu.m does.  Q (m x n) = the un-permuted L
+ * (lu.m's two-output form before the column selection), dropped columns zero; U_host (n*n) and
+ * skip_host (n) may be NULL. */
+int ofrr_lu_basis(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tcompute, int64_t m, int64_t n,
+                  const void* A /*dev*/, int64_t lda, void* Q /*dev*/, int64_t ldq, double select_tol, double* U_host,
+                  int* skip_host);
+
 /* ---- on-disk CSR matrices (CPP/io/matrix_reader.cpp:8-50) -------------------------- *
  * <prefix>_row_ptr.bin (int32, nrows+1), <prefix>_col_ind.bin (int32, 0-based, nnz) and
  * <prefix>_values.bin (float64, nnz); element counts from the file sizes, ncols = largest column
@@ -239,9 +249,10 @@ typedef enum { OFRR_MODE_REFERENCE = 0, OFRR_MODE_MIXED = 1, OFRR_MODE_FP64 = 2 
 /* Basis of a block: the Hessenberg process (orthogonalization-free, the default here); Gram-Schmidt
  * QR as the orthogonal comparison -- modified (MATLAB/+src/+qr/mgs.m, the reference's default
  * function_orth of subspace_iter_eig.m:114-115) or classical (cgs.m), both with the adaptive
- * re-orthogonalisation of those files.  si_eig / si_svd accept all three; arnoldi_eig the first two
+ * re-orthogonalisation of those files; or the column-pivoted LU basis (MATLAB/+src/+qr/lu.m, the
+ * un-permuted L).  si_eig / si_svd accept all four; arnoldi_eig the first two
  * (OFRR_ORTH_MGS there is the MGS Arnoldi of arnoldi_mgs_eig.m). */
-typedef enum { OFRR_ORTH_HESSENBERG = 0, OFRR_ORTH_MGS = 1, OFRR_ORTH_CGS = 2 } ofrr_orth;
+typedef enum { OFRR_ORTH_HESSENBERG = 0, OFRR_ORTH_MGS = 1, OFRR_ORTH_CGS = 2, OFRR_ORTH_LU = 3 } ofrr_orth;
 
 typedef struct {
   int mode;                /* ofrr_mode */

@@ -16,7 +16,7 @@ LIB_PATH = _PKG / "libofrr_gb300.so"
 F64, F32, F16, BF16 = 0, 1, 2, 3
 OP_DENSE, OP_CSR = 0, 1
 MODE_REFERENCE, MODE_MIXED, MODE_FP64 = 0, 1, 2
-ORTH_HESSENBERG, ORTH_MGS, ORTH_CGS = 0, 1, 2
+ORTH_HESSENBERG, ORTH_MGS, ORTH_CGS, ORTH_LU = 0, 1, 2, 3
 
 SUCCESS = 0
 ERR_SOLVER_MAX_ITERATIONS = 4001
@@ -138,6 +138,7 @@ SIGNATURES = {
     "ofrr_rand_points": (C.c_int, [_P, C.c_uint64, _I64, C.c_int, C.c_int, _P, _I64]),
     "ofrr_gaussian_kernel": (C.c_int, [_P, C.c_int, _I64, _I64, C.c_int, _P, _I64, _P, _I64, _D, _D, _D, C.c_int, _P,
                                        _I64]),
+    "ofrr_lu_basis": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _I64, _I64, _P, _I64, _P, _I64, _D, _DP, _IP]),
     "ofrr_csr_file_sizes": (C.c_int, [C.c_char_p, C.POINTER(_I64), C.POINTER(_I64)]),
     "ofrr_csr_file_read": (C.c_int, [_P, C.c_char_p, _I64, _I64, _P, _P, _P, C.POINTER(_I64), C.c_int]),
     "ofrr_read_singular_values": (C.c_int, [C.c_char_p, C.POINTER(_I64), _P]),

@@ -463,7 +463,26 @@ def gs_basis(A, classical: bool = False, precision_compute="double", precision_o
     return Q, R.reshape((n, n), order="F"), skip
 
 
-ORTH = {"hessenberg": L.ORTH_HESSENBERG, "mgs": L.ORTH_MGS, "cgs": L.ORTH_CGS}
+def lu_basis(A, precision_compute="double", precision_output=None, select_tol=None, precision_input=None):
+    """MATLAB/+src/+qr/lu.m: returns (Q, U, skip): Q the un-permuted L on the device (dropped columns
+    zero), U (n x n) and skip flags on the host."""
+    ctx = context()
+    pc = _p(precision_compute)
+    po = _p(precision_output or precision_compute)
+    pin = _p(precision_input) if precision_input else po
+    Ad = A if (is_cm(A) and dtype_of(A) == pin) else to_device_cm(A, pin)
+    m, n = Ad.shape
+    Q = empty_cm(m, n, po)
+    U = np.zeros(n * n)
+    skip = np.zeros(n, np.int32)
+    L.check(ctx.lib.ofrr_lu_basis(ctx.h, dtype_of(Ad), po, pc, m, n, Ad.data_ptr(), ld_of(Ad), Q.data_ptr(), ld_of(Q),
+                                  -1.0 if select_tol is None else select_tol,
+                                  U.ctypes.data_as(C.POINTER(C.c_double)), skip.ctypes.data_as(C.POINTER(C.c_int))),
+            "lu_basis")
+    return Q, U.reshape((n, n), order="F"), skip
+
+
+ORTH = {"hessenberg": L.ORTH_HESSENBERG, "mgs": L.ORTH_MGS, "cgs": L.ORTH_CGS, "lu": L.ORTH_LU}
 
 
 # ---- solvers ------------------------------------------------------------------------------------
@@ -544,7 +563,7 @@ def subspace_iter_eig(A, n: int, k: int, precision_compute="double", precision_o
                       generalized_tol=0.0, select_tol=None, symmetric=None, V0=None, mode="reference",
                       tol=0.0, nev=None, check_every=1, orth="hessenberg"):
     """MATLAB/+src/+subspace/subspace_iter_eig.m; returns (V, d, info) with V on the device.  orth: the
-    basis ("hessenberg"; "mgs" = the MATLAB file's default function_orth; "cgs")."""
+    basis ("hessenberg"; "mgs" = the MATLAB file's default function_orth; "cgs"; "lu")."""
     ctx = context()
     op = operator(A, symmetric)
     modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}

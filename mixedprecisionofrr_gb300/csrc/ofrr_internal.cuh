@@ -471,6 +471,9 @@ int fill_zero(ofrr_ctx* ctx, void* p, size_t bytes);
 int hessenberg_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n,
                     const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev,
                     int* select_dev, int* perm_dev, bool fast = false);
+// column-pivoted LU basis (MATLAB/+src/+qr/lu.m), same contract as the Hessenberg basis
+int lu_basis_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n, const void* A,
+                  int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev, int* select_dev);
 // Gram-Schmidt bases (orthogonal comparison path): MATLAB/+src/+qr/mgs.m, or cgs.m when classical
 int gs_basis_impl(ofrr_ctx* ctx, bool classical, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m,
                   int64_t n, const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R_dev,

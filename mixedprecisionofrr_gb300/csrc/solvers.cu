@@ -219,10 +219,12 @@ Precisions precisions_of(const ofrr_options* o) {
 // The basis of a block (the `function_orth` of subspace_iter_eig.m:65 / subspace_iter_svd.m): the
 // Hessenberg process (the orthogonalization-free default of this library), or a Gram-Schmidt QR --
 // mgs.m, the reference's own default (subspace_iter_eig.m:114-115), or cgs.m -- as the orthogonal
-// comparison.  Both leave Q at the input's column positions with select flags.
+// comparison, or the column-pivoted LU basis of lu.m.  All leave Q at the input's column positions
+// with select flags.
 int basis_impl(ofrr_ctx* ctx, int orth, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype tc, int64_t m, int64_t n,
                const void* A, int64_t lda, void* Q, int64_t ldq, double select_tol, double* R, int* sel, int* perm,
                bool fast) {
+  if (orth == OFRR_ORTH_LU) return lu_basis_impl(ctx, tin, tout, tc, m, n, A, lda, Q, ldq, select_tol, R, sel);
   if (orth == OFRR_ORTH_MGS || orth == OFRR_ORTH_CGS)
     return gs_basis_impl(ctx, orth == OFRR_ORTH_CGS, tin, tout, tc, m, n, A, lda, Q, ldq, select_tol, R, sel);
   return hessenberg_impl(ctx, tin, tout, tc, m, n, A, lda, Q, ldq, select_tol, R, sel, perm, fast);
@@ -232,7 +234,8 @@ int validate_options(const ofrr_options* o) {
   if (!o) return OFRR_ERR_INVALID_ARGUMENT;
   if (o->mode < 0 || o->mode > 2) return OFRR_ERR_INVALID_ARGUMENT;
   if (o->maxiter < 0 || o->step_size < 1 || o->block < 1 || o->nev < 0) return OFRR_ERR_INVALID_ARGUMENT;
-  if (o->orth != OFRR_ORTH_HESSENBERG && o->orth != OFRR_ORTH_MGS && o->orth != OFRR_ORTH_CGS)
+  if (o->orth != OFRR_ORTH_HESSENBERG && o->orth != OFRR_ORTH_MGS && o->orth != OFRR_ORTH_CGS &&
+      o->orth != OFRR_ORTH_LU)
     return OFRR_ERR_INVALID_ARGUMENT;
   const int ps[6] = {o->p_compute, o->p_output, o->p_hess_compute, o->p_hess_output, o->p_rr_compute,
                      o->p_rr_output};

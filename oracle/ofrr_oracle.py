@@ -582,6 +582,45 @@ def subspace_iter_eig(A, n: int, k: int, pc: str = "double", po: Optional[str] =
     return V, d
 
 
+def lu(A, pc: str = "double", po: Optional[str] = None, select_tol: Optional[float] = None, full: bool = False):
+    """``+src/+qr/lu.m:47-94``: right-looking LU with partial pivoting on A_work (rows swapped in
+    place; the pivot is the first maximum of |A_work(j:m, j)| in the current row order); a column whose
+    maximum is below select_tol is dropped (its row j is consumed all the same and U(j, j:n) keeps the
+    row).  Returns ``(L(rperm, select), U(select, :))`` as the two-output form, or
+    ``(L, U, perm, select)`` (0-based perm) with ``full``."""
+    po = po or pc
+    A = _cast(A, po)
+    m, n = A.shape
+    assert m >= n, "A must be a tall-thin matrix"
+    st = eps(po) if select_tol is None else float(_cast(select_tol, po))
+    W = A.copy()
+    L = np.zeros((m, n), dtype=_dt(po))
+    U = np.zeros((n, n), dtype=_dt(po))
+    perm = np.arange(m)
+    select = np.ones(n, dtype=bool)
+    for j in range(n):
+        col = np.abs(W[j:, j].astype(np.float64))
+        p = j + int(np.argmax(col))  # first maximum (MATLAB max)
+        if float(col[p - j]) < st:
+            select[j] = False
+            U[j, j:] = W[j, j:]
+            continue
+        if p != j:
+            W[[j, p], :] = W[[p, j], :]
+            L[[j, p], :j] = L[[p, j], :j]
+            perm[[j, p]] = perm[[p, j]]
+        U[j, j:] = W[j, j:]
+        L[j:, j] = _cast(_cast(W[j:, j], pc) / _cast(W[j, j], pc), po)
+        # rows i > j, every one as lu.m's loop (one product, one difference, each rounded)
+        W[j + 1:, j + 1:] = _cast(_cast(W[j + 1:, j + 1:], pc) - _cast(L[j + 1:, j], pc)[:, None]
+                                  * _cast(W[j, j + 1:], pc)[None, :], po)
+    if full:
+        return L, U, perm, select
+    rperm = np.empty(m, dtype=np.int64)
+    rperm[perm] = np.arange(m)
+    return L[rperm][:, select], U[select, :]
+
+
 def _basis(V, orth: str, ph_c: str, ph_o: str, select_tol):
     """``function_orth`` of ``subspace_iter_eig.m:65``: hessenberg (the orthogonalization-free runs),
     mgs (the file's default, ``:114-115``) or cgs; the two-output (economic) form."""
@@ -589,6 +628,8 @@ def _basis(V, orth: str, ph_c: str, ph_o: str, select_tol):
         return hessenberg_economic(V, ph_c, ph_o, select_tol)[0]
     if orth == "cgs":
         return cgs(V, ph_c, ph_o, select_tol)[0]
+    if orth == "lu":
+        return lu(V, ph_c, ph_o, select_tol)[0]
     return mgs(V, ph_c, ph_o, select_tol)[0]
 
 

@@ -135,3 +135,35 @@ def test_fp64_mode_orthogonal_vs_hessenberg(api, orc):
         out[orth] = np.asarray(d)[:4]
     assert np.allclose(out["mgs"], lam[:4], rtol=1e-9)
     assert np.allclose(out["hessenberg"], lam[:4], rtol=1e-9)
+
+
+@pytest.mark.parametrize("p,pc,stol", [("double", "double", 1e-12), ("single", "single", 1e-5),
+                                       ("half", "single", 1e-2), ("single", "double", 1e-5)])
+def test_lu_basis_bit_exact_vs_oracle(api, orc, p, pc, stol):
+    """lu.m on the GPU: element-wise arithmetic and an exact argmax with MATLAB's tie rule, so Q (the
+    un-permuted L), U and the skip flags equal the oracle's bit for bit"""
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((1500, 48))
+    A[:, 9] = A[:, 3]    # duplicated: dropped, its row consumed
+    A[:, 30] = 0.0       # zero: dropped at once
+    A[[5, 6], 12] = [4.0, -4.0]  # a tie in |value|: the first row in the current order wins
+    A = A.astype(orc._dt(p))
+    L, U, perm, sel = orc.lu(A, pc, p, select_tol=stol, full=True)
+    rperm = np.empty_like(perm)
+    rperm[perm] = np.arange(len(perm))
+    Lu = L[rperm]
+    Lu[:, ~sel] = 0
+    Q, R, skip = api.lu_basis(A, pc, p, select_tol=stol)
+    assert np.array_equal(skip == 0, sel)
+    Qh = api.to_numpy(Q)
+    assert np.array_equal(Qh.astype(np.float64), Lu.astype(np.float64))
+    assert np.array_equal(R, U.astype(np.float64))
+
+
+def test_si_eig_with_lu_basis_matches_oracle(api, orc):
+    A = orc.laplacian_2d(20).toarray()
+    n = A.shape[0]
+    V0 = orc.randn_block(42, n, 12)
+    _, do = orc.subspace_iter_eig(A, n, 12, "double", "double", maxiter=30, step_size=2, orth="lu", V0=V0)
+    V, d, info = api.subspace_iter_eig(A, n, 12, "double", "double", maxiter=30, step_size=2, V0=V0, orth="lu")
+    assert np.max(np.abs(np.asarray(d)[:8] - np.asarray(do)[:8])) < 1e-10 * np.max(np.abs(do))

@@ -172,3 +172,24 @@ def test_oracle_gram_schmidt_reference_contract(classical, p, tol, stol):
     Q, R, sel = f(A, p, p, select_tol=stol, full=True)
     assert [i for i in range(200) if not sel[i]] == [3, 4, 5]
     assert np.max(np.abs(A - Q.astype(np.float64) @ R.astype(np.float64))) < tol
+
+
+@pytest.mark.parametrize("p,stol", [("double", 1e-12), ("single", 1e-5)])
+def test_oracle_lu_basis(p, stol):
+    """lu.m restated: A_work = L U with rows permuted (A(perm, :) = L U up to rounding), |L| <= 1 with a
+    unit diagonal, duplicated columns dropped with their rows consumed."""
+    from oracle import ofrr_oracle as o
+
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((300, 40)).astype(o._dt(p))
+    L, U, perm, sel = o.lu(A, p, p, full=True)
+    assert sel.all()
+    Ld, Ud = L.astype(np.float64), U.astype(np.float64)
+    tol = 1e-12 if p == "double" else 1e-4
+    assert np.max(np.abs(A.astype(np.float64)[perm] - Ld @ Ud)) < tol * np.max(np.abs(A))
+    assert np.all(np.abs(Ld) <= 1.0) and np.all(np.diag(Ld[:40]) == 1.0)
+    A[:, 7] = A[:, 2]
+    A[:, 20] = A[:, 11]
+    Q, R = o.lu(A, p, p, select_tol=stol)
+    _, _, _, sel = o.lu(A, p, p, select_tol=stol, full=True)
+    assert [i for i in range(40) if not sel[i]] == [7, 20] and Q.shape == (300, 38)
