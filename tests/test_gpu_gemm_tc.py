@@ -114,7 +114,7 @@ def test_f64_emulated_gemm_zero_columns(api):
     assert np.allclose(C[3], B.sum(0), rtol=1e-12)
 
 
-@pytest.mark.parametrize("M,N,K", [(8192, 64, 2048), (2048, 64, 8192), (3000, 7, 5000), (700, 33, 4096),
+@pytest.mark.parametrize("M,N,K", [(8192, 64, 2048), (2048, 64, 8192), (1500, 9, 3000), (3000, 7, 5000), (700, 33, 4096),
                                    (4096, 64, 64), (6000, 5, 1000)])
 @pytest.mark.parametrize("pin", ["half", "bfloat16"])
 def test_tc_gemm_scalecols_fused(api, M, N, K, pin):

@@ -87,7 +87,7 @@ def plant(X, M):
     return X
 
 
-@pytest.mark.parametrize("M,N", [(700, 5), (2048, 64), (3000, 7), (4096, 9), (6000, 4), (8192, 64)])
+@pytest.mark.parametrize("M,N", [(700, 5), (1500, 6), (2048, 64), (3000, 7), (4096, 9), (6000, 4), (8192, 64)])
 def test_scale_slice_matches_scalecols_and_slicer(api, M, N):
     rng = np.random.default_rng(M + N)
     X = plant(rng.standard_normal((M, N)) * np.exp(rng.uniform(-20, 20, N))[None, :], M)
