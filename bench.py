@@ -343,6 +343,25 @@ def orth_compare_run(api, A, reps=3):
     return res
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's time of the timed region (every rank runs its own replica of the workload;
+    the whole-job value is the units all ranks processed over this time), then a barrier."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def job_value(steps: int, world: int, total_seconds: float) -> float:
+    """Whole-job throughput: NEV triplets per solve, `steps` solves on each of `world` replicas."""
+    return NEV * steps * world / total_seconds
+
+
 def measured_hbm_peak():
     pk = ROOT / "MEASURED_PEAKS.json"
     return json.loads(pk.read_text()).get("hbm_gbs") if pk.exists() else None
@@ -505,13 +524,10 @@ def main():
     with ClockSampler(local) as clk:
         times, infos, launches, s = time_solves(api, A, "mixed", args.steps, args.warmup, flush_buf)
     if world > 1:
-        t = torch.tensor([times.sum()], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total = float(t.item())
-        torch.distributed.barrier()
+        total = max_over_ranks(float(times.sum()), world, "cuda")
     else:
         total = float(times.sum())
-    value = NEV * args.steps * world / total
+    value = job_value(args.steps, world, total)
     err = float(np.max(np.abs(s[:NEV] - s_true[:NEV]) / s_true[:NEV]))
     maxres = float(max(i.max_residual for i in infos))
     statuses = sorted({i.status for i in infos})
