@@ -347,8 +347,11 @@ int ofrr_residual_norms(ofrr_ctx* ctx, const ofrr_operator* A, ofrr_dtype tx, in
  * (n <= 360 for FP64 output, <= 510 for FP32, <= 721 for 16-bit, and never above 1024); larger
  * n returns OFRR_ERR_BLAS_INVALID_SIZE with a message on stderr.  All calls share the array:
  * calls whose work overlaps on the GPU (different streams, or several threads) race and must be
- * serialised by the caller.  The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) and should come before any stream capture.
+ * serialised by the caller.  Every call looks up the array's device address (cudaGetSymbolAddress).
+ * With CUDA's default lazy module loading the module holding the array and the kernels is loaded by
+ * the first call on a device, and that load itself reserves device memory: make one call (any small
+ * size), or run with CUDA_MODULE_LOADING=EAGER, before the caller's pool takes all of HBM, and before
+ * any stream capture.  A, Q with A == Q must share the element type and leading dimension.
  * Outputs are device arrays: R (n x n, FP64, column-major), select (n ints, 1 = kept) and
  * perm (n ints, pivot rows, -1 for dropped columns).  ofrr_hessenberg_noalloc_scratch_bytes()
  * returns the scratch size. */

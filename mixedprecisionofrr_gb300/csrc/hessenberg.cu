@@ -17,8 +17,6 @@
 // happens inside the loop, so the whole build can be captured in a CUDA graph.
 #include "ofrr_internal.cuh"
 
-#include <mutex>
-
 namespace ofrr {
 
 template <class TO, class TC>
@@ -137,7 +135,9 @@ __global__ void __launch_bounds__(256) k_hess_col(int64_t m, int n, int i, TO* _
   const int64_t k = (f.v < 0.0) ? 0 : f.i;
   const TO pv = __ldcg(reinterpret_cast<const TO*>(Q + k + (int64_t)i * ldq));
   const double tol_o = to_c<double, TO>(from_c<TO, double>(select_tol));
-  const bool keep = (f.v >= 0.0) && (absd(pv) >= tol_o);
+  // kept unless |pivot| < select_tol: a column that is NaN throughout (no row wins the search, row 0
+  // is taken) stays selected, as in hessenberg.m where abs(NaN) < select_tol is false
+  const bool keep = !(absd(pv) < tol_o);
   for (int j = tid; j < i; j += blockDim.x) R[j + (int64_t)i * n] = s_sel[j] ? to_c<double, TC>(s_r[j]) : 0.0;
   if (keep) {
     for (int l = tid; l < i; l += blockDim.x) {
@@ -206,8 +206,9 @@ int hessenberg_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, ofrr_dtype t
   if (n <= 0 || m <= 0) return OFRR_SUCCESS;
   if (n > 4096) return OFRR_ERR_BLAS_INVALID_SIZE;
   if (select_tol < 0) select_tol = dtype_eps(tout);
-  // Q <- tout(A)
-  if (A != Q || tin != tout || lda != ldq) OFRR_TRY(cast_impl(ctx, tin, tout, m, n, A, lda, Q, ldq));
+  // Q <- tout(A); an in-place call must keep the element type and the leading dimension
+  if (A == Q && (tin != tout || lda != ldq)) return OFRR_ERR_INVALID_ARGUMENT;
+  if (A != Q) OFRR_TRY(cast_impl(ctx, tin, tout, m, n, A, lda, Q, ldq));
   WsScope scope(ctx);
   // blocked cluster schedule (hessenberg_blocked.cu) when the block fits on chip, else per column
   bool done = false;
@@ -323,26 +324,16 @@ constexpr size_t kNoAllocScratchBytes = size_t(1) << 20;
 constexpr int kNoAllocGrid = 304;  // 2 CTAs per SM: the argmax partials need this many slots
 __device__ __align__(256) unsigned char g_hess_noalloc_scratch[kNoAllocScratchBytes];
 
-std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[128] = {nullptr};
-
-// device address of the scratch array on the current device (set up once per device)
+// Device address of the scratch array on the current device.  Looked up on every call (cheap once the
+// module is loaded), so a device reset or a new primary context never leaves a stale address behind.
 int noalloc_scratch(unsigned char** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return map_cuda_error(e);
-  if (dev < 0 || dev >= 128) return OFRR_ERR_INVALID_ARGUMENT;
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_hess_noalloc_scratch);
-    if (e != cudaSuccess) {
-      note_cuda_error(e, "cudaGetSymbolAddress(g_hess_noalloc_scratch)", __FILE__, __LINE__);
-      return map_cuda_error(e);
-    }
-    g_noalloc_ptr[dev] = p;
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_hess_noalloc_scratch);
+  if (e != cudaSuccess) {
+    note_cuda_error(e, "cudaGetSymbolAddress(g_hess_noalloc_scratch)", __FILE__, __LINE__);
+    return map_cuda_error(e);
   }
-  *out = (unsigned char*)g_noalloc_ptr[dev];
+  *out = (unsigned char*)p;
   return OFRR_SUCCESS;
 }
 
@@ -405,7 +396,8 @@ extern "C" int ofrr_hessenberg_noalloc(void* stream, ofrr_dtype tin, ofrr_dtype 
   ofrr_ctx sctx;
   sctx.stream = (cudaStream_t)stream;
   if (select_tol < 0) select_tol = dtype_eps(tout);
-  if (A != Q || tin != tout || lda != ldq) OFRR_TRY(cast_impl(&sctx, tin, tout, m, n, A, lda, Q, ldq));
+  if (A == Q && (tin != tout || lda != ldq)) return OFRR_ERR_INVALID_ARGUMENT;
+  if (A != Q) OFRR_TRY(cast_impl(&sctx, tin, tout, m, n, A, lda, Q, ldq));
   OFRR_DISPATCH_STORAGE(tout, TO, OFRR_DISPATCH_COMPUTE(tcompute, TC, {
     OFRR_TRY((hess_run_noalloc<TO, TC>(&sctx, scratch, m, (int)n, (TO*)Q, ldq, select_tol, R, select, perm)));
   }));

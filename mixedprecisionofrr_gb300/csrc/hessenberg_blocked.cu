@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(HB_T) k_hess_inblock(int64_t m, int n, int c0,
     const TO* pr = rc[hit ? __ffs(hit) - 1 : 0].vals;  // the pivot row's current values
     const long long k = (bk < 0) ? 0 : bi;
     const TO pv = pr[t];
-    const bool keep = absd(pv) >= tol_o;
+    const bool keep = !(absd(pv) < tol_o);  // a NaN pivot keeps the column (hessenberg.m)
     // (2) bookkeeping (rank 0): pivot, selection, row i of R (R(i, c0+u) = r_{t,u} for u > t)
     if (rank == 0) {
       const int i = c0 + t;

@@ -7,7 +7,7 @@ golden.npz -- oracle outputs on seeded inputs (Hessenberg bases in half/single/d
     scalecols, small subspace-iteration and Krylov solves), used to pin the CUDA library and to
     regression-pin the oracle itself.
 
-Usage: python tests/golden/make_golden.py [--reference PATH]
+Usage: python tests/golden/make_golden.py --reference PATH
 """
 from __future__ import annotations
 
@@ -92,7 +92,7 @@ def golden() -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="checkout of the reference repository (read as text)")
     a = ap.parse_args()
     ka = known_answers(Path(a.reference))
     (HERE / "known_answers.json").write_text(json.dumps(ka, indent=1) + "\n")

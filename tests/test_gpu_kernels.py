@@ -143,6 +143,22 @@ def test_hessenberg_edge_shapes(api, orc):
         api.hessenberg(np.ones((3, 5)), "double")  # hessenberg.m:52 tall-thin assertion
 
 
+@pytest.mark.parametrize("m", [300, 20000])  # the clustered block kernel and the per-column kernel
+def test_hessenberg_all_nan_column_kept(api, orc, m):
+    """hessenberg.m keeps a column whose values are all NaN (abs(NaN) < select_tol is false): pivot row
+    0, the column scaled by NaN.  Later columns eliminate against it, so they turn NaN too."""
+    rng = np.random.default_rng(m)
+    A = rng.uniform(-1, 1, (m, 6))
+    A[:, 2] = np.nan
+    Q, R, sel, perm = api.hessenberg(A, "double")
+    Qo, Ro, selo, permo = orc.hessenberg(A, "double")
+    assert list(sel) == list(selo) and sel[2]
+    assert list(perm) == list(permo) and perm[2] == 0
+    Qn = api.to_numpy(Q)
+    assert np.array_equal(np.isnan(Qn), np.isnan(Qo))
+    assert np.array_equal(Qn[:, :2], Qo[:, :2])
+
+
 @pytest.mark.parametrize("pc,pin,po,tol", [("double", "double", "double", 1e-13), ("single", "single", "single", 1e-5),
                                            ("single", "half", "half", 2e-3), ("single", "half", "single", 1e-5),
                                            ("single", "bfloat16", "single", 1e-5)])

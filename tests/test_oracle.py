@@ -193,3 +193,12 @@ def test_oracle_lu_basis(p, stol):
     Q, R = o.lu(A, p, p, select_tol=stol)
     _, _, _, sel = o.lu(A, p, p, select_tol=stol, full=True)
     assert [i for i in range(40) if not sel[i]] == [7, 20] and Q.shape == (300, 38)
+
+
+def test_oracle_hessenberg_keeps_all_nan_column():
+    """hessenberg.m:62-70: max of an all-NaN column gives index 1 and abs(NaN) < select_tol is false,
+    so the column stays selected with pivot row 0."""
+    A = np.random.default_rng(0).uniform(-1, 1, (50, 4))
+    A[:, 1] = np.nan
+    Q, R, sel, perm = orc.hessenberg(A, "double")
+    assert sel[1] and perm[1] == 0 and np.all(np.isnan(Q[:, 1]))

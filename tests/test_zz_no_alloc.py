@@ -63,6 +63,40 @@ def test_noalloc_matches_hessenberg_twice(env, tin, tout, tc):
         assert np.array_equal(Rn, R)
 
 
+def test_noalloc_at_the_fp64_width_limit(env):
+    """n = 360 FP64 columns is the widest basis the 1 MiB array holds: it runs and matches."""
+    api, L, ctx = env
+    rng = np.random.default_rng(5)
+    A = rng.uniform(-1, 1, (2000, 360))
+    Qn, Rn, seln, permn = _noalloc(api, L, ctx, A, L.F64, L.F64, L.F64)
+    Q, R, sel, perm = api.hessenberg(A, "double", "double")
+    assert np.array_equal(permn, perm)
+    assert np.array_equal(seln, sel)
+    assert np.array_equal(Qn, api.to_numpy(Q))
+    assert np.array_equal(Rn, R)
+
+
+def test_noalloc_rejects_one_column_beyond_the_limit(env):
+    api, L, ctx = env
+    m, n = 2000, 361
+    A = api.empty_cm(m, n, L.F64)
+    Q = api.empty_cm(m, n, L.F64)
+    st = ctx.lib.ofrr_hessenberg_noalloc(C.c_void_p(ctx.stream.cuda_stream), L.F64, L.F64, L.F64, m, n,
+                                         A.data_ptr(), m, Q.data_ptr(), m, -1.0, Q.data_ptr(), Q.data_ptr(),
+                                         Q.data_ptr())
+    assert st == 2005  # OFRR_ERR_BLAS_INVALID_SIZE
+
+
+def test_noalloc_rejects_in_place_type_change(env):
+    api, L, ctx = env
+    m, n = 256, 8
+    A = api.empty_cm(m, n, L.F64)
+    st = ctx.lib.ofrr_hessenberg_noalloc(C.c_void_p(ctx.stream.cuda_stream), L.F64, L.F32, L.F64, m, n,
+                                         A.data_ptr(), m, A.data_ptr(), m, -1.0, A.data_ptr(), A.data_ptr(),
+                                         A.data_ptr())
+    assert st == 1000  # OFRR_ERR_INVALID_ARGUMENT
+
+
 def test_noalloc_rejects_width_beyond_scratch(env):
     api, L, ctx = env
     assert ctx.lib.ofrr_hessenberg_noalloc_scratch_bytes() == 1 << 20
