@@ -273,6 +273,12 @@ typedef struct {
   ofrr_dtype p_hess_compute, p_hess_output;  /* basis build */
   ofrr_dtype p_rr_compute, p_rr_output;      /* Rayleigh-Ritz Gram / update */
   int check_every;         /* residual check period in outer iterations (>= 1) */
+  /* Krylov restarts: Ritz vectors kept at a restart.  1 = arnoldi_hess_eig.m:99-106 (the leading Ritz
+   * vector alone; the reference mode always does this); 0 = the production default of OFRR_MODE_MIXED
+   * and OFRR_MODE_FP64 with a CSR operator: a thick restart keeping the invariant subspace of about
+   * max(nev + 4, 1.2 nev) leading Ritz values (at most kdim - 2) and the Galerkin residual direction
+   * (new behaviour); k > 1 keeps about k. */
+  int restart_keep;
 } ofrr_options;
 
 typedef struct {
@@ -325,11 +331,26 @@ int ofrr_rr_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, 
  * MATLAB/+src/+krylov/arnoldi_hess_eig.m:51-107) or MGS Arnoldi (OFRR_ORTH_MGS,
  * MATLAB/+src/+krylov/arnoldi_mgs_eig.m:54-113).  Replaces msvd::arnoldi_eig
  * (CPP/linalg/solvers/eig/arnoldi_eig.hpp:25-28, arnoldi_eig.cu:10-18).
- * v0: n (dev, type p_output) start vector when use_start_block; X: n x nev Ritz vectors out. */
+ * v0: n (dev, type p_output; FP64 in OFRR_MODE_MIXED / OFRR_MODE_FP64) start vector when
+ * use_start_block; X: n x nev Ritz vectors out (FP64 in those modes).  With a CSR operator the
+ * production modes use the thick restart of ofrr_options.restart_keep (kdim + 1 <= 129, nonsymmetric
+ * operators kdim + 1 <= 96 for the invariant-subspace restart); maxiter is the budget of Krylov steps.
+ * OFRR_MODE_MIXED: a 16-bit basis (p_output F16 or BF16) with the FP32 value copy of A and FP32
+ * arithmetic until the residuals stop improving, then an FP64 phase (FP64 values; Gram and Ritz products
+ * on the tensor cores through the exact-slice emulation). */
 int ofrr_arnoldi_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt,
                      const void* v0 /*dev|NULL*/, void* X /*dev*/, int64_t ldx,
                      double* evals /*host, nev*/, double* resid /*host|NULL*/,
                      ofrr_info* info /*host|NULL*/);
+
+/* Profiling form of one step of the thick-restart Krylov path (no reference counterpart; the step of
+ * arnoldi_hess_eig.m:73-87): builds a synthetic basis of i + 1 columns of type t (OFRR_F16 / OFRR_BF16 /
+ * OFRR_F32 with A's FP32 values and FP32 arithmetic, OFRR_F64 with FP64) on the square CSR operator A,
+ * runs the fused step kernel reps (>= 2) times and returns its mean time per launch (CUDA events on the
+ * context's stream, synchronous) and the step's algorithmic HBM bytes (CSR once, staging vector read and
+ * written, the new column written, i - 1 earlier columns read, pivot marks). */
+int ofrr_profile_krylov_step(ofrr_ctx* ctx, const ofrr_csr* A, ofrr_dtype t, int i, int reps, double* us_per_launch,
+                             double* bytes_per_launch);
 
 /* Residual norms ||A x_j - l_j x_j||_2 / (normA ||x_j||_2) in FP64 for ncols pairs
  * (MATLAB/+tests/+test4/test.m:340-350 with unit-norm scaling).  normA <= 0 uses max|l|. */

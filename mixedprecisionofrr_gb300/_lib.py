@@ -46,7 +46,7 @@ class ofrr_options(C.Structure):
         ("use_start_block", C.c_int), ("orth", C.c_int), ("reorth", C.c_int),
         ("p_compute", C.c_int), ("p_output", C.c_int), ("p_hess_compute", C.c_int),
         ("p_hess_output", C.c_int), ("p_rr_compute", C.c_int), ("p_rr_output", C.c_int),
-        ("check_every", C.c_int),
+        ("check_every", C.c_int), ("restart_keep", C.c_int),
     ]
 
 
@@ -104,6 +104,7 @@ SIGNATURES = {
                                                   _DP, _DP]),
     "ofrr_csrmm": (C.c_int, [_P, C.POINTER(ofrr_csr), C.c_int, C.c_int, C.c_int, C.c_int, _I64, _P, _I64, _P,
                              _I64]),
+    "ofrr_profile_krylov_step": (C.c_int, [_P, C.POINTER(ofrr_csr), C.c_int, C.c_int, C.c_int, _DP, _DP]),
     "ofrr_syev": (C.c_int, [_P, C.c_int, _P, C.c_int, _P]),
     "ofrr_sygv": (C.c_int, [_P, C.c_int, _P, C.c_int, _P, C.c_int, _P]),
     "ofrr_options_default": (None, [C.POINTER(ofrr_options)]),

@@ -551,10 +551,12 @@ class SolveInfo:
     basis_width: int
     max_residual: float
     residuals: np.ndarray
+    escalations: int = 0
 
 
 def _info(st, inf, res):
-    return SolveInfo(st, inf.iterations, inf.matvecs, inf.converged, inf.basis_width, inf.max_residual, res)
+    return SolveInfo(st, inf.iterations, inf.matvecs, inf.converged, inf.basis_width, inf.max_residual, res,
+                     inf.escalations)
 
 
 def subspace_iter_eig(A, n: int, k: int, precision_compute="double", precision_output=None, seed: int = 42,
@@ -618,15 +620,22 @@ def subspace_iter_svd(A, m: int, n: int, k: int, precision_compute="double", pre
 
 def arnoldi_hess_eig(A, n: int, k: int, precision_compute="double", precision_output=None, seed: int = 42,
                      maxiter: int = 5, kdim=None, select_tol=None, generalized_tol=0.0, symmetric=None, v0=None,
-                     mode="reference", tol=0.0):
-    """MATLAB/+src/+krylov/arnoldi_hess_eig.m; returns (V, d, info)."""
+                     mode="reference", tol=0.0, restart_keep: int = 0):
+    """MATLAB/+src/+krylov/arnoldi_hess_eig.m; returns (V, d, info).
+
+    mode "mixed" / "fp64" with a CSR operator: the thick-restart Hessenberg process (about restart_keep
+    leading Ritz values' invariant subspace kept, 0 = the default block; 1 = the reference's single-vector
+    restart); maxiter is the budget of Krylov steps, precision_output the 16-bit basis type of the mixed
+    mode ("half" or "bfloat16"), v0 and the returned vectors FP64."""
     ctx = context()
     op = operator(A, symmetric)
     modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
     kk = min(k, n)
+    if mode == "mixed" and precision_output is None:
+        precision_output = "half"
     o = options(mode=modes[mode], maxiter=maxiter, kdim=kdim or maxiter, nev=kk, tol=tol, use_generalized=1,
                 generalized_tol=generalized_tol, select_tol=-1.0 if select_tol is None else select_tol, seed=seed,
-                use_start_block=int(v0 is not None), orth=L.ORTH_HESSENBERG,
+                use_start_block=int(v0 is not None), orth=L.ORTH_HESSENBERG, restart_keep=restart_keep,
                 **_prec_opts(precision_compute, precision_output, None, None, None, None))
     po = o.p_output if mode == "reference" else L.F64
     v0d = to_device_cm(v0, po) if v0 is not None else None
@@ -664,6 +673,17 @@ def arnoldi_mgs_eig(A, n: int, k: int, precision_compute="double", precision_out
     if st not in (L.SUCCESS, L.ERR_SOLVER_MAX_ITERATIONS):
         L.check(st, "arnoldi_eig")
     return X, d, _info(st, inf, res)
+
+
+def profile_krylov_step(A: "CsrMatrix", precision: str, i: int, reps: int = 20):
+    """Mean time (us) and algorithmic HBM bytes of one fused Krylov step (column i, basis type
+    `precision`) on the CSR operator A (ofrr_profile_krylov_step)."""
+    ctx = context()
+    s = A.struct()
+    us, by = C.c_double(), C.c_double()
+    L.check(ctx.lib.ofrr_profile_krylov_step(ctx.h, C.byref(s), _p(precision), i, reps, C.byref(us), C.byref(by)),
+            "profile_krylov_step")
+    return us.value, by.value
 
 
 def residual_norms(A, X, lam, normA: float = -1.0, symmetric=None):

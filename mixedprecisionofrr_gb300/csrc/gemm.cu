@@ -24,6 +24,14 @@ static cudaDataType_t cuda_type(ofrr_dtype t) {
   return CUDA_R_32F;
 }
 
+constexpr int64_t kSlicedMaxK = int64_t(1) << 20;
+
+// C += T (FP64, M x N)
+__global__ void k_add_f64(int64_t m, int64_t n, const double* __restrict__ T, int64_t ldt, double* __restrict__ C,
+                          int64_t ldc) {
+  OFRR_FOR_2D(i, j, m, n) C[i + j * ldc] += T[i + j * ldt];
+}
+
 int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype tb, ofrr_dtype tc, ofrr_dtype tout,
               int64_t M, int64_t N, int64_t K, double alpha, const void* A, int64_t lda, const void* B, int64_t ldb,
               double beta, void* C, int64_t ldc) {
@@ -45,6 +53,24 @@ int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
   // FP64 TN products in the refinement phase of the mixed solver: exact BF16 slices on the tensor cores
   if (ctx->emulate_f64 && tc == OFRR_F64 && ta == OFRR_F64 && tb == OFRR_F64 && tout == OFRR_F64 && transB == 0 &&
       alpha == 1.0 && beta == 0.0 && K >= 16 && (transA == 1 || (M >= 1024 && K <= 1024))) {
+    if (K > kSlicedMaxK) {
+      // the exact integer combination holds for K <= 2^20: longer contractions (Gram products of
+      // millions of rows) are summed over K chunks in FP64, each chunk product emulated
+      double* T = ws_get<double>(ctx, (size_t)M * N, &st);
+      if (!T) return st;
+      for (int64_t k0 = 0; k0 < K; k0 += kSlicedMaxK) {
+        const int64_t kc = std::min<int64_t>(kSlicedMaxK, K - k0);
+        const double* Ak = (const double*)A + k0;  // transA == 1: A is K x M, its rows k0 ..
+        const double* Bk = (const double*)B + k0;
+        OFRR_TRY(gemm_impl(ctx, 1, 0, ta, tb, tc, tout, M, N, kc, 1.0, Ak, lda, Bk, ldb, 0.0, k0 ? T : C,
+                           k0 ? M : ldc));
+        if (k0) {
+          k_add_f64<<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, T, M, (double*)C, ldc);
+          OFRR_LAUNCHED(ctx, "k_add_f64");
+        }
+      }
+      return OFRR_SUCCESS;
+    }
     SlicedOperand As;
     if (transA == 1) {
       OFRR_TRY(sliced_prepare(ctx, K, M, (const double*)A, lda, &As));

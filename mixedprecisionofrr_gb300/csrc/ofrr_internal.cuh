@@ -12,6 +12,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <vector>
+#include <algorithm>
 
 #include "../../include/ofrr.h"
 
@@ -494,10 +495,16 @@ int geig_dev(ofrr_ctx* ctx, int n, const double* G, int ldg, const double* M, in
 // Rayleigh quotients of the final vectors
 // eig(C) for a nonsymmetric n x n C (n <= 128), FP32 Hessenberg-QR: real/imaginary parts, eigenvectors
 // (real parts, unit norm), unsorted
-int nonsym_eig_dev(ofrr_ctx* ctx, int n, const double* C, double* wr, double* wi, double* X, bool refine);
+int nonsym_eig_dev(ofrr_ctx* ctx, int n, const double* C, double* wr, double* wi, double* X, bool refine,
+                   bool pair_imag = false);
 // eig(G, M) for nonsymmetric G, SPD M (or M null): real parts descending, unit real-part eigenvectors;
 // refine = FP64 Newton steps on the real pairs (for FP32/FP64 bases)
-int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U, bool refine);
+int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U, bool refine,
+                bool pair_imag = false);
+// Y (n x p, ld n): basis of the invariant subspace of the pencil (G, M) (M SPD) for its p eigenvalues
+// with real part above sigma (matrix sign function of L^-1 G L^-T - sigma I); n <= 96
+int invariant_subspace_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double sigma, int p,
+                              double* Y);
 int geig_fast(ofrr_ctx* ctx, int n, const double* G, const double* M, double tau, double* lam, double* U,
               int refine = 2);
 int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const double* VV, double tau, double* sigma,
@@ -533,5 +540,44 @@ int sliced_gemm_tn(ofrr_ctx* ctx, const SlicedOperand& A, int64_t N, const doubl
 
 int residual_columns(ofrr_ctx* ctx, int64_t m, int64_t n, const double* AX, int64_t ldax,
                      const double* X, int64_t ldx, const double* lam_dev, double* out_dev);
+
+// ---- thick-restart Krylov steps (krylov_tr.cu) ----------------------------------------------
+// Device state of the Hessenberg-process Krylov steps of one solve: the basis V (ldv x nb, type t;
+// ldv = n rounded up to 8 so every column starts 16-byte aligned), two staging vectors and the
+// arithmetic (type te: FP32 for 16/32-bit bases, FP64 for FP64), pivot marks, the pivot rows and
+// reciprocals, L = Q(perm, :) and its explicit inverse (row-major, nb x nb), the next coefficients,
+// argmax partials, a ticket counter and the breakdown word (stop: -1 or the column that broke down).
+constexpr int kKryMaxNb = 129;
+struct KryState {
+  const ofrr_csr* A = nullptr;
+  ofrr_dtype t = OFRR_F16, te = OFRR_F32;
+  int64_t n = 0, ldv = 0;
+  int nb = 0, grid = 0;
+  double stol = 0.0;
+  void* V = nullptr;
+  void* S[2] = {nullptr, nullptr};
+  unsigned char* mark = nullptr;
+  int* perm = nullptr;
+  void *pvinv = nullptr, *coef = nullptr, *Lrows = nullptr, *Linv = nullptr, *partial = nullptr;
+  unsigned int* counter = nullptr;
+  int* stop = nullptr;
+};
+ofrr_dtype kry_arith_type(ofrr_dtype t);
+int64_t kry_ld(int64_t n);
+// allocates the state in ctx's current workspace scope; A's value copy of the arithmetic type is used
+int kry_state_init(ofrr_ctx* ctx, KryState* s, const ofrr_csr* A, ofrr_dtype t, int nb, double stol);
+// columns 0 .. q-1 of s.V final with pivot rows s.perm[0 .. q-1]: builds columns q .. nb-1
+int kry_cycle_steps(ofrr_ctx* ctx, KryState& s, int q);
+// Rayleigh-Ritz helpers: W = V Cf (FP32 arithmetic into an FP32 W for 16/32-bit V; FP64 through
+// gemm_impl otherwise), w += a (one column), x = M^-1 g (SPD, nc <= 129),
+// Cf = [U1(:, :k1), U2(:, :k2), -x], s = sum_j W(:, j) / nrm_j
+int kry_backtransform(ofrr_ctx* ctx, ofrr_dtype t, int64_t n, int nc, const void* V, int64_t ldv, const double* Cf,
+                      int k, ofrr_dtype tw, void* W, int64_t ldw);
+int kry_add_col(ofrr_ctx* ctx, ofrr_dtype tw, int64_t n, void* w, ofrr_dtype ta, const void* a);
+int kry_spd_solve(ofrr_ctx* ctx, int nc, const double* M, const double* g, double* x);
+int kry_coef_matrix(ofrr_ctx* ctx, int nc, int k1, const double* U1, int k2, const double* U2, const double* x,
+                    double* Cf);
+int kry_sum_unit_cols(ofrr_ctx* ctx, ofrr_dtype tw, int64_t n, int k, const void* W, int64_t ldw, const double* nrm,
+                      double* s);
 
 }  // namespace ofrr

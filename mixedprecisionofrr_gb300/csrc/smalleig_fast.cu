@@ -713,10 +713,233 @@ __global__ void k_unit_cols(int n, double* __restrict__ U) {
   for (int i = lane; i < n; i += 32) u[i] *= inv;
 }
 
+// ---- invariant subspace of a nonsymmetric pencil (the thick restart of the Krylov eigensolver) ----
+// The restart keeps span{Ritz vectors of the wanted Ritz values}; for a non-normal projected matrix two
+// close Ritz values can have nearly parallel eigenvectors, whose span then carries rounding noise of the
+// size eps / angle.  The invariant subspace itself is well conditioned when the wanted values are
+// separated from the others, and the matrix sign function gives it without eigenvectors:
+// S = sign(C - sigma I) (Newton, X <- (mu X + (mu X)^-1) / 2 with determinant scaling mu), P = (I + S) / 2
+// projects onto the eigenvalues with real part above sigma [N. J. Higham, Functions of Matrices,
+// SIAM 2008, ch. 5].  One CTA; Gauss-Jordan inversion with partial pivoting in shared memory.
+constexpr int kSignMaxN = 96;
+
+template <class T>
+__global__ void __launch_bounds__(256) k_sign_newton(int n, double* __restrict__ Xg, int maxit, double tol,
+                                                     int* __restrict__ flag) {
+  extern __shared__ unsigned char sgn_raw[];
+  T* X = reinterpret_cast<T*>(sgn_raw);  // n x n, column-major
+  T* Y = X + (size_t)n * n;              // its inverse (Gauss-Jordan in place)
+  __shared__ int piv[kSignMaxN];
+  __shared__ T s_col[kSignMaxN];
+  __shared__ int s_p;
+  __shared__ double s_logdet, s_num, s_den;
+  const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
+  const int nn = n * n;
+  if (*flag) return;  // an earlier stage met a singular matrix
+  for (int e = tid; e < nn; e += nthr) X[e] = (T)Xg[e];
+  __syncthreads();
+  for (int it = 0; it < maxit; ++it) {
+    for (int e = tid; e < nn; e += nthr) Y[e] = X[e];
+    if (tid == 0) s_logdet = 0.0;
+    __syncthreads();
+    bool singular = false;
+    for (int k = 0; k < n; ++k) {
+      if (tid < 32) {  // pivot: first largest |Y(i, k)|, i >= k
+        T best = T(-1);
+        int bi = k;
+        for (int i = k + lane; i < n; i += 32) {
+          const T a = fabs(Y[i + (size_t)k * n]);
+          if (a > best) {
+            best = a;
+            bi = i;
+          }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          const T ob = __shfl_down_sync(0xffffffffu, best, off);
+          const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+          if (ob > best || (ob == best && oi < bi)) {
+            best = ob;
+            bi = oi;
+          }
+        }
+        if (lane == 0) s_p = bi;
+      }
+      __syncthreads();
+      const int p = s_p;
+      if (p != k)
+        for (int j = tid; j < n; j += nthr) {
+          const T t = Y[k + (size_t)j * n];
+          Y[k + (size_t)j * n] = Y[p + (size_t)j * n];
+          Y[p + (size_t)j * n] = t;
+        }
+      if (tid == 0) piv[k] = p;
+      __syncthreads();
+      const T d = Y[k + (size_t)k * n];
+      if (!(fabs(d) > T(0))) {  // zero or NaN pivot: every thread sees the same value
+        singular = true;
+        break;
+      }
+      const T dinv = T(1) / d;
+      if (tid == 0) s_logdet += log(fabs((double)d));
+      for (int i = tid; i < n; i += nthr) s_col[i] = (i == k) ? T(0) : Y[i + (size_t)k * n];
+      __syncthreads();
+      for (int j = tid; j < n; j += nthr) Y[k + (size_t)j * n] = (j == k) ? dinv : Y[k + (size_t)j * n] * dinv;
+      for (int i = tid; i < n; i += nthr)
+        if (i != k) Y[i + (size_t)k * n] = T(0);
+      __syncthreads();
+      for (int e = tid; e < nn; e += nthr) {
+        const int i = e % n, j = e / n;
+        if (i != k) Y[e] -= s_col[i] * Y[k + (size_t)j * n];
+      }
+      __syncthreads();
+    }
+    if (singular) {
+      if (tid == 0) *flag = 1;
+      return;
+    }
+    for (int k = n - 1; k >= 0; --k) {  // undo the row interchanges as column interchanges of the inverse
+      const int p = piv[k];
+      if (p != k)
+        for (int i = tid; i < n; i += nthr) {
+          const T t = Y[i + (size_t)k * n];
+          Y[i + (size_t)k * n] = Y[i + (size_t)p * n];
+          Y[i + (size_t)p * n] = t;
+        }
+      __syncthreads();
+    }
+    const double mu = (it < 4) ? exp(-s_logdet / n) : 1.0;  // determinant scaling in the first steps
+    if (tid == 0) {
+      s_num = 0.0;
+      s_den = 0.0;
+    }
+    __syncthreads();
+    double num = 0.0, den = 0.0;
+    for (int e = tid; e < nn; e += nthr) {
+      const T xn = (T)(0.5 * (mu * (double)X[e] + (double)Y[e] / mu));
+      num += ((double)xn - (double)X[e]) * ((double)xn - (double)X[e]);
+      den += (double)xn * (double)xn;
+      X[e] = xn;
+    }
+    atomicAdd(&s_num, num);
+    atomicAdd(&s_den, den);
+    __syncthreads();
+    const bool done = s_num <= tol * tol * s_den;
+    __syncthreads();
+    if (done && it >= 1) break;
+  }
+  for (int e = tid; e < nn; e += nthr) Xg[e] = (double)X[e];
+}
+
+__global__ void k_shift_copy(int n, const double* __restrict__ C, double sigma, double* __restrict__ X) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += gridDim.x * blockDim.x)
+    X[e] = C[e] - ((e % n == e / n) ? sigma : 0.0);
+}
+
+// Q (n x p) = orthonormal basis of range((I + S) / 2): the projector applied to a fixed pseudo-random
+// block (splitmix64 hashes), then modified Gram-Schmidt twice (FP64, one CTA)
+__global__ void __launch_bounds__(256) k_proj_basis(int n, int p, const double* __restrict__ S, double* __restrict__ Q) {
+  extern __shared__ double pb[];  // n x p
+  __shared__ double s_red[8];
+  __shared__ double s_dot;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  for (int e = tid; e < n * p; e += nthr) {
+    const int i = e % n, c = e / n;
+    double acc = 0.0;
+    for (int k = 0; k < n; ++k) {
+      unsigned long long h = 0x9e3779b97f4a7c15ULL * (unsigned long long)(k + 1) + 0xbf58476d1ce4e5b9ULL * (c + 1);
+      h ^= h >> 31;
+      h *= 0x94d049bb133111ebULL;
+      h ^= h >> 29;
+      const double om = (double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+      const double pik = 0.5 * (S[i + (size_t)k * n] + ((i == k) ? 1.0 : 0.0));
+      acc += pik * om;
+    }
+    pb[e] = acc;
+  }
+  __syncthreads();
+  auto block_sum = [&](double v) -> double {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((tid & 31) == 0) s_red[tid >> 5] = v;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (nthr + 31) / 32; ++w) t += s_red[w];
+      s_dot = t;
+    }
+    __syncthreads();
+    const double r = s_dot;
+    __syncthreads();
+    return r;
+  };
+  for (int c = 0; c < p; ++c) {
+    double* qc = pb + (size_t)c * n;
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int c2 = 0; c2 < c; ++c2) {
+        const double* q2 = pb + (size_t)c2 * n;
+        double v = 0.0;
+        for (int i = tid; i < n; i += nthr) v += q2[i] * qc[i];
+        const double dt = block_sum(v);
+        for (int i = tid; i < n; i += nthr) qc[i] -= dt * q2[i];
+        __syncthreads();
+      }
+    }
+    double v = 0.0;
+    for (int i = tid; i < n; i += nthr) v += qc[i] * qc[i];
+    const double t = block_sum(v);
+    const double sc = (t > 0.0) ? 1.0 / sqrt(t) : 0.0;
+    for (int i = tid; i < n; i += nthr) qc[i] *= sc;
+    __syncthreads();
+  }
+  for (int e = tid; e < n * p; e += nthr) Q[e] = pb[e];
+}
+
+// Y (n x p, ld n) spanning the invariant subspace of the pencil (G, M) for its p eigenvalues with real
+// part above sigma: C = L^-1 G L^-T (M = L L'), Q = orth((I + sign(C - sigma I)) / 2), Y = L^-T Q.
+// Returns OFRR_ERR_SINGULAR_MATRIX when a Newton step meets a singular matrix (sigma an eigenvalue).
+int invariant_subspace_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double sigma, int p,
+                              double* Y) {
+  if (n <= 0 || p <= 0) return OFRR_SUCCESS;
+  if (n > kSignMaxN || p > n) return OFRR_ERR_BLAS_INVALID_SIZE;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  double *L = ws_get<double>(ctx, (size_t)n * n, &st), *Z = ws_get<double>(ctx, (size_t)n * n, &st),
+         *C = ws_get<double>(ctx, (size_t)n * n, &st), *X = ws_get<double>(ctx, (size_t)n * n, &st),
+         *Q = ws_get<double>(ctx, (size_t)n * p, &st);
+  int* flag = ws_get<int>(ctx, 1, &st);
+  if (!L || !Z || !C || !X || !Q || !flag) return st;
+  const double* Ms[1] = {M};
+  double* Ls[1] = {L};
+  OFRR_TRY(chol(ctx, n, 1, Ms, n, 0.0, Ls));
+  OFRR_TRY(trsm(ctx, n, n, L, G, n, 1, Z, 0));  // Z = L^-1 G'
+  OFRR_TRY(trsm(ctx, n, n, L, Z, n, 1, C, 0));  // C = L^-1 Z' = L^-1 G L^-T
+  k_shift_copy<<<(n * n + 255) / 256, 256, 0, ctx->stream>>>(n, C, sigma, X);
+  OFRR_LAUNCHED(ctx, "k_shift_copy");
+  OFRR_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
+  const size_t sm32 = 2 * (size_t)n * n * sizeof(float), sm64 = 2 * (size_t)n * n * sizeof(double);
+  OFRR_TRY(allow_smem(k_sign_newton<float>));
+  OFRR_TRY(allow_smem(k_sign_newton<double>));
+  // FP32 Newton steps to a 1e-6 fixed point, then FP64 steps (quadratic convergence) to 1e-14
+  k_sign_newton<float><<<1, 256, sm32, ctx->stream>>>(n, X, 60, 1e-6, flag);
+  OFRR_LAUNCHED(ctx, "k_sign_newton<f32>");
+  k_sign_newton<double><<<1, 256, sm64, ctx->stream>>>(n, X, 12, 1e-14, flag);
+  OFRR_LAUNCHED(ctx, "k_sign_newton<f64>");
+  OFRR_TRY(allow_smem(k_proj_basis));
+  k_proj_basis<<<1, 256, (size_t)n * p * sizeof(double), ctx->stream>>>(n, p, X, Q);
+  OFRR_LAUNCHED(ctx, "k_proj_basis");
+  OFRR_TRY(trsm(ctx, n, p, L, Q, n, 0, Y, 1));  // Y = L^-T Q
+  int hf = 0;
+  OFRR_CUDA(cudaMemcpyAsync(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  OFRR_TRY(sync_and_check(ctx));
+  return hf ? OFRR_ERR_SINGULAR_MATRIX : OFRR_SUCCESS;
+}
+
 // eig(G, M) for a nonsymmetric G and SPD M (M null: eig(G)): lam = real parts, descending (stable);
 // U (ld n) the real parts of the eigenvectors, unit 2-norm.  M is reduced away with its FP64
 // Cholesky factor (C = L^-1 G L^-T, U = L^-T X); C is solved in FP32 (smalleig_nonsym.cu).
-int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U, bool refine) {
+int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U, bool refine,
+                bool pair_imag) {
   if (n <= 0) return OFRR_SUCCESS;
   if (n > 128) return OFRR_ERR_BLAS_INVALID_SIZE;
   WsScope scope(ctx);
@@ -735,7 +958,7 @@ int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* 
     OFRR_TRY(trsm(ctx, n, n, L, Z, n, 1, C, 0));  // C = L^-1 Z' = L^-1 G L^-T
     Cs = C;
   }
-  OFRR_TRY(nonsym_eig_dev(ctx, n, Cs, wr, wi, X, refine));
+  OFRR_TRY(nonsym_eig_dev(ctx, n, Cs, wr, wi, X, refine, pair_imag));
   if (M) {
     OFRR_TRY(trsm(ctx, n, n, L, X, n, 0, W, 1));  // W = L^-T X
     k_unit_cols<<<(n + 3) / 4, 128, 0, ctx->stream>>>(n, W);

@@ -41,7 +41,8 @@ __device__ __forceinline__ void cdivf(float xr, float xi, float yr, float yi, fl
 // (real parts, unit norm), unsorted; *flag = 1 when the QR iteration did not converge.
 __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __restrict__ C, int ldc,
                                                        double* __restrict__ wr, double* __restrict__ wi,
-                                                       double* __restrict__ X, int* __restrict__ flag) {
+                                                       double* __restrict__ X, int* __restrict__ flag,
+                                                       int pair_imag) {
   extern __shared__ float sm[];
   const int ld = nn + 1;
   float* H = sm;             // n x n (row i, column j at i + j * ld)
@@ -437,7 +438,9 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
   for (int j = lane; j < nn; j += 32) {
     // the vector for eigenvalue j: column j, or for the second member of a complex pair the real part
     // (column j - 1) of the pair's vector
-    const int src = (e[j] < 0.f) ? j - 1 : j;
+    // (pair_imag: the imaginary part, column j, instead -- with the real part in column j - 1 the pair
+    // then spans the real invariant subspace of the two eigenvalues)
+    const int src = (e[j] < 0.f && !pair_imag) ? j - 1 : j;
     const int top = (e[j] != 0.f) ? ((e[j] > 0.f) ? j + 1 : j) : j;  // last nonzero row of column src
     float nrm = 0.f;
     for (int i = 0; i < nn; ++i) {
@@ -616,12 +619,13 @@ __global__ void k_frob(int n, const double* __restrict__ C, double* __restrict__
 
 // eig(C) for a nonsymmetric n x n C (FP64, ld n): wr/wi (n), X (n x n, ld n), unsorted.  refine: FP64
 // Newton steps on the real pairs (FP64 bases); without it the pairs are FP32-accurate.
-int nonsym_eig_dev(ofrr_ctx* ctx, int n, const double* C, double* wr, double* wi, double* X, bool refine) {
+int nonsym_eig_dev(ofrr_ctx* ctx, int n, const double* C, double* wr, double* wi, double* X, bool refine,
+                   bool pair_imag) {
   if (n <= 0) return OFRR_SUCCESS;
   if (n > NS_MAX) return OFRR_ERR_BLAS_INVALID_SIZE;
   const size_t smem = ((size_t)3 * n * (n + 1) + 3 * (size_t)n) * sizeof(float);
   OFRR_TRY(allow_smem(k_nonsym_eig_f32));
-  k_nonsym_eig_f32<<<1, 32, smem, ctx->stream>>>(n, C, n, wr, wi, X, ctx->dev_flags + 3);
+  k_nonsym_eig_f32<<<1, 32, smem, ctx->stream>>>(n, C, n, wr, wi, X, ctx->dev_flags + 3, pair_imag ? 1 : 0);
   OFRR_LAUNCHED(ctx, "k_nonsym_eig_f32");
   if (!refine) return OFRR_SUCCESS;
   // ||C||_F on the host side of the acceptance test: one small reduction, read back

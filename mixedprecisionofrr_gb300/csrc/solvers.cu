@@ -233,7 +233,8 @@ int basis_impl(ofrr_ctx* ctx, int orth, ofrr_dtype tin, ofrr_dtype tout, ofrr_dt
 int validate_options(const ofrr_options* o) {
   if (!o) return OFRR_ERR_INVALID_ARGUMENT;
   if (o->mode < 0 || o->mode > 2) return OFRR_ERR_INVALID_ARGUMENT;
-  if (o->maxiter < 0 || o->step_size < 1 || o->block < 1 || o->nev < 0) return OFRR_ERR_INVALID_ARGUMENT;
+  if (o->maxiter < 0 || o->step_size < 1 || o->block < 1 || o->nev < 0 || o->restart_keep < 0)
+    return OFRR_ERR_INVALID_ARGUMENT;
   if (o->orth != OFRR_ORTH_HESSENBERG && o->orth != OFRR_ORTH_MGS && o->orth != OFRR_ORTH_CGS &&
       o->orth != OFRR_ORTH_LU)
     return OFRR_ERR_INVALID_ARGUMENT;
@@ -932,6 +933,225 @@ extern "C" int ofrr_rr_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
 }
 
 // ======================================================================================
+// Krylov eigensolver, production modes: thick-restart Hessenberg process (new behaviour)
+// ======================================================================================
+// arnoldi_hess_eig.m:99-106 restarts from the leading Ritz vector alone; on 20 clustered eigenvalues
+// (the 3D convection-diffusion operator) that never reaches a tolerance.  The production modes keep a
+// block Y spanning the invariant subspace of the leading Ritz values at each restart -- the Ritz vectors
+// for a symmetric operator, the range of the matrix-sign projector otherwise (close Ritz values of a
+// non-normal projection can have nearly parallel Ritz vectors, whose span is lost to rounding and then
+// stalls the restarts) -- plus the Galerkin residual direction f = A v_last - V M^-1 V' A v_last.  The
+// residuals of the Ritz vectors of a Galerkin projection onto a Krylov space are all parallel to f, so
+// span{Y, f, A f, ...} is again a Krylov space (the thick restart of Wu and Simon, and of Stathopoulos,
+// Saad and Wu; Stewart's Krylov-Schur for the nonsymmetric case), here built on the oblique Hessenberg
+// basis: the block [Y, f] gets a Hessenberg basis, the Krylov steps continue from f (krylov_tr.cu), and
+// Rayleigh-Ritz is the generalized one of arnoldi_hess_eig.m:89-95 (eig(V'AV, V'V + tau I)).
+// Mixed mode: a 16-bit phase (16-bit basis, FP32 matvec on the FP32 value copy, FP32 arithmetic) until
+// its residuals stop improving, then an FP64 phase restarted from the sum of the unit Ritz vectors (the
+// 16-bit rounding leaves the kept block's residuals no longer parallel, and a kept block then stalls).
+static int default_keep(int nev, int kdim) { return std::min(std::max(nev + 4, (nev * 6 + 4) / 5), kdim - 2); }
+
+static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, const void* v0,
+                              void* X, int64_t ldx, double* evals, double* resid, ofrr_info* info) {
+  const int64_t n = A->nrows;
+  const int kdim = opt->kdim > 0 ? opt->kdim : opt->maxiter;
+  const int nb = kdim + 1;
+  const int nev = (int)std::min<int64_t>(opt->nev, n);
+  if (nb > kKryMaxNb || nb > n || kdim < 4) return OFRR_ERR_BLAS_INVALID_SIZE;
+  int keep = opt->restart_keep > 0 ? opt->restart_keep : default_keep(nev, kdim);
+  keep = std::min(std::max(keep, nev), kdim - 2);
+  if (nev > keep) return OFRR_ERR_INVALID_ARGUMENT;  // nev > kdim - 2
+  const bool symmetric = A->symmetric != 0;
+  const bool mixed = opt->mode == OFRR_MODE_MIXED;
+  const ofrr_dtype t16 = (opt->p_output == OFRR_BF16) ? OFRR_BF16 : OFRR_F16;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  Op op{A};
+  const int64_t ld = kry_ld(n);
+  const int wcols = nev + keep + 6;
+  double* AVb = ws_get<double>(ctx, (size_t)ld * nb, &st);
+  double* Wb = ws_get<double>(ctx, (size_t)ld * wcols, &st);
+  double* svec = ws_get<double>(ctx, (size_t)ld, &st);
+  if (!AVb || !Wb || !svec) return st;
+  double *G, *M, *U, *d, *xg, *Cf, *R, *nrm;
+  int *sel, *perm;
+  OFRR_TRY(dmalloc(ctx, &G, (size_t)nb * nb));
+  OFRR_TRY(dmalloc(ctx, &M, (size_t)nb * nb));
+  OFRR_TRY(dmalloc(ctx, &U, (size_t)nb * nb));
+  OFRR_TRY(dmalloc(ctx, &Cf, (size_t)nb * (wcols + keep + 6)));
+  OFRR_TRY(dmalloc(ctx, &R, (size_t)(keep + 6) * (keep + 6)));
+  OFRR_TRY(dmalloc(ctx, &d, (size_t)nb));
+  OFRR_TRY(dmalloc(ctx, &xg, (size_t)nb));
+  OFRR_TRY(dmalloc(ctx, &nrm, (size_t)nb));
+  OFRR_TRY(dmalloc(ctx, &sel, (size_t)nb));
+  OFRR_TRY(dmalloc(ctx, &perm, (size_t)nb));
+  // the start vector (FP64) as the first block
+  if (opt->use_start_block) {
+    OFRR_CUDA(cudaMemcpyAsync(Wb, v0, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
+    OFRR_TRY(ofrr_randn(ctx, opt->seed, n, 1, OFRR_F64, Wb, ld));
+  }
+  ofrr_dtype tw = OFRR_F64;  // type of the block in Wb
+  void* blk = Wb;            // the next block: q0 columns at blk (leading dimension ld)
+  int q0 = 1;
+  int phase = 0;
+  KryState S;
+  const double stol = opt->select_tol < 0 ? 0.0 : opt->select_tol;
+  OFRR_TRY(kry_state_init(ctx, &S, &A->csr, mixed ? t16 : OFRR_F64, nb, stol));
+  std::vector<double> hd(nb), hres(nb, INFINITY);
+  std::vector<int> hsel(nb), hperm(nb), cperm(nb);
+  int cycles = 0, steps = 0, nmv = 0, escalations = 0, ncols = 0, in_phase = 0, k = std::min(nev, nb);
+  double best_in_phase = INFINITY;
+  bool converged = false;
+  while (true) {
+    TraceScope ts(ctx, "krylov.block");
+    const ofrr_dtype t = S.t, ta = kry_arith_type(t);
+    // (1) Hessenberg basis of the block [Y, f] (columns scaled to a unit maximum first, so that the
+    //     selection threshold is relative): columns 0 .. q-1 of the new basis
+    int q = 0;
+    {
+      WsScope inner(ctx);
+      OFRR_TRY(scalecols_impl(ctx, tw, tw, n, q0, blk, ld, nullptr, tw == OFRR_F64));
+      const double stol_blk = (t == OFRR_F64) ? 1e-12 : 4.0 * dtype_eps(t);
+      OFRR_TRY(hessenberg_impl(ctx, tw, t, ta, n, q0, blk, ld, S.V, S.ldv, stol_blk, R, sel, perm, true));
+      OFRR_CUDA(cudaMemcpyAsync(hsel.data(), sel, sizeof(int) * q0, cudaMemcpyDeviceToHost, ctx->stream));
+      OFRR_CUDA(cudaMemcpyAsync(hperm.data(), perm, sizeof(int) * q0, cudaMemcpyDeviceToHost, ctx->stream));
+      OFRR_TRY(sync_and_check(ctx));
+      std::vector<int> s0(hsel.begin(), hsel.begin() + q0);
+      for (int j = 0; j < q0; ++j)
+        if (s0[j]) cperm[q++] = hperm[j];
+      int w = 0;
+      OFRR_TRY(compact_columns(ctx, t, n, S.V, S.ldv, s0, &w));
+    }
+    if (q == 0) return OFRR_ERR_SOLVER_DIVERGENCE;  // the start vector is zero
+    OFRR_CUDA(cudaMemcpyAsync(S.perm, cperm.data(), sizeof(int) * q, cudaMemcpyHostToDevice, ctx->stream));
+    // (2) Krylov steps q .. nb-1
+    ts.next("krylov.steps");
+    OFRR_TRY(kry_cycle_steps(ctx, S, q));
+    int hstop = -1;
+    OFRR_CUDA(cudaMemcpyAsync(&hstop, S.stop, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    OFRR_TRY(sync_and_check(ctx));
+    ncols = (hstop >= 0) ? hstop : nb;
+    steps += ncols - q;
+    // (3) generalized Rayleigh-Ritz on the ncols columns, the Ritz vectors, the kept block and the
+    //     residual direction
+    ts.next("rr");
+    const ofrr_dtype tav = ta;
+    int pp = 0;
+    {
+      WsScope inner(ctx);
+      OFRR_TRY(csrmm_impl(ctx, &A->csr, 0, t, ta, tav, ncols, S.V, S.ldv, AVb, ld));
+      nmv += ncols;
+      ctx->emulate_f64 = mixed && t == OFRR_F64;
+      int rst = gemm_impl(ctx, 1, 0, t, t, ta, OFRR_F64, ncols, ncols, n, 1.0, S.V, S.ldv, S.V, S.ldv, 0.0, M, ncols);
+      if (rst == OFRR_SUCCESS)
+        rst = gemm_impl(ctx, 1, 0, t, tav, ta, OFRR_F64, ncols, ncols, n, 1.0, S.V, S.ldv, AVb, ld, 0.0, G, ncols);
+      ctx->emulate_f64 = false;
+      OFRR_TRY(rst);
+      if (opt->generalized_tol != 0.0) {
+        k_add_diag<<<(ncols + 255) / 256, 256, 0, ctx->stream>>>(ncols, M, ncols, opt->generalized_tol);
+        OFRR_LAUNCHED(ctx, "k_add_diag");
+      }
+      if (symmetric) OFRR_TRY(geig_fast(ctx, ncols, G, M, 0.0, d, U, t == OFRR_F64 ? 2 : 1));
+      else OFRR_TRY(geig_nonsym(ctx, ncols, G, M, d, U, t == OFRR_F64, true));
+      OFRR_CUDA(cudaMemcpyAsync(hd.data(), d, sizeof(double) * ncols, cudaMemcpyDeviceToHost, ctx->stream));
+      OFRR_TRY(sync_and_check(ctx));
+      k = std::min(nev, ncols);
+      // the kept block ends at the widest gap of the real parts near `keep` (never inside a complex pair)
+      pp = std::min(keep, ncols - 1);
+      {
+        double best_gap = -1.0;
+        const int lo = std::max(nev, keep - 3), hi = std::min(keep + 4, ncols - 2);
+        for (int c = lo; c <= hi; ++c) {
+          const double gap = hd[c - 1] - hd[c];
+          if (gap > best_gap) {
+            best_gap = gap;
+            pp = c;
+          }
+        }
+        if (best_gap <= 0.0) pp = std::min(keep, ncols - 1);
+      }
+      OFRR_TRY(kry_spd_solve(ctx, ncols, M, G + (size_t)(ncols - 1) * ncols, xg));
+      const double* Yc = U;
+      double* Ys = Cf + (size_t)ncols * (k + pp + 1);
+      if (!symmetric && ncols <= 96 && pp < ncols) {
+        const double sigma = 0.5 * (hd[pp - 1] + hd[pp]);
+        const int ist = invariant_subspace_nonsym(ctx, ncols, G, M, sigma, pp, Ys);
+        if (ist == OFRR_SUCCESS) Yc = Ys;
+        else if (ist != OFRR_ERR_SINGULAR_MATRIX) return ist;
+      }
+      // Wb = V [U(:, :k), Yc, -M^-1 G(:, last)] (+ A v_last in the last column): the k Ritz vectors, then
+      // the next block
+      OFRR_TRY(kry_coef_matrix(ctx, ncols, k, U, pp, Yc, xg, Cf));
+      tw = (t == OFRR_F64) ? OFRR_F64 : OFRR_F32;
+      ctx->emulate_f64 = mixed && t == OFRR_F64;
+      rst = kry_backtransform(ctx, t, n, ncols, S.V, S.ldv, Cf, k + pp + 1, tw, Wb, ld);
+      ctx->emulate_f64 = false;
+      OFRR_TRY(rst);
+      OFRR_TRY(kry_add_col(ctx, tw, n, (char*)Wb + (size_t)(k + pp) * ld * dtype_size(tw), tav,
+                           (const char*)AVb + (size_t)(ncols - 1) * ld * dtype_size(tav)));
+    }
+    cycles++;
+    in_phase++;
+    // (4) true FP64 residuals of the k leading Ritz vectors
+    ts.next("check");
+    OFRR_TRY(residuals_dev(ctx, op, tw, Wb, ld, k, hd.data(), -1.0, hres.data()));
+    double maxres = 0;
+    for (int j = 0; j < k; ++j) maxres = std::max(maxres, hres[j]);
+    if (opt->tol > 0 && maxres <= opt->tol) {
+      converged = true;
+      break;
+    }
+    if (hstop >= 0 || steps >= opt->maxiter) break;  // invariant subspace found, or the step budget spent
+    // (5) next block: the kept block and the residual direction, or (phase change) the sum of the unit
+    //     Ritz vectors alone
+    const double switch_at = (t == OFRR_BF16) ? 1e-2 : 1e-3;
+    const bool stalled = in_phase >= 3 && maxres > 0.7 * best_in_phase;
+    best_in_phase = std::min(best_in_phase, maxres);
+    if (mixed && phase == 0 && (maxres <= switch_at || stalled)) {
+      OFRR_TRY(column_norms(ctx, tw, n, k, Wb, ld, nrm));
+      OFRR_TRY(kry_sum_unit_cols(ctx, tw, n, k, Wb, ld, nrm, svec));
+      OFRR_CUDA(cudaMemcpyAsync(Wb, svec, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+      tw = OFRR_F64;
+      blk = Wb;
+      q0 = 1;
+      phase = 1;
+      in_phase = 0;
+      best_in_phase = INFINITY;
+      escalations++;
+      OFRR_TRY(kry_state_init(ctx, &S, &A->csr, OFRR_F64, nb, stol));
+    } else {
+      blk = (char*)Wb + (size_t)k * ld * dtype_size(tw);
+      q0 = pp + 1;
+    }
+  }
+  // Ritz vectors (FP64) and values out
+  OFRR_TRY(cast_impl(ctx, tw, OFRR_F64, n, k, Wb, ld, X, ldx));
+  OFRR_TRY(sync_and_check(ctx));
+  int conv = 0;
+  double maxr = 0;
+  for (int j = 0; j < nev; ++j) {
+    evals[j] = (j < k) ? hd[j] : NAN;
+    if (resid) resid[j] = (j < k) ? hres[j] : NAN;
+  }
+  for (int j = 0; j < k; ++j) {
+    conv += (opt->tol > 0 && hres[j] <= opt->tol) ? 1 : 0;
+    maxr = std::max(maxr, hres[j]);
+  }
+  if (info) {
+    info->iterations = cycles;
+    info->matvecs = steps + nmv;
+    info->converged = conv;
+    info->basis_width = ncols;
+    info->max_residual = maxr;
+    info->escalations = escalations;
+    info->status_detail = 0;
+  }
+  if (opt->tol > 0 && !converged) return OFRR_ERR_SOLVER_MAX_ITERATIONS;
+  return OFRR_SUCCESS;
+}
+
+// ======================================================================================
 // Krylov eigensolver: Hessenberg process with restarts (arnoldi_hess_eig.m:51-107)
 // ======================================================================================
 static int arnoldi_eig_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, const void* v0,
@@ -942,6 +1162,11 @@ static int arnoldi_eig_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_op
   if (A->nrows != A->ncols) return OFRR_ERR_BLAS_INVALID_SIZE;
   if (opt->orth != OFRR_ORTH_HESSENBERG && opt->orth != OFRR_ORTH_MGS) return OFRR_ERR_INVALID_ARGUMENT;
   const bool mgs = opt->orth == OFRR_ORTH_MGS;
+  if (!mgs && opt->mode != OFRR_MODE_REFERENCE && A->kind == OFRR_OP_CSR && opt->restart_keep != 1) {
+    if (A->nrows == 0 || opt->nev <= 0) return OFRR_SUCCESS;
+    if (!X || ldx < A->nrows || !evals || (opt->use_start_block && !v0)) return OFRR_ERR_INVALID_ARGUMENT;
+    return arnoldi_thick_body(ctx, A, opt, v0, X, ldx, evals, resid, info);
+  }
   const int64_t n = A->nrows;
   const int kdim = opt->kdim > 0 ? opt->kdim : opt->maxiter;
   const int nev = (int)std::min<int64_t>(opt->nev, n);

@@ -724,6 +724,96 @@ def arnoldi_hess_eig(A, n: int, k: int, pc: str = "double", po: Optional[str] = 
     return Vout, d, info
 
 
+def arnoldi_thick_eig(A, n: int, k: int, kdim: int, tol: float, keep: Optional[int] = None, maxsteps: int = 100000,
+                      v0: Optional[np.ndarray] = None, seed: int = 42, symmetric: bool = False,
+                      generalized_tol: float = 0.0, callback: Optional[Callable] = None):
+    """Thick-restart Hessenberg-process Krylov eigensolver in FP64: the restatement of the library's
+    production Krylov path (its FP64 mode), for parity tests.
+
+    The Krylov steps follow ``+src/+krylov/arnoldi_hess_eig.m:73-87`` (A times the previous column,
+    eliminations in MGS order with the coefficients read at the earlier pivot rows, pivot on the first
+    largest entry, scale) and the Rayleigh-Ritz step its generalized form (``:89-95``, eig(V'AV, V'V)).
+    The restart is new (``:99-106`` keeps the leading Ritz vector alone): a basis Y of the invariant
+    subspace of the projected pencil for its leading eigenvalues (about ``keep`` of them, cut at the widest
+    gap of the real parts within keep-3 .. keep+4: the Ritz vectors for a symmetric operator, sorted real
+    Schur vectors otherwise) and the Galerkin residual direction f = A v_last - V (V'V)^-1 V' A v_last;
+    the next basis is the Hessenberg basis of [Y, f] (columns first scaled to a unit maximum,
+    near-dependent ones dropped below 1e-12) continued by Krylov steps from f.  Stops when the k leading
+    Ritz pairs have ||A x - l x|| / (max|l| ||x||) <= tol or after ``maxsteps`` Krylov steps.  Returns
+    (X (n x k, unit columns), d (k), info) with info = {'cycles', 'steps', 'residuals'}.
+    """
+    k = min(k, n)
+    if keep is None or keep <= 0:
+        keep = min(max(k + 4, (k * 6 + 4) // 5), kdim - 2)
+    keep = min(max(keep, k), kdim - 2)
+    nb = kdim + 1
+    W = (randn_block(seed, n, 1) if v0 is None else np.asarray(v0, dtype=np.float64).reshape(n, 1)).copy()
+    info = {"cycles": 0, "steps": 0, "residuals": None}
+    while True:
+        W = scalecols(W, "double", "double")
+        Q, R, sel, perm = hessenberg(W, "double", "double", select_tol=1e-12)
+        cols = [Q[:, j].copy() for j in range(W.shape[1]) if sel[j]]
+        piv = [int(perm[j]) for j in range(W.shape[1]) if sel[j]]
+        stop = False
+        while len(cols) < nb:
+            w = matvec_auto(A, "N", cols[-1], "double", "double")
+            info["steps"] += 1
+            for q, pv in zip(cols, piv):
+                w = w - w[pv] * q
+            w[piv] = 0.0
+            l = _argmax_abs(w)
+            if w[l] == 0.0:
+                stop = True
+                break
+            cols.append(w / w[l])
+            piv.append(l)
+        V = np.column_stack(cols)
+        AV = np.column_stack([matvec_auto(A, "N", V[:, j], "double", "double") for j in range(V.shape[1])])
+        G = V.T @ AV
+        M = V.T @ V + generalized_tol * np.eye(V.shape[1])
+        if symmetric:
+            lam, Z = sla.eigh(0.5 * (G + G.T), M)
+            idx = np.argsort(-lam, kind="stable")
+            w_all, Z = lam[idx].astype(complex), Z[:, idx].astype(complex)
+        else:
+            w_all, Z = sla.eig(G, M)
+            idx = np.argsort(-w_all.real, kind="stable")
+            w_all, Z = w_all[idx], Z[:, idx]
+        kk = min(k, V.shape[1])
+        X = (V @ Z[:, :kk]).real
+        lam = w_all[:kk].real
+        AX = matvec_auto(A, "N", X, "double", "double")
+        nrm = np.linalg.norm(X, axis=0)
+        scale = max(np.max(np.abs(lam)), 1e-300)
+        res = np.linalg.norm(AX - X * lam[None, :], axis=0) / (scale * nrm)
+        info["cycles"] += 1
+        info["residuals"] = res
+        if callback is not None:
+            callback(info["cycles"], lam, res)
+        if np.max(res) <= tol or stop or info["steps"] >= maxsteps:
+            return X / nrm[None, :], lam, info
+        nc = V.shape[1]
+        re = w_all.real
+        pp, best = min(keep, nc - 1), -1.0
+        for c in range(max(k, keep - 3), min(keep + 4, nc - 2) + 1):  # the widest gap near `keep`
+            if re[c - 1] - re[c] > best:
+                best, pp = re[c - 1] - re[c], c
+        if best <= 0:
+            pp = min(keep, nc - 1)
+        if symmetric:
+            Y = V @ Z[:, :pp].real
+        else:
+            # the invariant subspace of the eigenvalues with real part above sigma (sorted real Schur form;
+            # the GPU path gets the same subspace from the matrix sign function)
+            sigma = 0.5 * (re[pp - 1] + re[pp])
+            Lc = np.linalg.cholesky(M)
+            C = sla.solve_triangular(Lc, sla.solve_triangular(Lc, G.T, lower=True).T, lower=True)
+            T, S, sdim = sla.schur(C, output="real", sort=lambda x, y: x > sigma)
+            Y = V @ sla.solve_triangular(Lc.T, S[:, :sdim], lower=False)
+        f = AV[:, -1] - V @ np.linalg.solve(M, G[:, -1])
+        W = np.column_stack([Y, f])
+
+
 def arnoldi_mgs_eig(A, n: int, k: int, pc: str = "double", po: Optional[str] = None, peig: str = "double",
                     seed: int = 42, maxiter: int = 5, kdim: Optional[int] = None, reorth: bool = True,
                     use_generalized: bool = False, generalized_tol: float = 0.0,

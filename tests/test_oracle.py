@@ -202,3 +202,34 @@ def test_oracle_hessenberg_keeps_all_nan_column():
     A[:, 1] = np.nan
     Q, R, sel, perm = orc.hessenberg(A, "double")
     assert sel[1] and perm[1] == 0 and np.all(np.isnan(Q[:, 1]))
+
+
+def test_oracle_thick_restart_convdiff_analytic():
+    """The thick-restart restatement (the production Krylov path) converges to the analytic spectrum of the
+    nonsymmetric 3D convection-diffusion operator."""
+    A = orc.convdiff_3d(8)
+    ex = orc.convdiff_3d_eigs(8)
+    X, d, info = orc.arnoldi_thick_eig(orc.sparse2csr(A), A.shape[0], 12, 40, 1e-10)
+    assert np.max(info["residuals"]) <= 1e-10
+    assert np.max(np.abs(d - ex[:12])) <= 1e-9 * ex[0]
+    R = A @ X - X * d[None, :]
+    assert np.max(np.linalg.norm(R, axis=0)) <= 1e-10 * np.max(np.abs(d)) * 1.01
+
+
+def test_oracle_thick_restart_symmetric():
+    L = orc.laplacian_2d(16)
+    ex = orc.laplacian_2d_eigs(16)
+    X, d, info = orc.arnoldi_thick_eig(orc.sparse2csr(L), L.shape[0], 6, 30, 1e-11, symmetric=True)
+    assert np.max(np.abs(d - ex[:6])) <= 1e-10 * ex[0]
+
+
+def test_problem_generators_match_oracle():
+    """The package's host-side generators (the bench inputs) equal the oracle's operators."""
+    from mixedprecisionofrr_gb300 import problems
+
+    A = problems.convdiff_3d(6)
+    B = orc.convdiff_3d(6)
+    assert abs(A - B).max() == 0
+    assert np.allclose(problems.convdiff_3d_eigs(6), orc.convdiff_3d_eigs(6), rtol=0, atol=1e-9)
+    assert abs(problems.laplacian(7, 2) - orc.laplacian_2d(7)).max() == 0
+    assert np.allclose(problems.laplacian_eigs(7, 2), orc.laplacian_2d_eigs(7), rtol=0, atol=1e-9)
