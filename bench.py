@@ -51,6 +51,10 @@ def parse():
                     help="time the Gaussian kernel generator (16384 points in 3D) against the HBM peak")
     ap.add_argument("--csr-load", action="store_true",
                     help="time reading the 128^3 7-point CSR operator (on-disk format) into HBM")
+    ap.add_argument("--config", default="c2", choices=["c2", "c3"],
+                    help="c2: the dense SVD headline (default; also runs a compact C3 leg); c3: the 128^3 "
+                         "convection-diffusion Krylov workload alone")
+    ap.add_argument("--no-c3", action="store_true", help="skip the C3 leg of the default run")
     ap.add_argument("--mixed-config", default=None, metavar="B,S",
                     help="block width and power steps of the mixed path instead of the autotuner's choice")
     return ap.parse_args()
@@ -437,6 +441,129 @@ def csr_load_run(api, N=128, reps=3):
             "ms_host_path": times[False] * 1e3, "GBps_host_path": nbytes / times[False] / 1e9}
 
 
+C3_N, C3_NEV, C3_KDIM, C3_TOL = 128, 20, 64, 1e-8
+C3_METRIC = ("converged eigenpairs/s at residual <= 1e-8 (3D 7-point convection-diffusion 128^3, Pe 10, "
+             "20 eigenvalues of largest real part, Krylov dim 64 with thick restarts)")
+
+
+def c3_solve(api, Acsr, mode):
+    """One thick-restart Krylov solve of the 128^3 convection-diffusion operator; returns (X, d, info)."""
+    return api.arnoldi_hess_eig(Acsr, Acsr.shape[0], C3_NEV, "single", "half" if mode == "mixed" else None,
+                                maxiter=40000, kdim=C3_KDIM, mode=mode, tol=C3_TOL)
+
+
+def c3_cpu_sample(A, steps_total, cycles, nsteps=12, i_mid=32):
+    """The host cores on a bounded sample of the C3 solve (FP64 NumPy/SciPy, the oracle's arithmetic):
+    nsteps Krylov steps at the mean basis width (CSR matvec + eliminations against i_mid columns) and one
+    Rayleigh-Ritz (A V for 65 columns, the two Gram matrices), scaled to the GPU solve's step and cycle
+    counts.  Returns (seconds per solve, sample description)."""
+    from oracle import ofrr_oracle as orc
+
+    n = A.shape[0]
+    Ac = orc.sparse2csr(A)
+    rng = np.random.default_rng(0)
+    V = rng.standard_normal((n, C3_KDIM + 1))
+    piv = list(rng.choice(n, i_mid, replace=False))
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        w = orc.matvec_auto(Ac, "N", V[:, i_mid], "double", "double")
+        w = w - V[:, :i_mid] @ w[piv]
+        w[piv] = 0.0
+        V[:, i_mid] = w / w[int(np.argmax(np.abs(w)))]
+    t_step = (time.perf_counter() - t0) / nsteps
+    t0 = time.perf_counter()
+    AV = orc.matvec_auto(Ac, "N", V, "double", "double")
+    G = V.T @ AV
+    M = V.T @ V
+    t_rr = time.perf_counter() - t0
+    assert np.isfinite(G[0, 0] + M[0, 0])
+    secs = steps_total * t_step + cycles * t_rr
+    return secs, (f"{nsteps} FP64 Krylov steps at basis width {i_mid} ({1e3 * t_step:.0f} ms each) and one "
+                  f"Rayleigh-Ritz ({t_rr:.2f} s) on the 128^3 operator, scaled to the GPU solve's {steps_total} "
+                  f"operator applications and {cycles} cycles")
+
+
+def c3_run(api, steps, warmup, cpu=True):
+    """The nonsymmetric sparse workload: mixed path (16-bit then FP64 phase) vs the plain FP64 path."""
+    import torch
+    from mixedprecisionofrr_gb300 import problems
+
+    A = problems.convdiff_3d(C3_N)
+    ex = problems.convdiff_3d_eigs(C3_N, count=C3_NEV)
+    Acsr = api.CsrMatrix(A, symmetric=False)
+    stream = api.context().stream
+    out = {"workload": "3D convection-diffusion 128^3 (n 2,097,152, nnz 14,581,760), Pe 10, w (1,0.5,0.25), "
+                       "20 eigenvalues of largest real part, kdim 64, tol 1e-8",
+           "metric": C3_METRIC, "unit": "eigenpairs/s"}
+    for _ in range(warmup):
+        c3_solve(api, Acsr, "mixed")
+    ts, infos = [], []
+    d = None
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        X, d, info = c3_solve(api, Acsr, "mixed")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) / 1e3)
+        infos.append(info)
+    ts = np.array(ts)
+    out.update({"value": C3_NEV * len(ts) / float(ts.sum()), "ms_per_solve": 1e3 * float(ts.mean()),
+                "p50_ms": 1e3 * float(np.percentile(ts, 50)), "p99_ms": 1e3 * float(np.percentile(ts, 99)),
+                "status": sorted({i.status for i in infos}), "cycles": infos[-1].iterations,
+                "matvecs": infos[-1].matvecs, "escalations": infos[-1].escalations,
+                "max_residual": float(max(i.max_residual for i in infos)),
+                "max_rel_eig_err": float(np.max(np.abs(d - ex)) / ex[0]),
+                "dtype": "f16 basis / f32 matvec+arithmetic, then f64 (Grams and Ritz products emulated on tcgen05)"})
+    # plain FP64 GPU path (same algorithm, every operand FP64, library DGEMM for the Gram and Ritz products)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    X64, d64, i64 = c3_solve(api, Acsr, "fp64")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t64 = e0.elapsed_time(e1) / 1e3
+    out["fp64_path"] = {"value": C3_NEV / t64, "ms_per_solve": 1e3 * t64, "cycles": i64.iterations,
+                        "matvecs": i64.matvecs, "status": i64.status, "max_residual": i64.max_residual,
+                        "max_rel_eig_err": float(np.max(np.abs(d64 - ex)) / ex[0])}
+    out["speedup_vs_fp64"] = out["value"] / out["fp64_path"]["value"]
+    # end to end: CSR arrays from pinned host memory, the solve, Ritz vectors and values back
+    ip = torch.from_numpy(A.indptr.astype(np.int32)).pin_memory()
+    ix = torch.from_numpy(A.indices.astype(np.int32)).pin_memory()
+    vd = torch.from_numpy(A.data.astype(np.float64)).pin_memory()
+    vs = torch.from_numpy(A.data.astype(np.float32)).pin_memory()
+    Xh = torch.empty((C3_NEV, A.shape[0]), dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Ae = api.CsrMatrix.__new__(api.CsrMatrix)
+    Ae.shape, Ae.nnz, Ae.symmetric = A.shape, A.nnz, False
+    Ae.indptr, Ae.indices = ip.to("cuda", non_blocking=True), ix.to("cuda", non_blocking=True)
+    Ae.a_double, Ae.a_single = vd.to("cuda", non_blocking=True), vs.to("cuda", non_blocking=True)
+    Ae.a_half = Ae.a_single  # never read by this path
+    torch.cuda.synchronize()
+    Xe, de, ie = c3_solve(api, Ae, "mixed")
+    Xh.copy_(Xe.t(), non_blocking=True)
+    torch.cuda.synchronize()
+    te = time.perf_counter() - t0
+    h2d = (A.indptr.size + A.indices.size) * 4 + A.data.size * 12
+    out["e2e"] = {"value": C3_NEV / te, "unit": "eigenpairs/s", "ms_per_step": 1e3 * te, "h2d_bytes_per_step": h2d,
+                  "d2h_bytes_per_step": C3_NEV * A.shape[0] * 8 + C3_NEV * 8, "status": ie.status}
+    # roofline of the dominant kernel, the fused Krylov step (live CUDA events; the operator and the basis,
+    # 125 + 272 MB, exceed L2, so back-to-back launches stream from HBM)
+    pk = ROOT / "MEASURED_PEAKS.json"
+    peaks = json.loads(pk.read_text()) if pk.exists() else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    roof = {"peak_GBps": hbm, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+    for prec, i in (("half", 16), ("half", 40), ("half", 64), ("double", 40)):
+        us, by = api.profile_krylov_step(Acsr, prec, i, reps=20)
+        roof[f"{prec}_i{i}"] = {"us": us, "bytes": by, "GBps": by / us / 1e3, "frac": by / us / 1e3 / hbm}
+    out["roofline_krylov_step"] = roof
+    if cpu:
+        secs, sample = c3_cpu_sample(A, out["matvecs"], out["cycles"])
+        out["cpu_baseline"] = {"value": C3_NEV / secs, "unit": "eigenpairs/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": sample}
+    return out
+
+
 CPU_GRID = ((64, 96, 128), (4, 6, 8))  # block widths x power steps, the GPU autotuner's grid
 
 
@@ -525,6 +652,9 @@ def main():
         return
     if args.csr_load:
         print(json.dumps(csr_load_run(api)))
+        return
+    if args.config == "c3":
+        print(json.dumps(c3_run(api, args.steps, args.warmup)))
         return
     A, s_true = make_problem_gpu()
     if args.orth_compare:
@@ -633,6 +763,7 @@ def main():
             "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof,
             "roofline_16bit_phase": roof16, "cpu_baseline": cpu,
+            "c3": None if args.no_c3 else c3_run(api, min(args.steps, 2), 1, cpu=not args.no_cpu_baseline),
         }
         print(json.dumps(out))
     if world > 1:
