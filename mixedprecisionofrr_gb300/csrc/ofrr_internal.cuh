@@ -455,6 +455,9 @@ int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
               int64_t lda, const void* B, int64_t ldb, double beta, void* C, int64_t ldc);
 int csrmm_impl(ofrr_ctx* ctx, const ofrr_csr* A, int trans, ofrr_dtype tx, ofrr_dtype tc, ofrr_dtype ty,
                int64_t nrhs, const void* X, int64_t ldx, void* Y, int64_t ldy);
+// A' as CSR (row pointers, rows sorted within each column, every value copy present in A), in ctx's
+// current workspace scope; deterministic
+int csr_transpose_impl(ofrr_ctx* ctx, const ofrr_csr* A, ofrr_csr* At);
 int cast_transpose_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, int64_t m, int64_t n, const void* in,
                         int64_t ldin, void* out, int64_t ldout);
 int cast_impl(ofrr_ctx* ctx, ofrr_dtype tin, ofrr_dtype tout, int64_t m, int64_t n, const void* in,

@@ -61,7 +61,10 @@ struct Op {
   // once, subspace_iter_eig.m:56-58), computed in tc, stored as ty.
   int apply(ofrr_ctx* ctx, int trans, ofrr_dtype ta, ofrr_dtype tx, const void* X, int64_t ldx, int64_t nrhs,
             ofrr_dtype tc, ofrr_dtype ty, void* Y, int64_t ldy) {
-    if (A->kind == OFRR_OP_CSR) return csrmm_impl(ctx, &A->csr, trans, tx, tc, ty, nrhs, X, ldx, Y, ldy);
+    if (A->kind == OFRR_OP_CSR) {
+      if (trans && have_csrT) return csrmm_impl(ctx, &csrT, 0, tx, tc, ty, nrhs, X, ldx, Y, ldy);
+      return csrmm_impl(ctx, &A->csr, trans, tx, tc, ty, nrhs, X, ldx, Y, ldy);
+    }
     const void* Ad;
     int64_t lda;
     const int64_t M = trans ? n() : m(), K = trans ? m() : n();
@@ -146,6 +149,17 @@ struct Op {
     SlicedOperand t;
     OFRR_TRY(sliced_prepare_into(ctx, n(), m(), At, n(), sAt.stack, sAt.expo, &t));
     have_sAt = true;
+    return OFRR_SUCCESS;
+  }
+
+  // the transpose of a CSR operator, built once per solve for the A' U products (deterministic); must be
+  // called in the solve's outermost workspace scope
+  ofrr_csr csrT{};
+  bool have_csrT = false;
+  int prepare_csr_t(ofrr_ctx* ctx) {
+    if (A->kind != OFRR_OP_CSR || have_csrT) return OFRR_SUCCESS;
+    OFRR_TRY(csr_transpose_impl(ctx, &A->csr, &csrT));
+    have_csrT = true;
     return OFRR_SUCCESS;
   }
 
@@ -572,6 +586,7 @@ extern "C" int ofrr_rr_eig(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
   const Precisions P = precisions_of(opt);
   WsScope scope(ctx);
   Op op{A};
+  OFRR_TRY(op.prepare_csr_t(ctx));
   double* d;
   OFRR_TRY(dmalloc(ctx, &d, (size_t)ncols));
   // eig_rr on V (type p_output): pmc = p_rr_compute, pmo = p_rr_output, A-matvec in (p_compute, p_output)
@@ -915,6 +930,7 @@ extern "C" int ofrr_rr_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
   const Precisions P = precisions_of(opt);
   WsScope scope(ctx);
   Op op{A};
+  OFRR_TRY(op.prepare_csr_t(ctx));
   double* d;
   OFRR_TRY(dmalloc(ctx, &d, (size_t)ncols));
   const int b = (int)ncols;
@@ -1647,6 +1663,7 @@ static int si_eig_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
   WsScope scope(ctx);
   int st = OFRR_SUCCESS;
   Op op{A};
+  OFRR_TRY(op.prepare_csr_t(ctx));
   const int nev = std::min(opt->nev > 0 ? opt->nev : b0, b0);
   PhaseState S;
   S.b = b0;
@@ -1738,6 +1755,7 @@ static int si_svd_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
   WsScope scope(ctx);
   int st = OFRR_SUCCESS;
   Op op{A};
+  OFRR_TRY(op.prepare_csr_t(ctx));
   const int nev = std::min(opt->nev > 0 ? opt->nev : b0, b0);
   PhaseState S;
   S.b = b0;

@@ -2,9 +2,17 @@
 //
 // Behaviour: MATLAB/+src/+csr/csrmv.m:27-78 -- the value copy of the compute precision is used
 // (sparse2csr.m:48-49), products are accumulated in that precision and the result is stored in
-// the output type.  Layout: thread per row, right-hand sides in register chunks of RC columns;
-// for stencil matrices consecutive rows touch consecutive columns, so a warp's gathers of X are
-// coalesced, and the row's nonzeros are read once per chunk.  'T' is a scatter with atomics.
+// the output type.
+//
+// Layout ('N'): a CTA owns 256 consecutive rows, one per thread.  The CTA's nonzeros (a contiguous
+// range of the value and index arrays) are first copied into shared memory with coalesced loads, so
+// the CSR arrays are read from HBM once for all right-hand sides; each thread then walks its row in
+// shared memory for every chunk of RC columns.  For stencil operators consecutive rows touch
+// consecutive columns, so a warp's gathers of X are coalesced.  CTAs whose nonzeros exceed the staging
+// capacity read them from global memory instead (same arithmetic, same order).
+// 'T' applies the 'N' kernel to the transpose, built once per call (or once per solve, Op::prepare_csr_t)
+// with a deterministic counting sort, so results never depend on the schedule (no floating-point
+// atomics).
 #include "ofrr_internal.cuh"
 
 namespace ofrr {
@@ -19,45 +27,207 @@ template <> struct CsrVals<float> {
   using T = float;
 };
 
+constexpr int kSpmmRows = 256;
+constexpr int kSpmmCap = 2048;  // staged nonzeros per CTA (8 per row on average)
+
 template <class TX, class TC, class TY, int RC>
-__global__ void __launch_bounds__(256) k_csrmm_n(int64_t nrows, const int32_t* __restrict__ indptr,
-                                                 const int32_t* __restrict__ indices, const TC* __restrict__ vals,
-                                                 int64_t nrhs, const TX* __restrict__ X, int64_t ldx,
-                                                 TY* __restrict__ Y, int64_t ldy) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < nrows; row += stride) {
-    const int32_t p0 = __ldg(indptr + row), p1 = __ldg(indptr + row + 1);
-    for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
-      TC acc[RC];
+__global__ void __launch_bounds__(kSpmmRows) k_csrmm_n(int64_t nrows, const int32_t* __restrict__ indptr,
+                                                       const int32_t* __restrict__ indices,
+                                                       const TC* __restrict__ vals, int64_t nrhs,
+                                                       const TX* __restrict__ X, int64_t ldx, TY* __restrict__ Y,
+                                                       int64_t ldy) {
+  __shared__ TC s_val[kSpmmCap];
+  __shared__ int32_t s_idx[kSpmmCap];
+  const int64_t r0 = (int64_t)blockIdx.x * kSpmmRows;
+  if (r0 >= nrows) return;
+  const int64_t rend = min(nrows, r0 + kSpmmRows);
+  const int32_t pbase = __ldg(indptr + r0), pend = __ldg(indptr + rend);
+  const bool staged = (pend - pbase) <= kSpmmCap;
+  if (staged) {
+    for (int32_t e = threadIdx.x; e < pend - pbase; e += kSpmmRows) {
+      s_val[e] = __ldg(vals + pbase + e);
+      s_idx[e] = __ldg(indices + pbase + e);
+    }
+  }
+  __syncthreads();
+  const int64_t row = r0 + threadIdx.x;
+  if (row >= rend) return;
+  const int32_t p0 = __ldg(indptr + row), p1 = __ldg(indptr + row + 1);
+  for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
+    TC acc[RC];
 #pragma unroll
-      for (int r = 0; r < RC; ++r) acc[r] = TC(0);
-      for (int32_t p = p0; p < p1; ++p) {
-        const int64_t col = __ldg(indices + p);
-        const TC a = __ldg(vals + p);
+    for (int r = 0; r < RC; ++r) acc[r] = TC(0);
+    for (int32_t p = p0; p < p1; ++p) {
+      const int64_t col = staged ? s_idx[p - pbase] : __ldg(indices + p);
+      const TC a = staged ? s_val[p - pbase] : __ldg(vals + p);
 #pragma unroll
-        for (int r = 0; r < RC; ++r) {
-          if (c0 + r < nrhs) acc[r] = fma(a, to_c<TC, TX>(X[col + (c0 + r) * ldx]), acc[r]);
-        }
+      for (int r = 0; r < RC; ++r) {
+        if (c0 + r < nrhs) acc[r] = fma(a, to_c<TC, TX>(X[col + (c0 + r) * ldx]), acc[r]);
       }
+    }
 #pragma unroll
-      for (int r = 0; r < RC; ++r)
-        if (c0 + r < nrhs) Y[row + (c0 + r) * ldy] = from_c<TY, TC>(acc[r]);
+    for (int r = 0; r < RC; ++r)
+      if (c0 + r < nrhs) Y[row + (c0 + r) * ldy] = from_c<TY, TC>(acc[r]);
+  }
+}
+
+// ---- deterministic CSR transpose -------------------------------------------------------------
+__global__ void k_csrt_count(int64_t nnz, const int32_t* __restrict__ indices, int32_t* __restrict__ cnt) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnz; p += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&cnt[indices[p]], 1);  // integer counts: the result does not depend on the order
+}
+
+// exclusive scan of n counts into out (n + 1 entries) by one CTA of 1024 threads, chunk by chunk
+__global__ void __launch_bounds__(1024) k_csrt_scan(int64_t n, const int32_t* __restrict__ cnt,
+                                                    int32_t* __restrict__ out) {
+  __shared__ int32_t s[1024];
+  __shared__ int32_t s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < n; base += 1024) {
+    const int64_t i = base + threadIdx.x;
+    const int32_t v = (i < n) ? cnt[i] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {  // Hillis-Steele inclusive scan
+      const int32_t t = (threadIdx.x >= off) ? s[threadIdx.x - off] : 0;
+      __syncthreads();
+      s[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < n) out[i] = s_carry + s[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += s[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = s_carry;
+}
+
+// each nonzero (row i, column j) goes to column j's segment; rows taken in order by one thread per row
+// chunk would serialise, so the slot comes from an atomic cursor and each segment is sorted afterwards
+__global__ void k_csrt_fill(int64_t nrows, const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                            const int32_t* __restrict__ colptr, int32_t* __restrict__ cursor,
+                            int32_t* __restrict__ rowidx, int32_t* __restrict__ src) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
+    for (int32_t p = indptr[r]; p < indptr[r + 1]; ++p) {
+      const int32_t j = indices[p];
+      const int32_t slot = colptr[j] + atomicAdd(&cursor[j], 1);
+      rowidx[slot] = (int32_t)r;
+      src[slot] = p;
     }
   }
 }
 
-template <class TX, class TC>
-__global__ void k_csrmm_t(int64_t nrows, const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
-                          const TC* __restrict__ vals, int64_t nrhs, const TX* __restrict__ X, int64_t ldx,
-                          TC* __restrict__ Yacc, int64_t ldy) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < nrows; row += stride) {
-    const int32_t p0 = indptr[row], p1 = indptr[row + 1];
-    for (int64_t c = 0; c < nrhs; ++c) {
-      const TC x = to_c<TC, TX>(X[row + c * ldx]);
-      for (int32_t p = p0; p < p1; ++p) atomicAdd(&Yacc[indices[p] + c * ldy], vals[p] * x);
+// sort each column segment by row (insertion sort: segments of sparse operators are short), carrying
+// the source position; then gather the values of every precision present
+__global__ void k_csrt_sort(int64_t ncols, const int32_t* __restrict__ colptr, int32_t* __restrict__ rowidx,
+                            int32_t* __restrict__ src) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < ncols; j += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t b = colptr[j], e = colptr[j + 1];
+    for (int32_t p = b + 1; p < e; ++p) {
+      const int32_t r = rowidx[p], sp = src[p];
+      int32_t q = p - 1;
+      while (q >= b && rowidx[q] > r) {
+        rowidx[q + 1] = rowidx[q];
+        src[q + 1] = src[q];
+        --q;
+      }
+      rowidx[q + 1] = r;
+      src[q + 1] = sp;
     }
   }
+}
+
+template <class TV>
+__global__ void k_csrt_gather(int64_t nnz, const int32_t* __restrict__ src, const TV* __restrict__ v,
+                              TV* __restrict__ vt) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnz; p += (int64_t)gridDim.x * blockDim.x)
+    vt[p] = v[src[p]];
+}
+
+int csr_transpose_impl(ofrr_ctx* ctx, const ofrr_csr* A, ofrr_csr* At) {
+  int st = OFRR_SUCCESS;
+  const int64_t m = A->nrows, n = A->ncols, nnz = A->nnz;
+  *At = ofrr_csr{};
+  At->nrows = n;
+  At->ncols = m;
+  At->nnz = nnz;
+  int32_t* colptr = ws_get<int32_t>(ctx, (size_t)n + 1, &st);
+  int32_t* cursor = ws_get<int32_t>(ctx, (size_t)n + 1, &st);
+  int32_t* rowidx = ws_get<int32_t>(ctx, (size_t)std::max<int64_t>(nnz, 1), &st);
+  int32_t* src = ws_get<int32_t>(ctx, (size_t)std::max<int64_t>(nnz, 1), &st);
+  if (!colptr || !cursor || !rowidx || !src) return st;
+  OFRR_TRY(fill_zero(ctx, cursor, sizeof(int32_t) * ((size_t)n + 1)));
+  const int g = grid_for(std::max<int64_t>(nnz, 1), 256, 152 * 16);
+  if (nnz > 0) {
+    k_csrt_count<<<g, 256, 0, ctx->stream>>>(nnz, A->indices, cursor);
+    OFRR_LAUNCHED(ctx, "k_csrt_count");
+  }
+  k_csrt_scan<<<1, 1024, 0, ctx->stream>>>(n, cursor, colptr);
+  OFRR_LAUNCHED(ctx, "k_csrt_scan");
+  OFRR_TRY(fill_zero(ctx, cursor, sizeof(int32_t) * ((size_t)n + 1)));
+  if (nnz > 0) {
+    k_csrt_fill<<<grid_for(m, 256, 152 * 16), 256, 0, ctx->stream>>>(m, A->indptr, A->indices, colptr,
+                                                                             cursor, rowidx, src);
+    OFRR_LAUNCHED(ctx, "k_csrt_fill");
+    k_csrt_sort<<<grid_for(n, 256, 152 * 16), 256, 0, ctx->stream>>>(n, colptr, rowidx, src);
+    OFRR_LAUNCHED(ctx, "k_csrt_sort");
+  }
+  At->indptr = colptr;
+  At->indices = rowidx;
+  if (A->a_double) {
+    double* v = ws_get<double>(ctx, (size_t)std::max<int64_t>(nnz, 1), &st);
+    if (!v) return st;
+    if (nnz > 0) {
+      k_csrt_gather<double><<<g, 256, 0, ctx->stream>>>(nnz, src, A->a_double, v);
+      OFRR_LAUNCHED(ctx, "k_csrt_gather");
+    }
+    At->a_double = v;
+  }
+  if (A->a_single) {
+    float* v = ws_get<float>(ctx, (size_t)std::max<int64_t>(nnz, 1), &st);
+    if (!v) return st;
+    if (nnz > 0) {
+      k_csrt_gather<float><<<g, 256, 0, ctx->stream>>>(nnz, src, A->a_single, v);
+      OFRR_LAUNCHED(ctx, "k_csrt_gather");
+    }
+    At->a_single = v;
+  }
+  if (A->a_half) {
+    __half* v = ws_get<__half>(ctx, (size_t)std::max<int64_t>(nnz, 1), &st);
+    if (!v) return st;
+    if (nnz > 0) {
+      k_csrt_gather<__half><<<g, 256, 0, ctx->stream>>>(nnz, src, (const __half*)A->a_half, v);
+      OFRR_LAUNCHED(ctx, "k_csrt_gather");
+    }
+    At->a_half = v;
+  }
+  return OFRR_SUCCESS;
+}
+
+static int csrmm_n(ofrr_ctx* ctx, const ofrr_csr* A, ofrr_dtype tx, ofrr_dtype tc, ofrr_dtype ty, int64_t nrhs,
+                   const void* X, int64_t ldx, void* Y, int64_t ldy) {
+  const int64_t blocks = (A->nrows + kSpmmRows - 1) / kSpmmRows;
+  if (blocks > 0x7fffffffLL) return OFRR_ERR_BLAS_INVALID_SIZE;
+  const unsigned grid = (unsigned)blocks;
+  OFRR_DISPATCH_COMPUTE(tc, TC, {
+    const TC* vals = CsrVals<TC>::get(A);
+    if (!vals) return OFRR_ERR_INVALID_ARGUMENT;
+    OFRR_DISPATCH_STORAGE(tx, TX, OFRR_DISPATCH_STORAGE(ty, TY, {
+      if (nrhs == 1) {
+        k_csrmm_n<TX, TC, TY, 1><<<grid, kSpmmRows, 0, ctx->stream>>>(A->nrows, A->indptr, A->indices, vals, nrhs,
+                                                                      (const TX*)X, ldx, (TY*)Y, ldy);
+      } else if (nrhs <= 4) {
+        k_csrmm_n<TX, TC, TY, 4><<<grid, kSpmmRows, 0, ctx->stream>>>(A->nrows, A->indptr, A->indices, vals, nrhs,
+                                                                      (const TX*)X, ldx, (TY*)Y, ldy);
+      } else {
+        k_csrmm_n<TX, TC, TY, 8><<<grid, kSpmmRows, 0, ctx->stream>>>(A->nrows, A->indptr, A->indices, vals, nrhs,
+                                                                      (const TX*)X, ldx, (TY*)Y, ldy);
+      }
+      OFRR_LAUNCHED(ctx, "k_csrmm_n");
+    }));
+  });
+  return OFRR_SUCCESS;
 }
 
 int csrmm_impl(ofrr_ctx* ctx, const ofrr_csr* A, int trans, ofrr_dtype tx, ofrr_dtype tc, ofrr_dtype ty,
@@ -65,45 +235,12 @@ int csrmm_impl(ofrr_ctx* ctx, const ofrr_csr* A, int trans, ofrr_dtype tx, ofrr_
   if (nrhs <= 0) return OFRR_SUCCESS;
   const int64_t nout = trans ? A->ncols : A->nrows;
   if (nout <= 0) return OFRR_SUCCESS;
-  const int block = 256;
-  if (!trans) {
-    const int grid = grid_for(A->nrows, block, 1 << 20);
-    OFRR_DISPATCH_COMPUTE(tc, TC, {
-      const TC* vals = CsrVals<TC>::get(A);
-      if (!vals) return OFRR_ERR_INVALID_ARGUMENT;
-      OFRR_DISPATCH_STORAGE(tx, TX, OFRR_DISPATCH_STORAGE(ty, TY, {
-        if (nrhs == 1) {
-          k_csrmm_n<TX, TC, TY, 1><<<grid, block, 0, ctx->stream>>>(A->nrows, A->indptr, A->indices, vals, nrhs,
-                                                                      (const TX*)X, ldx, (TY*)Y, ldy);
-        } else if (nrhs <= 4) {
-          k_csrmm_n<TX, TC, TY, 4><<<grid, block, 0, ctx->stream>>>(A->nrows, A->indptr, A->indices, vals, nrhs,
-                                                                      (const TX*)X, ldx, (TY*)Y, ldy);
-        } else {
-          k_csrmm_n<TX, TC, TY, 8><<<grid, block, 0, ctx->stream>>>(A->nrows, A->indptr, A->indices, vals, nrhs,
-                                                                      (const TX*)X, ldx, (TY*)Y, ldy);
-        }
-        OFRR_LAUNCHED(ctx, "k_csrmm_n");
-      }));
-    });
-    return OFRR_SUCCESS;
-  }
-  // transposed: accumulate in the compute type, then store
+  if (!trans) return csrmm_n(ctx, A, tx, tc, ty, nrhs, X, ldx, Y, ldy);
+  // transposed: the 'N' product of the transpose (same arithmetic per output entry in a fixed order)
   WsScope scope(ctx);
-  int st = OFRR_SUCCESS;
-  void* acc = ws_alloc(ctx, (size_t)nout * nrhs * dtype_size(tc), &st);
-  if (!acc) return st;
-  OFRR_TRY(fill_zero(ctx, acc, (size_t)nout * nrhs * dtype_size(tc)));
-  const int grid = grid_for(A->nrows, block, 1 << 20);
-  OFRR_DISPATCH_COMPUTE(tc, TC, {
-    const TC* vals = CsrVals<TC>::get(A);
-    if (!vals) return OFRR_ERR_INVALID_ARGUMENT;
-    OFRR_DISPATCH_STORAGE(tx, TX, {
-      k_csrmm_t<TX, TC><<<grid, block, 0, ctx->stream>>>(A->nrows, A->indptr, A->indices, vals, nrhs, (const TX*)X,
-                                                          ldx, (TC*)acc, nout);
-      OFRR_LAUNCHED(ctx, "k_csrmm_t");
-    });
-  });
-  return cast_impl(ctx, tc, ty, nout, nrhs, acc, nout, Y, ldy);
+  ofrr_csr At;
+  OFRR_TRY(csr_transpose_impl(ctx, A, &At));
+  return csrmm_n(ctx, &At, tx, tc, ty, nrhs, X, ldx, Y, ldy);
 }
 
 }  // namespace ofrr

@@ -199,6 +199,37 @@ def test_csrmm_vs_scipy(api, orc, pc, tol):
     assert np.allclose(Y, C.T @ X[:125, :3], rtol=tol * 10, atol=tol * 1e3)
 
 
+def test_csrmm_transposed_deterministic_and_wide(api, orc):
+    """The transposed product runs on a transpose built by a deterministic counting sort (no floating-point
+    atomics): two calls give bit-identical results, equal to the 'N' product of the explicit transpose.
+    Rectangular operator with rows of 0 .. 40 nonzeros (some CTAs exceed the staging capacity), 65
+    right-hand sides (several column chunks over one staging of the nonzeros)."""
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(4)
+    m, n = 3000, 1700
+    lens = rng.integers(0, 41, m)
+    lens[:300] = 40  # the first CTAs hold more nonzeros than the shared-memory staging holds
+    rows = np.repeat(np.arange(m), lens)
+    cols = rng.integers(0, n, rows.size)
+    A = sp.csr_matrix((rng.standard_normal(rows.size), (rows, cols)), shape=(m, n))
+    A.sum_duplicates()
+    A.sort_indices()
+    Ac = api.CsrMatrix(A)
+    X = rng.standard_normal((m, 65))
+    Y1 = api.to_numpy(api.csrmv(Ac, "T", X, "double", "double"))
+    Y2 = api.to_numpy(api.csrmv(Ac, "T", X, "double", "double"))
+    assert np.array_equal(Y1, Y2)
+    At = sp.csr_matrix(A.T)
+    At.sort_indices()
+    Y3 = api.to_numpy(api.csrmv(api.CsrMatrix(At), "N", X, "double", "double"))
+    assert np.array_equal(Y1, Y3)
+    assert np.allclose(Y1, A.T @ X, rtol=1e-13, atol=1e-12)
+    Z = rng.standard_normal((n, 65))
+    YN = api.to_numpy(api.csrmv(Ac, "N", Z, "double", "double"))
+    assert np.allclose(YN, A @ Z, rtol=1e-13, atol=1e-12)
+
+
 def test_syev_sygv_known_answers(api):
     n = 10
     A = np.diag(2 * np.ones(n)) - np.diag(np.ones(n - 1), 1) - np.diag(np.ones(n - 1), -1)
