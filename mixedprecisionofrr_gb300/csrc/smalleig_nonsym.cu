@@ -22,9 +22,10 @@ namespace ofrr {
 
 constexpr int NS_MAX = 128;
 
-__device__ __forceinline__ void cdivf(float xr, float xi, float yr, float yi, float& cr, float& ci) {
-  float r, d;
-  if (fabsf(yr) > fabsf(yi)) {
+template <class T>
+__device__ __forceinline__ void cdivf(T xr, T xi, T yr, T yi, T& cr, T& ci) {
+  T r, d;
+  if (fabs(yr) > fabs(yi)) {
     r = yi / yr;
     d = yr + r * yi;
     cr = (xr + r * xi) / d;
@@ -39,59 +40,61 @@ __device__ __forceinline__ void cdivf(float xr, float xi, float yr, float yi, fl
 
 // One warp.  C: n x n (FP64, ld ldc).  Outputs: wr, wi (n), X (n x n, FP64, ld n): eigenvectors of C
 // (real parts, unit norm), unsorted; *flag = 1 when the QR iteration did not converge.
-__global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __restrict__ C, int ldc,
+template <class T>
+__global__ void __launch_bounds__(32) k_nonsym_eig(int nn, const double* __restrict__ C, int ldc,
                                                        double* __restrict__ wr, double* __restrict__ wi,
                                                        double* __restrict__ X, int* __restrict__ flag,
                                                        int pair_imag) {
-  extern __shared__ float sm[];
+  extern __shared__ unsigned char sm_raw[];
+  T* sm = reinterpret_cast<T*>(sm_raw);
   const int ld = nn + 1;
-  float* H = sm;             // n x n (row i, column j at i + j * ld)
-  float* V = H + nn * ld;    // Schur vectors
-  float* Y = V + nn * ld;    // eigenvectors of the quasi-triangular factor
-  float* ort = Y + nn * ld;  // n
-  float* d = ort + nn;       // n
-  float* e = d + nn;         // n
+  T* H = sm;             // n x n (row i, column j at i + j * ld)
+  T* V = H + nn * ld;    // Schur vectors
+  T* Y = V + nn * ld;    // eigenvectors of the quasi-triangular factor
+  T* ort = Y + nn * ld;  // n
+  T* d = ort + nn;       // n
+  T* e = d + nn;         // n
   const int lane = threadIdx.x;
 #define HH(i, j) H[(i) + (j) * ld]
 #define VV(i, j) V[(i) + (j) * ld]
 #define YY(i, j) Y[(i) + (j) * ld]
   for (int idx = lane; idx < nn * nn; idx += 32) {
     const int i = idx % nn, j = idx / nn;
-    HH(i, j) = (float)C[i + (size_t)j * ldc];
-    VV(i, j) = (i == j) ? 1.f : 0.f;
-    YY(i, j) = 0.f;
+    HH(i, j) = (T)C[i + (size_t)j * ldc];
+    VV(i, j) = (i == j) ? T(1.) : T(0.);
+    YY(i, j) = T(0.);
   }
   __syncwarp();
   const int low = 0, high = nn - 1;
   // ---- Householder reduction to upper Hessenberg form ----
   for (int m = low + 1; m <= high - 1; ++m) {
-    float scale = 0.f;
-    for (int i = m + lane; i <= high; i += 32) scale += fabsf(HH(i, m - 1));
+    T scale = T(0.);
+    for (int i = m + lane; i <= high; i += 32) scale += fabs(HH(i, m - 1));
     for (int o = 16; o > 0; o >>= 1) scale += __shfl_xor_sync(0xffffffffu, scale, o);
-    if (scale == 0.f) continue;
-    float h = 0.f;
+    if (scale == T(0.)) continue;
+    T h = T(0.);
     for (int i = m + lane; i <= high; i += 32) {
       ort[i] = HH(i, m - 1) / scale;
       h += ort[i] * ort[i];
     }
     for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
     __syncwarp();
-    float g = sqrtf(h);
-    if (ort[m] > 0.f) g = -g;
+    T g = sqrt(h);
+    if (ort[m] > T(0.)) g = -g;
     h = h - ort[m] * g;
     __syncwarp();
     if (lane == 0) ort[m] = ort[m] - g;
     __syncwarp();
     // H = (I - u u'/h) H (I - u u'/h)
     for (int j = m + lane; j < nn; j += 32) {
-      float f = 0.f;
+      T f = T(0.);
       for (int i = high; i >= m; --i) f += ort[i] * HH(i, j);
       f /= h;
       for (int i = m; i <= high; ++i) HH(i, j) -= f * ort[i];
     }
     __syncwarp();
     for (int i = lane; i <= high; i += 32) {
-      float f = 0.f;
+      T f = T(0.);
       for (int j = high; j >= m; --j) f += ort[j] * HH(i, j);
       f /= h;
       for (int j = m; j <= high; ++j) HH(i, j) -= f * ort[j];
@@ -105,11 +108,11 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
   }
   // accumulate the transformations (the reflectors below the subdiagonal and in ort)
   for (int m = high - 1; m >= low + 1; --m) {
-    if (HH(m, m - 1) == 0.f) continue;
+    if (HH(m, m - 1) == T(0.)) continue;
     for (int i = m + 1 + lane; i <= high; i += 32) ort[i] = HH(i, m - 1);
     __syncwarp();
     for (int j = m + lane; j <= high; j += 32) {
-      float g = 0.f;
+      T g = T(0.);
       for (int i = m; i <= high; ++i) g += ort[i] * VV(i, j);
       g = (g / ort[m]) / HH(m, m - 1);  // double division avoids underflow
       for (int i = m; i <= high; ++i) VV(i, j) += g * ort[i];
@@ -118,45 +121,45 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
   }
   for (int idx = lane; idx < nn * nn; idx += 32) {  // clear the reflector storage below the subdiagonal
     const int i = idx % nn, j = idx / nn;
-    if (i > j + 1) HH(i, j) = 0.f;
+    if (i > j + 1) HH(i, j) = T(0.);
   }
   __syncwarp();
 
   // ---- Francis double-shift QR to real Schur form (EISPACK hqr2) ----
-  const float eps = 1.1920929e-07f;
+  const T eps = (sizeof(T) == 8) ? T(2.220446049250313e-16) : T(1.1920929e-07);
   int n = nn - 1;
-  float exshift = 0.f, p = 0.f, q = 0.f, r = 0.f, s = 0.f, z = 0.f, t, w, x, y;
-  float norm = 0.f;
+  T exshift = T(0.), p = T(0.), q = T(0.), r = T(0.), s = T(0.), z = T(0.), t, w, x, y;
+  T norm = T(0.);
   for (int i = 0; i < nn; ++i)
-    for (int j = (i > 0 ? i - 1 : 0); j < nn; ++j) norm += fabsf(HH(i, j));
+    for (int j = (i > 0 ? i - 1 : 0); j < nn; ++j) norm += fabs(HH(i, j));
   int iter = 0, total_iter = 0;
   const int max_total = 40 * nn;
   bool failed = false;
   while (n >= low) {
     int l = n;
     while (l > low) {
-      s = fabsf(HH(l - 1, l - 1)) + fabsf(HH(l, l));
-      if (s == 0.f) s = norm;
-      if (fabsf(HH(l, l - 1)) < eps * s) break;
+      s = fabs(HH(l - 1, l - 1)) + fabs(HH(l, l));
+      if (s == T(0.)) s = norm;
+      if (fabs(HH(l, l - 1)) < eps * s) break;
       --l;
     }
     if (l == n) {  // one root
-      const float hn = HH(n, n) + exshift;
+      const T hn = HH(n, n) + exshift;
       __syncwarp();
       if (lane == 0) {
         HH(n, n) = hn;
         d[n] = hn;
-        e[n] = 0.f;
+        e[n] = T(0.);
       }
       __syncwarp();
       --n;
       iter = 0;
     } else if (l == n - 1) {  // two roots
       w = HH(n, n - 1) * HH(n - 1, n);
-      p = (HH(n - 1, n - 1) - HH(n, n)) / 2.f;
+      p = (HH(n - 1, n - 1) - HH(n, n)) / T(2.);
       q = p * p + w;
-      z = sqrtf(fabsf(q));
-      const float hnn = HH(n, n) + exshift, hmm = HH(n - 1, n - 1) + exshift;
+      z = sqrt(fabs(q));
+      const T hnn = HH(n, n) + exshift, hmm = HH(n - 1, n - 1) + exshift;
       __syncwarp();
       if (lane == 0) {
         HH(n, n) = hnn;
@@ -164,37 +167,37 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
       }
       __syncwarp();
       x = hnn;
-      if (q >= 0.f) {  // real pair
-        z = (p >= 0.f) ? p + z : p - z;
-        const float dn1 = x + z;
-        const float dn = (z != 0.f) ? x - w / z : dn1;
+      if (q >= T(0.)) {  // real pair
+        z = (p >= T(0.)) ? p + z : p - z;
+        const T dn1 = x + z;
+        const T dn = (z != T(0.)) ? x - w / z : dn1;
         x = HH(n, n - 1);
-        s = fabsf(x) + fabsf(z);
+        s = fabs(x) + fabs(z);
         p = x / s;
         q = z / s;
-        r = sqrtf(p * p + q * q);
+        r = sqrt(p * p + q * q);
         p /= r;
         q /= r;
         __syncwarp();
         if (lane == 0) {
           d[n - 1] = dn1;
           d[n] = dn;
-          e[n - 1] = 0.f;
-          e[n] = 0.f;
+          e[n - 1] = T(0.);
+          e[n] = T(0.);
         }
         for (int j = n - 1 + lane; j < nn; j += 32) {  // row modification
-          const float zz = HH(n - 1, j);
+          const T zz = HH(n - 1, j);
           HH(n - 1, j) = q * zz + p * HH(n, j);
           HH(n, j) = q * HH(n, j) - p * zz;
         }
         __syncwarp();
         for (int i = lane; i <= n; i += 32) {  // column modification
-          const float zz = HH(i, n - 1);
+          const T zz = HH(i, n - 1);
           HH(i, n - 1) = q * zz + p * HH(i, n);
           HH(i, n) = q * HH(i, n) - p * zz;
         }
         for (int i = low + lane; i <= high; i += 32) {  // accumulate
-          const float zz = VV(i, n - 1);
+          const T zz = VV(i, n - 1);
           VV(i, n - 1) = q * zz + p * VV(i, n);
           VV(i, n) = q * VV(i, n) - p * zz;
         }
@@ -217,8 +220,8 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
         break;
       }
       x = HH(n, n);
-      y = 0.f;
-      w = 0.f;
+      y = T(0.);
+      w = T(0.);
       if (l < n) {
         y = HH(n - 1, n - 1);
         w = HH(n, n - 1) * HH(n - 1, n);
@@ -228,22 +231,22 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
         __syncwarp();
         for (int i = low + lane; i <= n; i += 32) HH(i, i) -= x;
         __syncwarp();
-        s = fabsf(HH(n, n - 1)) + fabsf(HH(n - 1, n - 2));
-        x = y = 0.75f * s;
-        w = -0.4375f * s * s;
+        s = fabs(HH(n, n - 1)) + fabs(HH(n - 1, n - 2));
+        x = y = T(0.75) * s;
+        w = -T(0.4375) * s * s;
       }
       if (iter == 30) {  // the second ad hoc shift
-        s = (y - x) / 2.f;
+        s = (y - x) / T(2.);
         s = s * s + w;
-        if (s > 0.f) {
-          s = sqrtf(s);
+        if (s > T(0.)) {
+          s = sqrt(s);
           if (y < x) s = -s;
-          s = x - w / ((y - x) / 2.f + s);
+          s = x - w / ((y - x) / T(2.) + s);
           __syncwarp();
           for (int i = low + lane; i <= n; i += 32) HH(i, i) -= s;
           __syncwarp();
           exshift += s;
-          x = y = w = 0.964f;
+          x = y = w = T(0.964);
         }
       }
       ++iter;
@@ -256,20 +259,20 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
         p = (r * s - w) / HH(m + 1, m) + HH(m, m + 1);
         q = HH(m + 1, m + 1) - z - r - s;
         r = HH(m + 2, m + 1);
-        s = fabsf(p) + fabsf(q) + fabsf(r);
+        s = fabs(p) + fabs(q) + fabs(r);
         p /= s;
         q /= s;
         r /= s;
         if (m == l) break;
-        if (fabsf(HH(m, m - 1)) * (fabsf(q) + fabsf(r)) <
-            eps * (fabsf(p) * (fabsf(HH(m - 1, m - 1)) + fabsf(z) + fabsf(HH(m + 1, m + 1)))))
+        if (fabs(HH(m, m - 1)) * (fabs(q) + fabs(r)) <
+            eps * (fabs(p) * (fabs(HH(m - 1, m - 1)) + fabs(z) + fabs(HH(m + 1, m + 1)))))
           break;
         --m;
       }
       __syncwarp();
       for (int i = m + 2 + lane; i <= n; i += 32) {
-        HH(i, i - 2) = 0.f;
-        if (i > m + 2) HH(i, i - 3) = 0.f;
+        HH(i, i - 2) = T(0.);
+        if (i > m + 2) HH(i, i - 3) = T(0.);
       }
       __syncwarp();
       // double QR step on rows l..n and columns m..n
@@ -278,17 +281,17 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
         if (k != m) {
           p = HH(k, k - 1);
           q = HH(k + 1, k - 1);
-          r = notlast ? HH(k + 2, k - 1) : 0.f;
-          x = fabsf(p) + fabsf(q) + fabsf(r);
-          if (x == 0.f) continue;
+          r = notlast ? HH(k + 2, k - 1) : T(0.);
+          x = fabs(p) + fabs(q) + fabs(r);
+          if (x == T(0.)) continue;
           p /= x;
           q /= x;
           r /= x;
         }
-        s = sqrtf(p * p + q * q + r * r);
-        if (p < 0.f) s = -s;
-        if (s == 0.f) continue;
-        const float hk = (k != m) ? -s * x : ((l != m) ? -HH(k, k - 1) : 0.f);
+        s = sqrt(p * p + q * q + r * r);
+        if (p < T(0.)) s = -s;
+        if (s == T(0.)) continue;
+        const T hk = (k != m) ? -s * x : ((l != m) ? -HH(k, k - 1) : T(0.));
         const bool set_hk = (k != m) || (l != m);
         p = p + s;
         x = p / s;
@@ -299,7 +302,7 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
         __syncwarp();
         if (lane == 0 && set_hk) HH(k, k - 1) = hk;
         for (int j = k + lane; j < nn; j += 32) {  // row modification
-          float pp = HH(k, j) + q * HH(k + 1, j);
+          T pp = HH(k, j) + q * HH(k + 1, j);
           if (notlast) {
             pp += r * HH(k + 2, j);
             HH(k + 2, j) -= pp * z;
@@ -310,7 +313,7 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
         __syncwarp();
         const int imax = (n < k + 3) ? n : k + 3;
         for (int i = lane; i <= imax; i += 32) {  // column modification
-          float pp = x * HH(i, k) + y * HH(i, k + 1);
+          T pp = x * HH(i, k) + y * HH(i, k + 1);
           if (notlast) {
             pp += z * HH(i, k + 2);
             HH(i, k + 2) -= pp * r;
@@ -319,7 +322,7 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
           HH(i, k + 1) -= pp * q;
         }
         for (int i = low + lane; i <= high; i += 32) {  // accumulate
-          float pp = x * VV(i, k) + y * VV(i, k + 1);
+          T pp = x * VV(i, k) + y * VV(i, k + 1);
           if (notlast) {
             pp += z * VV(i, k + 2);
             VV(i, k + 2) -= pp * r;
@@ -342,78 +345,78 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
   }
   __syncwarp();
   // ---- eigenvectors of the quasi-triangular factor: one lane per eigenvalue ----
-  if (norm != 0.f) {
+  if (norm != T(0.)) {
     for (int nv = nn - 1 - lane; nv >= 0; nv -= 32) {
-      const float pr = d[nv], qi = e[nv];
-      if (qi == 0.f) {  // real vector
+      const T pr = d[nv], qi = e[nv];
+      if (qi == T(0.)) {  // real vector
         int l = nv;
-        YY(nv, nv) = 1.f;
-        float zs = 0.f, ss = 0.f;
+        YY(nv, nv) = T(1.);
+        T zs = T(0.), ss = T(0.);
         for (int i = nv - 1; i >= 0; --i) {
-          const float ww = HH(i, i) - pr;
-          float rr = 0.f;
+          const T ww = HH(i, i) - pr;
+          T rr = T(0.);
           for (int j = l; j <= nv; ++j) rr += HH(i, j) * YY(j, nv);
-          if (e[i] < 0.f) {
+          if (e[i] < T(0.)) {
             zs = ww;
             ss = rr;
           } else {
             l = i;
-            if (e[i] == 0.f) {
-              YY(i, nv) = (ww != 0.f) ? -rr / ww : -rr / (eps * norm);
+            if (e[i] == T(0.)) {
+              YY(i, nv) = (ww != T(0.)) ? -rr / ww : -rr / (eps * norm);
             } else {  // real 2x2 block
-              const float xx = HH(i, i + 1), yy = HH(i + 1, i);
-              const float qq = (d[i] - pr) * (d[i] - pr) + e[i] * e[i];
-              const float tt = (xx * ss - zs * rr) / qq;
+              const T xx = HH(i, i + 1), yy = HH(i + 1, i);
+              const T qq = (d[i] - pr) * (d[i] - pr) + e[i] * e[i];
+              const T tt = (xx * ss - zs * rr) / qq;
               YY(i, nv) = tt;
-              YY(i + 1, nv) = (fabsf(xx) > fabsf(zs)) ? (-rr - ww * tt) / xx : (-ss - yy * tt) / zs;
+              YY(i + 1, nv) = (fabs(xx) > fabs(zs)) ? (-rr - ww * tt) / xx : (-ss - yy * tt) / zs;
             }
-            const float tt = fabsf(YY(i, nv));
-            if ((eps * tt) * tt > 1.f)
+            const T tt = fabs(YY(i, nv));
+            if ((eps * tt) * tt > T(1.))
               for (int j = i; j <= nv; ++j) YY(j, nv) /= tt;
           }
         }
-      } else if (qi < 0.f) {  // complex vector: columns nv-1 (real part) and nv (imaginary part)
+      } else if (qi < T(0.)) {  // complex vector: columns nv-1 (real part) and nv (imaginary part)
         int l = nv - 1;
-        if (fabsf(HH(nv, nv - 1)) > fabsf(HH(nv - 1, nv))) {
+        if (fabs(HH(nv, nv - 1)) > fabs(HH(nv - 1, nv))) {
           YY(nv - 1, nv - 1) = qi / HH(nv, nv - 1);
           YY(nv - 1, nv) = -(HH(nv, nv) - pr) / HH(nv, nv - 1);
         } else {
-          float cr, ci;
-          cdivf(0.f, -HH(nv - 1, nv), HH(nv - 1, nv - 1) - pr, qi, cr, ci);
+          T cr, ci;
+          cdivf(T(0.), -HH(nv - 1, nv), HH(nv - 1, nv - 1) - pr, qi, cr, ci);
           YY(nv - 1, nv - 1) = cr;
           YY(nv - 1, nv) = ci;
         }
-        YY(nv, nv - 1) = 0.f;
-        YY(nv, nv) = 1.f;
-        float zs = 0.f, rs = 0.f, ss = 0.f;
+        YY(nv, nv - 1) = T(0.);
+        YY(nv, nv) = T(1.);
+        T zs = T(0.), rs = T(0.), ss = T(0.);
         for (int i = nv - 2; i >= 0; --i) {
-          float ra = 0.f, sa = 0.f;
+          T ra = T(0.), sa = T(0.);
           for (int j = l; j <= nv; ++j) {
             ra += HH(i, j) * YY(j, nv - 1);
             sa += HH(i, j) * YY(j, nv);
           }
-          const float ww = HH(i, i) - pr;
-          if (e[i] < 0.f) {
+          const T ww = HH(i, i) - pr;
+          if (e[i] < T(0.)) {
             zs = ww;
             rs = ra;
             ss = sa;
           } else {
             l = i;
-            float cr, ci;
-            if (e[i] == 0.f) {
+            T cr, ci;
+            if (e[i] == T(0.)) {
               cdivf(-ra, -sa, ww, qi, cr, ci);
               YY(i, nv - 1) = cr;
               YY(i, nv) = ci;
             } else {
-              const float xx = HH(i, i + 1), yy = HH(i + 1, i);
-              float vr = (d[i] - pr) * (d[i] - pr) + e[i] * e[i] - qi * qi;
-              const float vi = (d[i] - pr) * 2.f * qi;
-              if (vr == 0.f && vi == 0.f)
-                vr = eps * norm * (fabsf(ww) + fabsf(qi) + fabsf(xx) + fabsf(yy) + fabsf(zs));
+              const T xx = HH(i, i + 1), yy = HH(i + 1, i);
+              T vr = (d[i] - pr) * (d[i] - pr) + e[i] * e[i] - qi * qi;
+              const T vi = (d[i] - pr) * T(2.) * qi;
+              if (vr == T(0.) && vi == T(0.))
+                vr = eps * norm * (fabs(ww) + fabs(qi) + fabs(xx) + fabs(yy) + fabs(zs));
               cdivf(xx * rs - zs * ra + qi * sa, xx * ss - zs * sa - qi * ra, vr, vi, cr, ci);
               YY(i, nv - 1) = cr;
               YY(i, nv) = ci;
-              if (fabsf(xx) > fabsf(zs) + fabsf(qi)) {
+              if (fabs(xx) > fabs(zs) + fabs(qi)) {
                 YY(i + 1, nv - 1) = (-ra - ww * YY(i, nv - 1) + qi * YY(i, nv)) / xx;
                 YY(i + 1, nv) = (-sa - ww * YY(i, nv) - qi * YY(i, nv - 1)) / xx;
               } else {
@@ -422,8 +425,8 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
                 YY(i + 1, nv) = ci;
               }
             }
-            const float tt = fmaxf(fabsf(YY(i, nv - 1)), fabsf(YY(i, nv)));
-            if ((eps * tt) * tt > 1.f)
+            const T tt = fmaxf(fabs(YY(i, nv - 1)), fabs(YY(i, nv)));
+            if ((eps * tt) * tt > T(1.))
               for (int j = i; j <= nv; ++j) {
                 YY(j, nv - 1) /= tt;
                 YY(j, nv) /= tt;
@@ -440,16 +443,16 @@ __global__ void __launch_bounds__(32) k_nonsym_eig_f32(int nn, const double* __r
     // (column j - 1) of the pair's vector
     // (pair_imag: the imaginary part, column j, instead -- with the real part in column j - 1 the pair
     // then spans the real invariant subspace of the two eigenvalues)
-    const int src = (e[j] < 0.f && !pair_imag) ? j - 1 : j;
-    const int top = (e[j] != 0.f) ? ((e[j] > 0.f) ? j + 1 : j) : j;  // last nonzero row of column src
-    float nrm = 0.f;
+    const int src = (e[j] < T(0.) && !pair_imag) ? j - 1 : j;
+    const int top = (e[j] != T(0.)) ? ((e[j] > T(0.)) ? j + 1 : j) : j;  // last nonzero row of column src
+    T nrm = T(0.);
     for (int i = 0; i < nn; ++i) {
-      float zz = 0.f;
+      T zz = T(0.);
       for (int k = 0; k <= top; ++k) zz += VV(i, k) * YY(k, src);
       nrm += zz * zz;
       X[i + (size_t)j * nn] = (double)zz;
     }
-    const double inv = (nrm > 0.f) ? 1.0 / sqrt((double)nrm) : 0.0;
+    const double inv = (nrm > T(0.)) ? 1.0 / sqrt((double)nrm) : 0.0;
     for (int i = 0; i < nn; ++i) X[i + (size_t)j * nn] *= inv;
     wr[j] = (double)d[j];
     wi[j] = (double)e[j];
@@ -623,9 +626,18 @@ int nonsym_eig_dev(ofrr_ctx* ctx, int n, const double* C, double* wr, double* wi
                    bool pair_imag) {
   if (n <= 0) return OFRR_SUCCESS;
   if (n > NS_MAX) return OFRR_ERR_BLAS_INVALID_SIZE;
+  // refine: the whole Hessenberg-QR in FP64 when it fits in shared memory (backward stable to FP64; the
+  // Newton refinement below cannot separate clustered eigenvalues from an FP32 start), else FP32 + Newton
+  const size_t smem64 = ((size_t)3 * n * (n + 1) + 3 * (size_t)n) * sizeof(double);
+  if (refine && smem64 <= 227 * 1024) {
+    OFRR_TRY(allow_smem(k_nonsym_eig<double>));
+    k_nonsym_eig<double><<<1, 32, smem64, ctx->stream>>>(n, C, n, wr, wi, X, ctx->dev_flags + 3, pair_imag ? 1 : 0);
+    OFRR_LAUNCHED(ctx, "k_nonsym_eig_f64");
+    return OFRR_SUCCESS;
+  }
   const size_t smem = ((size_t)3 * n * (n + 1) + 3 * (size_t)n) * sizeof(float);
-  OFRR_TRY(allow_smem(k_nonsym_eig_f32));
-  k_nonsym_eig_f32<<<1, 32, smem, ctx->stream>>>(n, C, n, wr, wi, X, ctx->dev_flags + 3, pair_imag ? 1 : 0);
+  OFRR_TRY(allow_smem(k_nonsym_eig<float>));
+  k_nonsym_eig<float><<<1, 32, smem, ctx->stream>>>(n, C, n, wr, wi, X, ctx->dev_flags + 3, pair_imag ? 1 : 0);
   OFRR_LAUNCHED(ctx, "k_nonsym_eig_f32");
   if (!refine) return OFRR_SUCCESS;
   // ||C||_F on the host side of the acceptance test: one small reduction, read back
