@@ -51,9 +51,12 @@ def parse():
                     help="time the Gaussian kernel generator (16384 points in 3D) against the HBM peak")
     ap.add_argument("--csr-load", action="store_true",
                     help="time reading the 128^3 7-point CSR operator (on-disk format) into HBM")
-    ap.add_argument("--config", default="c2", choices=["c2", "c3"],
+    ap.add_argument("--config", default="c2", choices=["c2", "c3", "c5"],
                     help="c2: the dense SVD headline (default; also runs a compact C3 leg); c3: the 128^3 "
-                         "convection-diffusion Krylov workload alone")
+                         "convection-diffusion Krylov workload alone; c5: the serving stream")
+    ap.add_argument("--requests", type=int, default=400, help="c5: requests replayed from the seeded stream")
+    ap.add_argument("--time-scale", type=float, default=1.0,
+                    help="c5: arrival times multiplied by this (1 = the stream's 2000 req/s)")
     ap.add_argument("--no-c3", action="store_true", help="skip the C3 leg of the default run")
     ap.add_argument("--mixed-config", default=None, metavar="B,S",
                     help="block width and power steps of the mixed path instead of the autotuner's choice")
@@ -564,6 +567,42 @@ def c3_run(api, steps, warmup, cpu=True):
     return out
 
 
+def c5_run(api, count, time_scale, parity_every=25):
+    """The serving stream: the first `count` requests of the seeded Poisson stream (2000 req/s, 60 % dense
+    SVD, 40 % Laplacian eigenproblems, k in [4, 64], tol in {1e-6, 1e-8, 1e-10}) replayed in real time
+    through the solve engine with a 150 GB budget; then every parity_every-th request solved alone and
+    compared with its result in the mix."""
+    from mixedprecisionofrr_gb300 import serve_stream as ss
+
+    reqs = ss.make_stream(seed=2024, count=count)
+    out = ss.run_stream(reqs, time_scale=time_scale)
+    recs = out.pop("records")
+    byidx = {r["idx"]: r for r in recs}
+    parity = []
+    for req in reqs[::parity_every]:
+        st, keep = ss.solve_alone(req)
+        r = byidx[req.idx]
+        va, vm = np.asarray(keep[-3]), r["values"]
+        parity.append({"idx": req.idx, "kind": req.kind, "status_alone": st, "status_mix": r["status"],
+                       "identical": bool(np.array_equal(va, vm, equal_nan=True))})
+    for r in recs:
+        r.pop("values", None)
+    kinds = {}
+    for r in recs:
+        kk = kinds.setdefault(r["kind"], {"count": 0, "ok": 0, "lat": []})
+        kk["count"] += 1
+        kk["ok"] += int(r["status"] == 0)
+        kk["lat"].append(r["latency_ms"])
+    for kk in kinds.values():
+        lat = np.array(kk.pop("lat"))
+        kk["p50_ms"], kk["p99_ms"] = float(np.percentile(lat, 50)), float(np.percentile(lat, 99))
+    out.update({"metric": "serving stream: requests/s, converged eigen/singular pairs/s, p50/p99 latency "
+                          "(arrival to completion)", "stream": {"seed": 2024, "requests": count, "rate_req_s": 2000,
+                                                                "time_scale": time_scale},
+                "by_kind": kinds, "parity_sample": parity})
+    return out
+
+
 CPU_GRID = ((64, 96, 128), (4, 6, 8))  # block widths x power steps, the GPU autotuner's grid
 
 
@@ -655,6 +694,9 @@ def main():
         return
     if args.config == "c3":
         print(json.dumps(c3_run(api, args.steps, args.warmup)))
+        return
+    if args.config == "c5":
+        print(json.dumps(c5_run(api, args.requests, args.time_scale)))
         return
     A, s_true = make_problem_gpu()
     if args.orth_compare:

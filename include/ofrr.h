@@ -181,6 +181,13 @@ int ofrr_gs_basis(ofrr_ctx* ctx, int classical, ofrr_dtype tin, ofrr_dtype tout,
  * gaussian.m:21-27 (K(X, Y) = f^2 exp(-D2 / (2 l^2)) + s^2 eye, D2 = -2 X Y' + |x|^2 + |y|^2).
  * l <= 0, s < 0, non-positive sizes: OFRR_ERR_INVALID_ARGUMENT (the reference throws). */
 int ofrr_rand_points(ofrr_ctx* ctx, uint64_t seed, int64_t n, int d, int type, double* X /*dev*/, int64_t ldx);
+/* Dense test matrices with a prescribed spectrum (no reference counterpart; the inputs of the batched and
+ * serving workloads): symmetric = 0: A (m x n, m >= n) = H_1 .. H_r [diag(s); 0] G_1 .. G_r, singular values
+ * exactly s; symmetric = 1: A (n x n) = H_1 .. H_r diag(s) H_r .. H_1, eigenvalues exactly s.  H, G are
+ * Householder reflectors (r = reflectors <= 16 per side) with Gaussian vectors from the library's
+ * generator keyed by seed.  s: host array of n values; A: device, FP64, column-major. */
+int ofrr_test_matrix_spectrum(ofrr_ctx* ctx, int symmetric, uint64_t seed, int64_t m, int64_t n, int reflectors,
+                              const double* s /*host*/, double* A /*dev*/, int64_t lda);
 int ofrr_gaussian_kernel(ofrr_ctx* ctx, int form, int64_t m, int64_t n, int d, const double* X /*dev*/, int64_t ldx,
                          const double* Y /*dev*/, int64_t ldy, double l, double f, double s, ofrr_dtype tout,
                          void* K /*dev*/, int64_t ldk);
@@ -450,6 +457,13 @@ int ofrr_debug_scale_slice(ofrr_ctx* ctx, int mode, int64_t M, int64_t N, int64_
  * OFRR_ERR_INVALID_ARGUMENT when the shape or layout (16-byte aligned operands) does not take that path. */
 int ofrr_debug_gemm16_scalecols(ofrr_ctx* ctx, int t16, int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
                                 const void* B, int64_t ldb, void* C, int64_t ldc, int fast);
+
+/* Self-test of the thick-restart Krylov path's restart block (no reference counterpart): Y (n x p) spanning
+ * the invariant subspace of the pencil (G, M) (M SPD) for its eigenvalues with real part above sigma,
+ * from the matrix sign function; G, M, Y device FP64 column-major with ld n, n <= 96.
+ * OFRR_ERR_SINGULAR_MATRIX when sigma is an eigenvalue. */
+int ofrr_debug_invariant_subspace(ofrr_ctx* ctx, int n, const double* G, const double* M, double sigma, int p,
+                                  double* Y);
 
 /* Per-solve tracing: with a path set, every si_eig / si_svd / arnoldi_eig solve on this context appends
  * one JSON line to that file (solver, sizes, status, iterations, residual, kernel launches, total and

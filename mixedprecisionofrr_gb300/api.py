@@ -675,6 +675,30 @@ def arnoldi_mgs_eig(A, n: int, k: int, precision_compute="double", precision_out
     return X, d, _info(st, inf, res)
 
 
+def test_matrix_spectrum(s, m: int, n: int, seed: int = 0, symmetric: bool = False, reflectors: int = 3):
+    """Dense FP64 device matrix (column-major) with singular values (symmetric: eigenvalues) exactly s:
+    Householder reflectors around [diag(s); 0] (ofrr_test_matrix_spectrum)."""
+    ctx = context()
+    s = np.ascontiguousarray(s, dtype=np.float64)
+    A = empty_cm(m, n, L.F64)
+    L.check(ctx.lib.ofrr_test_matrix_spectrum(ctx.h, int(symmetric), seed, m, n, reflectors, _dp(s), A.data_ptr(),
+                                              ld_of(A)), "test_matrix_spectrum")
+    return A
+
+
+def debug_invariant_subspace(G, M, sigma: float, p: int) -> np.ndarray:
+    """Basis (n x p) of the invariant subspace of the pencil (G, M) for eigenvalues with real part above
+    sigma (ofrr_debug_invariant_subspace; the restart block of the nonsymmetric Krylov path)."""
+    ctx = context()
+    n = G.shape[0]
+    Gd = to_device_cm(np.asarray(G, np.float64), L.F64)
+    Md = to_device_cm(np.asarray(M, np.float64), L.F64)
+    Y = empty_cm(n, p, L.F64)
+    L.check(ctx.lib.ofrr_debug_invariant_subspace(ctx.h, n, Gd.data_ptr(), Md.data_ptr(), float(sigma), p,
+                                                  Y.data_ptr()), "debug_invariant_subspace")
+    return to_numpy(Y)
+
+
 def profile_krylov_step(A: "CsrMatrix", precision: str, i: int, reps: int = 20):
     """Mean time (us) and algorithmic HBM bytes of one fused Krylov step (column i, basis type
     `precision`) on the CSR operator A (ofrr_profile_krylov_step)."""
@@ -754,6 +778,23 @@ class Server:
         req = L.ofrr_request(kind=L.REQ_SI_SVD, A=op.op, opt=o, V=V.data_ptr(), ldv=ld_of(V), U=U.data_ptr(),
                              ldu=ld_of(U), values=_dp(sv), resid=_dp(res), info=C.pointer(inf))
         return self._submit(req, (op, U, V, sv, res, inf))
+
+    def submit_arnoldi_eig(self, A, k: int, kdim: int = 64, mode: str = "mixed", tol: float = 1e-8,
+                           maxiter: int = 100000, p_output: str = "half", symmetric=None, seed: int = 42,
+                           restart_keep: int = 0):
+        """Thick-restart Krylov eigensolve of a CSR operator (ofrr_arnoldi_eig) as a request."""
+        op = operator(A, symmetric)
+        modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
+        o = options(mode=modes[mode], maxiter=maxiter, kdim=kdim, nev=min(k, op.n), tol=tol, seed=seed,
+                    use_generalized=1, restart_keep=restart_keep, orth=L.ORTH_HESSENBERG,
+                    p_output=p_output if mode == "mixed" else None)
+        X = empty_cm(op.m, o.nev, L.F64)
+        d = np.zeros(o.nev)
+        res = np.zeros(o.nev)
+        inf = L.ofrr_info()
+        req = L.ofrr_request(kind=L.REQ_ARNOLDI_EIG, A=op.op, opt=o, V=X.data_ptr(), ldv=ld_of(X), values=_dp(d),
+                             resid=_dp(res), info=C.pointer(inf))
+        return self._submit(req, (op, X, d, res, inf))
 
     def poll(self, ticket: int):
         done, st = C.c_int(), C.c_int()

@@ -1042,3 +1042,14 @@ int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const dou
 }
 
 }  // namespace ofrr
+
+using namespace ofrr;
+
+// Self-test of the restart block of the nonsymmetric thick-restart Krylov path (no reference
+// counterpart): Y (n x p, ld n) spanning the invariant subspace of (G, M) for the eigenvalues with real
+// part above sigma.  G, M, Y: device FP64, column-major, ld n; n <= 96.
+extern "C" int ofrr_debug_invariant_subspace(ofrr_ctx* ctx, int n, const double* G, const double* M, double sigma,
+                                             int p, double* Y) {
+  if (!ctx || !G || !M || !Y || n < 1 || p < 1 || p > n) return OFRR_ERR_INVALID_ARGUMENT;
+  return invariant_subspace_nonsym(ctx, n, G, M, sigma, p, Y);
+}

@@ -1019,6 +1019,7 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
   int cycles = 0, steps = 0, nmv = 0, escalations = 0, ncols = 0, in_phase = 0, k = std::min(nev, nb);
   double best_in_phase = INFINITY;
   bool converged = false;
+  const bool kry_debug = getenv("OFRR_KRYLOV_DEBUG") != nullptr;  // per-cycle progress on stderr
   while (true) {
     TraceScope ts(ctx, "krylov.block");
     const ofrr_dtype t = S.t, ta = kry_arith_type(t);
@@ -1054,6 +1055,7 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
     ts.next("rr");
     const ofrr_dtype tav = ta;
     int pp = 0;
+    bool sign_ok = false;
     {
       WsScope inner(ctx);
       OFRR_TRY(csrmm_impl(ctx, &A->csr, 0, t, ta, tav, ncols, S.V, S.ldv, AVb, ld));
@@ -1095,6 +1097,7 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
         const int ist = invariant_subspace_nonsym(ctx, ncols, G, M, sigma, pp, Ys);
         if (ist == OFRR_SUCCESS) Yc = Ys;
         else if (ist != OFRR_ERR_SINGULAR_MATRIX) return ist;
+        sign_ok = (ist == OFRR_SUCCESS);
       }
       // Wb = V [U(:, :k), Yc, -M^-1 G(:, last)] (+ A v_last in the last column): the k Ritz vectors, then
       // the next block
@@ -1114,6 +1117,9 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
     OFRR_TRY(residuals_dev(ctx, op, tw, Wb, ld, k, hd.data(), -1.0, hres.data()));
     double maxres = 0;
     for (int j = 0; j < k; ++j) maxres = std::max(maxres, hres[j]);
+    if (kry_debug)
+      fprintf(stderr, "[ofrr krylov] cycle %d phase %d type %d q %d ncols %d pp %d sign %d maxres %.3e d0 %.10e\n",
+              cycles, phase, (int)t, q, ncols, pp, sign_ok ? 1 : 0, maxres, hd[0]);
     if (opt->tol > 0 && maxres <= opt->tol) {
       converged = true;
       break;

@@ -192,3 +192,81 @@ extern "C" int ofrr_gaussian_kernel(ofrr_ctx* ctx, int form, int64_t m, int64_t 
   });
   return OFRR_SUCCESS;
 }
+
+// ---- dense matrices with a prescribed spectrum (the batched and serving workloads) ------------------
+// A = H_1 .. H_r [diag(s); 0] G_1 .. G_r (SVD form, m x n, m >= n) or A = H_1 .. H_r diag(s) H_r .. H_1
+// (symmetric form, m = n), with Householder reflectors H = I - 2 u u' / (u'u) whose vectors u are
+// Gaussian draws of the library's generator: the singular values (eigenvalues) are exactly s, the
+// singular vectors dense.  Each reflector is one matrix-vector product and one rank-1 update in FP64.
+namespace ofrr {
+namespace {
+__global__ void k_diag_fill(int64_t m, int64_t n, const double* __restrict__ s, double* __restrict__ A, int64_t lda) {
+  OFRR_FOR_2D(i, j, m, n) A[i + j * lda] = (i == j) ? s[j] : 0.0;
+}
+// y (m) = A x (trans 0) or y (n) = A' x (trans 1), one thread per output entry (FP64)
+__global__ void k_gemv_f64(int trans, int64_t m, int64_t n, const double* __restrict__ A, int64_t lda,
+                           const double* __restrict__ x, double* __restrict__ y) {
+  const int64_t nout = trans ? n : m;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < nout; o += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    if (trans) {
+      for (int64_t i = 0; i < m; ++i) acc = fma(A[i + o * lda], x[i], acc);
+    } else {
+      for (int64_t j = 0; j < n; ++j) acc = fma(A[o + j * lda], x[j], acc);
+    }
+    y[o] = acc;
+  }
+}
+// A -= alpha x y'
+__global__ void k_rank1_f64(int64_t m, int64_t n, double alpha, const double* __restrict__ x,
+                            const double* __restrict__ y, double* __restrict__ A, int64_t lda) {
+  OFRR_FOR_2D(i, j, m, n) A[i + j * lda] -= alpha * x[i] * y[j];
+}
+}  // namespace
+}  // namespace ofrr
+
+extern "C" int ofrr_test_matrix_spectrum(ofrr_ctx* ctx, int symmetric, uint64_t seed, int64_t m, int64_t n,
+                                         int reflectors, const double* s, double* A, int64_t lda) {
+  using namespace ofrr;
+  if (!ctx || !s || !A || m < 1 || n < 1 || lda < m || reflectors < 0 || reflectors > 16)
+    return OFRR_ERR_INVALID_ARGUMENT;
+  if ((symmetric && m != n) || (!symmetric && m < n)) return OFRR_ERR_BLAS_INVALID_SIZE;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  double *sd = ws_get<double>(ctx, (size_t)n, &st), *u = ws_get<double>(ctx, (size_t)m, &st),
+         *w = ws_get<double>(ctx, (size_t)std::max(m, n), &st);
+  if (!sd || !u || !w) return st;
+  OFRR_CUDA(cudaMemcpyAsync(sd, s, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  k_diag_fill<<<grid_2d(m, n, 256), 256, 0, ctx->stream>>>(m, n, sd, A, lda);
+  OFRR_LAUNCHED(ctx, "k_diag_fill");
+  const int gv = grid_for(std::max(m, n), 128, 152 * 8);
+  for (int r = 0; r < reflectors; ++r) {
+    for (int side = 0; side < 2; ++side) {  // side 0: from the left (length m), 1: from the right (length n)
+      const int64_t len = side ? n : m;
+      OFRR_TRY(ofrr_randn(ctx, seed * 64 + 2 * r + side + 1, len, 1, OFRR_F64, u, len));
+      std::vector<double> hu(len);
+      OFRR_CUDA(cudaMemcpyAsync(hu.data(), u, sizeof(double) * len, cudaMemcpyDeviceToHost, ctx->stream));
+      OFRR_TRY(sync_and_check(ctx));
+      double uu = 0.0;
+      for (double v : hu) uu += v * v;
+      if (side == 0) {  // A = (I - 2 u u'/uu) A: w = A' u, A -= (2/uu) u w'
+        k_gemv_f64<<<gv, 128, 0, ctx->stream>>>(1, m, n, A, lda, u, w);
+        OFRR_LAUNCHED(ctx, "k_gemv_f64");
+        k_rank1_f64<<<grid_2d(m, n, 256), 256, 0, ctx->stream>>>(m, n, 2.0 / uu, u, w, A, lda);
+      } else {  // A = A (I - 2 u u'/uu): w = A u, A -= (2/uu) w u'
+        k_gemv_f64<<<gv, 128, 0, ctx->stream>>>(0, m, n, A, lda, u, w);
+        OFRR_LAUNCHED(ctx, "k_gemv_f64");
+        k_rank1_f64<<<grid_2d(m, n, 256), 256, 0, ctx->stream>>>(m, n, 2.0 / uu, w, u, A, lda);
+      }
+      OFRR_LAUNCHED(ctx, "k_rank1_f64");
+      if (symmetric && side == 0) {  // the same reflector on the right keeps A symmetric
+        k_gemv_f64<<<gv, 128, 0, ctx->stream>>>(0, m, n, A, lda, u, w);
+        OFRR_LAUNCHED(ctx, "k_gemv_f64");
+        k_rank1_f64<<<grid_2d(m, n, 256), 256, 0, ctx->stream>>>(m, n, 2.0 / uu, w, u, A, lda);
+        OFRR_LAUNCHED(ctx, "k_rank1_f64");
+        break;
+      }
+    }
+  }
+  return OFRR_SUCCESS;
+}
