@@ -430,6 +430,23 @@ int ofrr_serve_stats(ofrr_serve* engine, ofrr_serve_report* stats);
 int ofrr_batch_si_eig(ofrr_serve* engine, int count, const ofrr_operator* ops, const ofrr_options* opt,
                       void* const* V /*dev*/, const int64_t* ldv, double* const* evals /*host*/,
                       double* const* resid /*host|NULL*/, ofrr_info* infos /*host|NULL*/, int* statuses);
+/* Batched dense symmetric eigensolves in one persistent launch (no reference counterpart; the per-matrix
+ * algorithm is subspace_iter_eig.m:50-68 with the Hessenberg basis and eig_rr.m).  count matrices A_i
+ * (n_i x n_i, b <= n_i <= 1024, FP64, column-major, packed in one device buffer at element offsets
+ * offset[i]); opt: block (<= 16), nev (<= 8), step_size, maxiter (outer iterations), tol (residual
+ * ||A x - l x|| / max|l| target, >= 1e-7 in the FP32 phase, certified in FP64), p_output (OFRR_BF16 or
+ * OFRR_F16: the storage type of A in the first phase), seed.  Phases per matrix: 16-bit A with FP32
+ * accumulation, then FP32 A, on the CUDA cores of one SM per matrix (a persistent grid pulling matrices
+ * largest first); then a second persistent pass takes the nev leading Ritz pairs to FP64 accuracy (block
+ * Rayleigh-Ritz on [X, A X - X L] with FP64 products) and computes their FP64 residuals.  Outputs: X
+ * (device, n_i x nev unit-norm FP64 Ritz vectors at element offsets xoffset[i]), evals (host, count x nev,
+ * descending), resid (host, count x nev, or NULL), iterations (host, count, or NULL: outer iterations of
+ * the first pass), statuses (host, count: OFRR_SUCCESS or OFRR_ERR_SOLVER_MAX_ITERATIONS). */
+int ofrr_batch_sym_eig(ofrr_ctx* ctx, int count, const int64_t* n /*host*/, const int64_t* offset /*host*/,
+                       const double* A /*dev*/, const ofrr_options* opt, double* X /*dev*/,
+                       const int64_t* xoffset /*host*/, double* evals /*host*/, double* resid /*host|NULL*/,
+                       int* iterations /*host|NULL*/, int* statuses /*host*/);
+
 /* releases a context's cached workspace (no allocation of it may be live: call between solves) */
 int ofrr_ctx_trim(ofrr_ctx* ctx);
 

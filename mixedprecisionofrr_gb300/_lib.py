@@ -107,6 +107,8 @@ SIGNATURES = {
     "ofrr_profile_krylov_step": (C.c_int, [_P, C.POINTER(ofrr_csr), C.c_int, C.c_int, C.c_int, _DP, _DP]),
     "ofrr_test_matrix_spectrum": (C.c_int, [_P, C.c_int, C.c_uint64, _I64, _I64, C.c_int, _DP, _P, _I64]),
     "ofrr_debug_invariant_subspace": (C.c_int, [_P, C.c_int, _P, _P, _D, C.c_int, _P]),
+    "ofrr_batch_sym_eig": (C.c_int, [_P, C.c_int, _P, _P, _P, C.POINTER(ofrr_options), _P, _P, _DP, _DP, _IP,
+                                     _IP]),
     "ofrr_syev": (C.c_int, [_P, C.c_int, _P, C.c_int, _P]),
     "ofrr_sygv": (C.c_int, [_P, C.c_int, _P, C.c_int, _P, C.c_int, _P]),
     "ofrr_options_default": (None, [C.POINTER(ofrr_options)]),

@@ -699,6 +699,32 @@ def debug_invariant_subspace(G, M, sigma: float, p: int) -> np.ndarray:
     return to_numpy(Y)
 
 
+def batch_sym_eig(A_packed, ns, offsets, nev: int = 8, block: int = 16, tol: float = 1e-7, step_size: int = 2,
+                  maxiter: int = 500, p_output: str = "bfloat16", seed: int = 42):
+    """Batched dense symmetric eigensolves in one persistent launch (ofrr_batch_sym_eig).  A_packed: FP64
+    device tensor holding every matrix column-major at its element offset.  Returns (X list of device
+    n_i x nev FP64 tensors, evals (count x nev), resid (count x nev), iterations, statuses)."""
+    import torch
+
+    ctx = context()
+    count = len(ns)
+    ns = np.ascontiguousarray(ns, dtype=np.int64)
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    xo = np.concatenate([[0], np.cumsum(ns * nev)[:-1]]).astype(np.int64)
+    X = torch.empty(int((ns * nev).sum()), dtype=torch.float64, device=A_packed.device)
+    ev = np.zeros((count, nev))
+    res = np.zeros((count, nev))
+    its = np.zeros(count, dtype=np.int32)
+    sts = np.zeros(count, dtype=np.int32)
+    o = options(mode=L.MODE_MIXED, nev=nev, block=block, tol=tol, step_size=step_size, maxiter=maxiter, seed=seed,
+                p_output=p_output)
+    L.check(ctx.lib.ofrr_batch_sym_eig(ctx.h, count, ns.ctypes.data, offsets.ctypes.data, A_packed.data_ptr(),
+                                       C.byref(o), X.data_ptr(), xo.ctypes.data, _dp(ev), _dp(res), _ip(its),
+                                       _ip(sts)), "batch_sym_eig")
+    Xs = [X[int(xo[i]):int(xo[i] + ns[i] * nev)].view(nev, int(ns[i])).t() for i in range(count)]
+    return Xs, ev, res, its, sts
+
+
 def profile_krylov_step(A: "CsrMatrix", precision: str, i: int, reps: int = 20):
     """Mean time (us) and algorithmic HBM bytes of one fused Krylov step (column i, basis type
     `precision`) on the CSR operator A (ofrr_profile_krylov_step)."""

@@ -720,7 +720,7 @@ __global__ void k_unit_cols(int n, double* __restrict__ U) {
 // separated from the others, and the matrix sign function gives it without eigenvectors:
 // S = sign(C - sigma I) (Newton, X <- (mu X + (mu X)^-1) / 2 with determinant scaling mu), P = (I + S) / 2
 // projects onto the eigenvalues with real part above sigma [N. J. Higham, Functions of Matrices,
-// SIAM 2008, ch. 5].  One CTA; Gauss-Jordan inversion with partial pivoting in shared memory.
+// SIAM 2008, ch. 5].  One CTA, FP64; Gauss-Jordan inversion with partial pivoting in shared memory.
 constexpr int kSignMaxN = 96;
 
 template <class T>
@@ -917,14 +917,12 @@ int invariant_subspace_nonsym(ofrr_ctx* ctx, int n, const double* G, const doubl
   k_shift_copy<<<(n * n + 255) / 256, 256, 0, ctx->stream>>>(n, C, sigma, X);
   OFRR_LAUNCHED(ctx, "k_shift_copy");
   OFRR_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
-  const size_t sm32 = 2 * (size_t)n * n * sizeof(float), sm64 = 2 * (size_t)n * n * sizeof(double);
-  OFRR_TRY(allow_smem(k_sign_newton<float>));
+  // FP64 throughout: the iteration converges to the sign of the matrix it is given, so rounding errors of
+  // a lower-precision start are not corrected by later FP64 steps (they change the matrix, not the path)
+  const size_t sm64 = 2 * (size_t)n * n * sizeof(double);
   OFRR_TRY(allow_smem(k_sign_newton<double>));
-  // FP32 Newton steps to a 1e-6 fixed point, then FP64 steps (quadratic convergence) to 1e-14
-  k_sign_newton<float><<<1, 256, sm32, ctx->stream>>>(n, X, 60, 1e-6, flag);
-  OFRR_LAUNCHED(ctx, "k_sign_newton<f32>");
-  k_sign_newton<double><<<1, 256, sm64, ctx->stream>>>(n, X, 12, 1e-14, flag);
-  OFRR_LAUNCHED(ctx, "k_sign_newton<f64>");
+  k_sign_newton<double><<<1, 256, sm64, ctx->stream>>>(n, X, 80, 1e-14, flag);
+  OFRR_LAUNCHED(ctx, "k_sign_newton");
   OFRR_TRY(allow_smem(k_proj_basis));
   k_proj_basis<<<1, 256, (size_t)n * p * sizeof(double), ctx->stream>>>(n, p, X, Q);
   OFRR_LAUNCHED(ctx, "k_proj_basis");
