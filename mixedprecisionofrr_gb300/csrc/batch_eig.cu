@@ -620,9 +620,22 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_refine(RefineDev d) {
         const double res = (s_lam[k + c] > 0.0) ? sqrt(rr / s_lam[k + c]) / lmax : INFINITY;
         if (tid == 0) d.res[(int64_t)mi * k + c] = res;
         maxres = fmax(maxres, res);
+        // unit columns for the block step: X (and A X) and the residual direction (the span is unchanged,
+        // and the Gram matrix of [X, R] stays well scaled however small the residuals are)
+        const double sx = (s_lam[k + c] > 0.0) ? 1.0 / sqrt(s_lam[k + c]) : 0.0;
+        const double sr = (rr > 0.0) ? 1.0 / sqrt(rr) : 0.0;
+        for (int i = tid; i < n; i += BE_T) {
+          Sx[i + c * n] *= sx;
+          Sa[i + c * n] *= sx;
+          Sx[i + (c + k) * n] *= sr;
+        }
       }
       __syncthreads();
-      if (step == d.steps || maxres <= 1e-13) break;
+      if (step == d.steps || maxres <= 1e-13) {
+        if (tid < k) s_lam[k + tid] = 1.0;  // the columns are unit now
+        __syncthreads();
+        break;
+      }
       // block step: Rayleigh-Ritz on [X, R] (FP64 products)
       br_matmul(n, k, A, Sx + (size_t)k * n, Sa + (size_t)k * n);
       for (int e = tid; e < 2 * k2 * k2; e += BE_T) {
