@@ -446,6 +446,11 @@ int ofrr_batch_sym_eig(ofrr_ctx* ctx, int count, const int64_t* n /*host*/, cons
                        const double* A /*dev*/, const ofrr_options* opt, double* X /*dev*/,
                        const int64_t* xoffset /*host*/, double* evals /*host*/, double* resid /*host|NULL*/,
                        int* iterations /*host|NULL*/, int* statuses /*host*/);
+/* ofrr_batch_sym_eig with each matrix's time from leaving the queue to its certified result (host, count,
+ * milliseconds, from the GPU's global timer); no reference counterpart. */
+int ofrr_batch_sym_eig_timed(ofrr_ctx* ctx, int count, const int64_t* n, const int64_t* offset, const double* A,
+                             const ofrr_options* opt, double* X, const int64_t* xoffset, double* evals, double* resid,
+                             int* iterations, int* statuses, double* latency_ms /*host*/);
 
 /* releases a context's cached workspace (no allocation of it may be live: call between solves) */
 int ofrr_ctx_trim(ofrr_ctx* ctx);

@@ -109,6 +109,8 @@ SIGNATURES = {
     "ofrr_debug_invariant_subspace": (C.c_int, [_P, C.c_int, _P, _P, _D, C.c_int, _P]),
     "ofrr_batch_sym_eig": (C.c_int, [_P, C.c_int, _P, _P, _P, C.POINTER(ofrr_options), _P, _P, _DP, _DP, _IP,
                                      _IP]),
+    "ofrr_batch_sym_eig_timed": (C.c_int, [_P, C.c_int, _P, _P, _P, C.POINTER(ofrr_options), _P, _P, _DP, _DP,
+                                           _IP, _IP, _DP]),
     "ofrr_syev": (C.c_int, [_P, C.c_int, _P, C.c_int, _P]),
     "ofrr_sygv": (C.c_int, [_P, C.c_int, _P, C.c_int, _P, C.c_int, _P]),
     "ofrr_options_default": (None, [C.POINTER(ofrr_options)]),

@@ -700,7 +700,7 @@ def debug_invariant_subspace(G, M, sigma: float, p: int) -> np.ndarray:
 
 
 def batch_sym_eig(A_packed, ns, offsets, nev: int = 8, block: int = 16, tol: float = 1e-7, step_size: int = 2,
-                  maxiter: int = 500, p_output: str = "bfloat16", seed: int = 42):
+                  maxiter: int = 500, p_output: str = "bfloat16", seed: int = 42, return_latency: bool = False):
     """Batched dense symmetric eigensolves in one persistent launch (ofrr_batch_sym_eig).  A_packed: FP64
     device tensor holding every matrix column-major at its element offset.  Returns (X list of device
     n_i x nev FP64 tensors, evals (count x nev), resid (count x nev), iterations, statuses)."""
@@ -718,10 +718,13 @@ def batch_sym_eig(A_packed, ns, offsets, nev: int = 8, block: int = 16, tol: flo
     sts = np.zeros(count, dtype=np.int32)
     o = options(mode=L.MODE_MIXED, nev=nev, block=block, tol=tol, step_size=step_size, maxiter=maxiter, seed=seed,
                 p_output=p_output)
-    L.check(ctx.lib.ofrr_batch_sym_eig(ctx.h, count, ns.ctypes.data, offsets.ctypes.data, A_packed.data_ptr(),
-                                       C.byref(o), X.data_ptr(), xo.ctypes.data, _dp(ev), _dp(res), _ip(its),
-                                       _ip(sts)), "batch_sym_eig")
+    lat = np.zeros(count)
+    L.check(ctx.lib.ofrr_batch_sym_eig_timed(ctx.h, count, ns.ctypes.data, offsets.ctypes.data, A_packed.data_ptr(),
+                                             C.byref(o), X.data_ptr(), xo.ctypes.data, _dp(ev), _dp(res), _ip(its),
+                                             _ip(sts), _dp(lat)), "batch_sym_eig")
     Xs = [X[int(xo[i]):int(xo[i] + ns[i] * nev)].view(nev, int(ns[i])).t() for i in range(count)]
+    if return_latency:
+        return Xs, ev, res, its, sts, lat
     return Xs, ev, res, its, sts
 
 

@@ -43,6 +43,7 @@ struct BatchDev {
   float* lam;              // count x BE_B Ritz values (descending)
   int* iters;              // count: outer iterations
   int* phase2;             // count: outer iteration at which the FP32 phase began (-1: never)
+  unsigned long long* tstart;  // count: global timer when the matrix was taken from the queue
   unsigned int* queue;
   int count, b, nev, step, maxit;
   float tol16, tol32;      // residual targets that end the 16-bit and the FP32 phase
@@ -52,6 +53,12 @@ struct BatchDev {
 __device__ __forceinline__ float be_ld(const __half* p) { return __half2float(*p); }
 __device__ __forceinline__ float be_ld(const __nv_bfloat16* p) { return __bfloat162float(*p); }
 __device__ __forceinline__ float be_ld(const float* p) { return *p; }
+
+__device__ __forceinline__ unsigned long long tc_globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 __device__ __forceinline__ uint64_t be_mix(uint64_t x) {
   x += 0x9E3779B97F4A7C15ull;
@@ -249,6 +256,7 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
     __syncthreads();
     if (job >= d.count) return;
     const int mi = d.order[job];
+    if (tid == 0) d.tstart[mi] = tc_globaltimer();
     const int n = (int)d.n[mi];
     const int64_t off = d.off[mi];
     const T16* A16 = reinterpret_cast<const T16*>(d.A16) + off;
@@ -536,6 +544,7 @@ struct RefineDev {
   double* lam;          // out: count x nev
   double* res;          // out: count x nev (FP64 residuals / max|l|)
   double* scratch;      // per CTA: 4 x BE_NMAX x BE_NEV doubles
+  unsigned long long* tend;  // count: global timer when the matrix's refinement finished
   unsigned int* queue;
   int count, nev, steps;
 };
@@ -770,6 +779,7 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_refine(RefineDev d) {
       if (tid == 0) d.lam[(int64_t)mi * k + c] = s_lam[c];
     }
     __syncthreads();
+    if (tid == 0) d.tend[mi] = tc_globaltimer();
   }
 }
 
@@ -784,9 +794,9 @@ __global__ void k_be_convert(int64_t count, const TI* __restrict__ in, TO* __res
 
 using namespace ofrr;
 
-extern "C" int ofrr_batch_sym_eig(ofrr_ctx* ctx, int count, const int64_t* n_host, const int64_t* offset_host,
-                                  const double* A, const ofrr_options* opt, double* X, const int64_t* xoffset_host,
-                                  double* evals, double* resid, int* iterations, int* statuses) {
+static int batch_sym_eig_impl(ofrr_ctx* ctx, int count, const int64_t* n_host, const int64_t* offset_host,
+                              const double* A, const ofrr_options* opt, double* X, const int64_t* xoffset_host,
+                              double* evals, double* resid, int* iterations, int* statuses, double* latency_ms) {
   if (!ctx || count < 0 || !n_host || !offset_host || !A || !opt || !X || !xoffset_host || !evals || !statuses)
     return OFRR_ERR_INVALID_ARGUMENT;
   if (count == 0) return OFRR_SUCCESS;
@@ -823,13 +833,14 @@ extern "C" int ofrr_batch_sym_eig(ofrr_ctx* ctx, int count, const int64_t* n_hos
   double* dlam = ws_get<double>(ctx, (size_t)count * nev, &st);
   double* dres = ws_get<double>(ctx, (size_t)count * nev, &st);
   unsigned int* queues = ws_get<unsigned int>(ctx, 2, &st);
+  unsigned long long* times = ws_get<unsigned long long>(ctx, (size_t)2 * count, &st);
   int dev = 0, sms = 0;
   OFRR_CUDA(cudaGetDevice(&dev));
   OFRR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int grid = std::max(1, std::min(sms, count));
   double* scratch = ws_get<double>(ctx, (size_t)grid * 4 * BE_NMAX * 2 * BE_NEV, &st);
   if (!A32 || !A16 || !X32 || !lam32 || !dn || !doff || !dxo || !dxo64 || !dorder || !dit || !dlam || !dres ||
-      !queues || !scratch)
+      !queues || !scratch || !times)
     return st;
   OFRR_CUDA(cudaMemcpyAsync(dn, n_host, sizeof(int64_t) * count, cudaMemcpyHostToDevice, ctx->stream));
   OFRR_CUDA(cudaMemcpyAsync(doff, offset_host, sizeof(int64_t) * count, cudaMemcpyHostToDevice, ctx->stream));
@@ -856,6 +867,7 @@ extern "C" int ofrr_batch_sym_eig(ofrr_ctx* ctx, int count, const int64_t* n_hos
   d.lam = lam32;
   d.iters = dit;
   d.phase2 = dit + count;
+  d.tstart = times;
   d.queue = queues;
   d.count = count;
   d.b = b;
@@ -887,6 +899,7 @@ extern "C" int ofrr_batch_sym_eig(ofrr_ctx* ctx, int count, const int64_t* n_hos
   r.lam = dlam;
   r.res = dres;
   r.scratch = scratch;
+  r.tend = times + count;
   r.queue = queues + 1;
   r.count = count;
   r.nev = nev;
@@ -898,7 +911,12 @@ extern "C" int ofrr_batch_sym_eig(ofrr_ctx* ctx, int count, const int64_t* n_hos
   OFRR_CUDA(cudaMemcpyAsync(evals, dlam, sizeof(double) * count * nev, cudaMemcpyDeviceToHost, ctx->stream));
   OFRR_CUDA(cudaMemcpyAsync(hres.data(), dres, sizeof(double) * count * nev, cudaMemcpyDeviceToHost, ctx->stream));
   OFRR_CUDA(cudaMemcpyAsync(hit.data(), dit, sizeof(int) * 2 * count, cudaMemcpyDeviceToHost, ctx->stream));
+  std::vector<unsigned long long> ht(2 * (size_t)count);
+  OFRR_CUDA(cudaMemcpyAsync(ht.data(), times, sizeof(unsigned long long) * 2 * count, cudaMemcpyDeviceToHost,
+                            ctx->stream));
   OFRR_TRY(sync_and_check(ctx));
+  if (latency_ms)
+    for (int i = 0; i < count; ++i) latency_ms[i] = 1e-6 * (double)(ht[count + i] - ht[i]);
   for (int i = 0; i < count; ++i) {
     double mr = 0.0;
     for (int j = 0; j < nev; ++j) mr = std::max(mr, hres[(size_t)i * nev + j]);
@@ -907,4 +925,21 @@ extern "C" int ofrr_batch_sym_eig(ofrr_ctx* ctx, int count, const int64_t* n_hos
   }
   if (resid) std::copy(hres.begin(), hres.end(), resid);
   return OFRR_SUCCESS;
+}
+
+extern "C" int ofrr_batch_sym_eig(ofrr_ctx* ctx, int count, const int64_t* n_host, const int64_t* offset_host,
+                                  const double* A, const ofrr_options* opt, double* X, const int64_t* xoffset_host,
+                                  double* evals, double* resid, int* iterations, int* statuses) {
+  return batch_sym_eig_impl(ctx, count, n_host, offset_host, A, opt, X, xoffset_host, evals, resid, iterations,
+                            statuses, nullptr);
+}
+
+// Same, also returning each matrix's time from leaving the queue to its certified result (ms), for the
+// per-matrix latency of the batch (no reference counterpart).
+extern "C" int ofrr_batch_sym_eig_timed(ofrr_ctx* ctx, int count, const int64_t* n_host, const int64_t* offset_host,
+                                        const double* A, const ofrr_options* opt, double* X,
+                                        const int64_t* xoffset_host, double* evals, double* resid, int* iterations,
+                                        int* statuses, double* latency_ms) {
+  return batch_sym_eig_impl(ctx, count, n_host, offset_host, A, opt, X, xoffset_host, evals, resid, iterations,
+                            statuses, latency_ms);
 }
