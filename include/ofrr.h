@@ -123,6 +123,15 @@ int ofrr_gemm(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
               double alpha, const void* A /*dev*/, int64_t lda, const void* B /*dev*/,
               int64_t ldb, double beta, void* C /*dev*/, int64_t ldc);
 
+/* Tile autotuner of the 16-bit tcgen05 product (no reference counterpart): times every tile width
+ * BN in {32, 64, 128} and K split in {1, 2, ..., 64} of C (M x N, FP32) = A' B (A: K x M, B: K x N, type t16)
+ * over reps launches on seeded operands and keeps the fastest plan for that exact shape and type
+ * (process-wide); later 16-bit products of the shape use it.  ofrr_gemm16_plan reports the plan a
+ * product of a shape would use (tuned = 1 when it came from the autotuner). */
+int ofrr_autotune_gemm16(ofrr_ctx* ctx, int t16, int64_t M, int64_t N, int64_t K, int reps, int* best_bn,
+                         int* best_splits, double* best_us);
+int ofrr_gemm16_plan(int t16, int64_t M, int64_t N, int64_t K, int* bn, int* splits, int* tuned);
+
 /* C (M x N) = A' B for FP64 A (K x M) and B (K x N), computed on the tcgen05 tensor cores from
  * exact BF16 digit slices of both operands (five 7-bit digits per column after a power-of-two
  * column scaling; digit products summed exactly in FP32, combined in FP64).  Element error is

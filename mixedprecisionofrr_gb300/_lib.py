@@ -100,6 +100,8 @@ SIGNATURES = {
     "ofrr_gemm": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _I64, _I64, _I64, _D,
                             _P, _I64, _P, _I64, _D, _P, _I64]),
     "ofrr_gemm_f64_emulated": (C.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64]),
+    "ofrr_autotune_gemm16": (C.c_int, [_P, C.c_int, _I64, _I64, _I64, C.c_int, _IP, _IP, _DP]),
+    "ofrr_gemm16_plan": (C.c_int, [C.c_int, _I64, _I64, _I64, _IP, _IP, _IP]),
     "ofrr_profile_gemm_f64_emulated": (C.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, C.c_int,
                                                   _DP, _DP]),
     "ofrr_csrmm": (C.c_int, [_P, C.POINTER(ofrr_csr), C.c_int, C.c_int, C.c_int, C.c_int, _I64, _P, _I64, _P,

@@ -880,6 +880,23 @@ def batch_si_eig(server: Server, As, k: int, mode: str = "mixed", tol: float = 1
 
 
 # ---- autotuner -------------------------------------------------------------------------------
+def autotune_gemm16(M: int, N: int, K: int, precision: str = "half", reps: int = 5) -> dict:
+    """Tile plan (BN, K split) of the 16-bit tcgen05 product C (M x N) = A' B for this shape, chosen by
+    timing every candidate (ofrr_autotune_gemm16); later products of the shape use it."""
+    ctx = context()
+    bn, sp = np.zeros(1, np.int32), np.zeros(1, np.int32)
+    us = np.zeros(1)
+    L.check(ctx.lib.ofrr_autotune_gemm16(ctx.h, _p(precision), M, N, K, reps, _ip(bn), _ip(sp), _dp(us)),
+            "autotune_gemm16")
+    return {"M": M, "N": N, "K": K, "BN": int(bn[0]), "splits": int(sp[0]), "us": float(us[0])}
+
+
+def gemm16_plan(M: int, N: int, K: int, precision: str = "half") -> dict:
+    bn, sp, tu = np.zeros(1, np.int32), np.zeros(1, np.int32), np.zeros(1, np.int32)
+    L.check(L.load().ofrr_gemm16_plan(_p(precision), M, N, K, _ip(bn), _ip(sp), _ip(tu)), "gemm16_plan")
+    return {"BN": int(bn[0]), "splits": int(sp[0]), "tuned": bool(tu[0])}
+
+
 def autotune_svd(A, m: int, n: int, nev: int, tol: float, mode: str = "mixed", blocks=(64, 96, 128),
                  steps=(4, 6, 8), reps: int = 2, min_block: int = 40, **kw):
     """Pick the block width and power-step count of subspace_iter_svd for this problem by timing
@@ -889,9 +906,14 @@ def autotune_svd(A, m: int, n: int, nev: int, tol: float, mode: str = "mixed", b
     stream = torch.cuda.current_stream()
     table = []
     best = None
+    tiles = []
+    p16 = kw.get("precision_output", "half")
     for b in blocks:
         if b < max(min_block, nev) or b > min(m, n):
             continue
+        if mode == "mixed":  # tile plans of the 16-bit products of this block width: A V, A' U, the Grams
+            for shp in ((m, b, n), (n, b, m), (b, b, m), (b, b, n)):
+                tiles.append(autotune_gemm16(*shp, precision=p16))
         for st in steps:
             args = dict(maxiter=kw.get("maxiter", 80), step_size=st, mode=mode, tol=tol, nev=nev,
                         check_every=kw.get("check_every", 1), generalized_tol=kw.get("generalized_tol", 0.0))
@@ -915,4 +937,5 @@ def autotune_svd(A, m: int, n: int, nev: int, tol: float, mode: str = "mixed", b
     if best is None:
         raise RuntimeError("autotune_svd: no candidate converged")
     best["table"] = table
+    best["tiles"] = tiles
     return best

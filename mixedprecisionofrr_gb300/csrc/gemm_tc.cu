@@ -22,6 +22,8 @@
 #include "ofrr_internal.cuh"
 #include "tcgen05.cuh"
 
+#include <mutex>
+
 namespace ofrr {
 namespace tc {
 
@@ -328,6 +330,37 @@ static int launch(ofrr_ctx* ctx, const CUtensorMap& ma, const CUtensorMap& mb, i
 
 namespace tc {
 // enough CTAs to cover the SMs: split K when the output grid is small
+// Tile plans found by the autotuner (ofrr_autotune_gemm16), process-wide, keyed by the exact shape and type;
+// shapes without a tuned plan take the heuristic below.
+struct TunedPlan {
+  int64_t M, N, K;
+  int t16, BN, splits;
+};
+static std::mutex g_plan_mu;
+static std::vector<TunedPlan> g_plans;
+
+static bool find_plan(int64_t M, int64_t N, int64_t K, int t16, int* BN, int* splits) {
+  std::lock_guard<std::mutex> lock(g_plan_mu);
+  for (const TunedPlan& p : g_plans)
+    if (p.M == M && p.N == N && p.K == K && p.t16 == t16) {
+      *BN = p.BN;
+      *splits = p.splits;
+      return true;
+    }
+  return false;
+}
+
+static void store_plan(int64_t M, int64_t N, int64_t K, int t16, int BN, int splits) {
+  std::lock_guard<std::mutex> lock(g_plan_mu);
+  for (TunedPlan& p : g_plans)
+    if (p.M == M && p.N == N && p.K == K && p.t16 == t16) {
+      p.BN = BN;
+      p.splits = splits;
+      return;
+    }
+  g_plans.push_back(TunedPlan{M, N, K, t16, BN, splits});
+}
+
 static int plan_splits(int64_t M, int64_t N, int64_t K, int BN) {
   const int tiles = (int)(((M + BM - 1) / BM) * ((N + BN - 1) / BN));
   const int kbt = (int)((K + BK - 1) / BK);
@@ -335,6 +368,13 @@ static int plan_splits(int64_t M, int64_t N, int64_t K, int BN) {
   while (tiles * splits < 148 && splits * 2 <= kbt && splits < 64) splits *= 2;
   if (const char* e = getenv("OFRR_TC_SPLITS")) splits = std::max(1, std::min(atoi(e), kbt));  // tuning override
   return splits;
+}
+
+// the tile width and K split of a product: the tuned plan when there is one, else the heuristic
+static void choose_plan(int64_t M, int64_t N, int64_t K, int t16, int* BN, int* splits) {
+  if (find_plan(M, N, K, t16, BN, splits)) return;
+  *BN = (N <= 32) ? 32 : (N <= 64 ? 64 : 128);
+  *splits = plan_splits(M, N, K, *BN);
 }
 }  // namespace tc
 
@@ -348,11 +388,11 @@ int gemm_tc_try(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype t16, int64_t M
   if (K < 16 || M < 1 || N < 1 || M > (1 << 30) || N > (1 << 30) || K > (1 << 30)) return OFRR_SUCCESS;
   if (((uintptr_t)A & 15) || ((uintptr_t)B & 15) || ((lda * 2) & 15) || ((ldb * 2) & 15)) return OFRR_SUCCESS;
   if (getenv("OFRR_DISABLE_TC")) return OFRR_SUCCESS;
-  const int BN = (N <= 32) ? 32 : (N <= 64 ? 64 : 128);
+  int BN = 64, splits = 1;
+  tc::choose_plan(M, N, K, t16, &BN, &splits);
   CUtensorMap ma, mb;
   if (!tc::make_map(&ma, t16, A, K, M, lda, tc::BM)) return OFRR_SUCCESS;
   if (!tc::make_map(&mb, t16, B, K, N, ldb, BN)) return OFRR_SUCCESS;
-  const int splits = tc::plan_splits(M, N, K, BN);
   int st = OFRR_SUCCESS;
   OFRR_DISPATCH_STORAGE(tout, TO, {
     if (BN == 32) st = tc::launch<32, TO>(ctx, ma, mb, (int)M, (int)N, (int)K, t16, (TO*)C, ldc, splits);
@@ -375,11 +415,11 @@ int gemm_tc_scalecols(ofrr_ctx* ctx, ofrr_dtype t16, int64_t M, int64_t N, int64
   if (K < 16 || M < 1 || N < 1 || M > 8192 || N > 65535 || K > (1 << 30)) return OFRR_SUCCESS;
   if (((uintptr_t)A & 15) || ((uintptr_t)B & 15) || ((lda * 2) & 15) || ((ldb * 2) & 15)) return OFRR_SUCCESS;
   if (getenv("OFRR_DISABLE_TC")) return OFRR_SUCCESS;
-  const int BN = (N <= 32) ? 32 : (N <= 64 ? 64 : 128);
+  int BN = 64, splits = 1;
+  tc::choose_plan(M, N, K, t16, &BN, &splits);
   CUtensorMap ma, mb;
   if (!tc::make_map(&ma, t16, A, K, M, lda, tc::BM)) return OFRR_SUCCESS;
   if (!tc::make_map(&mb, t16, B, K, N, ldb, BN)) return OFRR_SUCCESS;
-  const int splits = tc::plan_splits(M, N, K, BN);
   const int sc = fast ? 1 : 0;
   int st;
   if (t16 == OFRR_F16) {
@@ -410,4 +450,78 @@ extern "C" int ofrr_debug_gemm16_scalecols(ofrr_ctx* ctx, int t16, int64_t M, in
   bool handled = false;
   OFRR_TRY(gemm_tc_scalecols(ctx, (ofrr_dtype)t16, M, N, K, A, lda, B, ldb, C, ldc, fast != 0, &handled));
   return handled ? OFRR_SUCCESS : OFRR_ERR_INVALID_ARGUMENT;
+}
+
+// Tile autotuner of the 16-bit tcgen05 product (no reference counterpart): for C (M x N, FP32) = A' B with
+// A (K x M) and B (K x N) of type t16, every tile width BN in {32, 64, 128} and K split in {1, 2, 4, ...,
+// 64} (at most the number of 64-wide K blocks) is timed over reps launches (CUDA events, synchronous) on
+// seeded operands of that shape; the fastest plan is kept for the shape and used by every later product of
+// exactly that shape and type (the 16-bit power steps, Gram products and Ritz updates).
+extern "C" int ofrr_autotune_gemm16(ofrr_ctx* ctx, int t16, int64_t M, int64_t N, int64_t K, int reps, int* best_bn,
+                                    int* best_splits, double* best_us) {
+  if (!ctx || (t16 != OFRR_F16 && t16 != OFRR_BF16) || M < 1 || N < 1 || K < 16 || reps < 1)
+    return OFRR_ERR_INVALID_ARGUMENT;
+  if (M > (1 << 30) || N > (1 << 30) || K > (1 << 30)) return OFRR_ERR_BLAS_INVALID_SIZE;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  const int64_t Kp = (K + 7) / 8 * 8;
+  void* A = ws_alloc(ctx, (size_t)Kp * M * 2, &st);
+  void* B = ws_alloc(ctx, (size_t)Kp * N * 2, &st);
+  float* C = ws_get<float>(ctx, (size_t)M * N, &st);
+  if (!A || !B || !C) return st;
+  OFRR_TRY(ofrr_randn(ctx, 1, K, M, (ofrr_dtype)t16, A, Kp));
+  OFRR_TRY(ofrr_randn(ctx, 2, K, N, (ofrr_dtype)t16, B, Kp));
+  cudaEvent_t e0, e1;
+  OFRR_CUDA(cudaEventCreate(&e0));
+  OFRR_CUDA(cudaEventCreate(&e1));
+  const int kbt = (int)((K + tc::BK - 1) / tc::BK);
+  double best = INFINITY;
+  int bbn = 64, bsp = 1;
+  const int bns[3] = {32, 64, 128};
+  for (int bi = 0; bi < 3 && st == OFRR_SUCCESS; ++bi) {
+    const int BN = bns[bi];
+    CUtensorMap ma, mb;
+    if (!tc::make_map(&ma, (ofrr_dtype)t16, A, K, M, Kp, tc::BM) || !tc::make_map(&mb, (ofrr_dtype)t16, B, K, N, Kp, BN)) {
+      st = OFRR_ERR_INTERNAL;
+      break;
+    }
+    for (int sp = 1; sp <= 64 && sp <= kbt && st == OFRR_SUCCESS; sp *= 2) {
+      auto run = [&]() {
+        if (BN == 32) return tc::launch<32, float>(ctx, ma, mb, (int)M, (int)N, (int)K, (ofrr_dtype)t16, C, M, sp);
+        if (BN == 64) return tc::launch<64, float>(ctx, ma, mb, (int)M, (int)N, (int)K, (ofrr_dtype)t16, C, M, sp);
+        return tc::launch<128, float>(ctx, ma, mb, (int)M, (int)N, (int)K, (ofrr_dtype)t16, C, M, sp);
+      };
+      st = run();  // warm-up
+      if (st != OFRR_SUCCESS) break;
+      st = map_cuda_error(cudaEventRecord(e0, ctx->stream));
+      for (int r = 0; r < reps && st == OFRR_SUCCESS; ++r) st = run();
+      if (st == OFRR_SUCCESS) st = map_cuda_error(cudaEventRecord(e1, ctx->stream));
+      if (st == OFRR_SUCCESS) st = sync_and_check(ctx);
+      float ms = 0.f;
+      if (st == OFRR_SUCCESS) st = map_cuda_error(cudaEventElapsedTime(&ms, e0, e1));
+      const double us = 1e3 * ms / reps;
+      if (st == OFRR_SUCCESS && us < best) {
+        best = us;
+        bbn = BN;
+        bsp = sp;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  OFRR_TRY(st);
+  tc::store_plan(M, N, K, t16, bbn, bsp);
+  if (best_bn) *best_bn = bbn;
+  if (best_splits) *best_splits = bsp;
+  if (best_us) *best_us = best;
+  return OFRR_SUCCESS;
+}
+
+// The plan a 16-bit product of this shape would use now; *tuned = 1 when it came from the autotuner.
+extern "C" int ofrr_gemm16_plan(int t16, int64_t M, int64_t N, int64_t K, int* bn, int* splits, int* tuned) {
+  if (!bn || !splits) return OFRR_ERR_INVALID_ARGUMENT;
+  const bool t = tc::find_plan(M, N, K, t16, bn, splits);
+  if (!t) tc::choose_plan(M, N, K, t16, bn, splits);
+  if (tuned) *tuned = t ? 1 : 0;
+  return OFRR_SUCCESS;
 }

@@ -138,3 +138,21 @@ def test_tc_gemm_scalecols_fused(api, M, N, K, pin):
                                                    api.ld_of(Bd), Cd.data_ptr(), api.ld_of(Cd), fast) == L.SUCCESS
         assert ctx.lib.ofrr_ctx_synchronize(ctx.h) == L.SUCCESS
         assert torch.equal(Cd.view(torch.int16), ref.view(torch.int16))
+
+
+@pytest.mark.parametrize("M,N,K", [(8192, 64, 2048), (2048, 64, 8192), (64, 64, 8192), (300, 40, 1000)])
+def test_tile_autotuner_plan_is_used_and_correct(api, M, N, K):
+    """The autotuner times every tile width and K split of a shape and keeps the fastest; the product of
+    that shape then runs with the tuned plan and stays within the FP32-accumulation tolerance."""
+    t = api.autotune_gemm16(M, N, K, "half", reps=3)
+    assert t["BN"] in (32, 64, 128) and t["splits"] >= 1 and t["us"] > 0
+    plan = api.gemm16_plan(M, N, K, "half")
+    assert plan["tuned"] and plan["BN"] == t["BN"] and plan["splits"] == t["splits"]
+    rng = np.random.default_rng(M + N + K)
+    p = api.PREC["half"]
+    Ad = api.to_device_cm(rng.standard_normal((K, M)), p)
+    Bd = api.to_device_cm(rng.standard_normal((K, N)), p)
+    ref = Ad.double().cpu().numpy().T @ Bd.double().cpu().numpy()
+    Cd = api.gemm(Ad, "T", Bd, "single", "single")
+    got = Cd.double().cpu().numpy()
+    assert np.max(np.abs(got - ref)) <= 2e-6 * np.sqrt(K) * np.max(np.abs(ref))
