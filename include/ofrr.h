@@ -123,6 +123,12 @@ int ofrr_gemm(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
               double alpha, const void* A /*dev*/, int64_t lda, const void* B /*dev*/,
               int64_t ldb, double beta, void* C /*dev*/, int64_t ldc);
 
+/* C (M x N, FP32) = A' B for FP32 A (K x M, K >= 32) and B (K x N): both quantized per column to E4M3
+ * with power-of-two scales, multiplied on the tcgen05 tensor cores (kind::f8f6f4, FP32 accumulation) and
+ * scaled back (no reference counterpart; the product of the FP8 variant of the power steps). */
+int ofrr_gemm_e4m3(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const float* A /*dev*/, int64_t lda,
+                   const float* B /*dev*/, int64_t ldb, float* C /*dev*/, int64_t ldc);
+
 /* Tile autotuner of the 16-bit tcgen05 product (no reference counterpart): times every tile width
  * BN in {32, 64, 128} and K split in {1, 2, ..., 64} of C (M x N, FP32) = A' B (A: K x M, B: K x N, type t16)
  * over reps launches on seeded operands and keeps the fastest plan for that exact shape and type
@@ -295,6 +301,10 @@ typedef struct {
    * max(nev + 4, 1.2 nev) leading Ritz values (at most kdim - 2) and the Galerkin residual direction
    * (new behaviour); k > 1 keeps about k. */
   int restart_keep;
+  /* OFRR_MODE_MIXED si_svd with a dense operator: 1 = the FP8 variant of the 16-bit phase, whose power
+   * steps multiply E4M3 copies of A (per-row power-of-two scales, made once per solve) and of the basis
+   * block (per column) on the tensor cores (kind::f8f6f4, FP32 accumulation); 0 = 16-bit products. */
+  int power_fp8;
 } ofrr_options;
 
 typedef struct {

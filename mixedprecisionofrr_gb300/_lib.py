@@ -46,7 +46,7 @@ class ofrr_options(C.Structure):
         ("use_start_block", C.c_int), ("orth", C.c_int), ("reorth", C.c_int),
         ("p_compute", C.c_int), ("p_output", C.c_int), ("p_hess_compute", C.c_int),
         ("p_hess_output", C.c_int), ("p_rr_compute", C.c_int), ("p_rr_output", C.c_int),
-        ("check_every", C.c_int), ("restart_keep", C.c_int),
+        ("check_every", C.c_int), ("restart_keep", C.c_int), ("power_fp8", C.c_int),
     ]
 
 
@@ -101,6 +101,7 @@ SIGNATURES = {
                             _P, _I64, _P, _I64, _D, _P, _I64]),
     "ofrr_gemm_f64_emulated": (C.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64]),
     "ofrr_autotune_gemm16": (C.c_int, [_P, C.c_int, _I64, _I64, _I64, C.c_int, _IP, _IP, _DP]),
+    "ofrr_gemm_e4m3": (C.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64]),
     "ofrr_gemm16_plan": (C.c_int, [C.c_int, _I64, _I64, _I64, _IP, _IP, _IP]),
     "ofrr_profile_gemm_f64_emulated": (C.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, C.c_int,
                                                   _DP, _DP]),

@@ -592,9 +592,10 @@ def subspace_iter_svd(A, m: int, n: int, k: int, precision_compute="double", pre
                       maxiter: int = 5, step_size: int = 1, precision_hess_compute=None, precision_hess_output=None,
                       precision_rr_compute=None, precision_rr_output=None, use_generalized=True,
                       generalized_tol=0.0, select_tol=None, V0=None, mode="reference", tol=0.0, nev=None,
-                      check_every=1, orth="hessenberg"):
+                      check_every=1, orth="hessenberg", power_fp8=False):
     """MATLAB/+src/+subspace/subspace_iter_svd.m; returns (U, s, V, info) with U, V on the device.  orth:
-    the basis of both blocks ("hessenberg", "mgs" or "cgs")."""
+    the basis of both blocks ("hessenberg", "mgs" or "cgs").  power_fp8 (mixed mode, dense A): the FP8
+    variant, E4M3 products in the 16-bit power steps."""
     ctx = context()
     op = operator(A, False)
     modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
@@ -603,6 +604,7 @@ def subspace_iter_svd(A, m: int, n: int, k: int, precision_compute="double", pre
                 use_generalized=int(use_generalized), generalized_tol=generalized_tol,
                 select_tol=-1.0 if select_tol is None else select_tol, seed=seed,
                 use_start_block=int(V0 is not None), check_every=check_every, orth=ORTH[orth],
+                power_fp8=int(power_fp8),
                 **_prec_opts(precision_compute, precision_output, precision_hess_compute, precision_hess_output,
                              precision_rr_compute, precision_rr_output))
     po = o.p_output if mode == "reference" else L.F64
@@ -889,6 +891,20 @@ def autotune_gemm16(M: int, N: int, K: int, precision: str = "half", reps: int =
     L.check(ctx.lib.ofrr_autotune_gemm16(ctx.h, _p(precision), M, N, K, reps, _ip(bn), _ip(sp), _dp(us)),
             "autotune_gemm16")
     return {"M": M, "N": N, "K": K, "BN": int(bn[0]), "splits": int(sp[0]), "us": float(us[0])}
+
+
+def gemm_e4m3(A, B):
+    """A' B through E4M3 copies (per-column power-of-two scales) on the tensor cores; A (K x M), B (K x N)
+    FP32 (ofrr_gemm_e4m3).  Returns the FP32 M x N device result."""
+    ctx = context()
+    Ad = A if is_cm(A) else to_device_cm(A, L.F32)
+    Bd = B if is_cm(B) else to_device_cm(B, L.F32)
+    K, M = Ad.shape
+    N = Bd.shape[1]
+    Cd = empty_cm(M, N, L.F32)
+    L.check(ctx.lib.ofrr_gemm_e4m3(ctx.h, M, N, K, Ad.data_ptr(), ld_of(Ad), Bd.data_ptr(), ld_of(Bd), Cd.data_ptr(),
+                                   ld_of(Cd)), "gemm_e4m3")
+    return Cd
 
 
 def gemm16_plan(M: int, N: int, K: int, precision: str = "half") -> dict:

@@ -13,6 +13,7 @@
 // Every mbarrier wait is bounded by a ~2 s timer; on timeout the kernel records an error word,
 // drains and returns, so a fault in the pipeline cannot hang the GPU.
 #include <cuda.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
 #include <atomic>
@@ -38,11 +39,14 @@ struct Smem {
   static constexpr int TOTAL = STAGES * STAGE + 1024 /*align*/ + 256 /*barriers*/;
 };
 
-template <int BN, class TOUT>
+// F8: E4M3 operands (kind::f8f6f4, 128-element K blocks of the same 128 bytes), the FP32 result scaled by
+// sa[row] sb[col] (powers of two, so the scaling is exact and commutes with the split-K sum)
+template <int BN, class TOUT, bool F8 = false>
 __global__ void __launch_bounds__(THREADS, 1)
     k_gemm_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N,
               int kblocks_total, int kblocks_per_split, uint32_t idesc, TOUT* __restrict__ D, int64_t ldd,
-              float* __restrict__ partial, int* __restrict__ err) {
+              float* __restrict__ partial, int* __restrict__ err, const float* __restrict__ sa = nullptr,
+              const float* __restrict__ sb = nullptr) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = base;
@@ -88,7 +92,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int s = i % STAGES;
         if (i >= STAGES && !mbar_wait(&empty[s], ((i / STAGES) + 1) & 1, err, 11)) break;
         mbar_expect_tx(&full[s], Smem<BN>::STAGE);
-        const int kx = (kb0 + i) * BK;
+        const int kx = (kb0 + i) * (F8 ? 2 * BK : BK);
         tma_load_2d(&tmA, &full[s], sA + s * Smem<BN>::A_BYTES, kx, m0);
         tma_load_2d(&tmB, &full[s], sB + s * Smem<BN>::B_BYTES, kx, n0);
         issued = i + 1;
@@ -106,7 +110,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t b0 = smem_u32(sB + s * Smem<BN>::B_BYTES);
 #pragma unroll
         for (int k = 0; k < BK / 16; ++k) {
-          umma_f16(tmem, desc_sw128(a0 + 32 * k), desc_sw128(b0 + 32 * k), idesc, (i > 0 || k > 0) ? 1u : 0u);
+          if (F8)
+            umma_f8(tmem, desc_sw128(a0 + 32 * k), desc_sw128(b0 + 32 * k), idesc, (i > 0 || k > 0) ? 1u : 0u);
+          else
+            umma_f16(tmem, desc_sw128(a0 + 32 * k), desc_sw128(b0 + 32 * k), idesc, (i > 0 || k > 0) ? 1u : 0u);
         }
         umma_commit(&empty[s]);
       }
@@ -127,6 +134,14 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (!ok || nkb == 0) {
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] = 0.f;
+      }
+      if (F8 && row < M) {
+        const float ra = sa[row];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int n = n0 + c + j;
+          v[j] *= ra * ((n < N) ? sb[n] : 0.f);
+        }
       }
       if (row < M) {
         if (split) {
@@ -370,6 +385,39 @@ static int plan_splits(int64_t M, int64_t N, int64_t K, int BN) {
   return splits;
 }
 
+// E4M3 product C (M x N, FP32) = diag(sa) (A8' B8) diag(sb): A8 (K x M) and B8 (K x N) E4M3 bytes,
+// K-contiguous with leading dimensions lda8, ldb8 (multiples of 16 bytes)
+template <int BN>
+static int launch_f8(ofrr_ctx* ctx, const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int K, float* D,
+                     int64_t ldd, int splits, const float* sa, const float* sb) {
+  const int kbt = (K + 2 * BK - 1) / (2 * BK);
+  splits = std::max(1, std::min(splits, kbt));
+  const int kbps = (kbt + splits - 1) / splits;
+  splits = (kbt + kbps - 1) / kbps;
+  const int gm = (M + BM - 1) / BM, gn = (N + BN - 1) / BN;
+  int st = OFRR_SUCCESS;
+  WsScope scope(ctx);
+  float* partial = nullptr;
+  if (splits > 1) {
+    partial = ws_get<float>(ctx, (size_t)splits * M * N, &st);
+    if (!partial) return st;
+  }
+  static std::atomic<bool> attr_set{false};
+  if (!attr_set) {
+    OFRR_TRY(allow_smem(k_gemm_tn<BN, float, true>));
+    attr_set = true;
+  }
+  dim3 grid(gm, gn, splits);
+  k_gemm_tn<BN, float, true><<<grid, THREADS, Smem<BN>::TOTAL, ctx->stream>>>(
+      ma, mb, M, N, kbt, kbps, make_idesc(OFRR_F16, BN), D, ldd, partial, ctx->dev_flags + kFlagTcWait, sa, sb);
+  OFRR_LAUNCHED(ctx, "k_gemm_tn_e4m3");
+  if (splits > 1) {
+    k_splitk_reduce<float, false><<<grid_2d(M, N, 256), 256, 0, ctx->stream>>>(M, N, splits, partial, D, ldd);
+    OFRR_LAUNCHED(ctx, "k_splitk_reduce");
+  }
+  return OFRR_SUCCESS;
+}
+
 // the tile width and K split of a product: the tuned plan when there is one, else the heuristic
 static void choose_plan(int64_t M, int64_t N, int64_t K, int t16, int* BN, int* splits) {
   if (find_plan(M, N, K, t16, BN, splits)) return;
@@ -524,4 +572,84 @@ extern "C" int ofrr_gemm16_plan(int t16, int64_t M, int64_t N, int64_t K, int* b
   if (!t) tc::choose_plan(M, N, K, t16, bn, splits);
   if (tuned) *tuned = t ? 1 : 0;
   return OFRR_SUCCESS;
+}
+
+namespace ofrr {
+namespace {
+// Per-column E4M3 copy of X (K x M, type TI, column-major): scale_j = 2^e with 2^e >= max_k |X(k, j)| / 448,
+// X8(k, j) = e4m3(X(k, j) / scale_j) (saturating); one CTA per column, ld8 bytes between columns
+template <class TI>
+__global__ void __launch_bounds__(256) k_quant_e4m3(int64_t K, int64_t M, const TI* __restrict__ X, int64_t ldx,
+                                                    __nv_fp8_e4m3* __restrict__ X8, int64_t ld8,
+                                                    float* __restrict__ scale) {
+  __shared__ float red[8];
+  const int64_t j = blockIdx.x;
+  const TI* x = X + j * ldx;
+  float mx = 0.f;
+  for (int64_t k = threadIdx.x; k < K; k += blockDim.x) mx = fmaxf(mx, fabsf(to_c<float, TI>(x[k])));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  float m = 0.f;
+  for (int w = 0; w < 8; ++w) m = fmaxf(m, red[w]);
+  // power-of-two scale: the largest entry lands in [224, 448]
+  const float sc = (m > 0.f) ? exp2f(ceilf(log2f(m / 448.f))) : 1.f;
+  const float inv = 1.f / sc;
+  if (threadIdx.x == 0) scale[j] = sc;
+  __nv_fp8_e4m3* y = X8 + j * ld8;
+  for (int64_t k = threadIdx.x; k < ld8; k += blockDim.x)
+    y[k] = (k < K) ? __nv_fp8_e4m3(to_c<float, TI>(x[k]) * inv) : __nv_fp8_e4m3(0.f);
+}
+}  // namespace
+
+int quant_e4m3(ofrr_ctx* ctx, ofrr_dtype tin, int64_t K, int64_t M, const void* X, int64_t ldx, void* X8,
+               int64_t ld8, float* scale) {
+  if (M <= 0) return OFRR_SUCCESS;
+  if (M > 0x7fffffffLL) return OFRR_ERR_BLAS_INVALID_SIZE;
+  OFRR_DISPATCH_STORAGE(tin, TI, {
+    k_quant_e4m3<TI><<<(unsigned)M, 256, 0, ctx->stream>>>(K, M, (const TI*)X, ldx, (__nv_fp8_e4m3*)X8, ld8, scale);
+    OFRR_LAUNCHED(ctx, "k_quant_e4m3");
+  });
+  return OFRR_SUCCESS;
+}
+
+// C (M x N, FP32) = diag(sa) A8' B8 diag(sb) on the tcgen05 tensor cores (kind::f8f6f4)
+int gemm_e4m3_tn(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const void* A8, int64_t lda8, const float* sa,
+                 const void* B8, int64_t ldb8, const float* sb, float* C, int64_t ldc) {
+  if (M < 1 || N < 1 || K < 32 || M > (1 << 30) || N > (1 << 30) || K > (1 << 30)) return OFRR_ERR_BLAS_INVALID_SIZE;
+  if (((uintptr_t)A8 & 15) || ((uintptr_t)B8 & 15) || (lda8 & 15) || (ldb8 & 15)) return OFRR_ERR_INVALID_ARGUMENT;
+  const int BN = (N <= 32) ? 32 : (N <= 64 ? 64 : 128);
+  CUtensorMap ma, mb;
+  if (!tc::make_map_u8(&ma, A8, K, M, lda8, tc::BM) || !tc::make_map_u8(&mb, B8, K, N, ldb8, BN))
+    return OFRR_ERR_INTERNAL;
+  const int tiles = (int)(((M + tc::BM - 1) / tc::BM) * ((N + BN - 1) / BN));
+  const int kbt = (int)((K + 127) / 128);
+  int splits = 1;
+  while (tiles * splits < 148 && splits * 2 <= kbt && splits < 64) splits *= 2;
+  if (BN == 32) return tc::launch_f8<32>(ctx, ma, mb, (int)M, (int)N, (int)K, C, ldc, splits, sa, sb);
+  if (BN == 64) return tc::launch_f8<64>(ctx, ma, mb, (int)M, (int)N, (int)K, C, ldc, splits, sa, sb);
+  return tc::launch_f8<128>(ctx, ma, mb, (int)M, (int)N, (int)K, C, ldc, splits, sa, sb);
+}
+
+}  // namespace ofrr
+
+// C (M x N, FP32) = A' B with FP32 A (K x M) and B (K x N): both quantized per column to E4M3 with
+// power-of-two scales, multiplied on the tensor cores (FP32 accumulation), scaled back (no reference
+// counterpart; the FP8 variant of the 16-bit power steps).
+extern "C" int ofrr_gemm_e4m3(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const float* A, int64_t lda,
+                              const float* B, int64_t ldb, float* C, int64_t ldc) {
+  if (!ctx || !A || !B || !C || M < 1 || N < 1 || K < 32 || lda < K || ldb < K || ldc < M)
+    return OFRR_ERR_INVALID_ARGUMENT;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  const int64_t ld8 = (K + 127) / 128 * 128;
+  void* A8 = ws_alloc(ctx, (size_t)ld8 * M, &st);
+  void* B8 = ws_alloc(ctx, (size_t)ld8 * N, &st);
+  float* sa = ws_get<float>(ctx, (size_t)M, &st);
+  float* sb = ws_get<float>(ctx, (size_t)N, &st);
+  if (!A8 || !B8 || !sa || !sb) return st;
+  OFRR_TRY(quant_e4m3(ctx, OFRR_F32, K, M, A, lda, A8, ld8, sa));
+  OFRR_TRY(quant_e4m3(ctx, OFRR_F32, K, N, B, ldb, B8, ld8, sb));
+  return gemm_e4m3_tn(ctx, M, N, ld8, A8, ld8, sa, B8, ld8, sb, C, ldc);
 }

@@ -80,6 +80,7 @@ struct ofrr_ctx {
   unsigned int* dev_counters = nullptr;  // grid "last block" counters (self-resetting)
   void* pinned = nullptr;          // small pinned host staging buffer
   bool emulate_f64 = false;        // FP64 TN products through exact BF16 slices on the tensor cores
+  bool power_f8 = false;           // 16-bit power steps through E4M3 copies (the FP8 variant)
   size_t pinned_size = 0;
   ofrr_ctx* aux = nullptr;         // second stream + workspace for independent work run beside this one
   ofrr::Tracer* tracer = nullptr;  // per-solve phase events and the JSON-lines sink (trace.cu), or null
@@ -455,6 +456,12 @@ int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
               int64_t lda, const void* B, int64_t ldb, double beta, void* C, int64_t ldc);
 int csrmm_impl(ofrr_ctx* ctx, const ofrr_csr* A, int trans, ofrr_dtype tx, ofrr_dtype tc, ofrr_dtype ty,
                int64_t nrhs, const void* X, int64_t ldx, void* Y, int64_t ldy);
+// E4M3 copies with per-column power-of-two scales (rows past K up to ld8 zero) and their tcgen05 product
+// C (M x N, FP32) = diag(sa) A8' B8 diag(sb) (K a multiple of 128, ld8 multiples of 16 bytes)
+int quant_e4m3(ofrr_ctx* ctx, ofrr_dtype tin, int64_t K, int64_t M, const void* X, int64_t ldx, void* X8,
+               int64_t ld8, float* scale);
+int gemm_e4m3_tn(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const void* A8, int64_t lda8, const float* sa,
+                 const void* B8, int64_t ldb8, const float* sb, float* C, int64_t ldc);
 // A' as CSR (row pointers, rows sorted within each column, every value copy present in A), in ctx's
 // current workspace scope; deterministic
 int csr_transpose_impl(ofrr_ctx* ctx, const ofrr_csr* A, ofrr_csr* At);

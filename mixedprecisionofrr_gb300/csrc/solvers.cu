@@ -84,9 +84,47 @@ struct Op {
 
   // Y = op(A) X, then scalecols(Y) (storage t, compute tc): one power step.  16-bit dense products with
   // FP32 accumulation combine their split-K partial sums inside the scaling kernel (same results).
+  // E4M3 copies of A for the FP8 variant of the 16-bit power steps: f8[0] = A' (K = n, for A V), f8[1] = A
+  // (K = m, for A' U), each column (one output row) with its power-of-two scale; made once per solve in the
+  // solve's outermost workspace scope
+  void* f8[2] = {nullptr, nullptr};
+  float* f8s[2] = {nullptr, nullptr};
+  int64_t f8ld[2] = {0, 0};
+  int prepare_f8(ofrr_ctx* ctx, ofrr_dtype t16) {
+    if (A->kind != OFRR_OP_DENSE) return OFRR_SUCCESS;
+    int st = OFRR_SUCCESS;
+    for (int trans = 0; trans < 2; ++trans) {
+      const int64_t M = trans ? n() : m(), K = trans ? m() : n();
+      const void* Ap;
+      int64_t lda;
+      if (trans) OFRR_TRY(dense_as(ctx, t16, &Ap, &lda));
+      else OFRR_TRY(dense_t_as(ctx, t16, &Ap, &lda));
+      f8ld[trans] = (K + 127) / 128 * 128;
+      if (!(f8[trans] = ws_alloc(ctx, (size_t)f8ld[trans] * M, &st))) return st;
+      if (!(f8s[trans] = ws_get<float>(ctx, (size_t)M, &st))) return st;
+      OFRR_TRY(quant_e4m3(ctx, t16, K, M, Ap, lda, f8[trans], f8ld[trans], f8s[trans]));
+    }
+    return OFRR_SUCCESS;
+  }
+
   int apply_scale(ofrr_ctx* ctx, int trans, ofrr_dtype t, ofrr_dtype tc, const void* X, int64_t ldx, int64_t nrhs,
                   void* Y, int64_t ldy, bool fast) {
     const int64_t M = trans ? n() : m(), K = trans ? m() : n();
+    if (ctx->power_f8 && f8[trans] && (t == OFRR_F16 || t == OFRR_BF16)) {
+      // the FP8 variant: the basis block quantized per column, the E4M3 product on the tensor cores, the
+      // FP32 result rounded to the 16-bit basis and scaled (scalecols)
+      WsScope tmp(ctx);
+      int st = OFRR_SUCCESS;
+      const int64_t ld8 = f8ld[trans];
+      void* X8 = ws_alloc(ctx, (size_t)ld8 * nrhs, &st);
+      float* sx = ws_get<float>(ctx, (size_t)nrhs, &st);
+      float* C = ws_get<float>(ctx, (size_t)M * nrhs, &st);
+      if (!X8 || !sx || !C) return st;
+      OFRR_TRY(quant_e4m3(ctx, t, K, nrhs, X, ldx, X8, ld8, sx));
+      OFRR_TRY(gemm_e4m3_tn(ctx, M, nrhs, ld8, f8[trans], ld8, f8s[trans], X8, ld8, sx, C, M));
+      OFRR_TRY(cast_impl(ctx, OFRR_F32, t, M, nrhs, C, M, Y, ldy));
+      return scalecols_impl(ctx, t, tc, M, nrhs, Y, ldy, nullptr, fast);
+    }
     if (A->kind == OFRR_OP_DENSE && tc == OFRR_F32 && (t == OFRR_F16 || t == OFRR_BF16)) {
       const void* Ad;
       int64_t lda;
@@ -1786,10 +1824,15 @@ static int si_svd_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
       int64_t l;
       OFRR_TRY(op.dense_as(ctx, L.po, &p, &l));
       OFRR_TRY(op.dense_t_as(ctx, L.po, &p, &l));
+      if (opt->power_fp8) OFRR_TRY(op.prepare_f8(ctx, L.po));
     }
     // the 16-bit phase cannot reach tolerances below ~1e-4: skip its FP64 residual checks then
     const double low_tol = opt->tol >= 1e-4 ? opt->tol : 0.0;
-    OFRR_TRY(svd_phase(ctx, op, L, opt, U16, m, V16, n, opt->maxiter, low_tol, nev, stag, S, d));
+    ctx->power_f8 = opt->power_fp8 != 0;
+    const int lst = svd_phase(ctx, op, L, opt, U16, m, V16, n, opt->maxiter, low_tol, nev,
+                              opt->power_fp8 ? 1e-3 : stag, S, d);
+    ctx->power_f8 = false;
+    OFRR_TRY(lst);
     OFRR_TRY(cast_impl(ctx, L.po, OFRR_F64, m, S.b, U16, m, U, ldu));
     OFRR_TRY(cast_impl(ctx, L.po, OFRR_F64, n, S.b, V16, n, V, ldv));
     escalations = 1;

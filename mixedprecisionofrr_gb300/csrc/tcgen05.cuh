@@ -76,6 +76,15 @@ __device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
+// E4M3 x E4M3 -> FP32 (kind::f8f6f4): K = 32 bytes per instruction, the same descriptors as the 16-bit form
+__device__ __forceinline__ void umma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
@@ -148,6 +157,21 @@ inline bool make_map(CUtensorMap* map, ofrr_dtype t, const void* ptr, int64_t K,
   return r == CUDA_SUCCESS;
 }
 
+// 2D map over a K-contiguous byte operand (E4M3): dims {K, rows}, row stride ld bytes, box {128, box_rows}
+inline bool make_map_u8(CUtensorMap* map, const void* ptr, int64_t K, int64_t rows, int64_t ld, int box_rows) {
+  EncodeTiledFn enc = get_encode();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld};
+  cuuint32_t box[2] = {(cuuint32_t)(2 * BK), (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// kind::f16: F16 = 0, BF16 = 1; kind::f8f6f4: E4M3 = 0 (so the F16 encoding serves E4M3 operands)
 inline uint32_t make_idesc(ofrr_dtype t, int BN) {
   const uint32_t fmt = (t == OFRR_BF16) ? 1u : 0u;
   uint32_t d = 0;

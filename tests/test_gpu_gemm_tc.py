@@ -156,3 +156,29 @@ def test_tile_autotuner_plan_is_used_and_correct(api, M, N, K):
     Cd = api.gemm(Ad, "T", Bd, "single", "single")
     got = Cd.double().cpu().numpy()
     assert np.max(np.abs(got - ref)) <= 2e-6 * np.sqrt(K) * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 128), (8192, 64, 2048), (300, 40, 1000), (64, 16, 8192)])
+def test_e4m3_gemm_exact_on_representable_inputs(api, M, N, K):
+    """The E4M3 tensor-core product: inputs that E4M3 holds exactly (small integers times powers of two,
+    so the per-column scales reproduce them) give the exact product (FP32 sums of integers below 2^24)."""
+    rng = np.random.default_rng(M + N + K)
+    A = rng.integers(-7, 8, (K, M)).astype(np.float32) * 2.0 ** rng.integers(-3, 4, (1, M))
+    B = rng.integers(-7, 8, (K, N)).astype(np.float32) * 2.0 ** rng.integers(-3, 4, (1, N))
+    A[:, 0] = 0.0  # an all-zero column (scale 1, product zero)
+    C = api.to_numpy(api.gemm_e4m3(A, B)).astype(np.float64)
+    ref = A.astype(np.float64).T @ B.astype(np.float64)
+    assert np.array_equal(C, ref)
+
+
+def test_e4m3_gemm_quantisation_error(api):
+    """Gaussian inputs: the product of the E4M3 copies is within the format's rounding (2^-4 relative per
+    entry) of the exact product, in the Cauchy-Schwarz scale."""
+    rng = np.random.default_rng(9)
+    K, M, N = 2048, 512, 64
+    A = rng.standard_normal((K, M)).astype(np.float32)
+    B = rng.standard_normal((K, N)).astype(np.float32)
+    C = api.to_numpy(api.gemm_e4m3(A, B)).astype(np.float64)
+    ref = A.astype(np.float64).T @ B.astype(np.float64)
+    bound = 2.0 ** -3 * np.sqrt(np.sum(A.astype(np.float64) ** 2, 0))[:, None] * np.sqrt(np.sum(B.astype(np.float64) ** 2, 0))[None, :]
+    assert np.all(np.abs(C - ref) <= bound)

@@ -258,6 +258,19 @@ def test_si_svd_mixed_benchmark_size(api, orc, block, step):
     assert np.all(r <= info.residuals[:32] * (1 + 1e-6) + 1e-15)
 
 
+def test_si_svd_fp8_variant_certified(api, orc):
+    """The FP8 variant of the mixed SVD (E4M3 products in the 16-bit power steps, then the FP64 phase):
+    the same certified tolerance and singular values as the 16-bit path on a quarter of the benchmark."""
+    A, U, s, V = orc.dense_svd_problem(4096, 1024, seed=7, smin=1e-6)
+    Ug, sg, Vg, info = api.subspace_iter_svd(A, 4096, 1024, 64, "single", "half", maxiter=80, step_size=6,
+                                             mode="mixed", tol=1e-8, nev=16, check_every=1, generalized_tol=0.0,
+                                             power_fp8=True)
+    assert info.status == 0, info
+    assert np.allclose(sg[:16], s[:16], rtol=1e-9)
+    r = orc.svd_residual_norms(A, api.to_numpy(Ug)[:, :16], sg[:16], api.to_numpy(Vg)[:, :16])
+    assert np.max(r) <= 1e-8
+
+
 def test_si_eig_mixed_dense_certified(api, orc):
     """Dense symmetric 2048 x 2048 (Haar Q, log-uniform spectrum), mixed mode, tol 1e-8: eigenvalues,
     true FP64 residuals and the certified residuals as an upper bound."""
