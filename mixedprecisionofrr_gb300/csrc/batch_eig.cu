@@ -17,9 +17,10 @@
 //    schedule).  The Gram matrices sum 64-row chunks in FP32 and the chunks in FP64; the 16 x 16 pencil
 //    is reduced by an FP64 Cholesky factor and solved by an FP32 Jacobi method.
 //  * k_batch_refine: FP32 arithmetic cannot certify residuals near 1e-7 (its own rounding is ~1e-7 of
-//    ||A||), so a second persistent pass takes the nev Ritz vectors of each matrix to FP64 accuracy: one
-//    or two block steps of Rayleigh-Ritz on [X, A X - X diag(l)] with FP64 products from the FP64 input,
-//    then the FP64 residuals that decide convergence.
+//    ||A||), so a second persistent pass takes each matrix's FP32 block (the nev wanted vectors and the
+//    guard columns) to FP64 accuracy: block steps of Rayleigh-Ritz on [X, A X - X diag(l)] with FP64
+//    products from the FP64 input until the FP64 residuals of the nev leading pairs meet tol (usually one
+//    or two steps; at most 8).
 // No spin waits: the queue is one atomic counter per kernel.
 #include "ofrr_internal.cuh"
 
@@ -543,22 +544,25 @@ struct RefineDev {
   const int64_t* xoff64;
   double* lam;          // out: count x nev
   double* res;          // out: count x nev (FP64 residuals / max|l|)
-  double* scratch;      // per CTA: 4 x BE_NMAX x BE_NEV doubles
+  double* scratch;      // per CTA: 3 x BE_NMAX x 2 BE_B doubles
   unsigned long long* tend;  // count: global timer when the matrix's refinement finished
   unsigned int* queue;
-  int count, nev, steps;
+  int count, nev, b, steps;
+  double tol;
 };
+
+constexpr int BR_K2 = 2 * BE_B;  // width of [X, R]
 
 // Y (n x k, ld n, FP64) = A (n x n) X (n x k, ld n) in FP64, threads over rows
 __device__ void br_matmul(int n, int k, const double* __restrict__ A, const double* X, double* Y) {
   for (int i = threadIdx.x; i < n; i += BE_T) {
-    double acc[2 * BE_NEV];
+    double acc[BE_B];
 #pragma unroll
-    for (int c = 0; c < 2 * BE_NEV; ++c) acc[c] = 0.0;
+    for (int c = 0; c < BE_B; ++c) acc[c] = 0.0;
     for (int kk = 0; kk < n; ++kk) {
       const double a = A[i + (int64_t)kk * n];
 #pragma unroll
-      for (int c = 0; c < 2 * BE_NEV; ++c)
+      for (int c = 0; c < BE_B; ++c)
         if (c < k) acc[c] = fma(a, X[kk + (int64_t)c * n], acc[c]);
     }
     for (int c = 0; c < k; ++c) Y[i + (int64_t)c * n] = acc[c];
@@ -577,16 +581,122 @@ __device__ double br_block_sum(double v, double* red) {
   return t;
 }
 
+// Rayleigh-Ritz of the symmetric pencil (G, M) of k2 unit columns, on one thread in FP64: M + tiny I = L L'
+// with columns whose part outside the span of the earlier ones is below 1e-4 of their norm dropped (their
+// row and column of the pencil removed), C = L^-1 sym(G) L^-T by a cyclic Jacobi method, and the kb largest
+// eigenvalues' vectors Z = L^-T U (k2 x kb, row-major, into Zout).  L, T, U are k2 x k2 scratch arrays.
+__device__ void br_rayleigh_ritz(int k2, int kb, double* G, double* M, double* L, double* T, double* Zout) {
+  bool drop[BR_K2];
+  double mx = 0.0;
+  for (int i = 0; i < k2; ++i) mx = fmax(mx, M[i * k2 + i]);
+  for (int j = 0; j < k2; ++j) {
+    double dj = M[j * k2 + j] + 1e-14 * mx;
+    for (int q = 0; q < j; ++q) dj -= L[j * k2 + q] * L[j * k2 + q];
+    drop[j] = !(dj > 1e-8 * M[j * k2 + j]);
+    for (int i = 0; i < j; ++i) L[i * k2 + j] = 0.0;
+    if (drop[j]) {
+      for (int q = 0; q < k2; ++q) L[j * k2 + q] = (q == j) ? 1.0 : 0.0;
+      for (int i = j + 1; i < k2; ++i) L[i * k2 + j] = 0.0;
+      for (int q = 0; q < k2; ++q) G[j * k2 + q] = G[q * k2 + j] = 0.0;
+      continue;
+    }
+    dj = sqrt(dj);
+    L[j * k2 + j] = dj;
+    for (int i = j + 1; i < k2; ++i) {
+      double v = M[i * k2 + j];
+      for (int q = 0; q < j; ++q) v -= L[i * k2 + q] * L[j * k2 + q];
+      L[i * k2 + j] = v / dj;
+    }
+  }
+  // rows of L for columns after a dropped one: entries L[i][j] of a dropped j are already zero
+  for (int c = 0; c < k2; ++c)
+    for (int i = 0; i < k2; ++i) {
+      double v = 0.5 * (G[i * k2 + c] + G[c * k2 + i]);
+      for (int q = 0; q < i; ++q) v -= L[i * k2 + q] * T[q * k2 + c];
+      T[i * k2 + c] = v / L[i * k2 + i];
+    }
+  double* Cm = M;  // C = T L^-T
+  for (int r = 0; r < k2; ++r)
+    for (int i = 0; i < k2; ++i) {
+      double v = T[r * k2 + i];
+      for (int q = 0; q < i; ++q) v -= L[i * k2 + q] * Cm[r * k2 + q];
+      Cm[r * k2 + i] = v / L[i * k2 + i];
+    }
+  double* U = G;
+  for (int e = 0; e < k2 * k2; ++e) U[e] = (e / k2 == e % k2) ? 1.0 : 0.0;
+  for (int i = 0; i < k2; ++i)
+    for (int j = i + 1; j < k2; ++j) {
+      const double a = 0.5 * (Cm[i * k2 + j] + Cm[j * k2 + i]);
+      Cm[i * k2 + j] = a;
+      Cm[j * k2 + i] = a;
+    }
+  for (int sweep = 0; sweep < 30; ++sweep) {
+    double off = 0.0, dn = 0.0;
+    for (int i = 0; i < k2; ++i)
+      for (int j = 0; j < k2; ++j) (i == j ? dn : off) += Cm[i * k2 + j] * Cm[i * k2 + j];
+    if (off <= 1e-30 * dn) break;
+    for (int p = 0; p < k2 - 1; ++p)
+      for (int q = p + 1; q < k2; ++q) {
+        const double apq = Cm[p * k2 + q];
+        if (fabs(apq) < 1e-300) continue;
+        const double theta = (Cm[q * k2 + q] - Cm[p * k2 + p]) / (2.0 * apq);
+        const double t = copysign(1.0, theta) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int q2 = 0; q2 < k2; ++q2) {
+          const double a1 = Cm[q2 * k2 + p], a2 = Cm[q2 * k2 + q];
+          Cm[q2 * k2 + p] = c * a1 - s * a2;
+          Cm[q2 * k2 + q] = s * a1 + c * a2;
+        }
+        for (int q2 = 0; q2 < k2; ++q2) {
+          const double a1 = Cm[p * k2 + q2], a2 = Cm[q * k2 + q2];
+          Cm[p * k2 + q2] = c * a1 - s * a2;
+          Cm[q * k2 + q2] = s * a1 + c * a2;
+          const double u1 = U[q2 * k2 + p], u2 = U[q2 * k2 + q];
+          U[q2 * k2 + p] = c * u1 - s * u2;
+          U[q2 * k2 + q] = s * u1 + c * u2;
+        }
+      }
+  }
+  // the kb largest eigenvalues among the kept directions (a dropped index keeps U = e_j, C_jj = 0)
+  int idx[BR_K2];
+  int nk = 0;
+  for (int i = 0; i < k2; ++i)
+    if (!drop[i]) idx[nk++] = i;
+  for (int i = 1; i < nk; ++i) {
+    const int v = idx[i];
+    int j = i - 1;
+    while (j >= 0 && Cm[idx[j] * k2 + idx[j]] < Cm[v * k2 + v]) {
+      idx[j + 1] = idx[j];
+      --j;
+    }
+    idx[j + 1] = v;
+  }
+  for (int c = 0; c < kb; ++c) {
+    const int src = idx[c < nk ? c : nk - 1];
+    for (int i = k2 - 1; i >= 0; --i) {
+      double v = U[i * k2 + src];
+      for (int q = i + 1; q < k2; ++q) v -= L[q * k2 + i] * T[q * k2 + c];
+      T[i * k2 + c] = v / L[i * k2 + i];
+    }
+  }
+  for (int e = 0; e < k2 * kb; ++e) Zout[e] = T[(e / kb) * k2 + (e % kb)];
+}
+
+// The whole FP32 block (b columns, the nev wanted plus guard vectors) is refined: block steps of
+// Rayleigh-Ritz on [X, A X - X diag(l)] with FP64 products from the FP64 input, until the FP64 residuals of
+// the nev leading pairs meet tol (or `steps` steps).  The guard columns keep the nearby part of the
+// spectrum inside the search space, so each step removes the error along it instead of only damping it.
 __global__ void __launch_bounds__(BE_T, 1) k_batch_refine(RefineDev d) {
   __shared__ double s_red[BE_T / 32];
-  __shared__ double s_G[4 * BE_NEV * BE_NEV], s_M[4 * BE_NEV * BE_NEV], s_Z[4 * BE_NEV * BE_NEV];
-  __shared__ double s_lam[2 * BE_NEV];
+  __shared__ double s_G[BR_K2 * BR_K2], s_M[BR_K2 * BR_K2], s_L[BR_K2 * BR_K2], s_T[BR_K2 * BR_K2];
+  __shared__ double s_Z[BR_K2 * BE_B];
+  __shared__ double s_lam[2 * BE_B];
   __shared__ int s_job;
   const int tid = threadIdx.x;
-  const int k = d.nev, k2 = 2 * d.nev;
-  double* Sx = d.scratch + (size_t)blockIdx.x * 4 * BE_NMAX * 2 * BE_NEV;  // [X | R] (n x 2k)
-  double* Sa = Sx + (size_t)BE_NMAX * 2 * BE_NEV;                           // A [X | R]
-  double* Sy = Sa + (size_t)BE_NMAX * 2 * BE_NEV;                           // new X, A X
+  const int kb = d.b, k2 = 2 * d.b, nev = d.nev;
+  double* Sx = d.scratch + (size_t)blockIdx.x * 3 * BE_NMAX * BR_K2;  // [X | R] (n x 2 kb)
+  double* Sa = Sx + (size_t)BE_NMAX * BR_K2;                          // A [X | R]
+  double* Sy = Sa + (size_t)BE_NMAX * BR_K2;                          // new X, A X
   while (true) {
     if (tid == 0) s_job = (int)atomicAdd(d.queue, 1u);
     __syncthreads();
@@ -597,12 +707,12 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_refine(RefineDev d) {
     const int n = (int)d.n[mi];
     const double* A = d.A64 + d.off[mi];
     const float* X32 = d.X32 + d.xoff[mi];
-    for (int e = tid; e < n * k; e += BE_T) Sx[e] = (double)X32[e];  // columns 0 .. k-1 of the FP32 block
+    for (int e = tid; e < n * kb; e += BE_T) Sx[e] = (double)X32[e];
     __syncthreads();
-    br_matmul(n, k, A, Sx, Sa);
-    for (int step = 0; step <= d.steps; ++step) {
-      // Rayleigh quotients and residuals R = A X - X diag(l) (into columns k .. 2k-1 of Sx)
-      for (int c = 0; c < k; ++c) {
+    br_matmul(n, kb, A, Sx, Sa);
+    for (int step = 0;; ++step) {
+      // Rayleigh quotients and residuals R = A X - X diag(l) (into columns kb .. 2kb-1 of Sx)
+      for (int c = 0; c < kb; ++c) {
         double xax = 0.0, xx = 0.0;
         for (int i = tid; i < n; i += BE_T) {
           xax = fma(Sx[i + c * n], Sa[i + c * n], xax);
@@ -611,172 +721,85 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_refine(RefineDev d) {
         xax = br_block_sum(xax, s_red);
         xx = br_block_sum(xx, s_red);
         if (tid == 0) s_lam[c] = (xx > 0.0) ? xax / xx : 0.0;
-        if (tid == 0) s_lam[k + c] = xx;
+        if (tid == 0) s_lam[kb + c] = xx;
         __syncthreads();
       }
       double lmax = 0.0;
-      for (int c = 0; c < k; ++c) lmax = fmax(lmax, fabs(s_lam[c]));
+      for (int c = 0; c < nev; ++c) lmax = fmax(lmax, fabs(s_lam[c]));
       if (lmax == 0.0) lmax = 1.0;
       double maxres = 0.0;
-      for (int c = 0; c < k; ++c) {
+      for (int c = 0; c < kb; ++c) {
         double rr = 0.0;
         for (int i = tid; i < n; i += BE_T) {
           const double r = Sa[i + c * n] - s_lam[c] * Sx[i + c * n];
-          Sx[i + (c + k) * n] = r;
+          Sx[i + (c + kb) * n] = r;
           rr = fma(r, r, rr);
         }
         rr = br_block_sum(rr, s_red);
-        const double res = (s_lam[k + c] > 0.0) ? sqrt(rr / s_lam[k + c]) / lmax : INFINITY;
-        if (tid == 0) d.res[(int64_t)mi * k + c] = res;
-        maxres = fmax(maxres, res);
+        if (c < nev) {
+          const double res = (s_lam[kb + c] > 0.0) ? sqrt(rr / s_lam[kb + c]) / lmax : INFINITY;
+          if (tid == 0) d.res[(int64_t)mi * nev + c] = res;
+          maxres = fmax(maxres, res);
+        }
         // unit columns for the block step: X (and A X) and the residual direction (the span is unchanged,
         // and the Gram matrix of [X, R] stays well scaled however small the residuals are)
-        const double sx = (s_lam[k + c] > 0.0) ? 1.0 / sqrt(s_lam[k + c]) : 0.0;
+        const double sx = (s_lam[kb + c] > 0.0) ? 1.0 / sqrt(s_lam[kb + c]) : 0.0;
         const double sr = (rr > 0.0) ? 1.0 / sqrt(rr) : 0.0;
         for (int i = tid; i < n; i += BE_T) {
           Sx[i + c * n] *= sx;
           Sa[i + c * n] *= sx;
-          Sx[i + (c + k) * n] *= sr;
+          Sx[i + (c + kb) * n] *= sr;
         }
       }
       __syncthreads();
-      if (step == d.steps || maxres <= 1e-13) {
-        if (tid < k) s_lam[k + tid] = 1.0;  // the columns are unit now
+      if (step >= d.steps || maxres <= d.tol) {
+        if (tid < kb) s_lam[kb + tid] = 1.0;  // the columns are unit now
         __syncthreads();
         break;
       }
       // block step: Rayleigh-Ritz on [X, R] (FP64 products)
-      br_matmul(n, k, A, Sx + (size_t)k * n, Sa + (size_t)k * n);
+      br_matmul(n, kb, A, Sx + (size_t)kb * n, Sa + (size_t)kb * n);
       for (int e = tid; e < 2 * k2 * k2; e += BE_T) {
         const int which = e / (k2 * k2), pr = e % (k2 * k2), r = pr / k2, c = pr % k2;
+        if (c < r) continue;  // both matrices are symmetric: upper triangle, mirrored below
         double acc = 0.0;
         const double* Bc = which ? Sx : Sa;
         for (int i = 0; i < n; ++i) acc = fma(Sx[i + r * n], Bc[i + c * n], acc);
-        if (which) s_M[pr] = acc;
-        else s_G[pr] = acc;
+        double* D = which ? s_M : s_G;
+        D[pr] = acc;
+        D[c * k2 + r] = acc;
       }
       __syncthreads();
-      if (tid == 0) {
-        // M + tiny I = L L' (in s_Z lower), C = L^-1 sym(G) L^-T, cyclic Jacobi in FP64
-        double* L = s_Z;
-        double mx = 0.0;
-        for (int i = 0; i < k2; ++i) mx = fmax(mx, s_M[i * k2 + i]);
-        for (int j = 0; j < k2; ++j) {
-          double dj = s_M[j * k2 + j] + 1e-14 * mx;
-          for (int q = 0; q < j; ++q) dj -= L[j * k2 + q] * L[j * k2 + q];
-          dj = sqrt(fmax(dj, 1e-300));
-          L[j * k2 + j] = dj;
-          for (int i = j + 1; i < k2; ++i) {
-            double v = s_M[i * k2 + j];
-            for (int q = 0; q < j; ++q) v -= L[i * k2 + q] * L[j * k2 + q];
-            L[i * k2 + j] = v / dj;
-          }
-          for (int i = 0; i < j; ++i) L[i * k2 + j] = 0.0;
-        }
-        double T[4 * BE_NEV * BE_NEV];
-        for (int c = 0; c < k2; ++c)
-          for (int i = 0; i < k2; ++i) {
-            double v = 0.5 * (s_G[i * k2 + c] + s_G[c * k2 + i]);
-            for (int q = 0; q < i; ++q) v -= L[i * k2 + q] * T[q * k2 + c];
-            T[i * k2 + c] = v / L[i * k2 + i];
-          }
-        double* Cm = s_M;  // reuse: C = T L^-T
-        for (int r = 0; r < k2; ++r)
-          for (int i = 0; i < k2; ++i) {
-            double v = T[r * k2 + i];
-            for (int q = 0; q < i; ++q) v -= L[i * k2 + q] * Cm[r * k2 + q];
-            Cm[r * k2 + i] = v / L[i * k2 + i];
-          }
-        double* U = s_G;  // eigenvectors
-        for (int e = 0; e < k2 * k2; ++e) U[e] = (e / k2 == e % k2) ? 1.0 : 0.0;
-        for (int e = 0; e < k2 * k2; ++e) {  // symmetrise
-          const int i = e / k2, j = e % k2;
-          if (i < j) {
-            const double a = 0.5 * (Cm[i * k2 + j] + Cm[j * k2 + i]);
-            Cm[i * k2 + j] = a;
-            Cm[j * k2 + i] = a;
-          }
-        }
-        for (int sweep = 0; sweep < 30; ++sweep) {
-          double off = 0.0, dn = 0.0;
-          for (int i = 0; i < k2; ++i)
-            for (int j = 0; j < k2; ++j) (i == j ? dn : off) += Cm[i * k2 + j] * Cm[i * k2 + j];
-          if (off <= 1e-30 * dn) break;
-          for (int p = 0; p < k2 - 1; ++p)
-            for (int q = p + 1; q < k2; ++q) {
-              const double apq = Cm[p * k2 + q];
-              if (fabs(apq) < 1e-300) continue;
-              const double theta = (Cm[q * k2 + q] - Cm[p * k2 + p]) / (2.0 * apq);
-              const double t = copysign(1.0, theta) / (fabs(theta) + sqrt(theta * theta + 1.0));
-              const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-              for (int q2 = 0; q2 < k2; ++q2) {
-                const double a1 = Cm[q2 * k2 + p], a2 = Cm[q2 * k2 + q];
-                Cm[q2 * k2 + p] = c * a1 - s * a2;
-                Cm[q2 * k2 + q] = s * a1 + c * a2;
-              }
-              for (int q2 = 0; q2 < k2; ++q2) {
-                const double a1 = Cm[p * k2 + q2], a2 = Cm[q * k2 + q2];
-                Cm[p * k2 + q2] = c * a1 - s * a2;
-                Cm[q * k2 + q2] = s * a1 + c * a2;
-                const double u1 = U[q2 * k2 + p], u2 = U[q2 * k2 + q];
-                U[q2 * k2 + p] = c * u1 - s * u2;
-                U[q2 * k2 + q] = s * u1 + c * u2;
-              }
-            }
-        }
-        // the k largest eigenvalues; their vectors Z = L^-T U (columns) into T
-        int idx[4 * BE_NEV];
-        for (int i = 0; i < k2; ++i) idx[i] = i;
-        for (int i = 1; i < k2; ++i) {
-          const int v = idx[i];
-          int j = i - 1;
-          while (j >= 0 && Cm[idx[j] * k2 + idx[j]] < Cm[v * k2 + v]) {
-            idx[j + 1] = idx[j];
-            --j;
-          }
-          idx[j + 1] = v;
-        }
-        for (int c = 0; c < k; ++c) {
-          const int src = idx[c];
-          for (int i = k2 - 1; i >= 0; --i) {
-            double v = U[i * k2 + src];
-            for (int q = i + 1; q < k2; ++q) v -= L[q * k2 + i] * T[q * k2 + c];
-            T[i * k2 + c] = v / L[i * k2 + i];
-          }
-        }
-        for (int e = 0; e < k2 * k; ++e) s_M[e] = T[(e / k) * k2 + (e % k)];  // Z (k2 x k), row-major
-      }
+      if (tid == 0) br_rayleigh_ritz(k2, kb, s_G, s_M, s_L, s_T, s_Z);
       __syncthreads();
       // X <- [X R] Z, A X <- [AX AR] Z
-      for (int i = tid; i < n; i += BE_T) {
-        double xr[2 * BE_NEV], ar[2 * BE_NEV];
-        for (int r = 0; r < k2; ++r) {
-          xr[r] = Sx[i + r * n];
-          ar[r] = Sa[i + r * n];
-        }
-        for (int c = 0; c < k; ++c) {
-          double x = 0.0, ax = 0.0;
-          for (int r = 0; r < k2; ++r) {
-            x = fma(xr[r], s_M[r * k + c], x);
-            ax = fma(ar[r], s_M[r * k + c], ax);
-          }
-          Sy[i + c * n] = x;
-          Sy[i + (c + k) * n] = ax;
+      for (int e = tid; e < 2 * n; e += BE_T) {
+        const int i = e % n, which = e / n;
+        const double* src = which ? Sa : Sx;
+        double vr[BR_K2];
+#pragma unroll
+        for (int r = 0; r < BR_K2; ++r) vr[r] = (r < k2) ? src[i + r * n] : 0.0;
+        for (int c = 0; c < kb; ++c) {
+          double x = 0.0;
+#pragma unroll
+          for (int r = 0; r < BR_K2; ++r)
+            if (r < k2) x = fma(vr[r], s_Z[r * kb + c], x);
+          Sy[i + (c + which * kb) * n] = x;
         }
       }
       __syncthreads();
-      for (int e = tid; e < n * k; e += BE_T) {
+      for (int e = tid; e < n * kb; e += BE_T) {
         Sx[e] = Sy[e];
-        Sa[e] = Sy[e + (size_t)k * n];
+        Sa[e] = Sy[e + (size_t)kb * n];
       }
       __syncthreads();
     }
-    // outputs: unit-norm FP64 Ritz vectors, Rayleigh quotients
+    // outputs: unit-norm FP64 Ritz vectors of the nev leading pairs, their Rayleigh quotients
     double* Xo = d.X64 + d.xoff64[mi];
-    for (int c = 0; c < k; ++c) {
-      const double inv = 1.0 / sqrt(fmax(s_lam[k + c], 1e-300));
+    for (int c = 0; c < nev; ++c) {
+      const double inv = 1.0 / sqrt(fmax(s_lam[kb + c], 1e-300));
       for (int i = tid; i < n; i += BE_T) Xo[i + (int64_t)c * n] = Sx[i + c * n] * inv;
-      if (tid == 0) d.lam[(int64_t)mi * k + c] = s_lam[c];
+      if (tid == 0) d.lam[(int64_t)mi * nev + c] = s_lam[c];
     }
     __syncthreads();
     if (tid == 0) d.tend[mi] = tc_globaltimer();
@@ -838,7 +861,7 @@ static int batch_sym_eig_impl(ofrr_ctx* ctx, int count, const int64_t* n_host, c
   OFRR_CUDA(cudaGetDevice(&dev));
   OFRR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int grid = std::max(1, std::min(sms, count));
-  double* scratch = ws_get<double>(ctx, (size_t)grid * 4 * BE_NMAX * 2 * BE_NEV, &st);
+  double* scratch = ws_get<double>(ctx, (size_t)grid * 3 * BE_NMAX * BR_K2, &st);
   if (!A32 || !A16 || !X32 || !lam32 || !dn || !doff || !dxo || !dxo64 || !dorder || !dit || !dlam || !dres ||
       !queues || !scratch || !times)
     return st;
@@ -903,7 +926,9 @@ static int batch_sym_eig_impl(ofrr_ctx* ctx, int count, const int64_t* n_host, c
   r.queue = queues + 1;
   r.count = count;
   r.nev = nev;
-  r.steps = 2;
+  r.b = b;
+  r.steps = 8;
+  r.tol = opt->tol > 0 ? opt->tol : 1e-7;
   k_batch_refine<<<grid, BE_T, 0, ctx->stream>>>(r);
   OFRR_LAUNCHED(ctx, "k_batch_refine");
   std::vector<double> hres((size_t)count * nev);
