@@ -55,6 +55,8 @@ def parse():
                     help="c2: the dense SVD headline (default; also runs a compact C3 leg); c3: the 128^3 "
                          "convection-diffusion Krylov workload alone; c5: the serving stream")
     ap.add_argument("--requests", type=int, default=400, help="c5: requests replayed from the seeded stream")
+    ap.add_argument("--batch-count", type=int, default=None,
+                    help="c4: matrices in the batch (default 4096; smaller only for profiler captures)")
     ap.add_argument("--time-scale", type=float, default=1.0,
                     help="c5: arrival times multiplied by this (1 = the stream's 2000 req/s)")
     ap.add_argument("--no-c3", action="store_true", help="skip the C3 leg of the default run")
@@ -150,18 +152,19 @@ def flush_l2(buf):
     buf.add_(1.0)
 
 
-def run_solver(api, A, mode, V0=None):
+def run_solver(api, A, mode, V0=None, fp8=False):
     b, st = CFG.get(mode, (BLOCK, STEP))
     return api.subspace_iter_svd(A, M_ROWS, N_COLS, b, "single", "half", maxiter=MAXITER, step_size=st,
-                                 mode=mode, tol=TOL, nev=NEV, check_every=1, V0=V0, generalized_tol=0.0)
+                                 mode=mode, tol=TOL, nev=NEV, check_every=1, V0=V0, generalized_tol=0.0,
+                                 power_fp8=fp8)
 
 
-def time_solves(api, A, mode, steps, warmup, flush_buf):
+def time_solves(api, A, mode, steps, warmup, flush_buf, fp8=False):
     import torch
 
     stream = torch.cuda.current_stream()
     for _ in range(warmup):
-        run_solver(api, A, mode)
+        run_solver(api, A, mode, fp8=fp8)
     torch.cuda.synchronize()
     times, infos = [], []
     ctx = api.context()
@@ -172,7 +175,7 @@ def time_solves(api, A, mode, steps, warmup, flush_buf):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        U, s, V, info = run_solver(api, A, mode)
+        U, s, V, info = run_solver(api, A, mode, fp8=fp8)
         e1.record(stream)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
@@ -593,11 +596,11 @@ def c4_problem(api, count=C4_COUNT, seed=4096):
     return buf, ns, offs, np.array(lams)
 
 
-def c4_run(api, steps, warmup, cpu=True):
+def c4_run(api, steps, warmup, cpu=True, count=None):
     """The batched workload: 4096 matrices in one persistent launch (plus the FP64 refinement launch)."""
     import torch
 
-    buf, ns, offs, lams = c4_problem(api)
+    buf, ns, offs, lams = c4_problem(api, count=count or C4_COUNT)
     stream = api.context().stream
     for _ in range(warmup):
         api.batch_sym_eig(buf, ns, offs, nev=C4_NEV, tol=C4_TOL)
@@ -777,10 +780,19 @@ def main():
         print(json.dumps(csr_load_run(api)))
         return
     if args.config == "c3":
+        if args.profile_solve:  # one mixed solve (for launch lists and captures)
+            from mixedprecisionofrr_gb300 import problems
+
+            Acsr = api.CsrMatrix(problems.convdiff_3d(C3_N), symmetric=False)
+            X, d, info = c3_solve(api, Acsr, "mixed")
+            torch.cuda.synchronize()
+            print(json.dumps({"profile_solve": True, "config": "c3", "status": info.status, "cycles": info.iterations,
+                              "matvecs": info.matvecs, "max_residual": info.max_residual}))
+            return
         print(json.dumps(c3_run(api, args.steps, args.warmup)))
         return
     if args.config == "c4":
-        print(json.dumps(c4_run(api, args.steps, args.warmup)))
+        print(json.dumps(c4_run(api, args.steps, args.warmup, cpu=not args.no_cpu_baseline, count=args.batch_count)))
         return
     if args.config == "c5":
         print(json.dumps(c5_run(api, args.requests, args.time_scale)))
@@ -837,6 +849,14 @@ def main():
             fp64 = {"value": NEV * k64 / float(t64.sum()), "unit": UNIT, "ms_per_solve": 1e3 * float(t64.mean()),
                     "iterations": float(np.mean([i.iterations for i in inf64])),
                     "max_residual": float(max(i.max_residual for i in inf64))}
+        # the FP8 (E4M3, per-column power-of-two scales) power-step variant on the same configuration
+        t8, inf8, _, s8 = time_solves(api, A, "mixed", args.steps, 1, flush_buf, fp8=True)
+        fp8 = {"value": NEV * args.steps / float(t8.sum()), "unit": UNIT, "ms_per_solve": 1e3 * float(t8.mean()),
+               "iterations": float(np.mean([i.iterations for i in inf8])),
+               "max_residual": float(max(i.max_residual for i in inf8)),
+               "status": sorted({i.status for i in inf8}),
+               "max_rel_sigma_err": float(np.max(np.abs(s8[:NEV] - s_true[:NEV]) / s_true[:NEV])),
+               "dtype": "e4m3 power steps (per-column 2^e scales, FP32 accumulate), f16 basis / Gram, f64 pencil"}
         # end to end through the C ABI with host buffers
         A_host = torch.empty((N_COLS, M_ROWS), dtype=torch.float64).pin_memory()
         A_host.copy_(A.t())
@@ -890,6 +910,7 @@ def main():
             "iterations": iters, "max_residual": maxres, "max_rel_sigma_err": err, "status": statuses,
             "fp64_path": fp64,
             "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
+            "fp8_variant": fp8,
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof,
             "roofline_16bit_phase": roof16, "cpu_baseline": cpu,
             "c3": None if args.no_c3 else c3_run(api, min(args.steps, 2), 1, cpu=not args.no_cpu_baseline),

@@ -23,6 +23,7 @@
 //    or two steps; at most 8).
 // No spin waits: the queue is one atomic counter per kernel.
 #include "ofrr_internal.cuh"
+#include "tcgen05.cuh"
 
 namespace ofrr {
 namespace {
@@ -34,7 +35,7 @@ constexpr int BE_NEV = 8;      // leading pairs certified by the refinement
 
 struct BatchDev {
   const int64_t* n;        // count
-  const int64_t* off;      // element offset of matrix i in the FP64 / FP32 / 16-bit copies
+  const int64_t* offp;     // element offset of matrix i in the padded FP32 / 16-bit copies (ld = n rounded to 8)
   const int* order;        // processing order (largest first)
   const double* A64;
   const float* A32;
@@ -46,6 +47,7 @@ struct BatchDev {
   int* phase2;             // count: outer iteration at which the FP32 phase began (-1: never)
   unsigned long long* tstart;  // count: global timer when the matrix was taken from the queue
   unsigned int* queue;
+  int* err;                // device status word of bounded waits
   int count, b, nev, step, maxit;
   float tol16, tol32;      // residual targets that end the 16-bit and the FP32 phase
   uint64_t seed;
@@ -68,97 +70,236 @@ __device__ __forceinline__ uint64_t be_mix(uint64_t x) {
   return x ^ (x >> 31);
 }
 
-// block sum of one float per thread (all threads get the result); red: BE_T / 32 floats
-__device__ __forceinline__ float be_block_sum(float v, float* red) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  float t = 0.f;
-  for (int w = 0; w < BE_T / 32; ++w) t += red[w];
-  __syncthreads();
-  return t;
+// ---- A streamed through shared memory: a ring of BE_NS stages filled by bulk asynchronous copies ----
+// The FP32 and 16-bit copies of every matrix are stored column-major with the leading dimension rounded up
+// to 8 elements (zero rows below n) at 16-byte aligned offsets, so kc consecutive columns are one
+// contiguous, aligned block: one cp.async.bulk per stage, completing on the stage's `full` mbarrier.
+// Every warp arrives on the stage's `empty` mbarrier once it has read the stage; thread 0 refills a stage
+// after its `empty` phase completes.  The chunk counter runs on across products, so the barrier parities
+// follow from it.  Every wait is bounded (about 2 s); a wait that runs out records a status word and the
+// CTA leaves the kernel after the copies it issued have landed (again bounded).
+constexpr int BE_NS = 4;           // stages
+constexpr int BE_STAGE = 16384;    // bytes per stage
+
+struct BeRing {
+  unsigned char* buf;  // BE_NS x BE_STAGE (shared)
+  uint64_t* full;      // BE_NS (shared)
+  uint64_t* empty;     // BE_NS (shared)
+  uint32_t count;      // chunks consumed so far (uniform across the CTA)
+  int* err;            // device status word
+};
+
+__device__ __forceinline__ void be_bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   tc::smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(tc::smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void be_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
 }
 
-// W (n x b, row-major, shared) = A (n x n, column-major, global, type TA) V (n x b, row-major, shared).
-// G thread groups split k; group g's partial sums land in P (G x n x b) and are added in group order.
-template <class TA>
-__device__ void be_matmul(int n, int b, const TA* __restrict__ A, const float* V, float* W, float* P) {
-  const int tid = threadIdx.x;
-  const int npad = (n + 31) & ~31;
-  const int G = max(1, min(BE_T / npad, 16));
-  const int g = tid / npad, i0 = tid % npad;
-  const int kper = (n + G - 1) / G;
-  if (g < G) {
-    const int k0 = g * kper, k1 = min(n, k0 + kper);
-    for (int i = i0; i < n; i += (G == 1 ? BE_T : n + 1)) {  // G > 1: one row per thread
-      float acc[BE_B];
-#pragma unroll
-      for (int c = 0; c < BE_B; ++c) acc[c] = 0.f;
-      const TA* Ai = A + i;
-#pragma unroll 4
-      for (int k = k0; k < k1; ++k) {
-        const float a = be_ld(Ai + (int64_t)k * n);
-        const float* vk = V + k * BE_B;
-#pragma unroll
-        for (int c = 0; c < BE_B; ++c) acc[c] = fmaf(a, vk[c], acc[c]);
+// Row layout of a product for n rows: G thread groups split the columns of A (round-robin within a chunk),
+// each group of Tg threads (a multiple of 32) covers the rows with R rows per thread.  Chosen to keep
+// the most threads busy: maximise G / R subject to Tg R >= n.
+__device__ __forceinline__ void be_layout(int n, int* G, int* R) {
+  int bg = 1, br = 4;
+  for (int r = 1; r <= 4; ++r)
+    for (int g = 1; g <= 16; ++g) {
+      const int tg = ((BE_T / g) / 32) * 32;
+      if (tg * r >= n && g * br > bg * r) {
+        bg = g;
+        br = r;
       }
-      float* dst = (G == 1) ? (W + i * BE_B) : (P + ((size_t)g * n + i) * BE_B);
-#pragma unroll
-      for (int c = 0; c < BE_B; ++c) dst[c] = (c < b) ? acc[c] : 0.f;
-      if (G > 1) break;
+    }
+  *G = bg;
+  *R = br;
+}
+
+// W (n x b, row-major, shared) = A (n x n, column-major with leading dimension ld, global, type TA)
+// V (n x b, row-major, shared), FP32 accumulation.  Partial sums of the G groups are added in group order
+// (results do not depend on timing).  Returns false (uniformly) when a bounded wait ran out.
+template <class TA, int R>
+__device__ bool be_matmul_r(int n, int ld, const TA* __restrict__ A, const float* V, float* W, BeRing& rg, int G) {
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int Tg = ((BE_T / G) / 32) * 32;
+  const int g = tid / Tg, t = tid % Tg;
+  const bool active = g < G;
+  const int kc = min(n, BE_STAGE / (ld * (int)sizeof(TA)));
+  const int nck = (n + kc - 1) / kc;
+  const uint32_t base = rg.count;
+  auto issue = [&](int c) {
+    const uint32_t gc = base + (uint32_t)c;
+    const int st = (int)(gc % BE_NS);
+    const int k0 = c * kc, cols = min(kc, n - k0);
+    const uint32_t bytes = (uint32_t)(cols * ld * (int)sizeof(TA));
+    tc::mbar_expect_tx(&rg.full[st], bytes);
+    be_bulk_g2s(rg.buf + (size_t)st * BE_STAGE, A + (int64_t)k0 * ld, bytes, &rg.full[st]);
+  };
+  // refills wait for the stage's previous use to be released (that use belongs to an earlier chunk, or
+  // to the previous product)
+  bool bad = false;
+  if (tid == 0) {
+    for (int c = 0; c < min(nck, BE_NS); ++c) {
+      const uint32_t gc = base + (uint32_t)c;
+      if (gc >= BE_NS && !tc::mbar_wait(&rg.empty[gc % BE_NS], ((gc / BE_NS) + 1) & 1, rg.err, 21)) {
+        bad = true;
+        break;
+      }
+      issue(c);
     }
   }
-  __syncthreads();
-  if (G > 1) {
-    for (int e = tid; e < n * BE_B; e += BE_T) {
-      float s = 0.f;
-      for (int gg = 0; gg < G; ++gg) s += P[(size_t)gg * n * BE_B + e];
-      W[e] = s;
+  float acc[R][BE_B];
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int c = 0; c < BE_B; ++c) acc[r][c] = 0.f;
+  int c = 0;
+  for (; c < nck && !bad; ++c) {
+    const uint32_t gc = base + (uint32_t)c;
+    const int st = (int)(gc % BE_NS);
+    if (!tc::mbar_wait(&rg.full[st], (gc / BE_NS) & 1, rg.err, 22)) {
+      bad = true;
+      break;
+    }
+    const TA* sA = reinterpret_cast<const TA*>(rg.buf + (size_t)st * BE_STAGE);
+    const int k0 = c * kc, cols = min(kc, n - k0);
+    if (active) {
+      for (int kk = g; kk < cols; kk += G) {
+        const float4* vk = reinterpret_cast<const float4*>(V + (k0 + kk) * BE_B);
+        float v[BE_B];
+#pragma unroll
+        for (int q = 0; q < BE_B / 4; ++q) {
+          const float4 x = vk[q];
+          v[4 * q] = x.x;
+          v[4 * q + 1] = x.y;
+          v[4 * q + 2] = x.z;
+          v[4 * q + 3] = x.w;
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int i = t + r * Tg;
+          const float a = (i < n) ? be_ld(sA + kk * ld + i) : 0.f;
+#pragma unroll
+          for (int q = 0; q < BE_B; ++q) acc[r][q] = fmaf(a, v[q], acc[r][q]);
+        }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) be_arrive(&rg.empty[st]);
+    if (tid == 0 && c + BE_NS < nck) {
+      const uint32_t gn = base + (uint32_t)(c + BE_NS);
+      if (!tc::mbar_wait(&rg.empty[st], ((gn / BE_NS) + 1) & 1, rg.err, 23)) {
+        bad = true;
+        break;
+      }
+      issue(c + BE_NS);
+    }
+  }
+  if (__syncthreads_or(bad)) {
+    // leave only after every copy this CTA issued has landed (bounded)
+    if (tid == 0)
+      for (int j = 0; j < nck && j < c + BE_NS; ++j) {
+        const uint32_t gc = base + (uint32_t)j;
+        if (j >= c) tc::mbar_wait(&rg.full[gc % BE_NS], (gc / BE_NS) & 1, rg.err, 24);
+      }
+    __syncthreads();
+    return false;
+  }
+  rg.count = base + (uint32_t)nck;
+  for (int gg = 0; gg < G; ++gg) {
+    if (g == gg) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int i = t + r * Tg;
+        if (i < n) {
+          float4* w = reinterpret_cast<float4*>(W + i * BE_B);
+#pragma unroll
+          for (int q = 0; q < BE_B / 4; ++q) {
+            float4 x = make_float4(acc[r][4 * q], acc[r][4 * q + 1], acc[r][4 * q + 2], acc[r][4 * q + 3]);
+            if (gg > 0) {
+              const float4 y = w[q];
+              x.x += y.x;
+              x.y += y.y;
+              x.z += y.z;
+              x.w += y.w;
+            }
+            w[q] = x;
+          }
+        }
+      }
     }
     __syncthreads();
   }
+  return true;
 }
 
-// per column of X (n x b, row-major): the signed value of largest magnitude (first row on ties)
+template <class TA>
+__device__ bool be_matmul(int n, int ld, const TA* A, const float* V, float* W, BeRing& rg) {
+  int G, R;
+  be_layout(n, &G, &R);
+  switch (R) {
+    case 1: return be_matmul_r<TA, 1>(n, ld, A, V, W, rg, G);
+    case 2: return be_matmul_r<TA, 2>(n, ld, A, V, W, rg, G);
+    case 3: return be_matmul_r<TA, 3>(n, ld, A, V, W, rg, G);
+    default: return be_matmul_r<TA, 4>(n, ld, A, V, W, rg, G);
+  }
+}
+
+// per column of X (n x b, row-major): the signed value of largest magnitude (first row on ties), all
+// columns in one pass; redv / redi: (BE_T / 32) x BE_B scratch
 __device__ void be_colmax(int n, int b, const float* X, float* out, float* redv, int* redi) {
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  for (int c = 0; c < b; ++c) {
-    float best = -1.f;
-    int bi = 0x7fffffff;
-    for (int i = tid; i < n; i += BE_T) {
+  float best[BE_B];
+  int bi[BE_B];
+#pragma unroll
+  for (int c = 0; c < BE_B; ++c) {
+    best[c] = -1.f;
+    bi[c] = 0x7fffffff;
+  }
+  for (int i = tid; i < n; i += BE_T) {
+#pragma unroll
+    for (int c = 0; c < BE_B; ++c) {
       const float a = fabsf(X[i * BE_B + c]);
-      if (a > best) {
-        best = a;
-        bi = i;
+      if (a > best[c]) {
+        best[c] = a;
+        bi[c] = i;
       }
     }
+  }
+#pragma unroll
+  for (int c = 0; c < BE_B; ++c) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ob > best || (ob == best && oi < bi)) {
-        best = ob;
-        bi = oi;
+      const float ob = __shfl_xor_sync(0xffffffffu, best[c], o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi[c], o);
+      if (ob > best[c] || (ob == best[c] && oi < bi[c])) {
+        best[c] = ob;
+        bi[c] = oi;
       }
     }
-    if (lane == 0) {
-      redv[wid] = best;
-      redi[wid] = bi;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      float bb = -1.f;
-      int ii = 0x7fffffff;
-      for (int w = 0; w < BE_T / 32; ++w)
-        if (redv[w] > bb || (redv[w] == bb && redi[w] < ii)) {
-          bb = redv[w];
-          ii = redi[w];
-        }
-      out[c] = (ii < n) ? X[ii * BE_B + c] : 0.f;
-    }
-    __syncthreads();
   }
+  if (lane == 0)
+#pragma unroll
+    for (int c = 0; c < BE_B; ++c) {
+      redv[wid * BE_B + c] = best[c];
+      redi[wid * BE_B + c] = bi[c];
+    }
+  __syncthreads();
+  if (tid < b) {
+    float bb = -1.f;
+    int ii = 0x7fffffff;
+    for (int w = 0; w < BE_T / 32; ++w) {
+      const float v = redv[w * BE_B + tid];
+      const int vi = redi[w * BE_B + tid];
+      if (v > bb || (v == bb && vi < ii)) {
+        bb = v;
+        ii = vi;
+      }
+    }
+    out[tid] = (ii < n) ? X[ii * BE_B + tid] : 0.f;
+  }
+  __syncthreads();
 }
 
 // Symmetric 16 x 16 Jacobi eigensolver in FP32 on one warp, parallel (round-robin) ordering: every round
@@ -232,12 +373,14 @@ __device__ void be_jacobi(float* S, float* U, float* w, float* cs, int* pq) {
 
 template <class T16>
 __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
-  extern __shared__ float be_sm[];
+  extern __shared__ __align__(128) float be_sm[];
   float* V = be_sm;                  // BE_NMAX x BE_B
   float* W = V + BE_NMAX * BE_B;     // BE_NMAX x BE_B
-  float* P = W + BE_NMAX * BE_B;     // partial sums of small matrices: 16 x 32 x BE_B (also Gram chunks)
-  __shared__ float s_red[BE_T / 32];
-  __shared__ int s_redi[BE_T / 32];
+  unsigned char* ring = reinterpret_cast<unsigned char*>(W + BE_NMAX * BE_B);  // BE_NS x BE_STAGE
+  __shared__ uint64_t s_full[BE_NS], s_empty[BE_NS];
+  __shared__ float s_red[BE_T / 32 * BE_B];
+  __shared__ int s_redi[BE_T / 32 * BE_B];
+  __shared__ float s_c[BE_B];
   __shared__ float s_piv[BE_B];
   __shared__ int s_perm[BE_B];
   __shared__ int s_sel[BE_B];
@@ -250,6 +393,15 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
   __shared__ int s_job;
   const int tid = threadIdx.x;
   const int b = d.b;
+  if (tid == 0) {
+    for (int st = 0; st < BE_NS; ++st) {
+      tc::mbar_init(&s_full[st], 1);
+      tc::mbar_init(&s_empty[st], BE_T / 32);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  BeRing rg{ring, s_full, s_empty, 0u, d.err};
   while (true) {
     if (tid == 0) s_job = (int)atomicAdd(d.queue, 1u);
     __syncthreads();
@@ -259,7 +411,8 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
     const int mi = d.order[job];
     if (tid == 0) d.tstart[mi] = tc_globaltimer();
     const int n = (int)d.n[mi];
-    const int64_t off = d.off[mi];
+    const int ld = (n + 7) & ~7;
+    const int64_t off = d.offp[mi];
     const T16* A16 = reinterpret_cast<const T16*>(d.A16) + off;
     const float* A32 = d.A32 + off;
     // start block: Gaussian-like draws (sum of uniforms) from the matrix's key, scaled to unit maximum
@@ -275,8 +428,7 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
     for (; it < d.maxit; ++it) {
       // ---- power steps: V = scalecols(A V) ----
       for (int s = 0; s < d.step; ++s) {
-        if (phase == 0) be_matmul<T16>(n, b, A16, V, W, P);
-        else be_matmul<float>(n, b, A32, V, W, P);
+        if (!(phase == 0 ? be_matmul<T16>(n, ld, A16, V, W, rg) : be_matmul<float>(n, ld, A32, V, W, rg))) return;
         be_colmax(n, b, W, s_piv, s_red, s_redi);
         for (int e = tid; e < n * BE_B; e += BE_T) {
           const int c = e % BE_B;
@@ -285,20 +437,30 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
         }
         __syncthreads();
       }
-      // ---- Hessenberg basis of V (in place): MGS order, pivot on the first largest entry ----
+      // ---- Hessenberg basis of V (in place): MGS order, pivot on the first largest entry.  The
+      //      coefficients of column j come from a forward substitution on the pivot rows (thread 0, the
+      //      same fused multiply-adds in the same order as the column-by-column eliminations), then one
+      //      pass updates the column and finds its pivot ----
       for (int j = 0; j < b; ++j) {
-        for (int l = 0; l < j; ++l) {
-          if (!s_sel[l]) continue;
-          const float cl = V[s_perm[l] * BE_B + j];
-          __syncthreads();
-          for (int i = tid; i < n; i += BE_T) V[i * BE_B + j] -= cl * V[i * BE_B + l];
-          __syncthreads();
+        if (tid == 0) {
+          for (int l = 0; l < j; ++l) {
+            float cl = 0.f;
+            if (s_sel[l]) {
+              const float* Vp = V + s_perm[l] * BE_B;
+              cl = Vp[j];
+              for (int l2 = 0; l2 < l; ++l2) cl = fmaf(-s_c[l2], Vp[l2], cl);
+            }
+            s_c[l] = cl;
+          }
         }
-        // pivot of column j
+        __syncthreads();
         float bv = -1.f;
         int bi = 0x7fffffff;
         for (int i = tid; i < n; i += BE_T) {
-          const float a = fabsf(V[i * BE_B + j]);
+          float v = V[i * BE_B + j];
+          for (int l = 0; l < j; ++l) v = fmaf(-s_c[l], V[i * BE_B + l], v);
+          V[i * BE_B + j] = v;
+          const float a = fabsf(v);
           if (a > bv) {
             bv = a;
             bi = i;
@@ -337,8 +499,7 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
         __syncthreads();
       }
       // ---- Rayleigh-Ritz: W = A Q, G = Q' W, M = Q' Q (64-row FP32 chunks summed in FP64) ----
-      if (phase == 0) be_matmul<T16>(n, b, A16, V, W, P);
-      else be_matmul<float>(n, b, A32, V, W, P);
+      if (!(phase == 0 ? be_matmul<T16>(n, ld, A16, V, W, rg) : be_matmul<float>(n, ld, A32, V, W, rg))) return;
       {
         const int pairs = BE_B * BE_B;
         const int nch = (n + 63) / 64;
@@ -449,7 +610,7 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
           q[c] = V[i * BE_B + c];
           a[c] = W[i * BE_B + c];
         }
-#pragma unroll
+#pragma unroll 1
         for (int c = 0; c < BE_B; ++c) {
           float x = 0.f, ax = 0.f;
 #pragma unroll
@@ -464,18 +625,43 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
       __syncthreads();
       float maxres = 0.f;
       const float lmax = fmaxf(fabsf(s_lam[0]), 1e-30f);
-      for (int c = 0; c < d.nev; ++c) {
-        float rr = 0.f, xx = 0.f;
+      {
+        // residual and vector norms of the nev leading columns in one pass (sums in a fixed order)
+        float rr[BE_NEV], xx[BE_NEV];
+#pragma unroll
+        for (int c = 0; c < BE_NEV; ++c) rr[c] = xx[c] = 0.f;
         for (int i = tid; i < n; i += BE_T) {
-          const float x = V[i * BE_B + c];
-          const float r = W[i * BE_B + c] - s_lam[c] * x;
-          rr = fmaf(r, r, rr);
-          xx = fmaf(x, x, xx);
+#pragma unroll
+          for (int c = 0; c < BE_NEV; ++c) {
+            const float x = V[i * BE_B + c];
+            const float r = W[i * BE_B + c] - s_lam[c] * x;
+            rr[c] = fmaf(r, r, rr[c]);
+            xx[c] = fmaf(x, x, xx[c]);
+          }
         }
-        rr = be_block_sum(rr, s_red);
-        xx = be_block_sum(xx, s_red);
-        const float res = (xx > 0.f) ? sqrtf(rr / xx) / lmax : INFINITY;
-        maxres = fmaxf(maxres, res);
+#pragma unroll
+        for (int c = 0; c < BE_NEV; ++c)
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            rr[c] += __shfl_xor_sync(0xffffffffu, rr[c], o);
+            xx[c] += __shfl_xor_sync(0xffffffffu, xx[c], o);
+          }
+        if ((tid & 31) == 0)
+#pragma unroll
+          for (int c = 0; c < BE_NEV; ++c) {
+            s_red[(tid >> 5) * BE_B + c] = rr[c];
+            s_red[(tid >> 5) * BE_B + BE_NEV + c] = xx[c];
+          }
+        __syncthreads();
+        for (int c = 0; c < d.nev; ++c) {
+          float r2 = 0.f, x2 = 0.f;
+          for (int w = 0; w < BE_T / 32; ++w) {
+            r2 += s_red[w * BE_B + c];
+            x2 += s_red[w * BE_B + BE_NEV + c];
+          }
+          maxres = fmaxf(maxres, (x2 > 0.f) ? sqrtf(r2 / x2) / lmax : INFINITY);
+        }
+        __syncthreads();
       }
       // ---- phase and stop decisions (uniform across the CTA): a phase ends at its target or when the
       //      residual has not improved by 10 % over 8 iterations (its rounding floor) ----
@@ -553,21 +739,77 @@ struct RefineDev {
 
 constexpr int BR_K2 = 2 * BE_B;  // width of [X, R]
 
-// Y (n x k, ld n, FP64) = A (n x n) X (n x k, ld n) in FP64, threads over rows
-__device__ void br_matmul(int n, int k, const double* __restrict__ A, const double* X, double* Y) {
-  for (int i = threadIdx.x; i < n; i += BE_T) {
-    double acc[BE_B];
-#pragma unroll
-    for (int c = 0; c < BE_B; ++c) acc[c] = 0.0;
-    for (int kk = 0; kk < n; ++kk) {
-      const double a = A[i + (int64_t)kk * n];
-#pragma unroll
-      for (int c = 0; c < BE_B; ++c)
-        if (c < k) acc[c] = fma(a, X[kk + (int64_t)c * n], acc[c]);
-    }
-    for (int c = 0; c < k; ++c) Y[i + (int64_t)c * n] = acc[c];
+// Y (n x k, ld n, global FP64) = A (n x n, column-major, FP64) X (n x k, ld n, global).  X is first copied
+// into shared memory row-major (Xs: n x BE_B doubles) so that its values are broadcast reads; A is read
+// once per column pass with coalesced loads.  GB300's FP64 pipe (about 1.7 FMA per clock per SM), not
+// HBM, bounds this product, so the layout keeps every thread busy: G groups split the columns of A,
+// each thread covers R <= 2 rows and 16 / R columns of X per pass; the groups' partial sums are added in
+// group order (results do not depend on timing).
+__device__ void br_matmul(int n, int k, const double* __restrict__ A, const double* X, double* Y, double* Xs) {
+  const int tid = threadIdx.x;
+  for (int e = tid; e < n * BE_B; e += BE_T) {
+    const int i = e / BE_B, c = e % BE_B;
+    Xs[e] = (c < k) ? X[i + (int64_t)c * n] : 0.0;
   }
+  int G = 1, R = 2;
+  for (int r = 1; r <= 2; ++r)
+    for (int g = 1; g <= 16; ++g) {
+      const int tg = ((BE_T / g) / 32) * 32;
+      if (tg * r >= n && g * R > G * r) {
+        G = g;
+        R = r;
+      }
+    }
   __syncthreads();
+  const int Tg = ((BE_T / G) / 32) * 32;
+  const int g = tid / Tg, t = tid % Tg;
+  const int CW = BE_B / R;
+  for (int c0 = 0; c0 < k; c0 += CW) {
+    double acc[2][BE_B];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < BE_B; ++c) acc[r][c] = 0.0;
+    if (g < G) {
+      const int i0 = t, i1 = t + Tg;
+      const bool v0 = i0 < n, v1 = (R == 2) && i1 < n;
+      if (R == 1) {
+        for (int kk = g; kk < n; kk += G) {
+          const double a0 = v0 ? __ldg(A + i0 + (int64_t)kk * n) : 0.0;
+          const double* xr = Xs + kk * BE_B;
+#pragma unroll
+          for (int c = 0; c < BE_B; ++c) acc[0][c] = fma(a0, xr[c], acc[0][c]);
+        }
+      } else {
+        for (int kk = g; kk < n; kk += G) {
+          const double a0 = v0 ? __ldg(A + i0 + (int64_t)kk * n) : 0.0;
+          const double a1 = v1 ? __ldg(A + i1 + (int64_t)kk * n) : 0.0;
+          const double* xr = Xs + kk * BE_B + c0;
+#pragma unroll
+          for (int c = 0; c < BE_B / 2; ++c) {
+            acc[0][c] = fma(a0, xr[c], acc[0][c]);
+            acc[1][c] = fma(a1, xr[c], acc[1][c]);
+          }
+        }
+      }
+    }
+    for (int gg = 0; gg < G; ++gg) {
+      if (g == gg) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const int i = t + r * Tg;
+          if (r >= R || i >= n) continue;
+#pragma unroll
+          for (int c = 0; c < BE_B; ++c) {
+            if (c >= CW || c0 + c >= k) continue;
+            double* y = Y + i + (int64_t)(c0 + c) * n;
+            *y = (gg == 0) ? acc[r][c] : *y + acc[r][c];
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
 }
 
 __device__ double br_block_sum(double v, double* red) {
@@ -581,105 +823,164 @@ __device__ double br_block_sum(double v, double* red) {
   return t;
 }
 
-// Rayleigh-Ritz of the symmetric pencil (G, M) of k2 unit columns, on one thread in FP64: M + tiny I = L L'
-// with columns whose part outside the span of the earlier ones is below 1e-4 of their norm dropped (their
-// row and column of the pencil removed), C = L^-1 sym(G) L^-T by a cyclic Jacobi method, and the kb largest
-// eigenvalues' vectors Z = L^-T U (k2 x kb, row-major, into Zout).  L, T, U are k2 x k2 scratch arrays.
-__device__ void br_rayleigh_ritz(int k2, int kb, double* G, double* M, double* L, double* T, double* Zout) {
-  bool drop[BR_K2];
+// Rayleigh-Ritz of the symmetric pencil (G, M) of k2 <= 32 unit columns on one warp in FP64 (lane l owns
+// row / column l): M + tiny I = L L' with columns whose part outside the span of the earlier ones is
+// below 1e-4 of their norm dropped (their row and column of the pencil removed), C = L^-1 sym(G) L^-T,
+// a parallel cyclic Jacobi method (round-robin pairs, every round rotating k2 / 2 disjoint pairs), and
+// the kb largest eigenvalues' vectors Z = L^-T U (k2 x kb, row-major, into Zout).  All arrays k2 x k2
+// row-major in shared memory; G becomes U, M becomes C.
+__device__ void br_rayleigh_ritz_warp(int k2, int kb, double* G, double* M, double* L, double* T, double* Zout,
+                                      double* cs, int* pq, int* s_idx) {
+  const int lane = threadIdx.x & 31;
+  __shared__ int s_drop[BR_K2];
   double mx = 0.0;
   for (int i = 0; i < k2; ++i) mx = fmax(mx, M[i * k2 + i]);
+  for (int e = lane; e < k2 * k2; e += 32) L[e] = 0.0;
+  __syncwarp();
   for (int j = 0; j < k2; ++j) {
+    // row j of L left of the diagonal is final
     double dj = M[j * k2 + j] + 1e-14 * mx;
     for (int q = 0; q < j; ++q) dj -= L[j * k2 + q] * L[j * k2 + q];
-    drop[j] = !(dj > 1e-8 * M[j * k2 + j]);
-    for (int i = 0; i < j; ++i) L[i * k2 + j] = 0.0;
-    if (drop[j]) {
-      for (int q = 0; q < k2; ++q) L[j * k2 + q] = (q == j) ? 1.0 : 0.0;
-      for (int i = j + 1; i < k2; ++i) L[i * k2 + j] = 0.0;
-      for (int q = 0; q < k2; ++q) G[j * k2 + q] = G[q * k2 + j] = 0.0;
+    const bool drop = !(dj > 1e-8 * M[j * k2 + j]);
+    if (lane == 0) s_drop[j] = drop ? 1 : 0;
+    if (drop) {
+      __syncwarp();
+      for (int q = lane; q < k2; q += 32) {
+        L[j * k2 + q] = (q == j) ? 1.0 : 0.0;
+        G[j * k2 + q] = 0.0;
+        G[q * k2 + j] = 0.0;
+      }
+      __syncwarp();
       continue;
     }
     dj = sqrt(dj);
-    L[j * k2 + j] = dj;
-    for (int i = j + 1; i < k2; ++i) {
+    const int i = lane;
+    double lij = 0.0;
+    if (i > j && i < k2) {
       double v = M[i * k2 + j];
       for (int q = 0; q < j; ++q) v -= L[i * k2 + q] * L[j * k2 + q];
-      L[i * k2 + j] = v / dj;
+      lij = v / dj;
     }
+    __syncwarp();
+    if (i > j && i < k2) L[i * k2 + j] = lij;
+    if (lane == 0) L[j * k2 + j] = dj;
+    __syncwarp();
   }
-  // rows of L for columns after a dropped one: entries L[i][j] of a dropped j are already zero
-  for (int c = 0; c < k2; ++c)
+  // T = L^-1 sym(G): lane c solves column c
+  for (int c = lane; c < k2; c += 32)
     for (int i = 0; i < k2; ++i) {
       double v = 0.5 * (G[i * k2 + c] + G[c * k2 + i]);
       for (int q = 0; q < i; ++q) v -= L[i * k2 + q] * T[q * k2 + c];
       T[i * k2 + c] = v / L[i * k2 + i];
     }
-  double* Cm = M;  // C = T L^-T
-  for (int r = 0; r < k2; ++r)
+  __syncwarp();
+  // C = T L^-T: lane r solves row r (into M)
+  for (int r = lane; r < k2; r += 32)
     for (int i = 0; i < k2; ++i) {
       double v = T[r * k2 + i];
-      for (int q = 0; q < i; ++q) v -= L[i * k2 + q] * Cm[r * k2 + q];
-      Cm[r * k2 + i] = v / L[i * k2 + i];
+      for (int q = 0; q < i; ++q) v -= L[i * k2 + q] * M[r * k2 + q];
+      M[r * k2 + i] = v / L[i * k2 + i];
     }
+  __syncwarp();
+  double* Cm = M;
   double* U = G;
-  for (int e = 0; e < k2 * k2; ++e) U[e] = (e / k2 == e % k2) ? 1.0 : 0.0;
-  for (int i = 0; i < k2; ++i)
-    for (int j = i + 1; j < k2; ++j) {
+  for (int e = lane; e < k2 * k2; e += 32) {
+    const int i = e / k2, j = e % k2;
+    U[e] = (i == j) ? 1.0 : 0.0;
+    if (i < j) {
       const double a = 0.5 * (Cm[i * k2 + j] + Cm[j * k2 + i]);
       Cm[i * k2 + j] = a;
       Cm[j * k2 + i] = a;
     }
-  for (int sweep = 0; sweep < 30; ++sweep) {
+  }
+  __syncwarp();
+  const int np = k2 / 2;
+  for (int sweep = 0; sweep < 20; ++sweep) {
     double off = 0.0, dn = 0.0;
-    for (int i = 0; i < k2; ++i)
-      for (int j = 0; j < k2; ++j) (i == j ? dn : off) += Cm[i * k2 + j] * Cm[i * k2 + j];
-    if (off <= 1e-30 * dn) break;
-    for (int p = 0; p < k2 - 1; ++p)
-      for (int q = p + 1; q < k2; ++q) {
+    for (int e = lane; e < k2 * k2; e += 32) {
+      const double v = Cm[e] * Cm[e];
+      if (e / k2 != e % k2) off += v;
+      else dn += v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      dn += __shfl_xor_sync(0xffffffffu, dn, o);
+    }
+    if (off <= 1e-28 * dn) break;
+    for (int round = 0; round < k2 - 1; ++round) {
+      if (lane < np) {  // round-robin pairs: position 0 fixed, the others rotate
+        const int a = (lane == 0) ? 0 : 1 + (lane - 1 + round) % (k2 - 1);
+        const int b = 1 + (k2 - 2 - lane + round) % (k2 - 1);
+        const int p = min(a, b), q = max(a, b);
         const double apq = Cm[p * k2 + q];
-        if (fabs(apq) < 1e-300) continue;
-        const double theta = (Cm[q * k2 + q] - Cm[p * k2 + p]) / (2.0 * apq);
-        const double t = copysign(1.0, theta) / (fabs(theta) + sqrt(theta * theta + 1.0));
-        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-        for (int q2 = 0; q2 < k2; ++q2) {
-          const double a1 = Cm[q2 * k2 + p], a2 = Cm[q2 * k2 + q];
-          Cm[q2 * k2 + p] = c * a1 - s * a2;
-          Cm[q2 * k2 + q] = s * a1 + c * a2;
+        double c = 1.0, sn = 0.0;
+        if (fabs(apq) > 1e-300) {
+          const double theta = (Cm[q * k2 + q] - Cm[p * k2 + p]) / (2.0 * apq);
+          const double tt = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
+          c = 1.0 / sqrt(fma(tt, tt, 1.0));
+          sn = tt * c;
         }
-        for (int q2 = 0; q2 < k2; ++q2) {
-          const double a1 = Cm[p * k2 + q2], a2 = Cm[q * k2 + q2];
-          Cm[p * k2 + q2] = c * a1 - s * a2;
-          Cm[q * k2 + q2] = s * a1 + c * a2;
-          const double u1 = U[q2 * k2 + p], u2 = U[q2 * k2 + q];
-          U[q2 * k2 + p] = c * u1 - s * u2;
-          U[q2 * k2 + q] = s * u1 + c * u2;
+        cs[2 * lane] = c;
+        cs[2 * lane + 1] = sn;
+        pq[2 * lane] = p;
+        pq[2 * lane + 1] = q;
+      }
+      __syncwarp();
+      if (lane < k2) {  // columns: C = C J, U = U J (row `lane`)
+        for (int m = 0; m < np; ++m) {
+          const int p = pq[2 * m], q = pq[2 * m + 1];
+          const double c = cs[2 * m], sn = cs[2 * m + 1];
+          const double sp = Cm[lane * k2 + p], sq = Cm[lane * k2 + q];
+          Cm[lane * k2 + p] = c * sp - sn * sq;
+          Cm[lane * k2 + q] = sn * sp + c * sq;
+          const double up = U[lane * k2 + p], uq = U[lane * k2 + q];
+          U[lane * k2 + p] = c * up - sn * uq;
+          U[lane * k2 + q] = sn * up + c * uq;
         }
       }
+      __syncwarp();
+      if (lane < k2) {  // rows: C = J' C (column `lane`)
+        for (int m = 0; m < np; ++m) {
+          const int p = pq[2 * m], q = pq[2 * m + 1];
+          const double c = cs[2 * m], sn = cs[2 * m + 1];
+          const double sp = Cm[p * k2 + lane], sq = Cm[q * k2 + lane];
+          Cm[p * k2 + lane] = c * sp - sn * sq;
+          Cm[q * k2 + lane] = sn * sp + c * sq;
+        }
+      }
+      __syncwarp();
+    }
   }
   // the kb largest eigenvalues among the kept directions (a dropped index keeps U = e_j, C_jj = 0)
-  int idx[BR_K2];
-  int nk = 0;
-  for (int i = 0; i < k2; ++i)
-    if (!drop[i]) idx[nk++] = i;
-  for (int i = 1; i < nk; ++i) {
-    const int v = idx[i];
-    int j = i - 1;
-    while (j >= 0 && Cm[idx[j] * k2 + idx[j]] < Cm[v * k2 + v]) {
-      idx[j + 1] = idx[j];
-      --j;
+  if (lane == 0) {
+    int nk = 0;
+    for (int i = 0; i < k2; ++i)
+      if (!s_drop[i]) s_idx[nk++] = i;
+    for (int i = 1; i < nk; ++i) {
+      const int v = s_idx[i];
+      int j = i - 1;
+      while (j >= 0 && Cm[s_idx[j] * k2 + s_idx[j]] < Cm[v * k2 + v]) {
+        s_idx[j + 1] = s_idx[j];
+        --j;
+      }
+      s_idx[j + 1] = v;
     }
-    idx[j + 1] = v;
+    for (int i = nk; i < k2; ++i) s_idx[i] = s_idx[nk > 0 ? nk - 1 : 0];
   }
-  for (int c = 0; c < kb; ++c) {
-    const int src = idx[c < nk ? c : nk - 1];
+  __syncwarp();
+  // Z = L^-T U(:, idx): lane c solves column c (into T, then Zout)
+  for (int c = lane; c < kb; c += 32) {
+    const int src = s_idx[c];
     for (int i = k2 - 1; i >= 0; --i) {
       double v = U[i * k2 + src];
       for (int q = i + 1; q < k2; ++q) v -= L[q * k2 + i] * T[q * k2 + c];
       T[i * k2 + c] = v / L[i * k2 + i];
     }
   }
-  for (int e = 0; e < k2 * kb; ++e) Zout[e] = T[(e / kb) * k2 + (e % kb)];
+  __syncwarp();
+  for (int e = lane; e < k2 * kb; e += 32) Zout[e] = T[(e / kb) * k2 + (e % kb)];
+  __syncwarp();
 }
 
 // The whole FP32 block (b columns, the nev wanted plus guard vectors) is refined: block steps of
@@ -687,10 +988,13 @@ __device__ void br_rayleigh_ritz(int k2, int kb, double* G, double* M, double* L
 // the nev leading pairs meet tol (or `steps` steps).  The guard columns keep the nearby part of the
 // spectrum inside the search space, so each step removes the error along it instead of only damping it.
 __global__ void __launch_bounds__(BE_T, 1) k_batch_refine(RefineDev d) {
+  extern __shared__ __align__(16) double br_sm[];  // BE_NMAX x BE_B: the right-hand block of a product
   __shared__ double s_red[BE_T / 32];
   __shared__ double s_G[BR_K2 * BR_K2], s_M[BR_K2 * BR_K2], s_L[BR_K2 * BR_K2], s_T[BR_K2 * BR_K2];
   __shared__ double s_Z[BR_K2 * BE_B];
   __shared__ double s_lam[2 * BE_B];
+  __shared__ double s_cs[BR_K2];
+  __shared__ int s_pq[BR_K2], s_idx[BR_K2];
   __shared__ int s_job;
   const int tid = threadIdx.x;
   const int kb = d.b, k2 = 2 * d.b, nev = d.nev;
@@ -709,7 +1013,7 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_refine(RefineDev d) {
     const float* X32 = d.X32 + d.xoff[mi];
     for (int e = tid; e < n * kb; e += BE_T) Sx[e] = (double)X32[e];
     __syncthreads();
-    br_matmul(n, kb, A, Sx, Sa);
+    br_matmul(n, kb, A, Sx, Sa, br_sm);
     for (int step = 0;; ++step) {
       // Rayleigh quotients and residuals R = A X - X diag(l) (into columns kb .. 2kb-1 of Sx)
       for (int c = 0; c < kb; ++c) {
@@ -758,19 +1062,33 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_refine(RefineDev d) {
         break;
       }
       // block step: Rayleigh-Ritz on [X, R] (FP64 products)
-      br_matmul(n, kb, A, Sx + (size_t)kb * n, Sa + (size_t)kb * n);
-      for (int e = tid; e < 2 * k2 * k2; e += BE_T) {
-        const int which = e / (k2 * k2), pr = e % (k2 * k2), r = pr / k2, c = pr % k2;
-        if (c < r) continue;  // both matrices are symmetric: upper triangle, mirrored below
-        double acc = 0.0;
-        const double* Bc = which ? Sx : Sa;
-        for (int i = 0; i < n; ++i) acc = fma(Sx[i + r * n], Bc[i + c * n], acc);
-        double* D = which ? s_M : s_G;
-        D[pr] = acc;
-        D[c * k2 + r] = acc;
+      br_matmul(n, kb, A, Sx + (size_t)kb * n, Sa + (size_t)kb * n, br_sm);
+      {
+        // G = S' A S and M = S' S (both symmetric: the upper triangles, mirrored), one warp per entry
+        const int lane = tid & 31, wid = tid >> 5;
+        const int ntri = k2 * (k2 + 1) / 2;
+        for (int e = wid; e < 2 * ntri; e += BE_T / 32) {
+          const int which = e / ntri;
+          int pr = e % ntri, r = 0;
+          while (pr >= k2 - r) {
+            pr -= k2 - r;
+            ++r;
+          }
+          const int c = r + pr;
+          const double* Bc = which ? Sx : Sa;
+          double acc = 0.0;
+          for (int i = lane; i < n; i += 32) acc = fma(Sx[i + r * n], Bc[i + c * n], acc);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+          if (lane == 0) {
+            double* D = which ? s_M : s_G;
+            D[r * k2 + c] = acc;
+            D[c * k2 + r] = acc;
+          }
+        }
       }
       __syncthreads();
-      if (tid == 0) br_rayleigh_ritz(k2, kb, s_G, s_M, s_L, s_T, s_Z);
+      if (tid < 32) br_rayleigh_ritz_warp(k2, kb, s_G, s_M, s_L, s_T, s_Z, s_cs, s_pq, s_idx);
       __syncthreads();
       // X <- [X R] Z, A X <- [AX AR] Z
       for (int e = tid; e < 2 * n; e += BE_T) {
@@ -806,10 +1124,24 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_refine(RefineDev d) {
   }
 }
 
-template <class TI, class TO>
-__global__ void k_be_convert(int64_t count, const TI* __restrict__ in, TO* __restrict__ out) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
-    out[e] = from_c<TO, double>(to_c<double, TI>(in[e]));
+// The FP32 and 16-bit working copies of every matrix, one CTA per matrix: column-major with the leading
+// dimension rounded up to 8 (zero rows below n) at the padded offsets, each value rounded once from FP64.
+template <class T16>
+__global__ void k_be_pack(const int64_t* __restrict__ n, const int64_t* __restrict__ off,
+                          const int64_t* __restrict__ offp, const double* __restrict__ A, float* __restrict__ A32,
+                          T16* __restrict__ A16) {
+  const int mi = blockIdx.x;
+  const int nn = (int)n[mi], ld = (nn + 7) & ~7;
+  const double* src = A + off[mi];
+  float* d32 = A32 + offp[mi];
+  T16* d16 = A16 + offp[mi];
+  const int64_t total = (int64_t)nn * ld;
+  for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
+    const int j = (int)(e / ld), i = (int)(e % ld);
+    const double v = (i < nn) ? src[(int64_t)j * nn + i] : 0.0;
+    d32[e] = (float)v;
+    d16[e] = from_c<T16, double>(v);
+  }
 }
 
 }  // namespace
@@ -829,9 +1161,11 @@ static int batch_sym_eig_impl(ofrr_ctx* ctx, int count, const int64_t* n_host, c
   const ofrr_dtype t16 = (opt->p_output == OFRR_F16) ? OFRR_F16 : OFRR_BF16;
   int64_t total = 0, xtot = 0;
   std::vector<int> order(count);
+  std::vector<int64_t> offp(count);
   for (int i = 0; i < count; ++i) {
     if (n_host[i] < b || n_host[i] > BE_NMAX || offset_host[i] < 0) return OFRR_ERR_BLAS_INVALID_SIZE;
-    total = std::max(total, offset_host[i] + n_host[i] * n_host[i]);
+    offp[i] = total;
+    total += n_host[i] * ((n_host[i] + 7) & ~7);  // padded copies: ld = n rounded up to 8
     order[i] = i;
   }
   std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return n_host[a] > n_host[c]; });
@@ -849,6 +1183,7 @@ static int batch_sym_eig_impl(ofrr_ctx* ctx, int count, const int64_t* n_host, c
   float* lam32 = ws_get<float>(ctx, (size_t)count * BE_B, &st);
   int64_t* dn = ws_get<int64_t>(ctx, (size_t)count, &st);
   int64_t* doff = ws_get<int64_t>(ctx, (size_t)count, &st);
+  int64_t* doffp = ws_get<int64_t>(ctx, (size_t)count, &st);
   int64_t* dxo = ws_get<int64_t>(ctx, (size_t)count, &st);
   int64_t* dxo64 = ws_get<int64_t>(ctx, (size_t)count, &st);
   int* dorder = ws_get<int>(ctx, (size_t)count, &st);
@@ -862,25 +1197,24 @@ static int batch_sym_eig_impl(ofrr_ctx* ctx, int count, const int64_t* n_host, c
   OFRR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int grid = std::max(1, std::min(sms, count));
   double* scratch = ws_get<double>(ctx, (size_t)grid * 3 * BE_NMAX * BR_K2, &st);
-  if (!A32 || !A16 || !X32 || !lam32 || !dn || !doff || !dxo || !dxo64 || !dorder || !dit || !dlam || !dres ||
+  if (!A32 || !A16 || !X32 || !lam32 || !dn || !doff || !doffp || !dxo || !dxo64 || !dorder || !dit || !dlam || !dres ||
       !queues || !scratch || !times)
     return st;
   OFRR_CUDA(cudaMemcpyAsync(dn, n_host, sizeof(int64_t) * count, cudaMemcpyHostToDevice, ctx->stream));
   OFRR_CUDA(cudaMemcpyAsync(doff, offset_host, sizeof(int64_t) * count, cudaMemcpyHostToDevice, ctx->stream));
+  OFRR_CUDA(cudaMemcpyAsync(doffp, offp.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, ctx->stream));
   OFRR_CUDA(cudaMemcpyAsync(dxo, xo32.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, ctx->stream));
   OFRR_CUDA(cudaMemcpyAsync(dxo64, xo64.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, ctx->stream));
   OFRR_CUDA(cudaMemcpyAsync(dorder, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, ctx->stream));
   OFRR_CUDA(cudaMemsetAsync(queues, 0, 2 * sizeof(unsigned int), ctx->stream));
   // the FP32 and 16-bit copies of every matrix (one pass over the FP64 input)
-  const int gc = grid_for(total, 256, 152 * 16);
-  k_be_convert<double, float><<<gc, 256, 0, ctx->stream>>>(total, A, A32);
-  OFRR_LAUNCHED(ctx, "k_be_convert");
-  if (t16 == OFRR_F16) k_be_convert<double, __half><<<gc, 256, 0, ctx->stream>>>(total, A, (__half*)A16);
-  else k_be_convert<double, __nv_bfloat16><<<gc, 256, 0, ctx->stream>>>(total, A, (__nv_bfloat16*)A16);
-  OFRR_LAUNCHED(ctx, "k_be_convert");
+  if (t16 == OFRR_F16) k_be_pack<__half><<<count, 256, 0, ctx->stream>>>(dn, doff, doffp, A, A32, (__half*)A16);
+  else k_be_pack<__nv_bfloat16><<<count, 256, 0, ctx->stream>>>(dn, doff, doffp, A, A32, (__nv_bfloat16*)A16);
+  OFRR_LAUNCHED(ctx, "k_be_pack");
   BatchDev d{};
   d.n = dn;
-  d.off = doff;
+  d.offp = doffp;
+  d.err = ctx->dev_flags + kFlagTcWait;
   d.order = dorder;
   d.A64 = A;
   d.A32 = A32;
@@ -900,7 +1234,7 @@ static int batch_sym_eig_impl(ofrr_ctx* ctx, int count, const int64_t* n_host, c
   d.tol16 = (t16 == OFRR_F16) ? 2e-3f : 1e-2f;
   d.tol32 = (float)std::max(opt->tol, 1e-7);
   d.seed = opt->seed;
-  const size_t smem = (size_t)(2 * BE_NMAX * BE_B + 16 * 32 * BE_B) * sizeof(float);
+  const size_t smem = (size_t)2 * BE_NMAX * BE_B * sizeof(float) + (size_t)BE_NS * BE_STAGE;
   if (t16 == OFRR_F16) {
     OFRR_TRY(allow_smem(k_batch_si<__half>));
     k_batch_si<__half><<<grid, BE_T, smem, ctx->stream>>>(d);
@@ -929,7 +1263,8 @@ static int batch_sym_eig_impl(ofrr_ctx* ctx, int count, const int64_t* n_host, c
   r.b = b;
   r.steps = 8;
   r.tol = opt->tol > 0 ? opt->tol : 1e-7;
-  k_batch_refine<<<grid, BE_T, 0, ctx->stream>>>(r);
+  OFRR_TRY(allow_smem(k_batch_refine));
+  k_batch_refine<<<grid, BE_T, (size_t)BE_NMAX * BE_B * sizeof(double), ctx->stream>>>(r);
   OFRR_LAUNCHED(ctx, "k_batch_refine");
   std::vector<double> hres((size_t)count * nev);
   std::vector<int> hit(2 * (size_t)count);

@@ -1096,8 +1096,10 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
     bool sign_ok = false;
     {
       WsScope inner(ctx);
+      TraceScope tsr(ctx, "rr.spmm");
       OFRR_TRY(csrmm_impl(ctx, &A->csr, 0, t, ta, tav, ncols, S.V, S.ldv, AVb, ld));
       nmv += ncols;
+      tsr.next(t == OFRR_F64 ? "rr.gram.f64" : "rr.gram.16bit");
       ctx->emulate_f64 = mixed && t == OFRR_F64;
       int rst = gemm_impl(ctx, 1, 0, t, t, ta, OFRR_F64, ncols, ncols, n, 1.0, S.V, S.ldv, S.V, S.ldv, 0.0, M, ncols);
       if (rst == OFRR_SUCCESS)
@@ -1108,6 +1110,7 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
         k_add_diag<<<(ncols + 255) / 256, 256, 0, ctx->stream>>>(ncols, M, ncols, opt->generalized_tol);
         OFRR_LAUNCHED(ctx, "k_add_diag");
       }
+      tsr.next(t == OFRR_F64 ? "rr.eig.f64" : "rr.eig.16bit");
       if (symmetric) OFRR_TRY(geig_fast(ctx, ncols, G, M, 0.0, d, U, t == OFRR_F64 ? 2 : 1));
       else OFRR_TRY(geig_nonsym(ctx, ncols, G, M, d, U, t == OFRR_F64, true));
       OFRR_CUDA(cudaMemcpyAsync(hd.data(), d, sizeof(double) * ncols, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1130,6 +1133,7 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
       OFRR_TRY(kry_spd_solve(ctx, ncols, M, G + (size_t)(ncols - 1) * ncols, xg));
       const double* Yc = U;
       double* Ys = Cf + (size_t)ncols * (k + pp + 1);
+      tsr.next("rr.sign");
       if (!symmetric && ncols <= 96 && pp < ncols) {
         const double sigma = 0.5 * (hd[pp - 1] + hd[pp]);
         const int ist = invariant_subspace_nonsym(ctx, ncols, G, M, sigma, pp, Ys);
@@ -1139,6 +1143,7 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
       }
       // Wb = V [U(:, :k), Yc, -M^-1 G(:, last)] (+ A v_last in the last column): the k Ritz vectors, then
       // the next block
+      tsr.next("rr.update");
       OFRR_TRY(kry_coef_matrix(ctx, ncols, k, U, pp, Yc, xg, Cf));
       tw = (t == OFRR_F64) ? OFRR_F64 : OFRR_F32;
       ctx->emulate_f64 = mixed && t == OFRR_F64;

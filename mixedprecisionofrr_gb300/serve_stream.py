@@ -38,18 +38,19 @@ class Request:
 
 
 def make_stream(seed: int, count: int, rate: float = 2000.0) -> list:
-    """The first `count` requests of the seeded stream."""
+    """The first `count` requests of the seeded stream (request i does not depend on count)."""
     rng = np.random.default_rng(seed)
-    t = np.cumsum(rng.exponential(1.0 / rate, count))
     out = []
+    t_now = 0.0
     for i in range(count):
+        t_now += float(rng.exponential(1.0 / rate))
         k = int(rng.integers(4, 65))
         tol = float(rng.choice([1e-6, 1e-8, 1e-10]))
         if rng.random() < 0.6:
             m = int(rng.integers(512, 16385))
             n = int(rng.integers(max(m // 8, 2 * k + 16), max(m // 4, 2 * k + 16) + 1))
             n = min(n, m)
-            out.append(Request(i, float(t[i]), "svd", m, n, min(k, n // 2), tol, seed=seed * 1000003 + i))
+            out.append(Request(i, t_now, "svd", m, n, min(k, n // 2), tol, seed=seed * 1000003 + i))
         else:
             dim = int(rng.choice([2, 3]))
             ntot = int(rng.integers(10_000, 1_000_001))
@@ -60,7 +61,7 @@ def make_stream(seed: int, count: int, rate: float = 2000.0) -> list:
                 N = max(int(round(ntot ** (1.0 / 3.0))), 8)
                 grid = (N, N + 1, N + 2)
             nn = int(np.prod(grid))
-            out.append(Request(i, float(t[i]), "lap", nn, nn, k, tol, dim=dim, grid=grid, seed=seed * 1000003 + i))
+            out.append(Request(i, t_now, "lap", nn, nn, k, tol, dim=dim, grid=grid, seed=seed * 1000003 + i))
     return out
 
 
