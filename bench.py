@@ -623,6 +623,8 @@ def c4_run(api, steps, warmup, cpu=True, count=None):
            "max_rel_eig_err": err, "iterations_mean": float(its.mean()), "iterations_max": int(its.max()),
            "per_matrix_latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
            "bytes_16bit_A": abytes,
+           "failed": [{"matrix": int(i), "n": int(ns[i]), "iterations": int(its[i]), "max_residual": float(res[i].max()),
+                       "status": int(sts[i])} for i in np.nonzero(sts != 0)[0][:20]],
            "dtype": "bf16 A / f32 accumulate, then f32 A; f64 refinement of the 8 leading pairs"}
     out["value"] = conv / float(ts.mean())
     if cpu:
@@ -802,6 +804,8 @@ def main():
         print(json.dumps(orth_compare_run(api, A)))
         return
     if args.profile_solve:
+        if args.mixed_config:
+            CFG["mixed"] = tuple(int(x) for x in args.mixed_config.split(","))
         run_solver(api, A, "mixed")
         torch.cuda.synchronize()
         U, s, V, info = run_solver(api, A, "mixed")
@@ -878,6 +882,11 @@ def main():
                 "achieved": bytes_s / dt_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
                 "frac": bytes_s / dt_s / 1e9 / hbm_peak, "traffic": profiled_traffic() if bb == 64 else None,
                 "algorithmic_bytes": bytes_s, "peak_source": src, "us_per_launch": dt_s * 1e6}
+        # the same launch against the FP64 operands it stands for (A 8 B per element instead of its 10 B digit
+        # stack, V and the FP64 result C once)
+        fp64_bytes = 8.0 * (M_ROWS * N_COLS + N_COLS * bb + M_ROWS * bb)
+        roof["frac_fp64_operand"] = fp64_bytes / dt_s / 1e9 / hbm_peak
+        roof["fp64_operand_bytes"] = fp64_bytes
         dt_g, bytes_g, flops_g = gemm_roofline(api)
         roof16 = {"kernel": f"k_gemm_tn: A.V 16-bit TN GEMM 8192x2048x{bb} (FP32 accumulate, incl. split-K reduce)",
                   "bound": "hbm", "achieved": bytes_g / dt_g / 1e9, "peak": hbm_peak, "unit": "GB/s",

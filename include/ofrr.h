@@ -359,7 +359,7 @@ int ofrr_rr_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, 
  * (CPP/linalg/solvers/eig/arnoldi_eig.hpp:25-28, arnoldi_eig.cu:10-18).
  * v0: n (dev, type p_output; FP64 in OFRR_MODE_MIXED / OFRR_MODE_FP64) start vector when
  * use_start_block; X: n x nev Ritz vectors out (FP64 in those modes).  With a CSR operator the
- * production modes use the thick restart of ofrr_options.restart_keep (kdim + 1 <= 129, nonsymmetric
+ * production modes use the thick restart of ofrr_options.restart_keep (kdim + 1 <= 128, nonsymmetric
  * operators kdim + 1 <= 96 for the invariant-subspace restart); maxiter is the budget of Krylov steps.
  * OFRR_MODE_MIXED: a 16-bit basis (p_output F16 or BF16) with the FP32 value copy of A and FP32
  * arithmetic until the residuals stop improving, then an FP64 phase (FP64 values; Gram and Ritz products

@@ -9,19 +9,20 @@
 // Design:
 //  * k_batch_si: a persistent grid (one 512-thread CTA per SM) pulls matrices from an atomic queue, the
 //    largest first.  A CTA keeps its matrix's block (n x b, b <= 16, FP32) and the product block in
-//    shared memory (row-major, 2 x 64 KB at n = 1024) and streams A from HBM for every product: phase 1
-//    reads a 16-bit copy of A (half the bytes), phase 2 (once the 16-bit residuals stop improving) the
-//    FP32 copy; products accumulate in FP32 on the CUDA cores (16 FMAs per element of A streamed, so the
-//    16-bit phase is bound by HBM, not by the FP32 pipe).  Rows are split over thread groups when n is
-//    small (each group a slice of k, partial sums added in a fixed order: results do not depend on the
-//    schedule).  The Gram matrices sum 64-row chunks in FP32 and the chunks in FP64; the 16 x 16 pencil
-//    is reduced by an FP64 Cholesky factor and solved by an FP32 Jacobi method.
-//  * k_batch_refine: FP32 arithmetic cannot certify residuals near 1e-7 (its own rounding is ~1e-7 of
-//    ||A||), so a second persistent pass takes each matrix's FP32 block (the nev wanted vectors and the
-//    guard columns) to FP64 accuracy: block steps of Rayleigh-Ritz on [X, A X - X diag(l)] with FP64
-//    products from the FP64 input until the FP64 residuals of the nev leading pairs meet tol (usually one
-//    or two steps; at most 8).
-// No spin waits: the queue is one atomic counter per kernel.
+//    shared memory (row-major, 2 x 64 KB at n = 1024) and streams A through a ring of bulk asynchronous
+//    copies for every product: phase 1 reads a 16-bit copy of A (half the bytes), phase 2 (once the
+//    16-bit residuals stop improving) the FP32 copy; products accumulate in FP32 on the CUDA cores (16
+//    FMAs per element of A streamed).  Rows are split over thread groups when n is small (each group a
+//    slice of k, partial sums added in a fixed order: results do not depend on the schedule).  The Gram
+//    matrices sum 64-row chunks in FP32 and the chunks in FP64; the 16 x 16 pencil is reduced by an FP64
+//    Cholesky factor and solved by an FP32 Jacobi method.
+//  * FP64 refinement (be_refine_one, same CTA, right after the matrix's FP32 phase, so a matrix's latency
+//    is its own work): FP32 arithmetic cannot certify residuals near 1e-7 (its own rounding is ~1e-7 of
+//    ||A||), so the CTA takes the FP32 block (the nev wanted vectors and the guard columns) to FP64
+//    accuracy: block steps of Rayleigh-Ritz on [X, A X - X diag(l)] with FP64 products from the FP64
+//    input until the FP64 residuals of the nev leading pairs meet tol (usually one step; at most 12).
+// Bounded waits only: the queue is one atomic counter; the copy ring's mbarrier waits give up after ~2 s
+// (status word, then the CTA leaves).
 #include "ofrr_internal.cuh"
 #include "tcgen05.cuh"
 
@@ -32,6 +33,25 @@ constexpr int BE_T = 512;      // threads per CTA
 constexpr int BE_B = 16;       // block width (columns)
 constexpr int BE_NMAX = 1024;  // largest matrix dimension held in shared memory
 constexpr int BE_NEV = 8;      // leading pairs certified by the refinement
+
+// ---- FP64 refinement of the nev leading Ritz pairs of every matrix ------------------------------------
+struct RefineDev {
+  const int64_t* n;
+  const int64_t* off;
+  const int* order;
+  const double* A64;
+  const float* X32;     // from k_batch_si (n x BE_B per matrix at xoff)
+  const int64_t* xoff;
+  const float* lam32;
+  double* X64;          // out: n x nev per matrix at xoff64
+  const int64_t* xoff64;
+  double* lam;          // out: count x nev
+  double* res;          // out: count x nev (FP64 residuals / max|l|)
+  double* scratch;      // per CTA: 3 x BE_NMAX x 2 BE_B doubles
+  unsigned long long* tend;  // count: global timer when the matrix's refinement finished
+  int count, nev, b, steps;
+  double tol;
+};
 
 struct BatchDev {
   const int64_t* n;        // count
@@ -48,6 +68,7 @@ struct BatchDev {
   unsigned long long* tstart;  // count: global timer when the matrix was taken from the queue
   unsigned int* queue;
   int* err;                // device status word of bounded waits
+  RefineDev rf;            // the FP64 refinement, run by the same CTA right after a matrix's FP32 phase
   int count, b, nev, step, maxit;
   float tol16, tol32;      // residual targets that end the 16-bit and the FP32 phase
   uint64_t seed;
@@ -370,6 +391,392 @@ __device__ void be_jacobi(float* S, float* U, float* w, float* cs, int* pq) {
   if (lane < BE_B) w[lane] = S[lane * BE_B + lane];
   __syncwarp();
 }
+
+
+constexpr int BR_K2 = 2 * BE_B;  // width of [X, R]
+
+// Y (n x k, ld n, global FP64) = A (n x n, column-major, FP64) X (n x k, ld n, global).  X is first copied
+// into shared memory row-major (Xs: n x BE_B doubles) so that its values are broadcast reads; A is read
+// once per column pass with coalesced loads.  GB300's FP64 pipe (about 1.7 FMA per clock per SM), not
+// HBM, bounds this product, so the layout keeps every thread busy: G groups split the columns of A,
+// each thread covers R <= 2 rows and 16 / R columns of X per pass; the groups' partial sums are added in
+// group order (results do not depend on timing).
+__device__ void br_matmul(int n, int k, const double* __restrict__ A, const double* X, double* Y, double* Xs) {
+  const int tid = threadIdx.x;
+  for (int e = tid; e < n * BE_B; e += BE_T) {
+    const int i = e / BE_B, c = e % BE_B;
+    Xs[e] = (c < k) ? X[i + (int64_t)c * n] : 0.0;
+  }
+  int G = 1, R = 2;
+  for (int r = 1; r <= 2; ++r)
+    for (int g = 1; g <= 16; ++g) {
+      const int tg = ((BE_T / g) / 32) * 32;
+      if (tg * r >= n && g * R > G * r) {
+        G = g;
+        R = r;
+      }
+    }
+  __syncthreads();
+  const int Tg = ((BE_T / G) / 32) * 32;
+  const int g = tid / Tg, t = tid % Tg;
+  const int CW = BE_B / R;
+  for (int c0 = 0; c0 < k; c0 += CW) {
+    double acc[2][BE_B];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < BE_B; ++c) acc[r][c] = 0.0;
+    if (g < G) {
+      const int i0 = t, i1 = t + Tg;
+      const bool v0 = i0 < n, v1 = (R == 2) && i1 < n;
+      if (R == 1) {
+        for (int kk = g; kk < n; kk += G) {
+          const double a0 = v0 ? __ldg(A + i0 + (int64_t)kk * n) : 0.0;
+          const double* xr = Xs + kk * BE_B;
+#pragma unroll
+          for (int c = 0; c < BE_B; ++c) acc[0][c] = fma(a0, xr[c], acc[0][c]);
+        }
+      } else {
+        for (int kk = g; kk < n; kk += G) {
+          const double a0 = v0 ? __ldg(A + i0 + (int64_t)kk * n) : 0.0;
+          const double a1 = v1 ? __ldg(A + i1 + (int64_t)kk * n) : 0.0;
+          const double* xr = Xs + kk * BE_B + c0;
+#pragma unroll
+          for (int c = 0; c < BE_B / 2; ++c) {
+            acc[0][c] = fma(a0, xr[c], acc[0][c]);
+            acc[1][c] = fma(a1, xr[c], acc[1][c]);
+          }
+        }
+      }
+    }
+    for (int gg = 0; gg < G; ++gg) {
+      if (g == gg) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const int i = t + r * Tg;
+          if (r >= R || i >= n) continue;
+#pragma unroll
+          for (int c = 0; c < BE_B; ++c) {
+            if (c >= CW || c0 + c >= k) continue;
+            double* y = Y + i + (int64_t)(c0 + c) * n;
+            *y = (gg == 0) ? acc[r][c] : *y + acc[r][c];
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__device__ double br_block_sum(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < BE_T / 32; ++w) t += red[w];
+  __syncthreads();
+  return t;
+}
+
+// Rayleigh-Ritz of the symmetric pencil (G, M) of k2 <= 32 unit columns on one warp in FP64 (lane l owns
+// row / column l): M + tiny I = L L' with columns whose part outside the span of the earlier ones is
+// below 1e-4 of their norm dropped (their row and column of the pencil removed), C = L^-1 sym(G) L^-T,
+// a parallel cyclic Jacobi method (round-robin pairs, every round rotating k2 / 2 disjoint pairs), and
+// the kb largest eigenvalues' vectors Z = L^-T U (k2 x kb, row-major, into Zout).  All arrays k2 x k2
+// row-major in shared memory; G becomes U, M becomes C.
+__device__ void br_rayleigh_ritz_warp(int k2, int kb, double* G, double* M, double* L, double* T, double* Zout,
+                                      double* cs, int* pq, int* s_idx) {
+  const int lane = threadIdx.x & 31;
+  __shared__ int s_drop[BR_K2];
+  double mx = 0.0;
+  for (int i = 0; i < k2; ++i) mx = fmax(mx, M[i * k2 + i]);
+  for (int e = lane; e < k2 * k2; e += 32) L[e] = 0.0;
+  __syncwarp();
+  for (int j = 0; j < k2; ++j) {
+    // row j of L left of the diagonal is final
+    double dj = M[j * k2 + j] + 1e-14 * mx;
+    for (int q = 0; q < j; ++q) dj -= L[j * k2 + q] * L[j * k2 + q];
+    const bool drop = !(dj > 1e-8 * M[j * k2 + j]);
+    if (lane == 0) s_drop[j] = drop ? 1 : 0;
+    if (drop) {
+      __syncwarp();
+      for (int q = lane; q < k2; q += 32) {
+        L[j * k2 + q] = (q == j) ? 1.0 : 0.0;
+        G[j * k2 + q] = 0.0;
+        G[q * k2 + j] = 0.0;
+      }
+      __syncwarp();
+      continue;
+    }
+    dj = sqrt(dj);
+    const int i = lane;
+    double lij = 0.0;
+    if (i > j && i < k2) {
+      double v = M[i * k2 + j];
+      for (int q = 0; q < j; ++q) v -= L[i * k2 + q] * L[j * k2 + q];
+      lij = v / dj;
+    }
+    __syncwarp();
+    if (i > j && i < k2) L[i * k2 + j] = lij;
+    if (lane == 0) L[j * k2 + j] = dj;
+    __syncwarp();
+  }
+  // T = L^-1 sym(G): lane c solves column c
+  for (int c = lane; c < k2; c += 32)
+    for (int i = 0; i < k2; ++i) {
+      double v = 0.5 * (G[i * k2 + c] + G[c * k2 + i]);
+      for (int q = 0; q < i; ++q) v -= L[i * k2 + q] * T[q * k2 + c];
+      T[i * k2 + c] = v / L[i * k2 + i];
+    }
+  __syncwarp();
+  // C = T L^-T: lane r solves row r (into M)
+  for (int r = lane; r < k2; r += 32)
+    for (int i = 0; i < k2; ++i) {
+      double v = T[r * k2 + i];
+      for (int q = 0; q < i; ++q) v -= L[i * k2 + q] * M[r * k2 + q];
+      M[r * k2 + i] = v / L[i * k2 + i];
+    }
+  __syncwarp();
+  double* Cm = M;
+  double* U = G;
+  for (int e = lane; e < k2 * k2; e += 32) {
+    const int i = e / k2, j = e % k2;
+    U[e] = (i == j) ? 1.0 : 0.0;
+    if (i < j) {
+      const double a = 0.5 * (Cm[i * k2 + j] + Cm[j * k2 + i]);
+      Cm[i * k2 + j] = a;
+      Cm[j * k2 + i] = a;
+    }
+  }
+  __syncwarp();
+  const int np = k2 / 2;
+  for (int sweep = 0; sweep < 20; ++sweep) {
+    double off = 0.0, dn = 0.0;
+    for (int e = lane; e < k2 * k2; e += 32) {
+      const double v = Cm[e] * Cm[e];
+      if (e / k2 != e % k2) off += v;
+      else dn += v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      dn += __shfl_xor_sync(0xffffffffu, dn, o);
+    }
+    if (off <= 1e-28 * dn) break;
+    for (int round = 0; round < k2 - 1; ++round) {
+      if (lane < np) {  // round-robin pairs: position 0 fixed, the others rotate
+        const int a = (lane == 0) ? 0 : 1 + (lane - 1 + round) % (k2 - 1);
+        const int b = 1 + (k2 - 2 - lane + round) % (k2 - 1);
+        const int p = min(a, b), q = max(a, b);
+        const double apq = Cm[p * k2 + q];
+        double c = 1.0, sn = 0.0;
+        if (fabs(apq) > 1e-300) {
+          const double theta = (Cm[q * k2 + q] - Cm[p * k2 + p]) / (2.0 * apq);
+          const double tt = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
+          c = 1.0 / sqrt(fma(tt, tt, 1.0));
+          sn = tt * c;
+        }
+        cs[2 * lane] = c;
+        cs[2 * lane + 1] = sn;
+        pq[2 * lane] = p;
+        pq[2 * lane + 1] = q;
+      }
+      __syncwarp();
+      if (lane < k2) {  // columns: C = C J, U = U J (row `lane`)
+        for (int m = 0; m < np; ++m) {
+          const int p = pq[2 * m], q = pq[2 * m + 1];
+          const double c = cs[2 * m], sn = cs[2 * m + 1];
+          const double sp = Cm[lane * k2 + p], sq = Cm[lane * k2 + q];
+          Cm[lane * k2 + p] = c * sp - sn * sq;
+          Cm[lane * k2 + q] = sn * sp + c * sq;
+          const double up = U[lane * k2 + p], uq = U[lane * k2 + q];
+          U[lane * k2 + p] = c * up - sn * uq;
+          U[lane * k2 + q] = sn * up + c * uq;
+        }
+      }
+      __syncwarp();
+      if (lane < k2) {  // rows: C = J' C (column `lane`)
+        for (int m = 0; m < np; ++m) {
+          const int p = pq[2 * m], q = pq[2 * m + 1];
+          const double c = cs[2 * m], sn = cs[2 * m + 1];
+          const double sp = Cm[p * k2 + lane], sq = Cm[q * k2 + lane];
+          Cm[p * k2 + lane] = c * sp - sn * sq;
+          Cm[q * k2 + lane] = sn * sp + c * sq;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // the kb largest eigenvalues among the kept directions (a dropped index keeps U = e_j, C_jj = 0)
+  if (lane == 0) {
+    int nk = 0;
+    for (int i = 0; i < k2; ++i)
+      if (!s_drop[i]) s_idx[nk++] = i;
+    for (int i = 1; i < nk; ++i) {
+      const int v = s_idx[i];
+      int j = i - 1;
+      while (j >= 0 && Cm[s_idx[j] * k2 + s_idx[j]] < Cm[v * k2 + v]) {
+        s_idx[j + 1] = s_idx[j];
+        --j;
+      }
+      s_idx[j + 1] = v;
+    }
+    for (int i = nk; i < k2; ++i) s_idx[i] = s_idx[nk > 0 ? nk - 1 : 0];
+  }
+  __syncwarp();
+  // Z = L^-T U(:, idx): lane c solves column c (into T, then Zout)
+  for (int c = lane; c < kb; c += 32) {
+    const int src = s_idx[c];
+    for (int i = k2 - 1; i >= 0; --i) {
+      double v = U[i * k2 + src];
+      for (int q = i + 1; q < k2; ++q) v -= L[q * k2 + i] * T[q * k2 + c];
+      T[i * k2 + c] = v / L[i * k2 + i];
+    }
+  }
+  __syncwarp();
+  for (int e = lane; e < k2 * kb; e += 32) Zout[e] = T[(e / kb) * k2 + (e % kb)];
+  __syncwarp();
+}
+
+// The whole FP32 block (b columns, the nev wanted plus guard vectors) is refined: block steps of
+// Rayleigh-Ritz on [X, A X - X diag(l)] with FP64 products from the FP64 input, until the FP64 residuals of
+// the nev leading pairs meet tol (or `steps` steps).  The guard columns keep the nearby part of the
+// spectrum inside the search space, so each step removes the error along it instead of only damping it.
+// One matrix (index mi, order n) from its FP32 block in d.X32.  Xs: BE_NMAX x BE_B doubles of shared memory
+// (the right-hand block of a product); arena: 4 BR_K2^2 + BR_K2 BE_B doubles of shared memory (the pencil).
+__device__ void be_refine_one(const RefineDev& d, int mi, int n, double* Xs, double* arena) {
+  __shared__ double s_red[BE_T / 32];
+  __shared__ double s_lam[2 * BE_B];
+  __shared__ double s_cs[BR_K2];
+  __shared__ int s_pq[BR_K2], s_idx[BR_K2];
+  double* s_G = arena;
+  double* s_M = s_G + BR_K2 * BR_K2;
+  double* s_L = s_M + BR_K2 * BR_K2;
+  double* s_T = s_L + BR_K2 * BR_K2;
+  double* s_Z = s_T + BR_K2 * BR_K2;
+  double* br_sm = Xs;
+  const int tid = threadIdx.x;
+  const int kb = d.b, k2 = 2 * d.b, nev = d.nev;
+  double* Sx = d.scratch + (size_t)blockIdx.x * 3 * BE_NMAX * BR_K2;  // [X | R] (n x 2 kb)
+  double* Sa = Sx + (size_t)BE_NMAX * BR_K2;                          // A [X | R]
+  double* Sy = Sa + (size_t)BE_NMAX * BR_K2;                          // new X, A X
+  {
+    const double* A = d.A64 + d.off[mi];
+    const float* X32 = d.X32 + d.xoff[mi];
+    for (int e = tid; e < n * kb; e += BE_T) Sx[e] = (double)X32[e];
+    __syncthreads();
+    br_matmul(n, kb, A, Sx, Sa, br_sm);
+    for (int step = 0;; ++step) {
+      // Rayleigh quotients and residuals R = A X - X diag(l) (into columns kb .. 2kb-1 of Sx)
+      for (int c = 0; c < kb; ++c) {
+        double xax = 0.0, xx = 0.0;
+        for (int i = tid; i < n; i += BE_T) {
+          xax = fma(Sx[i + c * n], Sa[i + c * n], xax);
+          xx = fma(Sx[i + c * n], Sx[i + c * n], xx);
+        }
+        xax = br_block_sum(xax, s_red);
+        xx = br_block_sum(xx, s_red);
+        if (tid == 0) s_lam[c] = (xx > 0.0) ? xax / xx : 0.0;
+        if (tid == 0) s_lam[kb + c] = xx;
+        __syncthreads();
+      }
+      double lmax = 0.0;
+      for (int c = 0; c < nev; ++c) lmax = fmax(lmax, fabs(s_lam[c]));
+      if (lmax == 0.0) lmax = 1.0;
+      double maxres = 0.0;
+      for (int c = 0; c < kb; ++c) {
+        double rr = 0.0;
+        for (int i = tid; i < n; i += BE_T) {
+          const double r = Sa[i + c * n] - s_lam[c] * Sx[i + c * n];
+          Sx[i + (c + kb) * n] = r;
+          rr = fma(r, r, rr);
+        }
+        rr = br_block_sum(rr, s_red);
+        if (c < nev) {
+          const double res = (s_lam[kb + c] > 0.0) ? sqrt(rr / s_lam[kb + c]) / lmax : INFINITY;
+          if (tid == 0) d.res[(int64_t)mi * nev + c] = res;
+          maxres = fmax(maxres, res);
+        }
+        // unit columns for the block step: X (and A X) and the residual direction (the span is unchanged,
+        // and the Gram matrix of [X, R] stays well scaled however small the residuals are)
+        const double sx = (s_lam[kb + c] > 0.0) ? 1.0 / sqrt(s_lam[kb + c]) : 0.0;
+        const double sr = (rr > 0.0) ? 1.0 / sqrt(rr) : 0.0;
+        for (int i = tid; i < n; i += BE_T) {
+          Sx[i + c * n] *= sx;
+          Sa[i + c * n] *= sx;
+          Sx[i + (c + kb) * n] *= sr;
+        }
+      }
+      __syncthreads();
+      if (step >= d.steps || maxres <= d.tol) {
+        if (tid < kb) s_lam[kb + tid] = 1.0;  // the columns are unit now
+        __syncthreads();
+        break;
+      }
+      // block step: Rayleigh-Ritz on [X, R] (FP64 products)
+      br_matmul(n, kb, A, Sx + (size_t)kb * n, Sa + (size_t)kb * n, br_sm);
+      {
+        // G = S' A S and M = S' S (both symmetric: the upper triangles, mirrored), one warp per entry
+        const int lane = tid & 31, wid = tid >> 5;
+        const int ntri = k2 * (k2 + 1) / 2;
+        for (int e = wid; e < 2 * ntri; e += BE_T / 32) {
+          const int which = e / ntri;
+          int pr = e % ntri, r = 0;
+          while (pr >= k2 - r) {
+            pr -= k2 - r;
+            ++r;
+          }
+          const int c = r + pr;
+          const double* Bc = which ? Sx : Sa;
+          double acc = 0.0;
+          for (int i = lane; i < n; i += 32) acc = fma(Sx[i + r * n], Bc[i + c * n], acc);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+          if (lane == 0) {
+            double* D = which ? s_M : s_G;
+            D[r * k2 + c] = acc;
+            D[c * k2 + r] = acc;
+          }
+        }
+      }
+      __syncthreads();
+      if (tid < 32) br_rayleigh_ritz_warp(k2, kb, s_G, s_M, s_L, s_T, s_Z, s_cs, s_pq, s_idx);
+      __syncthreads();
+      // X <- [X R] Z, A X <- [AX AR] Z
+      for (int e = tid; e < 2 * n; e += BE_T) {
+        const int i = e % n, which = e / n;
+        const double* src = which ? Sa : Sx;
+        double vr[BR_K2];
+#pragma unroll
+        for (int r = 0; r < BR_K2; ++r) vr[r] = (r < k2) ? src[i + r * n] : 0.0;
+        for (int c = 0; c < kb; ++c) {
+          double x = 0.0;
+#pragma unroll
+          for (int r = 0; r < BR_K2; ++r)
+            if (r < k2) x = fma(vr[r], s_Z[r * kb + c], x);
+          Sy[i + (c + which * kb) * n] = x;
+        }
+      }
+      __syncthreads();
+      for (int e = tid; e < n * kb; e += BE_T) {
+        Sx[e] = Sy[e];
+        Sa[e] = Sy[e + (size_t)kb * n];
+      }
+      __syncthreads();
+    }
+    // outputs: unit-norm FP64 Ritz vectors of the nev leading pairs, their Rayleigh quotients
+    double* Xo = d.X64 + d.xoff64[mi];
+    for (int c = 0; c < nev; ++c) {
+      const double inv = 1.0 / sqrt(fmax(s_lam[kb + c], 1e-300));
+      for (int i = tid; i < n; i += BE_T) Xo[i + (int64_t)c * n] = Sx[i + c * n] * inv;
+      if (tid == 0) d.lam[(int64_t)mi * nev + c] = s_lam[c];
+    }
+    __syncthreads();
+    if (tid == 0) d.tend[mi] = tc_globaltimer();
+  }
+}
+
 
 template <class T16>
 __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
@@ -714,413 +1121,12 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
       d.phase2[mi] = p2;
     }
     __syncthreads();
-  }
-}
-
-// ---- FP64 refinement of the nev leading Ritz pairs of every matrix ------------------------------------
-struct RefineDev {
-  const int64_t* n;
-  const int64_t* off;
-  const int* order;
-  const double* A64;
-  const float* X32;     // from k_batch_si (n x BE_B per matrix at xoff)
-  const int64_t* xoff;
-  const float* lam32;
-  double* X64;          // out: n x nev per matrix at xoff64
-  const int64_t* xoff64;
-  double* lam;          // out: count x nev
-  double* res;          // out: count x nev (FP64 residuals / max|l|)
-  double* scratch;      // per CTA: 3 x BE_NMAX x 2 BE_B doubles
-  unsigned long long* tend;  // count: global timer when the matrix's refinement finished
-  unsigned int* queue;
-  int count, nev, b, steps;
-  double tol;
-};
-
-constexpr int BR_K2 = 2 * BE_B;  // width of [X, R]
-
-// Y (n x k, ld n, global FP64) = A (n x n, column-major, FP64) X (n x k, ld n, global).  X is first copied
-// into shared memory row-major (Xs: n x BE_B doubles) so that its values are broadcast reads; A is read
-// once per column pass with coalesced loads.  GB300's FP64 pipe (about 1.7 FMA per clock per SM), not
-// HBM, bounds this product, so the layout keeps every thread busy: G groups split the columns of A,
-// each thread covers R <= 2 rows and 16 / R columns of X per pass; the groups' partial sums are added in
-// group order (results do not depend on timing).
-__device__ void br_matmul(int n, int k, const double* __restrict__ A, const double* X, double* Y, double* Xs) {
-  const int tid = threadIdx.x;
-  for (int e = tid; e < n * BE_B; e += BE_T) {
-    const int i = e / BE_B, c = e % BE_B;
-    Xs[e] = (c < k) ? X[i + (int64_t)c * n] : 0.0;
-  }
-  int G = 1, R = 2;
-  for (int r = 1; r <= 2; ++r)
-    for (int g = 1; g <= 16; ++g) {
-      const int tg = ((BE_T / g) / 32) * 32;
-      if (tg * r >= n && g * R > G * r) {
-        G = g;
-        R = r;
-      }
-    }
-  __syncthreads();
-  const int Tg = ((BE_T / G) / 32) * 32;
-  const int g = tid / Tg, t = tid % Tg;
-  const int CW = BE_B / R;
-  for (int c0 = 0; c0 < k; c0 += CW) {
-    double acc[2][BE_B];
-#pragma unroll
-    for (int r = 0; r < 2; ++r)
-#pragma unroll
-      for (int c = 0; c < BE_B; ++c) acc[r][c] = 0.0;
-    if (g < G) {
-      const int i0 = t, i1 = t + Tg;
-      const bool v0 = i0 < n, v1 = (R == 2) && i1 < n;
-      if (R == 1) {
-        for (int kk = g; kk < n; kk += G) {
-          const double a0 = v0 ? __ldg(A + i0 + (int64_t)kk * n) : 0.0;
-          const double* xr = Xs + kk * BE_B;
-#pragma unroll
-          for (int c = 0; c < BE_B; ++c) acc[0][c] = fma(a0, xr[c], acc[0][c]);
-        }
-      } else {
-        for (int kk = g; kk < n; kk += G) {
-          const double a0 = v0 ? __ldg(A + i0 + (int64_t)kk * n) : 0.0;
-          const double a1 = v1 ? __ldg(A + i1 + (int64_t)kk * n) : 0.0;
-          const double* xr = Xs + kk * BE_B + c0;
-#pragma unroll
-          for (int c = 0; c < BE_B / 2; ++c) {
-            acc[0][c] = fma(a0, xr[c], acc[0][c]);
-            acc[1][c] = fma(a1, xr[c], acc[1][c]);
-          }
-        }
-      }
-    }
-    for (int gg = 0; gg < G; ++gg) {
-      if (g == gg) {
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-          const int i = t + r * Tg;
-          if (r >= R || i >= n) continue;
-#pragma unroll
-          for (int c = 0; c < BE_B; ++c) {
-            if (c >= CW || c0 + c >= k) continue;
-            double* y = Y + i + (int64_t)(c0 + c) * n;
-            *y = (gg == 0) ? acc[r][c] : *y + acc[r][c];
-          }
-        }
-      }
-      __syncthreads();
-    }
-  }
-}
-
-__device__ double br_block_sum(double v, double* red) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double t = 0.0;
-  for (int w = 0; w < BE_T / 32; ++w) t += red[w];
-  __syncthreads();
-  return t;
-}
-
-// Rayleigh-Ritz of the symmetric pencil (G, M) of k2 <= 32 unit columns on one warp in FP64 (lane l owns
-// row / column l): M + tiny I = L L' with columns whose part outside the span of the earlier ones is
-// below 1e-4 of their norm dropped (their row and column of the pencil removed), C = L^-1 sym(G) L^-T,
-// a parallel cyclic Jacobi method (round-robin pairs, every round rotating k2 / 2 disjoint pairs), and
-// the kb largest eigenvalues' vectors Z = L^-T U (k2 x kb, row-major, into Zout).  All arrays k2 x k2
-// row-major in shared memory; G becomes U, M becomes C.
-__device__ void br_rayleigh_ritz_warp(int k2, int kb, double* G, double* M, double* L, double* T, double* Zout,
-                                      double* cs, int* pq, int* s_idx) {
-  const int lane = threadIdx.x & 31;
-  __shared__ int s_drop[BR_K2];
-  double mx = 0.0;
-  for (int i = 0; i < k2; ++i) mx = fmax(mx, M[i * k2 + i]);
-  for (int e = lane; e < k2 * k2; e += 32) L[e] = 0.0;
-  __syncwarp();
-  for (int j = 0; j < k2; ++j) {
-    // row j of L left of the diagonal is final
-    double dj = M[j * k2 + j] + 1e-14 * mx;
-    for (int q = 0; q < j; ++q) dj -= L[j * k2 + q] * L[j * k2 + q];
-    const bool drop = !(dj > 1e-8 * M[j * k2 + j]);
-    if (lane == 0) s_drop[j] = drop ? 1 : 0;
-    if (drop) {
-      __syncwarp();
-      for (int q = lane; q < k2; q += 32) {
-        L[j * k2 + q] = (q == j) ? 1.0 : 0.0;
-        G[j * k2 + q] = 0.0;
-        G[q * k2 + j] = 0.0;
-      }
-      __syncwarp();
-      continue;
-    }
-    dj = sqrt(dj);
-    const int i = lane;
-    double lij = 0.0;
-    if (i > j && i < k2) {
-      double v = M[i * k2 + j];
-      for (int q = 0; q < j; ++q) v -= L[i * k2 + q] * L[j * k2 + q];
-      lij = v / dj;
-    }
-    __syncwarp();
-    if (i > j && i < k2) L[i * k2 + j] = lij;
-    if (lane == 0) L[j * k2 + j] = dj;
-    __syncwarp();
-  }
-  // T = L^-1 sym(G): lane c solves column c
-  for (int c = lane; c < k2; c += 32)
-    for (int i = 0; i < k2; ++i) {
-      double v = 0.5 * (G[i * k2 + c] + G[c * k2 + i]);
-      for (int q = 0; q < i; ++q) v -= L[i * k2 + q] * T[q * k2 + c];
-      T[i * k2 + c] = v / L[i * k2 + i];
-    }
-  __syncwarp();
-  // C = T L^-T: lane r solves row r (into M)
-  for (int r = lane; r < k2; r += 32)
-    for (int i = 0; i < k2; ++i) {
-      double v = T[r * k2 + i];
-      for (int q = 0; q < i; ++q) v -= L[i * k2 + q] * M[r * k2 + q];
-      M[r * k2 + i] = v / L[i * k2 + i];
-    }
-  __syncwarp();
-  double* Cm = M;
-  double* U = G;
-  for (int e = lane; e < k2 * k2; e += 32) {
-    const int i = e / k2, j = e % k2;
-    U[e] = (i == j) ? 1.0 : 0.0;
-    if (i < j) {
-      const double a = 0.5 * (Cm[i * k2 + j] + Cm[j * k2 + i]);
-      Cm[i * k2 + j] = a;
-      Cm[j * k2 + i] = a;
-    }
-  }
-  __syncwarp();
-  const int np = k2 / 2;
-  for (int sweep = 0; sweep < 20; ++sweep) {
-    double off = 0.0, dn = 0.0;
-    for (int e = lane; e < k2 * k2; e += 32) {
-      const double v = Cm[e] * Cm[e];
-      if (e / k2 != e % k2) off += v;
-      else dn += v;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      off += __shfl_xor_sync(0xffffffffu, off, o);
-      dn += __shfl_xor_sync(0xffffffffu, dn, o);
-    }
-    if (off <= 1e-28 * dn) break;
-    for (int round = 0; round < k2 - 1; ++round) {
-      if (lane < np) {  // round-robin pairs: position 0 fixed, the others rotate
-        const int a = (lane == 0) ? 0 : 1 + (lane - 1 + round) % (k2 - 1);
-        const int b = 1 + (k2 - 2 - lane + round) % (k2 - 1);
-        const int p = min(a, b), q = max(a, b);
-        const double apq = Cm[p * k2 + q];
-        double c = 1.0, sn = 0.0;
-        if (fabs(apq) > 1e-300) {
-          const double theta = (Cm[q * k2 + q] - Cm[p * k2 + p]) / (2.0 * apq);
-          const double tt = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
-          c = 1.0 / sqrt(fma(tt, tt, 1.0));
-          sn = tt * c;
-        }
-        cs[2 * lane] = c;
-        cs[2 * lane + 1] = sn;
-        pq[2 * lane] = p;
-        pq[2 * lane + 1] = q;
-      }
-      __syncwarp();
-      if (lane < k2) {  // columns: C = C J, U = U J (row `lane`)
-        for (int m = 0; m < np; ++m) {
-          const int p = pq[2 * m], q = pq[2 * m + 1];
-          const double c = cs[2 * m], sn = cs[2 * m + 1];
-          const double sp = Cm[lane * k2 + p], sq = Cm[lane * k2 + q];
-          Cm[lane * k2 + p] = c * sp - sn * sq;
-          Cm[lane * k2 + q] = sn * sp + c * sq;
-          const double up = U[lane * k2 + p], uq = U[lane * k2 + q];
-          U[lane * k2 + p] = c * up - sn * uq;
-          U[lane * k2 + q] = sn * up + c * uq;
-        }
-      }
-      __syncwarp();
-      if (lane < k2) {  // rows: C = J' C (column `lane`)
-        for (int m = 0; m < np; ++m) {
-          const int p = pq[2 * m], q = pq[2 * m + 1];
-          const double c = cs[2 * m], sn = cs[2 * m + 1];
-          const double sp = Cm[p * k2 + lane], sq = Cm[q * k2 + lane];
-          Cm[p * k2 + lane] = c * sp - sn * sq;
-          Cm[q * k2 + lane] = sn * sp + c * sq;
-        }
-      }
-      __syncwarp();
-    }
-  }
-  // the kb largest eigenvalues among the kept directions (a dropped index keeps U = e_j, C_jj = 0)
-  if (lane == 0) {
-    int nk = 0;
-    for (int i = 0; i < k2; ++i)
-      if (!s_drop[i]) s_idx[nk++] = i;
-    for (int i = 1; i < nk; ++i) {
-      const int v = s_idx[i];
-      int j = i - 1;
-      while (j >= 0 && Cm[s_idx[j] * k2 + s_idx[j]] < Cm[v * k2 + v]) {
-        s_idx[j + 1] = s_idx[j];
-        --j;
-      }
-      s_idx[j + 1] = v;
-    }
-    for (int i = nk; i < k2; ++i) s_idx[i] = s_idx[nk > 0 ? nk - 1 : 0];
-  }
-  __syncwarp();
-  // Z = L^-T U(:, idx): lane c solves column c (into T, then Zout)
-  for (int c = lane; c < kb; c += 32) {
-    const int src = s_idx[c];
-    for (int i = k2 - 1; i >= 0; --i) {
-      double v = U[i * k2 + src];
-      for (int q = i + 1; q < k2; ++q) v -= L[q * k2 + i] * T[q * k2 + c];
-      T[i * k2 + c] = v / L[i * k2 + i];
-    }
-  }
-  __syncwarp();
-  for (int e = lane; e < k2 * kb; e += 32) Zout[e] = T[(e / kb) * k2 + (e % kb)];
-  __syncwarp();
-}
-
-// The whole FP32 block (b columns, the nev wanted plus guard vectors) is refined: block steps of
-// Rayleigh-Ritz on [X, A X - X diag(l)] with FP64 products from the FP64 input, until the FP64 residuals of
-// the nev leading pairs meet tol (or `steps` steps).  The guard columns keep the nearby part of the
-// spectrum inside the search space, so each step removes the error along it instead of only damping it.
-__global__ void __launch_bounds__(BE_T, 1) k_batch_refine(RefineDev d) {
-  extern __shared__ __align__(16) double br_sm[];  // BE_NMAX x BE_B: the right-hand block of a product
-  __shared__ double s_red[BE_T / 32];
-  __shared__ double s_G[BR_K2 * BR_K2], s_M[BR_K2 * BR_K2], s_L[BR_K2 * BR_K2], s_T[BR_K2 * BR_K2];
-  __shared__ double s_Z[BR_K2 * BE_B];
-  __shared__ double s_lam[2 * BE_B];
-  __shared__ double s_cs[BR_K2];
-  __shared__ int s_pq[BR_K2], s_idx[BR_K2];
-  __shared__ int s_job;
-  const int tid = threadIdx.x;
-  const int kb = d.b, k2 = 2 * d.b, nev = d.nev;
-  double* Sx = d.scratch + (size_t)blockIdx.x * 3 * BE_NMAX * BR_K2;  // [X | R] (n x 2 kb)
-  double* Sa = Sx + (size_t)BE_NMAX * BR_K2;                          // A [X | R]
-  double* Sy = Sa + (size_t)BE_NMAX * BR_K2;                          // new X, A X
-  while (true) {
-    if (tid == 0) s_job = (int)atomicAdd(d.queue, 1u);
+    // ---- FP64 refinement of this matrix by the same CTA: the product block in the V / W area, the
+    //      pencil in the ring (no copy is in flight between products) ----
+    be_refine_one(d.rf, mi, n, reinterpret_cast<double*>(be_sm), reinterpret_cast<double*>(ring));
+    // the ring was written through the generic proxy: order that before the next bulk copies into it
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    const int job = s_job;
-    __syncthreads();
-    if (job >= d.count) return;
-    const int mi = d.order[job];
-    const int n = (int)d.n[mi];
-    const double* A = d.A64 + d.off[mi];
-    const float* X32 = d.X32 + d.xoff[mi];
-    for (int e = tid; e < n * kb; e += BE_T) Sx[e] = (double)X32[e];
-    __syncthreads();
-    br_matmul(n, kb, A, Sx, Sa, br_sm);
-    for (int step = 0;; ++step) {
-      // Rayleigh quotients and residuals R = A X - X diag(l) (into columns kb .. 2kb-1 of Sx)
-      for (int c = 0; c < kb; ++c) {
-        double xax = 0.0, xx = 0.0;
-        for (int i = tid; i < n; i += BE_T) {
-          xax = fma(Sx[i + c * n], Sa[i + c * n], xax);
-          xx = fma(Sx[i + c * n], Sx[i + c * n], xx);
-        }
-        xax = br_block_sum(xax, s_red);
-        xx = br_block_sum(xx, s_red);
-        if (tid == 0) s_lam[c] = (xx > 0.0) ? xax / xx : 0.0;
-        if (tid == 0) s_lam[kb + c] = xx;
-        __syncthreads();
-      }
-      double lmax = 0.0;
-      for (int c = 0; c < nev; ++c) lmax = fmax(lmax, fabs(s_lam[c]));
-      if (lmax == 0.0) lmax = 1.0;
-      double maxres = 0.0;
-      for (int c = 0; c < kb; ++c) {
-        double rr = 0.0;
-        for (int i = tid; i < n; i += BE_T) {
-          const double r = Sa[i + c * n] - s_lam[c] * Sx[i + c * n];
-          Sx[i + (c + kb) * n] = r;
-          rr = fma(r, r, rr);
-        }
-        rr = br_block_sum(rr, s_red);
-        if (c < nev) {
-          const double res = (s_lam[kb + c] > 0.0) ? sqrt(rr / s_lam[kb + c]) / lmax : INFINITY;
-          if (tid == 0) d.res[(int64_t)mi * nev + c] = res;
-          maxres = fmax(maxres, res);
-        }
-        // unit columns for the block step: X (and A X) and the residual direction (the span is unchanged,
-        // and the Gram matrix of [X, R] stays well scaled however small the residuals are)
-        const double sx = (s_lam[kb + c] > 0.0) ? 1.0 / sqrt(s_lam[kb + c]) : 0.0;
-        const double sr = (rr > 0.0) ? 1.0 / sqrt(rr) : 0.0;
-        for (int i = tid; i < n; i += BE_T) {
-          Sx[i + c * n] *= sx;
-          Sa[i + c * n] *= sx;
-          Sx[i + (c + kb) * n] *= sr;
-        }
-      }
-      __syncthreads();
-      if (step >= d.steps || maxres <= d.tol) {
-        if (tid < kb) s_lam[kb + tid] = 1.0;  // the columns are unit now
-        __syncthreads();
-        break;
-      }
-      // block step: Rayleigh-Ritz on [X, R] (FP64 products)
-      br_matmul(n, kb, A, Sx + (size_t)kb * n, Sa + (size_t)kb * n, br_sm);
-      {
-        // G = S' A S and M = S' S (both symmetric: the upper triangles, mirrored), one warp per entry
-        const int lane = tid & 31, wid = tid >> 5;
-        const int ntri = k2 * (k2 + 1) / 2;
-        for (int e = wid; e < 2 * ntri; e += BE_T / 32) {
-          const int which = e / ntri;
-          int pr = e % ntri, r = 0;
-          while (pr >= k2 - r) {
-            pr -= k2 - r;
-            ++r;
-          }
-          const int c = r + pr;
-          const double* Bc = which ? Sx : Sa;
-          double acc = 0.0;
-          for (int i = lane; i < n; i += 32) acc = fma(Sx[i + r * n], Bc[i + c * n], acc);
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-          if (lane == 0) {
-            double* D = which ? s_M : s_G;
-            D[r * k2 + c] = acc;
-            D[c * k2 + r] = acc;
-          }
-        }
-      }
-      __syncthreads();
-      if (tid < 32) br_rayleigh_ritz_warp(k2, kb, s_G, s_M, s_L, s_T, s_Z, s_cs, s_pq, s_idx);
-      __syncthreads();
-      // X <- [X R] Z, A X <- [AX AR] Z
-      for (int e = tid; e < 2 * n; e += BE_T) {
-        const int i = e % n, which = e / n;
-        const double* src = which ? Sa : Sx;
-        double vr[BR_K2];
-#pragma unroll
-        for (int r = 0; r < BR_K2; ++r) vr[r] = (r < k2) ? src[i + r * n] : 0.0;
-        for (int c = 0; c < kb; ++c) {
-          double x = 0.0;
-#pragma unroll
-          for (int r = 0; r < BR_K2; ++r)
-            if (r < k2) x = fma(vr[r], s_Z[r * kb + c], x);
-          Sy[i + (c + which * kb) * n] = x;
-        }
-      }
-      __syncthreads();
-      for (int e = tid; e < n * kb; e += BE_T) {
-        Sx[e] = Sy[e];
-        Sa[e] = Sy[e + (size_t)kb * n];
-      }
-      __syncthreads();
-    }
-    // outputs: unit-norm FP64 Ritz vectors of the nev leading pairs, their Rayleigh quotients
-    double* Xo = d.X64 + d.xoff64[mi];
-    for (int c = 0; c < nev; ++c) {
-      const double inv = 1.0 / sqrt(fmax(s_lam[kb + c], 1e-300));
-      for (int i = tid; i < n; i += BE_T) Xo[i + (int64_t)c * n] = Sx[i + c * n] * inv;
-      if (tid == 0) d.lam[(int64_t)mi * nev + c] = s_lam[c];
-    }
-    __syncthreads();
-    if (tid == 0) d.tend[mi] = tc_globaltimer();
   }
 }
 
@@ -1234,15 +1240,6 @@ static int batch_sym_eig_impl(ofrr_ctx* ctx, int count, const int64_t* n_host, c
   d.tol16 = (t16 == OFRR_F16) ? 2e-3f : 1e-2f;
   d.tol32 = (float)std::max(opt->tol, 1e-7);
   d.seed = opt->seed;
-  const size_t smem = (size_t)2 * BE_NMAX * BE_B * sizeof(float) + (size_t)BE_NS * BE_STAGE;
-  if (t16 == OFRR_F16) {
-    OFRR_TRY(allow_smem(k_batch_si<__half>));
-    k_batch_si<__half><<<grid, BE_T, smem, ctx->stream>>>(d);
-  } else {
-    OFRR_TRY(allow_smem(k_batch_si<__nv_bfloat16>));
-    k_batch_si<__nv_bfloat16><<<grid, BE_T, smem, ctx->stream>>>(d);
-  }
-  OFRR_LAUNCHED(ctx, "k_batch_si");
   RefineDev r{};
   r.n = dn;
   r.off = doff;
@@ -1257,15 +1254,21 @@ static int batch_sym_eig_impl(ofrr_ctx* ctx, int count, const int64_t* n_host, c
   r.res = dres;
   r.scratch = scratch;
   r.tend = times + count;
-  r.queue = queues + 1;
   r.count = count;
   r.nev = nev;
   r.b = b;
-  r.steps = 8;
+  r.steps = 12;
   r.tol = opt->tol > 0 ? opt->tol : 1e-7;
-  OFRR_TRY(allow_smem(k_batch_refine));
-  k_batch_refine<<<grid, BE_T, (size_t)BE_NMAX * BE_B * sizeof(double), ctx->stream>>>(r);
-  OFRR_LAUNCHED(ctx, "k_batch_refine");
+  d.rf = r;
+  const size_t smem = (size_t)2 * BE_NMAX * BE_B * sizeof(float) + (size_t)BE_NS * BE_STAGE;
+  if (t16 == OFRR_F16) {
+    OFRR_TRY(allow_smem(k_batch_si<__half>));
+    k_batch_si<__half><<<grid, BE_T, smem, ctx->stream>>>(d);
+  } else {
+    OFRR_TRY(allow_smem(k_batch_si<__nv_bfloat16>));
+    k_batch_si<__nv_bfloat16><<<grid, BE_T, smem, ctx->stream>>>(d);
+  }
+  OFRR_LAUNCHED(ctx, "k_batch_si");
   std::vector<double> hres((size_t)count * nev);
   std::vector<int> hit(2 * (size_t)count);
   OFRR_CUDA(cudaMemcpyAsync(evals, dlam, sizeof(double) * count * nev, cudaMemcpyDeviceToHost, ctx->stream));

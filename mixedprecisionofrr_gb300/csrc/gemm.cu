@@ -32,6 +32,133 @@ __global__ void k_add_f64(int64_t m, int64_t n, const double* __restrict__ T, in
   OFRR_FOR_2D(i, j, m, n) C[i + j * ldc] += T[i + j * ldt];
 }
 
+// ---- FP64 Gram products on the CUDA cores ------------------------------------------------------------
+// C (M x N) = A' B for FP64 A (K x M), B (K x N), M, N <= 128: the Gram and cross-Gram matrices of a
+// Rayleigh-Ritz step.  The exact-slice emulation's element error (2^-35 of |A|'|B|) is amplified by the
+// condition number of a non-orthogonal basis (10^3 .. 10^4 for power-iterated Hessenberg bases), which
+// capped the Ritz values near 1e-9 relative; these products are small (K M N FMAs), so they run in FP64.
+// One CTA per K chunk: 32-row slabs of both operands staged in shared memory, a 64 x 64 output tile per
+// pass (4 x 4 per thread of a 16 x 16 grid), the chunk's partial written out; k_gram_sum adds the
+// partials in chunk order (results do not depend on the schedule).
+constexpr int kGramSlab = 32;
+
+__global__ void __launch_bounds__(256) k_gram_f64(int64_t K, int M, int N, const double* __restrict__ A, int64_t lda,
+                                                  const double* __restrict__ B, int64_t ldb, int64_t kc,
+                                                  double* __restrict__ partial) {
+  __shared__ double sA[kGramSlab][65], sB[kGramSlab][65];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t k0 = (int64_t)blockIdx.x * kc, k1 = min(K, k0 + kc);
+  double* P = partial + (size_t)blockIdx.x * M * N;
+  for (int m0 = 0; m0 < M; m0 += 64)
+    for (int n0 = 0; n0 < N; n0 += 64) {
+      double acc[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+      for (int64_t kb = k0; kb < k1; kb += kGramSlab) {
+        for (int e = threadIdx.x; e < kGramSlab * 64; e += 256) {
+          const int r = e % kGramSlab, c = e / kGramSlab;
+          const int64_t k = kb + r;
+          sA[r][c] = (k < k1 && m0 + c < M) ? A[k + (int64_t)(m0 + c) * lda] : 0.0;
+          sB[r][c] = (k < k1 && n0 + c < N) ? B[k + (int64_t)(n0 + c) * ldb] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < kGramSlab; ++kk) {
+          double a[4], b[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            a[i] = sA[kk][ty + 16 * i];
+            b[i] = sB[kk][tx + 16 * i];
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int m = m0 + ty + 16 * i, n = n0 + tx + 16 * j;
+          if (m < M && n < N) P[m + (size_t)n * M] = acc[i][j];
+        }
+    }
+}
+
+__global__ void k_gram_sum(int M, int N, int chunks, const double* __restrict__ partial, double* __restrict__ C,
+                           int64_t ldc) {
+  const int mn = M * N;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < mn; e += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int c = 0; c < chunks; ++c) s += partial[(size_t)c * mn + e];
+    C[(e % M) + (int64_t)(e / M) * ldc] = s;
+  }
+}
+
+int gram_f64(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* B,
+             int64_t ldb, double* C, int64_t ldc) {
+  if (M > 128 || N > 128 || M < 1 || N < 1) return OFRR_ERR_BLAS_INVALID_SIZE;
+  int st = OFRR_SUCCESS;
+  const int64_t slabs = (K + kGramSlab - 1) / kGramSlab;
+  const int chunks = (int)std::max<int64_t>(1, std::min<int64_t>(slabs, 152 * 2));
+  const int64_t kc = ((slabs + chunks - 1) / chunks) * kGramSlab;
+  const int used = (int)((K + kc - 1) / kc);
+  double* partial = ws_get<double>(ctx, (size_t)used * M * N, &st);
+  if (!partial) return st;
+  k_gram_f64<<<used, 256, 0, ctx->stream>>>(K, (int)M, (int)N, A, lda, B, ldb, kc, partial);
+  OFRR_LAUNCHED(ctx, "k_gram_f64");
+  k_gram_sum<<<(int)std::min<int64_t>((M * N + 255) / 256, 152 * 4), 256, 0, ctx->stream>>>((int)M, (int)N, used,
+                                                                                            partial, C, ldc);
+  OFRR_LAUNCHED(ctx, "k_gram_sum");
+  return OFRR_SUCCESS;
+}
+
+// C (M x N) = A (M x K) B (K x N) in FP64 for K, N <= 128: the Ritz-vector back-transform X = Q Z of a
+// Rayleigh-Ritz step.  Q is a non-orthogonal basis and Z's columns cancel across it (|Q||z| is 10^3 ..
+// 10^4 times |Qz|), so the emulation's error, relative to |Q||z|, left the Ritz vectors only ~1e-8
+// accurate; these products are small, so they run in FP64.  B in shared memory, a thread per row and 16
+// columns, A read with coalesced loads.
+__global__ void __launch_bounds__(128) k_tsmm_f64(int64_t M, int N, int K, const double* __restrict__ A, int64_t lda,
+                                                  const double* __restrict__ B, int64_t ldb, double* __restrict__ C,
+                                                  int64_t ldc) {
+  extern __shared__ double sBm[];  // K x 16 slice of B (row-major)
+  const int c0 = blockIdx.y * 16, nc = min(16, N - c0);
+  for (int e = threadIdx.x; e < K * 16; e += blockDim.x) {
+    const int k = e / 16, c = e % 16;
+    sBm[e] = (c < nc) ? B[k + (int64_t)(c0 + c) * ldb] : 0.0;
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (int64_t)gridDim.x * blockDim.x) {
+    double acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) acc[c] = 0.0;
+    for (int k = 0; k < K; ++k) {
+      const double a = A[i + (int64_t)k * lda];
+      const double* b = sBm + k * 16;
+#pragma unroll
+      for (int c = 0; c < 16; ++c) acc[c] = fma(a, b[c], acc[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < 16; ++c)
+      if (c < nc) C[i + (int64_t)(c0 + c) * ldc] = acc[c];
+  }
+}
+
+int tsmm_f64(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* B,
+             int64_t ldb, double* C, int64_t ldc) {
+  if (K > 256 || K < 1) return OFRR_ERR_BLAS_INVALID_SIZE;
+  const dim3 grid((unsigned)std::min<int64_t>((M + 127) / 128, 152 * 8), (unsigned)((N + 15) / 16));
+  const size_t smem = (size_t)K * 16 * sizeof(double);
+  if (smem > 48 * 1024) OFRR_TRY(allow_smem(k_tsmm_f64));
+  k_tsmm_f64<<<grid, 128, smem, ctx->stream>>>(M, (int)N, (int)K, A, lda, B, ldb, C, ldc);
+  OFRR_LAUNCHED(ctx, "k_tsmm_f64");
+  return OFRR_SUCCESS;
+}
+
 int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype tb, ofrr_dtype tc, ofrr_dtype tout,
               int64_t M, int64_t N, int64_t K, double alpha, const void* A, int64_t lda, const void* B, int64_t ldb,
               double beta, void* C, int64_t ldc) {
@@ -51,6 +178,12 @@ int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
     if (beta == 1.0) return OFRR_SUCCESS;
   }
   // FP64 TN products in the refinement phase of the mixed solver: exact BF16 slices on the tensor cores
+  if (ctx->emulate_f64 && tc == OFRR_F64 && ta == OFRR_F64 && tb == OFRR_F64 && tout == OFRR_F64 && transB == 0 &&
+      alpha == 1.0 && beta == 0.0 && transA == 1 && M <= 128 && N <= 128 && K * M * N <= (int64_t(1) << 28))
+    return gram_f64(ctx, M, N, K, (const double*)A, lda, (const double*)B, ldb, (double*)C, ldc);
+  if (ctx->emulate_f64 && tc == OFRR_F64 && ta == OFRR_F64 && tb == OFRR_F64 && tout == OFRR_F64 && transA == 0 &&
+      transB == 0 && alpha == 1.0 && beta == 0.0 && K <= 128 && N <= 128 && M * N * K <= (int64_t(1) << 28))
+    return tsmm_f64(ctx, M, N, K, (const double*)A, lda, (const double*)B, ldb, (double*)C, ldc);
   if (ctx->emulate_f64 && tc == OFRR_F64 && ta == OFRR_F64 && tb == OFRR_F64 && tout == OFRR_F64 && transB == 0 &&
       alpha == 1.0 && beta == 0.0 && K >= 16 && (transA == 1 || (M >= 1024 && K <= 1024))) {
     if (K > kSlicedMaxK) {

@@ -25,7 +25,8 @@ __global__ void __launch_bounds__(256) k_hess_col(int64_t m, int n, int i, TO* _
                                                    TO* __restrict__ pivrows, TO* __restrict__ pvals,
                                                    double* __restrict__ R, ArgMax* __restrict__ partial,
                                                    unsigned int* __restrict__ counter, double select_tol,
-                                                   int scale_prev, int* __restrict__ stop, int stage_L) {
+                                                   int scale_prev, int* __restrict__ stop, int stage_L,
+                                                   TO* __restrict__ snap = nullptr) {
   extern __shared__ unsigned char smem_raw[];
   TC* s_r = reinterpret_cast<TC*>(smem_raw);                       // n entries
   TO* s_x = reinterpret_cast<TO*>(s_r + n);                        // n entries
@@ -37,10 +38,13 @@ __global__ void __launch_bounds__(256) k_hess_col(int64_t m, int n, int i, TO* _
   const int tid = threadIdx.x;
   // Krylov mode: a breakdown earlier in this cycle turns the rest of the cycle into no-ops
   if (stop != nullptr && *((volatile int*)stop) >= 0) return;
+  // column i at the earlier pivot rows: from the snapshot the previous launch's last CTA took (every
+  // column is given up front), else from Q itself -- which is only safe while all CTAs of the launch
+  // read it before any of them rewrites its rows of column i, i.e. for grids that are resident at once
   for (int j = tid; j < i; j += blockDim.x) {
     int sj = select[j];
     s_sel[j] = sj;
-    s_x[j] = sj ? Q[(int64_t)perm[j] + (int64_t)i * ldq] : TO(0);
+    s_x[j] = sj ? (snap ? snap[j] : Q[(int64_t)perm[j] + (int64_t)i * ldq]) : TO(0);
   }
   if (tid == 0) s_pprev = (i > 0) ? to_c<TC, TO>(pvals[i - 1]) : TC(0);
   // stage the strictly lower i x i block of pivot rows in shared memory when it fits, so that the
@@ -144,6 +148,12 @@ __global__ void __launch_bounds__(256) k_hess_col(int64_t m, int n, int i, TO* _
       pivrows[(int64_t)i * n + l] = __ldcg(reinterpret_cast<const TO*>(Q + k + (int64_t)l * ldq));
     }
   }
+  if (snap && i + 1 < n) {  // column i + 1 (untouched so far) at the pivot rows 0 .. i
+    for (int j = tid; j <= i; j += blockDim.x) {
+      const int64_t row = (j == i) ? k : (int64_t)perm[j];
+      snap[j] = (j == i || s_sel[j]) ? __ldcg(reinterpret_cast<const TO*>(Q + row + (int64_t)(i + 1) * ldq)) : TO(0);
+    }
+  }
   if (tid == 0) {
     R[i + (int64_t)i * n] = to_c<double, TO>(pv);
     if (stop != nullptr && !keep) *stop = i;
@@ -176,9 +186,13 @@ static int hess_run(ofrr_ctx* ctx, int64_t m, int n, TO* Q, int64_t ldq, double 
   TO* pvals = ws_get<TO>(ctx, (size_t)n, &st);
   if (!pvals) return st;
   const int block = 128;  // one row per thread: 64 CTAs for 8192 rows
-  int grid = grid_for(m, block, 152 * 2);
+  // tall bases (millions of rows, the Krylov restart block): enough threads that each walks only a few
+  // rows -- a thread's rows are a chain of dependent loads of the earlier columns.  The launches read
+  // the next column's pivot-row values from a snapshot, so the grid need not be resident at once.
+  int grid = grid_for(m, block, 152 * 16);
   ArgMax* partial = ws_get<ArgMax>(ctx, grid, &st);
-  if (!partial) return st;
+  TO* snap = ws_get<TO>(ctx, (size_t)n, &st);
+  if (!partial || !snap) return st;
   OFRR_TRY(fill_zero(ctx, R, sizeof(double) * (size_t)n * n));
   OFRR_TRY(fill_zero(ctx, pivrows, sizeof(TO) * (size_t)n * n));
   const int stage = ((size_t)n * n * sizeof(TO) <= 96 * 1024) ? 1 : 0;
@@ -189,7 +203,7 @@ static int hess_run(ofrr_ctx* ctx, int64_t m, int n, TO* Q, int64_t ldq, double 
   }
   for (int i = 0; i < n; ++i) {
     k_hess_col<TO, TC><<<grid, block, smem, ctx->stream>>>(m, n, i, Q, ldq, select, perm, pivrows, pvals, R, partial,
-                                                            ctx->dev_counters, select_tol, 1, nullptr, stage);
+                                                            ctx->dev_counters, select_tol, 1, nullptr, stage, snap);
     OFRR_LAUNCHED(ctx, "k_hess_col");
   }
   k_hess_scale<TO, TC><<<grid, block, 0, ctx->stream>>>(m, n - 1, Q, ldq, select, pvals, nullptr);
@@ -225,7 +239,7 @@ template <class TO, class TC>
 static int kry_col(ofrr_ctx* ctx, int64_t m, int nb, int i, TO* V, int64_t ldv, double stol, int* sel, int* perm,
                    TO* pivrows, TO* pvals, double* R, int* stop) {
   const int block = 256;
-  const int grid = grid_for(m, block, 152 * 4);
+  const int grid = grid_for(m, block, 152 * 4);  // resident at once: column i is read from V itself
   int st = OFRR_SUCCESS;
   WsScope scope(ctx);
   ArgMax* partial = ws_get<ArgMax>(ctx, grid, &st);

@@ -476,8 +476,10 @@ __global__ void k_kry_sumcols(int64_t n, int k, const TW* __restrict__ W, int64_
 }
 
 int kry_backtransform(ofrr_ctx* ctx, ofrr_dtype t, int64_t n, int nc, const void* V, int64_t ldv, const double* Cf,
-                      int k, ofrr_dtype tw, void* W, int64_t ldw) {
+                      int k, ofrr_dtype tw, void* W, int64_t ldw, bool exact) {
   if (k <= 0) return OFRR_SUCCESS;
+  if (exact && t == OFRR_F64 && tw == OFRR_F64)
+    return tsmm_f64(ctx, n, k, nc, (const double*)V, ldv, Cf, nc, (double*)W, ldw);
   if (t == OFRR_F64 || tw == OFRR_F64)
     return gemm_impl(ctx, 0, 0, t, OFRR_F64, OFRR_F64, tw, n, k, nc, 1.0, V, ldv, Cf, nc, 0.0, W, ldw);
   if (tw != OFRR_F32 || nc > kKryMaxNb) return OFRR_ERR_INVALID_ARGUMENT;
@@ -525,6 +527,80 @@ int kry_coef_matrix(ofrr_ctx* ctx, int nc, int k1, const double* U1, int k2, con
                     double* Cf) {
   k_kry_coefmat<<<grid_for((int64_t)nc * (k1 + k2 + 1), 256, 64), 256, 0, ctx->stream>>>(nc, k1, U1, k2, U2, x, Cf);
   OFRR_LAUNCHED(ctx, "k_kry_coefmat");
+  return OFRR_SUCCESS;
+}
+
+// ---- cross-Gram V' (A V) of the 16-bit phase on the tensor cores --------------------------------------
+// A V is FP32 and V 16-bit, and a tcgen05 product takes one operand type: each column of A V is scaled by a
+// power of two (its maximum into [2^13, 2^14)), split into hi = T(y) and lo = T(y - hi), and
+// G = 2^e (V' hi + V' lo) with FP32 accumulation.  The split keeps about 22 bits of A V (FP16) -- the
+// library FP32 path that it replaces (operands widened to FP32, SGEMM with K in the millions and a 65 x 65
+// result) ran on a handful of SMs.
+__global__ void k_kry_colmax_f32(int64_t n, int nc, const float* __restrict__ X, int64_t ldx,
+                                 unsigned int* __restrict__ mx) {
+  const int c = blockIdx.y;
+  float m = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(X[i + (int64_t)c * ldx]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(mx + c, __float_as_uint(m));  // order-free for m >= 0
+}
+
+template <class T>
+__global__ void k_kry_split_hilo(int64_t n, int nc, const float* __restrict__ X, int64_t ldx,
+                                 const unsigned int* __restrict__ mx, T* __restrict__ hi, T* __restrict__ lo,
+                                 int64_t ldh) {
+  const int c = blockIdx.y;
+  const float m = __uint_as_float(mx[c]);
+  int e = 0;
+  if (m > 0.f) frexpf(m, &e);                // m = f 2^e, f in [0.5, 1)
+  const float sc = (m > 0.f) ? ldexpf(1.f, 14 - e) : 0.f;  // maximum into [2^13, 2^14)
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float y = X[i + (int64_t)c * ldx] * sc;
+    const T h = from_c<T, float>(y);
+    hi[i + (int64_t)c * ldh] = h;
+    lo[i + (int64_t)c * ldh] = from_c<T, float>(y - to_c<float, T>(h));
+  }
+}
+
+__global__ void k_kry_gram_combine(int nc, const double* __restrict__ G1, const double* __restrict__ G2,
+                                   const unsigned int* __restrict__ mx, double* __restrict__ G) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nc * nc; e += gridDim.x * blockDim.x) {
+    const int c = e / nc;
+    const float m = __uint_as_float(mx[c]);
+    int ex = 0;
+    if (m > 0.f) frexpf(m, &ex);
+    G[e] = (m > 0.f) ? ldexp(G1[e] + G2[e], ex - 14) : 0.0;
+  }
+}
+
+int kry_gram16(ofrr_ctx* ctx, ofrr_dtype t, int64_t n, int nc, const void* V, int64_t ldv, const float* AV,
+               int64_t ldav, double* G) {
+  if (t != OFRR_F16 && t != OFRR_BF16) return OFRR_ERR_INVALID_ARGUMENT;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  const int64_t ldh = kry_ld(n);
+  void* hi = ws_alloc(ctx, (size_t)ldh * nc * 2, &st);
+  void* lo = ws_alloc(ctx, (size_t)ldh * nc * 2, &st);
+  unsigned int* mx = ws_get<unsigned int>(ctx, (size_t)nc, &st);
+  double* G1 = ws_get<double>(ctx, (size_t)nc * nc, &st);
+  double* G2 = ws_get<double>(ctx, (size_t)nc * nc, &st);
+  if (!hi || !lo || !mx || !G1 || !G2) return st;
+  OFRR_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned int) * nc, ctx->stream));
+  const dim3 grid((unsigned)std::min<int64_t>((n + 255) / 256, 64), (unsigned)nc);
+  k_kry_colmax_f32<<<grid, 256, 0, ctx->stream>>>(n, nc, AV, ldav, mx);
+  OFRR_LAUNCHED(ctx, "k_kry_colmax_f32");
+  if (t == OFRR_F16)
+    k_kry_split_hilo<__half><<<grid, 256, 0, ctx->stream>>>(n, nc, AV, ldav, mx, (__half*)hi, (__half*)lo, ldh);
+  else
+    k_kry_split_hilo<__nv_bfloat16><<<grid, 256, 0, ctx->stream>>>(n, nc, AV, ldav, mx, (__nv_bfloat16*)hi,
+                                                                  (__nv_bfloat16*)lo, ldh);
+  OFRR_LAUNCHED(ctx, "k_kry_split_hilo");
+  OFRR_TRY(gemm_impl(ctx, 1, 0, t, t, OFRR_F32, OFRR_F64, nc, nc, n, 1.0, V, ldv, hi, ldh, 0.0, G1, nc));
+  OFRR_TRY(gemm_impl(ctx, 1, 0, t, t, OFRR_F32, OFRR_F64, nc, nc, n, 1.0, V, ldv, lo, ldh, 0.0, G2, nc));
+  k_kry_gram_combine<<<(nc * nc + 255) / 256, 256, 0, ctx->stream>>>(nc, G1, G2, mx, G);
+  OFRR_LAUNCHED(ctx, "k_kry_gram_combine");
   return OFRR_SUCCESS;
 }
 

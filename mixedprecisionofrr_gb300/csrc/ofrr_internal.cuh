@@ -515,6 +515,10 @@ int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* 
 // with real part above sigma (matrix sign function of L^-1 G L^-T - sigma I); n <= 96
 int invariant_subspace_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double sigma, int p,
                               double* Y);
+// the k leading Ritz pairs of (G, M) from a basis Y (n x p) of its invariant subspace for the p eigenvalues
+// of largest real part: FP64 Hessenberg-QR of the restricted p x p pencil; lam (k), U (n x k, ld n)
+int ritz_from_invariant(ofrr_ctx* ctx, int n, const double* G, const double* M, const double* Y, int p, int k,
+                        double* lam, double* U);
 int geig_fast(ofrr_ctx* ctx, int n, const double* G, const double* M, double tau, double* lam, double* U,
               int refine = 2);
 int gsvd_fast(ofrr_ctx* ctx, int b, const double* B, const double* UU, const double* VV, double tau, double* sigma,
@@ -582,12 +586,22 @@ int kry_cycle_steps(ofrr_ctx* ctx, KryState& s, int q);
 // gemm_impl otherwise), w += a (one column), x = M^-1 g (SPD, nc <= 129),
 // Cf = [U1(:, :k1), U2(:, :k2), -x], s = sum_j W(:, j) / nrm_j
 int kry_backtransform(ofrr_ctx* ctx, ofrr_dtype t, int64_t n, int nc, const void* V, int64_t ldv, const double* Cf,
-                      int k, ofrr_dtype tw, void* W, int64_t ldw);
+                      int k, ofrr_dtype tw, void* W, int64_t ldw, bool exact = false);
 int kry_add_col(ofrr_ctx* ctx, ofrr_dtype tw, int64_t n, void* w, ofrr_dtype ta, const void* a);
 int kry_spd_solve(ofrr_ctx* ctx, int nc, const double* M, const double* g, double* x);
 int kry_coef_matrix(ofrr_ctx* ctx, int nc, int k1, const double* U1, int k2, const double* U2, const double* x,
                     double* Cf);
 int kry_sum_unit_cols(ofrr_ctx* ctx, ofrr_dtype tw, int64_t n, int k, const void* W, int64_t ldw, const double* nrm,
                       double* s);
+// C (M x N) = A' B for FP64 A (K x M), B (K x N), M, N <= 128, FP64 on the CUDA cores (fixed-order
+// partial sums): the exact-arithmetic Gram products of a Rayleigh-Ritz step
+int gram_f64(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* B,
+             int64_t ldb, double* C, int64_t ldc);
+// C (M x N) = A (M x K) B (K x N), FP64 on the CUDA cores (K <= 256): exact-arithmetic back-transforms
+int tsmm_f64(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* B,
+             int64_t ldb, double* C, int64_t ldc);
+// G (nc x nc, FP64) = V' AV for a 16-bit V and an FP32 AV: hi/lo split of AV, two tensor-core products
+int kry_gram16(ofrr_ctx* ctx, ofrr_dtype t, int64_t n, int nc, const void* V, int64_t ldv, const float* AV,
+               int64_t ldav, double* G);
 
 }  // namespace ofrr

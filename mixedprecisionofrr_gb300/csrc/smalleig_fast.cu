@@ -933,6 +933,46 @@ int invariant_subspace_nonsym(ofrr_ctx* ctx, int n, const double* G, const doubl
   return hf ? OFRR_ERR_SINGULAR_MATRIX : OFRR_SUCCESS;
 }
 
+// unit 2-norm columns of U (n x k, ld n), one warp per column
+__global__ void k_unit_cols_nk(int n, int k, double* __restrict__ U) {
+  const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (w >= k) return;
+  double* u = U + (size_t)w * n;
+  double s = 0.0;
+  for (int i = lane; i < n; i += 32) s = fma(u[i], u[i], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  const double inv = (s > 0.0) ? 1.0 / sqrt(s) : 0.0;
+  for (int i = lane; i < n; i += 32) u[i] *= inv;
+}
+
+// The k leading Ritz pairs of the pencil (G, M) from a basis Y (n x p, ld n) of its invariant subspace for
+// the p eigenvalues of largest real part: the restricted pencil (Y'GY, Y'MY) has exactly those
+// eigenvalues, so its p x p FP64 Hessenberg-QR replaces the one of the whole n x n pencil (the QR's cost
+// grows as the cube of the order, and on one warp in FP64 it was the largest part of a restart).
+// lam: the k leading values (real parts, descending; the imaginary part for the second member of a
+// complex pair, as geig_nonsym with pair_imag); U (n x k, ld n): unit 2-norm coefficient vectors.
+int ritz_from_invariant(ofrr_ctx* ctx, int n, const double* G, const double* M, const double* Y, int p, int k,
+                        double* lam, double* U) {
+  if (k <= 0 || p <= 0) return OFRR_SUCCESS;
+  if (k > p || p > n || n > 128) return OFRR_ERR_BLAS_INVALID_SIZE;
+  WsScope scope(ctx);
+  int st = OFRR_SUCCESS;
+  double *GY = ws_get<double>(ctx, (size_t)n * p, &st), *MY = ws_get<double>(ctx, (size_t)n * p, &st),
+         *Gr = ws_get<double>(ctx, (size_t)p * p, &st), *Mr = ws_get<double>(ctx, (size_t)p * p, &st),
+         *lr = ws_get<double>(ctx, (size_t)p, &st), *Zr = ws_get<double>(ctx, (size_t)p * p, &st);
+  if (!GY || !MY || !Gr || !Mr || !lr || !Zr) return st;
+  OFRR_TRY(gemm_small2(ctx, GemmSmall{n, p, n, 1.0, G, n, 0, Y, n, 0, 0.0, GY, n},
+                       GemmSmall{n, p, n, 1.0, M, n, 0, Y, n, 0, 0.0, MY, n}));
+  OFRR_TRY(gemm_small2(ctx, GemmSmall{p, p, n, 1.0, Y, n, 1, GY, n, 0, 0.0, Gr, p},
+                       GemmSmall{p, p, n, 1.0, Y, n, 1, MY, n, 0, 0.0, Mr, p}));
+  OFRR_TRY(geig_nonsym(ctx, p, Gr, Mr, lr, Zr, true, true));
+  OFRR_TRY(gemm_small(ctx, n, k, p, 1.0, Y, n, 0, Zr, p, 0, 0.0, U, n));
+  k_unit_cols_nk<<<(k + 3) / 4, 128, 0, ctx->stream>>>(n, k, U);
+  OFRR_LAUNCHED(ctx, "k_unit_cols_nk");
+  OFRR_CUDA(cudaMemcpyAsync(lam, lr, sizeof(double) * k, cudaMemcpyDeviceToDevice, ctx->stream));
+  return OFRR_SUCCESS;
+}
+
 // eig(G, M) for a nonsymmetric G and SPD M (M null: eig(G)): lam = real parts, descending (stable);
 // U (ld n) the real parts of the eigenvectors, unit 2-norm.  M is reduced away with its FP64
 // Cholesky factor (C = L^-1 G L^-T, U = L^-T X); C is solved in FP32 (smalleig_nonsym.cu).

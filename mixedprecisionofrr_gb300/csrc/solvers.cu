@@ -1011,7 +1011,8 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
   const int kdim = opt->kdim > 0 ? opt->kdim : opt->maxiter;
   const int nb = kdim + 1;
   const int nev = (int)std::min<int64_t>(opt->nev, n);
-  if (nb > kKryMaxNb || nb > n || kdim < 4) return OFRR_ERR_BLAS_INVALID_SIZE;
+  // nb <= 128: the projected pencil's solvers hold at most 128 columns
+  if (nb > std::min(kKryMaxNb, 128) || nb > n || kdim < 4) return OFRR_ERR_BLAS_INVALID_SIZE;
   int keep = opt->restart_keep > 0 ? opt->restart_keep : default_keep(nev, kdim);
   keep = std::min(std::max(keep, nev), kdim - 2);
   if (nev > keep) return OFRR_ERR_INVALID_ARGUMENT;  // nev > kdim - 2
@@ -1055,8 +1056,9 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
   std::vector<double> hd(nb), hres(nb, INFINITY);
   std::vector<int> hsel(nb), hperm(nb), cperm(nb);
   int cycles = 0, steps = 0, nmv = 0, escalations = 0, ncols = 0, in_phase = 0, k = std::min(nev, nb);
-  double best_in_phase = INFINITY;
-  bool converged = false;
+  double best_in_phase = INFINITY, last_maxres = INFINITY, best64 = INFINITY;
+  int stall64 = 0;
+  bool converged = false, exact_rr = false;
   const bool kry_debug = getenv("OFRR_KRYLOV_DEBUG") != nullptr;  // per-cycle progress on stderr
   while (true) {
     TraceScope ts(ctx, "krylov.block");
@@ -1101,9 +1103,20 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
       nmv += ncols;
       tsr.next(t == OFRR_F64 ? "rr.gram.f64" : "rr.gram.16bit");
       ctx->emulate_f64 = mixed && t == OFRR_F64;
-      int rst = gemm_impl(ctx, 1, 0, t, t, ta, OFRR_F64, ncols, ncols, n, 1.0, S.V, S.ldv, S.V, S.ldv, 0.0, M, ncols);
-      if (rst == OFRR_SUCCESS)
-        rst = gemm_impl(ctx, 1, 0, t, tav, ta, OFRR_F64, ncols, ncols, n, 1.0, S.V, S.ldv, AVb, ld, 0.0, G, ncols);
+      int rst = OFRR_SUCCESS;
+      if (exact_rr && t == OFRR_F64) {  // FP64 arithmetic for the Grams once the emulated phase stalls
+        rst = gram_f64(ctx, ncols, ncols, n, (const double*)S.V, S.ldv, (const double*)S.V, S.ldv, M, ncols);
+        if (rst == OFRR_SUCCESS)
+          rst = gram_f64(ctx, ncols, ncols, n, (const double*)S.V, S.ldv, (const double*)AVb, ld, G, ncols);
+      } else {
+        rst = gemm_impl(ctx, 1, 0, t, t, ta, OFRR_F64, ncols, ncols, n, 1.0, S.V, S.ldv, S.V, S.ldv, 0.0, M, ncols);
+      }
+      if (rst == OFRR_SUCCESS && !(exact_rr && t == OFRR_F64)) {
+        if ((t == OFRR_F16 || t == OFRR_BF16) && tav == OFRR_F32)
+          rst = kry_gram16(ctx, t, n, ncols, S.V, S.ldv, (const float*)AVb, ld, G);
+        else
+          rst = gemm_impl(ctx, 1, 0, t, tav, ta, OFRR_F64, ncols, ncols, n, 1.0, S.V, S.ldv, AVb, ld, 0.0, G, ncols);
+      }
       ctx->emulate_f64 = false;
       OFRR_TRY(rst);
       if (opt->generalized_tol != 0.0) {
@@ -1111,8 +1124,11 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
         OFRR_LAUNCHED(ctx, "k_add_diag");
       }
       tsr.next(t == OFRR_F64 ? "rr.eig.f64" : "rr.eig.16bit");
+      // FP64 phase, nonsymmetric: the whole pencil in FP32 only to place the restart cut; the k leading
+      // pairs come in FP64 from the invariant subspace below (restricted pencil)
+      const bool restricted = !symmetric && t == OFRR_F64 && ncols <= 96;
       if (symmetric) OFRR_TRY(geig_fast(ctx, ncols, G, M, 0.0, d, U, t == OFRR_F64 ? 2 : 1));
-      else OFRR_TRY(geig_nonsym(ctx, ncols, G, M, d, U, t == OFRR_F64, true));
+      else OFRR_TRY(geig_nonsym(ctx, ncols, G, M, d, U, t == OFRR_F64 && !restricted, true));
       OFRR_CUDA(cudaMemcpyAsync(hd.data(), d, sizeof(double) * ncols, cudaMemcpyDeviceToHost, ctx->stream));
       OFRR_TRY(sync_and_check(ctx));
       k = std::min(nev, ncols);
@@ -1141,13 +1157,29 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
         else if (ist != OFRR_ERR_SINGULAR_MATRIX) return ist;
         sign_ok = (ist == OFRR_SUCCESS);
       }
+      if (restricted) {
+        tsr.next("rr.ritz.f64");
+        if (sign_ok) {
+          OFRR_TRY(ritz_from_invariant(ctx, ncols, G, M, Ys, pp, k, d, U));
+          OFRR_CUDA(cudaMemcpyAsync(hd.data(), d, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+        } else {  // no invariant subspace (sigma met an eigenvalue): the whole pencil in FP64
+          OFRR_TRY(geig_nonsym(ctx, ncols, G, M, d, U, true, true));
+          OFRR_CUDA(cudaMemcpyAsync(hd.data(), d, sizeof(double) * ncols, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        OFRR_TRY(sync_and_check(ctx));
+      }
       // Wb = V [U(:, :k), Yc, -M^-1 G(:, last)] (+ A v_last in the last column): the k Ritz vectors, then
       // the next block
       tsr.next("rr.update");
       OFRR_TRY(kry_coef_matrix(ctx, ncols, k, U, pp, Yc, xg, Cf));
       tw = (t == OFRR_F64) ? OFRR_F64 : OFRR_F32;
       ctx->emulate_f64 = mixed && t == OFRR_F64;
-      rst = kry_backtransform(ctx, t, n, ncols, S.V, S.ldv, Cf, k + pp + 1, tw, Wb, ld);
+      // the emulated back-transform's error is relative to |V||C| (the Krylov basis is not orthogonal), which
+      // floors the Ritz residuals near 1e-8 of ||A|| (higher for ill-conditioned bases of clustered
+      // spectra): targets below 1e-9, and a stalled FP64 phase, finish with FP64 arithmetic
+      const bool exact_bt = mixed && t == OFRR_F64 &&
+                            (exact_rr || (opt->tol > 0 && opt->tol < 1e-9 && last_maxres <= 1e3 * opt->tol));
+      rst = kry_backtransform(ctx, t, n, ncols, S.V, S.ldv, Cf, k + pp + 1, tw, Wb, ld, exact_bt);
       ctx->emulate_f64 = false;
       OFRR_TRY(rst);
       OFRR_TRY(kry_add_col(ctx, tw, n, (char*)Wb + (size_t)(k + pp) * ld * dtype_size(tw), tav,
@@ -1160,6 +1192,7 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
     OFRR_TRY(residuals_dev(ctx, op, tw, Wb, ld, k, hd.data(), -1.0, hres.data()));
     double maxres = 0;
     for (int j = 0; j < k; ++j) maxres = std::max(maxres, hres[j]);
+    last_maxres = maxres;
     if (kry_debug)
       fprintf(stderr, "[ofrr krylov] cycle %d phase %d type %d q %d ncols %d pp %d sign %d maxres %.3e d0 %.10e\n",
               cycles, phase, (int)t, q, ncols, pp, sign_ok ? 1 : 0, maxres, hd[0]);
@@ -1173,6 +1206,17 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
     const double switch_at = (t == OFRR_BF16) ? 1e-2 : 1e-3;
     const bool stalled = in_phase >= 3 && maxres > 0.7 * best_in_phase;
     best_in_phase = std::min(best_in_phase, maxres);
+    // FP64 phase: no 10 % gain over 6 cycles is the emulated products' floor -- FP64 products from here on
+    if (maxres < 0.9 * best64) {
+      best64 = maxres;
+      stall64 = 0;
+    } else {
+      ++stall64;
+    }
+    if (mixed && phase == 1 && stall64 >= 6 && !exact_rr) {
+      exact_rr = true;
+      stall64 = 0;
+    }
     if (mixed && phase == 0 && (maxres <= switch_at || stalled)) {
       OFRR_TRY(column_norms(ctx, tw, n, k, Wb, ld, nrm));
       OFRR_TRY(kry_sum_unit_cols(ctx, tw, n, k, Wb, ld, nrm, svec));
@@ -1183,6 +1227,8 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
       phase = 1;
       in_phase = 0;
       best_in_phase = INFINITY;
+      best64 = INFINITY;
+      stall64 = 0;
       escalations++;
       OFRR_TRY(kry_state_init(ctx, &S, &A->csr, OFRR_F64, nb, stol));
     } else {
@@ -1389,7 +1435,26 @@ struct PhaseState {
   bool done = false;   // all nev pairs at tol
   std::vector<double> d, res, dprev;
   double delta = INFINITY, delta_prev = INFINITY;
+  // emulated FP64 phase: best certified residual, checks without a 10 % gain, and the floor flag
+  double best_emul = INFINITY;
+  int stall_emul = 0;
+  bool emul_floor = false;
 };
+
+// The emulated products' accuracy floor: a certified check that has not improved the residual by 10 %
+// for 4 checks ends the emulated phase (the caller continues with FP64 products).
+bool emulation_floor(PhaseState& S, int kk) {
+  double mr = 0;
+  for (int j = 0; j < kk; ++j) mr = std::max(mr, S.res[j]);
+  if (mr < 0.9 * S.best_emul) {
+    S.best_emul = mr;
+    S.stall_emul = 0;
+  } else {
+    ++S.stall_emul;
+  }
+  S.emul_floor = S.stall_emul >= 4;
+  return S.emul_floor;
+}
 
 // Ritz-value stagnation test of the low-precision phase: relative change of the top nev values
 bool stagnated(PhaseState& S, int nev, double stag_tol, int iters_in_phase) {
@@ -1500,6 +1565,7 @@ int eig_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
       S.converged = 0;
       for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= tol) ? 1 : 0;
       if (S.converged >= kk) S.done = true;
+      if (!S.done && emulation_floor(S, kk)) break;
     } else if (check) {
       OFRR_TRY(residuals_dev(ctx, op, P.po, cur, ldcur, kk, S.d.data(), -1.0, S.res.data()));
       S.converged = 0;
@@ -1648,6 +1714,7 @@ int svd_phase(ofrr_ctx* ctx, Op& op, const Precisions& P, const ofrr_options* op
       S.converged = 0;
       for (int j = 0; j < kk; ++j) S.converged += (S.res[j] <= tol) ? 1 : 0;
       if (S.converged >= kk) S.done = true;
+      if (!S.done && emulation_floor(S, kk)) break;
     } else if (check) {
       OFRR_TRY(svd_residuals_dev(ctx, op, P.po, U, ldu, V, ldv, kk, S.d.data(), -1.0, S.res.data()));
       S.converged = 0;
@@ -1757,6 +1824,12 @@ static int si_eig_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
                      dense ? (int)L.po : -1);
       ctx->emulate_f64 = false;
       OFRR_TRY(st);
+      if (!S.done && S.emul_floor && S.it < opt->maxiter) {
+        // the emulated products' floor is above tol: the last iterations with FP64 products
+        TraceScope ts(ctx, "fp64.exact");
+        escalations = 2;
+        OFRR_TRY(eig_phase(ctx, op, all_f64(), opt, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d));
+      }
     }
   } else {
     const Precisions P = precisions_of(opt);
@@ -1856,6 +1929,12 @@ static int si_svd_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
                      dense ? (int)L.po : -1);
       ctx->emulate_f64 = false;
       OFRR_TRY(st);
+      if (!S.done && S.emul_floor && S.it < opt->maxiter) {
+        // the emulated products' floor is above tol: the last iterations with FP64 products
+        TraceScope ts(ctx, "fp64.exact");
+        escalations = 2;
+        OFRR_TRY(svd_phase(ctx, op, all_f64(), opt, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d));
+      }
     }
   } else {
     const Precisions P = precisions_of(opt);

@@ -7,7 +7,7 @@ The stream (sizes and tolerances from the serving workload's description):
   1e-6 (the matrix built on the GPU from Householder reflectors around diag(s): exact spectrum);
 * 40 % Laplacian eigenproblems: 2D or 3D Dirichlet Laplacian (integer stencil) with n uniform in
   [1e4, 1e6], grid sides N, N+1 (, N+2) so that no eigenvalue is exactly repeated, largest eigenvalues
-  by the thick-restart Krylov solver (Krylov dimension max(2k, k + 24), at most 128);
+  by the thick-restart Krylov solver (Krylov dimension max(2k, k + 24), at most 127);
 * k uniform in [4, 64], tol uniform over {1e-6, 1e-8, 1e-10}; mixed precision throughout.
 
 Admission: the engine's HBM budget (default 150 GB) charges each request's solver workspace; the driver
@@ -111,7 +111,7 @@ def submit(server: "api.Server", req: Request, A):
     if req.kind == "svd":
         return server.submit_si_svd(A, max(req.k + 16, int(1.5 * req.k)), mode="mixed", tol=req.tol, nev=req.k,
                                     maxiter=400, step_size=6, seed=req.seed & 0xFFFFFFFF)
-    kdim = min(max(2 * req.k, req.k + 24), 128)
+    kdim = min(max(2 * req.k, req.k + 24), 127)
     return server.submit_arnoldi_eig(A, req.k, kdim=kdim, mode="mixed", tol=req.tol, maxiter=200_000,
                                      seed=req.seed & 0xFFFFFFFF)
 
