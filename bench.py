@@ -769,6 +769,17 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from mixedprecisionofrr_gb300 import api
 
+    if args.roofline_only and args.config == "c3":
+        # the fused Krylov step alone on the 128^3 operator (FP64 basis, column 40, then FP16, column 40)
+        from mixedprecisionofrr_gb300 import problems
+
+        Acsr = api.CsrMatrix(problems.convdiff_3d(C3_N), symmetric=False)
+        res = {}
+        for prec, i in (("double", 40), ("half", 40)):
+            us, by = api.profile_krylov_step(Acsr, prec, i, reps=5)
+            res[f"{prec}_i{i}"] = {"us": us, "bytes": by, "GBps": by / us / 1e3}
+        print(json.dumps({"roofline_only": True, "config": "c3", "k_kry_step": res}))
+        return
     if args.roofline_only:
         dt_s, bytes_s = sliced_roofline(api)
         dt_g, bytes_g, flops_g = gemm_roofline(api)

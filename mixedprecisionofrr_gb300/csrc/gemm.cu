@@ -35,8 +35,9 @@ __global__ void k_add_f64(int64_t m, int64_t n, const double* __restrict__ T, in
 // ---- FP64 Gram products on the CUDA cores ------------------------------------------------------------
 // C (M x N) = A' B for FP64 A (K x M), B (K x N), M, N <= 128: the Gram and cross-Gram matrices of a
 // Rayleigh-Ritz step.  The exact-slice emulation's element error (2^-35 of |A|'|B|) is amplified by the
-// condition number of a non-orthogonal basis (10^3 .. 10^4 for power-iterated Hessenberg bases), which
-// capped the Ritz values near 1e-9 relative; these products are small (K M N FMAs), so they run in FP64.
+// condition number of a non-orthogonal basis (10^3 .. 10^4 for power-iterated Hessenberg bases); the small
+// products (K M N <= 2^22 FMAs: small requests) run in FP64, larger ones stay emulated until a solve meets
+// that floor (the solvers then switch to FP64 products).
 // One CTA per K chunk: 32-row slabs of both operands staged in shared memory, a 64 x 64 output tile per
 // pass (4 x 4 per thread of a 16 x 16 grid), the chunk's partial written out; k_gram_sum adds the
 // partials in chunk order (results do not depend on the schedule).
@@ -119,9 +120,9 @@ int gram_f64(ofrr_ctx* ctx, int64_t M, int64_t N, int64_t K, const double* A, in
 
 // C (M x N) = A (M x K) B (K x N) in FP64 for K, N <= 128: the Ritz-vector back-transform X = Q Z of a
 // Rayleigh-Ritz step.  Q is a non-orthogonal basis and Z's columns cancel across it (|Q||z| is 10^3 ..
-// 10^4 times |Qz|), so the emulation's error, relative to |Q||z|, left the Ritz vectors only ~1e-8
-// accurate; these products are small, so they run in FP64.  B in shared memory, a thread per row and 16
-// columns, A read with coalesced loads.
+// 10^4 times |Qz|), so the emulation's error is relative to a much larger number than the result; small
+// products (and every back-transform once a solve meets the emulation floor) run in FP64.  B in shared
+// memory, a thread per row and 16 columns, A read with coalesced loads.
 __global__ void __launch_bounds__(128) k_tsmm_f64(int64_t M, int N, int K, const double* __restrict__ A, int64_t lda,
                                                   const double* __restrict__ B, int64_t ldb, double* __restrict__ C,
                                                   int64_t ldc) {
@@ -179,10 +180,10 @@ int gemm_impl(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype ta, ofrr_dtype t
   }
   // FP64 TN products in the refinement phase of the mixed solver: exact BF16 slices on the tensor cores
   if (ctx->emulate_f64 && tc == OFRR_F64 && ta == OFRR_F64 && tb == OFRR_F64 && tout == OFRR_F64 && transB == 0 &&
-      alpha == 1.0 && beta == 0.0 && transA == 1 && M <= 128 && N <= 128 && K * M * N <= (int64_t(1) << 28))
+      alpha == 1.0 && beta == 0.0 && transA == 1 && M <= 128 && N <= 128 && K * M * N <= (int64_t(1) << 22))
     return gram_f64(ctx, M, N, K, (const double*)A, lda, (const double*)B, ldb, (double*)C, ldc);
   if (ctx->emulate_f64 && tc == OFRR_F64 && ta == OFRR_F64 && tb == OFRR_F64 && tout == OFRR_F64 && transA == 0 &&
-      transB == 0 && alpha == 1.0 && beta == 0.0 && K <= 128 && N <= 128 && M * N * K <= (int64_t(1) << 28))
+      transB == 0 && alpha == 1.0 && beta == 0.0 && K <= 128 && N <= 128 && M * N * K <= (int64_t(1) << 22))
     return tsmm_f64(ctx, M, N, K, (const double*)A, lda, (const double*)B, ldb, (double*)C, ldc);
   if (ctx->emulate_f64 && tc == OFRR_F64 && ta == OFRR_F64 && tb == OFRR_F64 && tout == OFRR_F64 && transB == 0 &&
       alpha == 1.0 && beta == 0.0 && K >= 16 && (transA == 1 || (M >= 1024 && K <= 1024))) {

@@ -1206,14 +1206,15 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
     const double switch_at = (t == OFRR_BF16) ? 1e-2 : 1e-3;
     const bool stalled = in_phase >= 3 && maxres > 0.7 * best_in_phase;
     best_in_phase = std::min(best_in_phase, maxres);
-    // FP64 phase: no 10 % gain over 6 cycles is the emulated products' floor -- FP64 products from here on
-    if (maxres < 0.9 * best64) {
+    // FP64 phase: no 2x gain over 16 cycles is the emulated products' floor -- FP64 products from here on
+    // (a slowly converging solve gains 2x in a few cycles; a floor does not move)
+    if (maxres < 0.5 * best64) {
       best64 = maxres;
       stall64 = 0;
     } else {
       ++stall64;
     }
-    if (mixed && phase == 1 && stall64 >= 6 && !exact_rr) {
+    if (mixed && phase == 1 && stall64 >= 16 && !exact_rr && maxres < 1e-6) {
       exact_rr = true;
       stall64 = 0;
     }
