@@ -34,6 +34,16 @@ constexpr int BE_B = 16;       // block width (columns)
 constexpr int BE_NMAX = 1024;  // largest matrix dimension held in shared memory
 constexpr int BE_NEV = 8;      // leading pairs certified by the refinement
 
+// The n x BE_B blocks in shared memory are row-major with the four float4 quads of row i stored at quad
+// position q ^ (i & 3): a column is then spread over 8 bank groups instead of 2 (column-wise passes,
+// one row per lane, had 16-way bank conflicts), while whole quads stay aligned for 16-byte accesses.
+__device__ __forceinline__ int be_at(int i, int c) { return i * BE_B + ((((c >> 2) ^ (i & 3))) << 2) + (c & 3); }
+// logical column of the element stored at physical offset e of the block
+__device__ __forceinline__ int be_col(int e) {
+  const int i = e / BE_B, p = e % BE_B;
+  return ((((p >> 2) ^ (i & 3))) << 2) + (p & 3);
+}
+
 // ---- FP64 refinement of the nev leading Ritz pairs of every matrix ------------------------------------
 struct RefineDev {
   const int64_t* n;
@@ -188,10 +198,11 @@ __device__ bool be_matmul_r(int n, int ld, const TA* __restrict__ A, const float
     if (active) {
       for (int kk = g; kk < cols; kk += G) {
         const float4* vk = reinterpret_cast<const float4*>(V + (k0 + kk) * BE_B);
+        const int sw = (k0 + kk) & 3;
         float v[BE_B];
 #pragma unroll
         for (int q = 0; q < BE_B / 4; ++q) {
-          const float4 x = vk[q];
+          const float4 x = vk[q ^ sw];
           v[4 * q] = x.x;
           v[4 * q + 1] = x.y;
           v[4 * q + 2] = x.z;
@@ -235,17 +246,18 @@ __device__ bool be_matmul_r(int n, int ld, const TA* __restrict__ A, const float
         const int i = t + r * Tg;
         if (i < n) {
           float4* w = reinterpret_cast<float4*>(W + i * BE_B);
+          const int sw = i & 3;
 #pragma unroll
           for (int q = 0; q < BE_B / 4; ++q) {
             float4 x = make_float4(acc[r][4 * q], acc[r][4 * q + 1], acc[r][4 * q + 2], acc[r][4 * q + 3]);
             if (gg > 0) {
-              const float4 y = w[q];
+              const float4 y = w[q ^ sw];
               x.x += y.x;
               x.y += y.y;
               x.z += y.z;
               x.w += y.w;
             }
-            w[q] = x;
+            w[q ^ sw] = x;
           }
         }
       }
@@ -281,7 +293,7 @@ __device__ void be_colmax(int n, int b, const float* X, float* out, float* redv,
   for (int i = tid; i < n; i += BE_T) {
 #pragma unroll
     for (int c = 0; c < BE_B; ++c) {
-      const float a = fabsf(X[i * BE_B + c]);
+      const float a = fabsf(X[be_at(i, c)]);
       if (a > best[c]) {
         best[c] = a;
         bi[c] = i;
@@ -318,7 +330,7 @@ __device__ void be_colmax(int n, int b, const float* X, float* out, float* redv,
         ii = vi;
       }
     }
-    out[tid] = (ii < n) ? X[ii * BE_B + tid] : 0.f;
+    out[tid] = (ii < n) ? X[be_at(ii, tid)] : 0.f;
   }
   __syncthreads();
 }
@@ -343,7 +355,8 @@ __device__ void be_jacobi(float* S, float* U, float* w, float* cs, int* pq) {
       off += __shfl_xor_sync(0xffffffffu, off, o);
       dn += __shfl_xor_sync(0xffffffffu, dn, o);
     }
-    if (off <= 1e-14f * dn || off == 0.f) break;
+    // FP32 rotations leave ~b eps^2 of dn off the diagonal: 1e-13 is reachable (off-diagonal ~3e-7)
+    if (off <= 1e-13f * dn || off == 0.f) break;
     for (int round = 0; round < BE_B - 1; ++round) {
       if (lane < BE_B / 2) {  // round-robin pairs: position 0 fixed, the others rotate
         const int a = (lane == 0) ? 0 : 1 + (lane - 1 + round) % (BE_B - 1);
@@ -824,7 +837,7 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
     const float* A32 = d.A32 + off;
     // start block: Gaussian-like draws (sum of uniforms) from the matrix's key, scaled to unit maximum
     for (int e = tid; e < n * BE_B; e += BE_T) {
-      const int i = e / BE_B, c = e % BE_B;
+      const int i = e / BE_B, c = be_col(e);
       const uint64_t h = be_mix(d.seed ^ be_mix((uint64_t)mi * 0x100000001b3ull + (uint64_t)(i * BE_B + c)));
       V[e] = (c < b) ? ((float)(h >> 40) * (1.f / 16777216.f) - 0.5f) : 0.f;
     }
@@ -838,7 +851,7 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
         if (!(phase == 0 ? be_matmul<T16>(n, ld, A16, V, W, rg) : be_matmul<float>(n, ld, A32, V, W, rg))) return;
         be_colmax(n, b, W, s_piv, s_red, s_redi);
         for (int e = tid; e < n * BE_B; e += BE_T) {
-          const int c = e % BE_B;
+          const int c = be_col(e);
           const float pv = s_piv[c];
           V[e] = (c < b && pv != 0.f) ? W[e] / pv : 0.f;
         }
@@ -853,9 +866,9 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
           for (int l = 0; l < j; ++l) {
             float cl = 0.f;
             if (s_sel[l]) {
-              const float* Vp = V + s_perm[l] * BE_B;
-              cl = Vp[j];
-              for (int l2 = 0; l2 < l; ++l2) cl = fmaf(-s_c[l2], Vp[l2], cl);
+              const int pr = s_perm[l];
+              cl = V[be_at(pr, j)];
+              for (int l2 = 0; l2 < l; ++l2) cl = fmaf(-s_c[l2], V[be_at(pr, l2)], cl);
             }
             s_c[l] = cl;
           }
@@ -864,9 +877,9 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
         float bv = -1.f;
         int bi = 0x7fffffff;
         for (int i = tid; i < n; i += BE_T) {
-          float v = V[i * BE_B + j];
-          for (int l = 0; l < j; ++l) v = fmaf(-s_c[l], V[i * BE_B + l], v);
-          V[i * BE_B + j] = v;
+          float v = V[be_at(i, j)];
+          for (int l = 0; l < j; ++l) v = fmaf(-s_c[l], V[be_at(i, l)], v);
+          V[be_at(i, j)] = v;
           const float a = fabsf(v);
           if (a > bv) {
             bv = a;
@@ -898,11 +911,11 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
           const bool keep = ii < n && bb >= 1e-5f;  // columns enter with unit maximum
           s_sel[j] = keep ? 1 : 0;
           s_perm[j] = keep ? ii : 0;
-          s_piv[j] = keep ? V[ii * BE_B + j] : 0.f;
+          s_piv[j] = keep ? V[be_at(ii, j)] : 0.f;
         }
         __syncthreads();
         const float pv = s_piv[j];
-        for (int i = tid; i < n; i += BE_T) V[i * BE_B + j] = (pv != 0.f) ? V[i * BE_B + j] / pv : 0.f;
+        for (int i = tid; i < n; i += BE_T) V[be_at(i, j)] = (pv != 0.f) ? V[be_at(i, j)] / pv : 0.f;
         __syncthreads();
       }
       // ---- Rayleigh-Ritz: W = A Q, G = Q' W, M = Q' Q (64-row FP32 chunks summed in FP64) ----
@@ -917,7 +930,7 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
             for (int ch = 0; ch < nch; ++ch) {
               float s = 0.f;
               const int i1 = min(n, ch * 64 + 64);
-              for (int i = ch * 64; i < i1; ++i) s = fmaf(V[i * BE_B + r], which ? V[i * BE_B + c] : W[i * BE_B + c], s);
+              for (int i = ch * 64; i < i1; ++i) s = fmaf(V[be_at(i, r)], which ? V[be_at(i, c)] : W[be_at(i, c)], s);
               acc += (double)s;
             }
           }
@@ -929,24 +942,29 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
       // ---- the b x b pencil on warp 0: M + tau I = L L' (FP64), C = L^-1 sym(G) L^-T, Jacobi (FP32) ----
       if (tid < 32) {
         const int lane = tid;
-        if (lane == 0) {
+        {
+          // Cholesky of M + tau I, row-major lower factor in s_L; lane i computes L(i, j) of column j
           double mx = 0.0;
           for (int i = 0; i < b; ++i) mx = fmax(mx, s_M[i * BE_B + i]);
-          for (int i = 0; i < b; ++i) s_M[i * BE_B + i] += 1e-12 * mx + 1e-300;
-          for (int j = 0; j < b; ++j) {  // Cholesky, row-major lower factor in s_L
-            double dj = s_M[j * BE_B + j];
+          const double tau = 1e-12 * mx + 1e-300;
+          for (int e = lane; e < BE_B * BE_B; e += 32) s_L[e] = 0.0;
+          __syncwarp();
+          for (int j = 0; j < b; ++j) {
+            double dj = s_M[j * BE_B + j] + tau;
             for (int k = 0; k < j; ++k) dj -= s_L[j * BE_B + k] * s_L[j * BE_B + k];
             dj = sqrt(fmax(dj, 1e-300));
-            s_L[j * BE_B + j] = dj;
-            for (int i = j + 1; i < b; ++i) {
-              double v = s_M[i * BE_B + j];
-              for (int k = 0; k < j; ++k) v -= s_L[i * BE_B + k] * s_L[j * BE_B + k];
-              s_L[i * BE_B + j] = v / dj;
+            double lij = 0.0;
+            if (lane > j && lane < b) {
+              double v = s_M[lane * BE_B + j];
+              for (int k = 0; k < j; ++k) v -= s_L[lane * BE_B + k] * s_L[j * BE_B + k];
+              lij = v / dj;
             }
-            for (int i = 0; i < j; ++i) s_L[i * BE_B + j] = 0.0;
+            __syncwarp();
+            if (lane > j && lane < b) s_L[lane * BE_B + j] = lij;
+            if (lane == 0) s_L[j * BE_B + j] = dj;
+            __syncwarp();
           }
         }
-        __syncwarp();
         // T = L^-1 sym(G) (column c by forward substitution, lanes over columns)
         for (int c = lane; c < b; c += 32) {
           for (int i = 0; i < b; ++i) {
@@ -1014,8 +1032,8 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
         float q[BE_B], a[BE_B];
 #pragma unroll
         for (int c = 0; c < BE_B; ++c) {
-          q[c] = V[i * BE_B + c];
-          a[c] = W[i * BE_B + c];
+          q[c] = V[be_at(i, c)];
+          a[c] = W[be_at(i, c)];
         }
 #pragma unroll 1
         for (int c = 0; c < BE_B; ++c) {
@@ -1025,8 +1043,8 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
             x = fmaf(q[r], s_Z[r * BE_B + c], x);
             ax = fmaf(a[r], s_Z[r * BE_B + c], ax);
           }
-          V[i * BE_B + c] = (c < b) ? x : 0.f;
-          W[i * BE_B + c] = (c < b) ? ax : 0.f;
+          V[be_at(i, c)] = (c < b) ? x : 0.f;
+          W[be_at(i, c)] = (c < b) ? ax : 0.f;
         }
       }
       __syncthreads();
@@ -1040,8 +1058,8 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
         for (int i = tid; i < n; i += BE_T) {
 #pragma unroll
           for (int c = 0; c < BE_NEV; ++c) {
-            const float x = V[i * BE_B + c];
-            const float r = W[i * BE_B + c] - s_lam[c] * x;
+            const float x = V[be_at(i, c)];
+            const float r = W[be_at(i, c)] - s_lam[c] * x;
             rr[c] = fmaf(r, r, rr[c]);
             xx[c] = fmaf(x, x, xx[c]);
           }
@@ -1092,7 +1110,7 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
       // (deselected by the basis) restarts from fresh draws
       be_colmax(n, b, V, s_piv, s_red, s_redi);
       for (int e = tid; e < n * BE_B; e += BE_T) {
-        const int i = e / BE_B, c = e % BE_B;
+        const int i = e / BE_B, c = be_col(e);
         const float pv = s_piv[c];
         float v = 0.f;
         if (c < b) {
@@ -1112,7 +1130,7 @@ __global__ void __launch_bounds__(BE_T, 1) k_batch_si(BatchDev d) {
     // ---- outputs: Ritz vectors (FP32, n x BE_B), values, counts ----
     float* X = d.X + d.xoff[mi];
     for (int e = tid; e < n * BE_B; e += BE_T) {
-      const int i = e / BE_B, c = e % BE_B;
+      const int i = e / BE_B, c = be_col(e);
       X[i + (int64_t)c * n] = V[e];
     }
     if (tid < BE_B) d.lam[(int64_t)mi * BE_B + tid] = (tid < b) ? s_lam[tid] : 0.f;

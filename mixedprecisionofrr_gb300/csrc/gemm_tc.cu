@@ -426,16 +426,38 @@ static void choose_plan(int64_t M, int64_t N, int64_t K, int t16, int* BN, int* 
 }
 }  // namespace tc
 
-// Route a 16-bit TN product to the tcgen05 kernel when its layout allows TMA (16-byte aligned
-// base and leading dimensions); *handled = false leaves the call to the caller's fallback.
+// A 16-bit K x cols operand as TMA takes it (16-byte aligned base and leading dimension): a misaligned
+// one (an odd row count) is copied once, as one pitched copy, into an aligned workspace buffer.  The
+// tensor-core path then serves every shape, so results never depend on a library fallback.
+static int tc_operand(ofrr_ctx* ctx, const void* X, int64_t ld, int64_t K, int64_t cols, const void** out,
+                      int64_t* ldo) {
+  if (!((uintptr_t)X & 15) && !((ld * 2) & 15)) {
+    *out = X;
+    *ldo = ld;
+    return OFRR_SUCCESS;
+  }
+  const int64_t ldp = (K + 7) & ~int64_t(7);
+  int st = OFRR_SUCCESS;
+  void* w = ws_alloc(ctx, (size_t)ldp * cols * 2, &st);
+  if (!w) return st;
+  OFRR_CUDA(cudaMemcpy2DAsync(w, (size_t)ldp * 2, X, (size_t)ld * 2, (size_t)K * 2, (size_t)cols,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+  *out = w;
+  *ldo = ldp;
+  return OFRR_SUCCESS;
+}
+
+// Route a 16-bit TN product to the tcgen05 kernel (operands staged to TMA-aligned layouts when needed);
+// *handled = false leaves the call to the caller's fallback.
 int gemm_tc_try(ofrr_ctx* ctx, int transA, int transB, ofrr_dtype t16, int64_t M, int64_t N, int64_t K,
                 const void* A, int64_t lda, const void* B, int64_t ldb, ofrr_dtype tout, void* C, int64_t ldc,
                 bool* handled) {
   *handled = false;
   if (!(transA == 1 && transB == 0)) return OFRR_SUCCESS;
   if (K < 16 || M < 1 || N < 1 || M > (1 << 30) || N > (1 << 30) || K > (1 << 30)) return OFRR_SUCCESS;
-  if (((uintptr_t)A & 15) || ((uintptr_t)B & 15) || ((lda * 2) & 15) || ((ldb * 2) & 15)) return OFRR_SUCCESS;
   if (getenv("OFRR_DISABLE_TC")) return OFRR_SUCCESS;
+  OFRR_TRY(tc_operand(ctx, A, lda, K, M, &A, &lda));
+  OFRR_TRY(tc_operand(ctx, B, ldb, K, N, &B, &ldb));
   int BN = 64, splits = 1;
   tc::choose_plan(M, N, K, t16, &BN, &splits);
   CUtensorMap ma, mb;
@@ -461,8 +483,9 @@ int gemm_tc_scalecols(ofrr_ctx* ctx, ofrr_dtype t16, int64_t M, int64_t N, int64
   *handled = false;
   if (t16 != OFRR_F16 && t16 != OFRR_BF16) return OFRR_SUCCESS;
   if (K < 16 || M < 1 || N < 1 || M > 8192 || N > 65535 || K > (1 << 30)) return OFRR_SUCCESS;
-  if (((uintptr_t)A & 15) || ((uintptr_t)B & 15) || ((lda * 2) & 15) || ((ldb * 2) & 15)) return OFRR_SUCCESS;
   if (getenv("OFRR_DISABLE_TC")) return OFRR_SUCCESS;
+  OFRR_TRY(tc_operand(ctx, A, lda, K, M, &A, &lda));
+  OFRR_TRY(tc_operand(ctx, B, ldb, K, N, &B, &ldb));
   int BN = 64, splits = 1;
   tc::choose_plan(M, N, K, t16, &BN, &splits);
   CUtensorMap ma, mb;

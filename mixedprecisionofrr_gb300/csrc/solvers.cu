@@ -44,12 +44,15 @@ struct Op {
         dense[t] = A->data;
         ld[t] = A->ld;
       } else {
+        // 16-bit copies with the leading dimension rounded up to 8 elements: 16-byte aligned columns, as
+        // the tensor-core product's TMA needs, whatever the row count
         int st = OFRR_SUCCESS;
-        void* w = ws_alloc(ctx, (size_t)m() * n() * dtype_size(t), &st);
+        const int64_t ldp = (dtype_size(t) == 2) ? ((m() + 7) & ~int64_t(7)) : m();
+        void* w = ws_alloc(ctx, (size_t)ldp * n() * dtype_size(t), &st);
         if (!w) return st;
-        OFRR_TRY(cast_impl(ctx, A->dtype, t, m(), n(), A->data, A->ld, w, m()));
+        OFRR_TRY(cast_impl(ctx, A->dtype, t, m(), n(), A->data, A->ld, w, ldp));
         dense[t] = w;
-        ld[t] = m();
+        ld[t] = ldp;
       }
     }
     *p = dense[t];
@@ -203,16 +206,19 @@ struct Op {
 
   // A' stored column-major (n x m) in type t, made once per solve
   const void* dense_t[4] = {nullptr, nullptr, nullptr, nullptr};
+  int64_t ldt[4] = {0, 0, 0, 0};
   int dense_t_as(ofrr_ctx* ctx, ofrr_dtype t, const void** p, int64_t* l) {
     if (!dense_t[t]) {
       int st = OFRR_SUCCESS;
-      void* w = ws_alloc(ctx, (size_t)m() * n() * dtype_size(t), &st);
+      const int64_t ldp = (dtype_size(t) == 2) ? ((n() + 7) & ~int64_t(7)) : n();
+      void* w = ws_alloc(ctx, (size_t)ldp * m() * dtype_size(t), &st);
       if (!w) return st;
-      OFRR_TRY(cast_transpose_impl(ctx, A->dtype, t, m(), n(), A->data, A->ld, w, n()));
+      OFRR_TRY(cast_transpose_impl(ctx, A->dtype, t, m(), n(), A->data, A->ld, w, ldp));
       dense_t[t] = w;
+      ldt[t] = ldp;
     }
     *p = dense_t[t];
-    *l = n();
+    *l = ldt[t];
     return OFRR_SUCCESS;
   }
 };
@@ -487,27 +493,28 @@ int emulation_bounds(ofrr_ctx* ctx, Op& op, int trans, ofrr_dtype t16, const dou
   if (trans) OFRR_TRY(op.dense_as(ctx, t16, &Ap, &lda));
   else OFRR_TRY(op.dense_t_as(ctx, t16, &Ap, &lda));
   const bool cached = op.absA[trans] != nullptr && op.abs_t == t16;
-  void* absA = cached ? op.absA[trans] : ws_alloc(ctx, (size_t)K * M * 2, &st);
-  void* absX = ws_alloc(ctx, (size_t)K * k * 2, &st);
+  const int64_t ldK = (K + 7) & ~int64_t(7);  // 16-byte aligned columns for the tensor-core product
+  void* absA = cached ? op.absA[trans] : ws_alloc(ctx, (size_t)ldK * M * 2, &st);
+  void* absX = ws_alloc(ctx, (size_t)ldK * k * 2, &st);
   float* Bnd = ws_get<float>(ctx, (size_t)M * k, &st);
   if (!absA || !absX || !Bnd) return st;
   if (t16 == OFRR_F16) {
     if (!cached) {
       k_abs_cast<__half, __half><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(K, M, (const __half*)Ap, lda,
-                                                                               (__half*)absA, K);
+                                                                               (__half*)absA, ldK);
       OFRR_LAUNCHED(ctx, "k_abs_cast");
     }
-    k_abs_cast_f64<<<grid_2d(K, k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, (__half*)absX, nullptr, K);
+    k_abs_cast_f64<<<grid_2d(K, k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, (__half*)absX, nullptr, ldK);
   } else {
     if (!cached) {
       k_abs_cast<__nv_bfloat16, __nv_bfloat16><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(
-          K, M, (const __nv_bfloat16*)Ap, lda, (__nv_bfloat16*)absA, K);
+          K, M, (const __nv_bfloat16*)Ap, lda, (__nv_bfloat16*)absA, ldK);
       OFRR_LAUNCHED(ctx, "k_abs_cast");
     }
-    k_abs_cast_f64<<<grid_2d(K, k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, nullptr, (__nv_bfloat16*)absX, K);
+    k_abs_cast_f64<<<grid_2d(K, k, 256), 256, 0, ctx->stream>>>(K, k, X, ldx, nullptr, (__nv_bfloat16*)absX, ldK);
   }
   OFRR_LAUNCHED(ctx, "k_abs_cast_f64");
-  OFRR_TRY(gemm_impl(ctx, 1, 0, t16, t16, OFRR_F32, OFRR_F32, M, k, K, 1.0, absA, K, absX, K, 0.0, Bnd, M));
+  OFRR_TRY(gemm_impl(ctx, 1, 0, t16, t16, OFRR_F32, OFRR_F32, M, k, K, 1.0, absA, ldK, absX, ldK, 0.0, Bnd, M));
   OFRR_TRY(column_norms(ctx, OFRR_F32, M, k, Bnd, M, out_dev));
   return OFRR_SUCCESS;
 }
@@ -523,14 +530,15 @@ int Op::prepare_abs(ofrr_ctx* ctx, ofrr_dtype t16) {
     int64_t lda;
     if (trans) OFRR_TRY(dense_as(ctx, t16, &Ap, &lda));
     else OFRR_TRY(dense_t_as(ctx, t16, &Ap, &lda));
-    void* w = ws_alloc(ctx, (size_t)K * M * 2, &st);
+    const int64_t ldK = (K + 7) & ~int64_t(7);
+    void* w = ws_alloc(ctx, (size_t)ldK * M * 2, &st);
     if (!w) return st;
     if (t16 == OFRR_F16)
       k_abs_cast<__half, __half><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(K, M, (const __half*)Ap, lda,
-                                                                               (__half*)w, K);
+                                                                               (__half*)w, ldK);
     else
       k_abs_cast<__nv_bfloat16, __nv_bfloat16><<<grid_2d(K, M, 256), 256, 0, ctx->stream>>>(
-          K, M, (const __nv_bfloat16*)Ap, lda, (__nv_bfloat16*)w, K);
+          K, M, (const __nv_bfloat16*)Ap, lda, (__nv_bfloat16*)w, ldK);
     OFRR_LAUNCHED(ctx, "k_abs_cast");
     absA[trans] = w;
   }
