@@ -6,8 +6,10 @@
 // overlap on the GPU.  Requests wait in a FIFO queue; admission charges each request an estimate of
 // its device workspace against an HBM budget, and a request starts only when its charge fits (the
 // head of the queue is never overtaken, so a large request cannot starve).  A worker whose cached
-// workspace exceeds its share of the budget releases it after a solve.  Results of a request do not
-// depend on what else runs: every kernel of the library reduces in a fixed order.
+// workspace exceeds its share of the budget releases it after a solve.  The library's own kernels reduce
+// in a fixed order; a request's result in the mix matches its result alone bit for bit on small solves
+// and within its tolerance on large dense SVDs (whose certification fallback and FP64 continuation use
+// the library GEMM), where the last bits can differ.
 //
 // Batched form (ofrr_batch_si_eig): submit every problem, then wait for all of them.
 #include <algorithm>

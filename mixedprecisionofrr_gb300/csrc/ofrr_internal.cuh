@@ -506,11 +506,12 @@ int geig_dev(ofrr_ctx* ctx, int n, const double* G, int ldg, const double* M, in
 // eig(C) for a nonsymmetric n x n C (n <= 128), FP32 Hessenberg-QR: real/imaginary parts, eigenvectors
 // (real parts, unit norm), unsorted
 int nonsym_eig_dev(ofrr_ctx* ctx, int n, const double* C, double* wr, double* wi, double* X, bool refine,
-                   bool pair_imag = false);
+                   bool pair_imag = false, bool values_only = false);
 // eig(G, M) for nonsymmetric G, SPD M (or M null): real parts descending, unit real-part eigenvectors;
 // refine = FP64 Newton steps on the real pairs (for FP32/FP64 bases)
+// values_only: lam alone (FP32 Hessenberg-QR without vectors; U is not written)
 int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U, bool refine,
-                bool pair_imag = false);
+                bool pair_imag = false, bool values_only = false);
 // Y (n x p, ld n): basis of the invariant subspace of the pencil (G, M) (M SPD) for its p eigenvalues
 // with real part above sigma (matrix sign function of L^-1 G L^-T - sigma I); n <= 96
 int invariant_subspace_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double sigma, int p,

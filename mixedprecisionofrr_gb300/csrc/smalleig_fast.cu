@@ -575,6 +575,7 @@ __global__ void __launch_bounds__(256) k_sort_desc(int n, const double* __restri
     lam_out[rank] = lam[i];
   }
   __syncthreads();
+  if (!W) return;  // values only
   for (int e0 = threadIdx.x; e0 < n * n; e0 += 16 * blockDim.x) {  // 16 loads per thread in flight
     double v[16];
 #pragma unroll
@@ -977,7 +978,7 @@ int ritz_from_invariant(ofrr_ctx* ctx, int n, const double* G, const double* M, 
 // U (ld n) the real parts of the eigenvectors, unit 2-norm.  M is reduced away with its FP64
 // Cholesky factor (C = L^-1 G L^-T, U = L^-T X); C is solved in FP32 (smalleig_nonsym.cu).
 int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* lam, double* U, bool refine,
-                bool pair_imag) {
+                bool pair_imag, bool values_only) {
   if (n <= 0) return OFRR_SUCCESS;
   if (n > 128) return OFRR_ERR_BLAS_INVALID_SIZE;
   WsScope scope(ctx);
@@ -996,7 +997,12 @@ int geig_nonsym(ofrr_ctx* ctx, int n, const double* G, const double* M, double* 
     OFRR_TRY(trsm(ctx, n, n, L, Z, n, 1, C, 0));  // C = L^-1 Z' = L^-1 G L^-T
     Cs = C;
   }
-  OFRR_TRY(nonsym_eig_dev(ctx, n, Cs, wr, wi, X, refine, pair_imag));
+  OFRR_TRY(nonsym_eig_dev(ctx, n, Cs, wr, wi, X, refine, pair_imag, values_only));
+  if (values_only) {
+    k_sort_desc<<<1, 256, 0, ctx->stream>>>(n, wr, nullptr, lam, nullptr);
+    OFRR_LAUNCHED(ctx, "k_sort_desc");
+    return OFRR_SUCCESS;
+  }
   if (M) {
     OFRR_TRY(trsm(ctx, n, n, L, X, n, 0, W, 1));  // W = L^-T X
     k_unit_cols<<<(n + 3) / 4, 128, 0, ctx->stream>>>(n, W);

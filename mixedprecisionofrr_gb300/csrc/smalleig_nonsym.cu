@@ -40,7 +40,9 @@ __device__ __forceinline__ void cdivf(T xr, T xi, T yr, T yi, T& cr, T& ci) {
 
 // One warp.  C: n x n (FP64, ld ldc).  Outputs: wr, wi (n), X (n x n, FP64, ld n): eigenvectors of C
 // (real parts, unit norm), unsorted; *flag = 1 when the QR iteration did not converge.
-template <class T>
+// VEC = false: eigenvalues only (EISPACK hqr instead of hqr2): no transformations accumulated, the QR
+// sweeps restricted to the active block, no eigenvectors (X is not written)
+template <class T, bool VEC = true>
 __global__ void __launch_bounds__(32) k_nonsym_eig(int nn, const double* __restrict__ C, int ldc,
                                                        double* __restrict__ wr, double* __restrict__ wi,
                                                        double* __restrict__ X, int* __restrict__ flag,
@@ -107,7 +109,7 @@ __global__ void __launch_bounds__(32) k_nonsym_eig(int nn, const double* __restr
     __syncwarp();
   }
   // accumulate the transformations (the reflectors below the subdiagonal and in ort)
-  for (int m = high - 1; m >= low + 1; --m) {
+  for (int m = high - 1; VEC && m >= low + 1; --m) {
     if (HH(m, m - 1) == T(0.)) continue;
     for (int i = m + 1 + lane; i <= high; i += 32) ort[i] = HH(i, m - 1);
     __syncwarp();
@@ -185,18 +187,18 @@ __global__ void __launch_bounds__(32) k_nonsym_eig(int nn, const double* __restr
           e[n - 1] = T(0.);
           e[n] = T(0.);
         }
-        for (int j = n - 1 + lane; j < nn; j += 32) {  // row modification
+        for (int j = n - 1 + lane; VEC && j < nn; j += 32) {  // row modification
           const T zz = HH(n - 1, j);
           HH(n - 1, j) = q * zz + p * HH(n, j);
           HH(n, j) = q * HH(n, j) - p * zz;
         }
         __syncwarp();
-        for (int i = lane; i <= n; i += 32) {  // column modification
+        for (int i = lane; VEC && i <= n; i += 32) {  // column modification
           const T zz = HH(i, n - 1);
           HH(i, n - 1) = q * zz + p * HH(i, n);
           HH(i, n) = q * HH(i, n) - p * zz;
         }
-        for (int i = low + lane; i <= high; i += 32) {  // accumulate
+        for (int i = low + lane; VEC && i <= high; i += 32) {  // accumulate
           const T zz = VV(i, n - 1);
           VV(i, n - 1) = q * zz + p * VV(i, n);
           VV(i, n) = q * VV(i, n) - p * zz;
@@ -301,7 +303,8 @@ __global__ void __launch_bounds__(32) k_nonsym_eig(int nn, const double* __restr
         r = r / p;
         __syncwarp();
         if (lane == 0 && set_hk) HH(k, k - 1) = hk;
-        for (int j = k + lane; j < nn; j += 32) {  // row modification
+        const int jmax = VEC ? nn - 1 : n;  // values only: the active block's columns
+        for (int j = k + lane; j <= jmax; j += 32) {  // row modification
           T pp = HH(k, j) + q * HH(k + 1, j);
           if (notlast) {
             pp += r * HH(k + 2, j);
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(32) k_nonsym_eig(int nn, const double* __restr
         }
         __syncwarp();
         const int imax = (n < k + 3) ? n : k + 3;
-        for (int i = lane; i <= imax; i += 32) {  // column modification
+        for (int i = (VEC ? 0 : l) + lane; i <= imax; i += 32) {  // column modification
           T pp = x * HH(i, k) + y * HH(i, k + 1);
           if (notlast) {
             pp += z * HH(i, k + 2);
@@ -321,7 +324,7 @@ __global__ void __launch_bounds__(32) k_nonsym_eig(int nn, const double* __restr
           HH(i, k) -= pp;
           HH(i, k + 1) -= pp * q;
         }
-        for (int i = low + lane; i <= high; i += 32) {  // accumulate
+        for (int i = low + lane; VEC && i <= high; i += 32) {  // accumulate
           T pp = x * VV(i, k) + y * VV(i, k + 1);
           if (notlast) {
             pp += z * VV(i, k + 2);
@@ -340,10 +343,17 @@ __global__ void __launch_bounds__(32) k_nonsym_eig(int nn, const double* __restr
       wr[i] = 0.0;
       wi[i] = 0.0;
     }
-    for (int idx = lane; idx < nn * nn; idx += 32) X[idx] = 0.0;
+    for (int idx = lane; VEC && idx < nn * nn; idx += 32) X[idx] = 0.0;
     return;
   }
   __syncwarp();
+  if (!VEC) {
+    for (int j = lane; j < nn; j += 32) {
+      wr[j] = (double)d[j];
+      wi[j] = (double)e[j];
+    }
+    return;
+  }
   // ---- eigenvectors of the quasi-triangular factor: one lane per eigenvalue ----
   if (norm != T(0.)) {
     for (int nv = nn - 1 - lane; nv >= 0; nv -= 32) {
@@ -623,9 +633,16 @@ __global__ void k_frob(int n, const double* __restrict__ C, double* __restrict__
 // eig(C) for a nonsymmetric n x n C (FP64, ld n): wr/wi (n), X (n x n, ld n), unsorted.  refine: FP64
 // Newton steps on the real pairs (FP64 bases); without it the pairs are FP32-accurate.
 int nonsym_eig_dev(ofrr_ctx* ctx, int n, const double* C, double* wr, double* wi, double* X, bool refine,
-                   bool pair_imag) {
+                   bool pair_imag, bool values_only) {
   if (n <= 0) return OFRR_SUCCESS;
   if (n > NS_MAX) return OFRR_ERR_BLAS_INVALID_SIZE;
+  if (values_only) {  // FP32 eigenvalues (no vectors, no refinement)
+    const size_t smem = ((size_t)3 * n * (n + 1) + 3 * (size_t)n) * sizeof(float);
+    OFRR_TRY(allow_smem(k_nonsym_eig<float, false>));
+    k_nonsym_eig<float, false><<<1, 32, smem, ctx->stream>>>(n, C, n, wr, wi, X, ctx->dev_flags + 3, 0);
+    OFRR_LAUNCHED(ctx, "k_nonsym_eig_values_f32");
+    return OFRR_SUCCESS;
+  }
   // refine: the whole Hessenberg-QR in FP64 when it fits in shared memory (backward stable to FP64; the
   // Newton refinement below cannot separate clustered eigenvalues from an FP32 start), else FP32 + Newton
   const size_t smem64 = ((size_t)3 * n * (n + 1) + 3 * (size_t)n) * sizeof(double);

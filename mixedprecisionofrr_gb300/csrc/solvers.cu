@@ -1136,7 +1136,7 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
       // pairs come in FP64 from the invariant subspace below (restricted pencil)
       const bool restricted = !symmetric && t == OFRR_F64 && ncols <= 96;
       if (symmetric) OFRR_TRY(geig_fast(ctx, ncols, G, M, 0.0, d, U, t == OFRR_F64 ? 2 : 1));
-      else OFRR_TRY(geig_nonsym(ctx, ncols, G, M, d, U, t == OFRR_F64 && !restricted, true));
+      else OFRR_TRY(geig_nonsym(ctx, ncols, G, M, d, U, t == OFRR_F64 && !restricted, true, restricted));
       OFRR_CUDA(cudaMemcpyAsync(hd.data(), d, sizeof(double) * ncols, cudaMemcpyDeviceToHost, ctx->stream));
       OFRR_TRY(sync_and_check(ctx));
       k = std::min(nev, ncols);
