@@ -563,6 +563,22 @@ def c3_run(api, steps, warmup, cpu=True):
         us, by = api.profile_krylov_step(Acsr, prec, i, reps=20)
         roof[f"{prec}_i{i}"] = {"us": us, "bytes": by, "GBps": by / us / 1e3, "frac": by / us / 1e3 / hbm}
     out["roofline_krylov_step"] = roof
+    # the Rayleigh-Ritz SpMM of the FP64 phase: A times the 65 FP64 basis columns (live CUDA events, 5 launches)
+    Xs = api.randn(13, A.shape[0], C3_KDIM + 1, "double")
+    api.csrmv(Acsr, "N", Xs, "double")
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(5):
+        Ys = api.csrmv(Acsr, "N", Xs, "double")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_sp = e0.elapsed_time(e1) / 5 * 1e-3
+    nrhs = C3_KDIM + 1
+    by_sp = A.nnz * 12 + (A.shape[0] + 1) * 4 + A.shape[0] * nrhs * 16
+    out["roofline_spmm"] = {"kernel": f"k_csrmm_n FP64, {nrhs} right-hand sides", "us": t_sp * 1e6, "bytes": by_sp,
+                            "GBps": by_sp / t_sp / 1e9, "frac": by_sp / t_sp / 1e9 / hbm}
+    del Xs, Ys
     if cpu:
         secs, sample = c3_cpu_sample(A, out["matvecs"], out["cycles"])
         out["cpu_baseline"] = {"value": C3_NEV / secs, "unit": "eigenpairs/s", "cores": os.cpu_count(),

@@ -701,7 +701,7 @@ def debug_invariant_subspace(G, M, sigma: float, p: int) -> np.ndarray:
     return to_numpy(Y)
 
 
-def batch_sym_eig(A_packed, ns, offsets, nev: int = 8, block: int = 16, tol: float = 1e-7, step_size: int = 2,
+def batch_sym_eig(A_packed, ns, offsets, nev: int = 8, block: int = 16, tol: float = 1e-7, step_size: int = 6,
                   maxiter: int = 500, p_output: str = "bfloat16", seed: int = 42, return_latency: bool = False):
     """Batched dense symmetric eigensolves in one persistent launch (ofrr_batch_sym_eig).  A_packed: FP64
     device tensor holding every matrix column-major at its element offset.  Returns (X list of device

@@ -35,10 +35,14 @@ __global__ void __launch_bounds__(kSpmmRows) k_csrmm_n(int64_t nrows, const int3
                                                        const int32_t* __restrict__ indices,
                                                        const TC* __restrict__ vals, int64_t nrhs,
                                                        const TX* __restrict__ X, int64_t ldx, TY* __restrict__ Y,
-                                                       int64_t ldy) {
+                                                       int64_t ldy, int nchunks) {
   __shared__ TC s_val[kSpmmCap];
   __shared__ int32_t s_idx[kSpmmCap];
-  const int64_t r0 = (int64_t)blockIdx.x * kSpmmRows;
+  // CTA b: row block b / nchunks, right-hand sides [RC (b % nchunks), ...) -- the CTAs of one row block are
+  // adjacent, so the block's nonzeros are read from HBM once and from L2 by the others
+  const int64_t r0 = (int64_t)(blockIdx.x / nchunks) * kSpmmRows;
+  const int64_t cbeg = (nchunks > 1) ? (int64_t)(blockIdx.x % nchunks) * RC : 0;
+  const int64_t cend = (nchunks > 1) ? min(nrhs, cbeg + RC) : nrhs;
   if (r0 >= nrows) return;
   const int64_t rend = min(nrows, r0 + kSpmmRows);
   const int32_t pbase = __ldg(indptr + r0), pend = __ldg(indptr + rend);
@@ -53,7 +57,7 @@ __global__ void __launch_bounds__(kSpmmRows) k_csrmm_n(int64_t nrows, const int3
   const int64_t row = r0 + threadIdx.x;
   if (row >= rend) return;
   const int32_t p0 = __ldg(indptr + row), p1 = __ldg(indptr + row + 1);
-  for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
+  for (int64_t c0 = cbeg; c0 < cend; c0 += RC) {
     TC acc[RC];
 #pragma unroll
     for (int r = 0; r < RC; ++r) acc[r] = TC(0);
@@ -62,12 +66,12 @@ __global__ void __launch_bounds__(kSpmmRows) k_csrmm_n(int64_t nrows, const int3
       const TC a = staged ? s_val[p - pbase] : __ldg(vals + p);
 #pragma unroll
       for (int r = 0; r < RC; ++r) {
-        if (c0 + r < nrhs) acc[r] = fma(a, to_c<TC, TX>(X[col + (c0 + r) * ldx]), acc[r]);
+        if (c0 + r < cend) acc[r] = fma(a, to_c<TC, TX>(X[col + (c0 + r) * ldx]), acc[r]);
       }
     }
 #pragma unroll
     for (int r = 0; r < RC; ++r)
-      if (c0 + r < nrhs) Y[row + (c0 + r) * ldy] = from_c<TY, TC>(acc[r]);
+      if (c0 + r < cend) Y[row + (c0 + r) * ldy] = from_c<TY, TC>(acc[r]);
   }
 }
 
@@ -208,21 +212,23 @@ int csr_transpose_impl(ofrr_ctx* ctx, const ofrr_csr* A, ofrr_csr* At) {
 static int csrmm_n(ofrr_ctx* ctx, const ofrr_csr* A, ofrr_dtype tx, ofrr_dtype tc, ofrr_dtype ty, int64_t nrhs,
                    const void* X, int64_t ldx, void* Y, int64_t ldy) {
   const int64_t blocks = (A->nrows + kSpmmRows - 1) / kSpmmRows;
-  if (blocks > 0x7fffffffLL) return OFRR_ERR_BLAS_INVALID_SIZE;
-  const unsigned grid = (unsigned)blocks;
+  // many right-hand sides: one CTA per (row block, 8-column chunk), for more loads in flight per SM
+  const int nchunks = (nrhs > 8) ? (int)((nrhs + 7) / 8) : 1;
+  if (blocks * nchunks > 0x7fffffffLL) return OFRR_ERR_BLAS_INVALID_SIZE;
+  const unsigned grid = (unsigned)(blocks * nchunks);
   OFRR_DISPATCH_COMPUTE(tc, TC, {
     const TC* vals = CsrVals<TC>::get(A);
     if (!vals) return OFRR_ERR_INVALID_ARGUMENT;
     OFRR_DISPATCH_STORAGE(tx, TX, OFRR_DISPATCH_STORAGE(ty, TY, {
       if (nrhs == 1) {
         k_csrmm_n<TX, TC, TY, 1><<<grid, kSpmmRows, 0, ctx->stream>>>(A->nrows, A->indptr, A->indices, vals, nrhs,
-                                                                      (const TX*)X, ldx, (TY*)Y, ldy);
+                                                                      (const TX*)X, ldx, (TY*)Y, ldy, nchunks);
       } else if (nrhs <= 4) {
         k_csrmm_n<TX, TC, TY, 4><<<grid, kSpmmRows, 0, ctx->stream>>>(A->nrows, A->indptr, A->indices, vals, nrhs,
-                                                                      (const TX*)X, ldx, (TY*)Y, ldy);
+                                                                      (const TX*)X, ldx, (TY*)Y, ldy, nchunks);
       } else {
         k_csrmm_n<TX, TC, TY, 8><<<grid, kSpmmRows, 0, ctx->stream>>>(A->nrows, A->indptr, A->indices, vals, nrhs,
-                                                                      (const TX*)X, ldx, (TY*)Y, ldy);
+                                                                      (const TX*)X, ldx, (TY*)Y, ldy, nchunks);
       }
       OFRR_LAUNCHED(ctx, "k_csrmm_n");
     }));
