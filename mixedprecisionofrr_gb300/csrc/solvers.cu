@@ -10,6 +10,7 @@
 #include "ofrr_internal.cuh"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -1066,6 +1067,7 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
   int cycles = 0, steps = 0, nmv = 0, escalations = 0, ncols = 0, in_phase = 0, k = std::min(nev, nb);
   double best_in_phase = INFINITY, last_maxres = INFINITY, best64 = INFINITY;
   int stall64 = 0;
+  std::array<double, 16> hist64{};  // the FP64 phase's last 16 residuals
   bool converged = false, exact_rr = false;
   const bool kry_debug = getenv("OFRR_KRYLOV_DEBUG") != nullptr;  // per-cycle progress on stderr
   while (true) {
@@ -1202,8 +1204,8 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
     for (int j = 0; j < k; ++j) maxres = std::max(maxres, hres[j]);
     last_maxres = maxres;
     if (kry_debug)
-      fprintf(stderr, "[ofrr krylov] cycle %d phase %d type %d q %d ncols %d pp %d sign %d maxres %.3e d0 %.10e\n",
-              cycles, phase, (int)t, q, ncols, pp, sign_ok ? 1 : 0, maxres, hd[0]);
+      fprintf(stderr, "[ofrr krylov] cycle %d phase %d exact %d type %d q %d ncols %d pp %d sign %d maxres %.3e d0 %.10e\n",
+              cycles, phase, exact_rr ? 1 : 0, (int)t, q, ncols, pp, sign_ok ? 1 : 0, maxres, hd[0]);
     if (opt->tol > 0 && maxres <= opt->tol) {
       converged = true;
       break;
@@ -1214,32 +1216,47 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
     const double switch_at = (t == OFRR_BF16) ? 1e-2 : 1e-3;
     const bool stalled = in_phase >= 3 && maxres > 0.7 * best_in_phase;
     best_in_phase = std::min(best_in_phase, maxres);
-    // FP64 phase: no 2x gain over 16 cycles is the emulated products' floor -- FP64 products from here on
-    // (a slowly converging solve gains 2x in a few cycles; a floor does not move)
-    if (maxres < 0.5 * best64) {
+    // FP64 phase: a floor of the emulated products -- FP64 products from here on.  A floor is flat: the
+    // last 16 residuals within 2x of each other (a clustered spectrum's slow convergence swings by 10x
+    // from cycle to cycle and is not a floor), and no gain over them -- 10 % for symmetric operators
+    // (clustered spectra give ill-conditioned Hessenberg bases, whose emulated products then stall the
+    // solve well above tol; below 1e-4), 2x for nonsymmetric ones (they gain slowly but steadily, and
+    // FP64 Grams cost ~50 ms per cycle at two million rows; below 1e-6)
+    const double gain = symmetric ? 0.9 : 0.5;
+    if (maxres < gain * best64) {
       best64 = maxres;
       stall64 = 0;
     } else {
       ++stall64;
     }
-    if (mixed && phase == 1 && stall64 >= 16 && !exact_rr && maxres < 1e-6) {
-      exact_rr = true;
-      stall64 = 0;
+    hist64[in_phase % 16] = maxres;
+    double wmin = INFINITY, wmax = 0.0;
+    for (double v : hist64) {
+      wmin = std::min(wmin, v);
+      wmax = std::max(wmax, v);
     }
-    if (mixed && phase == 0 && (maxres <= switch_at || stalled)) {
+    const bool to_exact = mixed && phase == 1 && !exact_rr && stall64 >= 16 && in_phase >= 16 &&
+                          wmax <= 2.0 * wmin && maxres < (symmetric ? 1e-4 : 1e-6);
+    const bool to_f64 = mixed && phase == 0 && (maxres <= switch_at || stalled);
+    if (to_f64 || to_exact) {
+      // a restart from one vector, the sum of the unit Ritz vectors: a thick restart carries the error
+      // of the Krylov relation A [Yc] = [Yc, f] H of the cycle before (the 16-bit basis's rounding, or
+      // the emulated products' floor) into every later cycle, so the residuals could not fall below it;
+      // one vector starts an exact Krylov relation in the new arithmetic
       OFRR_TRY(column_norms(ctx, tw, n, k, Wb, ld, nrm));
       OFRR_TRY(kry_sum_unit_cols(ctx, tw, n, k, Wb, ld, nrm, svec));
       OFRR_CUDA(cudaMemcpyAsync(Wb, svec, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
       tw = OFRR_F64;
       blk = Wb;
       q0 = 1;
+      if (to_exact) exact_rr = true;
       phase = 1;
       in_phase = 0;
       best_in_phase = INFINITY;
       best64 = INFINITY;
       stall64 = 0;
       escalations++;
-      OFRR_TRY(kry_state_init(ctx, &S, &A->csr, OFRR_F64, nb, stol));
+      if (to_f64) OFRR_TRY(kry_state_init(ctx, &S, &A->csr, OFRR_F64, nb, stol));
     } else {
       blk = (char*)Wb + (size_t)k * ld * dtype_size(tw);
       q0 = pp + 1;
