@@ -707,6 +707,9 @@ def c5_run(api, count, time_scale, parity_every=25):
                        "within_tol": bool(rel <= req.tol)})
     for r in recs:
         r.pop("values", None)
+    # one row per request: index, kind, n, k, tol, status, solve ms, latency ms, max residual
+    rows = [[r["idx"], r["kind"], r["n"], r["k"], r["tol"], r["status"], round(r["solve_ms"], 1),
+             round(r["latency_ms"], 1), float("%.3g" % r["max_residual"])] for r in sorted(recs, key=lambda r: r["idx"])]
     kinds = {}
     for r in recs:
         kk = kinds.setdefault(r["kind"], {"count": 0, "ok": 0, "lat": []})
@@ -719,7 +722,9 @@ def c5_run(api, count, time_scale, parity_every=25):
     out.update({"metric": "serving stream: requests/s, converged eigen/singular pairs/s, p50/p99 latency "
                           "(arrival to completion)", "stream": {"seed": 2024, "requests": count, "rate_req_s": 2000,
                                                                 "time_scale": time_scale},
-                "by_kind": kinds, "parity_sample": parity})
+                "by_kind": kinds, "parity_sample": parity,
+                "request_rows": {"columns": ["idx", "kind", "n", "k", "tol", "status", "solve_ms", "latency_ms",
+                                             "max_residual"], "rows": rows}})
     return out
 
 

@@ -1237,6 +1237,10 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
     }
     const bool to_exact = mixed && phase == 1 && !exact_rr && stall64 >= 16 && in_phase >= 16 &&
                           wmax <= 2.0 * wmin && maxres < (symmetric ? 1e-4 : 1e-6);
+    // a floor of the FP64 products themselves (the basis's conditioning): no gain over 32 cycles and the
+    // last 16 residuals within 10 % of each other (a plateau of a clustered spectrum's convergence moves
+    // more) -- the step budget cannot lower it, so the solve ends here (not converged, best pairs returned)
+    if (exact_rr && stall64 >= 32 && in_phase >= 32 && wmax <= 1.1 * wmin) break;
     const bool to_f64 = mixed && phase == 0 && (maxres <= switch_at || stalled);
     if (to_f64 || to_exact) {
       // a restart from one vector, the sum of the unit Ritz vectors: a thick restart carries the error
