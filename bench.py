@@ -576,8 +576,13 @@ def c3_run(api, steps, warmup, cpu=True):
     t_sp = e0.elapsed_time(e1) / 5 * 1e-3
     nrhs = C3_KDIM + 1
     by_sp = A.nnz * 12 + (A.shape[0] + 1) * 4 + A.shape[0] * nrhs * 16
+    # the FP64 kernel's bound is GB300's FP64 pipe, not HBM: nnz * nrhs FMAs against 1.68 FMA per clock per
+    # SM (stand-alone probe) x 152 SMs x 2070 MHz
+    fma_peak = 152 * 1.68 * 2.070e9
     out["roofline_spmm"] = {"kernel": f"k_csrmm_n FP64, {nrhs} right-hand sides", "us": t_sp * 1e6, "bytes": by_sp,
-                            "GBps": by_sp / t_sp / 1e9, "frac": by_sp / t_sp / 1e9 / hbm}
+                            "GBps": by_sp / t_sp / 1e9, "frac": by_sp / t_sp / 1e9 / hbm,
+                            "fp64_fma": A.nnz * nrhs, "fp64_fma_peak_per_s": fma_peak,
+                            "fp64_fma_frac": A.nnz * nrhs / t_sp / fma_peak}
     del Xs, Ys
     if cpu:
         secs, sample = c3_cpu_sample(A, out["matvecs"], out["cycles"])
