@@ -28,7 +28,7 @@ sys.path.insert(0, str(ROOT))
 
 M_ROWS, N_COLS, NEV, TOL = 8192, 2048, 32, 1e-8
 BLOCK, STEP, MAXITER = 64, 8, 80  # defaults (the reference arm's); main() autotunes each GPU path
-CFG = {"mixed": (BLOCK, STEP), "fp64": (BLOCK, STEP)}
+CFG = {"mixed": (BLOCK, STEP, 0), "fp64": (BLOCK, STEP, 0)}  # block, power steps, FP64-phase steps (0: same)
 METRIC = "converged singular triplets/s at residual <= 1e-8 (dense 8192x2048 geometric-spectrum SVD, top 32)"
 UNIT = "triplets/s"
 
@@ -60,8 +60,9 @@ def parse():
     ap.add_argument("--time-scale", type=float, default=1.0,
                     help="c5: arrival times multiplied by this (1 = the stream's 2000 req/s)")
     ap.add_argument("--no-c3", action="store_true", help="skip the C3 leg of the default run")
-    ap.add_argument("--mixed-config", default=None, metavar="B,S",
-                    help="block width and power steps of the mixed path instead of the autotuner's choice")
+    ap.add_argument("--mixed-config", default=None, metavar="B,S[,S64]",
+                    help="block width, power steps (and FP64-phase power steps) of the mixed path instead of the "
+                         "autotuner's choice")
     return ap.parse_args()
 
 
@@ -153,10 +154,10 @@ def flush_l2(buf):
 
 
 def run_solver(api, A, mode, V0=None, fp8=False):
-    b, st = CFG.get(mode, (BLOCK, STEP))
+    b, st, st64 = CFG.get(mode, (BLOCK, STEP, 0))
     return api.subspace_iter_svd(A, M_ROWS, N_COLS, b, "single", "half", maxiter=MAXITER, step_size=st,
                                  mode=mode, tol=TOL, nev=NEV, check_every=1, V0=V0, generalized_tol=0.0,
-                                 power_fp8=fp8)
+                                 power_fp8=fp8, step_size_f64=st64)
 
 
 def time_solves(api, A, mode, steps, warmup, flush_buf, fp8=False):
@@ -191,7 +192,7 @@ def time_e2e(api, A_host_pinned, steps, warmup):
 
     ctx = api.context()
     stream = torch.cuda.current_stream()
-    BLOCK, STEP = CFG["mixed"]
+    BLOCK, STEP, STEP64 = CFG["mixed"]
     A_dev = api.empty_cm(M_ROWS, N_COLS, L.F64)
     U_dev = api.empty_cm(M_ROWS, BLOCK, L.F64)
     V_dev = api.empty_cm(N_COLS, BLOCK, L.F64)
@@ -206,7 +207,7 @@ def time_e2e(api, A_host_pinned, steps, warmup):
     o = api.options(mode=L.MODE_MIXED, maxiter=MAXITER, step_size=STEP, block=BLOCK, nev=NEV, tol=TOL,
                     use_generalized=1, generalized_tol=0.0, seed=42, check_every=1, p_compute="single",
                     p_output="half", p_hess_compute="single", p_hess_output="half", p_rr_compute="single",
-                    p_rr_output="single")
+                    p_rr_output="single", step_size_f64=STEP64)
     lib = ctx.lib
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
 
@@ -344,7 +345,7 @@ def orth_compare_run(api, A, reps=3):
             ms_b, _ = timed(lambda: api.lu_basis(X, "double", "double"))
         else:
             ms_b, _ = timed(lambda: api.gs_basis(X, orth == "cgs", "double", "double"))
-        b, st = CFG.get("fp64", (BLOCK, STEP))
+        b, st, _ = CFG.get("fp64", (BLOCK, STEP, 0))
         ms_s, out = timed(lambda: api.subspace_iter_svd(A, M_ROWS, N_COLS, b, "double", "double", maxiter=MAXITER,
                                                         step_size=st, mode="fp64", tol=TOL, nev=NEV, orth=orth))
         info = out[3]
@@ -857,7 +858,7 @@ def main():
         return
     if args.profile_solve:
         if args.mixed_config:
-            CFG["mixed"] = tuple(int(x) for x in args.mixed_config.split(","))
+            CFG["mixed"] = tuple(int(x) for x in (args.mixed_config + ",0").split(",")[:3])
         run_solver(api, A, "mixed")
         torch.cuda.synchronize()
         U, s, V, info = run_solver(api, A, "mixed")
@@ -870,14 +871,15 @@ def main():
     tune = {}
     for mode in ("mixed",) + (() if args.no_fp64 else ("fp64",)):
         if mode == "mixed" and args.mixed_config:
-            b, st = (int(x) for x in args.mixed_config.split(","))
-            CFG[mode] = (b, st)
-            tune[mode] = {"block": b, "step_size": st, "fixed": True}
+            b, st, st64 = (int(x) for x in (args.mixed_config + ",0").split(",")[:3])
+            CFG[mode] = (b, st, st64)
+            tune[mode] = {"block": b, "step_size": st, "step_size_f64": st64, "fixed": True}
             continue
         t = api.autotune_svd(A, M_ROWS, N_COLS, NEV, TOL, mode=mode, blocks=(64, 96, 128), steps=(4, 6, 8),
                              reps=1 if mode == "fp64" else 3, maxiter=MAXITER)
-        CFG[mode] = (t["block"], t["step_size"])
-        tune[mode] = {"block": t["block"], "step_size": t["step_size"], "candidates": len(t["table"])}
+        CFG[mode] = (t["block"], t["step_size"], t["step_size_f64"])
+        tune[mode] = {"block": t["block"], "step_size": t["step_size"], "step_size_f64": t["step_size_f64"],
+                      "candidates": len(t["table"])}
         for row in t["table"]:
             print(f"autotune {mode}: {row}", file=sys.stderr)
     # mixed path (the product) -----------------------------------------------------------------
@@ -965,7 +967,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f16 basis / f32 accumulate / f64 pencil",
             "data": "synthetic (seeded Haar U, V; geometric s 1..1e-6)",
             "config": bench_config(world),
-            "tuning": {"gpu_mixed": {"block": CFG["mixed"][0], "step_size": CFG["mixed"][1]}, "gpu_autotune": tune,
+            "tuning": {"gpu_mixed": {"block": CFG["mixed"][0], "step_size": CFG["mixed"][1],
+                                     "step_size_f64": CFG["mixed"][2]}, "gpu_autotune": tune,
                        "cpu": cpu_tuning},
             "p50_ms": 1e3 * float(np.percentile(times, 50)), "p99_ms": 1e3 * float(np.percentile(times, 99)),
             "iterations": iters, "max_residual": maxres, "max_rel_sigma_err": err, "status": statuses,

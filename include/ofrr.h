@@ -305,6 +305,11 @@ typedef struct {
    * steps multiply E4M3 copies of A (per-row power-of-two scales, made once per solve) and of the basis
    * block (per column) on the tensor cores (kind::f8f6f4, FP32 accumulation); 0 = 16-bit products. */
   int power_fp8;
+  /* OFRR_MODE_MIXED si_svd / si_eig: power steps per outer iteration of the FP64 phase; 0 = step_size.
+   * The FP64 phase starts from 16-bit-accurate vectors, and each of its outer iterations carries a
+   * Hessenberg basis, a Rayleigh-Ritz and a certified check: more steps per iteration there means fewer
+   * of them for the same number of power steps (new behaviour; the reference has one step_size). */
+  int step_size_f64;
 } ofrr_options;
 
 typedef struct {

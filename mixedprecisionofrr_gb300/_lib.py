@@ -46,7 +46,7 @@ class ofrr_options(C.Structure):
         ("use_start_block", C.c_int), ("orth", C.c_int), ("reorth", C.c_int),
         ("p_compute", C.c_int), ("p_output", C.c_int), ("p_hess_compute", C.c_int),
         ("p_hess_output", C.c_int), ("p_rr_compute", C.c_int), ("p_rr_output", C.c_int),
-        ("check_every", C.c_int), ("restart_keep", C.c_int), ("power_fp8", C.c_int),
+        ("check_every", C.c_int), ("restart_keep", C.c_int), ("power_fp8", C.c_int), ("step_size_f64", C.c_int),
     ]
 
 

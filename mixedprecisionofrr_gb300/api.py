@@ -563,7 +563,7 @@ def subspace_iter_eig(A, n: int, k: int, precision_compute="double", precision_o
                       maxiter: int = 5, step_size: int = 1, precision_hess_compute=None, precision_hess_output=None,
                       precision_rr_compute=None, precision_rr_output=None, use_generalized=True,
                       generalized_tol=0.0, select_tol=None, symmetric=None, V0=None, mode="reference",
-                      tol=0.0, nev=None, check_every=1, orth="hessenberg"):
+                      tol=0.0, nev=None, check_every=1, orth="hessenberg", step_size_f64=0):
     """MATLAB/+src/+subspace/subspace_iter_eig.m; returns (V, d, info) with V on the device.  orth: the
     basis ("hessenberg"; "mgs" = the MATLAB file's default function_orth; "cgs"; "lu")."""
     ctx = context()
@@ -573,6 +573,7 @@ def subspace_iter_eig(A, n: int, k: int, precision_compute="double", precision_o
                 tol=tol, use_generalized=int(use_generalized), generalized_tol=generalized_tol,
                 select_tol=-1.0 if select_tol is None else select_tol, seed=seed,
                 use_start_block=int(V0 is not None), check_every=check_every, orth=ORTH[orth],
+                step_size_f64=step_size_f64,
                 **_prec_opts(precision_compute, precision_output, precision_hess_compute, precision_hess_output,
                              precision_rr_compute, precision_rr_output))
     po = o.p_output if mode == "reference" else L.F64
@@ -592,10 +593,11 @@ def subspace_iter_svd(A, m: int, n: int, k: int, precision_compute="double", pre
                       maxiter: int = 5, step_size: int = 1, precision_hess_compute=None, precision_hess_output=None,
                       precision_rr_compute=None, precision_rr_output=None, use_generalized=True,
                       generalized_tol=0.0, select_tol=None, V0=None, mode="reference", tol=0.0, nev=None,
-                      check_every=1, orth="hessenberg", power_fp8=False):
+                      check_every=1, orth="hessenberg", power_fp8=False, step_size_f64=0):
     """MATLAB/+src/+subspace/subspace_iter_svd.m; returns (U, s, V, info) with U, V on the device.  orth:
     the basis of both blocks ("hessenberg", "mgs" or "cgs").  power_fp8 (mixed mode, dense A): the FP8
-    variant, E4M3 products in the 16-bit power steps."""
+    variant, E4M3 products in the 16-bit power steps.  step_size_f64 (mixed mode): power steps per outer
+    iteration of the FP64 phase (0: step_size)."""
     ctx = context()
     op = operator(A, False)
     modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
@@ -604,7 +606,7 @@ def subspace_iter_svd(A, m: int, n: int, k: int, precision_compute="double", pre
                 use_generalized=int(use_generalized), generalized_tol=generalized_tol,
                 select_tol=-1.0 if select_tol is None else select_tol, seed=seed,
                 use_start_block=int(V0 is not None), check_every=check_every, orth=ORTH[orth],
-                power_fp8=int(power_fp8),
+                power_fp8=int(power_fp8), step_size_f64=step_size_f64,
                 **_prec_opts(precision_compute, precision_output, precision_hess_compute, precision_hess_output,
                              precision_rr_compute, precision_rr_output))
     po = o.p_output if mode == "reference" else L.F64
@@ -794,12 +796,13 @@ class Server:
 
     def submit_si_svd(self, A, k: int, mode: str = "mixed", tol: float = 1e-8, nev: Optional[int] = None,
                       maxiter: int = 200, step_size: int = 4, p_output: str = "half", seed: int = 42,
-                      check_every: int = 1):
+                      check_every: int = 1, step_size_f64: int = 0):
         op = operator(A, False)
         modes = {"reference": L.MODE_REFERENCE, "mixed": L.MODE_MIXED, "fp64": L.MODE_FP64}
         b = min(k, op.m, op.n)
         o = options(mode=modes[mode], maxiter=maxiter, step_size=step_size, block=b, nev=nev or b, tol=tol, seed=seed,
-                    check_every=check_every, p_output=p_output if mode == "mixed" else None)
+                    check_every=check_every, p_output=p_output if mode == "mixed" else None,
+                    step_size_f64=step_size_f64)
         po = o.p_output if mode == "reference" else L.F64
         U = empty_cm(op.m, b, po)
         V = empty_cm(op.n, b, po)
@@ -917,7 +920,8 @@ def autotune_svd(A, m: int, n: int, nev: int, tol: float, mode: str = "mixed", b
                  steps=(4, 6, 8), reps: int = 2, min_block: int = 40, **kw):
     """Pick the block width and power-step count of subspace_iter_svd for this problem by timing
     each candidate solve (CUDA events on the library's stream, median of reps after one warm-up)
-    and keeping the fastest one that converges.  Returns {"block", "step_size", "ms", "iterations",
+    and keeping the fastest one that converges; in mixed mode then the FP64 phase's power steps
+    (step_size_f64, 0 = the same).  Returns {"block", "step_size", "step_size_f64", "ms", "iterations",
     "table"}; the table lists every candidate."""
     stream = torch.cuda.current_stream()
     table = []
@@ -952,6 +956,32 @@ def autotune_svd(A, m: int, n: int, nev: int, tol: float, mode: str = "mixed", b
                 best = {"block": b, "step_size": st, "ms": ms, "iterations": info.iterations}
     if best is None:
         raise RuntimeError("autotune_svd: no candidate converged")
+    best["step_size_f64"] = 0
+    if mode == "mixed":
+        # the FP64 phase's own power steps (its iterations start from 16-bit-accurate vectors and each
+        # carries a basis, a Rayleigh-Ritz and a certified check): step_size x 1, 1.5 and 2
+        b, st = best["block"], best["step_size"]
+        for s64 in sorted({st + st // 2, 2 * st} - {st}):
+            args = dict(maxiter=kw.get("maxiter", 80), step_size=st, step_size_f64=s64, mode=mode, tol=tol, nev=nev,
+                        check_every=kw.get("check_every", 1), generalized_tol=kw.get("generalized_tol", 0.0))
+            subspace_iter_svd(A, m, n, b, kw.get("precision_compute", "single"), kw.get("precision_output", "half"),
+                              **args)
+            ts = []
+            for _ in range(reps):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                U, s, V, info = subspace_iter_svd(A, m, n, b, kw.get("precision_compute", "single"),
+                                                  kw.get("precision_output", "half"), **args)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ms = float(np.median(ts))
+            ok = info.status == 0 and info.max_residual <= tol
+            table.append({"block": b, "step_size": st, "step_size_f64": s64, "ms": ms, "iterations": info.iterations,
+                          "converged": ok})
+            if ok and ms < best["ms"]:
+                best.update({"step_size_f64": s64, "ms": ms, "iterations": info.iterations})
     best["table"] = table
     best["tiles"] = tiles
     return best

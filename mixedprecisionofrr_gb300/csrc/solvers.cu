@@ -292,7 +292,8 @@ int basis_impl(ofrr_ctx* ctx, int orth, ofrr_dtype tin, ofrr_dtype tout, ofrr_dt
 int validate_options(const ofrr_options* o) {
   if (!o) return OFRR_ERR_INVALID_ARGUMENT;
   if (o->mode < 0 || o->mode > 2) return OFRR_ERR_INVALID_ARGUMENT;
-  if (o->maxiter < 0 || o->step_size < 1 || o->block < 1 || o->nev < 0 || o->restart_keep < 0)
+  if (o->maxiter < 0 || o->step_size < 1 || o->step_size_f64 < 0 || o->block < 1 || o->nev < 0 ||
+      o->restart_keep < 0)
     return OFRR_ERR_INVALID_ARGUMENT;
   if (o->orth != OFRR_ORTH_HESSENBERG && o->orth != OFRR_ORTH_MGS && o->orth != OFRR_ORTH_CGS &&
       o->orth != OFRR_ORTH_LU)
@@ -1848,9 +1849,11 @@ static int si_eig_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
         OFRR_TRY(op.prepare_sliced(ctx));
         if (dense) OFRR_TRY(op.prepare_abs(ctx, L.po));
       }
-      // certified checks in the FP64 phase (see si_svd)
+      // certified checks in the FP64 phase (see si_svd); its own power steps per iteration
+      ofrr_options o64 = *opt;
+      if (opt->step_size_f64 > 0) o64.step_size = opt->step_size_f64;
       ctx->emulate_f64 = dense;
-      st = eig_phase(ctx, op, all_f64(), opt, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d,
+      st = eig_phase(ctx, op, all_f64(), &o64, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d,
                      dense ? (int)L.po : -1);
       ctx->emulate_f64 = false;
       OFRR_TRY(st);
@@ -1858,7 +1861,7 @@ static int si_eig_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
         // the emulated products' floor is above tol: the last iterations with FP64 products
         TraceScope ts(ctx, "fp64.exact");
         escalations = 2;
-        OFRR_TRY(eig_phase(ctx, op, all_f64(), opt, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d));
+        OFRR_TRY(eig_phase(ctx, op, all_f64(), &o64, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d));
       }
     }
   } else {
@@ -1953,9 +1956,12 @@ static int si_svd_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
         if (dense) OFRR_TRY(op.prepare_abs(ctx, L.po));
       }
       // the FP64 phase's checks are certified (emulated residuals plus the bounds on the emulation
-      // errors, true FP64 residuals for the columns that miss only by the bound)
+      // errors, true FP64 residuals for the columns that miss only by the bound); the phase has its own
+      // power steps per iteration (step_size_f64)
+      ofrr_options o64 = *opt;
+      if (opt->step_size_f64 > 0) o64.step_size = opt->step_size_f64;
       ctx->emulate_f64 = dense;
-      st = svd_phase(ctx, op, all_f64(), opt, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d,
+      st = svd_phase(ctx, op, all_f64(), &o64, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d,
                      dense ? (int)L.po : -1);
       ctx->emulate_f64 = false;
       OFRR_TRY(st);
@@ -1963,7 +1969,7 @@ static int si_svd_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
         // the emulated products' floor is above tol: the last iterations with FP64 products
         TraceScope ts(ctx, "fp64.exact");
         escalations = 2;
-        OFRR_TRY(svd_phase(ctx, op, all_f64(), opt, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d));
+        OFRR_TRY(svd_phase(ctx, op, all_f64(), &o64, U, ldu, V, ldv, opt->maxiter - S.it, opt->tol, nev, 0.0, S, d));
       }
     }
   } else {

@@ -54,3 +54,4 @@ def test_status_strings_and_defaults(built_lib):
     # MATLAB defaults: maxiter 5, step 1, seed 42 (subspace_iter_eig.m:105-113)
     assert (o.maxiter, o.step_size, o.seed, o.use_generalized) == (5, 1, 42, 1)
     assert o.select_tol < 0  # eps(output precision) by default
+    assert o.step_size_f64 == 0  # the FP64 phase of the mixed mode takes step_size unless set

@@ -242,15 +242,17 @@ def test_si_svd_mixed_dense_certified(api, orc):
     assert np.all(r <= info.residuals[:16] * (1 + 1e-6) + 1e-15)
 
 
-@pytest.mark.parametrize("block,step", [(64, 6), (128, 8)])
-def test_si_svd_mixed_benchmark_size(api, orc, block, step):
+@pytest.mark.parametrize("block,step,step64", [(64, 6, 0), (128, 8, 0), (64, 6, 9)])
+def test_si_svd_mixed_benchmark_size(api, orc, block, step, step64):
     """The benchmark configuration itself: dense 8192 x 2048 geometric-spectrum SVD (seed 42, the bench's
-    problem), top 32 triplets, mixed mode, tol 1e-8, at two of the autotuner's block / power-step
-    choices.  The true FP64 residuals computed here with NumPy meet tol and are bounded by the reported
-    (certified) residuals; the singular values match the construction to 1e-9 relative."""
+    problem), top 32 triplets, mixed mode, tol 1e-8, at three of the autotuner's block / power-step
+    choices (the last with its own FP64-phase power steps).  The true FP64 residuals computed here with
+    NumPy meet tol and are bounded by the reported (certified) residuals; the singular values match the
+    construction to 1e-9 relative."""
     A, U, s, V = orc.dense_svd_problem(8192, 2048, seed=42, smin=1e-6)
     Ug, sg, Vg, info = api.subspace_iter_svd(A, 8192, 2048, block, "single", "half", maxiter=80, step_size=step,
-                                             mode="mixed", tol=1e-8, nev=32, check_every=1, generalized_tol=0.0)
+                                             mode="mixed", tol=1e-8, nev=32, check_every=1, generalized_tol=0.0,
+                                             step_size_f64=step64)
     assert info.status == 0, info
     assert np.allclose(sg[:32], s[:32], rtol=1e-9)
     r = orc.svd_residual_norms(A, api.to_numpy(Ug)[:, :32], sg[:32], api.to_numpy(Vg)[:, :32])
@@ -271,12 +273,14 @@ def test_si_svd_fp8_variant_certified(api, orc):
     assert np.max(r) <= 1e-8
 
 
-def test_si_eig_mixed_dense_certified(api, orc):
+@pytest.mark.parametrize("step64", [0, 9])
+def test_si_eig_mixed_dense_certified(api, orc, step64):
     """Dense symmetric 2048 x 2048 (Haar Q, log-uniform spectrum), mixed mode, tol 1e-8: eigenvalues,
-    true FP64 residuals and the certified residuals as an upper bound."""
+    true FP64 residuals and the certified residuals as an upper bound (FP64-phase power steps as the
+    16-bit phase's, and 9)."""
     A, lam = orc.dense_sym_problem(2048, seed=11)
     Vg, d, info = api.subspace_iter_eig(A, 2048, 48, "single", "half", maxiter=200, step_size=6, mode="mixed",
-                                       tol=1e-8, nev=8, check_every=1, symmetric=True)
+                                       tol=1e-8, nev=8, check_every=1, symmetric=True, step_size_f64=step64)
     assert info.status == 0, info
     assert np.allclose(d[:8], lam[:8], rtol=1e-9)
     X = api.to_numpy(Vg)[:, :8]
