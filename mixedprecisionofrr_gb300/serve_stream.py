@@ -117,7 +117,7 @@ LAP_STEP_BUDGET = 20_000
 def submit(server: "api.Server", req: Request, A):
     if req.kind == "svd":
         return server.submit_si_svd(A, max(req.k + 16, int(1.5 * req.k)), mode="mixed", tol=req.tol, nev=req.k,
-                                    maxiter=400, step_size=6, step_size_f64=9, seed=req.seed & 0xFFFFFFFF)
+                                    maxiter=400, step_size=6, step_size_f64=12, seed=req.seed & 0xFFFFFFFF)
     kdim = min(max(2 * req.k, req.k + 24), 127)
     return server.submit_arnoldi_eig(A, req.k, kdim=kdim, mode="mixed", tol=req.tol, maxiter=LAP_STEP_BUDGET,
                                      seed=req.seed & 0xFFFFFFFF)
