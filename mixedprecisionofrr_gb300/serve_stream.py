@@ -9,10 +9,11 @@ The stream (sizes and tolerances from the serving workload's description):
   [1e4, 1e6], grid sides N, N+1 (, N+2) so that no eigenvalue is exactly repeated, largest eigenvalues
   by the thick-restart Krylov solver (Krylov dimension max(2k, k + 24), at most 127);
 * k uniform in [4, 64], tol uniform over {1e-6, 1e-8, 1e-10}; mixed precision throughout; SVD requests
-  run at most 400 outer iterations, Laplacian requests LAP_STEP_BUDGET Krylov steps.
+  run at most 400 outer iterations (6 power steps per 16-bit iteration, 12 per FP64 iteration),
+  Laplacian requests LAP_STEP_BUDGET Krylov steps.
 
-Admission: the engine's HBM budget (default 150 GB) charges each request's solver workspace; the driver
-additionally holds back arrivals while the inputs it has placed on the GPU exceed `input_cap` bytes.
+Admission: the engine's HBM budget (default 150 GB) charges each request's solver workspace; the replay
+loop additionally holds back arrivals while the inputs it has placed on the GPU exceed `input_cap` bytes.
 """
 from __future__ import annotations
 
