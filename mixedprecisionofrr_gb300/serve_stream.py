@@ -68,7 +68,8 @@ def make_stream(seed: int, count: int, rate: float = 2000.0) -> list:
 
 
 def laplacian_grid(grid: tuple):
-    """Dirichlet Laplacian (integer stencil) on a rectangular grid, CSR, and its eigenvalues (descending)."""
+    """Dirichlet Laplacian (integer stencil: 2 d on the diagonal, -1 per grid neighbour) on a rectangular
+    grid of d sides, as a sorted CSR matrix (SciPy)."""
     import scipy.sparse as sp
 
     Ts = [sp.diags([-np.ones(N - 1), 2.0 * np.ones(N), -np.ones(N - 1)], [-1, 0, 1], format="csr") for N in grid]
