@@ -297,9 +297,10 @@ typedef struct {
   int check_every;         /* residual check period in outer iterations (>= 1) */
   /* Krylov restarts: Ritz vectors kept at a restart.  1 = arnoldi_hess_eig.m:99-106 (the leading Ritz
    * vector alone; the reference mode always does this); 0 = the production default of OFRR_MODE_MIXED
-   * and OFRR_MODE_FP64 with a CSR operator: a thick restart keeping the invariant subspace of about
-   * max(nev + 4, 1.2 nev) leading Ritz values (at most kdim - 2) and the Galerkin residual direction
-   * (new behaviour); k > 1 keeps about k. */
+   * and OFRR_MODE_FP64 with a CSR operator: a thick restart keeping the invariant subspace of about nev
+   * (nonsymmetric operators) or max(nev + 4, 1.2 nev) (symmetric) leading Ritz values (cut at the widest
+   * gap nearby; at most kdim - 2) and the Galerkin residual direction (new behaviour); k > 1 keeps about
+   * k. */
   int restart_keep;
   /* OFRR_MODE_MIXED si_svd with a dense operator: 1 = the FP8 variant of the 16-bit phase, whose power
    * steps multiply E4M3 copies of A (per-row power-of-two scales, made once per solve) and of the basis

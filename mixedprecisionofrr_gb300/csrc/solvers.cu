@@ -1013,7 +1013,15 @@ extern "C" int ofrr_rr_svd(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_opt
 // Mixed mode: a 16-bit phase (16-bit basis, FP32 matvec on the FP32 value copy, FP32 arithmetic) until
 // its residuals stop improving, then an FP64 phase restarted from the sum of the unit Ritz vectors (the
 // 16-bit rounding leaves the kept block's residuals no longer parallel, and a kept block then stalls).
-static int default_keep(int nev, int kdim) { return std::min(std::max(nev + 4, (nev * 6 + 4) / 5), kdim - 2); }
+// Ritz vectors kept at a thick restart when the caller leaves restart_keep at 0 (the cut then sits at the
+// widest gap among the next few Ritz values).  Nonsymmetric operators: the nev wanted ones, so that each
+// cycle adds kdim - nev new directions -- on the 128^3 convection-diffusion operator (nev 20, kdim 64)
+// keep 20 converged in 70 cycles (2.63 s), 24 in 74 (2.89 s), 28 in 81, 32 in 92, 36 in 110.  Symmetric
+// operators: max(nev + 4, 1.2 nev) -- on ten of the serving stream's clustered Laplacians keeping only
+// nev converged 2 instead of 4.
+static int default_keep(int nev, int kdim, bool symmetric) {
+  return std::min(symmetric ? std::max(nev + 4, (nev * 6 + 4) / 5) : nev, kdim - 2);
+}
 
 static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options* opt, const void* v0,
                               void* X, int64_t ldx, double* evals, double* resid, ofrr_info* info) {
@@ -1023,7 +1031,7 @@ static int arnoldi_thick_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_
   const int nev = (int)std::min<int64_t>(opt->nev, n);
   // nb <= 128: the projected pencil's solvers hold at most 128 columns
   if (nb > std::min(kKryMaxNb, 128) || nb > n || kdim < 4) return OFRR_ERR_BLAS_INVALID_SIZE;
-  int keep = opt->restart_keep > 0 ? opt->restart_keep : default_keep(nev, kdim);
+  int keep = opt->restart_keep > 0 ? opt->restart_keep : default_keep(nev, kdim, A->symmetric != 0);
   keep = std::min(std::max(keep, nev), kdim - 2);
   if (nev > keep) return OFRR_ERR_INVALID_ARGUMENT;  // nev > kdim - 2
   const bool symmetric = A->symmetric != 0;
