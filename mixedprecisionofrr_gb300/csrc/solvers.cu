@@ -37,7 +37,6 @@ struct Op {
   int64_t ld[4] = {0, 0, 0, 0};
   int64_t m() const { return A->nrows; }
   int64_t n() const { return A->ncols; }
-  bool is_dense() const { return A->kind == OFRR_OP_DENSE; }
 
   int dense_as(ofrr_ctx* ctx, ofrr_dtype t, const void** p, int64_t* l) {
     if (!dense[t]) {
@@ -69,8 +68,8 @@ struct Op {
       if (trans && have_csrT) return csrmm_impl(ctx, &csrT, 0, tx, tc, ty, nrhs, X, ldx, Y, ldy);
       return csrmm_impl(ctx, &A->csr, trans, tx, tc, ty, nrhs, X, ldx, Y, ldy);
     }
-    const void* Ad;
-    int64_t lda;
+    const void* Ad = nullptr;
+    int64_t lda = 0;
     const int64_t M = trans ? n() : m(), K = trans ? m() : n();
     if (ctx->emulate_f64 && ta == OFRR_F64 && tx == OFRR_F64 && tc == OFRR_F64 && ty == OFRR_F64 &&
         (trans ? have_sA : have_sAt)) {
@@ -99,8 +98,8 @@ struct Op {
     int st = OFRR_SUCCESS;
     for (int trans = 0; trans < 2; ++trans) {
       const int64_t M = trans ? n() : m(), K = trans ? m() : n();
-      const void* Ap;
-      int64_t lda;
+      const void* Ap = nullptr;
+      int64_t lda = 0;
       if (trans) OFRR_TRY(dense_as(ctx, t16, &Ap, &lda));
       else OFRR_TRY(dense_t_as(ctx, t16, &Ap, &lda));
       f8ld[trans] = (K + 127) / 128 * 128;
@@ -130,8 +129,8 @@ struct Op {
       return scalecols_impl(ctx, t, tc, M, nrhs, Y, ldy, nullptr, fast);
     }
     if (A->kind == OFRR_OP_DENSE && tc == OFRR_F32 && (t == OFRR_F16 || t == OFRR_BF16)) {
-      const void* Ad;
-      int64_t lda;
+      const void* Ad = nullptr;
+      int64_t lda = 0;
       if (trans) OFRR_TRY(dense_as(ctx, t, &Ad, &lda));
       else OFRR_TRY(dense_t_as(ctx, t, &Ad, &lda));
       bool handled = false;
@@ -167,9 +166,9 @@ struct Op {
   int prepare_sliced(ofrr_ctx* ctx) {
     if (A->kind != OFRR_OP_DENSE) return OFRR_SUCCESS;
     const double* A64;
-    int64_t lda64;
+    int64_t lda64 = 0;
     {
-      const void* p;
+      const void* p = nullptr;
       OFRR_TRY(dense_as(ctx, OFRR_F64, &p, &lda64));
       A64 = (const double*)p;
     }
@@ -490,8 +489,8 @@ int emulation_bounds(ofrr_ctx* ctx, Op& op, int trans, ofrr_dtype t16, const dou
   const int64_t m = op.m(), n = op.n();
   const int64_t M = trans ? n : m, K = trans ? m : n;
   // |op(A)| as the K-contiguous operand of the TN kernel: A' (K = n) for A X, A itself (K = m) for A' X
-  const void* Ap;
-  int64_t lda;
+  const void* Ap = nullptr;
+  int64_t lda = 0;
   if (trans) OFRR_TRY(op.dense_as(ctx, t16, &Ap, &lda));
   else OFRR_TRY(op.dense_t_as(ctx, t16, &Ap, &lda));
   const bool cached = op.absA[trans] != nullptr && op.abs_t == t16;
@@ -528,8 +527,8 @@ int Op::prepare_abs(ofrr_ctx* ctx, ofrr_dtype t16) {
   int st = OFRR_SUCCESS;
   for (int trans = 0; trans < 2; ++trans) {
     const int64_t M = trans ? n() : m(), K = trans ? m() : n();
-    const void* Ap;
-    int64_t lda;
+    const void* Ap = nullptr;
+    int64_t lda = 0;
     if (trans) OFRR_TRY(dense_as(ctx, t16, &Ap, &lda));
     else OFRR_TRY(dense_t_as(ctx, t16, &Ap, &lda));
     const int64_t ldK = (K + 7) & ~int64_t(7);
@@ -1839,8 +1838,8 @@ static int si_eig_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
     OFRR_TRY(scalecols_impl(ctx, L.po, L.pc, n, b0, V16, n, nullptr));
     const double stag = (L.po == OFRR_BF16) ? 1e-4 : 1e-5;
     if (op.A->kind == OFRR_OP_DENSE) {  // operator copies live for the whole solve
-      const void* p;
-      int64_t l;
+      const void* p = nullptr;
+      int64_t l = 0;
       OFRR_TRY(op.dense_as(ctx, L.po, &p, &l));
       OFRR_TRY(op.dense_t_as(ctx, L.po, &p, &l));
     }
@@ -1942,8 +1941,8 @@ static int si_svd_body(ofrr_ctx* ctx, const ofrr_operator* A, const ofrr_options
     // on the dense 8192 x 2048 benchmark: 1e-5 took one more 16-bit iteration and 0.3 ms more per solve)
     const double stag = 1e-4;
     if (op.A->kind == OFRR_OP_DENSE) {  // operator copies live for the whole solve
-      const void* p;
-      int64_t l;
+      const void* p = nullptr;
+      int64_t l = 0;
       OFRR_TRY(op.dense_as(ctx, L.po, &p, &l));
       OFRR_TRY(op.dense_t_as(ctx, L.po, &p, &l));
       if (opt->power_fp8) OFRR_TRY(op.prepare_f8(ctx, L.po));
