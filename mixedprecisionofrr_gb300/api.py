@@ -154,7 +154,8 @@ class CsrMatrix:
         d = np.asarray(data, np.float64)
         self.a_double = torch.as_tensor(d, device=device)
         self.a_single = torch.as_tensor(d.astype(np.float32), device=device)
-        self.a_half = torch.as_tensor(d.astype(np.float16), device=device)
+        with np.errstate(over="ignore"):  # values beyond the FP16 range become +-inf, as sparse2csr.m's cast
+            self.a_half = torch.as_tensor(d.astype(np.float16), device=device)
         if symmetric is None:
             M = sp.csr_matrix((d, np.asarray(indices), np.asarray(indptr)), shape=shape)
             symmetric = shape[0] == shape[1] and abs(M - M.T).max() == 0

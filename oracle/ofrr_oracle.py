@@ -188,6 +188,8 @@ def sparse2csr(A) -> dict:
     """``+src/+csr/sparse2csr.m:21-50``: CSR with FP64/FP32/FP16 value copies (0-based here)."""
     A = sp.csr_matrix(A, dtype=np.float64)
     A.sort_indices()
+    with np.errstate(over="ignore"):  # half() of a value beyond the FP16 range is +-inf, as in MATLAB
+        a_half = A.data.astype(np.float16)
     return {
         "nrows": A.shape[0],
         "ncols": A.shape[1],
@@ -195,7 +197,7 @@ def sparse2csr(A) -> dict:
         "indices": A.indices.astype(np.int32),
         "a_double": A.data.astype(np.float64),
         "a_single": A.data.astype(np.float32),
-        "a_half": A.data.astype(np.float16),
+        "a_half": a_half,
     }
 
 
