@@ -736,17 +736,18 @@ def arnoldi_thick_eig(A, n: int, k: int, kdim: int, tol: float, keep: Optional[i
     eliminations in MGS order with the coefficients read at the earlier pivot rows, pivot on the first
     largest entry, scale) and the Rayleigh-Ritz step its generalized form (``:89-95``, eig(V'AV, V'V)).
     The restart is new (``:99-106`` keeps the leading Ritz vector alone): a basis Y of the invariant
-    subspace of the projected pencil for its leading eigenvalues (about ``keep`` of them, cut at the widest
-    gap of the real parts within keep-3 .. keep+4: the Ritz vectors for a symmetric operator, sorted real
-    Schur vectors otherwise) and the Galerkin residual direction f = A v_last - V (V'V)^-1 V' A v_last;
+    subspace of the projected pencil for its leading eigenvalues (about ``keep`` of them -- by default k for
+    a nonsymmetric operator and max(k + 4, 1.2 k) for a symmetric one -- cut at the widest gap of the real
+    parts within keep-3 .. keep+4: the Ritz vectors for a symmetric operator, sorted real Schur vectors
+    otherwise) and the Galerkin residual direction f = A v_last - V (V'V)^-1 V' A v_last;
     the next basis is the Hessenberg basis of [Y, f] (columns first scaled to a unit maximum,
     near-dependent ones dropped below 1e-12) continued by Krylov steps from f.  Stops when the k leading
     Ritz pairs have ||A x - l x|| / (max|l| ||x||) <= tol or after ``maxsteps`` Krylov steps.  Returns
     (X (n x k, unit columns), d (k), info) with info = {'cycles', 'steps', 'residuals'}.
     """
     k = min(k, n)
-    if keep is None or keep <= 0:
-        keep = min(max(k + 4, (k * 6 + 4) // 5), kdim - 2)
+    if keep is None or keep <= 0:  # the library's default: k for a nonsymmetric operator, more for a symmetric one
+        keep = min(max(k + 4, (k * 6 + 4) // 5) if symmetric else k, kdim - 2)
     keep = min(max(keep, k), kdim - 2)
     nb = kdim + 1
     W = (randn_block(seed, n, 1) if v0 is None else np.asarray(v0, dtype=np.float64).reshape(n, 1)).copy()
