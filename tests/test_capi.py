@@ -55,3 +55,38 @@ def test_status_strings_and_defaults(built_lib):
     assert (o.maxiter, o.step_size, o.seed, o.use_generalized) == (5, 1, 42, 1)
     assert o.select_tol < 0  # eps(output precision) by default
     assert o.step_size_f64 == 0  # the FP64 phase of the mixed mode takes step_size unless set
+
+
+def _header_structs():
+    """Field names, in order, of every `typedef struct { ... } name;` in include/ofrr.h."""
+    import re
+    from pathlib import Path
+
+    txt = (Path(__file__).resolve().parents[1] / "include" / "ofrr.h").read_text()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    txt = re.sub(r"//[^\n]*", "", txt)
+    out = {}
+    for body, name in re.findall(r"typedef\s+struct\s*\{(.*?)\}\s*(\w+)\s*;", txt, flags=re.S):
+        fields = []
+        for decl in body.split(";"):
+            decl = " ".join(decl.split())
+            if not decl:
+                continue
+            # "type a, b" or "const int32_t* indptr": the names are the comma-separated tails
+            first, *rest = decl.split(",")
+            fields.append(first.replace("*", " ").split()[-1])
+            fields += [r.replace("*", " ").strip() for r in rest]
+        out[name] = fields
+    return out
+
+
+def test_ctypes_structs_follow_the_header():
+    """The Python binding's structures list the C structures' fields in the header's order (an option
+    added to one side only would shift every later field across the ABI)."""
+    from mixedprecisionofrr_gb300 import _lib
+
+    hdr = _header_structs()
+    for name in ("ofrr_csr", "ofrr_operator", "ofrr_options", "ofrr_info", "ofrr_request", "ofrr_serve_report"):
+        assert name in hdr, name
+        py = [f[0] for f in getattr(_lib, name)._fields_]
+        assert py == hdr[name], (name, py, hdr[name])
